@@ -1,0 +1,135 @@
+/*
+ * tileqr.h -- C ABI of libtileqr.so, the GB300 (sm_103a) tile-QR library that
+ * stands in for NextLA.jl's in-place tile kernels.
+ *
+ * Conventions shared by every entry point
+ *   - Matrices are column-major with an explicit leading dimension; indices are
+ *     0-based.  A Julia caller passes pointer(A) and stride(A, 2) of its (view
+ *     of a) CuArray, exactly the storage NextLA's kernels index.
+ *   - All pointers are device pointers; nothing is allocated by the library.
+ *   - `work` / `lwork` / `ldwork` arguments exist for signature parity with
+ *     NextLA and may be NULL: the W blocks live in on-chip shared memory.
+ *   - Return value: 0 on success; -i when argument i (1-based position in the
+ *     C signature) is illegal, which is where NextLA throws ArgumentError;
+ *     a positive cudaError_t value when a launch failed.
+ *   - Calls are asynchronous on `stream`.  NextLA's kernels block until done;
+ *     a binding that keeps that behaviour synchronises the stream afterwards.
+ *   - Flags are the ASCII characters NextLA uses ('L'/'R', 'N'/'C'/'T',
+ *     'F'/'B', 'C'/'R').  'T' means the same as 'C' for real types.
+ *   - Each routine exists for double (tqr_d...) and float (tqr_s...).
+ */
+#ifndef TILEQR_H
+#define TILEQR_H
+
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* geqr2!(m, n, A, tau, work) -- src/geqr2.jl:107-121.
+ * Unblocked Householder QR of the m-by-n A; tau has min(m, n) entries. */
+int tqr_dgeqr2(int m, int n, double *A, int lda, double *tau, double *work, cudaStream_t stream);
+int tqr_sgeqr2(int m, int n, float *A, int lda, float *tau, float *work, cudaStream_t stream);
+
+/* larft!(direct, storev, n, k, V, tau, T) -- src/larft.jl:205-213.
+ * k-by-k triangular factor of H = I - V T V^H (all four direct/storev forms). */
+int tqr_dlarft(char direct, char storev, int n, int k, const double *V, int ldv, const double *tau,
+               double *T, int ldt, cudaStream_t stream);
+int tqr_slarft(char direct, char storev, int n, int k, const float *V, int ldv, const float *tau,
+               float *T, int ldt, cudaStream_t stream);
+
+/* larfb!(side, trans, direct, storev, m, n, k, V, ldv, T, C, work) -- src/larfb.jl:37-142.
+ * C := op(H) C or C op(H); direct 'F' and storev 'C' only, as in the reference. */
+int tqr_dlarfb(char side, char trans, char direct, char storev, int m, int n, int k,
+               const double *V, int ldv, const double *T, int ldt, double *C, int ldc,
+               double *work, int ldwork, cudaStream_t stream);
+int tqr_slarfb(char side, char trans, char direct, char storev, int m, int n, int k,
+               const float *V, int ldv, const float *T, int ldt, float *C, int ldc,
+               float *work, int ldwork, cudaStream_t stream);
+
+/* geqrt!(m, n, ib, A, T, tau, work) -- src/geqrt.jl:22-68.
+ * Blocked QR of an m-by-n tile: R above the diagonal, V below, T is ib-by-min(m,n)
+ * (block starting at column i in T[0:sb, i:i+sb]), tau has min(m, n) entries. */
+int tqr_dgeqrt(int m, int n, int ib, double *A, int lda, double *T, int ldt, double *tau,
+               double *work, cudaStream_t stream);
+int tqr_sgeqrt(int m, int n, int ib, float *A, int lda, float *T, int ldt, float *tau,
+               float *work, cudaStream_t stream);
+
+/* unmqr!(side, trans, m, n, k, ib, A, lda, T, C, work) -- src/unmqr.jl:52-149.
+ * C := op(Q) C or C op(Q) with Q from geqrt.  k is clamped to the order of Q;
+ * the reference also clamps to size(A, 2), which a binding applies before the call. */
+int tqr_dunmqr(char side, char trans, int m, int n, int k, int ib, const double *A, int lda,
+               const double *T, int ldt, double *C, int ldc, double *work, int ldwork,
+               cudaStream_t stream);
+int tqr_sunmqr(char side, char trans, int m, int n, int k, int ib, const float *A, int lda,
+               const float *T, int ldt, float *C, int ldc, float *work, int ldwork,
+               cudaStream_t stream);
+
+/* tsqrt!(m, n, ib, A1, A2, T, tau, work) -- src/tsqrt.jl:128-156.
+ * QR of [A1 (upper triangular); A2 (m-by-n)].  m1 = size(A1, 1), which the
+ * reference reads from the array (k = min(m1, n), src/tsqrt.jl:139-140). */
+int tqr_dtsqrt(int m, int n, int ib, int m1, double *A1, int lda1, double *A2, int lda2,
+               double *T, int ldt, double *tau, double *work, cudaStream_t stream);
+int tqr_stsqrt(int m, int n, int ib, int m1, float *A1, int lda1, float *A2, int lda2,
+               float *T, int ldt, float *tau, float *work, cudaStream_t stream);
+
+/* tsmqr!(side, trans, m1, n1, m2, n2, k, ib, A1, A2, V, T, work) -- src/tsmqr.jl:47-146.
+ * [A1; A2] := op(Q) [A1; A2] (side 'L') or [A1 A2] := [A1 A2] op(Q) (side 'R').
+ * k is clamped to m1 ('L') or n1 ('R'); the reference's clamp to the stored
+ * columns of V and T (src/tsmqr.jl:94-96) is applied by the binding. */
+int tqr_dtsmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, double *A1,
+               int lda1, double *A2, int lda2, const double *V, int ldv, const double *T, int ldt,
+               double *work, int lwork, cudaStream_t stream);
+int tqr_stsmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, float *A1,
+               int lda1, float *A2, int lda2, const float *V, int ldv, const float *T, int ldt,
+               float *work, int lwork, cudaStream_t stream);
+
+/* parfb!(side, trans, direct, storev, m1, n1, m2, n2, k, l, A1, A2, V, T, work)
+ * -- src/parfb.jl:44-191 with pamm! (src/pamm.jl:49-473).  Implemented for the
+ * pentagonal form tsmqr uses: l = 0, direct 'F', storev 'C' (other values of
+ * those three arguments return -10, -3, -4). */
+int tqr_dparfb(char side, char trans, char direct, char storev, int m1, int n1, int m2, int n2,
+               int k, int l, double *A1, int lda1, double *A2, int lda2, const double *V, int ldv,
+               const double *T, int ldt, double *work, int ldwork, cudaStream_t stream);
+int tqr_sparfb(char side, char trans, char direct, char storev, int m1, int n1, int m2, int n2,
+               int k, int l, float *A1, int lda1, float *A2, int lda2, const float *V, int ldv,
+               const float *T, int ldt, float *work, int ldwork, cudaStream_t stream);
+
+/* ---- Tile QR built from the kernels above (no counterpart in NextLA, which
+ * ships only the tile kernels; the composition is the flat-tree order its
+ * kernels are designed for). ----
+ * tile_geqrf: A (m-by-n, nb-by-nb tiles) := tile QR.  T is (MT*ib)-by-n with
+ * ldt >= MT*ib, T_ik in rows [i*ib, i*ib+ib), columns [k*nb, k*nb+nb); tau is
+ * n-by-MT with ldtau >= n.  MT = ceil(m / nb). */
+int tqr_dtile_geqrf(int m, int n, int nb, int ib, double *A, int lda, double *T, int ldt,
+                    double *tau, int ldtau, cudaStream_t stream);
+int tqr_stile_geqrf(int m, int n, int nb, int ib, float *A, int lda, float *T, int ldt,
+                    float *tau, int ldtau, cudaStream_t stream);
+
+/* B (m-by-nrhs) := Q^T B (trans 'C'/'T') or Q B (trans 'N'), Q from tile_geqrf. */
+int tqr_dtile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const double *A, int lda,
+                    const double *T, int ldt, double *B, int ldb, cudaStream_t stream);
+int tqr_stile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const float *A, int lda,
+                    const float *T, int ldt, float *B, int ldb, cudaStream_t stream);
+
+/* R X = B for the upper triangle of the n-by-n R; B (n-by-nrhs) is overwritten
+ * by X.  Arithmetic of NextLA's LeftUpperTRSM! (src/trsm.jl:38-63, 134-138),
+ * blocked so that n is not limited to 1024. */
+int tqr_dtrsm_lun(int n, int nrhs, const double *R, int ldr, double *B, int ldb,
+                  cudaStream_t stream);
+int tqr_strsm_lun(int n, int nrhs, const float *R, int ldr, float *B, int ldb,
+                  cudaStream_t stream);
+
+/* Least squares min ||A X - B||, m >= n: tile_geqrf, Q^T B, then R X = B[0:n].
+ * A, T, tau as for tile_geqrf; X overwrites B[0:n, 0:nrhs]. */
+int tqr_dtile_gels(int m, int n, int nrhs, int nb, int ib, double *A, int lda, double *T, int ldt,
+                   double *tau, int ldtau, double *B, int ldb, cudaStream_t stream);
+int tqr_stile_gels(int m, int n, int nrhs, int nb, int ib, float *A, int lda, float *T, int ldt,
+                   float *tau, int ldtau, float *B, int ldb, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TILEQR_H */

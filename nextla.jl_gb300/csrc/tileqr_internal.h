@@ -1,0 +1,27 @@
+// tileqr_internal.h -- launchers shared between the translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace tqr {
+
+// geqr2 (+ T when T != nullptr) on an m-by-nc panel, one CTA.
+template <typename R>
+cudaError_t launch_panel_qr(int m, int nc, R *A, int lda, R *tau, R *T, int ldt, cudaStream_t st);
+
+// One ib-block of tsqrt (pointers already offset to the block), one CTA.
+template <typename R>
+cudaError_t launch_tsqrt_block(int m, int sb, R *A1, int lda1, R *A2, int lda2, R *T, int ldt,
+                               R *tau, cudaStream_t st);
+
+template <typename R>
+cudaError_t launch_larft(int direct_f, int storev_c, int n, int k, const R *V, int ldv,
+                         const R *tau, R *T, int ldt, cudaStream_t st);
+
+// Block-reflector apply.  mode 0: larfb/unmqr on C (m-by-n); mode 1: tsmqr on
+// [A1; A2] (side L) or [A1 A2] (side R) with C = A2 (m-by-n).
+template <typename R>
+cudaError_t launch_apply(int mode, char side, char trans, int m, int n, int k, int ib, R *C,
+                         int ldc, R *A1, int lda1, const R *V, int ldv, const R *T, int ldt,
+                         cudaStream_t st);
+
+}  // namespace tqr

@@ -1,0 +1,348 @@
+"""tileqr -- Python front end of libtileqr.so, mirroring NextLA.jl's tile-QR API.
+
+Function names and argument lists follow NextLA's in-place kernels
+(`geqrt!`, `tsqrt!`, `tsmqr!`, `unmqr!`, `larfb!`, `larft!`, `geqr2!`,
+`parfb!`) and their allocating helper methods, dispatched on the number of
+arguments the way Julia dispatches on the method signature.  Arrays are
+column-major CUDA tensors (float64 or float32): build them with `empty`,
+`zeros` or `to_device`, and pass slices of them as NextLA passes `@view`s; the
+leading dimension is read from the column stride.
+
+Errors: an illegal argument raises ArgumentError (a ValueError), mirroring the
+reference's ArgumentError; a CUDA failure raises RuntimeError.  Calls are
+blocking by default, like the reference (every NextLA kernel synchronises);
+`set_blocking(False)` leaves them asynchronous on torch's current stream.
+"""
+import torch
+
+from . import _lib
+
+__all__ = [
+    "ArgumentError", "set_blocking", "empty", "zeros", "to_device", "to_numpy",
+    "geqr2", "larft", "larfb", "geqrt", "unmqr", "tsqrt", "tsmqr", "parfb",
+    "tile_geqrf", "tile_unmqr", "trsm_lun", "tile_gels", "tile_shapes",
+]
+
+_BLOCKING = True
+
+
+class ArgumentError(ValueError):
+    """Raised where NextLA.jl raises ArgumentError."""
+
+
+def set_blocking(flag):
+    global _BLOCKING
+    _BLOCKING = bool(flag)
+
+
+# ---- column-major tensors ---------------------------------------------------
+
+def empty(m, n, dtype=torch.float64, device="cuda"):
+    """m-by-n column-major tensor (stride (1, m))."""
+    return torch.empty((n, m), dtype=dtype, device=device).t()
+
+
+def zeros(m, n, dtype=torch.float64, device="cuda"):
+    return torch.zeros((n, m), dtype=dtype, device=device).t()
+
+
+def to_device(x, dtype=None, device="cuda"):
+    """Copy a numpy array or tensor into a column-major CUDA tensor."""
+    t = torch.as_tensor(x)
+    if dtype is not None:
+        t = t.to(dtype)
+    if t.dim() == 1:
+        return t.to(device).contiguous()
+    out = empty(t.shape[0], t.shape[1], dtype=t.dtype, device=device)
+    out.copy_(t)
+    return out
+
+
+def to_numpy(t):
+    import numpy as np
+    return np.asfortranarray(t.detach().cpu().numpy())
+
+
+# ---- plumbing ----------------------------------------------------------------
+
+def _prefix(*ts):
+    dt = None
+    for t in ts:
+        if t is None:
+            continue
+        if dt is None:
+            dt = t.dtype
+        elif t.dtype != dt:
+            raise TypeError("all arrays must share one element type")
+    if dt == torch.float64:
+        return "d"
+    if dt == torch.float32:
+        return "s"
+    raise TypeError(f"unsupported element type {dt}")
+
+
+def _mat(t):
+    """(device pointer, leading dimension) of a column-major matrix or view."""
+    if t is None:
+        return None, 1
+    if not t.is_cuda:
+        raise TypeError("tileqr works on CUDA tensors")
+    if t.dim() == 1:
+        if t.numel() > 1 and t.stride(0) != 1:
+            raise ArgumentError("vectors must be contiguous")
+        return t.data_ptr(), max(1, t.shape[0])
+    if t.dim() != 2:
+        raise ArgumentError("expected a matrix")
+    m, n = t.shape
+    if m > 1 and t.stride(0) != 1:
+        raise ArgumentError("matrices must be column-major (unit row stride)")
+    ld = t.stride(1) if n > 1 else m
+    return t.data_ptr(), max(1, ld)
+
+
+def _ptr(t):
+    return _mat(t)[0]
+
+
+def _ch(c):
+    if isinstance(c, bytes):
+        return c
+    return str(c).encode()
+
+
+def _call(prefix, name, *args):
+    st = torch.cuda.current_stream()
+    rc = _lib.fn(prefix, name)(*args, st.cuda_stream)
+    if rc < 0:
+        raise ArgumentError(f"{name}!: illegal value of argument {-rc}")
+    if rc > 0:
+        raise RuntimeError(f"{name}!: CUDA error {rc}")
+    if _BLOCKING:
+        st.synchronize()
+
+
+def _arity(name, args, *counts):
+    if len(args) not in counts:
+        raise TypeError(f"{name}: no method with {len(args)} arguments")
+
+
+# ---- NextLA kernels ---------------------------------------------------------
+
+def geqr2(*args):
+    """geqr2!(m, n, A, tau, work) | geqr2!(A, tau) -- src/geqr2.jl:107-140."""
+    _arity("geqr2", args, 5, 2)
+    if len(args) == 2:
+        A, tau = args
+        m, n = A.shape
+        return geqr2(m, n, A, tau, None)
+    m, n, A, tau, work = args
+    pa, lda = _mat(A)
+    _call(_prefix(A, tau), "geqr2", m, n, pa, lda, _ptr(tau), None)
+
+
+def larft(*args):
+    """larft!(direct, storev, n, k, V, tau, T) | larft!(direct, storev, V, tau, T)
+    -- src/larft.jl:205-272."""
+    _arity("larft", args, 7, 5)
+    if len(args) == 5:
+        direct, storev, V, tau, T = args
+        if _ch(storev) == b"C":
+            n, k = V.shape
+            if tau.shape[0] != k:
+                raise ArgumentError("For columnwise storage, length(tau) must equal size(V,2)")
+        else:
+            k, n = V.shape
+            if tau.shape[0] != k:
+                raise ArgumentError("For rowwise storage, length(tau) must equal size(V,1)")
+        return larft(direct, storev, n, k, V, tau, T)
+    direct, storev, n, k, V, tau, T = args
+    pv, ldv = _mat(V)
+    pt, ldt = _mat(T)
+    _call(_prefix(V, tau, T), "larft", _ch(direct), _ch(storev), n, k, pv, ldv, _ptr(tau), pt, ldt)
+
+
+def larfb(*args):
+    """larfb!(side, trans, direct, storev, m, n, k, V, ldv, T, C, work)
+    | larfb!(side, trans, direct, storev, V, T, C) -- src/larfb.jl:37-210."""
+    _arity("larfb", args, 12, 7)
+    if len(args) == 7:
+        side, trans, direct, storev, V, T, C = args
+        m, n = C.shape
+        k = T.shape[0]
+        return larfb(side, trans, direct, storev, m, n, k, V, V.shape[0], T, C, None)
+    side, trans, direct, storev, m, n, k, V, ldv, T, C, work = args
+    pv, _ = _mat(V)
+    pt, ldt = _mat(T)
+    pc, ldc = _mat(C)
+    _call(_prefix(V, T, C), "larfb", _ch(side), _ch(trans), _ch(direct), _ch(storev), m, n, k,
+          pv, ldv, pt, ldt, pc, ldc, None, 1)
+
+
+def geqrt(*args):
+    """geqrt!(m, n, ib, A, T, tau, work) | geqrt!(A, T) -- src/geqrt.jl:22-91.
+    The helper returns (A, T, tau)."""
+    _arity("geqrt", args, 7, 2)
+    if len(args) == 2:
+        A, T = args
+        m, n = A.shape
+        ib = T.shape[0]
+        tau = torch.zeros(min(m, n), dtype=A.dtype, device=A.device)
+        geqrt(m, n, ib, A, T, tau, None)
+        return A, T, tau
+    m, n, ib, A, T, tau, work = args
+    pa, lda = _mat(A)
+    pt, ldt = _mat(T)
+    _call(_prefix(A, T, tau), "geqrt", m, n, ib, pa, lda, pt, ldt, _ptr(tau), None)
+
+
+def unmqr(*args):
+    """unmqr!(side, trans, m, n, k, ib, A, lda, T, C, work)
+    | unmqr!(side, trans, A, T, C) -- src/unmqr.jl:52-237."""
+    _arity("unmqr", args, 11, 5)
+    if len(args) == 5:
+        side, trans, A, T, C = args
+        m, n = C.shape
+        ib, k = T.shape
+        nq = m if _ch(side) == b"L" else n
+        k = min(k, nq)
+        if ib <= 0:
+            raise ArgumentError(f"Block size ib must be positive, got {ib}")
+        if A.shape[0] != nq:
+            raise ArgumentError("A_qr rows must match the order of Q")
+        if A.shape[1] < k:
+            raise ArgumentError(f"A_qr columns ({A.shape[1]}) must be >= k ({k})")
+        lda = max(1, _mat(A)[1])
+        return unmqr(side, trans, m, n, k, ib, A, lda, T, C, None)
+    side, trans, m, n, k, ib, A, lda, T, C, work = args
+    if k >= 0:
+        k = min(k, A.shape[1])                 # src/unmqr.jl:83 (size(A, 2))
+    pa, _ = _mat(A)
+    pt, ldt = _mat(T)
+    pc, ldc = _mat(C)
+    _call(_prefix(A, T, C), "unmqr", _ch(side), _ch(trans), m, n, k, ib, pa, lda, pt, ldt,
+          pc, ldc, None, 1)
+
+
+def tsqrt(*args):
+    """tsqrt!(m, n, ib, A1, A2, T, tau, work) | tsqrt!(A1, A2, T) -- src/tsqrt.jl:128-211.
+    The helper returns (A1, A2, T, tau)."""
+    _arity("tsqrt", args, 8, 3)
+    if len(args) == 3:
+        A1, A2, T = args
+        m1, n = A1.shape
+        m = A2.shape[0]
+        ib = T.shape[0]
+        if ib <= 0:
+            raise ArgumentError(f"Block size ib must be positive, got {ib}")
+        tau = torch.zeros(min(m1, n), dtype=A1.dtype, device=A1.device)
+        tsqrt(m, n, ib, A1, A2, T, tau, None)
+        return A1, A2, T, tau
+    m, n, ib, A1, A2, T, tau, work = args
+    p1, ld1 = _mat(A1)
+    p2, ld2 = _mat(A2)
+    pt, ldt = _mat(T)
+    _call(_prefix(A1, A2, T, tau), "tsqrt", m, n, ib, A1.shape[0], p1, ld1, p2, ld2, pt, ldt,
+          _ptr(tau), None)
+
+
+def tsmqr(*args):
+    """tsmqr!(side, trans, m1, n1, m2, n2, k, ib, A1, A2, V, T, work)
+    | tsmqr!(side, trans, A1, A2, V, T) -- src/tsmqr.jl:47-228."""
+    _arity("tsmqr", args, 13, 6)
+    if len(args) == 6:
+        side, trans, A1, A2, V, T = args
+        m1, n1 = A1.shape
+        m2, n2 = A2.shape
+        ib, k = T.shape
+        if _ch(side) == b"L" and n2 != n1:
+            raise ArgumentError("For side='L', A1 and A2 must have same number of columns")
+        if _ch(side) == b"R" and m2 != m1:
+            raise ArgumentError("For side='R', A1 and A2 must have same number of rows")
+        if ib <= 0:
+            raise ArgumentError(f"Block size ib must be positive, got {ib}")
+        return tsmqr(side, trans, m1, n1, m2, n2, k, ib, A1, A2, V, T, None)
+    side, trans, m1, n1, m2, n2, k, ib, A1, A2, V, T, work = args
+    if k >= 0 and V is not None and T is not None:
+        k = min(k, V.shape[1], T.shape[1])     # src/tsmqr.jl:94-96 (stored columns)
+    p1, ld1 = _mat(A1)
+    p2, ld2 = _mat(A2)
+    pv, ldv = _mat(V)
+    pt, ldt = _mat(T)
+    _call(_prefix(A1, A2, V, T), "tsmqr", _ch(side), _ch(trans), m1, n1, m2, n2, k, ib,
+          p1, ld1, p2, ld2, pv, ldv, pt, ldt, None, 0)
+
+
+def parfb(*args):
+    """parfb!(side, trans, direct, storev, m1, n1, m2, n2, k, l, A1, A2, V, T, work)
+    | parfb!(side, trans, direct, storev, A1, A2, V, T) -- src/parfb.jl:44-239."""
+    _arity("parfb", args, 15, 8)
+    if len(args) == 8:
+        side, trans, direct, storev, A1, A2, V, T = args
+        m1, n1 = A1.shape
+        m2, n2 = A2.shape
+        k = T.shape[0]
+        l = V.shape[1]                         # the reference helper's choice (src/parfb.jl:226)
+        return parfb(side, trans, direct, storev, m1, n1, m2, n2, k, l, A1, A2, V, T, None)
+    side, trans, direct, storev, m1, n1, m2, n2, k, l, A1, A2, V, T, work = args
+    p1, ld1 = _mat(A1)
+    p2, ld2 = _mat(A2)
+    pv, ldv = _mat(V)
+    pt, ldt = _mat(T)
+    _call(_prefix(A1, A2, V, T), "parfb", _ch(side), _ch(trans), _ch(direct), _ch(storev),
+          m1, n1, m2, n2, k, l, p1, ld1, p2, ld2, pv, ldv, pt, ldt, None, 1)
+
+
+# ---- tile QR, Q application, solve ------------------------------------------
+
+def tile_shapes(m, n, nb, ib):
+    """Shapes of the T and tau arrays tile_geqrf fills."""
+    MT = (m + nb - 1) // nb
+    return (MT * ib, n), (n, MT)
+
+
+def tile_geqrf(A, nb=256, ib=32, T=None, tau=None):
+    """Flat-tree tile QR of A in place; returns (T, tau)."""
+    m, n = A.shape
+    ts, taus = tile_shapes(m, n, nb, ib)
+    if T is None:
+        T = zeros(*ts, dtype=A.dtype, device=A.device)
+    if tau is None:
+        tau = zeros(*taus, dtype=A.dtype, device=A.device)
+    pa, lda = _mat(A)
+    pt, ldt = _mat(T)
+    pu, ldu = _mat(tau)
+    _call(_prefix(A, T, tau), "tile_geqrf", m, n, nb, ib, pa, lda, pt, ldt, pu, ldu)
+    return T, tau
+
+
+def tile_unmqr(trans, A, T, B, nb=256, ib=32):
+    """B := Q^T B (trans 'C'/'T') or Q B (trans 'N') with Q from tile_geqrf."""
+    m, n = A.shape
+    pa, lda = _mat(A)
+    pt, ldt = _mat(T)
+    pb, ldb = _mat(B)
+    _call(_prefix(A, T, B), "tile_unmqr", _ch(trans), m, n, B.shape[1], nb, ib, pa, lda, pt, ldt,
+          pb, ldb)
+
+
+def trsm_lun(R, B):
+    """Solve R X = B in place (upper triangle of the square R)."""
+    pr, ldr = _mat(R)
+    pb, ldb = _mat(B)
+    _call(_prefix(R, B), "trsm_lun", R.shape[1], B.shape[1], pr, ldr, pb, ldb)
+
+
+def tile_gels(A, B, nb=256, ib=32):
+    """Least squares min ||A X - B|| (m >= n) in place: A := tile QR, B[:n] := X.
+    Returns (X view, T, tau)."""
+    m, n = A.shape
+    ts, taus = tile_shapes(m, n, nb, ib)
+    T = zeros(*ts, dtype=A.dtype, device=A.device)
+    tau = zeros(*taus, dtype=A.dtype, device=A.device)
+    pa, lda = _mat(A)
+    pt, ldt = _mat(T)
+    pu, ldu = _mat(tau)
+    pb, ldb = _mat(B)
+    _call(_prefix(A, T, tau, B), "tile_gels", m, n, B.shape[1], nb, ib, pa, lda, pt, ldt, pu, ldu,
+          pb, ldb)
+    return B[:n], T, tau

@@ -1,0 +1,67 @@
+"""Loader and ctypes declarations of libtileqr.so (include/tileqr.h).
+
+The library is built in-tree (nextla.jl_gb300/tileqr_build.py).  There is no CPU
+fallback: if the shared library is missing, every call raises.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libtileqr.so")
+
+_I = ctypes.c_int
+_C = ctypes.c_char
+_P = ctypes.c_void_p
+
+# name -> argument types (without the precision prefix); every entry point
+# returns int and ends with a cudaStream_t.
+SIGNATURES = {
+    "geqr2": [_I, _I, _P, _I, _P, _P, _P],
+    "larft": [_C, _C, _I, _I, _P, _I, _P, _P, _I, _P],
+    "larfb": [_C, _C, _C, _C, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
+    "geqrt": [_I, _I, _I, _P, _I, _P, _I, _P, _P, _P],
+    "unmqr": [_C, _C, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
+    "tsqrt": [_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _P, _P],
+    "tsmqr": [_C, _C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
+    "parfb": [_C, _C, _C, _C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
+    "tile_geqrf": [_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P],
+    "tile_unmqr": [_C, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P],
+    "trsm_lun": [_I, _I, _P, _I, _P, _I, _P],
+    "tile_gels": [_I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
+}
+
+_lib = None
+
+
+class LibraryMissing(RuntimeError):
+    pass
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise LibraryMissing(
+                f"{LIB_PATH} is not built; run nextla.jl_gb300/tileqr_build.py (no CPU fallback exists)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in SIGNATURES.items():
+            for p in ("d", "s"):
+                f = getattr(L, f"tqr_{p}{name}")
+                f.argtypes = args
+                f.restype = _I
+        _lib = L
+    return _lib
+
+
+def fn(prefix, name):
+    return getattr(lib(), f"tqr_{prefix}{name}")
+
+
+def exported_symbols():
+    """Every tqr_* symbol the header declares, as (name, present) pairs."""
+    L = lib()
+    out = []
+    for name in SIGNATURES:
+        for p in ("d", "s"):
+            out.append((f"tqr_{p}{name}", hasattr(L, f"tqr_{p}{name}")))
+    return out

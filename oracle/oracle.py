@@ -1,0 +1,210 @@
+"""ctypes front end of the CPU oracle (nextla_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke check and by the
+benchmark's CPU-baseline leg, never by the product library.
+
+The functions mirror NextLA.jl's low-level signatures (geqrt!, tsqrt!,
+tsmqr!, unmqr!, larfb!, larft!, geqr2!, parfb!) on column-major numpy
+arrays.  Views are allowed: the leading dimension is taken from the array's
+column stride, as Julia's `stride(A, 2)` would give it.  Argument errors
+raise ValueError (the reference raises ArgumentError).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(_HERE, "nextla_oracle.c")
+_LIB_PATH = os.path.join(_HERE, "liboracle.so")
+_lib = None
+
+# -ffp-contract=off keeps x86 and Arm builds rounding identically (no fused
+# multiply-add contraction), so the oracle gives the same bits on both hosts.
+CFLAGS = ["-O2", "-fPIC", "-shared", "-std=c11", "-ffp-contract=off"]
+
+
+def build(force=False):
+    """Compile liboracle.so next to this file (gcc, a second or two)."""
+    if force or not os.path.exists(_LIB_PATH) or (
+            os.path.getmtime(_LIB_PATH) < os.path.getmtime(_SRC)):
+        subprocess.check_call(["gcc", *CFLAGS, "-o", _LIB_PATH, _SRC, "-lm"])
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(_LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+_I = ctypes.c_int
+_C = ctypes.c_char
+_P = ctypes.c_void_p
+
+
+def _declare(L):
+    sig = {
+        "ora_dgeqr2": [_I, _I, _P, _I, _P, _P],
+        "ora_dlarft": [_C, _C, _I, _I, _P, _I, _P, _P, _I],
+        "ora_dlarfb": [_C, _C, _C, _C, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I],
+        "ora_dgeqrt": [_I, _I, _I, _P, _I, _P, _I, _P, _P],
+        "ora_dunmqr": [_C, _C, _I, _I, _I, _I, _P, _I, _I, _I, _P, _I, _P, _I, _P, _I],
+        "ora_dparfb": [_C, _C, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, _I],
+        "ora_dtsmqr": [_C, _C, _I, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
+        "ora_dtsqrt": [_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _P],
+        "ora_dtile_geqrf": [_I, _I, _I, _I, _P, _I, _P, _I, _P, _I],
+        "ora_dtile_unmqr": [_C, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I],
+        "ora_dtrsm_lun": [_I, _I, _P, _I, _P, _I],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = _I
+
+
+def _mat(A):
+    """(pointer, ld) of a column-major float64 matrix or view."""
+    if A is None:
+        return None, 1
+    if A.dtype != np.float64:
+        raise TypeError("oracle works on float64 arrays")
+    if A.ndim == 1:
+        if A.size > 1 and A.strides[0] != 8:
+            raise ValueError("vector must be contiguous")
+        return A.ctypes.data, max(1, A.shape[0])
+    if A.shape[0] > 1 and A.strides[0] != 8:
+        raise ValueError("matrix must be column-major (unit row stride)")
+    ld = A.strides[1] // 8 if A.shape[1] > 1 else A.shape[0]
+    return A.ctypes.data, max(1, ld)
+
+
+def _ch(c):
+    return c.encode() if isinstance(c, str) else c
+
+
+def _check(info, name):
+    if info < 0:
+        raise ValueError(f"{name}: illegal value of argument {-info}")
+    return info
+
+
+def fmat(shape, rng=None, kind="uniform01"):
+    """Column-major float64 matrix helper used by tests."""
+    if rng is None:
+        return np.zeros(shape, dtype=np.float64, order="F")
+    if kind == "uniform01":
+        return np.asfortranarray(rng.random(shape))
+    if kind == "uniform11":
+        return np.asfortranarray(rng.uniform(-1.0, 1.0, shape))
+    return np.asfortranarray(rng.standard_normal(shape))
+
+
+# ---- NextLA mirrors ---------------------------------------------------------
+
+def geqr2(m, n, A, tau, work):
+    pa, lda = _mat(A)
+    return _check(lib().ora_dgeqr2(m, n, pa, lda, _mat(tau)[0], _mat(work)[0]), "geqr2")
+
+
+def larft(direct, storev, n, k, V, tau, T):
+    pv, ldv = _mat(V)
+    pt, ldt = _mat(T)
+    return _check(lib().ora_dlarft(_ch(direct), _ch(storev), n, k, pv, ldv,
+                                   _mat(tau)[0], pt, ldt), "larft")
+
+
+def larfb(side, trans, direct, storev, m, n, k, V, ldv, T, C, work):
+    pv, _ = _mat(V)
+    pt, ldt = _mat(T)
+    pc, ldc = _mat(C)
+    pw, ldw = _mat(work)
+    return _check(lib().ora_dlarfb(_ch(side), _ch(trans), _ch(direct), _ch(storev), m, n, k,
+                                   pv, ldv, pt, ldt, pc, ldc, pw, ldw), "larfb")
+
+
+def geqrt(m, n, ib, A, T, tau, work):
+    pa, lda = _mat(A)
+    pt, ldt = _mat(T)
+    return _check(lib().ora_dgeqrt(m, n, ib, pa, lda, pt, ldt, _mat(tau)[0],
+                                   _mat(work)[0]), "geqrt")
+
+
+def unmqr(side, trans, m, n, k, ib, A, lda, T, C, work):
+    pa, _ = _mat(A)
+    pt, ldt = _mat(T)
+    pc, ldc = _mat(C)
+    pw, ldw = _mat(work)
+    return _check(lib().ora_dunmqr(_ch(side), _ch(trans), m, n, k, ib, pa, lda,
+                                   A.shape[0], A.shape[1], pt, ldt, pc, ldc, pw, ldw), "unmqr")
+
+
+def parfb(side, trans, m1, n1, m2, n2, k, A1, A2, V, T, work):
+    p1, ld1 = _mat(A1)
+    p2, ld2 = _mat(A2)
+    pv, ldv = _mat(V)
+    pt, ldt = _mat(T)
+    pw, ldw = _mat(work)
+    return _check(lib().ora_dparfb(_ch(side), _ch(trans), m1, n1, m2, n2, k, p1, ld1, p2, ld2,
+                                   pv, ldv, pt, ldt, pw, ldw), "parfb")
+
+
+def tsmqr(side, trans, m1, n1, m2, n2, k, ib, A1, A2, V, T, work):
+    p1, ld1 = _mat(A1)
+    p2, ld2 = _mat(A2)
+    pv, ldv = _mat(V)
+    pt, ldt = _mat(T)
+    kstored = min(V.shape[1], T.shape[1])
+    return _check(lib().ora_dtsmqr(_ch(side), _ch(trans), m1, n1, m2, n2, k, ib, kstored,
+                                   p1, ld1, p2, ld2, pv, ldv, pt, ldt, _mat(work)[0]), "tsmqr")
+
+
+def tsqrt(m, n, ib, A1, A2, T, tau, work):
+    p1, ld1 = _mat(A1)
+    p2, ld2 = _mat(A2)
+    pt, ldt = _mat(T)
+    return _check(lib().ora_dtsqrt(m, n, ib, A1.shape[0], p1, ld1, p2, ld2, pt, ldt,
+                                   _mat(tau)[0], _mat(work)[0]), "tsqrt")
+
+
+def tile_geqrf(A, nb, ib):
+    """Flat-tree tile QR of A in place; returns (T, tau) in the tile layouts."""
+    m, n = A.shape
+    MT = (m + nb - 1) // nb
+    T = np.zeros((MT * ib, n), order="F")
+    tau = np.zeros((n, MT), order="F")
+    pa, lda = _mat(A)
+    _check(lib().ora_dtile_geqrf(m, n, nb, ib, pa, lda, T.ctypes.data, MT * ib,
+                                 tau.ctypes.data, n), "tile_geqrf")
+    return T, tau
+
+
+def tile_unmqr(trans, A, T, B, nb, ib):
+    m, n = A.shape
+    pa, lda = _mat(A)
+    pt, ldt = _mat(T)
+    pb, ldb = _mat(B)
+    return _check(lib().ora_dtile_unmqr(_ch(trans), m, n, B.shape[1], nb, ib, pa, lda, pt, ldt,
+                                        pb, ldb), "tile_unmqr")
+
+
+def trsm_lun(R, B):
+    pr, ldr = _mat(R)
+    pb, ldb = _mat(B)
+    return _check(lib().ora_dtrsm_lun(R.shape[1], B.shape[1], pr, ldr, pb, ldb), "trsm")
+
+
+def tile_lstsq(A, B, nb, ib):
+    """min ||A X - B|| by tile QR: returns X (n-by-nrhs); A and B are copied."""
+    A = np.array(A, order="F", dtype=np.float64)
+    B = np.array(B, order="F", dtype=np.float64)
+    n = A.shape[1]
+    T, _ = tile_geqrf(A, nb, ib)
+    tile_unmqr("C", A, T, B, nb, ib)
+    X = np.array(B[:n], order="F")
+    trsm_lun(A[:n, :n], X)
+    return X

@@ -1,0 +1,113 @@
+"""Generate the LAPACK golden vectors that pin the oracle and the CUDA library.
+
+The reference (NextLA.jl) checks its tile kernels against LAPACK through
+libblastrampoline (test/lapack_helpers.jl: dtpqrt for tsqrt!, dtpmqrt for
+tsmqr!, ormqr/geqrt for geqrt!).  Julia is not available here, so the same
+LAPACK routines are called through scipy (scipy 1.18.1, OpenBLAS 0.3.34) on
+seeded inputs at the reference's own test shapes, plus one nb=256, ib=32 tile,
+the configuration the tile QR runs at.
+
+Run from the repository root:  python tests/golden/make_golden.py
+Writes tests/golden/lapack_golden.npz.
+"""
+import os
+
+import numpy as np
+from scipy.linalg import lapack
+
+OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lapack_golden.npz")
+
+
+def F(a):
+    return np.asfortranarray(a, dtype=np.float64)
+
+
+def Q24(a):
+    """Round inputs to 24 significant bits so the stored inputs compress well;
+    the LAPACK outputs computed from them stay full FP64."""
+    return F(np.ldexp(np.round(np.ldexp(a, 24)), -24))
+
+
+def main():
+    rng = np.random.default_rng(20240611)
+    g = {}
+    # geqrt (test/geqrt.jl:6-11 shapes) vs dgeqrt (same T layout, nb = ib).
+    for (m, n, ib) in [(20, 15, 4), (32, 32, 8), (64, 32, 16), (32, 64, 8), (256, 256, 32)]:
+        A = Q24(rng.random((m, n)))
+        a, t, info = lapack.dgeqrt(ib, A.copy(order="F"))
+        assert info == 0
+        key = f"geqrt_{m}_{n}_{ib}"
+        g[key + "_A"] = A
+        g[key + "_outA"] = F(a)
+        g[key + "_outT"] = F(t[:, : min(m, n)])
+    # tsqrt (test/tsqrt.jl:8-13 shapes, A1 = triu(rand) + 2I) vs dtpqrt(l=0, nb=ib).
+    for (m, n, ib) in [(32, 24, 8), (48, 32, 16), (64, 48, 16), (20, 20, 10), (256, 256, 32)]:
+        A1 = Q24(np.triu(rng.random((n, n))) + 2.0 * np.eye(n))
+        A2 = Q24(rng.random((m, n)))
+        a1, a2, t, info = lapack.dtpqrt(0, ib, A1.copy(order="F"), A2.copy(order="F"))
+        assert info == 0
+        key = f"tsqrt_{m}_{n}_{ib}"
+        g[key + "_A1"], g[key + "_A2"] = A1, A2
+        g[key + "_outA1"], g[key + "_outA2"], g[key + "_outT"] = F(a1), F(a2), F(t)
+    # tsmqr (test/tsmqr.jl:6-40: side x trans, random V, triu(T)) vs dtpmqrt(l=0).
+    for side in "LR":
+        for trans in "NC":
+            if side == "L":
+                m1, n1, m2, k, ib = 32, 24, 20, 16, 8
+                n2 = n1
+            else:
+                m1, n1, n2, k, ib = 24, 32, 20, 16, 8
+                m2 = m1
+            A1 = F(rng.random((m1, n1)))
+            A2 = F(rng.random((m2, n2)))
+            V = F(rng.random((m2, k) if side == "L" else (n2, k)))
+            T = F(np.triu(rng.random((ib, k))))
+            out1 = A1.copy(order="F")
+            sub = out1[:k] if side == "L" else out1[:, :k]
+            a1, a2, info = lapack.dtpmqrt(0, V, T, F(sub), A2.copy(order="F"), side=side,
+                                          trans="T" if trans == "C" else "N")
+            assert info == 0
+            if side == "L":
+                out1[:k] = a1
+            else:
+                out1[:, :k] = a1
+            key = f"tsmqr_{side}{trans}"
+            g[key + "_A1"], g[key + "_A2"], g[key + "_V"], g[key + "_T"] = A1, A2, V, T
+            g[key + "_outA1"], g[key + "_outA2"] = F(out1), F(a2)
+            g[key + "_dims"] = np.array([m1, n1, m2, n2, k, ib])
+    # tsmqr at the tile size the driver uses (nb = 256, ib = 32, 128 columns),
+    # left, transposed.
+    A1 = Q24(rng.standard_normal((256, 128)))
+    A2 = Q24(rng.standard_normal((256, 128)))
+    V = Q24(rng.standard_normal((256, 256)) / 16.0)
+    T = Q24(np.triu(rng.standard_normal((32, 256))) / 16.0)
+    a1, a2, info = lapack.dtpmqrt(0, V, T, A1.copy(order="F"), A2.copy(order="F"),
+                                  side="L", trans="T")
+    assert info == 0
+    g["tsmqr_big_A1"], g["tsmqr_big_A2"], g["tsmqr_big_V"], g["tsmqr_big_T"] = A1, A2, V, T
+    g["tsmqr_big_outA1"], g["tsmqr_big_outA2"] = F(a1), F(a2)
+    # unmqr (test/unmqr.jl:1-79, m, n, k, ib = 64, 48, 32, 8) vs dgemqrt.
+    m, n, k, ib = 64, 48, 32, 8
+    Aq = F(rng.random((m, k)))
+    aq, tq, info = lapack.dgeqrt(ib, Aq.copy(order="F"))
+    assert info == 0
+    g["unmqr_Aqr"], g["unmqr_T"] = F(aq), F(tq)
+    for side in "LR":
+        for trans in "NC":
+            C = F(rng.random((m, n) if side == "L" else (n, m)))
+            c, info = lapack.dgemqrt(aq, tq, C.copy(order="F"), side=side,
+                                     trans="T" if trans == "C" else "N")
+            assert info == 0
+            g[f"unmqr_{side}{trans}_C"], g[f"unmqr_{side}{trans}_out"] = C, F(c)
+    # larfg (test/larfg.jl:56-79) vs dlarfg.
+    for n in (2, 7, 33, 256):
+        x = rng.standard_normal(n)
+        alpha, xo, tau = lapack.dlarfg(n, x[0], x[1:].copy())
+        g[f"larfg_{n}_x"] = x
+        g[f"larfg_{n}_out"] = np.concatenate([[alpha], xo, [tau]])
+    np.savez_compressed(OUT, **g)
+    print("wrote", OUT, os.path.getsize(OUT), "bytes")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,105 @@
+"""Host-side checks of libtileqr.so that need no GPU.
+
+The library must load, export every entry point include/tileqr.h declares,
+and reject illegal arguments the way the reference throws ArgumentError
+(test/geqrt.jl:76-81, test/tsqrt.jl error set, test/tsmqr.jl:88-93,
+test/unmqr.jl:181-192) -- all before any CUDA call, so these run on a CPU host.
+Quick returns on empty sizes also return 0 without touching the device.
+"""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def L():
+    import tileqr_build
+    tileqr_build.build()
+    from tileqr import _lib
+    return _lib.lib()
+
+
+def header_symbols():
+    text = open(os.path.join(ROOT, "include", "tileqr.h")).read()
+    return sorted(set(re.findall(r"\b(tqr_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_exports_every_header_symbol(L):
+    syms = header_symbols()
+    assert len(syms) >= 24
+    missing = [s for s in syms if not hasattr(L, s)]
+    assert not missing, missing
+
+
+def test_python_signatures_cover_header():
+    from tileqr import _lib
+    declared = {f"tqr_{p}{n}" for n in _lib.SIGNATURES for p in "ds"}
+    assert set(header_symbols()) <= declared | set()
+
+
+NULL = None
+
+
+def test_geqrt_argument_errors(L):
+    assert L.tqr_dgeqrt(-1, 5, 2, NULL, 5, NULL, 2, NULL, NULL, NULL) == -1
+    assert L.tqr_dgeqrt(5, -1, 2, NULL, 5, NULL, 2, NULL, NULL, NULL) == -2
+    assert L.tqr_dgeqrt(5, 5, -1, NULL, 5, NULL, 2, NULL, NULL, NULL) == -3
+    assert L.tqr_dgeqrt(5, 5, 0, NULL, 5, NULL, 2, NULL, NULL, NULL) == -3
+    assert L.tqr_dgeqrt(0, 5, 0, NULL, 1, NULL, 1, NULL, NULL, NULL) == 0   # quick return
+    assert L.tqr_sgeqrt(-1, 5, 2, NULL, 5, NULL, 2, NULL, NULL, NULL) == -1
+
+
+def test_tsqrt_argument_errors(L):
+    assert L.tqr_dtsqrt(-1, 8, 4, 8, NULL, 8, NULL, 8, NULL, 4, NULL, NULL, NULL) == -1
+    assert L.tqr_dtsqrt(8, -1, 4, 8, NULL, 8, NULL, 8, NULL, 4, NULL, NULL, NULL) == -2
+    assert L.tqr_dtsqrt(8, 8, -1, 8, NULL, 8, NULL, 8, NULL, 4, NULL, NULL, NULL) == -3
+    assert L.tqr_dtsqrt(0, 8, 4, 8, NULL, 8, NULL, 8, NULL, 4, NULL, NULL, NULL) == 0
+
+
+def test_tsmqr_argument_errors(L):
+    args = (8, 8, 8, 8, 4, 2, NULL, 8, NULL, 8, NULL, 8, NULL, 2, NULL, 16, NULL)
+    assert L.tqr_dtsmqr(b"X", b"N", *args) == -1
+    assert L.tqr_dtsmqr(b"L", b"X", *args) == -2
+    # side 'L' needs n2 == n1, side 'R' needs m2 == m1 (src/tsmqr.jl:69-83)
+    assert L.tqr_dtsmqr(b"L", b"N", 8, 8, 8, 7, 4, 2, NULL, 8, NULL, 8, NULL, 8, NULL, 2, NULL, 16, NULL) == -6
+    assert L.tqr_dtsmqr(b"R", b"N", 8, 8, 7, 8, 4, 2, NULL, 8, NULL, 8, NULL, 8, NULL, 2, NULL, 16, NULL) == -5
+    # k = 0 is a no-op (test/tsmqr.jl:75-85)
+    assert L.tqr_dtsmqr(b"L", b"N", 8, 8, 8, 8, 0, 0, NULL, 8, NULL, 8, NULL, 8, NULL, 1, NULL, 0, NULL) == 0
+
+
+def test_unmqr_argument_errors(L):
+    a = (32, 24, 16, 4, NULL, 32, NULL, 4, NULL, 32, NULL, 24, NULL)
+    assert L.tqr_dunmqr(b"X", b"N", *a) == -1
+    assert L.tqr_dunmqr(b"L", b"X", *a) == -2
+    assert L.tqr_dunmqr(b"L", b"N", -1, 24, 16, 4, NULL, 32, NULL, 4, NULL, 32, NULL, 24, NULL) == -3
+    assert L.tqr_dunmqr(b"L", b"N", 32, 24, 0, 4, NULL, 32, NULL, 4, NULL, 32, NULL, 24, NULL) == 0
+
+
+def test_larfb_larft_edge_cases(L):
+    # test/larfb.jl:191-196 and test/larft.jl:207-210: empty work is a no-op
+    assert L.tqr_dlarfb(b"L", b"N", b"F", b"C", 0, 0, 0, NULL, 1, NULL, 1, NULL, 1, NULL, 1, NULL) == 0
+    assert L.tqr_dlarfb(b"L", b"N", b"F", b"C", 5, 5, 0, NULL, 5, NULL, 1, NULL, 5, NULL, 5, NULL) == 0
+    assert L.tqr_dlarfb(b"L", b"N", b"B", b"C", 5, 5, 2, NULL, 5, NULL, 2, NULL, 5, NULL, 5, NULL) == -3
+    assert L.tqr_dlarft(b"F", b"C", 0, 2, NULL, 1, NULL, NULL, 2, NULL) == 0
+
+
+def test_parfb_unsupported_forms_are_reported(L):
+    a = (4, 6, 4, 6, 3, 0, NULL, 4, NULL, 4, NULL, 4, NULL, 3, NULL, 3, NULL)
+    assert L.tqr_dparfb(b"L", b"N", b"F", b"R", *a) == -4
+    assert L.tqr_dparfb(b"L", b"N", b"B", b"C", *a) == -3
+    assert L.tqr_dparfb(b"L", b"N", b"F", b"C", 4, 6, 4, 6, 3, 4, NULL, 4, NULL, 4, NULL, 4, NULL, 3,
+                        NULL, 3, NULL) == -10   # l > k
+
+
+def test_tile_driver_argument_errors(L):
+    assert L.tqr_dtile_geqrf(-1, 4, 2, 1, NULL, 4, NULL, 2, NULL, 4, NULL) == -1
+    assert L.tqr_dtile_geqrf(4, 4, 0, 1, NULL, 4, NULL, 2, NULL, 4, NULL) == -3
+    assert L.tqr_dtile_geqrf(4, 4, 2, 3, NULL, 4, NULL, 2, NULL, 4, NULL) == -4
+    assert L.tqr_dtile_geqrf(0, 4, 2, 1, NULL, 1, NULL, 1, NULL, 4, NULL) == 0
+    assert L.tqr_dtile_unmqr(b"X", 4, 4, 1, 2, 1, NULL, 4, NULL, 2, NULL, 4, NULL) == -1
+    assert L.tqr_dtrsm_lun(-1, 1, NULL, 1, NULL, 1, NULL) == -1
+    assert L.tqr_dtile_gels(2, 4, 1, 2, 1, NULL, 2, NULL, 1, NULL, 4, NULL, 2, NULL) == -1
