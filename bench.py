@@ -1,0 +1,442 @@
+#!/usr/bin/env python3
+"""FP64 tile-QR throughput on GB300 -- the plain FP64 form of the tile QR.
+
+Workload (one "step"): flat-tree tile QR (geqrt on the diagonal tiles, tsqrt
+down each panel, unmqr/tsmqr trailing updates) of one 8192 x 8192 Float64
+matrix, tile nb = 256, inner block ib = 32, entries i.i.d. N(0, 1) from a
+fixed seed.  metric = algorithmic flops 4/3 n^3 per step / time, in TFLOP/s.
+
+Contract: `python bench.py --gpus N --steps K --warmup W [--impl reference]`
+prints ONE JSON line on rank 0.  Multi-GPU runs are replicas (one matrix per
+GPU; the single-matrix tile QR is not sharded), so scaling is weak.
+
+Timing: W untimed steps, then K steps between a barrier and a device sync on
+both sides, timed with CUDA events on the launching stream, max over ranks.
+Each step first restores A from a pristine copy (a 512 MiB device copy that
+is inside the timed region); A is larger than L2, so every step streams it.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "nextla.jl_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "tile-QR TFLOP/s (FP64, 8192^2)"
+UNIT = "TFLOP/s"
+NB, IB = 256, 32
+SEED = 20241203
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="tileqr", choices=["tileqr", "reference"])
+    p.add_argument("--n", type=int, default=8192, help="matrix order (default: the 8192^2 workload)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--kernel", default=None, choices=["tsmqr", "tsqrt", "geqrt"],
+                   help="time one tile kernel alone (for profiling) instead of the workload")
+    return p.parse_args()
+
+
+def kernel_bench(args):
+    """One tile kernel alone at the tile driver's shapes: tsmqr on a row band
+    (256 x (n - 256) pair of tiles rows), tsqrt / geqrt on one 256 x 256 tile."""
+    import torch
+
+    import tileqr as tq
+    import tileqr_build
+    tileqr_build.build()
+    tq.set_blocking(False)
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    n = args.n
+    res = {}
+    if args.kernel == "tsmqr":
+        w = n - NB
+        A1, A2, V = tq.empty(NB, w), tq.empty(NB, w), tq.empty(NB, NB)
+        for t in (A1, A2):
+            t.copy_(torch.randn(NB, w, generator=g, dtype=torch.float64, device="cuda"))
+        V.copy_(torch.randn(NB, NB, generator=g, dtype=torch.float64, device="cuda") / 16)
+        T = tq.empty(IB, NB)
+        T.copy_(torch.triu(torch.randn(IB, NB, generator=g, dtype=torch.float64, device="cuda")) / 16)
+        run = lambda: tq.tsmqr("L", "C", NB, w, NB, w, NB, IB, A1, A2, V, T, None)
+        fl = 4.0 * NB * NB * w
+    else:
+        A1 = tq.empty(NB, NB)
+        A2 = tq.empty(NB, NB)
+        R0 = torch.triu(torch.randn(NB, NB, generator=g, dtype=torch.float64, device="cuda"))
+        X0 = torch.randn(NB, NB, generator=g, dtype=torch.float64, device="cuda")
+        T = tq.zeros(IB, NB)
+        tau = torch.zeros(NB, dtype=torch.float64, device="cuda")
+
+        def run():
+            A1.copy_(R0 + 4 * torch.eye(NB, dtype=torch.float64, device="cuda"))
+            A2.copy_(X0)
+            if args.kernel == "tsqrt":
+                tq.tsqrt(NB, NB, IB, A1, A2, T, tau, None)
+            else:
+                tq.geqrt(NB, NB, IB, A2, T, tau, None)
+        fl = 2.0 * NB ** 3 if args.kernel == "tsqrt" else flops_square(NB)
+    for _ in range(max(1, args.warmup)):
+        run()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        run()
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    res = {"kernel": args.kernel, "n": n, "ms": min(times), "tflops": fl / min(times) / 1e9,
+           "all_ms": times}
+    print(json.dumps(res), flush=True)
+    return 0
+
+
+def flops_square(n):
+    return 4.0 / 3.0 * n ** 3
+
+
+def config(n, N):
+    return {"workload": f"flat-tree tile QR, {n}x{n} float64, nb={NB}, ib={IB}, entries N(0,1)",
+            "m": n, "n": n, "nb": NB, "ib": IB, "parallelism": f"replicas x{N}",
+            "l2": "inputs larger than L2 (A is 8 n^2 bytes, restored from a pristine copy each step)"}
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the oracle (C restatement of NextLA's kernels, flat-tree driver,
+# OpenMP over independent tile columns) on a bounded sample of the workload.
+# ---------------------------------------------------------------------------
+CPU_SAMPLE_N = 2048
+
+
+def cpu_sample_tflops(n=CPU_SAMPLE_N, reps=1):
+    import numpy as np
+    import oracle
+    oracle.build()
+    rng = np.random.default_rng(SEED)
+    A0 = np.asfortranarray(rng.standard_normal((n, n)))
+    best = None
+    times = []
+    for _ in range(reps):
+        A = A0.copy(order="F")
+        t0 = time.perf_counter()
+        oracle.tile_geqrf(A, NB, IB)
+        dt = time.perf_counter() - t0
+        times.append(dt)
+        best = dt if best is None else min(best, dt)
+    return flops_square(n) / best / 1e12, times
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def reduce_max(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args, world, rank):
+    """The reference arm: NextLA's algorithm on the host cores (the oracle port,
+    all host threads) on a bounded sample of the same workload."""
+    if rank != 0:
+        return 0
+    threads = cpu_threads()
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    n = CPU_SAMPLE_N
+    for _ in range(args.warmup):
+        cpu_sample_tflops(n)
+    times = []
+    for _ in range(args.steps):
+        _, t = cpu_sample_tflops(n)
+        times.append(t[0])
+    total = sum(times)
+    value = flops_square(n) * len(times) / total / 1e12
+    sample = (f"flat-tree tile QR of a {n}x{n} N(0,1) float64 matrix (nb={NB}, ib={IB}), the "
+              f"leading {n}x{n} block of the {args.n}^2 workload, per step")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic N(0,1), seeded", "config": config(args.n, args.gpus),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": ("Julia (the reference's language) is not installed on this host; the reference "
+                 "arm runs the C restatement of NextLA's kernels (oracle/nextla_oracle.c) with "
+                 "OpenMP over independent tile columns"),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def fp64_peak(tq_lib, torch):
+    """SIMT DFMA ceiling of this GPU (independent FMA chains), TFLOP/s."""
+    import ctypes
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, iters = sms * 8, 20000
+    out = torch.empty(blocks * 256, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream()
+    best = 0.0
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        rc = tq_lib.lib().tqr_fp64_peak_probe(blocks, iters, ctypes.c_void_p(out.data_ptr()),
+                                             ctypes.c_void_p(st.cuda_stream))
+        e1.record(st)
+        st.synchronize()
+        if rc != 0:
+            raise RuntimeError(f"fp64 probe failed: {rc}")
+        ms = e0.elapsed_time(e1)
+        best = max(best, 16.0 * iters * blocks * 256 / ms / 1e9)
+    return best
+
+
+def cublas_dgemm_tflops(torch, n=4096):
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    a @ b
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    a @ b
+    e1.record()
+    torch.cuda.synchronize()
+    return 2.0 * n ** 3 / e0.elapsed_time(e1) / 1e9
+
+
+def main():
+    args = parse()
+    if args.kernel:
+        return kernel_bench(args)
+    world, rank, local = dist_setup(args)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        rc = run_reference(args, world, rank)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return rc
+
+    import torch
+
+    import tileqr as tq
+    import tileqr_build
+    from tileqr import _lib
+
+    tileqr_build.build()
+    torch.cuda.set_device(local)
+    tq.set_blocking(False)
+    n = args.n
+    flops = flops_square(n)
+    g = torch.Generator(device="cuda").manual_seed(SEED + rank)
+    A0 = tq.empty(n, n)
+    A0.copy_(torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda"))
+    A = tq.empty(n, n)
+    ts, taus = tq.tile_shapes(n, n, NB, IB)
+    T = tq.zeros(*ts)
+    tau = tq.zeros(*taus)
+    st = torch.cuda.current_stream()
+
+    def step():
+        A.copy_(A0)
+        tq.tile_geqrf(A, NB, IB, T, tau)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+
+    clocks = Clocks(torch.cuda.current_device())
+    clocks.start()
+    _lib.profile_enable(True)
+    _lib.profile_read()
+    launches0 = _lib.launch_count()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(args.steps):
+        step()
+    e1.record(st)
+    torch.cuda.synchronize()
+    barrier(world)
+    launches = _lib.launch_count() - launches0
+    _lib.profile_enable(False)
+    prof_n, prof_ms, prof_flops = _lib.profile_read()
+    clk = clocks.stop()
+    ms_total = reduce_max(e0.elapsed_time(e1), world)
+    ms_step = ms_total / args.steps
+    value = flops * world * args.steps / (ms_total / 1e3) / 1e12
+
+    # roofline of the dominant kernel (the trailing update: band tsmqr/unmqr)
+    peak = fp64_peak(_lib, torch)
+    dgemm = cublas_dgemm_tflops(torch)
+    achieved = (prof_flops / prof_n) / (prof_ms / prof_n) / 1e9 if prof_n else None
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get("bytes_per_launch")
+        except (OSError, ValueError):
+            traffic = None
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "kernel": "k_apply (band tsmqr/unmqr trailing update), FP64 SIMT DFMA",
+                "peak_source": ("measured: DFMA-chain probe on this GPU (SIMT FP64 ceiling; "
+                                f"cuBLAS DGEMM measured alongside at {dgemm:.3f} TFLOP/s; the "
+                                "FP64 MMA path measured slower than SIMT on sm_103a)"),
+                "timed_launches": prof_n, "algorithmic_flops_per_launch": (prof_flops / prof_n) if prof_n else None,
+                "ms_per_launch": (prof_ms / prof_n) if prof_n else None}
+
+    # end to end through the public API: host buffers in, factor, host buffers out
+    e2e = None
+    if not args.no_e2e:
+        hA = torch.empty((n, n), dtype=torch.float64).pin_memory()
+        hA.copy_(A0.t().cpu())
+        hOut = torch.empty((n, n), dtype=torch.float64).pin_memory()
+        hT = torch.empty((ts[1], ts[0]), dtype=torch.float64).pin_memory()
+        Ad = tq.empty(n, n)
+
+        def e2e_step():
+            Ad.t().copy_(hA, non_blocking=True)         # H2D of the input matrix
+            tq.tile_geqrf(Ad, NB, IB, T, tau)
+            hOut.copy_(Ad.t(), non_blocking=True)       # D2H of R and V
+            hT.copy_(T.t(), non_blocking=True)          # D2H of T
+        e2e_step()
+        torch.cuda.synchronize()
+        ks = max(1, min(args.steps, 3))
+        barrier(world)
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(st)
+        for _ in range(ks):
+            e2e_step()
+        f1.record(st)
+        torch.cuda.synchronize()
+        ems = reduce_max(f0.elapsed_time(f1), world)
+        e2e = {"value": flops * world * ks / (ems / 1e3) / 1e12, "unit": UNIT,
+               "h2d_bytes_per_step": 8 * n * n, "d2h_bytes_per_step": 8 * n * n + 8 * ts[0] * ts[1],
+               "steps": ks, "ms_per_step": ems / ks}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = cpu_threads()
+        os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+        v, times = cpu_sample_tflops(CPU_SAMPLE_N, reps=2)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": (f"oracle (C restatement of NextLA's kernels, OpenMP over tile columns) "
+                          f"flat-tree tile QR of a {CPU_SAMPLE_N}x{CPU_SAMPLE_N} N(0,1) matrix, "
+                          f"nb={NB}, ib={IB}; best of {len(times)} runs of {min(times):.1f} s")}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic N(0,1), seeded", "config": config(n, world),
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -128,6 +128,20 @@ int tqr_dtile_gels(int m, int n, int nrhs, int nb, int ib, double *A, int lda, d
 int tqr_stile_gels(int m, int n, int nrhs, int nb, int ib, float *A, int lda, float *T, int ldt,
                    float *tau, int ldtau, float *B, int ldb, cudaStream_t stream);
 
+/* ---- Measurement hooks (no counterpart in NextLA; used by the benchmark) ----
+ * tqr_launch_count: kernels this library has launched since it was loaded.
+ * tqr_profile_enable / tqr_profile_read: while enabled, the tile driver brackets
+ * each trailing-update launch (the band unmqr and tsmqr calls) with CUDA events
+ * on the stream it runs on; read returns their count, summed device time (ms)
+ * and summed algorithmic flops (4 m2 k n per tsmqr, 2 n k (2 m - k) per
+ * unmqr), then forgets them.
+ * tqr_fp64_peak_probe: independent DFMA chains, 16 * iters * blocks * 256
+ * flops, writing blocks * 256 doubles to out -- the SIMT FP64 ceiling. */
+unsigned long long tqr_launch_count(void);
+void tqr_profile_enable(int on);
+int tqr_profile_read(long long *launches, double *device_ms, double *flops);
+int tqr_fp64_peak_probe(int blocks, int iters, double *out, cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

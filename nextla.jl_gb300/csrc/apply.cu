@@ -22,6 +22,7 @@
 // issue slots between DFMAs.  A CTA owns an NW-wide strip of columns (rows for
 // side R), so strips never interact and a call needs no global scratch.
 #include "common.cuh"
+#include "tileqr_internal.h"
 
 namespace tqr {
 
@@ -247,6 +248,7 @@ cudaError_t launch_apply(int mode, char side, char trans, int m, int n, int k, i
   if (e != cudaSuccess) return e;
   const int grid = (a.ncols + nw - 1) / nw;
   k_apply<R><<<grid, TQR_THREADS, sm, st>>>(a);
+  count_launch();
   return cudaGetLastError();
 }
 

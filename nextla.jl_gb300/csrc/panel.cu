@@ -26,6 +26,7 @@
 // trees), the Householder scalars (sqrt and two divisions) are computed once,
 // and the panel and T live in shared memory.
 #include "common.cuh"
+#include "tileqr_internal.h"
 
 namespace tqr {
 
@@ -418,6 +419,7 @@ cudaError_t launch_panel_qr(int m, int nc, R *A, int lda, R *tau, R *T, int ldt,
   cudaError_t e = allow_smem(k_panel_qr<R>, sm);
   if (e != cudaSuccess) return e;
   k_panel_qr<R><<<1, TQR_THREADS, sm, st>>>(m, nc, A, lda, tau, T, ldt, staged ? 1 : 0, stage_t ? 1 : 0);
+  count_launch();
   return cudaGetLastError();
 }
 
@@ -438,6 +440,7 @@ cudaError_t launch_tsqrt_block(int m, int sb, R *A1, int lda1, R *A2, int lda2, 
   cudaError_t e = allow_smem(k_tsqrt_block<R>, sm);
   if (e != cudaSuccess) return e;
   k_tsqrt_block<R><<<1, TQR_THREADS, sm, st>>>(m, sb, A1, lda1, A2, lda2, T, ldt, tau, staged ? 1 : 0);
+  count_launch();
   return cudaGetLastError();
 }
 
@@ -449,6 +452,7 @@ cudaError_t launch_larft(int direct_f, int storev_c, int n, int k, const R *V, i
   cudaError_t e = allow_smem(k_larft<R>, sm);
   if (e != cudaSuccess) return e;
   k_larft<R><<<1, TQR_THREADS, sm, st>>>(direct_f, storev_c, n, k, V, ldv, tau, T, ldt);
+  count_launch();
   return cudaGetLastError();
 }
 

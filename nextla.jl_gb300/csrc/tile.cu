@@ -134,8 +134,10 @@ int tile_geqrf(int m, int n, int nb, int ib, R *A, int lda, R *T, int ldt, R *ta
     if (ntrail > 0) {
       TQR_CU(cudaEventRecord(ds->ev_p, P));
       TQR_CU(cudaStreamWaitEvent(U, ds->ev_p, 0));
+      void *tok = prof_begin(U);
       TQR_TRY(K<R>::unmqr('L', 'C', mk, ntrail, kk, ib, Akk, lda, Tkk, ldt,
                           A + ix(k * nb, (k + 1) * nb, lda), lda, U));
+      prof_end(tok, U, 2.0 * ntrail * kk * (2.0 * mk - kk));
     }
     for (int i = k + 1; i < MT; ++i) {
       const int mi = nb < m - i * nb ? nb : m - i * nb;
@@ -145,8 +147,10 @@ int tile_geqrf(int m, int n, int nb, int ib, R *A, int lda, R *T, int ldt, R *ta
       if (ntrail > 0) {
         TQR_CU(cudaEventRecord(ds->ev_p, P));
         TQR_CU(cudaStreamWaitEvent(U, ds->ev_p, 0));
+        void *tok = prof_begin(U);
         TQR_TRY(K<R>::tsmqr('L', 'C', mk, ntrail, mi, ntrail, kk, ib, A + ix(k * nb, (k + 1) * nb, lda), lda,
                             A + ix(i * nb, (k + 1) * nb, lda), lda, Aik, lda, Tik, ldt, U));
+        prof_end(tok, U, 4.0 * mi * kk * (double)ntrail);
       }
     }
     TQR_CU(cudaEventRecord(ds->ev_u, U));
@@ -284,10 +288,12 @@ int trsm_lun(int n, int nrhs, const R *Rm, int ldr, R *B, int ldb, cudaStream_t 
   for (int b0 = ((n - 1) / bs) * bs; b0 >= 0; b0 -= bs) {
     const int nbk = bs < n - b0 ? bs : n - b0;
     k_trsv_block<R><<<nrhs, TQR_THREADS, 2 * nbk * sizeof(R), st>>>(nbk, Rm + ix(b0, b0, ldr), ldr, B + b0, ldb);
+    count_launch();
     TQR_CU(cudaGetLastError());
     if (b0 > 0) {
       dim3 grid((b0 + 63) / 64, (nrhs + 15) / 16);
       k_gemm_nn_sub<R><<<grid, TQR_THREADS, 0, st>>>(b0, nrhs, nbk, Rm + ix(0, b0, ldr), ldr, B + b0, ldb, B, ldb);
+      count_launch();
       TQR_CU(cudaGetLastError());
     }
   }

@@ -4,6 +4,13 @@
 
 namespace tqr {
 
+// Measurement hooks (diag.cu): every launcher counts its kernels; the tile
+// driver brackets its trailing-update launches with prof_begin/prof_end.
+void count_launch(unsigned long long n = 1);
+bool profiling();
+void *prof_begin(cudaStream_t st);
+void prof_end(void *tok, cudaStream_t st, double flops);
+
 // geqr2 (+ T when T != nullptr) on an m-by-nc panel, one CTA.
 template <typename R>
 cudaError_t launch_panel_qr(int m, int nc, R *A, int lda, R *tau, R *T, int ldt, cudaStream_t st);

@@ -30,6 +30,15 @@ SIGNATURES = {
     "tile_gels": [_I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
 }
 
+# measurement hooks without a precision prefix: name -> (argtypes, restype)
+DIAG = {
+    "tqr_launch_count": ([], ctypes.c_ulonglong),
+    "tqr_profile_enable": ([_I], None),
+    "tqr_profile_read": ([ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double),
+                          ctypes.POINTER(ctypes.c_double)], _I),
+    "tqr_fp64_peak_probe": ([_I, _I, _P, _P], _I),
+}
+
 _lib = None
 
 
@@ -49,8 +58,31 @@ def lib():
                 f = getattr(L, f"tqr_{p}{name}")
                 f.argtypes = args
                 f.restype = _I
+        for name, (args, res) in DIAG.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
         _lib = L
     return _lib
+
+
+def launch_count():
+    return int(lib().tqr_launch_count())
+
+
+def profile_enable(on):
+    lib().tqr_profile_enable(1 if on else 0)
+
+
+def profile_read():
+    """(launches, device ms, algorithmic flops) of the timed trailing updates."""
+    n = ctypes.c_longlong(0)
+    ms = ctypes.c_double(0)
+    fl = ctypes.c_double(0)
+    rc = lib().tqr_profile_read(ctypes.byref(n), ctypes.byref(ms), ctypes.byref(fl))
+    if rc != 0:
+        raise RuntimeError(f"tqr_profile_read: CUDA error {rc}")
+    return n.value, ms.value, fl.value
 
 
 def fn(prefix, name):

@@ -576,10 +576,16 @@ int ora_dtile_geqrf(int m, int n, int nb, int ib, double *A, int lda, double *T,
         double *Tkk = T + IDX(k * ib, k * nb, ldt);
         ora_dgeqrt(mk, nk, ib, Akk, lda, Tkk, ldt, tv, work);
         for (int c = 0; c < imin(mk, nk); ++c) tau[IDX(k * nb + c, k, ldtau)] = tv[c];
+        /* Tiles of different columns are independent: with OpenMP the column
+           loops run on all host threads (each call keeps its serial order, so
+           the result does not depend on the thread count). */
+#pragma omp parallel for schedule(dynamic)
         for (int j = k + 1; j < NT; ++j) {
             int nj = imin(nb, n - j * nb);
+            double *w = (double *)malloc(sizeof(double) * (size_t)nb * (size_t)nb);
             ora_dunmqr('L', 'C', mk, nj, imin(mk, nk), ib, Akk, lda, mk, nk, Tkk, ldt,
-                       A + IDX(k * nb, j * nb, lda), lda, work, nj);
+                       A + IDX(k * nb, j * nb, lda), lda, w, nj);
+            free(w);
         }
         for (int i = k + 1; i < MT; ++i) {
             int mi = imin(nb, m - i * nb);
@@ -587,11 +593,14 @@ int ora_dtile_geqrf(int m, int n, int nb, int ib, double *A, int lda, double *T,
             double *Tik = T + IDX(i * ib, k * nb, ldt);
             ora_dtsqrt(mi, nk, ib, mk, Akk, lda, Aik, lda, Tik, ldt, tv, work);
             for (int c = 0; c < imin(mk, nk); ++c) tau[IDX(k * nb + c, i, ldtau)] = tv[c];
+#pragma omp parallel for schedule(dynamic)
             for (int j = k + 1; j < NT; ++j) {
                 int nj = imin(nb, n - j * nb);
+                double *w = (double *)malloc(sizeof(double) * (size_t)nb * (size_t)nb);
                 ora_dtsmqr('L', 'C', mk, nj, mi, nj, imin(mk, nk), ib, imin(mk, nk),
                            A + IDX(k * nb, j * nb, lda), lda, A + IDX(i * nb, j * nb, lda), lda,
-                           Aik, lda, Tik, ldt, work);
+                           Aik, lda, Tik, ldt, w);
+                free(w);
             }
         }
     }

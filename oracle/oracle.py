@@ -22,7 +22,8 @@ _lib = None
 
 # -ffp-contract=off keeps x86 and Arm builds rounding identically (no fused
 # multiply-add contraction), so the oracle gives the same bits on both hosts.
-CFLAGS = ["-O2", "-fPIC", "-shared", "-std=c11", "-ffp-contract=off"]
+# -fopenmp parallelises only the tile driver's independent column loops.
+CFLAGS = ["-O2", "-fPIC", "-shared", "-std=c11", "-ffp-contract=off", "-fopenmp"]
 
 
 def build(force=False):

@@ -37,8 +37,8 @@ def test_exports_every_header_symbol(L):
 
 def test_python_signatures_cover_header():
     from tileqr import _lib
-    declared = {f"tqr_{p}{n}" for n in _lib.SIGNATURES for p in "ds"}
-    assert set(header_symbols()) <= declared | set()
+    declared = {f"tqr_{p}{n}" for n in _lib.SIGNATURES for p in "ds"} | set(_lib.DIAG)
+    assert set(header_symbols()) <= declared
 
 
 NULL = None

@@ -191,13 +191,14 @@ def test_tsqrt_zero_column_keeps_t(tq, oracle):
     n, m, ib = 16, 24, 8
     A10 = F(np.triu(rng.random((n, n))) + 2 * np.eye(n))
     A20 = F(rng.random((m, n)))
-    A20[:, 5] = 0.0
+    A20[:, 0] = 0.0          # column 0 is the only one no earlier reflector touches
     T0 = F(np.full((ib, n), 7.0))
     A1, A2, T, tau = dev(tq, A10), dev(tq, A20), dev(tq, T0), dev(tq, np.zeros(n))
     tq.tsqrt(m, n, ib, A1, A2, T, tau, None)
     A1o, A2o, To, tauo = A10.copy(order="F"), A20.copy(order="F"), T0.copy(order="F"), np.zeros(n)
     oracle.tsqrt(m, n, ib, A1o, A2o, To, tauo, np.zeros(ib * n))
-    assert host(tq, tau)[5] == 0.0
+    assert host(tq, tau)[0] == 0.0 and tauo[0] == 0.0
+    assert host(tq, T)[0, 0] == 7.0
     assert rel(host(tq, T), To) < RTOL
     assert rel(host(tq, A2), A2o) < RTOL
 

@@ -114,4 +114,5 @@ def test_full_size_properties(tq, m, n):
     Bh = B.cpu().numpy()
     Rh = R[:, cols].cpu().numpy()
     assert rel(Bh[:n], Rh) < 1e-12 * n
-    assert np.max(np.abs(Bh[n:])) < 1e-12 * n * np.max(np.abs(Rh))
+    if m > n:
+        assert np.max(np.abs(Bh[n:])) < 1e-12 * n * np.max(np.abs(Rh))
