@@ -107,6 +107,25 @@ int tqr_dtile_geqrf(int m, int n, int nb, int ib, double *A, int lda, double *T,
 int tqr_stile_geqrf(int m, int n, int nb, int ib, float *A, int lda, float *T, int ldt,
                     float *tau, int ldtau, cudaStream_t stream);
 
+/* The same factorisation as one persistent kernel over a task DAG (same
+ * results, bit for bit, as tqr_?tile_geqrf).  Needs m and n multiples of nb,
+ * nb <= 256 a multiple of ib; otherwise returns -3 (use tqr_?tile_geqrf).
+ * `work` is caller-owned device scratch of at least the size
+ * tqr_tile_dag_worksize reports, 256-byte aligned; it receives the task
+ * schedule and the dependency counters on every call.  Calls that overlap on
+ * the GPU need separate work buffers.  Every internal wait is bounded (20 s);
+ * tqr_tile_dag_status synchronises `stream` and reports 0 (ok) or 1 (a wait
+ * timed out: the result is invalid) with the task index. */
+int tqr_tile_dag_worksize(int m, int n, int nb, int ib, size_t *bytes);
+int tqr_dtile_geqrf_dag(int m, int n, int nb, int ib, double *A, int lda, double *T, int ldt,
+                        double *tau, int ldtau, void *work, size_t lwork, cudaStream_t stream);
+int tqr_stile_geqrf_dag(int m, int n, int nb, int ib, float *A, int lda, float *T, int ldt,
+                        float *tau, int ldtau, void *work, size_t lwork, cudaStream_t stream);
+int tqr_tile_dag_status(const void *work, int *status, int *task, cudaStream_t stream);
+/* Host-only self check of the schedule for a shape: replays the task list and
+ * confirms every closed-form wait target and the topological sort (0 = ok). */
+int tqr_tile_dag_check(int m, int n, int nb, int ib, long long *ntasks);
+
 /* B (m-by-nrhs) := Q^T B (trans 'C'/'T') or Q B (trans 'N'), Q from tile_geqrf. */
 int tqr_dtile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const double *A, int lda,
                     const double *T, int ldt, double *B, int ldb, cudaStream_t stream);

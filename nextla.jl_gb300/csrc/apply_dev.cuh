@@ -1,0 +1,211 @@
+// apply_dev.cuh -- one CTA applies a block reflector to one strip.
+//
+// Shared by the stand-alone apply kernel (apply.cu) and the persistent tile
+// DAG kernel (dag.cu).  Covers NextLA's larfb!, unmqr! (src/larfb.jl:37-142,
+// src/unmqr.jl:52-149) and tsmqr!/parfb!/pamm! with l = 0
+// (src/tsmqr.jl:47-146, src/parfb.jl:121-189, src/pamm.jl:104-128,306-325):
+//
+//   mode 0 (larfb/unmqr): the reflectors live in C's own rows; block b at row
+//          i uses V1 = unit-lower V[i:i+kb, i:i+kb] over C rows [i, i+kb) and
+//          V2 = V[i+kb:L, i:i+kb] over C rows [i+kb, L).
+//   mode 1 (tsmqr): V1 = I over a separate A1 (rows [i, i+kb)), V2 = V[0:L, i:i+kb]
+//          over all L rows of A2.
+//
+// For every block, in the reference's order:  W = A1/C1 rows + V^T C2,
+// W = op(T) W, A1/C1 rows -= W, C2 -= V W.  Right-side applies run the same
+// code on the transposed view (row stride ld, column stride 1): C op(Q) is
+// (op(Q)^T C^T)^T, which only swaps strides and whether T is transposed.
+//
+// GB300 mapping: FP64 runs at ~7.9 GFLOP/s per SM through the SIMT DFMA pipe
+// (the FP64 MMA path is slower on sm_103a) and every FP64 warp instruction
+// occupies an SM sub-partition's pipe for ~64 cycles.  So the strip (C, V
+// block, T block) sits in shared memory, each thread carries independent FMA
+// chains, and loads and index arithmetic hide between DFMAs.  Global reads go
+// through L2 (ld.global.cg): in the persistent kernel other SMs write the
+// same tiles between tasks, and L1 is not coherent with them.
+#pragma once
+#include "common.cuh"
+
+namespace tqr {
+
+template <typename R>
+struct ApplyArgs {
+  int mode;      // 0: larfb/unmqr, 1: tsmqr
+  int L;         // rows of the region (C rows for mode 0, A2 rows for mode 1), transposed view
+  int ncols;     // extent split into strips (columns of the transposed view)
+  int k, ib, fwd, transT;
+  R *C;          // element (r, c) at C[r * c_rs + c * c_cs]
+  int c_rs, c_cs;
+  R *A1;         // mode 1: element (r, c) at A1[r * a_rs + c * a_cs]
+  int a_rs, a_cs;
+  const R *V;    // column-major, ldv
+  int ldv;
+  const R *T;    // column-major, ldt; block at columns [i, i+kb)
+  int ldt;
+  int nw;        // strip width
+  int stage_c, stage_v, stage_t;
+};
+
+template <typename R>
+__device__ __forceinline__ R ldg_cg(const R *p) { return __ldcg(p); }
+
+__host__ __device__ inline size_t apply_smem_elems(int L, int ib, int nw, bool sc, bool sv, bool stt) {
+  size_t s = 2 * (size_t)ib * nw;
+  if (stt) s += (size_t)ib * ib;
+  if (sc) s += (size_t)odd_ld(L) * nw;
+  if (sv) s += (size_t)odd_ld(L) * ib;
+  return s;
+}
+
+// Apply to the strip of columns [c0, c0 + nw) (clamped to ncols).
+template <typename R>
+__device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_raw)
+{
+  const int tid = threadIdx.x;
+  const int nw = a.nw;
+  const int nwl = min(nw, a.ncols - c0);
+  if (nwl <= 0) return;
+  const int L = a.L, ib = a.ib;
+  const int ldw = ib;
+  const int ldcs = odd_ld(L), ldvs = odd_ld(L);
+
+  R *Ws = reinterpret_cast<R *>(smem_raw);                 // ib x nw
+  R *W2 = Ws + (size_t)ib * nw;                            // ib x nw
+  R *Ts = W2 + (size_t)ib * nw;                            // ib x ib (if staged)
+  R *Cs = Ts + (a.stage_t ? (size_t)ib * ib : 0);          // ldcs x nw (if staged)
+  R *Vs = Cs + (a.stage_c ? (size_t)ldcs * nw : 0);        // ldvs x ib (if staged)
+
+  // C strip: element (r, c) of the strip at Cp[r * crs + c * ccs]
+  R *const Cg = a.C + (size_t)c0 * a.c_cs;
+  R *Cp;
+  int crs, ccs;
+  if (a.stage_c) {
+    Cp = Cs; crs = 1; ccs = ldcs;
+    if (a.c_rs == 1) {
+      for (int idx = tid; idx < L * nwl; idx += TQR_THREADS) {
+        int r = idx % L, c = idx / L;
+        Cs[r + (size_t)c * ldcs] = ldg_cg(Cg + (size_t)r + (size_t)c * a.c_cs);
+      }
+    } else {
+      for (int idx = tid; idx < L * nwl; idx += TQR_THREADS) {
+        int c = idx % nwl, r = idx / nwl;
+        Cs[r + (size_t)c * ldcs] = ldg_cg(Cg + (size_t)r * a.c_rs + c);
+      }
+    }
+  } else {
+    Cp = Cg; crs = a.c_rs; ccs = a.c_cs;
+  }
+  R *const A1g = (a.mode == 1) ? a.A1 + (size_t)c0 * a.a_cs : nullptr;
+
+  const int nblk = (a.k + ib - 1) / ib;
+  for (int b = 0; b < nblk; ++b) {
+    const int i = a.fwd ? b * ib : (nblk - 1 - b) * ib;
+    const int kb = min(ib, a.k - i);
+    const int r0 = (a.mode == 0) ? i : 0;       // first region row this block touches
+    const int Lr = L - r0;
+    // V block: element (rr, p) = reflector i+p at region row r0+rr
+    const R *Vp;
+    int ldvp;
+    if (a.stage_v) {
+      for (int idx = tid; idx < Lr * kb; idx += TQR_THREADS) {
+        int rr = idx % Lr, p = idx / Lr;
+        R v;
+        if (a.mode == 0)
+          v = (rr < p) ? R(0) : (rr == p ? R(1) : ldg_cg(a.V + ix(r0 + rr, i + p, a.ldv)));
+        else
+          v = ldg_cg(a.V + ix(rr, i + p, a.ldv));
+        Vs[rr + (size_t)p * ldvs] = v;
+      }
+      Vp = Vs; ldvp = ldvs;
+    } else {
+      Vp = a.V + ix(r0, i, a.ldv); ldvp = a.ldv;
+    }
+    const R *Tp;
+    int ldtp;
+    if (a.stage_t) {
+      for (int idx = tid; idx < kb * kb; idx += TQR_THREADS) {
+        int p = idx % kb, q = idx / kb;
+        Ts[p + q * ib] = (p <= q) ? ldg_cg(a.T + ix(p, i + q, a.ldt)) : R(0);
+      }
+      Tp = Ts; ldtp = ib;
+    } else {
+      Tp = a.T + ix(0, i, a.ldt); ldtp = a.ldt;
+    }
+    __syncthreads();
+
+    // Phase 1: W[p, c] = (A1 or C1 row) + sum_rr V[rr, p] * C[r0 + rr, c]
+    // (mode 0 needs the unit-lower test only when V is read from global).
+    const bool vtri = (a.mode == 0) && !a.stage_v;
+    for (int e = tid; e < kb * nwl; e += TQR_THREADS) {
+      const int p = e % kb, c = e / kb;
+      R acc0 = 0, acc1 = 0;
+      const R *vcol = Vp + (size_t)p * ldvp;
+      const R *ccol = Cp + (size_t)r0 * crs + (size_t)c * ccs;
+      int rr = vtri ? p : 0;
+      if (vtri) { acc0 = ccol[(size_t)p * crs]; ++rr; }
+      for (; rr + 1 < Lr; rr += 2) {
+        acc0 = fma(vcol[rr], ccol[(size_t)rr * crs], acc0);
+        acc1 = fma(vcol[rr + 1], ccol[(size_t)(rr + 1) * crs], acc1);
+      }
+      if (rr < Lr) acc0 = fma(vcol[rr], ccol[(size_t)rr * crs], acc0);
+      R w = acc0 + acc1;
+      if (a.mode == 1) w += ldg_cg(A1g + (size_t)(i + p) * a.a_rs + (size_t)c * a.a_cs);
+      Ws[p + c * ldw] = w;
+    }
+    __syncthreads();
+    // Phase 2: W := op(T) W, T upper triangular kb-by-kb
+    for (int e = tid; e < kb * nwl; e += TQR_THREADS) {
+      const int p = e % kb, c = e / kb;
+      R acc = 0;
+      if (a.transT) {
+        for (int q = 0; q <= p; ++q) acc = fma(Tp[q + (size_t)p * ldtp], Ws[q + c * ldw], acc);
+      } else {
+        for (int q = p; q < kb; ++q) acc = fma(Tp[p + (size_t)q * ldtp], Ws[q + c * ldw], acc);
+      }
+      W2[p + c * ldw] = acc;
+    }
+    __syncthreads();
+    // Phase 3: C[r0 + rr, c] -= sum_p V[rr, p] W[p, c];  mode 1: A1 rows -= W
+    if (a.mode == 1) {
+      for (int e = tid; e < kb * nwl; e += TQR_THREADS) {
+        const int p = e % kb, c = e / kb;
+        R *dst = A1g + (size_t)(i + p) * a.a_rs + (size_t)c * a.a_cs;
+        *dst = ldg_cg(dst) - W2[p + c * ldw];
+      }
+    }
+    for (int rr = tid; rr < Lr; rr += TQR_THREADS) {
+      R acc[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) acc[c] = 0;
+      const int pmax = vtri ? min(kb, rr + 1) : kb;
+      for (int p = 0; p < pmax; ++p) {
+        R v = Vp[rr + (size_t)p * ldvp];
+        if (vtri && p == rr) v = R(1);
+        const R *wrow = W2 + p;
+#pragma unroll
+        for (int c = 0; c < 16; ++c)
+          if (c < nwl) acc[c] = fma(v, wrow[c * ldw], acc[c]);
+      }
+      R *crow = Cp + (size_t)(r0 + rr) * crs;
+#pragma unroll
+      for (int c = 0; c < 16; ++c)
+        if (c < nwl) crow[(size_t)c * ccs] -= acc[c];
+    }
+    __syncthreads();
+  }
+  if (a.stage_c) {
+    if (a.c_rs == 1) {
+      for (int idx = tid; idx < L * nwl; idx += TQR_THREADS) {
+        int r = idx % L, c = idx / L;
+        Cg[(size_t)r + (size_t)c * a.c_cs] = Cs[r + (size_t)c * ldcs];
+      }
+    } else {
+      for (int idx = tid; idx < L * nwl; idx += TQR_THREADS) {
+        int c = idx % nwl, r = idx / nwl;
+        Cg[(size_t)r * a.c_rs + c] = Cs[r + (size_t)c * ldcs];
+      }
+    }
+  }
+}
+
+}  // namespace tqr

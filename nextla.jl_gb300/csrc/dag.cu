@@ -1,0 +1,576 @@
+// dag.cu -- the tile QR as one persistent kernel over a task DAG.
+//
+// The flat-tree tile QR (NextLA's geqrt!/tsqrt!/unmqr!/tsmqr! composed in
+// PLASMA order, as the stream driver in tile.cu does) is cut into CTA-sized
+// tasks on nw-wide column strips of the nb-by-nb tiles:
+//
+//   GB(k,b)      geqr2 + T of block b of the diagonal tile (k,k)        1 CTA
+//   GA(k,b,s)    block b's reflectors applied to strip s of tile (k,k)   (larfb)
+//   UN(k,j,s)    all of (k,k)'s reflectors applied to strip s of (k,j)   (unmqr)
+//   TB(k,i,b)    tsqrt block b on [R of (k,k); tile (i,k)]               1 CTA
+//   TA(k,i,b,s)  that block applied to strip s of (k,k) and (i,k)        (tsmqr, one block)
+//   TM(k,i,j,s)  all of (i,k)'s reflectors applied to strip s of (k,j), (i,j)   (tsmqr)
+//
+// One launch with (SMs x resident CTAs) CTAs runs them all.  Each CTA takes
+// the next task index from a global counter, waits until the task's inputs
+// are written, runs it, and publishes its writes by bumping counters:
+//   ver(i,j,s)   number of completed tasks that wrote strip s of tile (i,j)
+//   done_g(k)    completed GB/GA tasks of diagonal tile k
+//   done_t(k,i)  completed TB/TA tasks of tsqrt(k,i)
+// Every writer of a strip is known in advance, so a task's wait targets are
+// closed-form counts (item_deps below); the host check tqr_tile_dag_check
+// recomputes them by replaying the task list.
+//
+// Task order: the host sorts the tasks by decreasing longest path to the end
+// of the DAG (estimated durations), which is a topological order that runs
+// the panel chain first.  Because tasks are taken strictly in that order, the
+// lowest unfinished task always has its inputs done, so the schedule cannot
+// deadlock even if only some CTAs are resident.  Every wait is still bounded
+// by a %globaltimer deadline: on expiry the task sets an error word in the
+// workspace and every CTA leaves; the host reads the word with
+// tqr_tile_dag_status.
+//
+// The DAG path needs m, n multiples of nb, nb a multiple of ib and ib a
+// multiple of nw (the benchmark shapes); other shapes use the stream driver.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "apply_dev.cuh"
+#include "panel_dev.cuh"
+#include "tileqr.h"
+#include "tileqr_internal.h"
+
+namespace tqr {
+
+enum : uint8_t { IT_GB = 0, IT_GA = 1, IT_UN = 2, IT_TB = 3, IT_TA = 4, IT_TM = 5 };
+
+struct DagItem {
+  uint8_t type, b;
+  uint16_t k, i, j, s;
+  uint16_t pad;
+};
+static_assert(sizeof(DagItem) == 12, "DagItem layout");
+
+struct DagGeom {
+  int m, n, nb, ib, nw;
+  int MT, NT, KT, NS, SPB, NBK;
+  __host__ __device__ int ver(int i, int j, int s) const { return (i * NT + j) * NS + s; }
+  __host__ __device__ int done_g(int k) const { return MT * NT * NS + k; }
+  __host__ __device__ int done_t(int k, int i) const { return MT * NT * NS + KT + k * MT + i; }
+  __host__ __device__ int ncounters() const { return MT * NT * NS + KT + KT * MT; }
+  // tasks of one geqrt (GB + GA) or one tsqrt (TB + TA)
+  __host__ __device__ int panel_tasks() const { return NBK + NBK * NS - SPB * NBK * (NBK + 1) / 2; }
+};
+
+constexpr int kMaxDeps = 2 * 16 + 1;
+
+// Wait targets: counter c must reach t before the task may run.
+__host__ __device__ inline int item_deps(const DagGeom &g, const DagItem &it, int *c, int *t) {
+  int n = 0;
+  const int k = it.k, i = it.i, j = it.j, b = it.b, s = it.s;
+  switch (it.type) {
+    case IT_GB:
+      for (int q = b * g.SPB; q < (b + 1) * g.SPB; ++q) { c[n] = g.ver(k, k, q); t[n++] = k + b; }
+      break;
+    case IT_GA:
+      c[n] = g.ver(k, k, s); t[n++] = k + b;
+      c[n] = g.ver(k, k, b * g.SPB); t[n++] = k + b + 1;
+      break;
+    case IT_UN:
+      c[n] = g.done_g(k); t[n++] = g.panel_tasks();
+      c[n] = g.ver(k, j, s); t[n++] = k;
+      break;
+    case IT_TB:
+      // (k,k): geqrt and each earlier tsqrt wrote b+1 times, this tsqrt b times
+      for (int q = b * g.SPB; q < (b + 1) * g.SPB; ++q) {
+        c[n] = g.ver(k, k, q); t[n++] = k + (i - k) * (b + 1) + b;
+        c[n] = g.ver(i, k, q); t[n++] = k + b;
+      }
+      break;
+    case IT_TA: {
+      const int bs = s / g.SPB;
+      c[n] = g.ver(k, k, s); t[n++] = k + (i - k) * (bs + 1) + b;
+      c[n] = g.ver(i, k, s); t[n++] = k + b;
+      c[n] = g.ver(i, k, b * g.SPB); t[n++] = k + b + 1;
+      break;
+    }
+    case IT_TM:
+      c[n] = g.done_t(k, i); t[n++] = g.panel_tasks();
+      c[n] = g.ver(k, j, s); t[n++] = i;
+      c[n] = g.ver(i, j, s); t[n++] = k;
+      break;
+  }
+  return n;
+}
+
+// Counters a task bumps when it is done.
+__host__ __device__ inline int item_updates(const DagGeom &g, const DagItem &it, int *c) {
+  int n = 0;
+  const int k = it.k, i = it.i, j = it.j, b = it.b, s = it.s;
+  switch (it.type) {
+    case IT_GB:
+      for (int q = b * g.SPB; q < (b + 1) * g.SPB; ++q) c[n++] = g.ver(k, k, q);
+      c[n++] = g.done_g(k);
+      break;
+    case IT_GA:
+      c[n++] = g.ver(k, k, s);
+      c[n++] = g.done_g(k);
+      break;
+    case IT_UN:
+      c[n++] = g.ver(k, j, s);
+      break;
+    case IT_TB:
+      for (int q = b * g.SPB; q < (b + 1) * g.SPB; ++q) {
+        c[n++] = g.ver(k, k, q);
+        c[n++] = g.ver(i, k, q);
+      }
+      c[n++] = g.done_t(k, i);
+      break;
+    case IT_TA:
+      c[n++] = g.ver(k, k, s);
+      c[n++] = g.ver(i, k, s);
+      c[n++] = g.done_t(k, i);
+      break;
+    case IT_TM:
+      c[n++] = g.ver(k, j, s);
+      c[n++] = g.ver(i, j, s);
+      break;
+  }
+  return n;
+}
+
+// ---------------------------------------------------------------------------
+// Workspace: [header 64 B][counters][items]
+// ---------------------------------------------------------------------------
+struct DagHeader {
+  int head;        // next task index
+  int error;       // 0 = ok; 1 = a wait timed out; 2 = schedule/arguments mismatch
+  int err_item;    // task index that reported the error
+  int err_type;
+  long long key;   // geometry key of the uploaded schedule
+  int nitems;
+  int pad[9];
+};
+static_assert(sizeof(DagHeader) == 64, "DagHeader layout");
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+template <typename R>
+struct DagArgs {
+  DagGeom g;
+  R *A; int lda;
+  R *T; int ldt;
+  R *tau; int ldtau;
+  DagHeader *hdr;
+  int *cnt;
+  const DagItem *items;
+  int nitems;
+  long long key;
+  unsigned long long timeout_ns;
+};
+
+__device__ __forceinline__ int ld_acquire(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+template <typename R>
+__device__ void run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *smem) {
+  const DagGeom &g = a.g;
+  const int nb = g.nb, ib = g.ib;
+  const int k = it.k, i = it.i, j = it.j, b = it.b, s = it.s;
+  auto tile = [&](int r, int c) { return a.A + ix(r * nb, c * nb, a.lda); };
+  auto ttile = [&](int r, int c) { return a.T + ix(r * ib, c * nb, a.ldt); };
+  auto tautile = [&](int r, int c) { return a.tau + ix(c * nb, r, a.ldtau); };
+  if (it.type == IT_GB) {
+    R *Ab = tile(k, k) + ix(b * ib, b * ib, a.lda);
+    panel_qr_cta<R>(nb - b * ib, ib, Ab, a.lda, tautile(k, k) + b * ib, ttile(k, k) + ix(0, b * ib, a.ldt),
+                    a.ldt, true, true, smem);
+    return;
+  }
+  if (it.type == IT_TB) {
+    tsqrt_block_cta<R>(nb, ib, tile(k, k) + ix(b * ib, b * ib, a.lda), a.lda, tile(i, k) + ix(0, b * ib, a.lda),
+                       a.lda, ttile(i, k) + ix(0, b * ib, a.ldt), a.ldt, tautile(i, k) + b * ib, true, smem);
+    return;
+  }
+  ApplyArgs<R> p;
+  p.ib = ib;
+  p.fwd = 1;
+  p.transT = 1;              // 'L', 'C': blocks forward, W := T^T W
+  p.c_rs = 1; p.c_cs = a.lda;
+  p.a_rs = 1; p.a_cs = a.lda;
+  p.ldv = a.lda;
+  p.ldt = a.ldt;
+  p.nw = g.nw;
+  p.ncols = nb;
+  p.stage_c = 1; p.stage_v = 1; p.stage_t = 1;
+  p.A1 = nullptr;
+  switch (it.type) {
+    case IT_GA:
+      p.mode = 0; p.L = nb - b * ib; p.k = ib;
+      p.C = tile(k, k) + ix(b * ib, 0, a.lda);
+      p.V = tile(k, k) + ix(b * ib, b * ib, a.lda);
+      p.T = ttile(k, k) + ix(0, b * ib, a.ldt);
+      break;
+    case IT_UN:
+      p.mode = 0; p.L = nb; p.k = nb;
+      p.C = tile(k, j);
+      p.V = tile(k, k);
+      p.T = ttile(k, k);
+      break;
+    case IT_TA:
+      p.mode = 1; p.L = nb; p.k = ib;
+      p.C = tile(i, k);
+      p.A1 = tile(k, k) + ix(b * ib, 0, a.lda);
+      p.V = tile(i, k) + ix(0, b * ib, a.lda);
+      p.T = ttile(i, k) + ix(0, b * ib, a.ldt);
+      break;
+    default:  // IT_TM
+      p.mode = 1; p.L = nb; p.k = nb;
+      p.C = tile(i, j);
+      p.A1 = tile(k, j);
+      p.V = tile(i, k);
+      p.T = ttile(i, k);
+      break;
+  }
+  apply_strip<R>(p, s * g.nw, smem);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(TQR_THREADS, 2)
+k_tile_dag(const DagArgs<R> a)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_it, s_err;
+  const int tid = threadIdx.x;
+  if (tid == 0) s_err = (a.hdr->key != a.key || a.hdr->nitems != a.nitems) ? 2 : 0;
+  __syncthreads();
+  if (s_err) {
+    if (tid == 0 && blockIdx.x == 0) atomicExch(&a.hdr->error, 2);
+    return;
+  }
+  for (;;) {
+    if (tid == 0) s_it = atomicAdd(&a.hdr->head, 1);
+    __syncthreads();
+    const int idx = s_it;
+    if (idx >= a.nitems) break;
+    const DagItem it = a.items[idx];
+    if (tid == 0) {
+      int c[kMaxDeps], t[kMaxDeps];
+      const int nd = item_deps(a.g, it, c, t);
+      const unsigned long long t0 = global_ns();
+      int err = 0;
+      for (int d = 0; d < nd && !err; ++d) {
+        while (ld_acquire(a.cnt + c[d]) < t[d]) {
+          if (ld_acquire(&a.hdr->error) != 0) { err = 1; break; }
+          if (global_ns() - t0 > a.timeout_ns) {
+            if (atomicCAS(&a.hdr->error, 0, 1) == 0) {
+              a.hdr->err_item = idx;
+              a.hdr->err_type = it.type;
+            }
+            err = 1;
+            break;
+          }
+          __nanosleep(128);
+        }
+      }
+      s_err = err;
+    }
+    __syncthreads();
+    if (s_err) break;
+    run_item<R>(a, it, smem_raw);
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      int c[kMaxDeps];
+      const int nu = item_updates(a.g, it, c);
+      for (int u = 0; u < nu; ++u) atomicAdd(a.cnt + c[u], 1);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host: schedule construction (cached per geometry)
+// ---------------------------------------------------------------------------
+struct Plan {
+  DagGeom g;
+  long long key;
+  std::vector<DagItem> items;       // sorted
+  // pinned host image of the upload: header at 0, items at 256 (page-locked so
+  // the copies stay asynchronous); falls back to pageable memory
+  unsigned char *pinned = nullptr;
+  std::vector<unsigned char> pageable;
+  size_t bytes_counters = 0, bytes_items = 0, bytes_total = 0;
+  const unsigned char *image() const { return pinned ? pinned : pageable.data(); }
+  ~Plan() {
+    if (pinned) cudaFreeHost(pinned);
+  }
+};
+
+static bool dag_geom(int m, int n, int nb, int ib, DagGeom *g) {
+  if (m <= 0 || n <= 0 || nb <= 0 || ib <= 0) return false;
+  if (m % nb || n % nb || nb % ib) return false;
+  if (nb > 256) return false;                  // one tile column of V per CTA in shared memory
+  int nw = 8;
+  while (nw > 1 && ib % nw) nw >>= 1;
+  g->m = m; g->n = n; g->nb = nb; g->ib = ib; g->nw = nw;
+  g->MT = m / nb; g->NT = n / nb; g->KT = std::min(g->MT, g->NT);
+  g->NS = nb / nw; g->SPB = ib / nw; g->NBK = nb / ib;
+  if (2 * g->SPB + 1 > kMaxDeps) return false;
+  if (g->MT > 65535 || g->NT > 65535 || g->NBK > 255) return false;
+  // every task's shared memory (checked for the wider type) must fit one CTA
+  const size_t sm = std::max({apply_smem_elems(nb, ib, nw, true, true, true) * sizeof(double),
+                              panel_smem<double>(nb, ib, true, true), tsqrt_smem<double>(nb, ib, true)});
+  if (sm > (size_t)TQR_SMEM_MAX) return false;
+  return true;
+}
+
+static long long geom_key(const DagGeom &g) {
+  long long h = 1469598103934665603LL;
+  for (int v : {g.m, g.n, g.nb, g.ib, g.nw}) h = (h ^ (long long)v) * 1099511628211LL;
+  return h & 0x7fffffffffffffffLL;
+}
+
+// Natural (generation) order: the algorithm's own loop order, topological.
+static void gen_items(const DagGeom &g, std::vector<DagItem> &v) {
+  v.clear();
+  auto push = [&](uint8_t type, int k, int i, int j, int b, int s) {
+    DagItem it;
+    it.type = type; it.b = (uint8_t)b; it.k = (uint16_t)k; it.i = (uint16_t)i; it.j = (uint16_t)j;
+    it.s = (uint16_t)s; it.pad = 0;
+    v.push_back(it);
+  };
+  for (int k = 0; k < g.KT; ++k) {
+    for (int b = 0; b < g.NBK; ++b) {
+      push(IT_GB, k, k, k, b, 0);
+      for (int s = (b + 1) * g.SPB; s < g.NS; ++s) push(IT_GA, k, k, k, b, s);
+    }
+    for (int j = k + 1; j < g.NT; ++j)
+      for (int s = 0; s < g.NS; ++s) push(IT_UN, k, k, j, 0, s);
+    for (int i = k + 1; i < g.MT; ++i) {
+      for (int b = 0; b < g.NBK; ++b) {
+        push(IT_TB, k, i, k, b, 0);
+        for (int s = (b + 1) * g.SPB; s < g.NS; ++s) push(IT_TA, k, i, k, b, s);
+      }
+      for (int j = k + 1; j < g.NT; ++j)
+        for (int s = 0; s < g.NS; ++s) push(IT_TM, k, i, j, 0, s);
+    }
+  }
+}
+
+static double item_cost(const DagGeom &g, const DagItem &it) {
+  // relative durations (FP64 FMAs per task, panel tasks weighted for their
+  // serial column steps)
+  const double nb = g.nb, ib = g.ib, nw = g.nw;
+  switch (it.type) {
+    case IT_GB: return 3.0 * (nb - it.b * ib) * ib * ib + 64.0 * ib * 600;
+    case IT_TB: return 3.0 * nb * ib * ib + 64.0 * ib * 600;
+    case IT_GA: return 4.0 * (nb - it.b * ib) * ib * nw;
+    case IT_TA: return 4.0 * nb * ib * nw;
+    case IT_UN: return 2.0 * nb * nb * nw;
+    default: return 4.0 * nb * nb * nw;
+  }
+}
+
+// Replays the natural order: for every counter the list of its writers.
+// Returns false if a wait target is not what the replay gives (tested on the
+// host by tqr_tile_dag_check).
+static bool build_schedule(const DagGeom &g, std::vector<DagItem> &sorted, bool verify) {
+  std::vector<DagItem> nat;
+  gen_items(g, nat);
+  const int N = (int)nat.size();
+  std::vector<std::vector<int>> writers(g.ncounters());
+  std::vector<std::vector<int>> preds(N);
+  int c[kMaxDeps], t[kMaxDeps];
+  bool ok = true;
+  for (int x = 0; x < N; ++x) {
+    const int nd = item_deps(g, nat[x], c, t);
+    for (int d = 0; d < nd; ++d) {
+      const auto &w = writers[c[d]];
+      // every target is exactly the number of writers generated before the
+      // task (for done counters: the whole group, which always precedes it)
+      if (verify && t[d] != (int)w.size()) ok = false;
+      if (t[d] > 0) {
+        if (t[d] <= (int)w.size()) preds[x].push_back(w[t[d] - 1]);
+        else ok = false;    // target never reached before this task
+      }
+    }
+    const int nu = item_updates(g, nat[x], c);
+    for (int u = 0; u < nu; ++u) writers[c[u]].push_back(x);
+  }
+  // done counters must end exactly at panel_tasks()
+  for (int k = 0; k < g.KT; ++k) {
+    if ((int)writers[g.done_g(k)].size() != g.panel_tasks()) ok = false;
+    for (int i = k + 1; i < g.MT; ++i)
+      if ((int)writers[g.done_t(k, i)].size() != g.panel_tasks()) ok = false;
+  }
+  // longest path to the end, natural order reversed
+  std::vector<double> rank(N, 0.0);
+  for (int x = N - 1; x >= 0; --x) {
+    rank[x] += item_cost(g, nat[x]);
+    for (int p : preds[x]) rank[p] = std::max(rank[p], rank[x]);
+  }
+  std::vector<int> order(N);
+  for (int x = 0; x < N; ++x) order[x] = x;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rank[a] > rank[b]; });
+  if (verify) {
+    std::vector<int> pos(N);
+    for (int x = 0; x < N; ++x) pos[order[x]] = x;
+    for (int x = 0; x < N; ++x)
+      for (int p : preds[x])
+        if (pos[p] >= pos[x]) ok = false;   // sorted order must stay topological
+  }
+  sorted.resize(N);
+  for (int x = 0; x < N; ++x) sorted[x] = nat[order[x]];
+  return ok;
+}
+
+static std::mutex g_plan_mu;
+static std::map<long long, std::shared_ptr<Plan>> g_plans;
+
+static std::shared_ptr<Plan> get_plan(const DagGeom &g) {
+  const long long key = geom_key(g);
+  std::lock_guard<std::mutex> l(g_plan_mu);
+  auto f = g_plans.find(key);
+  if (f != g_plans.end()) return f->second;
+  auto p = std::make_shared<Plan>();
+  p->g = g;
+  p->key = key;
+  build_schedule(g, p->items, false);
+  p->bytes_counters = align256(sizeof(int) * (size_t)g.ncounters());
+  p->bytes_items = align256(sizeof(DagItem) * p->items.size());
+  p->bytes_total = 256 + p->bytes_counters + p->bytes_items;
+  const size_t img = 256 + sizeof(DagItem) * p->items.size();
+  unsigned char *dst = nullptr;
+  if (cudaMallocHost((void **)&p->pinned, img) == cudaSuccess) {
+    dst = p->pinned;
+  } else {
+    p->pinned = nullptr;
+    cudaGetLastError();
+    p->pageable.resize(img);
+    dst = p->pageable.data();
+  }
+  DagHeader h;
+  std::memset(&h, 0, sizeof(h));
+  h.key = key;
+  h.nitems = (int)p->items.size();
+  std::memset(dst, 0, 256);
+  std::memcpy(dst, &h, sizeof(h));
+  std::memcpy(dst + 256, p->items.data(), sizeof(DagItem) * p->items.size());
+  g_plans[key] = p;
+  return p;
+}
+
+template <typename R>
+static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int ldt, R *tau,
+                          int ldtau, void *work, size_t lwork, cudaStream_t st) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (nb <= 0) return -3;
+  if (ib <= 0 || ib > nb) return -4;
+  if (m == 0 || n == 0) return 0;
+  DagGeom g;
+  if (!dag_geom(m, n, nb, ib, &g)) return -3;   // shape outside the DAG path
+  if (lda < m) return -6;
+  if (ldt < g.MT * ib) return -8;
+  if (ldtau < n) return -10;
+  if (!work || ((uintptr_t)work & 255)) return -11;
+  auto plan = get_plan(g);
+  if (lwork < plan->bytes_total) return -12;
+  unsigned char *w = (unsigned char *)work;
+  cudaError_t e;
+  // header (key, zero head and error) + zeroed counters + the schedule, all
+  // ordered on `st` ahead of the kernel
+  const unsigned char *img = plan->image();
+  if ((e = cudaMemcpyAsync(w, img, sizeof(DagHeader), cudaMemcpyHostToDevice, st)) != cudaSuccess) return (int)e;
+  if ((e = cudaMemsetAsync(w + 256, 0, plan->bytes_counters, st)) != cudaSuccess) return (int)e;
+  if ((e = cudaMemcpyAsync(w + 256 + plan->bytes_counters, img + 256, sizeof(DagItem) * plan->items.size(),
+                           cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    return (int)e;
+  DagArgs<R> a;
+  a.g = g;
+  a.A = A; a.lda = lda;
+  a.T = T; a.ldt = ldt;
+  a.tau = tau; a.ldtau = ldtau;
+  a.hdr = (DagHeader *)w;
+  a.cnt = (int *)(w + 256);
+  a.items = (const DagItem *)(w + 256 + plan->bytes_counters);
+  a.nitems = (int)plan->items.size();
+  a.key = plan->key;
+  a.timeout_ns = 20ull * 1000ull * 1000ull * 1000ull;   // 20 s for any single wait
+  const size_t sm = std::max({apply_smem_elems(nb, ib, g.nw, true, true, true) * sizeof(R),
+                              panel_smem<R>(nb, ib, true, true), tsqrt_smem<R>(nb, ib, true)});
+  if ((e = cudaFuncSetAttribute(k_tile_dag<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess)
+    return (int)e;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return (int)e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return (int)e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_dag<R>, TQR_THREADS, sm)) != cudaSuccess)
+    return (int)e;
+  if (per_sm < 1) return (int)cudaErrorInvalidConfiguration;
+  const int grid = std::min(sms * per_sm, a.nitems);
+  k_tile_dag<R><<<grid, TQR_THREADS, sm, st>>>(a);
+  count_launch();
+  e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : (int)e;
+}
+
+}  // namespace tqr
+
+using namespace tqr;
+
+extern "C" {
+
+int tqr_tile_dag_worksize(int m, int n, int nb, int ib, size_t *bytes) {
+  if (!bytes) return -5;
+  DagGeom g;
+  if (!dag_geom(m, n, nb, ib, &g)) {
+    *bytes = 0;
+    return 1;    // not eligible: use tqr_?tile_geqrf (stream driver, no workspace)
+  }
+  *bytes = get_plan(g)->bytes_total;
+  return 0;
+}
+
+int tqr_dtile_geqrf_dag(int m, int n, int nb, int ib, double *A, int lda, double *T, int ldt,
+                        double *tau, int ldtau, void *work, size_t lwork, cudaStream_t stream) {
+  return tile_geqrf_dag<double>(m, n, nb, ib, A, lda, T, ldt, tau, ldtau, work, lwork, stream);
+}
+
+int tqr_stile_geqrf_dag(int m, int n, int nb, int ib, float *A, int lda, float *T, int ldt,
+                        float *tau, int ldtau, void *work, size_t lwork, cudaStream_t stream) {
+  return tile_geqrf_dag<float>(m, n, nb, ib, A, lda, T, ldt, tau, ldtau, work, lwork, stream);
+}
+
+int tqr_tile_dag_status(const void *work, int *status, int *task, cudaStream_t stream) {
+  if (!work) return -1;
+  DagHeader h;
+  cudaError_t e = cudaMemcpyAsync(&h, work, sizeof(h), cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return (int)e;
+  if (status) *status = h.error;
+  if (task) *task = h.err_item;
+  return 0;
+}
+
+int tqr_tile_dag_check(int m, int n, int nb, int ib, long long *ntasks) {
+  DagGeom g;
+  if (!dag_geom(m, n, nb, ib, &g)) return 1;
+  std::vector<DagItem> items;
+  const bool ok = build_schedule(g, items, true);
+  if (ntasks) *ntasks = (long long)items.size();
+  return ok ? 0 : 2;
+}
+
+}  // extern "C"

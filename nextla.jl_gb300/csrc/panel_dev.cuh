@@ -1,0 +1,300 @@
+// panel_dev.cuh -- Householder panel factorisation by one CTA.
+//
+//  panel_qr_cta     geqr2 with the larft T build fused in (NextLA src/geqr2.jl:23-105
+//                   and src/larft.jl:53-86,112-124 for direct 'F', storev 'C').
+//  tsqrt_block_cta  one ib-block of tsqrt: reflectors of [A1 (upper); A2] and the
+//                   T block (NextLA src/tsqrt.jl:46-126).
+//
+// Shared by the stand-alone panel kernels (panel.cu) and the persistent tile
+// DAG kernel (dag.cu).  The reference runs each as a single work-item; here
+// the CTA works on every column together.  Both share one column step:
+//
+//   geqr2 at column i:  alpha = P[i,i], x = P[i+1:m, i], "row" = P[i, :]
+//   tsqrt at column i:  alpha = A1[i,i], x = A2[0:m, i], "row" = A1[i, :]
+//
+//   xnorm^2 = sum x^2; beta, tau, scale (one thread, broadcast); x *= scale;
+//   d_j = -tau (row[j] + x^T P[x rows, j]) for every other column j (j > i:
+//   the w of the rank-1 apply; j < i: the V^H v of the T column -- geqr2 keeps
+//   the row term there because row i of column j < i is part of v_j, tsqrt
+//   drops it because the A1 part of v_j is e_j);  row[j] += d_j and
+//   P[x rows, j] += x d_j for j > i;  T[0:i, i] = T[0:i, 0:i] d[0:i].
+//
+// On GB300 every FP64 warp instruction holds an SM sub-partition's FP64 pipe
+// for ~64 cycles whatever its active-lane count, and sqrt/div cost ~600 cycles.
+// So the step minimises dependent FP64 instructions: the dot products use one
+// thread per (column, row group) combined by a single add per group (no
+// shuffle trees), the Householder scalars are computed once, and the panel
+// and T live in shared memory.
+#pragma once
+#include "common.cuh"
+
+namespace tqr {
+
+template <typename R>
+struct ColumnStep {
+  R *P;       // x region rows live here (geqr2: the panel; tsqrt: A2)
+  int ldp;
+  R *row;     // row i of the factored matrix: row[j * rs]
+  int rs;
+  R *Ts;      // T (nc-by-nc upper), ld = ldts, or nullptr
+  int ldts;
+  R *part;    // TQR_THREADS partial sums
+  R *d;       // nc: -tau * (row[j] + x^T P[:, j])
+  R *scal;    // 4
+};
+
+// One column step.  x rows are [x0, m) of P, column i.  Returns false when
+// the reflector is the identity (tau = 0).  Contains the syncs it needs; all
+// threads call it with identical arguments.
+template <typename R>
+__device__ bool column_step(const ColumnStep<R> &c, int i, int x0, int m, int nc, bool tsqrt_form,
+                            R *tau_out, bool zero_t_on_skip)
+{
+  const int tid = threadIdx.x;
+  R *xcol = c.P + (size_t)i * c.ldp;
+  // ---- norm of x ----
+  R s = 0;
+  for (int r = x0 + tid; r < m; r += TQR_THREADS) {
+    R v = xcol[r];
+    s = fma(v, v, s);
+  }
+  s = warp_sum(s);
+  if ((tid & 31) == 0) c.part[tid >> 5] = s;
+  __syncthreads();
+  if (tid == 0) {
+    R t = 0;
+#pragma unroll
+    for (int w = 0; w < TQR_WARPS; ++w) t += c.part[w];
+    if (t != R(0)) {
+      R beta, tv, sc;
+      householder(c.row[(size_t)i * c.rs], t, beta, tv, sc);
+      c.scal[0] = beta; c.scal[1] = tv; c.scal[2] = sc; c.scal[3] = R(1);
+    } else {
+      c.scal[3] = R(0);
+    }
+  }
+  __syncthreads();
+  if (c.scal[3] == R(0)) {
+    if (tid == 0) *tau_out = R(0);
+    if (zero_t_on_skip && c.Ts)
+      for (int p = tid; p <= i; p += TQR_THREADS) c.Ts[p + (size_t)i * c.ldts] = R(0);
+    __syncthreads();
+    return false;
+  }
+  const R beta = c.scal[0], tv = c.scal[1], sc = c.scal[2];
+  for (int r = x0 + tid; r < m; r += TQR_THREADS) xcol[r] *= sc;
+  __syncthreads();
+  // ---- d_j for all j != i (j < i only when T is built) ----
+  const int jlo = c.Ts ? 0 : i + 1;
+  const int nj = nc - jlo;
+  if (nj > 0) {
+    if (nj <= TQR_THREADS) {
+      const int G = TQR_THREADS / nj;          // row groups
+      const int j = jlo + tid % nj, g = tid / nj;
+      if (g < G) {
+        R a0 = 0, a1 = 0;
+        if (j != i) {
+          const R *pc = c.P + (size_t)j * c.ldp;
+          int r = x0 + g;
+          for (; r + G < m; r += 2 * G) {
+            a0 = fma(pc[r], xcol[r], a0);
+            a1 = fma(pc[r + G], xcol[r + G], a1);
+          }
+          if (r < m) a0 = fma(pc[r], xcol[r], a0);
+        }
+        c.part[g * nj + (j - jlo)] = a0 + a1;
+      }
+      __syncthreads();
+      if (tid < nj) {
+        const int jj = jlo + tid;
+        R acc = 0;
+        for (int gg = 0; gg < G; ++gg) acc += c.part[gg * nj + tid];
+        if (jj > i || (!tsqrt_form && jj < i)) acc += c.row[(size_t)jj * c.rs];
+        c.d[jj] = -tv * acc;
+      }
+    } else {
+      const int lane = tid & 31, warp = tid >> 5;
+      for (int j = jlo + warp; j < nc; j += TQR_WARPS) {
+        if (j == i) continue;
+        const R *pc = c.P + (size_t)j * c.ldp;
+        R a = 0;
+        for (int r = x0 + lane; r < m; r += 32) a = fma(pc[r], xcol[r], a);
+        a = warp_sum(a);
+        if (lane == 0) {
+          if (j > i || (!tsqrt_form && j < i)) a += c.row[(size_t)j * c.rs];
+          c.d[j] = -tv * a;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // ---- rank-1 update of the columns right of i ----
+  {
+    const int ncol = nc - i - 1, rows = m - x0;
+    for (int j = i + 1 + tid; j < nc; j += TQR_THREADS) c.row[(size_t)j * c.rs] += c.d[j];
+    for (int idx = tid; idx < ncol * rows; idx += TQR_THREADS) {
+      const int rr = idx % rows, j = i + 1 + idx / rows;
+      R *pc = c.P + (size_t)j * c.ldp;
+      pc[x0 + rr] = fma(c.d[j], xcol[x0 + rr], pc[x0 + rr]);
+    }
+  }
+  // ---- T column i ----
+  if (c.Ts) {
+    for (int p = tid; p < i; p += TQR_THREADS) {
+      R acc = 0;
+      for (int q = p; q < i; ++q) acc = fma(c.Ts[p + (size_t)q * c.ldts], c.d[q], acc);
+      c.Ts[p + (size_t)i * c.ldts] = acc;
+    }
+    if (tid == 0) c.Ts[i + (size_t)i * c.ldts] = tv;
+  }
+  if (tid == 0) {
+    c.row[(size_t)i * c.rs] = beta;
+    *tau_out = tv;
+  }
+  __syncthreads();
+  return true;
+}
+
+template <typename R>
+__device__ inline R *carve(unsigned char *&p, size_t n) {
+  R *r = reinterpret_cast<R *>(p);
+  p += ((n * sizeof(R) + 15) / 16) * 16;
+  return r;
+}
+
+__host__ __device__ inline size_t rnd16(size_t b) { return ((b + 15) / 16) * 16; }
+
+template <typename R>
+__host__ __device__ inline size_t panel_smem(int m, int nc, bool staged, bool stage_t) {
+  size_t s = rnd16(sizeof(R) * TQR_THREADS) + rnd16(sizeof(R) * nc) + rnd16(sizeof(R) * 4);
+  if (stage_t) s += rnd16(sizeof(R) * (size_t)odd_ld(nc) * nc);
+  if (staged) s += rnd16(sizeof(R) * (size_t)odd_ld(m) * nc);
+  return s;
+}
+
+template <typename R>
+__host__ __device__ inline size_t tsqrt_smem(int m, int sb, bool staged) {
+  size_t s = rnd16(sizeof(R) * TQR_THREADS) + rnd16(sizeof(R) * sb) + rnd16(sizeof(R) * 4) +
+             2 * rnd16(sizeof(R) * (size_t)odd_ld(sb) * sb);
+  if (staged) s += rnd16(sizeof(R) * (size_t)odd_ld(m) * sb);
+  return s;
+}
+
+// geqr2 (+ T) on the m-by-nc panel A; T (nc-by-nc, ldt) may be nullptr.
+template <typename R>
+__device__ void panel_qr_cta(int m, int nc, R *A, int lda, R *tau, R *T, int ldt, bool staged,
+                             bool stage_t, unsigned char *smem_raw)
+{
+  unsigned char *sp = smem_raw;
+  const int tid = threadIdx.x;
+  ColumnStep<R> c;
+  c.part = carve<R>(sp, TQR_THREADS);
+  c.d = carve<R>(sp, nc);
+  c.scal = carve<R>(sp, 4);
+  if (T && stage_t) {
+    c.ldts = odd_ld(nc);
+    c.Ts = carve<R>(sp, (size_t)c.ldts * nc);
+  } else {
+    c.Ts = T;
+    c.ldts = ldt;
+  }
+  if (staged) {
+    c.ldp = odd_ld(m);
+    c.P = carve<R>(sp, (size_t)c.ldp * nc);
+    for (int idx = tid; idx < m * nc; idx += TQR_THREADS) {
+      int r = idx % m, cc = idx / m;
+      c.P[ix(r, cc, c.ldp)] = __ldcg(A + ix(r, cc, lda));
+    }
+  } else {
+    c.P = A;
+    c.ldp = lda;
+  }
+  __syncthreads();
+  const int k = min(m, nc);
+  for (int i = 0; i < k; ++i) {
+    c.row = c.P + i;
+    c.rs = c.ldp;
+    if (m - i <= 1) {                                  // geqr2.jl:32-35
+      if (tid == 0) tau[i] = R(0);
+      if (c.Ts)
+        for (int p = tid; p <= i; p += TQR_THREADS) c.Ts[p + (size_t)i * c.ldts] = R(0);
+      __syncthreads();
+      continue;
+    }
+    column_step<R>(c, i, i + 1, m, nc, false, tau + i, true);
+  }
+  if (staged) {
+    for (int idx = tid; idx < m * nc; idx += TQR_THREADS) {
+      int r = idx % m, cc = idx / m;
+      A[ix(r, cc, lda)] = c.P[ix(r, cc, c.ldp)];
+    }
+  }
+  if (T && stage_t) {
+    for (int idx = tid; idx < k * k; idx += TQR_THREADS) {
+      int p = idx % k, q = idx / k;
+      if (p <= q) T[ix(p, q, ldt)] = c.Ts[p + (size_t)q * c.ldts];
+    }
+  }
+  __syncthreads();
+}
+
+// One ib-block of tsqrt.  A1 points at A1[ii, ii] (sb-by-sb diagonal block,
+// only its upper triangle is read or written), A2 at A2[0, ii] (m-by-sb),
+// T at T[0, ii], tau at tau[ii].  A column whose A2 part is exactly zero gets
+// tau = 0 and leaves its T column untouched, as the reference does
+// (tsqrt.jl:61-64).
+template <typename R>
+__device__ void tsqrt_block_cta(int m, int sb, R *A1, int lda1, R *A2, int lda2, R *T, int ldt,
+                                R *tau, bool staged, unsigned char *smem_raw)
+{
+  unsigned char *sp = smem_raw;
+  const int tid = threadIdx.x;
+  ColumnStep<R> c;
+  c.part = carve<R>(sp, TQR_THREADS);
+  c.d = carve<R>(sp, sb);
+  c.scal = carve<R>(sp, 4);
+  const int ldb = odd_ld(sb);
+  R *B = carve<R>(sp, (size_t)ldb * sb);
+  c.ldts = odd_ld(sb);
+  c.Ts = carve<R>(sp, (size_t)c.ldts * sb);
+  for (int idx = tid; idx < sb * sb; idx += TQR_THREADS) {
+    int r = idx % sb, cc = idx / sb;
+    if (r <= cc) {
+      B[ix(r, cc, ldb)] = __ldcg(A1 + ix(r, cc, lda1));
+      c.Ts[r + (size_t)cc * c.ldts] = __ldcg(T + ix(r, cc, ldt));   // skipped columns keep T
+    }
+  }
+  if (staged) {
+    c.ldp = odd_ld(m);
+    c.P = carve<R>(sp, (size_t)c.ldp * sb);
+    for (int idx = tid; idx < m * sb; idx += TQR_THREADS) {
+      int r = idx % m, cc = idx / m;
+      c.P[ix(r, cc, c.ldp)] = __ldcg(A2 + ix(r, cc, lda2));
+    }
+  } else {
+    c.P = A2;
+    c.ldp = lda2;
+  }
+  __syncthreads();
+  c.rs = ldb;
+  for (int i = 0; i < sb; ++i) {
+    c.row = B + i;
+    column_step<R>(c, i, 0, m, sb, true, tau + i, false);
+  }
+  for (int idx = tid; idx < sb * sb; idx += TQR_THREADS) {
+    int r = idx % sb, cc = idx / sb;
+    if (r <= cc) {
+      A1[ix(r, cc, lda1)] = B[ix(r, cc, ldb)];
+      T[ix(r, cc, ldt)] = c.Ts[r + (size_t)cc * c.ldts];
+    }
+  }
+  if (staged) {
+    for (int idx = tid; idx < m * sb; idx += TQR_THREADS) {
+      int r = idx % m, cc = idx / m;
+      A2[ix(r, cc, lda2)] = c.P[ix(r, cc, c.ldp)];
+    }
+  }
+  __syncthreads();
+}
+
+}  // namespace tqr

@@ -300,8 +300,57 @@ def tile_shapes(m, n, nb, ib):
     return (MT * ib, n), (n, MT)
 
 
-def tile_geqrf(A, nb=256, ib=32, T=None, tau=None):
-    """Flat-tree tile QR of A in place; returns (T, tau)."""
+_WORK = {}
+
+
+def dag_worksize(m, n, nb, ib):
+    """Scratch bytes of the persistent-kernel tile QR, or None if the shape
+    is outside it (m, n multiples of nb <= 256, nb a multiple of ib)."""
+    import ctypes
+    b = ctypes.c_size_t(0)
+    rc = _lib.lib().tqr_tile_dag_worksize(m, n, nb, ib, ctypes.byref(b))
+    return int(b.value) if rc == 0 else None
+
+
+def dag_workspace(m, n, nb, ib, device):
+    """Cached device scratch for the DAG tile QR (one per shape and device)."""
+    size = dag_worksize(m, n, nb, ib)
+    if size is None:
+        return None
+    key = (str(device), size)
+    w = _WORK.get(key)
+    if w is None:
+        w = torch.empty(size + 256, dtype=torch.uint8, device=device)
+        _WORK[key] = w
+    off = (-w.data_ptr()) % 256
+    return w, off, size
+
+
+def dag_check(m, n, nb, ib):
+    """Host replay of the task schedule for a shape: (status, number of tasks)."""
+    import ctypes
+    nt = ctypes.c_longlong(0)
+    rc = _lib.lib().tqr_tile_dag_check(m, n, nb, ib, ctypes.byref(nt))
+    return rc, int(nt.value)
+
+
+def dag_status(work_ptr):
+    import ctypes
+    s, t = ctypes.c_int(0), ctypes.c_int(0)
+    rc = _lib.lib().tqr_tile_dag_status(ctypes.c_void_p(work_ptr), ctypes.byref(s), ctypes.byref(t),
+                                        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    if rc != 0:
+        raise RuntimeError(f"tile_dag_status: CUDA error {rc}")
+    return s.value, t.value
+
+
+def tile_geqrf(A, nb=256, ib=32, T=None, tau=None, dag=True):
+    """Flat-tree tile QR of A in place; returns (T, tau).
+
+    dag=True runs the single persistent-kernel schedule when the shape allows
+    it (scratch from a cached workspace), otherwise the stream driver; both
+    give the same bits."""
+    import ctypes
     m, n = A.shape
     ts, taus = tile_shapes(m, n, nb, ib)
     if T is None:
@@ -311,7 +360,24 @@ def tile_geqrf(A, nb=256, ib=32, T=None, tau=None):
     pa, lda = _mat(A)
     pt, ldt = _mat(T)
     pu, ldu = _mat(tau)
-    _call(_prefix(A, T, tau), "tile_geqrf", m, n, nb, ib, pa, lda, pt, ldt, pu, ldu)
+    ws = dag_workspace(m, n, nb, ib, A.device) if dag else None
+    if ws is None:
+        _call(_prefix(A, T, tau), "tile_geqrf", m, n, nb, ib, pa, lda, pt, ldt, pu, ldu)
+        return T, tau
+    w, off, size = ws
+    wp = w.data_ptr() + off
+    p = _prefix(A, T, tau)
+    st = torch.cuda.current_stream()
+    rc = getattr(_lib.lib(), f"tqr_{p}tile_geqrf_dag")(m, n, nb, ib, pa, lda, pt, ldt, pu, ldu,
+                                                      ctypes.c_void_p(wp), size, st.cuda_stream)
+    if rc < 0:
+        raise ArgumentError(f"tile_geqrf: illegal value of argument {-rc}")
+    if rc > 0:
+        raise RuntimeError(f"tile_geqrf: CUDA error {rc}")
+    if _BLOCKING:
+        status, task = dag_status(wp)
+        if status != 0:
+            raise RuntimeError(f"tile_geqrf: schedule wait timed out at task {task} (status {status})")
     return T, tau
 
 

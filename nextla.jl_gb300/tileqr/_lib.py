@@ -37,6 +37,11 @@ DIAG = {
     "tqr_profile_read": ([ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double),
                           ctypes.POINTER(ctypes.c_double)], _I),
     "tqr_fp64_peak_probe": ([_I, _I, _P, _P], _I),
+    "tqr_tile_dag_worksize": ([_I, _I, _I, _I, ctypes.POINTER(ctypes.c_size_t)], _I),
+    "tqr_dtile_geqrf_dag": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, ctypes.c_size_t, _P], _I),
+    "tqr_stile_geqrf_dag": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, ctypes.c_size_t, _P], _I),
+    "tqr_tile_dag_status": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I), _P], _I),
+    "tqr_tile_dag_check": ([_I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)], _I),
 }
 
 _lib = None

@@ -103,3 +103,22 @@ def test_tile_driver_argument_errors(L):
     assert L.tqr_dtile_unmqr(b"X", 4, 4, 1, 2, 1, NULL, 4, NULL, 2, NULL, 4, NULL) == -1
     assert L.tqr_dtrsm_lun(-1, 1, NULL, 1, NULL, 1, NULL) == -1
     assert L.tqr_dtile_gels(2, 4, 1, 2, 1, NULL, 2, NULL, 1, NULL, 4, NULL, 2, NULL) == -1
+
+
+@pytest.mark.parametrize("shape", [(1024, 1024, 256, 32), (2048, 1024, 256, 32), (1024, 2048, 256, 32),
+                                   (512, 512, 128, 32), (768, 512, 128, 16), (256, 256, 256, 32),
+                                   (1024, 1024, 256, 64), (8192, 8192, 256, 32), (65536, 512, 256, 32)])
+def test_dag_schedule_replay(L, shape):
+    """The persistent kernel's closed-form wait targets equal a replay of the task
+    list, every counter group completes, and the priority sort stays topological."""
+    import tileqr
+    rc, ntasks = tileqr.dag_check(*shape)
+    assert rc == 0 and ntasks > 0
+
+
+def test_dag_shape_eligibility(L):
+    import tileqr
+    assert tileqr.dag_worksize(1000, 1000, 256, 32) is None      # not a multiple of nb
+    assert tileqr.dag_worksize(1024, 1024, 512, 32) is None      # tile wider than one CTA holds
+    assert tileqr.dag_worksize(1024, 1024, 256, 128) is None     # T/V blocks exceed shared memory
+    assert tileqr.dag_worksize(8192, 8192, 256, 32) > 0

@@ -45,6 +45,43 @@ def test_tile_qr_vs_oracle(tq, oracle, m, n, nb, ib):
     assert rel(np.triu(tq.to_numpy(A)[:k]), np.triu(Ao[:k])) < tol
 
 
+@pytest.mark.parametrize("m,n,nb,ib", [(1024, 1024, 256, 32), (2048, 1024, 256, 32),
+                                       (1024, 2048, 256, 32), (512, 512, 128, 32),
+                                       (768, 512, 128, 16), (1024, 1024, 256, 64)])
+def test_dag_equals_stream_driver(tq, oracle, m, n, nb, ib):
+    """The persistent-kernel schedule runs the same per-strip arithmetic as the
+    stream driver, so the two agree bit for bit; both match the oracle."""
+    import torch
+    rng = np.random.default_rng(m + 3 * n + ib)
+    A0 = F(rng.standard_normal((m, n)))
+    Ad, As = tq.to_device(A0), tq.to_device(A0)
+    Td, taud = tq.tile_geqrf(Ad, nb, ib, dag=True)
+    Ts, taus = tq.tile_geqrf(As, nb, ib, dag=False)
+    torch.cuda.synchronize()
+    assert torch.equal(Ad, As)
+    assert torch.equal(Td, Ts)
+    assert torch.equal(taud, taus)
+    Ao = A0.copy(order="F")
+    To, _ = oracle.tile_geqrf(Ao, nb, ib)
+    assert rel(tq.to_numpy(Ad), Ao) < 1e-12 * max(m, n)
+    assert rel(tq.to_numpy(Td), To) < 1e-12 * max(m, n)
+
+
+def test_dag_repeated_calls_reuse_workspace(tq):
+    """Back-to-back factorisations through the same cached workspace."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(7)
+    A0 = tq.empty(1024, 1024)
+    A0.copy_(torch.randn(1024, 1024, generator=g, dtype=torch.float64, device="cuda"))
+    outs = []
+    for _ in range(3):
+        A = A0.clone()
+        T, _ = tq.tile_geqrf(A, 256, 32)
+        outs.append((A, T))
+    for A, T in outs[1:]:
+        assert torch.equal(A, outs[0][0]) and torch.equal(T, outs[0][1])
+
+
 @pytest.mark.parametrize("trans", ["C", "N"])
 def test_tile_unmqr_vs_oracle(tq, oracle, trans):
     """Config 1's second half: Q applied to 16 seeded right-hand sides."""
