@@ -358,6 +358,7 @@ def main():
     _lib.profile_enable(False)
     prof_n, prof_ms, prof_flops = _lib.profile_read()
     clk = clocks.stop()
+    dag = tq.dag_stats()
     ms_total = reduce_max(e0.elapsed_time(e1), world)
     ms_step = ms_total / args.steps
     value = flops * world * args.steps / (ms_total / 1e3) / 1e12
@@ -375,7 +376,8 @@ def main():
             traffic = None
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                "kernel": "k_apply (band tsmqr/unmqr trailing update), FP64 SIMT DFMA",
+                "kernel": ("k_tile_dag (one persistent launch per factorisation: panel, unmqr and "
+                           "tsmqr tasks), FP64 SIMT DFMA; algorithmic flops 4/3 n^3 per launch"),
                 "peak_source": ("measured: DFMA-chain probe on this GPU (SIMT FP64 ceiling; "
                                 f"cuBLAS DGEMM measured alongside at {dgemm:.3f} TFLOP/s; the "
                                 "FP64 MMA path measured slower than SIMT on sm_103a)"),
@@ -430,6 +432,7 @@ def main():
             "data": "synthetic N(0,1), seeded", "config": config(n, world),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": launches,
+            "dag_stats_last_step": dag,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -122,6 +122,11 @@ int tqr_dtile_geqrf_dag(int m, int n, int nb, int ib, double *A, int lda, double
 int tqr_stile_geqrf_dag(int m, int n, int nb, int ib, float *A, int lda, float *T, int ldt,
                         float *tau, int ldtau, void *work, size_t lwork, cudaStream_t stream);
 int tqr_tile_dag_status(const void *work, int *status, int *task, cudaStream_t stream);
+/* Statistics of the last run in `work` (synchronises `stream`), nanoseconds
+ * summed over CTAs: out[0..5] time running each task type (GB, GA, UN, TB,
+ * TA, TM), out[6] time waiting for inputs, out[7]/out[8] first and last
+ * %globaltimer stamps of the run. */
+int tqr_tile_dag_stats(const void *work, unsigned long long *out, cudaStream_t stream);
 /* Host-only self check of the schedule for a shape: replays the task list and
  * confirms every closed-form wait target and the topological sort (0 = ok). */
 int tqr_tile_dag_check(int m, int n, int nb, int ib, long long *ntasks);

@@ -7,18 +7,18 @@
 
 namespace tqr {
 
-template <typename R>
+template <typename R, int NW>
 __global__ void __launch_bounds__(TQR_THREADS)
 k_apply(const ApplyArgs<R> a)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  apply_strip<R>(a, blockIdx.x * a.nw, smem_raw);
+  apply_strip<R, NW>(a, blockIdx.x * NW, smem_raw);
 }
 
 template <typename R>
 ApplyArgs<R> make_apply_args(int mode, char side, char trans, int m, int n, int k, int ib, R *C,
                              int ldc, R *A1, int lda1, const R *V, int ldv, const R *T, int ldt,
-                             int nw_force, size_t *smem_bytes)
+                             size_t *smem_bytes)
 {
   ApplyArgs<R> a;
   const bool left = (side == 'L');
@@ -34,20 +34,36 @@ ApplyArgs<R> make_apply_args(int mode, char side, char trans, int m, int n, int 
   if (left) { a.L = m; a.ncols = n; a.c_rs = 1; a.c_cs = ldc; a.a_rs = 1; a.a_cs = lda1; }
   else      { a.L = n; a.ncols = m; a.c_rs = ldc; a.c_cs = 1; a.a_rs = lda1; a.a_cs = 1; }
   // Strip width and staging: prefer everything in shared memory with two
-  // CTAs per SM, then one CTA per SM, then read V / C from global.
+  // CTAs per SM and 16-wide strips, then narrower strips, then one CTA per SM,
+  // then V and C read from global.
   const size_t cap = (size_t)TQR_SMEM_MAX;
   const size_t half = cap / 2 - 1024;
-  int nw = nw_force > 0 ? nw_force : 16;
   bool sc = true, sv = true, stt = (ib <= 64);
   auto bytes = [&](int w) { return apply_smem_elems(a.L, ib, w, sc, sv, stt) * sizeof(R); };
-  if (nw_force <= 0 && bytes(nw) > half && bytes(8) <= half) nw = 8;
+  int nw = 16;
+  if (bytes(16) > half) {
+    if (bytes(8) <= half) nw = 8;
+    else if (bytes(16) <= cap) nw = 16;
+    else if (bytes(8) <= cap) nw = 8;
+  }
   if (bytes(nw) > cap) sv = false;
   if (bytes(nw) > cap) sc = false;
-  while (bytes(nw) > cap && nw > 1) nw >>= 1;
+  while (bytes(nw) > cap && nw > 1) nw = (nw == 16) ? 8 : (nw == 8 ? 4 : 1);
   a.nw = nw;
   a.stage_c = sc; a.stage_v = sv; a.stage_t = stt;
   *smem_bytes = bytes(nw);
   return a;
+}
+
+template <typename R, int NW>
+static cudaError_t launch_nw(const ApplyArgs<R> &a, size_t sm, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(k_apply<R, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)TQR_SMEM_MAX);
+  if (e != cudaSuccess) return e;
+  const int grid = (a.ncols + NW - 1) / NW;
+  k_apply<R, NW><<<grid, TQR_THREADS, sm, st>>>(a);
+  count_launch();
+  return cudaGetLastError();
 }
 
 // side: 'L' or 'R'; trans: 'N' or not.  For mode 0, C is the m-by-n matrix the
@@ -61,14 +77,14 @@ cudaError_t launch_apply(int mode, char side, char trans, int m, int n, int k, i
   if (m <= 0 || n <= 0 || k <= 0) return cudaSuccess;
   size_t sm = 0;
   ApplyArgs<R> a = make_apply_args<R>(mode, side, trans, m, n, k, ib, C, ldc, A1, lda1, V, ldv, T,
-                                      ldt, 0, &sm);
+                                      ldt, &sm);
   if (sm > (size_t)TQR_SMEM_MAX) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(k_apply<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TQR_SMEM_MAX);
-  if (e != cudaSuccess) return e;
-  const int grid = (a.ncols + a.nw - 1) / a.nw;
-  k_apply<R><<<grid, TQR_THREADS, sm, st>>>(a);
-  count_launch();
-  return cudaGetLastError();
+  switch (a.nw) {
+    case 16: return launch_nw<R, 16>(a, sm, st);
+    case 8: return launch_nw<R, 8>(a, sm, st);
+    case 4: return launch_nw<R, 4>(a, sm, st);
+    default: return launch_nw<R, 1>(a, sm, st);
+  }
 }
 
 template cudaError_t launch_apply<double>(int, char, char, int, int, int, int, double *, int, double *, int,

@@ -18,11 +18,13 @@
 //
 // GB300 mapping: FP64 runs at ~7.9 GFLOP/s per SM through the SIMT DFMA pipe
 // (the FP64 MMA path is slower on sm_103a) and every FP64 warp instruction
-// occupies an SM sub-partition's pipe for ~64 cycles.  So the strip (C, V
-// block, T block) sits in shared memory, each thread carries independent FMA
-// chains, and loads and index arithmetic hide between DFMAs.  Global reads go
-// through L2 (ld.global.cg): in the persistent kernel other SMs write the
-// same tiles between tasks, and L1 is not coherent with them.
+// occupies an SM sub-partition's pipe for ~64 cycles, whatever its active or
+// predicated lanes.  So the strip width NW is a compile-time constant (no
+// predicated-off FMAs in the inner loops), the strip, V block and T block sit
+// in shared memory, and each thread carries independent FMA chains; loads and
+// index arithmetic hide between DFMAs.  Global reads go through L2
+// (ld.global.cg): in the persistent kernel other SMs write the same tiles
+// between tasks, and L1 is not coherent with them.
 #pragma once
 #include "common.cuh"
 
@@ -42,38 +44,46 @@ struct ApplyArgs {
   int ldv;
   const R *T;    // column-major, ldt; block at columns [i, i+kb)
   int ldt;
-  int nw;        // strip width
+  int nw;        // strip width (the template argument of apply_strip)
   int stage_c, stage_v, stage_t;
 };
 
 template <typename R>
 __device__ __forceinline__ R ldg_cg(const R *p) { return __ldcg(p); }
 
+// Phase 2 keeps op(T) W in registers (up to kW2Regs entries per thread) and
+// only needs a second W buffer beyond that.
+constexpr int kW2Regs = 4;
+
+__host__ __device__ inline bool apply_w2_buffer(int ib, int nw) { return ib * nw > kW2Regs * TQR_THREADS; }
+
 __host__ __device__ inline size_t apply_smem_elems(int L, int ib, int nw, bool sc, bool sv, bool stt) {
-  size_t s = 2 * (size_t)ib * nw;
+  size_t s = (size_t)ib * nw;
+  if (apply_w2_buffer(ib, nw)) s += (size_t)ib * nw;
   if (stt) s += (size_t)ib * ib;
   if (sc) s += (size_t)odd_ld(L) * nw;
   if (sv) s += (size_t)odd_ld(L) * ib;
   return s;
 }
 
-// Apply to the strip of columns [c0, c0 + nw) (clamped to ncols).
-template <typename R>
+// Apply to the strip of columns [c0, c0 + NW) (clamped to ncols).
+template <typename R, int NW>
 __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_raw)
 {
   const int tid = threadIdx.x;
-  const int nw = a.nw;
-  const int nwl = min(nw, a.ncols - c0);
+  const int nwl = min(NW, a.ncols - c0);
   if (nwl <= 0) return;
   const int L = a.L, ib = a.ib;
   const int ldw = ib;
   const int ldcs = odd_ld(L), ldvs = odd_ld(L);
+  const bool w2buf = apply_w2_buffer(ib, NW);
 
-  R *Ws = reinterpret_cast<R *>(smem_raw);                 // ib x nw
-  R *W2 = Ws + (size_t)ib * nw;                            // ib x nw
-  R *Ts = W2 + (size_t)ib * nw;                            // ib x ib (if staged)
-  R *Cs = Ts + (a.stage_t ? (size_t)ib * ib : 0);          // ldcs x nw (if staged)
-  R *Vs = Cs + (a.stage_c ? (size_t)ldcs * nw : 0);        // ldvs x ib (if staged)
+  R *Ws = reinterpret_cast<R *>(smem_raw);                 // ib x NW
+  R *W2 = Ws + (w2buf ? (size_t)ib * NW : 0);              // ib x NW (only if w2buf)
+  R *Ts = W2 + (size_t)ib * NW;                            // ib x ib (if staged)
+  if (!w2buf) Ts = Ws + (size_t)ib * NW;
+  R *Cs = Ts + (a.stage_t ? (size_t)ib * ib : 0);          // ldcs x NW (if staged)
+  R *Vs = Cs + (a.stage_c ? (size_t)ldcs * NW : 0);        // ldvs x ib (if staged)
 
   // C strip: element (r, c) of the strip at Cp[r * crs + c * ccs]
   R *const Cg = a.C + (size_t)c0 * a.c_cs;
@@ -153,43 +163,93 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
       Ws[p + c * ldw] = w;
     }
     __syncthreads();
-    // Phase 2: W := op(T) W, T upper triangular kb-by-kb
-    for (int e = tid; e < kb * nwl; e += TQR_THREADS) {
+    // Phase 2: W := op(T) W, T upper triangular kb-by-kb (two partial sums per
+    // entry to halve the dependent FMA chain)
+    auto t_entry = [&](int e) -> R {
       const int p = e % kb, c = e / kb;
-      R acc = 0;
+      const R *wc = Ws + c * ldw;
+      R s0 = 0, s1 = 0;
       if (a.transT) {
-        for (int q = 0; q <= p; ++q) acc = fma(Tp[q + (size_t)p * ldtp], Ws[q + c * ldw], acc);
+        int q = 0;
+        for (; q + 1 <= p; q += 2) {
+          s0 = fma(Tp[q + (size_t)p * ldtp], wc[q], s0);
+          s1 = fma(Tp[q + 1 + (size_t)p * ldtp], wc[q + 1], s1);
+        }
+        if (q <= p) s0 = fma(Tp[q + (size_t)p * ldtp], wc[q], s0);
       } else {
-        for (int q = p; q < kb; ++q) acc = fma(Tp[p + (size_t)q * ldtp], Ws[q + c * ldw], acc);
+        int q = p;
+        for (; q + 1 < kb; q += 2) {
+          s0 = fma(Tp[p + (size_t)q * ldtp], wc[q], s0);
+          s1 = fma(Tp[p + (size_t)(q + 1) * ldtp], wc[q + 1], s1);
+        }
+        if (q < kb) s0 = fma(Tp[p + (size_t)q * ldtp], wc[q], s0);
       }
-      W2[p + c * ldw] = acc;
+      return s0 + s1;
+    };
+    const int ne = kb * nwl;
+    if (w2buf) {
+      for (int e = tid; e < ne; e += TQR_THREADS) W2[(e % kb) + (e / kb) * ldw] = t_entry(e);
+      __syncthreads();
+    } else {
+      R reg[kW2Regs];
+#pragma unroll
+      for (int u = 0; u < kW2Regs; ++u) {
+        const int e = tid + u * TQR_THREADS;
+        if (e < ne) reg[u] = t_entry(e);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int u = 0; u < kW2Regs; ++u) {
+        const int e = tid + u * TQR_THREADS;
+        if (e < ne) Ws[(e % kb) + (e / kb) * ldw] = reg[u];
+      }
+      __syncthreads();
     }
-    __syncthreads();
+    const R *Wf = w2buf ? W2 : Ws;
     // Phase 3: C[r0 + rr, c] -= sum_p V[rr, p] W[p, c];  mode 1: A1 rows -= W
     if (a.mode == 1) {
-      for (int e = tid; e < kb * nwl; e += TQR_THREADS) {
+      for (int e = tid; e < ne; e += TQR_THREADS) {
         const int p = e % kb, c = e / kb;
         R *dst = A1g + (size_t)(i + p) * a.a_rs + (size_t)c * a.a_cs;
-        *dst = ldg_cg(dst) - W2[p + c * ldw];
+        *dst = ldg_cg(dst) - Wf[p + c * ldw];
       }
     }
-    for (int rr = tid; rr < Lr; rr += TQR_THREADS) {
-      R acc[16];
+    if (nwl == NW) {
+      for (int rr = tid; rr < Lr; rr += TQR_THREADS) {
+        R acc[NW];
 #pragma unroll
-      for (int c = 0; c < 16; ++c) acc[c] = 0;
-      const int pmax = vtri ? min(kb, rr + 1) : kb;
-      for (int p = 0; p < pmax; ++p) {
-        R v = Vp[rr + (size_t)p * ldvp];
-        if (vtri && p == rr) v = R(1);
-        const R *wrow = W2 + p;
+        for (int c = 0; c < NW; ++c) acc[c] = 0;
+        const int pmax = vtri ? min(kb, rr + 1) : kb;
+        for (int p = 0; p < pmax; ++p) {
+          R v = Vp[rr + (size_t)p * ldvp];
+          if (vtri && p == rr) v = R(1);
+          const R *wrow = Wf + p;
 #pragma unroll
-        for (int c = 0; c < 16; ++c)
-          if (c < nwl) acc[c] = fma(v, wrow[c * ldw], acc[c]);
+          for (int c = 0; c < NW; ++c) acc[c] = fma(v, wrow[c * ldw], acc[c]);
+        }
+        R *crow = Cp + (size_t)(r0 + rr) * crs;
+#pragma unroll
+        for (int c = 0; c < NW; ++c) crow[(size_t)c * ccs] -= acc[c];
       }
-      R *crow = Cp + (size_t)(r0 + rr) * crs;
+    } else {
+      for (int rr = tid; rr < Lr; rr += TQR_THREADS) {
+        R acc[NW];
 #pragma unroll
-      for (int c = 0; c < 16; ++c)
-        if (c < nwl) crow[(size_t)c * ccs] -= acc[c];
+        for (int c = 0; c < NW; ++c) acc[c] = 0;
+        const int pmax = vtri ? min(kb, rr + 1) : kb;
+        for (int p = 0; p < pmax; ++p) {
+          R v = Vp[rr + (size_t)p * ldvp];
+          if (vtri && p == rr) v = R(1);
+          const R *wrow = Wf + p;
+#pragma unroll
+          for (int c = 0; c < NW; ++c)
+            if (c < nwl) acc[c] = fma(v, wrow[c * ldw], acc[c]);
+        }
+        R *crow = Cp + (size_t)(r0 + rr) * crs;
+#pragma unroll
+        for (int c = 0; c < NW; ++c)
+          if (c < nwl) crow[(size_t)c * ccs] -= acc[c];
+      }
     }
     __syncthreads();
   }

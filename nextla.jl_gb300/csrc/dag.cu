@@ -153,9 +153,15 @@ struct DagHeader {
   int err_type;
   long long key;   // geometry key of the uploaded schedule
   int nitems;
-  int pad[9];
+  int pad0;
+  // statistics (nanoseconds summed over CTAs): time running each task type,
+  // time spent waiting for inputs, and the first/last timestamps of the launch
+  unsigned long long busy_ns[6];
+  unsigned long long wait_ns;
+  unsigned long long t_first, t_last;
+  unsigned long long pad1[19];
 };
-static_assert(sizeof(DagHeader) == 64, "DagHeader layout");
+static_assert(sizeof(DagHeader) == 256, "DagHeader layout");
 
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -185,7 +191,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
-template <typename R>
+template <typename R, int NW>
 __device__ void run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *smem) {
   const DagGeom &g = a.g;
   const int nb = g.nb, ib = g.ib;
@@ -244,16 +250,18 @@ __device__ void run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *
       p.T = ttile(i, k);
       break;
   }
-  apply_strip<R>(p, s * g.nw, smem);
+  apply_strip<R, NW>(p, s * NW, smem);
 }
 
-template <typename R>
+template <typename R, int NW>
 __global__ void __launch_bounds__(TQR_THREADS, 2)
 k_tile_dag(const DagArgs<R> a)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_it, s_err;
   const int tid = threadIdx.x;
+  __shared__ unsigned long long s_tstart;
+  bool first = true;
   if (tid == 0) s_err = (a.hdr->key != a.key || a.hdr->nitems != a.nitems) ? 2 : 0;
   __syncthreads();
   if (s_err) {
@@ -286,12 +294,19 @@ k_tile_dag(const DagArgs<R> a)
         }
       }
       s_err = err;
+      const unsigned long long t1 = global_ns();
+      s_tstart = t1;
+      if (t1 > t0) atomicAdd(&a.hdr->wait_ns, t1 - t0);
+      if (first) { atomicMin(&a.hdr->t_first, t0); first = false; }
     }
     __syncthreads();
     if (s_err) break;
-    run_item<R>(a, it, smem_raw);
+    run_item<R, NW>(a, it, smem_raw);
     __syncthreads();
     if (tid == 0) {
+      const unsigned long long t2 = global_ns();
+      atomicAdd(&a.hdr->busy_ns[it.type], t2 - s_tstart);
+      atomicMax(&a.hdr->t_last, t2);
       __threadfence();
       int c[kMaxDeps];
       const int nu = item_updates(a.g, it, c);
@@ -322,8 +337,12 @@ static bool dag_geom(int m, int n, int nb, int ib, DagGeom *g) {
   if (m <= 0 || n <= 0 || nb <= 0 || ib <= 0) return false;
   if (m % nb || n % nb || nb % ib) return false;
   if (nb > 256) return false;                  // one tile column of V per CTA in shared memory
-  int nw = 8;
-  while (nw > 1 && ib % nw) nw >>= 1;
+  // 16-wide strips when two CTAs still fit per SM, else 8 (ib must be a multiple)
+  int nw = 16;
+  if (ib % 16 || 2 * (apply_smem_elems(nb, ib, 16, true, true, true) * sizeof(double) + 1024) >
+                     (size_t)TQR_SMEM_MAX + 1024)
+    nw = 8;
+  if (ib % nw) return false;
   g->m = m; g->n = n; g->nb = nb; g->ib = ib; g->nw = nw;
   g->MT = m / nb; g->NT = n / nb; g->KT = std::min(g->MT, g->NT);
   g->NS = nb / nw; g->SPB = ib / nw; g->NBK = nb / ib;
@@ -465,11 +484,34 @@ static std::shared_ptr<Plan> get_plan(const DagGeom &g) {
   std::memset(&h, 0, sizeof(h));
   h.key = key;
   h.nitems = (int)p->items.size();
+  h.t_first = ~0ull;
   std::memset(dst, 0, 256);
   std::memcpy(dst, &h, sizeof(h));
   std::memcpy(dst + 256, p->items.data(), sizeof(DagItem) * p->items.size());
   g_plans[key] = p;
   return p;
+}
+
+template <typename R, int NW>
+static int launch_dag(const DagArgs<R> &a, size_t sm, double flops, cudaStream_t st) {
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_tile_dag<R, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) !=
+      cudaSuccess)
+    return (int)e;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return (int)e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return (int)e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_dag<R, NW>, TQR_THREADS, sm)) !=
+      cudaSuccess)
+    return (int)e;
+  if (per_sm < 1) return (int)cudaErrorInvalidConfiguration;
+  const int grid = std::min(sms * per_sm, a.nitems);
+  void *tok = prof_begin(st);
+  k_tile_dag<R, NW><<<grid, TQR_THREADS, sm, st>>>(a);
+  prof_end(tok, st, flops);
+  count_launch();
+  e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : (int)e;
 }
 
 template <typename R>
@@ -511,19 +553,9 @@ static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int
   a.timeout_ns = 20ull * 1000ull * 1000ull * 1000ull;   // 20 s for any single wait
   const size_t sm = std::max({apply_smem_elems(nb, ib, g.nw, true, true, true) * sizeof(R),
                               panel_smem<R>(nb, ib, true, true), tsqrt_smem<R>(nb, ib, true)});
-  if ((e = cudaFuncSetAttribute(k_tile_dag<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess)
-    return (int)e;
-  int dev = 0, sms = 0, per_sm = 0;
-  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return (int)e;
-  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return (int)e;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_dag<R>, TQR_THREADS, sm)) != cudaSuccess)
-    return (int)e;
-  if (per_sm < 1) return (int)cudaErrorInvalidConfiguration;
-  const int grid = std::min(sms * per_sm, a.nitems);
-  k_tile_dag<R><<<grid, TQR_THREADS, sm, st>>>(a);
-  count_launch();
-  e = cudaGetLastError();
-  return e == cudaSuccess ? 0 : (int)e;
+  const double mn = (double)std::max(m, n), kn = (double)std::min(m, n);
+  const double flops = 2.0 * mn * kn * kn - 2.0 * kn * kn * kn / 3.0;
+  return g.nw == 16 ? launch_dag<R, 16>(a, sm, flops, st) : launch_dag<R, 8>(a, sm, flops, st);
 }
 
 }  // namespace tqr
@@ -561,6 +593,19 @@ int tqr_tile_dag_status(const void *work, int *status, int *task, cudaStream_t s
   if (e != cudaSuccess) return (int)e;
   if (status) *status = h.error;
   if (task) *task = h.err_item;
+  return 0;
+}
+
+int tqr_tile_dag_stats(const void *work, unsigned long long *out, cudaStream_t stream) {
+  if (!work || !out) return -1;
+  DagHeader h;
+  cudaError_t e = cudaMemcpyAsync(&h, work, sizeof(h), cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return (int)e;
+  for (int q = 0; q < 6; ++q) out[q] = h.busy_ns[q];
+  out[6] = h.wait_ns;
+  out[7] = h.t_first;
+  out[8] = h.t_last;
   return 0;
 }
 

@@ -344,6 +344,28 @@ def dag_status(work_ptr):
     return s.value, t.value
 
 
+_LAST_DAG_WORK = None
+
+DAG_TASKS = ("GB", "GA", "UN", "TB", "TA", "TM")
+
+
+def dag_stats():
+    """Busy time per task type, total wait time and span (ms, summed over CTAs)
+    of the last persistent-kernel tile QR; synchronises the current stream."""
+    import ctypes
+    if _LAST_DAG_WORK is None:
+        return None
+    out = (ctypes.c_ulonglong * 9)()
+    rc = _lib.lib().tqr_tile_dag_stats(ctypes.c_void_p(_LAST_DAG_WORK), out,
+                                       ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    if rc != 0:
+        raise RuntimeError(f"tile_dag_stats: CUDA error {rc}")
+    res = {f"busy_ms_{t}": out[q] / 1e6 for q, t in enumerate(DAG_TASKS)}
+    res["wait_ms"] = out[6] / 1e6
+    res["span_ms"] = (out[8] - out[7]) / 1e6 if out[8] > out[7] else None
+    return res
+
+
 def tile_geqrf(A, nb=256, ib=32, T=None, tau=None, dag=True):
     """Flat-tree tile QR of A in place; returns (T, tau).
 
@@ -364,8 +386,10 @@ def tile_geqrf(A, nb=256, ib=32, T=None, tau=None, dag=True):
     if ws is None:
         _call(_prefix(A, T, tau), "tile_geqrf", m, n, nb, ib, pa, lda, pt, ldt, pu, ldu)
         return T, tau
+    global _LAST_DAG_WORK
     w, off, size = ws
     wp = w.data_ptr() + off
+    _LAST_DAG_WORK = wp
     p = _prefix(A, T, tau)
     st = torch.cuda.current_stream()
     rc = getattr(_lib.lib(), f"tqr_{p}tile_geqrf_dag")(m, n, nb, ib, pa, lda, pt, ldt, pu, ldu,
