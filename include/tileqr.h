@@ -131,6 +131,25 @@ int tqr_tile_dag_stats(const void *work, unsigned long long *out, cudaStream_t s
  * confirms every closed-form wait target and the topological sort (0 = ok). */
 int tqr_tile_dag_check(int m, int n, int nb, int ib, long long *ntasks);
 
+/* Allocation-free tile QR (no counterpart in NextLA).  Same factorisation and
+ * the same bits as tqr_dtile_geqrf_dag, but it needs no `work` argument: for
+ * callers that cannot hand the library device memory -- code running while a
+ * framework's caching allocator owns the device, host code that must not
+ * take the implicit synchronisation of cudaMalloc/cudaFree mid-pipeline, or
+ * bindings with nowhere to keep a scratch buffer between calls.  The
+ * schedule and its counters live in a fixed 4 MiB device array inside this
+ * library (held by every GPU that loads it until exit), which covers e.g.
+ * every square matrix up to 8192 with nb = 256, ib = 32; larger problems get
+ * TQR_ERR_SCRATCH_TOO_SMALL and nothing is launched.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress), so make
+ * that first call before any stream capture.  Each call clears the counters
+ * it needs; all calls share the one array, so calls whose kernels overlap on
+ * the GPU (different streams, several host threads) race and must be
+ * serialised by the caller.  No cudaMalloc, cudaFree or other allocation. */
+#define TQR_ERR_SCRATCH_TOO_SMALL (-1000)
+int tqr_dtile_geqrf_noalloc(int m, int n, int nb, int ib, double *A, int lda, double *T, int ldt,
+                            double *tau, int ldtau, cudaStream_t stream);
+
 /* B (m-by-nrhs) := Q^T B (trans 'C'/'T') or Q B (trans 'N'), Q from tile_geqrf. */
 int tqr_dtile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const double *A, int lda,
                     const double *T, int ldt, double *B, int ldb, cudaStream_t stream);

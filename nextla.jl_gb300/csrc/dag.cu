@@ -362,30 +362,45 @@ static long long geom_key(const DagGeom &g) {
 }
 
 // Natural (generation) order: the algorithm's own loop order, topological.
-static void gen_items(const DagGeom &g, std::vector<DagItem> &v) {
-  v.clear();
-  auto push = [&](uint8_t type, int k, int i, int j, int b, int s) {
+// Tasks of step k in the algorithm's loop order.
+__host__ __device__ inline long long step_tasks(const DagGeom &g, int k) {
+  const long long pt = g.panel_tasks(), right = (long long)(g.NT - k - 1) * g.NS;
+  return pt + right + (long long)(g.MT - k - 1) * (pt + right);
+}
+
+// Writes the tasks of step k into out[] in loop order; returns their count.
+__host__ __device__ inline long long gen_step(const DagGeom &g, int k, DagItem *out) {
+  long long n = 0;
+  auto push = [&](uint8_t type, int i, int j, int b, int s) {
     DagItem it;
     it.type = type; it.b = (uint8_t)b; it.k = (uint16_t)k; it.i = (uint16_t)i; it.j = (uint16_t)j;
     it.s = (uint16_t)s; it.pad = 0;
-    v.push_back(it);
+    out[n++] = it;
   };
-  for (int k = 0; k < g.KT; ++k) {
+  for (int b = 0; b < g.NBK; ++b) {
+    push(IT_GB, k, k, b, 0);
+    for (int s = (b + 1) * g.SPB; s < g.NS; ++s) push(IT_GA, k, k, b, s);
+  }
+  for (int j = k + 1; j < g.NT; ++j)
+    for (int s = 0; s < g.NS; ++s) push(IT_UN, k, j, 0, s);
+  for (int i = k + 1; i < g.MT; ++i) {
     for (int b = 0; b < g.NBK; ++b) {
-      push(IT_GB, k, k, k, b, 0);
-      for (int s = (b + 1) * g.SPB; s < g.NS; ++s) push(IT_GA, k, k, k, b, s);
+      push(IT_TB, i, k, b, 0);
+      for (int s = (b + 1) * g.SPB; s < g.NS; ++s) push(IT_TA, i, k, b, s);
     }
     for (int j = k + 1; j < g.NT; ++j)
-      for (int s = 0; s < g.NS; ++s) push(IT_UN, k, k, j, 0, s);
-    for (int i = k + 1; i < g.MT; ++i) {
-      for (int b = 0; b < g.NBK; ++b) {
-        push(IT_TB, k, i, k, b, 0);
-        for (int s = (b + 1) * g.SPB; s < g.NS; ++s) push(IT_TA, k, i, k, b, s);
-      }
-      for (int j = k + 1; j < g.NT; ++j)
-        for (int s = 0; s < g.NS; ++s) push(IT_TM, k, i, j, 0, s);
-    }
+      for (int s = 0; s < g.NS; ++s) push(IT_TM, i, j, 0, s);
   }
+  return n;
+}
+
+// Natural (generation) order: the algorithm's own loop order, topological.
+static void gen_items(const DagGeom &g, std::vector<DagItem> &v) {
+  long long total = 0;
+  for (int k = 0; k < g.KT; ++k) total += step_tasks(g, k);
+  v.resize((size_t)total);
+  long long off = 0;
+  for (int k = 0; k < g.KT; ++k) off += gen_step(g, k, v.data() + off);
 }
 
 static double item_cost(const DagGeom &g, const DagItem &it) {
@@ -493,7 +508,7 @@ static std::shared_ptr<Plan> get_plan(const DagGeom &g) {
 }
 
 template <typename R, int NW>
-static int launch_dag(const DagArgs<R> &a, size_t sm, double flops, cudaStream_t st) {
+static int launch_dag(const DagArgs<R> &a, size_t sm, double flops, cudaStream_t st, bool timed = true) {
   cudaError_t e;
   if ((e = cudaFuncSetAttribute(k_tile_dag<R, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) !=
       cudaSuccess)
@@ -506,9 +521,9 @@ static int launch_dag(const DagArgs<R> &a, size_t sm, double flops, cudaStream_t
     return (int)e;
   if (per_sm < 1) return (int)cudaErrorInvalidConfiguration;
   const int grid = std::min(sms * per_sm, a.nitems);
-  void *tok = prof_begin(st);
+  void *tok = timed ? prof_begin(st) : nullptr;
   k_tile_dag<R, NW><<<grid, TQR_THREADS, sm, st>>>(a);
-  prof_end(tok, st, flops);
+  if (timed) prof_end(tok, st, flops);
   count_launch();
   e = cudaGetLastError();
   return e == cudaSuccess ? 0 : (int)e;
@@ -558,6 +573,111 @@ static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int
   return g.nw == 16 ? launch_dag<R, 16>(a, sm, flops, st) : launch_dag<R, 8>(a, sm, flops, st);
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant.  Some callers cannot hand the library device
+// memory for the schedule: code that runs while a framework's caching
+// allocator owns the whole device (no room for a second allocator), host code
+// that must not take the implicit device synchronisation of cudaMalloc /
+// cudaFree in the middle of a pipeline, and bindings that have no way to keep
+// a scratch buffer alive between calls.  For them the schedule and its
+// counters live in one file-scope device array of fixed size that every GPU
+// loading this library keeps until exit.  The task list is written on the
+// device (loop order, which is topological), so neither the host nor the
+// device allocates anything per call.
+// ---------------------------------------------------------------------------
+constexpr size_t kStaticScratchBytes = size_t(4) << 20;   // 4 MiB (see tileqr.h)
+static __device__ __align__(256) unsigned char g_tile_scratch[kStaticScratchBytes];
+
+static std::mutex g_static_mu;
+static void *g_static_ptr[64];
+
+// Device address of g_tile_scratch on the current device (set-up on the
+// first call per device; in host code the symbol itself is only a stand-in).
+static cudaError_t static_scratch(void **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> l(g_static_mu);
+  if (!g_static_ptr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_tile_scratch);
+    if (e != cudaSuccess) return e;
+    g_static_ptr[dev] = p;
+  }
+  *out = g_static_ptr[dev];
+  return cudaSuccess;
+}
+
+// Clears the header and counters and writes the task list (CTA k writes step
+// k at its offset).  Everything the DAG kernel expects to start at zero is
+// cleared here on every call, because the array keeps the previous call's
+// contents.
+__global__ void k_static_schedule(DagGeom g, unsigned char *w, size_t bytes_counters, long long key,
+                                  int nitems) {
+  int *cnt = reinterpret_cast<int *>(w + 256);
+  const int ncnt = g.ncounters();
+  for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < ncnt; x += gridDim.x * blockDim.x) cnt[x] = 0;
+  if (blockIdx.x == 0) {
+    int *hw = reinterpret_cast<int *>(w);
+    for (int x = threadIdx.x; x < (int)(sizeof(DagHeader) / sizeof(int)); x += blockDim.x) hw[x] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      DagHeader *h = reinterpret_cast<DagHeader *>(w);
+      h->key = key;
+      h->nitems = nitems;
+      h->t_first = ~0ull;
+    }
+  }
+  if (threadIdx.x == 0 && (int)blockIdx.x < g.KT) {
+    long long off = 0;
+    for (int k = 0; k < (int)blockIdx.x; ++k) off += step_tasks(g, k);
+    gen_step(g, blockIdx.x, reinterpret_cast<DagItem *>(w + 256 + bytes_counters) + off);
+  }
+}
+
+static int tile_geqrf_noalloc(int m, int n, int nb, int ib, double *A, int lda, double *T, int ldt,
+                              double *tau, int ldtau, cudaStream_t st) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (nb <= 0) return -3;
+  if (ib <= 0 || ib > nb) return -4;
+  if (m == 0 || n == 0) return 0;
+  DagGeom g;
+  if (!dag_geom(m, n, nb, ib, &g)) return -3;
+  if (lda < m) return -6;
+  if (ldt < g.MT * ib) return -8;
+  if (ldtau < n) return -10;
+  long long nitems = 0;
+  for (int k = 0; k < g.KT; ++k) nitems += step_tasks(g, k);
+  const size_t bytes_counters = align256(sizeof(int) * (size_t)g.ncounters());
+  const size_t need = 256 + bytes_counters + sizeof(DagItem) * (size_t)nitems;
+  if (need > kStaticScratchBytes || nitems > 0x7fffffff) return TQR_ERR_SCRATCH_TOO_SMALL;
+  void *wv = nullptr;
+  cudaError_t e = static_scratch(&wv);
+  if (e != cudaSuccess) return (int)e;
+  unsigned char *w = static_cast<unsigned char *>(wv);
+  const long long key = geom_key(g);
+  k_static_schedule<<<std::max(g.KT, 1), TQR_THREADS, 0, st>>>(g, w, bytes_counters, key, (int)nitems);
+  count_launch();
+  if ((e = cudaGetLastError()) != cudaSuccess) return (int)e;
+  DagArgs<double> a;
+  a.g = g;
+  a.A = A; a.lda = lda;
+  a.T = T; a.ldt = ldt;
+  a.tau = tau; a.ldtau = ldtau;
+  a.hdr = reinterpret_cast<DagHeader *>(w);
+  a.cnt = reinterpret_cast<int *>(w + 256);
+  a.items = reinterpret_cast<const DagItem *>(w + 256 + bytes_counters);
+  a.nitems = (int)nitems;
+  a.key = key;
+  a.timeout_ns = 20ull * 1000ull * 1000ull * 1000ull;
+  const size_t sm = std::max({apply_smem_elems(nb, ib, g.nw, true, true, true) * sizeof(double),
+                              panel_smem<double>(nb, ib, true, true), tsqrt_smem<double>(nb, ib, true)});
+  return g.nw == 16 ? launch_dag<double, 16>(a, sm, 0.0, st, false)
+                    : launch_dag<double, 8>(a, sm, 0.0, st, false);
+}
+
 }  // namespace tqr
 
 using namespace tqr;
@@ -594,6 +714,11 @@ int tqr_tile_dag_status(const void *work, int *status, int *task, cudaStream_t s
   if (status) *status = h.error;
   if (task) *task = h.err_item;
   return 0;
+}
+
+int tqr_dtile_geqrf_noalloc(int m, int n, int nb, int ib, double *A, int lda, double *T, int ldt,
+                            double *tau, int ldtau, cudaStream_t stream) {
+  return tile_geqrf_noalloc(m, n, nb, ib, A, lda, T, ldt, tau, ldtau, stream);
 }
 
 int tqr_tile_dag_stats(const void *work, unsigned long long *out, cudaStream_t stream) {

@@ -43,6 +43,7 @@ DIAG = {
     "tqr_tile_dag_status": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I), _P], _I),
     "tqr_tile_dag_check": ([_I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)], _I),
     "tqr_tile_dag_stats": ([_P, ctypes.POINTER(ctypes.c_ulonglong), _P], _I),
+    "tqr_dtile_geqrf_noalloc": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P], _I),
 }
 
 _lib = None
