@@ -46,6 +46,11 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--kernel", default=None, choices=["tsmqr", "tsqrt", "geqrt"],
                    help="time one tile kernel alone (for profiling) instead of the workload")
+    p.add_argument("--no-ls", action="store_true", help="skip the least-squares comparison")
+    p.add_argument("--ls-only", action="store_true", help="run only the least-squares comparison")
+    p.add_argument("--ls-m", type=int, default=32768)
+    p.add_argument("--ls-n", type=int, default=4096)
+    p.add_argument("--ls-no-orth", action="store_true")
     return p.parse_args()
 
 
@@ -257,6 +262,97 @@ def run_reference(args, world, rank):
     return 0
 
 
+def haar(m, n, g, torch):
+    Z = torch.randn(m, n, generator=g, dtype=torch.float64, device="cuda")
+    Q, R = torch.linalg.qr(Z)
+    return Q * torch.sign(torch.diagonal(R)).unsqueeze(0)
+
+
+def ls_problem(m, n, k, torch, seed=SEED):
+    """The mixed-precision least-squares configuration: Float32-stored
+    A = U diag(sigma) V^T (Haar U, V; sigma geometric from 1 to 1e-6),
+    b = A x_true + 1e-10 N(0,1), k right-hand sides (synthetic, seeded)."""
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    U = haar(m, n, g, torch)
+    V = haar(n, n, g, torch)
+    sigma = torch.logspace(0, -6, n, dtype=torch.float64, device="cuda")
+    A = ((U * sigma.unsqueeze(0)) @ V.t()).float()
+    del U, V
+    x_true = torch.randn(n, k, generator=g, dtype=torch.float64, device="cuda")
+    b = A.double() @ x_true + 1e-10 * torch.randn(m, k, generator=g, dtype=torch.float64, device="cuda")
+    return A, b
+
+
+def ls_bench(tq, torch, m=32768, n=4096, k=4, steps=2, warmup=1, orth=True):
+    """Plain FP64 GPU least squares (FP64 tile QR, Q^T b, R x = c) against the
+    mixed solve (FP32 tile QR + FP64 CGLS refinement) on the same problem."""
+    A32, b = ls_problem(m, n, k, torch)
+    A64 = A32.double()
+    Ac = tq.empty(m, n, dtype=torch.float32)
+    Ac.copy_(A32)
+    bc = tq.empty(m, k)
+    bc.copy_(b)
+    Af = tq.empty(m, n)
+    Bf = tq.empty(m, k)
+    st = torch.cuda.current_stream()
+
+    def timed(fn):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        out = fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return out, e0.elapsed_time(e1)
+
+    t64, tmx = [], []
+    for rep in range(warmup + steps):
+        Af.copy_(A64)
+        Bf.copy_(b)
+        torch.cuda.synchronize()
+        X64, ms = timed(lambda: tq.lstsq_fp64(Af, Bf, NB, IB))
+        if rep >= warmup:
+            t64.append(ms)
+        (Xm, it, rr), ms = timed(lambda: tq.lstsq_mixed(Ac, bc, NB, IB, maxit=60, tol=1e-13))
+        if rep >= warmup:
+            tmx.append(ms)
+            phases = tq.dsgels_phases()
+    X64 = X64.clone()
+    normA = 1.0   # sigma_max = 1 by construction
+
+    def berr(x):
+        r = b - A64 @ x
+        nb_ = (torch.linalg.norm(r, dim=0) / (normA * torch.linalg.norm(x, dim=0) +
+                                              torch.linalg.norm(b, dim=0))).max().item()
+        ls_ = (torch.linalg.norm(A64.t() @ r, dim=0) / (normA * torch.linalg.norm(r, dim=0))).max().item()
+        return nb_, ls_
+
+    be64, ls64 = berr(X64)
+    bem, lsm = berr(Xm)
+    res = {"workload": f"least squares, Float32-stored {m}x{n} A = U diag(sigma) V^T, sigma geometric "
+                       f"1..1e-6, b = A x_true + 1e-10 N(0,1), {k} RHS",
+           "fp64_ms": min(t64), "mixed_ms": min(tmx), "speedup": min(t64) / min(tmx),
+           "mixed_iterations": it, "mixed_relres": rr, "mixed_phases_ms": phases,
+           "normwise_backward_error_fp64": be64, "normwise_backward_error_mixed": bem,
+           "ls_backward_error_fp64": ls64, "ls_backward_error_mixed": lsm,
+           "rel_diff_mixed_vs_fp64": (torch.linalg.norm(Xm - X64) / torch.linalg.norm(X64)).item(),
+           "note": ("normwise backward error ||b - Ax||/(||A|| ||x|| + ||b||) is bounded below by the "
+                    "1e-10 noise for any least-squares solution; both forms reach the same value")}
+    if orth:
+        for tag, dt, src in (("mixed", torch.float32, A32), ("fp64", torch.float64, A64)):
+            F = tq.empty(m, n, dtype=dt)
+            F.copy_(src)
+            T, _ = tq.tile_geqrf(F, NB, IB)
+            Q = tq.empty(m, n, dtype=dt)
+            Q.copy_(torch.eye(m, n, dtype=dt, device="cuda"))
+            tq.tile_unmqr("N", F, T, Q, NB, IB)
+            Qd = Q.double()
+            res[f"orth_I_minus_QtQ_fro_{tag}"] = torch.linalg.norm(
+                Qd.t() @ Qd - torch.eye(n, dtype=torch.float64, device="cuda")).item()
+            del F, Q, Qd, T
+    return res
+
+
 def fp64_peak(tq_lib, torch):
     """SIMT DFMA ceiling of this GPU (independent FMA chains), TFLOP/s."""
     import ctypes
@@ -298,6 +394,17 @@ def main():
     args = parse()
     if args.kernel:
         return kernel_bench(args)
+    if args.ls_only:
+        import torch
+
+        import tileqr as tq
+        import tileqr_build
+        tileqr_build.build()
+        tq.set_blocking(False)
+        res = ls_bench(tq, torch, args.ls_m, args.ls_n, 4, max(1, args.steps), max(1, args.warmup),
+                       orth=not args.ls_no_orth)
+        print(json.dumps(res), flush=True)
+        return 0
     world, rank, local = dist_setup(args)
     if world > 1:
         import torch
@@ -424,6 +531,10 @@ def main():
                           f"flat-tree tile QR of a {CPU_SAMPLE_N}x{CPU_SAMPLE_N} N(0,1) matrix, "
                           f"nb={NB}, ib={IB}; best of {len(times)} runs of {min(times):.1f} s")}
 
+    ls = None
+    if rank == 0 and world == 1 and not args.no_ls:
+        ls = ls_bench(tq, torch, args.ls_m, args.ls_n, 4, 2, 1, orth=not args.ls_no_orth)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -433,6 +544,7 @@ def main():
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": launches,
             "dag_stats_last_step": dag,
+            "least_squares_mixed_vs_fp64": ls,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -130,6 +130,20 @@ int tqr_tile_dag_stats(const void *work, unsigned long long *out, cudaStream_t s
 /* Host-only self check of the schedule for a shape: replays the task list and
  * confirms every closed-form wait target and the topological sort (0 = ok). */
 int tqr_tile_dag_check(int m, int n, int nb, int ib, long long *ntasks);
+int tqr_tile_dag_check_rhs(int m, int n, int nrhs, int nb, int ib, long long *ntasks);
+
+/* Least squares in one persistent launch plus a triangular solve (m >= n,
+ * same shape rules as tqr_?tile_geqrf_dag, 0 < nrhs <= nb): B (m-by-nrhs)
+ * rides along as one more tile column of the factorisation, so it leaves as
+ * Q^T B, then R X = (Q^T B)[0:n]; X overwrites B[0:n].  A, T, tau as for
+ * tile_geqrf; `work` from tqr_tile_gels_worksize. */
+int tqr_tile_gels_worksize(int m, int n, int nrhs, int nb, int ib, size_t *bytes);
+int tqr_dtile_gels_dag(int m, int n, int nrhs, int nb, int ib, double *A, int lda, double *T, int ldt,
+                       double *tau, int ldtau, double *B, int ldb, void *work, size_t lwork,
+                       cudaStream_t stream);
+int tqr_stile_gels_dag(int m, int n, int nrhs, int nb, int ib, float *A, int lda, float *T, int ldt,
+                       float *tau, int ldtau, float *B, int ldb, void *work, size_t lwork,
+                       cudaStream_t stream);
 
 /* Allocation-free tile QR (no counterpart in NextLA).  Same factorisation and
  * the same bits as tqr_dtile_geqrf_dag, but it needs no `work` argument: for
@@ -170,6 +184,26 @@ int tqr_dtile_gels(int m, int n, int nrhs, int nb, int ib, double *A, int lda, d
                    double *tau, int ldtau, double *B, int ldb, cudaStream_t stream);
 int tqr_stile_gels(int m, int n, int nrhs, int nb, int ib, float *A, int lda, float *T, int ldt,
                    float *tau, int ldtau, float *B, int ldb, cudaStream_t stream);
+
+/* ---- Mixed-precision least squares (no counterpart in NextLA; its poster lists
+ * mixed precision as future work) ----
+ * min ||A X - B|| for a Float32 A (m-by-n, m >= n, lda) and Float64 B
+ * (m-by-nrhs, nrhs <= 16): tile QR of a copy of A in FP32 (persistent kernel
+ * when m, n are multiples of nb), X0 = R^-1 (Q^T B)[0:n] in FP32, then CGLS in
+ * FP64 on the right-preconditioned problem min ||A R^-1 Y - B|| (X = R^-1 Y),
+ * every product with A in FP64 on A's FP32 entries.  Stops when the
+ * preconditioned normal-equation residual of every column has dropped by
+ * `tol` or after `maxit` iterations; `iters` and `relres` (that ratio) report
+ * where it stopped.  A and B are not modified.  `work` (256-byte aligned) holds
+ * the FP32 factor and the iteration vectors; its size comes from
+ * tqr_dsgels_worksize.  Synchronises `stream` once per iteration. */
+int tqr_dsgels_worksize(int m, int n, int nrhs, int nb, int ib, size_t *bytes);
+int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, const double *B,
+               int ldb, double *X, int ldx, int maxit, double tol, void *work, size_t lwork,
+               int *iters, double *relres, cudaStream_t stream);
+/* Device time (ms) of the last tqr_dsgels call's phases: ms[0] FP32 tile QR,
+ * ms[1] X0 = R^-1 Q^T B, ms[2] FP64 CGLS refinement; iters its iterations. */
+int tqr_dsgels_phases(double *ms, int *iters);
 
 /* ---- Measurement hooks (no counterpart in NextLA; used by the benchmark) ----
  * tqr_launch_count: kernels this library has launched since it was loaded.

@@ -58,6 +58,12 @@ static_assert(sizeof(DagItem) == 12, "DagItem layout");
 struct DagGeom {
   int m, n, nb, ib, nw;
   int MT, NT, KT, NS, SPB, NBK;
+  // Optional right-hand sides: nrhs > 0 adds one tile column (index NTA) of
+  // width nrhs that only receives trailing updates, so the factorisation also
+  // forms Q^T B.  NTA is the number of tile columns of A.
+  int nrhs, NTA;
+  __host__ __device__ int strips(int j) const { return j < NTA ? NS : (nrhs + nw - 1) / nw; }
+  __host__ __device__ int width(int j) const { return j < NTA ? nb : nrhs; }
   __host__ __device__ int ver(int i, int j, int s) const { return (i * NT + j) * NS + s; }
   __host__ __device__ int done_g(int k) const { return MT * NT * NS + k; }
   __host__ __device__ int done_t(int k, int i) const { return MT * NT * NS + KT + k * MT + i; }
@@ -169,6 +175,7 @@ template <typename R>
 struct DagArgs {
   DagGeom g;
   R *A; int lda;
+  R *B; int ldb;    // right-hand sides (tile column NTA) when g.nrhs > 0
   R *T; int ldt;
   R *tau; int ldtau;
   DagHeader *hdr;
@@ -196,7 +203,10 @@ __device__ void run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *
   const DagGeom &g = a.g;
   const int nb = g.nb, ib = g.ib;
   const int k = it.k, i = it.i, j = it.j, b = it.b, s = it.s;
-  auto tile = [&](int r, int c) { return a.A + ix(r * nb, c * nb, a.lda); };
+  auto tile = [&](int r, int c) {
+    return c < g.NTA ? a.A + ix(r * nb, c * nb, a.lda) : a.B + ix(r * nb, 0, a.ldb);
+  };
+  auto tld = [&](int c) { return c < g.NTA ? a.lda : a.ldb; };
   auto ttile = [&](int r, int c) { return a.T + ix(r * ib, c * nb, a.ldt); };
   auto tautile = [&](int r, int c) { return a.tau + ix(c * nb, r, a.ldtau); };
   if (it.type == IT_GB) {
@@ -232,6 +242,8 @@ __device__ void run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *
     case IT_UN:
       p.mode = 0; p.L = nb; p.k = nb;
       p.C = tile(k, j);
+      p.c_cs = tld(j);
+      p.ncols = g.width(j);
       p.V = tile(k, k);
       p.T = ttile(k, k);
       break;
@@ -246,6 +258,8 @@ __device__ void run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *
       p.mode = 1; p.L = nb; p.k = nb;
       p.C = tile(i, j);
       p.A1 = tile(k, j);
+      p.c_cs = p.a_cs = tld(j);
+      p.ncols = g.width(j);
       p.V = tile(i, k);
       p.T = ttile(i, k);
       break;
@@ -333,9 +347,10 @@ struct Plan {
   }
 };
 
-static bool dag_geom(int m, int n, int nb, int ib, DagGeom *g) {
-  if (m <= 0 || n <= 0 || nb <= 0 || ib <= 0) return false;
+static bool dag_geom(int m, int n, int nb, int ib, DagGeom *g, int nrhs = 0) {
+  if (m <= 0 || n <= 0 || nb <= 0 || ib <= 0 || nrhs < 0 || nrhs > nb) return false;
   if (m % nb || n % nb || nb % ib) return false;
+  if (nrhs > 0 && m < n) return false;         // the RHS tile column is never a panel
   if (nb > 256) return false;                  // one tile column of V per CTA in shared memory
   // 16-wide strips when two CTAs still fit per SM, else 8 (ib must be a multiple)
   int nw = 16;
@@ -344,7 +359,9 @@ static bool dag_geom(int m, int n, int nb, int ib, DagGeom *g) {
     nw = 8;
   if (ib % nw) return false;
   g->m = m; g->n = n; g->nb = nb; g->ib = ib; g->nw = nw;
-  g->MT = m / nb; g->NT = n / nb; g->KT = std::min(g->MT, g->NT);
+  g->nrhs = nrhs;
+  g->NTA = n / nb;
+  g->MT = m / nb; g->NT = g->NTA + (nrhs > 0 ? 1 : 0); g->KT = std::min(g->MT, g->NTA);
   g->NS = nb / nw; g->SPB = ib / nw; g->NBK = nb / ib;
   if (2 * g->SPB + 1 > kMaxDeps) return false;
   if (g->MT > 65535 || g->NT > 65535 || g->NBK > 255) return false;
@@ -357,14 +374,15 @@ static bool dag_geom(int m, int n, int nb, int ib, DagGeom *g) {
 
 static long long geom_key(const DagGeom &g) {
   long long h = 1469598103934665603LL;
-  for (int v : {g.m, g.n, g.nb, g.ib, g.nw}) h = (h ^ (long long)v) * 1099511628211LL;
+  for (int v : {g.m, g.n, g.nb, g.ib, g.nw, g.nrhs}) h = (h ^ (long long)v) * 1099511628211LL;
   return h & 0x7fffffffffffffffLL;
 }
 
 // Natural (generation) order: the algorithm's own loop order, topological.
 // Tasks of step k in the algorithm's loop order.
 __host__ __device__ inline long long step_tasks(const DagGeom &g, int k) {
-  const long long pt = g.panel_tasks(), right = (long long)(g.NT - k - 1) * g.NS;
+  const long long pt = g.panel_tasks();
+  const long long right = (long long)(g.NTA - k - 1) * g.NS + (g.NT > g.NTA ? g.strips(g.NTA) : 0);
   return pt + right + (long long)(g.MT - k - 1) * (pt + right);
 }
 
@@ -382,14 +400,14 @@ __host__ __device__ inline long long gen_step(const DagGeom &g, int k, DagItem *
     for (int s = (b + 1) * g.SPB; s < g.NS; ++s) push(IT_GA, k, k, b, s);
   }
   for (int j = k + 1; j < g.NT; ++j)
-    for (int s = 0; s < g.NS; ++s) push(IT_UN, k, j, 0, s);
+    for (int s = 0; s < g.strips(j); ++s) push(IT_UN, k, j, 0, s);
   for (int i = k + 1; i < g.MT; ++i) {
     for (int b = 0; b < g.NBK; ++b) {
       push(IT_TB, i, k, b, 0);
       for (int s = (b + 1) * g.SPB; s < g.NS; ++s) push(IT_TA, i, k, b, s);
     }
     for (int j = k + 1; j < g.NT; ++j)
-      for (int s = 0; s < g.NS; ++s) push(IT_TM, i, j, 0, s);
+      for (int s = 0; s < g.strips(j); ++s) push(IT_TM, i, j, 0, s);
   }
   return n;
 }
@@ -412,8 +430,8 @@ static double item_cost(const DagGeom &g, const DagItem &it) {
     case IT_TB: return 3.0 * nb * ib * ib + 64.0 * ib * 600;
     case IT_GA: return 4.0 * (nb - it.b * ib) * ib * nw;
     case IT_TA: return 4.0 * nb * ib * nw;
-    case IT_UN: return 2.0 * nb * nb * nw;
-    default: return 4.0 * nb * nb * nw;
+    case IT_UN: return 2.0 * nb * nb * std::min<double>(nw, g.width(it.j));
+    default: return 4.0 * nb * nb * std::min<double>(nw, g.width(it.j));
   }
 }
 
@@ -531,18 +549,20 @@ static int launch_dag(const DagArgs<R> &a, size_t sm, double flops, cudaStream_t
 
 template <typename R>
 static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int ldt, R *tau,
-                          int ldtau, void *work, size_t lwork, cudaStream_t st) {
+                          int ldtau, void *work, size_t lwork, cudaStream_t st, int nrhs = 0,
+                          R *B = nullptr, int ldb = 1) {
   if (m < 0) return -1;
   if (n < 0) return -2;
   if (nb <= 0) return -3;
   if (ib <= 0 || ib > nb) return -4;
   if (m == 0 || n == 0) return 0;
   DagGeom g;
-  if (!dag_geom(m, n, nb, ib, &g)) return -3;   // shape outside the DAG path
+  if (!dag_geom(m, n, nb, ib, &g, nrhs)) return -3;   // shape outside the DAG path
   if (lda < m) return -6;
   if (ldt < g.MT * ib) return -8;
   if (ldtau < n) return -10;
   if (!work || ((uintptr_t)work & 255)) return -11;
+  if (nrhs > 0 && (!B || ldb < m)) return -13;
   auto plan = get_plan(g);
   if (lwork < plan->bytes_total) return -12;
   unsigned char *w = (unsigned char *)work;
@@ -558,6 +578,7 @@ static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int
   DagArgs<R> a;
   a.g = g;
   a.A = A; a.lda = lda;
+  a.B = B; a.ldb = ldb;
   a.T = T; a.ldt = ldt;
   a.tau = tau; a.ldtau = ldtau;
   a.hdr = (DagHeader *)w;
@@ -664,6 +685,7 @@ static int tile_geqrf_noalloc(int m, int n, int nb, int ib, double *A, int lda, 
   DagArgs<double> a;
   a.g = g;
   a.A = A; a.lda = lda;
+  a.B = nullptr; a.ldb = 1;
   a.T = T; a.ldt = ldt;
   a.tau = tau; a.ldtau = ldtau;
   a.hdr = reinterpret_cast<DagHeader *>(w);
@@ -693,6 +715,38 @@ int tqr_tile_dag_worksize(int m, int n, int nb, int ib, size_t *bytes) {
   }
   *bytes = get_plan(g)->bytes_total;
   return 0;
+}
+
+int tqr_tile_gels_worksize(int m, int n, int nrhs, int nb, int ib, size_t *bytes) {
+  if (!bytes) return -6;
+  DagGeom g;
+  if (!dag_geom(m, n, nb, ib, &g, nrhs)) {
+    *bytes = 0;
+    return 1;
+  }
+  *bytes = get_plan(g)->bytes_total;
+  return 0;
+}
+
+// Least squares in one persistent launch plus a triangular solve: B rides
+// along as an extra tile column of the factorisation (so it leaves as Q^T B),
+// then R X = (Q^T B)[0:n].  X overwrites B[0:n, 0:nrhs].
+int tqr_dtile_gels_dag(int m, int n, int nrhs, int nb, int ib, double *A, int lda, double *T, int ldt,
+                       double *tau, int ldtau, double *B, int ldb, void *work, size_t lwork,
+                       cudaStream_t stream) {
+  if (nrhs < 0 || nrhs > nb) return -3;
+  int rc = tile_geqrf_dag<double>(m, n, nb, ib, A, lda, T, ldt, tau, ldtau, work, lwork, stream, nrhs, B, ldb);
+  if (rc != 0) return rc;
+  return nrhs > 0 ? tqr_dtrsm_lun(n, nrhs, A, lda, B, ldb, stream) : 0;
+}
+
+int tqr_stile_gels_dag(int m, int n, int nrhs, int nb, int ib, float *A, int lda, float *T, int ldt,
+                       float *tau, int ldtau, float *B, int ldb, void *work, size_t lwork,
+                       cudaStream_t stream) {
+  if (nrhs < 0 || nrhs > nb) return -3;
+  int rc = tile_geqrf_dag<float>(m, n, nb, ib, A, lda, T, ldt, tau, ldtau, work, lwork, stream, nrhs, B, ldb);
+  if (rc != 0) return rc;
+  return nrhs > 0 ? tqr_strsm_lun(n, nrhs, A, lda, B, ldb, stream) : 0;
 }
 
 int tqr_dtile_geqrf_dag(int m, int n, int nb, int ib, double *A, int lda, double *T, int ldt,
@@ -732,6 +786,15 @@ int tqr_tile_dag_stats(const void *work, unsigned long long *out, cudaStream_t s
   out[7] = h.t_first;
   out[8] = h.t_last;
   return 0;
+}
+
+int tqr_tile_dag_check_rhs(int m, int n, int nrhs, int nb, int ib, long long *ntasks) {
+  DagGeom g;
+  if (!dag_geom(m, n, nb, ib, &g, nrhs)) return 1;
+  std::vector<DagItem> items;
+  const bool ok = build_schedule(g, items, true);
+  if (ntasks) *ntasks = (long long)items.size();
+  return ok ? 0 : 2;
 }
 
 int tqr_tile_dag_check(int m, int n, int nb, int ib, long long *ntasks) {

@@ -1,0 +1,527 @@
+// ls.cu -- least squares on top of the tile QR: the mixed-precision solve.
+//
+// Not a NextLA routine: NextLA ships the tile kernels, and its poster lists a
+// mixed-precision solver as future work.  min ||A X - B||_2 for a Float32-stored
+// A (m >= n) and Float64 right-hand sides:
+//
+//   1. copy A into the factor workspace F and tile-QR it in FP32 (the same
+//      persistent kernel as the FP64 form, float instantiation);
+//   2. X0 = R^-1 (Q^T B)[0:n] in FP32 (tile Q application + triangular solve);
+//   3. refine in FP64 with CGLS on the right-preconditioned problem
+//      min || (A R^-1) Y - B ||, X = R^-1 Y: every product with A uses the FP32
+//      entries of A exactly (converted to FP64 in registers), every solve with R
+//      runs in FP64 on R's FP32 entries.  A R^-1 is within O(kappa(A) u_32) of
+//      orthonormal, so CGLS converges in a few iterations to the FP64 least-
+//      squares solution; no product with Q is needed.
+//
+// On GB300 the FP32 pipe is ~55x the FP64 pipe, so steps 1-2 cost a small part
+// of the FP64 factorisation and the FP64 work left is a handful of A*x and
+// A^T*r products (4 m n k flops per iteration) and triangular solves.
+//
+// Kernels here (all FP64 arithmetic on FP32 matrix entries):
+//   k_gemm_sd_n   Y = alpha A X + beta Y          (A m-by-n FP32, X n-by-k)
+//   k_gemm_sd_t   Z += alpha A^T R               (split over row blocks, FP64 atomics)
+//   k_trsv_sd     triangular solve of one diagonal block, all k columns
+//   small column kernels for the CGLS recurrences (dots, axpys)
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "common.cuh"
+#include "tileqr.h"
+#include "tileqr_internal.h"
+
+namespace tqr {
+
+constexpr int kLsMaxRhs = 16;
+
+// Y[r, c] += alpha * sum_j A[r, j] X[j, c] for K right-hand sides (a
+// compile-time count: FP64 instructions cost full pipe time even when
+// predicated off); the n columns are split over gridDim.y CTAs that add their
+// partial sums with FP64 atomics.
+template <int K>
+__global__ void __launch_bounds__(TQR_THREADS)
+k_gemm_sd_n(int m, int n, const float *__restrict__ A, int lda, const double *__restrict__ X,
+            int ldx, double *__restrict__ Y, int ldy, double alpha, int jchunk)
+{
+  __shared__ double Xs[256][K];
+  const int r = blockIdx.x * TQR_THREADS + threadIdx.x;
+  const int j0 = blockIdx.y * jchunk, j1 = min(n, j0 + jchunk);
+  double acc[K];
+#pragma unroll
+  for (int c = 0; c < K; ++c) acc[c] = 0.0;
+  for (int jb = j0; jb < j1; jb += 256) {
+    const int jn = min(256, j1 - jb);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < jn * K; idx += TQR_THREADS) {
+      int jj = idx % jn, c = idx / jn;
+      Xs[jj][c] = X[ix(jb + jj, c, ldx)];
+    }
+    __syncthreads();
+    if (r < m) {
+      const float *ap = A + ix(r, jb, lda);
+      for (int jj = 0; jj < jn; ++jj) {
+        const double a = (double)__ldg(ap + (size_t)jj * lda);
+#pragma unroll
+        for (int c = 0; c < K; ++c) acc[c] = fma(a, Xs[jj][c], acc[c]);
+      }
+    }
+  }
+  if (r < m)
+#pragma unroll
+    for (int c = 0; c < K; ++c) atomicAdd(Y + ix(r, c, ldy), alpha * acc[c]);
+}
+
+// Z[j, c] += alpha * sum_r A[r, j] R[r, c] over the row block of this CTA;
+// one warp per column, lanes over rows, one atomic add per (column, rhs).
+template <int K>
+__global__ void __launch_bounds__(TQR_THREADS)
+k_gemm_sd_t(int m, int n, const float *__restrict__ A, int lda, const double *__restrict__ R,
+            int ldr, double *__restrict__ Z, int ldz, double alpha, int rchunk, int cols_per_cta)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double *Rs = reinterpret_cast<double *>(smem_raw);   // rchunk x K
+  const int r0 = blockIdx.x * rchunk, r1 = min(m, r0 + rchunk), rn = r1 - r0;
+  const int j0 = blockIdx.y * cols_per_cta, j1 = min(n, j0 + cols_per_cta);
+  for (int idx = threadIdx.x; idx < rn * K; idx += TQR_THREADS) {
+    int rr = idx % rn, c = idx / rn;
+    Rs[rr + c * rchunk] = R[ix(r0 + rr, c, ldr)];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int j = j0 + warp; j < j1; j += TQR_WARPS) {
+    double acc[K];
+#pragma unroll
+    for (int c = 0; c < K; ++c) acc[c] = 0.0;
+    const float *ap = A + ix(r0, j, lda);
+    for (int rr = lane; rr < rn; rr += 32) {
+      const double a = (double)__ldg(ap + rr);
+#pragma unroll
+      for (int c = 0; c < K; ++c) acc[c] = fma(a, Rs[rr + c * rchunk], acc[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < K; ++c) {
+      double v = warp_sum(acc[c]);
+      if (lane == 0) atomicAdd(Z + ix(j, c, ldz), alpha * v);
+    }
+  }
+}
+
+// One diagonal block of R (FP32, upper) solved in FP64 for all k columns of B:
+// trans = 0: R_bb x = b (back substitution); trans = 1: R_bb^T x = b (forward).
+// 1 / R_ii is formed once per row in parallel before the sequential sweep.
+__global__ void __launch_bounds__(TQR_THREADS)
+k_trsv_sd(int nb, int k, int trans, const float *__restrict__ Rm, int ldr, double *__restrict__ B, int ldb)
+{
+  __shared__ double x[256][kLsMaxRhs];
+  __shared__ double rinv[256];
+  for (int idx = threadIdx.x; idx < nb; idx += TQR_THREADS) rinv[idx] = 1.0 / (double)Rm[ix(idx, idx, ldr)];
+  for (int idx = threadIdx.x; idx < nb * k; idx += TQR_THREADS) {
+    int r = idx % nb, c = idx / nb;
+    x[r][c] = B[ix(r, c, ldb)];
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  for (int step = 0; step < nb; ++step) {
+    const int i = trans ? step : nb - 1 - step;
+    if (t < k) x[i][t] *= rinv[i];
+    __syncthreads();
+    // rows still to solve: r < i (back) or r > i (forward)
+    const bool live = trans ? (t > i && t < nb) : (t < i);
+    if (live) {
+      const double a = trans ? (double)Rm[ix(i, t, ldr)] : (double)Rm[ix(t, i, ldr)];
+      for (int c = 0; c < k; ++c) x[t][c] = fma(-a, x[i][c], x[t][c]);
+    }
+    __syncthreads();
+  }
+  for (int idx = threadIdx.x; idx < nb * k; idx += TQR_THREADS) {
+    int r = idx % nb, c = idx / nb;
+    B[ix(r, c, ldb)] = x[r][c];
+  }
+}
+
+// column-wise sums of squares of an m-by-k matrix into out[c] (FP64 atomics)
+__global__ void k_colnorm2(int m, int k, const double *__restrict__ X, int ldx, double *out) {
+  const int c = blockIdx.y;
+  double s = 0.0;
+  for (int r = blockIdx.x * TQR_THREADS + threadIdx.x; r < m; r += gridDim.x * TQR_THREADS) {
+    double v = X[ix(r, c, ldx)];
+    s = fma(v, v, s);
+  }
+  __shared__ double red[TQR_WARPS];
+  s = block_sum(s, red);
+  if (threadIdx.x == 0) atomicAdd(out + c, s);
+}
+
+// Y[:, c] += f(c) * X[:, c] with f = scale[c] (or -scale[c] when neg)
+__global__ void k_axpy_cols(int m, int k, const double *__restrict__ scale, int neg, const double *__restrict__ X,
+                            int ldx, double *__restrict__ Y, int ldy) {
+  const int c = blockIdx.y;
+  const double a = neg ? -scale[c] : scale[c];
+  for (int r = blockIdx.x * TQR_THREADS + threadIdx.x; r < m; r += gridDim.x * TQR_THREADS)
+    Y[ix(r, c, ldy)] = fma(a, X[ix(r, c, ldx)], Y[ix(r, c, ldy)]);
+}
+
+// P[:, c] = S[:, c] + beta[c] P[:, c]
+__global__ void k_xpby_cols(int m, int k, const double *__restrict__ S, int lds, const double *__restrict__ beta,
+                            double *__restrict__ P, int ldp) {
+  const int c = blockIdx.y;
+  const double b = beta[c];
+  for (int r = blockIdx.x * TQR_THREADS + threadIdx.x; r < m; r += gridDim.x * TQR_THREADS)
+    P[ix(r, c, ldp)] = fma(b, P[ix(r, c, ldp)], S[ix(r, c, lds)]);
+}
+
+// CGLS scalars: alpha = gamma / qq, then (after the new gamma) beta = gnew / gamma.
+// A column whose preconditioned normal-equation residual has dropped below
+// tol2 * g0 is frozen (alpha = 0): iterating past the attainable accuracy
+// only feeds rounding noise back into the iterate.
+__global__ void k_cgls_alpha(int k, const double *gamma, const double *qq, const double *g0, double tol2,
+                             double *alpha) {
+  const int c = threadIdx.x;
+  if (c < k) alpha[c] = (qq[c] > 0.0 && gamma[c] > tol2 * g0[c]) ? gamma[c] / qq[c] : 0.0;
+}
+__global__ void k_cgls_beta(int k, double *gamma, const double *gnew, double *beta) {
+  const int c = threadIdx.x;
+  if (c < k) {
+    beta[c] = (gamma[c] > 0.0) ? gnew[c] / gamma[c] : 0.0;
+    gamma[c] = gnew[c];
+  }
+}
+
+__global__ void k_f64_to_f32(long long n, const double *__restrict__ x, float *__restrict__ y) {
+  for (long long i = blockIdx.x * (long long)TQR_THREADS + threadIdx.x; i < n; i += (long long)gridDim.x * TQR_THREADS)
+    y[i] = (float)x[i];
+}
+__global__ void k_f32_to_f64_mat(int m, int k, const float *__restrict__ x, int ldx, double *__restrict__ y, int ldy) {
+  const int c = blockIdx.y;
+  for (int r = blockIdx.x * TQR_THREADS + threadIdx.x; r < m; r += gridDim.x * TQR_THREADS)
+    y[ix(r, c, ldy)] = (double)x[ix(r, c, ldx)];
+}
+__global__ void k_f64_to_f32_mat(int m, int k, const double *__restrict__ x, int ldx, float *__restrict__ y, int ldy) {
+  const int c = blockIdx.y;
+  for (int r = blockIdx.x * TQR_THREADS + threadIdx.x; r < m; r += gridDim.x * TQR_THREADS)
+    y[ix(r, c, ldy)] = (float)x[ix(r, c, ldx)];
+}
+__global__ void k_copy_f32_mat(int m, int n, const float *__restrict__ x, int ldx, float *__restrict__ y, int ldy) {
+  for (long long idx = blockIdx.x * (long long)TQR_THREADS + threadIdx.x; idx < (long long)m * n;
+       idx += (long long)gridDim.x * TQR_THREADS) {
+    const int r = (int)(idx % m), c = (int)(idx / m);
+    y[ix(r, c, ldy)] = x[ix(r, c, ldx)];
+  }
+}
+
+static inline int blocks_for(long long n) { return (int)std::min<long long>(4096, (n + TQR_THREADS - 1) / TQR_THREADS); }
+
+#define LS_CU(x)                            \
+  do {                                      \
+    cudaError_t _e = (x);                   \
+    if (_e != cudaSuccess) return (int)_e;  \
+  } while (0)
+#define LS_TRY(x)                           \
+  do {                                      \
+    int _r = (x);                           \
+    if (_r != 0) return _r;                 \
+  } while (0)
+
+template <int K>
+static int gemm_sd_n_k(int m, int n, const float *A, int lda, const double *X, int ldx, double *Y, int ldy,
+                       double alpha, cudaStream_t st) {
+  const int gx = (m + TQR_THREADS - 1) / TQR_THREADS;
+  int gy = std::max(1, std::min((n + 255) / 256, (4 * 152 + gx - 1) / gx));
+  const int jchunk = ((n + gy - 1) / gy + 255) / 256 * 256;
+  gy = (n + jchunk - 1) / jchunk;
+  k_gemm_sd_n<K><<<dim3(gx, gy), TQR_THREADS, 0, st>>>(m, n, A, lda, X, ldx, Y, ldy, alpha, jchunk);
+  count_launch();
+  return (int)cudaGetLastError();
+}
+
+// Y = alpha A X + beta Y, beta 0 or 1 (right-hand sides in groups of 4, 2, 1)
+static int gemm_sd_n(int m, int n, int k, const float *A, int lda, const double *X, int ldx, double *Y, int ldy,
+                     double alpha, double beta, cudaStream_t st) {
+  if (m <= 0 || k <= 0) return 0;
+  if (beta == 0.0) {
+    for (int c = 0; c < k; ++c) LS_CU(cudaMemsetAsync(Y + ix(0, c, ldy), 0, sizeof(double) * m, st));
+  } else if (beta != 1.0) {
+    return -1;   // not needed by the solver
+  }
+  if (n <= 0) return 0;
+  for (int c = 0; c < k;) {
+    const int rem = k - c;
+    const double *Xc = X + ix(0, c, ldx);
+    double *Yc = Y + ix(0, c, ldy);
+    if (rem >= 4) { LS_TRY(gemm_sd_n_k<4>(m, n, A, lda, Xc, ldx, Yc, ldy, alpha, st)); c += 4; }
+    else if (rem >= 2) { LS_TRY(gemm_sd_n_k<2>(m, n, A, lda, Xc, ldx, Yc, ldy, alpha, st)); c += 2; }
+    else { LS_TRY(gemm_sd_n_k<1>(m, n, A, lda, Xc, ldx, Yc, ldy, alpha, st)); c += 1; }
+  }
+  return 0;
+}
+
+template <int K>
+static int gemm_sd_t_k(int m, int n, const float *A, int lda, const double *R, int ldr, double *Z, int ldz,
+                       double alpha, cudaStream_t st) {
+  const int rchunk = 1024, cols = 64;
+  dim3 grid((m + rchunk - 1) / rchunk, (n + cols - 1) / cols);
+  const size_t sm = sizeof(double) * rchunk * K;
+  k_gemm_sd_t<K><<<grid, TQR_THREADS, sm, st>>>(m, n, A, lda, R, ldr, Z, ldz, alpha, rchunk, cols);
+  count_launch();
+  return (int)cudaGetLastError();
+}
+
+// Z = alpha A^T R + beta Z (beta 0 or 1)
+static int gemm_sd_t(int m, int n, int k, const float *A, int lda, const double *R, int ldr, double *Z, int ldz,
+                     double alpha, double beta, cudaStream_t st) {
+  if (n <= 0 || k <= 0) return 0;
+  if (beta == 0.0) {
+    for (int c = 0; c < k; ++c) LS_CU(cudaMemsetAsync(Z + ix(0, c, ldz), 0, sizeof(double) * n, st));
+  } else if (beta != 1.0) {
+    return -1;
+  }
+  if (m <= 0) return 0;
+  for (int c = 0; c < k;) {
+    const int rem = k - c;
+    const double *Rc = R + ix(0, c, ldr);
+    double *Zc = Z + ix(0, c, ldz);
+    if (rem >= 4) { LS_TRY(gemm_sd_t_k<4>(m, n, A, lda, Rc, ldr, Zc, ldz, alpha, st)); c += 4; }
+    else if (rem >= 2) { LS_TRY(gemm_sd_t_k<2>(m, n, A, lda, Rc, ldr, Zc, ldz, alpha, st)); c += 2; }
+    else { LS_TRY(gemm_sd_t_k<1>(m, n, A, lda, Rc, ldr, Zc, ldz, alpha, st)); c += 1; }
+  }
+  return 0;
+}
+
+// Solve R X = B (trans 0) or R^T X = B (trans 1) for the upper triangle of the
+// n-by-n FP32 R, in FP64, B n-by-k overwritten.  Blocked by 256.
+static int trsm_sd(int trans, int n, int k, const float *Rm, int ldr, double *B, int ldb, cudaStream_t st) {
+  const int bs = 256;
+  const int nblk = (n + bs - 1) / bs;
+  for (int q = 0; q < nblk; ++q) {
+    const int b = trans ? q : nblk - 1 - q;
+    const int b0 = b * bs, nbk = std::min(bs, n - b0);
+    k_trsv_sd<<<1, TQR_THREADS, 0, st>>>(nbk, k, trans, Rm + ix(b0, b0, ldr), ldr, B + b0, ldb);
+    count_launch();
+    LS_CU(cudaGetLastError());
+    if (!trans && b0 > 0) {
+      // B[0:b0] -= R[0:b0, b0:b0+nbk] X_b
+      LS_TRY(gemm_sd_n(b0, nbk, k, Rm + ix(0, b0, ldr), ldr, B + b0, ldb, B, ldb, -1.0, 1.0, st));
+    } else if (trans && b0 + nbk < n) {
+      // B[b1:n] -= R[b0:b1, b1:n]^T X_b
+      const int b1 = b0 + nbk;
+      LS_TRY(gemm_sd_t(nbk, n - b1, k, Rm + ix(b0, b1, ldr), ldr, B + b0, ldb, B + b1, ldb, -1.0, 1.0, st));
+    }
+  }
+  return 0;
+}
+
+static int colnorm2(int m, int k, const double *X, int ldx, double *out, cudaStream_t st) {
+  LS_CU(cudaMemsetAsync(out, 0, sizeof(double) * k, st));
+  k_colnorm2<<<dim3(std::min(256, blocks_for(m)), k), TQR_THREADS, 0, st>>>(m, k, X, ldx, out);
+  count_launch();
+  return (int)cudaGetLastError();
+}
+
+static int axpy_cols(int m, int k, const double *scale, int neg, const double *X, int ldx, double *Y, int ldy,
+                     cudaStream_t st) {
+  k_axpy_cols<<<dim3(blocks_for(m), k), TQR_THREADS, 0, st>>>(m, k, scale, neg, X, ldx, Y, ldy);
+  count_launch();
+  return (int)cudaGetLastError();
+}
+
+// Phase times of the last tqr_dsgels call (FP32 factorisation, X0, CGLS), from
+// CUDA events on the solve's stream; read by tqr_dsgels_phases.
+static double g_phase_ms[3] = {0, 0, 0};
+static int g_phase_iters = 0;
+
+struct PhaseTimer {
+  cudaStream_t st;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool ok = true;
+  explicit PhaseTimer(cudaStream_t s) : st(s) {
+    for (auto &e : ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    if (ok) cudaEventRecord(ev[0], st);
+  }
+  void mark(int i) {
+    if (ok) cudaEventRecord(ev[i], st);
+  }
+  void finish(int iters) {
+    if (!ok) return;
+    cudaEventSynchronize(ev[3]);
+    for (int i = 0; i < 3; ++i) {
+      float t = 0;
+      cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
+      g_phase_ms[i] = t;
+    }
+    g_phase_iters = iters;
+  }
+  ~PhaseTimer() {
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+};
+
+// Workspace layout (bytes, each piece 256-aligned)
+struct MixedWs {
+  size_t F, T, tau, dag, x32, r, s, p, t, q, sc, total;
+};
+
+static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+
+static int mixed_ws(int m, int n, int k, int nb, int ib, MixedWs *w) {
+  const int MT = (m + nb - 1) / nb;
+  size_t off = 0;
+  auto take = [&](size_t bytes) { size_t o = off; off += a256(bytes); return o; };
+  w->F = take(sizeof(float) * (size_t)m * n);
+  w->T = take(sizeof(float) * (size_t)MT * ib * n);
+  w->tau = take(sizeof(float) * (size_t)n * MT);
+  size_t dag = 0;
+  if (tqr_tile_gels_worksize(m, n, k, nb, ib, &dag) != 0) dag = 0;
+  w->dag = take(dag ? dag : 256);
+  w->x32 = take(sizeof(float) * (size_t)m * k);
+  w->r = take(sizeof(double) * (size_t)m * k);
+  w->s = take(sizeof(double) * (size_t)n * k);
+  w->p = take(sizeof(double) * (size_t)n * k);
+  w->t = take(sizeof(double) * (size_t)n * k);
+  w->q = take(sizeof(double) * (size_t)m * k);
+  w->sc = take(sizeof(double) * 8 * kLsMaxRhs);
+  w->total = off;
+  return dag ? 0 : 1;
+}
+
+}  // namespace tqr
+
+using namespace tqr;
+
+extern "C" {
+
+int tqr_dsgels_phases(double *ms, int *iters) {
+  if (ms)
+    for (int i = 0; i < 3; ++i) ms[i] = g_phase_ms[i];
+  if (iters) *iters = g_phase_iters;
+  return 0;
+}
+
+int tqr_dsgels_worksize(int m, int n, int nrhs, int nb, int ib, size_t *bytes) {
+  if (!bytes) return -6;
+  MixedWs w;
+  mixed_ws(m, n, nrhs, nb, ib, &w);
+  *bytes = w.total;
+  return 0;
+}
+
+int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, const double *B, int ldb,
+               double *X, int ldx, int maxit, double tol, void *work, size_t lwork, int *iters,
+               double *relres, cudaStream_t stream) {
+  if (m < 0) return -1;
+  if (n < 0 || n > m) return -2;
+  if (nrhs < 0 || nrhs > kLsMaxRhs) return -3;
+  if (nb <= 0 || nb > 256) return -4;
+  if (ib <= 0 || ib > nb || nb % ib) return -5;
+  if (lda < m) return -7;
+  if (ldb < m) return -9;
+  if (ldx < n) return -11;
+  if (maxit < 0) return -12;
+  if (m == 0 || n == 0 || nrhs == 0) {
+    if (iters) *iters = 0;
+    return 0;
+  }
+  MixedWs w;
+  mixed_ws(m, n, nrhs, nb, ib, &w);
+  if (!work || ((uintptr_t)work & 255)) return -14;
+  if (lwork < w.total) return -15;
+  unsigned char *base = (unsigned char *)work;
+  float *F = (float *)(base + w.F);
+  float *T = (float *)(base + w.T);
+  float *tau = (float *)(base + w.tau);
+  float *x32 = (float *)(base + w.x32);
+  double *r = (double *)(base + w.r), *s = (double *)(base + w.s), *p = (double *)(base + w.p);
+  double *t = (double *)(base + w.t), *q = (double *)(base + w.q), *sc = (double *)(base + w.sc);
+  double *gamma = sc, *gnew = sc + kLsMaxRhs, *qq = sc + 2 * kLsMaxRhs, *alpha = sc + 3 * kLsMaxRhs,
+         *beta = sc + 4 * kLsMaxRhs, *g0d = sc + 5 * kLsMaxRhs;
+  const int MT = (m + nb - 1) / nb, k = nrhs;
+  cudaStream_t st = stream;
+  PhaseTimer pt(st);
+  // 1. FP32 tile QR of a copy of A
+  k_copy_f32_mat<<<blocks_for((long long)m * n), TQR_THREADS, 0, st>>>(m, n, A, lda, F, m);
+  count_launch();
+  LS_CU(cudaGetLastError());
+  k_f64_to_f32_mat<<<dim3(blocks_for(m), k), TQR_THREADS, 0, st>>>(m, k, B, ldb, x32, m);
+  count_launch();
+  LS_CU(cudaGetLastError());
+  size_t dagb = 0;
+  if (tqr_tile_gels_worksize(m, n, k, nb, ib, &dagb) == 0) {
+    // 1+2 in one persistent launch: B (in FP32) rides along as an extra tile
+    // column, so the factorisation leaves Q^T B behind; then R X0 = (Q^T B)[0:n]
+    LS_TRY(tqr_stile_gels_dag(m, n, k, nb, ib, F, m, T, MT * ib, tau, n, x32, m, base + w.dag, dagb, st));
+    pt.mark(1);
+  } else {
+    LS_TRY(tqr_stile_geqrf(m, n, nb, ib, F, m, T, MT * ib, tau, n, st));
+    pt.mark(1);
+    LS_TRY(tqr_stile_unmqr('C', m, n, k, nb, ib, F, m, T, MT * ib, x32, m, st));
+    LS_TRY(tqr_strsm_lun(n, k, F, m, x32, m, st));
+  }
+  // 2. X0 = R^-1 (Q^T B)[0:n] in FP32, promoted
+  k_f32_to_f64_mat<<<dim3(blocks_for(n), k), TQR_THREADS, 0, st>>>(n, k, x32, m, X, ldx);
+  count_launch();
+  LS_CU(cudaGetLastError());
+  pt.mark(2);
+  // 3. CGLS on min ||A R^-1 Y - B||, tracking X = R^-1 Y
+  //    r = B - A X
+  for (int c = 0; c < k; ++c)
+    LS_CU(cudaMemcpyAsync(r + ix(0, c, m), B + ix(0, c, ldb), sizeof(double) * m, cudaMemcpyDeviceToDevice, st));
+  LS_TRY(gemm_sd_n(m, n, k, A, lda, X, ldx, r, m, -1.0, 1.0, st));
+  //    s = R^-T A^T r ; p = s ; gamma = |s|^2
+  LS_TRY(gemm_sd_t(m, n, k, A, lda, r, m, s, n, 1.0, 0.0, st));
+  LS_TRY(trsm_sd(1, n, k, F, m, s, n, st));
+  LS_CU(cudaMemcpyAsync(p, s, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, st));
+  LS_TRY(colnorm2(n, k, s, n, gamma, st));
+  LS_CU(cudaMemcpyAsync(g0d, gamma, sizeof(double) * k, cudaMemcpyDeviceToDevice, st));
+  double g0[kLsMaxRhs], gh[kLsMaxRhs];
+  LS_CU(cudaMemcpyAsync(g0, gamma, sizeof(double) * k, cudaMemcpyDeviceToHost, st));
+  LS_CU(cudaStreamSynchronize(st));
+  int it = 0, no_gain = 0;
+  double worst = 0.0, best = 1.0;
+  const double tol2 = tol * tol;
+  for (int c = 0; c < k; ++c) worst = std::max(worst, g0[c] > 0 ? 1.0 : 0.0);
+  // Stops when every column is below tol (columns below it are frozen), or
+  // when the worst column has not improved for three iterations (the
+  // attainable accuracy is reached).
+  while (it < maxit && worst > 0.0) {
+    // t = R^-1 p ; q = A t ; alpha = gamma / |q|^2
+    LS_CU(cudaMemcpyAsync(t, p, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, st));
+    LS_TRY(trsm_sd(0, n, k, F, m, t, n, st));
+    LS_TRY(gemm_sd_n(m, n, k, A, lda, t, n, q, m, 1.0, 0.0, st));
+    LS_TRY(colnorm2(m, k, q, m, qq, st));
+    k_cgls_alpha<<<1, 32, 0, st>>>(k, gamma, qq, g0d, tol2, alpha);
+    count_launch();
+    //    X += alpha t ; r -= alpha q
+    LS_TRY(axpy_cols(n, k, alpha, 0, t, n, X, ldx, st));
+    LS_TRY(axpy_cols(m, k, alpha, 1, q, m, r, m, st));
+    //    s = R^-T A^T r ; beta = |s|^2 / gamma ; p = s + beta p
+    LS_TRY(gemm_sd_t(m, n, k, A, lda, r, m, s, n, 1.0, 0.0, st));
+    LS_TRY(trsm_sd(1, n, k, F, m, s, n, st));
+    LS_TRY(colnorm2(n, k, s, n, gnew, st));
+    k_cgls_beta<<<1, 32, 0, st>>>(k, gamma, gnew, beta);
+    count_launch();
+    k_xpby_cols<<<dim3(blocks_for(n), k), TQR_THREADS, 0, st>>>(n, k, s, n, beta, p, n);
+    count_launch();
+    LS_CU(cudaGetLastError());
+    ++it;
+    LS_CU(cudaMemcpyAsync(gh, gamma, sizeof(double) * k, cudaMemcpyDeviceToHost, st));
+    LS_CU(cudaStreamSynchronize(st));
+    worst = 0.0;
+    for (int c = 0; c < k; ++c)
+      if (g0[c] > 0) worst = std::max(worst, std::sqrt(gh[c] / g0[c]));
+    if (worst <= tol) break;
+    if (worst < best) {
+      best = worst;
+      no_gain = 0;
+    } else if (++no_gain >= 3) {
+      break;
+    }
+  }
+  pt.mark(3);
+  pt.finish(it);
+  if (iters) *iters = it;
+  if (relres) *relres = worst;
+  return 0;
+}
+
+}  // extern "C"

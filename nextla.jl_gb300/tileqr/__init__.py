@@ -436,3 +436,92 @@ def tile_gels(A, B, nb=256, ib=32):
     _call(_prefix(A, T, tau, B), "tile_gels", m, n, B.shape[1], nb, ib, pa, lda, pt, ldt, pu, ldu,
           pb, ldb)
     return B[:n], T, tau
+
+
+# ---- mixed-precision least squares -----------------------------------------
+
+def lstsq_mixed(A32, B, nb=256, ib=32, maxit=50, tol=1e-13):
+    """min ||A X - B|| for a float32 A and float64 B: FP32 tile QR, FP64 CGLS
+    refinement preconditioned by R (tqr_dsgels).  Returns (X, iterations,
+    relative preconditioned residual reached).  A and B are left unchanged."""
+    import ctypes
+    if A32.dtype != torch.float32 or B.dtype != torch.float64:
+        raise TypeError("lstsq_mixed wants a float32 A and a float64 B")
+    m, n = A32.shape
+    k = B.shape[1]
+    pa, lda = _mat(A32)
+    pb, ldb = _mat(B)
+    X = zeros(n, k, dtype=torch.float64, device=A32.device)
+    px, ldx = _mat(X)
+    L = _lib.lib()
+    size = ctypes.c_size_t(0)
+    L.tqr_dsgels_worksize(m, n, k, nb, ib, ctypes.byref(size))
+    key = ("sgels", str(A32.device), size.value)
+    w = _WORK.get(key)
+    if w is None:
+        w = torch.empty(size.value + 256, dtype=torch.uint8, device=A32.device)
+        _WORK[key] = w
+    wp = w.data_ptr() + ((-w.data_ptr()) % 256)
+    it = ctypes.c_int(0)
+    rr = ctypes.c_double(0)
+    st = torch.cuda.current_stream()
+    rc = L.tqr_dsgels(m, n, k, nb, ib, pa, lda, pb, ldb, px, ldx, maxit, tol, ctypes.c_void_p(wp),
+                      size.value, ctypes.byref(it), ctypes.byref(rr), st.cuda_stream)
+    if rc < 0:
+        raise ArgumentError(f"dsgels: illegal value of argument {-rc}")
+    if rc > 0:
+        raise RuntimeError(f"dsgels: CUDA error {rc}")
+    if _BLOCKING:
+        st.synchronize()
+    return X, it.value, rr.value
+
+
+def dsgels_phases():
+    """Device ms of the last mixed solve: (FP32 QR, X0, CGLS), iterations."""
+    import ctypes
+    ms = (ctypes.c_double * 3)()
+    it = ctypes.c_int(0)
+    _lib.lib().tqr_dsgels_phases(ms, ctypes.byref(it))
+    return {"qr32_ms": ms[0], "x0_ms": ms[1], "cgls_ms": ms[2], "iterations": it.value}
+
+
+def lstsq_fp64(A, B, nb=256, ib=32):
+    """The plain FP64 least-squares solve on the tile QR: factors A in place
+    (persistent kernel when the shape allows), B := Q^T B, then R X = B[0:n].
+    Returns the view of B holding X."""
+    import ctypes
+    m, n = A.shape
+    k = B.shape[1]
+    size = ctypes.c_size_t(0)
+    L = _lib.lib()
+    if 0 < k <= nb and L.tqr_tile_gels_worksize(m, n, k, nb, ib, ctypes.byref(size)) == 0:
+        # one persistent launch factors A with B as an extra tile column, then R X = Q^T B
+        ts, taus = tile_shapes(m, n, nb, ib)
+        T = zeros(*ts, dtype=A.dtype, device=A.device)
+        tau = zeros(*taus, dtype=A.dtype, device=A.device)
+        key = ("gels", str(A.device), size.value)
+        w = _WORK.get(key)
+        if w is None:
+            w = torch.empty(size.value + 256, dtype=torch.uint8, device=A.device)
+            _WORK[key] = w
+        wp = w.data_ptr() + ((-w.data_ptr()) % 256)
+        pa, lda = _mat(A)
+        pt, ldt = _mat(T)
+        pu, ldu = _mat(tau)
+        pb, ldb = _mat(B)
+        p = _prefix(A, B)
+        st = torch.cuda.current_stream()
+        rc = getattr(L, f"tqr_{p}tile_gels_dag")(m, n, k, nb, ib, pa, lda, pt, ldt, pu, ldu, pb, ldb,
+                                                 ctypes.c_void_p(wp), size.value, st.cuda_stream)
+        if rc < 0:
+            raise ArgumentError(f"tile_gels: illegal value of argument {-rc}")
+        if rc > 0:
+            raise RuntimeError(f"tile_gels: CUDA error {rc}")
+        if _BLOCKING:
+            st.synchronize()
+        return B[:n]
+    T, _ = tile_geqrf(A, nb, ib)
+    tile_unmqr("C", A, T, B, nb, ib)
+    X = B[:n]
+    trsm_lun(A[:n, :n], X)
+    return X

@@ -122,3 +122,12 @@ def test_dag_shape_eligibility(L):
     assert tileqr.dag_worksize(1024, 1024, 512, 32) is None      # tile wider than one CTA holds
     assert tileqr.dag_worksize(1024, 1024, 256, 128) is None     # T/V blocks exceed shared memory
     assert tileqr.dag_worksize(8192, 8192, 256, 32) > 0
+
+
+@pytest.mark.parametrize("shape", [(1024, 1024, 4, 256, 32), (32768, 4096, 4, 256, 32),
+                                   (2048, 512, 3, 256, 32), (4096, 1024, 16, 256, 32),
+                                   (768, 512, 1, 128, 16)])
+def test_dag_schedule_replay_with_rhs_tile(L, shape):
+    """Least-squares schedules: B rides along as one extra tile column."""
+    nt = ctypes.c_longlong(0)
+    assert L.tqr_tile_dag_check_rhs(*shape, ctypes.byref(nt)) == 0 and nt.value > 0
