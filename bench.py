@@ -46,6 +46,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--kernel", default=None, choices=["tsmqr", "tsqrt", "geqrt"],
                    help="time one tile kernel alone (for profiling) instead of the workload")
+    p.add_argument("--dtype", default="f64", choices=["f64", "f32"], help="element type for --kernel")
     p.add_argument("--no-ls", action="store_true", help="skip the least-squares comparison")
     p.add_argument("--ls-only", action="store_true", help="run only the least-squares comparison")
     p.add_argument("--ls-m", type=int, default=32768)
@@ -68,11 +69,12 @@ def kernel_bench(args):
     res = {}
     if args.kernel == "tsmqr":
         w = n - NB
-        A1, A2, V = tq.empty(NB, w), tq.empty(NB, w), tq.empty(NB, NB)
+        dt = torch.float32 if args.dtype == "f32" else torch.float64
+        A1, A2, V = tq.empty(NB, w, dtype=dt), tq.empty(NB, w, dtype=dt), tq.empty(NB, NB, dtype=dt)
         for t in (A1, A2):
             t.copy_(torch.randn(NB, w, generator=g, dtype=torch.float64, device="cuda"))
         V.copy_(torch.randn(NB, NB, generator=g, dtype=torch.float64, device="cuda") / 16)
-        T = tq.empty(IB, NB)
+        T = tq.empty(IB, NB, dtype=dt)
         T.copy_(torch.triu(torch.randn(IB, NB, generator=g, dtype=torch.float64, device="cuda")) / 16)
         run = lambda: tq.tsmqr("L", "C", NB, w, NB, w, NB, IB, A1, A2, V, T, None)
         fl = 4.0 * NB * NB * w

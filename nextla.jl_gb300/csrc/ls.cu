@@ -21,7 +21,7 @@
 // Kernels here (all FP64 arithmetic on FP32 matrix entries):
 //   k_gemm_sd_n   Y = alpha A X + beta Y          (A m-by-n FP32, X n-by-k)
 //   k_gemm_sd_t   Z += alpha A^T R               (split over row blocks, FP64 atomics)
-//   k_trsv_sd     triangular solve of one diagonal block, all k columns
+//   k_trinv_diag / k_blk_solve  triangular solves through inverted diagonal blocks
 //   small column kernels for the CGLS recurrences (dots, axpys)
 #include <algorithm>
 #include <cmath>
@@ -104,39 +104,6 @@ k_gemm_sd_t(int m, int n, const float *__restrict__ A, int lda, const double *__
       double v = warp_sum(acc[c]);
       if (lane == 0) atomicAdd(Z + ix(j, c, ldz), alpha * v);
     }
-  }
-}
-
-// One diagonal block of R (FP32, upper) solved in FP64 for all k columns of B:
-// trans = 0: R_bb x = b (back substitution); trans = 1: R_bb^T x = b (forward).
-// 1 / R_ii is formed once per row in parallel before the sequential sweep.
-__global__ void __launch_bounds__(TQR_THREADS)
-k_trsv_sd(int nb, int k, int trans, const float *__restrict__ Rm, int ldr, double *__restrict__ B, int ldb)
-{
-  __shared__ double x[256][kLsMaxRhs];
-  __shared__ double rinv[256];
-  for (int idx = threadIdx.x; idx < nb; idx += TQR_THREADS) rinv[idx] = 1.0 / (double)Rm[ix(idx, idx, ldr)];
-  for (int idx = threadIdx.x; idx < nb * k; idx += TQR_THREADS) {
-    int r = idx % nb, c = idx / nb;
-    x[r][c] = B[ix(r, c, ldb)];
-  }
-  __syncthreads();
-  const int t = threadIdx.x;
-  for (int step = 0; step < nb; ++step) {
-    const int i = trans ? step : nb - 1 - step;
-    if (t < k) x[i][t] *= rinv[i];
-    __syncthreads();
-    // rows still to solve: r < i (back) or r > i (forward)
-    const bool live = trans ? (t > i && t < nb) : (t < i);
-    if (live) {
-      const double a = trans ? (double)Rm[ix(i, t, ldr)] : (double)Rm[ix(t, i, ldr)];
-      for (int c = 0; c < k; ++c) x[t][c] = fma(-a, x[i][c], x[t][c]);
-    }
-    __syncthreads();
-  }
-  for (int idx = threadIdx.x; idx < nb * k; idx += TQR_THREADS) {
-    int r = idx % nb, c = idx / nb;
-    B[ix(r, c, ldb)] = x[r][c];
   }
 }
 
@@ -288,24 +255,102 @@ static int gemm_sd_t(int m, int n, int k, const float *A, int lda, const double 
   return 0;
 }
 
-// Solve R X = B (trans 0) or R^T X = B (trans 1) for the upper triangle of the
-// n-by-n FP32 R, in FP64, B n-by-k overwritten.  Blocked by 256.
-static int trsm_sd(int trans, int n, int k, const float *Rm, int ldr, double *B, int ldb, cudaStream_t st) {
-  const int bs = 256;
-  const int nblk = (n + bs - 1) / bs;
+// ---- triangular solves through inverted diagonal blocks -------------------
+// A serial back substitution costs ~450 cycles per row on GB300 (every FP64
+// instruction holds the pipe ~64 cycles), so the refinement inverts R's
+// 256-by-256 diagonal blocks once (in parallel, FP64) and every later solve
+// is a chain of small parallel products.
+
+// Rinv_b = R_bb^-1 (FP64, upper, 256-by-256 per block, ld 256) for column
+// chunk blockIdx.y (16 columns of the identity) of block blockIdx.x.
+__global__ void __launch_bounds__(TQR_THREADS)
+k_trinv_diag(int n, const float *__restrict__ Rm, int ldr, double *__restrict__ Rinv)
+{
+  __shared__ double x[256][17];
+  __shared__ double rinv[256];
+  const int b = blockIdx.x, b0 = b * 256, nbk = min(256, n - b0);
+  const int c0 = blockIdx.y * 16;
+  if (c0 >= nbk) return;
+  const int nc = min(16, nbk - c0);
+  const float *R = Rm + ix(b0, b0, ldr);
+  double *out = Rinv + (size_t)b * 256 * 256;
+  for (int idx = threadIdx.x; idx < nbk; idx += TQR_THREADS) rinv[idx] = 1.0 / (double)R[ix(idx, idx, ldr)];
+  for (int idx = threadIdx.x; idx < 256 * 16; idx += TQR_THREADS) {
+    int r = idx % 256, c = idx / 256;
+    x[r][c] = (r == c0 + c) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  // rows above c0 + nc - 1 are the only ones the identity columns reach
+  for (int i = c0 + nc - 1; i >= 0; --i) {
+    if (t < nc) x[i][t] *= rinv[i];
+    __syncthreads();
+    if (t < i) {
+      const double a = (double)R[ix(t, i, ldr)];
+      for (int c = 0; c < nc; ++c) x[t][c] = fma(-a, x[i][c], x[t][c]);
+    }
+    __syncthreads();
+  }
+  for (int idx = threadIdx.x; idx < 256 * nc; idx += TQR_THREADS) {
+    int r = idx % 256, c = idx / 256;
+    out[ix(r, c0 + c, 256)] = (r < nbk) ? x[r][c] : 0.0;
+  }
+}
+
+// X_b = op(Rinv_b) B_b for one diagonal block: trans 0 uses Rinv_b (upper),
+// trans 1 its transpose.  Threads: consecutive rows in a warp, k columns.
+__global__ void __launch_bounds__(TQR_THREADS)
+k_blk_solve(int trans, int nbk, int k, const double *__restrict__ Ri, const double *__restrict__ B, int ldb,
+            double *__restrict__ X, int ldx)
+{
+  const int rows = TQR_THREADS / k;
+  const int r = blockIdx.x * rows + threadIdx.x % rows, c = threadIdx.x / rows;
+  if (c >= k || r >= nbk || threadIdx.x >= rows * k) return;
+  const double *bc = B + ix(0, c, ldb);
+  double s0 = 0.0, s1 = 0.0;
+  if (!trans) {
+    int q = r;
+    for (; q + 1 < nbk; q += 2) {
+      s0 = fma(Ri[ix(r, q, 256)], bc[q], s0);
+      s1 = fma(Ri[ix(r, q + 1, 256)], bc[q + 1], s1);
+    }
+    if (q < nbk) s0 = fma(Ri[ix(r, q, 256)], bc[q], s0);
+  } else {
+    int q = 0;
+    for (; q + 1 <= r; q += 2) {
+      s0 = fma(Ri[ix(q, r, 256)], bc[q], s0);
+      s1 = fma(Ri[ix(q + 1, r, 256)], bc[q + 1], s1);
+    }
+    if (q <= r) s0 = fma(Ri[ix(q, r, 256)], bc[q], s0);
+  }
+  X[ix(r, c, ldx)] = s0 + s1;
+}
+
+static int trinv_diag(int n, const float *Rm, int ldr, double *Rinv, cudaStream_t st) {
+  const int nblk = (n + 255) / 256;
+  k_trinv_diag<<<dim3(nblk, 16), TQR_THREADS, 0, st>>>(n, Rm, ldr, Rinv);
+  count_launch();
+  return (int)cudaGetLastError();
+}
+
+// X = op(R)^-1 B for the FP32 upper R with its inverted diagonal blocks; B
+// (n-by-k) is consumed as scratch, X receives the solution.
+static int trsm_sd_inv(int trans, int n, int k, const float *Rm, int ldr, const double *Rinv, double *B, int ldb,
+                       double *X, int ldx, cudaStream_t st) {
+  const int nblk = (n + 255) / 256;
+  const int rows = TQR_THREADS / k;
   for (int q = 0; q < nblk; ++q) {
     const int b = trans ? q : nblk - 1 - q;
-    const int b0 = b * bs, nbk = std::min(bs, n - b0);
-    k_trsv_sd<<<1, TQR_THREADS, 0, st>>>(nbk, k, trans, Rm + ix(b0, b0, ldr), ldr, B + b0, ldb);
+    const int b0 = b * 256, nbk = std::min(256, n - b0);
+    k_blk_solve<<<(nbk + rows - 1) / rows, TQR_THREADS, 0, st>>>(trans, nbk, k, Rinv + (size_t)b * 65536,
+                                                                B + b0, ldb, X + b0, ldx);
     count_launch();
     LS_CU(cudaGetLastError());
     if (!trans && b0 > 0) {
-      // B[0:b0] -= R[0:b0, b0:b0+nbk] X_b
-      LS_TRY(gemm_sd_n(b0, nbk, k, Rm + ix(0, b0, ldr), ldr, B + b0, ldb, B, ldb, -1.0, 1.0, st));
+      LS_TRY(gemm_sd_n(b0, nbk, k, Rm + ix(0, b0, ldr), ldr, X + b0, ldx, B, ldb, -1.0, 1.0, st));
     } else if (trans && b0 + nbk < n) {
-      // B[b1:n] -= R[b0:b1, b1:n]^T X_b
       const int b1 = b0 + nbk;
-      LS_TRY(gemm_sd_t(nbk, n - b1, k, Rm + ix(b0, b1, ldr), ldr, B + b0, ldb, B + b1, ldb, -1.0, 1.0, st));
+      LS_TRY(gemm_sd_t(nbk, n - b1, k, Rm + ix(b0, b1, ldr), ldr, X + b0, ldx, B + b1, ldb, -1.0, 1.0, st));
     }
   }
   return 0;
@@ -359,7 +404,7 @@ struct PhaseTimer {
 
 // Workspace layout (bytes, each piece 256-aligned)
 struct MixedWs {
-  size_t F, T, tau, dag, x32, r, s, p, t, q, sc, total;
+  size_t F, T, tau, dag, x32, r, s, p, t, q, sc, rinv, tmpn, total;
 };
 
 static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -381,6 +426,8 @@ static int mixed_ws(int m, int n, int k, int nb, int ib, MixedWs *w) {
   w->t = take(sizeof(double) * (size_t)n * k);
   w->q = take(sizeof(double) * (size_t)m * k);
   w->sc = take(sizeof(double) * 8 * kLsMaxRhs);
+  w->rinv = take(sizeof(double) * 65536 * (size_t)((n + 255) / 256));
+  w->tmpn = take(sizeof(double) * (size_t)n * k);
   w->total = off;
   return dag ? 0 : 1;
 }
@@ -467,9 +514,11 @@ int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, 
   for (int c = 0; c < k; ++c)
     LS_CU(cudaMemcpyAsync(r + ix(0, c, m), B + ix(0, c, ldb), sizeof(double) * m, cudaMemcpyDeviceToDevice, st));
   LS_TRY(gemm_sd_n(m, n, k, A, lda, X, ldx, r, m, -1.0, 1.0, st));
-  //    s = R^-T A^T r ; p = s ; gamma = |s|^2
-  LS_TRY(gemm_sd_t(m, n, k, A, lda, r, m, s, n, 1.0, 0.0, st));
-  LS_TRY(trsm_sd(1, n, k, F, m, s, n, st));
+  //    R's diagonal blocks inverted once; s = R^-T A^T r ; p = s ; gamma = |s|^2
+  double *Rinv = (double *)(base + w.rinv), *tmpn = (double *)(base + w.tmpn);
+  LS_TRY(trinv_diag(n, F, m, Rinv, st));
+  LS_TRY(gemm_sd_t(m, n, k, A, lda, r, m, tmpn, n, 1.0, 0.0, st));
+  LS_TRY(trsm_sd_inv(1, n, k, F, m, Rinv, tmpn, n, s, n, st));
   LS_CU(cudaMemcpyAsync(p, s, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, st));
   LS_TRY(colnorm2(n, k, s, n, gamma, st));
   LS_CU(cudaMemcpyAsync(g0d, gamma, sizeof(double) * k, cudaMemcpyDeviceToDevice, st));
@@ -485,8 +534,8 @@ int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, 
   // attainable accuracy is reached).
   while (it < maxit && worst > 0.0) {
     // t = R^-1 p ; q = A t ; alpha = gamma / |q|^2
-    LS_CU(cudaMemcpyAsync(t, p, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, st));
-    LS_TRY(trsm_sd(0, n, k, F, m, t, n, st));
+    LS_CU(cudaMemcpyAsync(tmpn, p, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, st));
+    LS_TRY(trsm_sd_inv(0, n, k, F, m, Rinv, tmpn, n, t, n, st));
     LS_TRY(gemm_sd_n(m, n, k, A, lda, t, n, q, m, 1.0, 0.0, st));
     LS_TRY(colnorm2(m, k, q, m, qq, st));
     k_cgls_alpha<<<1, 32, 0, st>>>(k, gamma, qq, g0d, tol2, alpha);
@@ -495,8 +544,8 @@ int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, 
     LS_TRY(axpy_cols(n, k, alpha, 0, t, n, X, ldx, st));
     LS_TRY(axpy_cols(m, k, alpha, 1, q, m, r, m, st));
     //    s = R^-T A^T r ; beta = |s|^2 / gamma ; p = s + beta p
-    LS_TRY(gemm_sd_t(m, n, k, A, lda, r, m, s, n, 1.0, 0.0, st));
-    LS_TRY(trsm_sd(1, n, k, F, m, s, n, st));
+    LS_TRY(gemm_sd_t(m, n, k, A, lda, r, m, tmpn, n, 1.0, 0.0, st));
+    LS_TRY(trsm_sd_inv(1, n, k, F, m, Rinv, tmpn, n, s, n, st));
     LS_TRY(colnorm2(n, k, s, n, gnew, st));
     k_cgls_beta<<<1, 32, 0, st>>>(k, gamma, gnew, beta);
     count_launch();
