@@ -52,6 +52,9 @@ def parse():
     p.add_argument("--ls-m", type=int, default=32768)
     p.add_argument("--ls-n", type=int, default=4096)
     p.add_argument("--ls-no-orth", action="store_true")
+    p.add_argument("--no-batched", action="store_true", help="skip the batched uneven QR + solve")
+    p.add_argument("--batched-only", action="store_true", help="run only the batched uneven QR + solve")
+    p.add_argument("--batched-n", type=int, default=4096, help="problems per batch")
     return p.parse_args()
 
 
@@ -355,6 +358,81 @@ def ls_bench(tq, torch, m=32768, n=4096, k=4, steps=2, warmup=1, orth=True):
     return res
 
 
+def batched_bench(torch, nprob=4096, steps=5, warmup=3, peak=None):
+    """Batched uneven QR + least squares: nprob problems, m ~ U[32,512],
+    n ~ U[16,m], k ~ U[1,8], N(0,1) entries, one persistent launch replayed
+    from a CUDA graph.  Per precision: problems/s with inputs resident
+    (device restore of the packed A, B outside the events, replay timed) and
+    end to end (pinned host A, B copied in, replay, X copied out, all timed),
+    plus the per-problem residual ||A^T(B - AX)|| / (||A|| (||A|| ||X|| + ||B||))."""
+    from tileqr import _lib
+    from tileqr import batched as Bt
+    st = torch.cuda.current_stream()
+    out = {"workload": (f"{nprob} independent least-squares problems, m ~ U[32,512], n ~ U[16,m], "
+                        f"k ~ U[1,8] right-hand sides, N(0,1) entries (seeded); one persistent "
+                        f"launch per batch, replayed from a CUDA graph"),
+           "unit": "problems/s"}
+    ms_, ns_, ks_ = Bt.random_sizes(nprob, seed=SEED % 1000)
+    for tag, dt in (("f64", torch.float64), ("f32", torch.float32)):
+        bg = Bt.BatchedGels(ms_, ns_, ks_, dtype=dt, tune=True)
+        g = torch.Generator(device="cuda").manual_seed(SEED)
+        A0 = torch.randn(bg.A.shape, generator=g, device="cuda", dtype=torch.float64).to(dt)
+        B0 = torch.randn(bg.B.shape, generator=g, device="cuda", dtype=torch.float64).to(dt)
+        bg.capture()
+        times = []
+        launches0 = _lib.launch_count()
+        for rep in range(warmup + steps):
+            bg.A.copy_(A0)
+            bg.B.copy_(B0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            bg.replay(sync=False)
+            e1.record(st)
+            torch.cuda.synchronize()
+            if rep >= warmup:
+                times.append(e0.elapsed_time(e1))
+        launches = _lib.launch_count() - launches0
+        bad = bg.status()
+        res = bg.residuals(A0, B0)
+        # end to end: pinned host buffers in, replay, X out
+        hA = A0.cpu().pin_memory()
+        hB = B0.cpu().pin_memory()
+        hX = torch.empty_like(hB).pin_memory()
+        ets = []
+        for rep in range(1 + min(steps, 3)):
+            f0 = torch.cuda.Event(enable_timing=True)
+            f1 = torch.cuda.Event(enable_timing=True)
+            f0.record(st)
+            bg.A.copy_(hA, non_blocking=True)
+            bg.B.copy_(hB, non_blocking=True)
+            bg.replay(sync=False)
+            hX.copy_(bg.B, non_blocking=True)
+            f1.record(st)
+            torch.cuda.synchronize()
+            if rep >= 1:
+                ets.append(f0.elapsed_time(f1))
+        esz = A0.element_size()
+        ms = statistics.median(times)
+        fl = bg.flops()
+        out[tag] = {
+            "problems_per_s": nprob / (ms / 1e3), "ms_per_batch": ms, "ms_min": min(times),
+            "tflops": fl / (ms / 1e3) / 1e12, "algorithmic_flops_per_batch": fl,
+            "frac_of_fp64_simt_peak": (fl / (ms / 1e3) / 1e12 / peak) if (peak and tag == "f64") else None,
+            "gpu_launches_per_batch": launches / (warmup + steps),
+            "rejected_descriptors": bad[0],
+            "residual_max": float(res.max().item()), "residual_median": float(res.median().item()),
+            "e2e": {"value": nprob / (statistics.median(ets) / 1e3), "unit": "problems/s",
+                    "ms_per_batch": statistics.median(ets),
+                    "h2d_bytes_per_step": esz * (A0.numel() + B0.numel()),
+                    "d2h_bytes_per_step": esz * B0.numel()},
+            "tuning_ib_nw_by_n_class": {c: Bt.tuning(dt, c) for c in (32, 64, 128, 256, 512)},
+        }
+        bg.close()
+        del bg, A0, B0, hA, hB, hX
+    return out
+
+
 def fp64_peak(tq_lib, torch):
     """SIMT DFMA ceiling of this GPU (independent FMA chains), TFLOP/s."""
     import ctypes
@@ -405,6 +483,16 @@ def main():
         tq.set_blocking(False)
         res = ls_bench(tq, torch, args.ls_m, args.ls_n, 4, max(1, args.steps), max(1, args.warmup),
                        orth=not args.ls_no_orth)
+        print(json.dumps(res), flush=True)
+        return 0
+    if args.batched_only:
+        import torch
+
+        import tileqr_build
+        from tileqr import _lib
+        tileqr_build.build()
+        res = batched_bench(torch, args.batched_n, max(1, args.steps), max(3, args.warmup),
+                            peak=fp64_peak(_lib, torch))
         print(json.dumps(res), flush=True)
         return 0
     world, rank, local = dist_setup(args)
@@ -537,6 +625,10 @@ def main():
     if rank == 0 and world == 1 and not args.no_ls:
         ls = ls_bench(tq, torch, args.ls_m, args.ls_n, 4, 2, 1, orth=not args.ls_no_orth)
 
+    bat = None
+    if rank == 0 and world == 1 and not args.no_batched:
+        bat = batched_bench(torch, args.batched_n, 5, 3, peak=peak)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -547,6 +639,7 @@ def main():
             "gpu_launches": launches,
             "dag_stats_last_step": dag,
             "least_squares_mixed_vs_fp64": ls,
+            "batched_uneven_gels": bat,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

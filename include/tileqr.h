@@ -205,6 +205,60 @@ int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, 
  * ms[1] X0 = R^-1 Q^T B, ms[2] FP64 CGLS refinement; iters its iterations. */
 int tqr_dsgels_phases(double *ms, int *iters);
 
+/* ---- Batched uneven QR + least squares (no counterpart in NextLA, which
+ * factors one matrix at a time) ----
+ * nprob independent problems min ||A_q X_q - B_q||, A_q m_q-by-n_q with
+ * 1 <= n_q <= m_q <= TQR_BATCH_MAX_M and 0 <= k_q <= TQR_BATCH_MAX_K right-hand
+ * sides (k_q = 0: QR only).  Each problem is geqrt! on its A_q (the
+ * arithmetic of src/geqrt.jl:22-68 with inner block ib_q), the same
+ * reflectors applied to B_q (unmqr!, src/unmqr.jl:52-149, 'L','T'), then
+ * LeftUpperTRSM! (src/trsm.jl:36-63) on the first n_q rows.  On return A_q
+ * holds geqrt!'s R and V, and B_q's rows 0:n_q hold X_q.
+ *
+ * tqr_batched_plan (host only): from the sizes, fills nprob descriptors of
+ * tqr_batched_problem_bytes() bytes each -- int m, n, k, ib, nw, pad;
+ * int64 a_off, b_off -- with A_q packed column-major at A + a_off (lda = m_q)
+ * and B_q at B + b_off (ldb = m_q), every problem 32-element aligned, ib and
+ * the strip width nw taken from the tuning table, and `order`, the problems by
+ * decreasing flops; a_elems, b_elems are the packed lengths.  Returns
+ * -(1000 + q) if problem q is out of range.
+ * tqr_?batched_gels: one persistent launch (plus a counter reset) over the
+ * device copies of the descriptors and order; work (256-byte aligned,
+ * tqr_batched_worksize bytes) holds the counter and per-CTA scratch.
+ * Descriptors the kernel finds out of range are skipped and counted:
+ * tqr_batched_status reads that count and the first bad index (synchronises
+ * stream).  No allocation, no host synchronisation.
+ * tqr_batched_graph: captures the same launch into an instantiated CUDA graph
+ * (cudaGraphExec_t) for replay with tqr_batched_graph_launch.
+ * tqr_batched_autotune: times every (ib, nw) candidate on synthetic problems
+ * of each column-count class and stores the fastest in the table (allocates;
+ * call it before planning and outside any capture); tqr_batched_tuning reads
+ * the table entry for a column count.
+ * tqr_?batched_residual: per problem ||A^T (B - A X)||_F /
+ * (||A||_F (||A||_F ||X||_F + ||B||_F)) in FP64 from the original A, B and the
+ * solution (in B's layout); -1 marks a rejected descriptor. */
+#define TQR_BATCH_MAX_M 512
+#define TQR_BATCH_MAX_K 8
+int tqr_batched_problem_bytes(void);
+int tqr_batched_plan(int dtype_bytes, int nprob, const int *m, const int *n, const int *k, void *problems,
+                     int *order, long long *a_elems, long long *b_elems);
+int tqr_batched_worksize(int dtype_bytes, size_t *bytes);
+int tqr_batched_autotune(int dtype_bytes, int force, cudaStream_t stream);
+int tqr_batched_tuning(int dtype_bytes, int n, int *ib, int *nw);
+int tqr_dbatched_gels(int nprob, const void *problems, const int *order, double *A, double *B, void *work,
+                      size_t lwork, cudaStream_t stream);
+int tqr_sbatched_gels(int nprob, const void *problems, const int *order, float *A, float *B, void *work,
+                      size_t lwork, cudaStream_t stream);
+int tqr_batched_status(const void *work, int *bad, int *first_bad, cudaStream_t stream);
+int tqr_dbatched_residual(int nprob, const void *problems, const double *A0, const double *B0,
+                          const double *X, double *res, cudaStream_t stream);
+int tqr_sbatched_residual(int nprob, const void *problems, const float *A0, const float *B0,
+                          const float *X, double *res, cudaStream_t stream);
+int tqr_batched_graph(int dtype_bytes, int nprob, const void *problems, const int *order, void *A, void *B,
+                      void *work, size_t lwork, void **graph_exec);
+int tqr_batched_graph_launch(void *graph_exec, cudaStream_t stream);
+int tqr_batched_graph_destroy(void *graph_exec);
+
 /* ---- Measurement hooks (no counterpart in NextLA; used by the benchmark) ----
  * tqr_launch_count: kernels this library has launched since it was loaded.
  * tqr_profile_enable / tqr_profile_read: while enabled, the tile driver brackets

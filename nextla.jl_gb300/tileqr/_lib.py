@@ -52,6 +52,20 @@ DIAG = {
     "tqr_dsgels_phases": ([ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I)], _I),
     "tqr_dsgels": ([_I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _I, ctypes.c_double, _P, ctypes.c_size_t,
                     ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_double), _P], _I),
+    "tqr_batched_problem_bytes": ([], _I),
+    "tqr_batched_plan": ([_I, _I, _P, _P, _P, _P, _P, ctypes.POINTER(ctypes.c_longlong),
+                          ctypes.POINTER(ctypes.c_longlong)], _I),
+    "tqr_batched_worksize": ([_I, ctypes.POINTER(ctypes.c_size_t)], _I),
+    "tqr_batched_autotune": ([_I, _I, _P], _I),
+    "tqr_batched_tuning": ([_I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
+    "tqr_dbatched_gels": ([_I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
+    "tqr_sbatched_gels": ([_I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
+    "tqr_batched_status": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I), _P], _I),
+    "tqr_dbatched_residual": ([_I, _P, _P, _P, _P, _P, _P], _I),
+    "tqr_sbatched_residual": ([_I, _P, _P, _P, _P, _P, _P], _I),
+    "tqr_batched_graph": ([_I, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, ctypes.POINTER(_P)], _I),
+    "tqr_batched_graph_launch": ([_P, _P], _I),
+    "tqr_batched_graph_destroy": ([_P], _I),
 }
 
 _lib = None
