@@ -259,6 +259,37 @@ int tqr_batched_graph(int dtype_bytes, int nprob, const void *problems, const in
 int tqr_batched_graph_launch(void *graph_exec, cudaStream_t stream);
 int tqr_batched_graph_destroy(void *graph_exec);
 
+/* ---- Differentiable batched QR (no counterpart in NextLA, which has no
+ * derivative rules) ----
+ * batch problems of one shape m-by-n, 1 <= n <= 256, m >= n, each stored
+ * column-major and packed (problem p at offset p m n, ld m; n-by-n matrices
+ * at p n n, ld n; tau at p ceil(m/256) n).  Every problem is a flat-tree tile
+ * QR over 256-row tiles -- geqrt! on the top tile (src/geqrt.jl:22-68), tsqrt!
+ * of the top triangle against each further tile (src/tsqrt.jl:46-126), inner
+ * block ib -- run by one CTA of a persistent launch.
+ * tqr_?qr_batched_fwd: F (in: A; out: the packed factor, R on/above the top
+ * tile's diagonal and the reflectors V below), tau, the explicit thin Q
+ * (m-by-n) and R (n-by-n, zero below the diagonal).
+ * tqr_?qr_batched_bwd: the adjoint Abar = (Qbar + Q copyltu(M)) R^-T with
+ * M = R Rbar^T - Qbar^T Q and copyltu(M) = tril(M) + tril(M,-1)^T, from the
+ * saved F and tau (every T factor is recomputed from V and tau by the larft!
+ * recursion, src/larft.jl:53-86, so none is kept between the passes) and the
+ * cotangents Qbar (m-by-n) and Rbar (n-by-n; only its upper triangle is read).
+ * work: 256-byte aligned, tqr_qr_batched_worksize bytes (per-CTA T and n-by-n
+ * scratch), shared by both passes.  Argument errors: -1 batch, -2 m, -3 n,
+ * -4 ib, -5.. pointers, -8 work too small. */
+int tqr_qr_batched_worksize(int dtype_bytes, int m, int n, int ib, size_t *bytes);
+int tqr_dqr_batched_fwd(int batch, int m, int n, int ib, double *F, double *tau, double *Q, double *R,
+                        void *work, size_t lwork, cudaStream_t stream);
+int tqr_sqr_batched_fwd(int batch, int m, int n, int ib, float *F, float *tau, float *Q, float *R,
+                        void *work, size_t lwork, cudaStream_t stream);
+int tqr_dqr_batched_bwd(int batch, int m, int n, int ib, const double *F, const double *tau,
+                        const double *Qbar, const double *Rbar, double *Abar, void *work, size_t lwork,
+                        cudaStream_t stream);
+int tqr_sqr_batched_bwd(int batch, int m, int n, int ib, const float *F, const float *tau,
+                        const float *Qbar, const float *Rbar, float *Abar, void *work, size_t lwork,
+                        cudaStream_t stream);
+
 /* ---- Measurement hooks (no counterpart in NextLA; used by the benchmark) ----
  * tqr_launch_count: kernels this library has launched since it was loaded.
  * tqr_profile_enable / tqr_profile_read: while enabled, the tile driver brackets

@@ -66,6 +66,11 @@ DIAG = {
     "tqr_batched_graph": ([_I, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, ctypes.POINTER(_P)], _I),
     "tqr_batched_graph_launch": ([_P, _P], _I),
     "tqr_batched_graph_destroy": ([_P], _I),
+    "tqr_qr_batched_worksize": ([_I, _I, _I, _I, ctypes.POINTER(ctypes.c_size_t)], _I),
+    "tqr_dqr_batched_fwd": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
+    "tqr_sqr_batched_fwd": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
+    "tqr_dqr_batched_bwd": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
+    "tqr_sqr_batched_bwd": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
 }
 
 _lib = None

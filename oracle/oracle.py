@@ -209,3 +209,46 @@ def tile_lstsq(A, B, nb, ib):
     X = np.array(B[:n], order="F")
     trsm_lun(A[:n, :n], X)
     return X
+
+
+# ---------------------------------------------------------------------------
+# Differentiable QR: FP64 CPU reference of the forward (explicit thin Q) and of
+# the adjoint.  The forward is the same flat-tree tile QR as above (one tile
+# column when n <= nb), so Q and R carry the same diagonal signs as the GPU's.
+# ---------------------------------------------------------------------------
+
+def qr_explicit(A, nb=256, ib=32):
+    """(Q, R, F): thin Q (m-by-n), R (n-by-n upper) and the packed factor."""
+    F = np.array(A, order="F", dtype=np.float64)
+    m, n = F.shape
+    T, _ = tile_geqrf(F, nb, ib)
+    Q = np.asfortranarray(np.eye(m, n))
+    tile_unmqr("N", F, T, Q, nb, ib)
+    R = np.triu(F[:n, :n])
+    return Q, R, F
+
+
+def qr_adjoint(Q, R, Qbar, Rbar):
+    """Thin-QR pullback (Walter & Lehmann 2018, Algorithms for the QR
+    adjoint; Liao, Liu, Wang & Xiang 2019): M = R Rbar^T - Qbar^T Q,
+    Abar = (Qbar + Q copyltu(M)) R^-T, copyltu(M) = tril(M) + tril(M, -1)^T.
+    Only the upper triangle of Rbar enters (R has no other entries)."""
+    from scipy.linalg import solve_triangular
+    M = R @ np.triu(Rbar).T - Qbar.T @ Q
+    C = np.tril(M) + np.tril(M, -1).T
+    Y = Qbar + Q @ C
+    return solve_triangular(R, Y.T, lower=False).T
+
+
+def ls_loss_cotangents(Q, R, b, y, dQ, dR):
+    """Value and (Qbar, Rbar) of f = 1/2 ||R^-1 Q^T b - y||^2 + <dQ, Q> + <dR, R>
+    for one problem (b: m, y: n)."""
+    from scipy.linalg import solve_triangular
+    c = Q.T @ b
+    x = solve_triangular(R, c, lower=False)
+    r = x - y
+    f = 0.5 * float(r @ r) + float(np.sum(dQ * Q)) + float(np.sum(dR * np.triu(R)))
+    cbar = solve_triangular(R, r, lower=False, trans="T")
+    Qbar = dQ + np.outer(b, cbar)
+    Rbar = np.triu(dR) - np.triu(np.outer(cbar, x))
+    return f, Qbar, Rbar
