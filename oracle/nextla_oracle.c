@@ -330,16 +330,26 @@ int ora_dunmqr(char side, char trans, int m, int n, int k, int ib, const double 
 }
 
 /* ------------------------------------------------------------------------ */
-/* pamm (l = 0, columnwise, forward) and parfb (src/pamm.jl:97-128,301-325, */
-/* src/parfb.jl:121-129,189): the two GEMMs of the pentagonal apply.         */
+/* pamm and parfb, columnwise, forward (src/pamm.jl:97-175,301-368,         */
+/* src/parfb.jl:121-137,189): the two GEMMs of the pentagonal apply.         */
+/* V's first l columns are trapezoidal: over the last l of the mv rows they */
+/* hold only an upper triangle (pamm's 'U' trimatmul on V[mp:mp+l-1, 1:l]);  */
+/* the strictly lower part of that triangle is never read.  l = 0 is the    */
+/* rectangular form tsmqr uses.                                             */
 /* ------------------------------------------------------------------------ */
-static void parfb_l0(char side, char trans, int m2, int n2, int k,
+static double vtrap(const double *V, int ldv, int r, int p, int mv, int l)
+{
+    if (p < l && r >= mv - l && r - (mv - l) > p) return 0.0;
+    return V[IDX(r, p, ldv)];
+}
+
+static void parfb_lv(char side, char trans, int m2, int n2, int k, int l,
                      double *A1, int lda1, double *A2, int lda2,
                      const double *V, int ldv, const double *T, int ldt, double *W, int ldw)
 {
 #define A1m(r, c) A1[IDX(r, c, lda1)]
 #define A2m(r, c) A2[IDX(r, c, lda2)]
-#define Vm(r, c) V[IDX(r, c, ldv)]
+#define Vm(r, c) vtrap(V, ldv, r, c, side == 'L' ? m2 : n2, l)
 #define Tm(r, c) T[IDX(r, c, ldt)]
 #define Wm(r, c) W[IDX(r, c, ldw)]
     int tr = (trans != 'N');                                /* tfun = adjoint */
@@ -432,7 +442,26 @@ int ora_dparfb(char side, char trans, int m1, int n1, int m2, int n2, int k,
            reference tests never reach.  Treat it as a no-op. */
         return 0;
     }
-    parfb_l0(side, trans, m2, n2, k, A1, lda1, A2, lda2, V, ldv, T, ldt, W, ldw);
+    parfb_lv(side, trans, m2, n2, k, 0, A1, lda1, A2, lda2, V, ldv, T, ldt, W, ldw);
+    return 0;
+}
+
+/* parfb with a trapezoidal part of order l (parfb.jl:44-189; the form     */
+/* ttqrt!/ttmqr! call, src/ttqrt.jl:104-112, src/ttmqr.jl:60-90).           */
+int ora_dparfb_l(char side, char trans, int m1, int n1, int m2, int n2, int k, int l,
+                 double *A1, int lda1, double *A2, int lda2, const double *V, int ldv,
+                 const double *T, int ldt, double *W, int ldw)
+{
+    if (side != 'L' && side != 'R') return -1;              /* parfb.jl:47-85 */
+    if (trans != 'N' && trans != 'C' && trans != 'T') return -2;
+    if (m1 < 0) return -3;
+    if (n1 < 0) return -4;
+    if (m2 < 0 || (side == 'R' && m1 != m2)) return -5;
+    if (n2 < 0 || (side == 'L' && n1 != n2)) return -6;
+    if (k < 0) return -7;
+    if (l < 0 || l > k) return -8;
+    if (m1 == 0 || n1 == 0 || n2 == 0 || k == 0 || m2 == 0) return 0;
+    parfb_lv(side, trans, m2, n2, k, l, A1, lda1, A2, lda2, V, ldv, T, ldt, W, ldw);
     return 0;
 }
 
@@ -667,5 +696,288 @@ int ora_dtrsm_lun(int n, int nrhs, const double *A, int lda, double *B, int ldb)
         for (int i = n - 1; i >= 0; --i)
             for (int r = 0; r < i; ++r) b[r] -= (A[IDX(r, i, lda)] / A[IDX(r, r, lda)]) * b[i];
     }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* ttqrt: QR of [A1 (upper); A2 (upper)] (src/ttqrt.jl:1-119).              */
+/* Column r's reflector uses A2 rows [0, min(r+1, m)) (ttqrt.jl:9).  The T  */
+/* column T[0:i, r] = -tau T[0:i,0:i] V^T v_r sums each product over the    */
+/* rows both reflectors occupy, i.e. the upper triangle of A2 only: the     */
+/* reference's loop (ttqrt.jl:66-71) runs to row min(r-1, m) and so also    */
+/* reads A2 below the diagonal of the earlier columns, which is zero on     */
+/* the upper-triangular tiles its tests pass (test/ttqrt.jl:13-14) and      */
+/* holds geqrt's reflectors in a tree factorisation; LAPACK's dtpqrt        */
+/* (l = n), which those tests compare against, reads only the triangle too. */
+/* ------------------------------------------------------------------------ */
+int ora_dttqrt(int m, int n, int ib, double *A1, int lda1, double *A2, int lda2,
+               double *T, int ldt, double *tau, double *work)
+{
+    if (m < 0) return -1;                                   /* ttqrt.jl:88-98 */
+    if (n < 0) return -2;
+    if (ib < 0) return -3;
+    if (m == 0 || n == 0 || ib == 0) return 0;
+    int k = imin(m, n);
+#define A1m(r, c) A1[IDX(r, c, lda1)]
+#define A2m(r, c) A2[IDX(r, c, lda2)]
+#define Tm(r, c) T[IDX(r, c, ldt)]
+    for (int ii = 0; ii < k; ii += ib) {                    /* ttqrt.jl:103 */
+        int sb = imin(k - ii, ib);
+        for (int i = 0; i < sb; ++i) {                      /* ttqrt_block_kernel! */
+            int r = ii + i;
+            int mi = imin(r + 1, m);
+            double alpha = A1m(r, r);
+            double xnorm_sq = 0.0;
+            for (int p = 0; p < mi; ++p) { double vp = A2m(p, r); xnorm_sq += vp * vp; }
+            double xnorm = sqrt(xnorm_sq);
+            if (xnorm == 0.0) { tau[r] = 0.0; continue; }  /* ttqrt.jl:21-24: T untouched */
+            double beta = -copysign(sqrt(alpha * alpha + xnorm_sq), alpha);
+            double tv = (beta - alpha) / beta;
+            double scale = 1.0 / (alpha - beta);
+            for (int p = 0; p < mi; ++p) A2m(p, r) *= scale;
+            A1m(r, r) = beta;
+            tau[r] = tv;
+            if ((sb - i - 1) > 0 && (r + 1) < n) {          /* ttqrt.jl:37-56 */
+                int ncc = sb - i - 1;
+                for (int j = 1; j <= ncc; ++j) {
+                    double wj = A1m(r, r + j);
+                    for (int p = 0; p < mi; ++p) wj += A2m(p, r + j) * A2m(p, r);
+                    work[j - 1] = wj;
+                }
+                for (int j = 1; j <= ncc; ++j) A1m(r, r + j) -= tv * work[j - 1];
+                for (int j = 1; j <= ncc; ++j) {
+                    double wj = work[j - 1];
+                    for (int p = 0; p < mi; ++p) A2m(p, r + j) -= tv * A2m(p, r) * wj;
+                }
+            }
+            if (i > 0) {                                    /* ttqrt.jl:58-79 */
+                for (int p = 0; p < i; ++p) {
+                    int mq = imin(ii + p + 1, m);
+                    double acc = 0.0;
+                    for (int q = 0; q < mq; ++q) acc += A2m(q, ii + p) * A2m(q, r);
+                    Tm(p, r) = (-tv) * acc;
+                }
+                for (int p = 0; p < i; ++p) work[p] = Tm(p, r);
+                for (int p = 0; p < i; ++p) {
+                    double acc = 0.0;
+                    for (int q = p; q < i; ++q) acc += Tm(p, ii + q) * work[q];
+                    Tm(p, r) = acc;
+                }
+            }
+            Tm(i, r) = tv;
+        }
+        if (n > ii + sb) {                                  /* ttqrt.jl:105-116 */
+            int mi2 = imin(ii + sb, m), ni = n - (ii + sb);
+            int l = imin(sb, imax(0, mi2 - ii));
+            ora_dparfb_l('L', 'C', sb, ni, mi2, ni, sb, l, A1 + IDX(ii, ii + sb, lda1), lda1,
+                         A2 + IDX(0, ii + sb, lda2), lda2, A2 + IDX(0, ii, lda2), lda2,
+                         T + IDX(0, ii, ldt), ldt, work, sb);
+        }
+    }
+#undef A1m
+#undef A2m
+#undef Tm
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* ttmqr: apply the Q of ttqrt to [A1; A2] or [A1 A2] (src/ttmqr.jl:1-95).  */
+/* Block i touches A2 rows (side L; columns for R) [0, min(i+kb, m2)), its  */
+/* last l of them triangular with l = min(kb, rows - i), the count ttqrt!   */
+/* itself passes (ttqrt.jl:108).  ttmqr! computes l = min(kb, m2 - i - 1)  */
+/* (0-based i; ttmqr.jl:66,79), one smaller for the block that ends on the  */
+/* tile's last row, which adds that row's below-diagonal entry of each      */
+/* reflector -- zero in its tests (test/ttmqr.jl:14: V = triu(randn)).      */
+/* ------------------------------------------------------------------------ */
+int ora_dttmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib,
+               double *A1, int lda1, double *A2, int lda2, const double *V, int ldv,
+               const double *T, int ldt, double *work)
+{
+    if (side != 'L' && side != 'R') return -1;              /* ttmqr.jl:3-37 */
+    if (trans != 'N' && trans != 'C' && trans != 'T') return -2;
+    if (m1 < 0) return -3;
+    if (n1 < 0) return -4;
+    if (m2 < 0 || (m2 != m1 && side == 'R')) return -5;
+    if (n2 < 0 || (n2 != n1 && side == 'L')) return -6;
+    if (k < 0) return -7;
+    k = imin(k, side == 'L' ? m1 : n1);
+    if (ib < 0) return -8;
+    if (m1 == 0 || n1 == 0 || m2 == 0 || n2 == 0 || k == 0 || ib == 0) return 0;
+    int fwd = (side == 'L' && trans != 'N') || (side == 'R' && trans == 'N');
+    int i1, i3;
+    if (fwd) { i1 = 0; i3 = ib; } else { i1 = ((k - 1) / ib) * ib; i3 = -ib; }
+    int nblk = (k - 1) / ib + 1;
+    for (int b = 0, i = i1; b < nblk; ++b, i += i3) {
+        int kb = imin(ib, k - i);
+        if (side == 'L') {
+            int mi2 = imin(i + kb, m2);
+            int l = imin(kb, imax(0, mi2 - i));
+            ora_dparfb_l('L', trans, kb, n1, mi2, n2, kb, l, A1 + IDX(i, 0, lda1), lda1, A2, lda2,
+                         V + IDX(0, i, ldv), ldv, T + IDX(0, i, ldt), ldt, work, kb);
+        } else {
+            int ni2 = imin(i + kb, n2);
+            int l = imin(kb, imax(0, ni2 - i));
+            ora_dparfb_l('R', trans, m1, kb, m2, ni2, kb, l, A1 + IDX(0, i, lda1), lda1, A2, lda2,
+                         V + IDX(0, i, ldv), ldv, T + IDX(0, i, ldt), ldt, work, m1);
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Tile QR with a binary reduction tree per panel (the TT kernels' use,    */
+/* PLASMA's tree variant).  For panel k: geqrt every tile A_ik (i >= k) and */
+/* unmqr('L','C') its row's trailing tiles; then for s = 1, 2, 4, ...:      */
+/* ttqrt(A_ik, A_{i+s,k}) for i = k, k+2s, ... and ttmqr('L','C') on        */
+/* (A_ij, A_{i+s,j}).  A ragged last row tile with fewer rows than the      */
+/* panel has columns would be a wide trapezoid after geqrt, which ttqrt     */
+/* (min(m, n) reflectors, src/ttqrt.jl:100) cannot reduce; it is instead    */
+/* merged whole into the tile above it by tsqrt/tsmqr before the tree.      */
+/* Tile A_ik keeps geqrt's reflectors below its diagonal (T_ik, tau_ik in   */
+/* T, tau) and, for i > k, the ttqrt (or merging tsqrt) reflectors in its   */
+/* upper triangle (or whole tile) with T2_ik, tau2_ik (same layouts).       */
+/* ------------------------------------------------------------------------ */
+static int tree_ragged(int m, int nb, int MT, int k, int nk)
+{
+    int p = MT - 1;
+    return p > k && imin(nb, m - p * nb) < nk;
+}
+
+int ora_dtile_geqrf_tree(int m, int n, int nb, int ib, double *A, int lda, double *T, int ldt,
+                         double *tau, int ldtau, double *T2, double *tau2)
+{
+    if (m < 0) return -1;
+    if (n < 0) return -2;
+    if (nb <= 0) return -3;
+    if (ib <= 0 || ib > nb) return -4;
+    if (m == 0 || n == 0) return 0;
+    int MT = (m + nb - 1) / nb, NT = (n + nb - 1) / nb, KT = imin(MT, NT);
+    if (lda < m) return -6;
+    if (ldt < MT * ib) return -8;
+    if (ldtau < n) return -10;
+    for (int k = 0; k < KT; ++k) {
+        int nk = imin(nb, n - k * nb);
+        int rag = tree_ragged(m, nb, MT, k, nk);
+        int MTt = rag ? MT - 1 : MT;             /* tiles the tree reduces */
+#pragma omp parallel for schedule(dynamic)
+        for (int i = k; i < MTt; ++i) {
+            int mi = imin(nb, m - i * nb), kk = imin(mi, nk);
+            double *w = (double *)malloc(sizeof(double) * (size_t)nb * (size_t)nb);
+            double *tv = (double *)malloc(sizeof(double) * (size_t)nb);
+            double *Aik = A + IDX(i * nb, k * nb, lda);
+            double *Tik = T + IDX(i * ib, k * nb, ldt);
+            ora_dgeqrt(mi, nk, ib, Aik, lda, Tik, ldt, tv, w);
+            for (int c = 0; c < kk; ++c) tau[IDX(k * nb + c, i, ldtau)] = tv[c];
+            for (int j = k + 1; j < NT; ++j) {
+                int nj = imin(nb, n - j * nb);
+                ora_dunmqr('L', 'C', mi, nj, kk, ib, Aik, lda, mi, nk, Tik, ldt,
+                           A + IDX(i * nb, j * nb, lda), lda, w, nj);
+            }
+            free(w);
+            free(tv);
+        }
+        if (rag) {
+            int p = MT - 1, q = p - 1, mp = imin(nb, m - p * nb);
+            double *w = (double *)malloc(sizeof(double) * (size_t)nb * (size_t)nb);
+            double *tv = (double *)malloc(sizeof(double) * (size_t)nb);
+            double *Apk = A + IDX(p * nb, k * nb, lda);
+            double *T2p = T2 + IDX(p * ib, k * nb, ldt);
+            ora_dtsqrt(mp, nk, ib, nb, A + IDX(q * nb, k * nb, lda), lda, Apk, lda, T2p, ldt, tv, w);
+            for (int c = 0; c < nk; ++c) tau2[IDX(k * nb + c, p, ldtau)] = tv[c];
+#pragma omp parallel for schedule(dynamic)
+            for (int j = k + 1; j < NT; ++j) {
+                int nj = imin(nb, n - j * nb);
+                double *wj = (double *)malloc(sizeof(double) * (size_t)nb * (size_t)nb);
+                ora_dtsmqr('L', 'C', nb, nj, mp, nj, nk, ib, nk, A + IDX(q * nb, j * nb, lda), lda,
+                           A + IDX(p * nb, j * nb, lda), lda, Apk, lda, T2p, ldt, wj);
+                free(wj);
+            }
+            free(w);
+            free(tv);
+        }
+        for (int s = 1; k + s < MTt; s *= 2) {
+#pragma omp parallel for schedule(dynamic)
+            for (int i = k; i < MTt - s; i += 2 * s) {
+                int p = i + s;
+                int mp = imin(nb, m - p * nb), kt = imin(mp, nk);
+                double *w = (double *)malloc(sizeof(double) * (size_t)nb * (size_t)nb);
+                double *tv = (double *)malloc(sizeof(double) * (size_t)nb);
+                double *Apk = A + IDX(p * nb, k * nb, lda);
+                double *T2p = T2 + IDX(p * ib, k * nb, ldt);
+                ora_dttqrt(mp, nk, ib, A + IDX(i * nb, k * nb, lda), lda, Apk, lda, T2p, ldt, tv, w);
+                for (int c = 0; c < kt; ++c) tau2[IDX(k * nb + c, p, ldtau)] = tv[c];
+                for (int j = k + 1; j < NT; ++j) {
+                    int nj = imin(nb, n - j * nb);
+                    ora_dttmqr('L', 'C', nb, nj, mp, nj, kt, ib, A + IDX(i * nb, j * nb, lda), lda,
+                               A + IDX(p * nb, j * nb, lda), lda, Apk, lda, T2p, ldt, w);
+                }
+                free(w);
+                free(tv);
+            }
+        }
+    }
+    return 0;
+}
+
+/* B := Q^T B (trans 'C'/'T') or Q B ('N') for Q of ora_dtile_geqrf_tree.   */
+int ora_dtile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, const double *A,
+                         int lda, const double *T, int ldt, const double *T2, double *B, int ldb)
+{
+    if (trans != 'N' && trans != 'C' && trans != 'T') return -1;
+    if (m < 0) return -2;
+    if (n < 0) return -3;
+    if (nrhs < 0) return -4;
+    if (nb <= 0) return -5;
+    if (ib <= 0 || ib > nb) return -6;
+    if (m == 0 || n == 0 || nrhs == 0) return 0;
+    int MT = (m + nb - 1) / nb, NT = (n + nb - 1) / nb, KT = imin(MT, NT);
+    double *work = (double *)malloc(sizeof(double) * (size_t)nrhs * (size_t)nb);
+    if (!work) return -100;
+    const int tr = (trans != 'N');
+    for (int kx = 0; kx < KT; ++kx) {
+        int k = tr ? kx : KT - 1 - kx;
+        int nk = imin(nb, n - k * nb);
+        int rag = tree_ragged(m, nb, MT, k, nk);
+        int MTt = rag ? MT - 1 : MT;
+        int smax = 1;
+        while (k + smax < MTt) smax *= 2;
+        int p = MT - 1, q = p - 1, mp = imin(nb, m - p * nb);
+        if (tr) {
+            for (int i = k; i < MTt; ++i) {
+                int mi = imin(nb, m - i * nb);
+                ora_dunmqr('L', 'C', mi, nrhs, imin(mi, nk), ib, A + IDX(i * nb, k * nb, lda), lda, mi,
+                           nk, T + IDX(i * ib, k * nb, ldt), ldt, B + IDX(i * nb, 0, ldb), ldb, work, nrhs);
+            }
+            if (rag)
+                ora_dtsmqr('L', 'C', nb, nrhs, mp, nrhs, nk, ib, nk, B + IDX(q * nb, 0, ldb), ldb,
+                           B + IDX(p * nb, 0, ldb), ldb, A + IDX(p * nb, k * nb, lda), lda,
+                           T2 + IDX(p * ib, k * nb, ldt), ldt, work);
+            for (int s = 1; k + s < MTt; s *= 2)
+                for (int i = k; i < MTt - s; i += 2 * s) {
+                    int pp = i + s, mpp = imin(nb, m - pp * nb);
+                    ora_dttmqr('L', 'C', nb, nrhs, mpp, nrhs, imin(mpp, nk), ib, B + IDX(i * nb, 0, ldb),
+                               ldb, B + IDX(pp * nb, 0, ldb), ldb, A + IDX(pp * nb, k * nb, lda), lda,
+                               T2 + IDX(pp * ib, k * nb, ldt), ldt, work);
+                }
+        } else {
+            for (int s = smax / 2; s >= 1; s /= 2)
+                for (int i = k; i < MTt - s; i += 2 * s) {
+                    int pp = i + s, mpp = imin(nb, m - pp * nb);
+                    ora_dttmqr('L', 'N', nb, nrhs, mpp, nrhs, imin(mpp, nk), ib, B + IDX(i * nb, 0, ldb),
+                               ldb, B + IDX(pp * nb, 0, ldb), ldb, A + IDX(pp * nb, k * nb, lda), lda,
+                               T2 + IDX(pp * ib, k * nb, ldt), ldt, work);
+                }
+            if (rag)
+                ora_dtsmqr('L', 'N', nb, nrhs, mp, nrhs, nk, ib, nk, B + IDX(q * nb, 0, ldb), ldb,
+                           B + IDX(p * nb, 0, ldb), ldb, A + IDX(p * nb, k * nb, lda), lda,
+                           T2 + IDX(p * ib, k * nb, ldt), ldt, work);
+            for (int i = k; i < MTt; ++i) {
+                int mi = imin(nb, m - i * nb);
+                ora_dunmqr('L', 'N', mi, nrhs, imin(mi, nk), ib, A + IDX(i * nb, k * nb, lda), lda, mi,
+                           nk, T + IDX(i * ib, k * nb, ldt), ldt, B + IDX(i * nb, 0, ldb), ldb, work, nrhs);
+            }
+        }
+    }
+    free(work);
     return 0;
 }

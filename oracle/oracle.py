@@ -61,6 +61,11 @@ def _declare(L):
         "ora_dtile_geqrf": [_I, _I, _I, _I, _P, _I, _P, _I, _P, _I],
         "ora_dtile_unmqr": [_C, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I],
         "ora_dtrsm_lun": [_I, _I, _P, _I, _P, _I],
+        "ora_dparfb_l": [_C, _C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, _I],
+        "ora_dttqrt": [_I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _P],
+        "ora_dttmqr": [_C, _C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
+        "ora_dtile_geqrf_tree": [_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _P],
+        "ora_dtile_unmqr_tree": [_C, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _P, _I],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -197,6 +202,56 @@ def trsm_lun(R, B):
     pr, ldr = _mat(R)
     pb, ldb = _mat(B)
     return _check(lib().ora_dtrsm_lun(R.shape[1], B.shape[1], pr, ldr, pb, ldb), "trsm")
+
+
+def parfb_l(side, trans, m1, n1, m2, n2, k, l, A1, A2, V, T, work):
+    p1, ld1 = _mat(A1)
+    p2, ld2 = _mat(A2)
+    pv, ldv = _mat(V)
+    pt, ldt = _mat(T)
+    pw, ldw = _mat(work)
+    return _check(lib().ora_dparfb_l(_ch(side), _ch(trans), m1, n1, m2, n2, k, l, p1, ld1, p2, ld2,
+                                     pv, ldv, pt, ldt, pw, ldw), "parfb")
+
+
+def ttqrt(m, n, ib, A1, A2, T, tau, work):
+    p1, ld1 = _mat(A1)
+    p2, ld2 = _mat(A2)
+    pt, ldt = _mat(T)
+    return _check(lib().ora_dttqrt(m, n, ib, p1, ld1, p2, ld2, pt, ldt, _mat(tau)[0],
+                                   _mat(work)[0]), "ttqrt")
+
+
+def ttmqr(side, trans, m1, n1, m2, n2, k, ib, A1, A2, V, T, work):
+    p1, ld1 = _mat(A1)
+    p2, ld2 = _mat(A2)
+    pv, ldv = _mat(V)
+    pt, ldt = _mat(T)
+    return _check(lib().ora_dttmqr(_ch(side), _ch(trans), m1, n1, m2, n2, k, ib, p1, ld1, p2, ld2,
+                                   pv, ldv, pt, ldt, _mat(work)[0]), "ttmqr")
+
+
+def tile_geqrf_tree(A, nb, ib):
+    """Tile QR with a binary reduction tree per panel, in place; returns
+    (T, tau, T2, tau2): geqrt's factors of every tile and the ttqrt ones."""
+    m, n = A.shape
+    MT = (m + nb - 1) // nb
+    T = np.zeros((MT * ib, n), order="F")
+    T2 = np.zeros((MT * ib, n), order="F")
+    tau = np.zeros((n, MT), order="F")
+    tau2 = np.zeros((n, MT), order="F")
+    pa, lda = _mat(A)
+    _check(lib().ora_dtile_geqrf_tree(m, n, nb, ib, pa, lda, T.ctypes.data, MT * ib, tau.ctypes.data, n,
+                                      T2.ctypes.data, tau2.ctypes.data), "tile_geqrf_tree")
+    return T, tau, T2, tau2
+
+
+def tile_unmqr_tree(trans, A, T, T2, B, nb, ib):
+    m, n = A.shape
+    pa, lda = _mat(A)
+    pb, ldb = _mat(B)
+    return _check(lib().ora_dtile_unmqr_tree(_ch(trans), m, n, B.shape[1], nb, ib, pa, lda, T.ctypes.data,
+                                             T.shape[0], T2.ctypes.data, pb, ldb), "tile_unmqr_tree")
 
 
 def tile_lstsq(A, B, nb, ib):

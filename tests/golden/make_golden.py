@@ -105,6 +105,47 @@ def main():
         alpha, xo, tau = lapack.dlarfg(n, x[0], x[1:].copy())
         g[f"larfg_{n}_x"] = x
         g[f"larfg_{n}_out"] = np.concatenate([[alpha], xo, [tau]])
+    # ttqrt (test/ttqrt.jl:6-11 shapes, A1, A2 = triu(randn) + 2I) vs dtpqrt(l = n, nb = ib);
+    # appended after the vectors above so their random streams are unchanged.
+    for (n, ib) in [(16, 4), (24, 8), (32, 8), (48, 16), (256, 32)]:
+        A1 = Q24(np.triu(rng.standard_normal((n, n))) + 2.0 * np.eye(n))
+        A2 = Q24(np.triu(rng.standard_normal((n, n))) + 2.0 * np.eye(n))
+        a1, a2, t, info = lapack.dtpqrt(n, ib, A1.copy(order="F"), A2.copy(order="F"))
+        assert info == 0
+        key = f"ttqrt_{n}_{ib}"
+        g[key + "_A1"], g[key + "_A2"] = A1, A2
+        g[key + "_outA1"], g[key + "_outA2"], g[key + "_outT"] = F(a1), F(a2), F(t)
+        # the Q of that factorisation applied to a random pair (ttmqr 'L', both
+        # trans) vs dtpmqrt(l = n)
+        for trans in "NC":
+            C1 = Q24(rng.standard_normal((n, 40)))
+            C2 = Q24(rng.standard_normal((n, 40)))
+            c1, c2, info = lapack.dtpmqrt(n, F(a2), F(t), C1.copy(order="F"), C2.copy(order="F"),
+                                          side="L", trans="T" if trans == "C" else "N")
+            assert info == 0
+            g[f"{key}_L{trans}_C1"], g[f"{key}_L{trans}_C2"] = C1, C2
+            g[f"{key}_L{trans}_out1"], g[f"{key}_L{trans}_out2"] = F(c1), F(c2)
+    # ttmqr (test/ttmqr.jl:6-37: n = 24, k = 16, ib = 8, V = triu(randn(n, k)),
+    # T = triu(rand(ib, k))) vs dtpmqrt(l = 0), all four side x trans forms.
+    for side in "LR":
+        for trans in "NC":
+            n, k, ib = 24, 16, 8
+            A1 = F(rng.standard_normal((n, n)))
+            A2 = F(rng.standard_normal((n, n)))
+            V = F(np.triu(rng.standard_normal((n, k))))
+            T = F(np.triu(rng.random((ib, k))))
+            out1 = A1.copy(order="F")
+            sub = out1[:k] if side == "L" else out1[:, :k]
+            a1, a2, info = lapack.dtpmqrt(0, V, T, F(sub), A2.copy(order="F"), side=side,
+                                          trans="T" if trans == "C" else "N")
+            assert info == 0
+            if side == "L":
+                out1[:k] = a1
+            else:
+                out1[:, :k] = a1
+            key = f"ttmqr_{side}{trans}"
+            g[key + "_A1"], g[key + "_A2"], g[key + "_V"], g[key + "_T"] = A1, A2, V, T
+            g[key + "_outA1"], g[key + "_outA2"] = F(out1), F(a2)
     np.savez_compressed(OUT, **g)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")
 
