@@ -57,6 +57,8 @@ def parse():
     p.add_argument("--batched-n", type=int, default=4096, help="problems per batch")
     p.add_argument("--no-adjoint", action="store_true", help="skip the differentiable QR")
     p.add_argument("--adjoint-only", action="store_true", help="run only the differentiable QR")
+    p.add_argument("--no-tall", action="store_true", help="skip the tall-skinny flat vs tree comparison")
+    p.add_argument("--tall-only", action="store_true", help="run only the tall-skinny flat vs tree comparison")
     return p.parse_args()
 
 
@@ -435,6 +437,43 @@ def batched_bench(torch, nprob=4096, steps=5, warmup=3, peak=None):
     return out
 
 
+def tall_bench(tq, torch, m=65536, n=512, steps=3, warmup=2, peak=None, dtype="f64"):
+    """Tall-skinny tile QR (m x n, N(0,1), nb = 256, ib = 32): the flat-tree
+    persistent kernel against the binary-tree driver (geqrt on every tile,
+    ttqrt/ttmqr merges), flops 2mn^2 - 2n^3/3 per factorisation."""
+    dt = torch.float64 if dtype == "f64" else torch.float32
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    A0 = tq.empty(m, n, dtype=dt)
+    A0.copy_(torch.randn(m, n, generator=g, dtype=torch.float64, device="cuda"))
+    A = tq.empty(m, n, dtype=dt)
+    st = torch.cuda.current_stream()
+    flops = 2.0 * m * n * n - 2.0 * n ** 3 / 3
+
+    def timed(fn):
+        ts = []
+        for rep in range(warmup + steps):
+            A.copy_(A0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fn()
+            e1.record(st)
+            torch.cuda.synchronize()
+            if rep >= warmup:
+                ts.append(e0.elapsed_time(e1))
+        return min(ts)
+
+    t_flat = timed(lambda: tq.tile_geqrf(A, NB, IB))
+    t_tree = timed(lambda: tq.tile_geqrf_tree(A, NB, IB))
+    out = {"workload": f"tall-skinny tile QR {m}x{n} {dtype} N(0,1), nb={NB}, ib={IB}",
+           "flops": flops, "flat_dag_ms": t_flat, "tree_ms": t_tree,
+           "flat_dag_tflops": flops / t_flat / 1e9, "tree_tflops": flops / t_tree / 1e9,
+           "speedup_tree_vs_flat": t_flat / t_tree}
+    if peak and dtype == "f64":
+        out["tree_frac_of_fp64_simt_peak"] = flops / t_tree / 1e9 / peak
+    return out
+
+
 def adjoint_bench(torch, batch=256, m=2048, n=256, steps=3, warmup=3, peak=None):
     """Differentiable QR: (Q, R) = qr(A) for a batch of 256 Float64 2048x256
     N(0,1) matrices, loss 1/2||R^-1 Q^T b - y||^2 + <dQ, Q> + <dR, R> with
@@ -578,6 +617,18 @@ def main():
         tq.set_blocking(False)
         res = ls_bench(tq, torch, args.ls_m, args.ls_n, 4, max(1, args.steps), max(1, args.warmup),
                        orth=not args.ls_no_orth)
+        print(json.dumps(res), flush=True)
+        return 0
+    if args.tall_only:
+        import torch
+
+        import tileqr as tq
+        import tileqr_build
+        from tileqr import _lib
+        tileqr_build.build()
+        tq.set_blocking(False)
+        peak = fp64_peak(_lib, torch)
+        res = {"f64": tall_bench(tq, torch, peak=peak), "f32": tall_bench(tq, torch, dtype="f32")}
         print(json.dumps(res), flush=True)
         return 0
     if args.adjoint_only:
@@ -734,6 +785,10 @@ def main():
     if rank == 0 and world == 1 and not args.no_batched:
         bat = batched_bench(torch, args.batched_n, 5, 3, peak=peak)
 
+    tall = None
+    if rank == 0 and world == 1 and not args.no_tall:
+        tall = tall_bench(tq, torch, peak=peak)
+
     adj = None
     if rank == 0 and world == 1 and not args.no_adjoint:
         adj = adjoint_bench(torch, 256, 2048, 256, 3, 3, peak=peak)
@@ -750,6 +805,7 @@ def main():
             "least_squares_mixed_vs_fp64": ls,
             "batched_uneven_gels": bat,
             "differentiable_qr": adj,
+            "tall_skinny_65536x512": tall,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

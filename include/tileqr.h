@@ -86,15 +86,40 @@ int tqr_stsmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int
                float *work, int lwork, cudaStream_t stream);
 
 /* parfb!(side, trans, direct, storev, m1, n1, m2, n2, k, l, A1, A2, V, T, work)
- * -- src/parfb.jl:44-191 with pamm! (src/pamm.jl:49-473).  Implemented for the
- * pentagonal form tsmqr uses: l = 0, direct 'F', storev 'C' (other values of
- * those three arguments return -10, -3, -4). */
+ * -- src/parfb.jl:44-191 with pamm! (src/pamm.jl:49-473).  Implemented for
+ * forward, columnwise reflectors (direct 'B' returns -3, storev 'R' -4) with
+ * any triangular order 0 <= l <= k: V's first l columns hold, over the last
+ * l of the m2 (side 'R': n2) rows, only an upper triangle, whose strictly
+ * lower part is not read. */
 int tqr_dparfb(char side, char trans, char direct, char storev, int m1, int n1, int m2, int n2,
                int k, int l, double *A1, int lda1, double *A2, int lda2, const double *V, int ldv,
                const double *T, int ldt, double *work, int ldwork, cudaStream_t stream);
 int tqr_sparfb(char side, char trans, char direct, char storev, int m1, int n1, int m2, int n2,
                int k, int l, float *A1, int lda1, float *A2, int lda2, const float *V, int ldv,
                const float *T, int ldt, float *work, int ldwork, cudaStream_t stream);
+
+/* ttqrt!(m, n, ib, A1, A2, T, tau, work) -- src/ttqrt.jl:81-119.
+ * QR of [A1 (upper triangular); A2 (upper triangular, m-by-n)], k = min(m, n)
+ * reflectors; column r's reflector occupies A2 rows [0, min(r + 1, m)).
+ * Reads and writes only the upper triangle of A2 (LAPACK dtpqrt with l = n);
+ * the reference's T recursion (src/ttqrt.jl:66-71) also sums A2 entries
+ * below the diagonal, which are zero on upper-triangular input.  A zero
+ * column leaves tau = 0 and its T column untouched, as the reference does. */
+int tqr_dttqrt(int m, int n, int ib, double *A1, int lda1, double *A2, int lda2, double *T, int ldt,
+               double *tau, double *work, cudaStream_t stream);
+int tqr_sttqrt(int m, int n, int ib, float *A1, int lda1, float *A2, int lda2, float *T, int ldt,
+               float *tau, float *work, cudaStream_t stream);
+
+/* ttmqr!(side, trans, m1, n1, m2, n2, k, ib, A1, A2, V, T, work) -- src/ttmqr.jl:1-95.
+ * As tsmqr! with the reflectors of ttqrt!: reflector q of V holds rows
+ * (side 'R': columns) [0, q] of A2's space, so block i touches A2 rows
+ * [0, min(i + kb, m2)).  k is clamped to m1 ('L') or n1 ('R'). */
+int tqr_dttmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, double *A1,
+               int lda1, double *A2, int lda2, const double *V, int ldv, const double *T, int ldt,
+               double *work, int lwork, cudaStream_t stream);
+int tqr_sttmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, float *A1,
+               int lda1, float *A2, int lda2, const float *V, int ldv, const float *T, int ldt,
+               float *work, int lwork, cudaStream_t stream);
 
 /* ---- Tile QR built from the kernels above (no counterpart in NextLA, which
  * ships only the tile kernels; the composition is the flat-tree order its
@@ -163,6 +188,29 @@ int tqr_stile_gels_dag(int m, int n, int nrhs, int nb, int ib, float *A, int lda
 #define TQR_ERR_SCRATCH_TOO_SMALL (-1000)
 int tqr_dtile_geqrf_noalloc(int m, int n, int nb, int ib, double *A, int lda, double *T, int ldt,
                             double *tau, int ldtau, cudaStream_t stream);
+
+/* Tile QR with a binary reduction tree per panel (no counterpart in NextLA;
+ * the composition its TT kernels exist for).  Panel k: geqrt! on every tile
+ * (i, k), i >= k, and unmqr! on its row's trailing tiles; then ttqrt!/ttmqr!
+ * merge tile pairs at distance 1, 2, 4, ... (a last row tile shorter than the
+ * panel is wide is first merged whole into the tile above by tsqrt!/tsmqr!).
+ * The serial chain per panel is 1 + ceil(log2(MT - k)) tile steps instead of
+ * MT - k.  T, T2 are (MT*ib)-by-n, ldt >= MT*ib (T2 is zeroed by the call);
+ * tau, tau2 n-by-MT, ldtau >= n: geqrt's factors of tile (i,k) in T/tau at
+ * rows i*ib / column i, the merge factors of tile (i,k), i > k, in T2/tau2.
+ * nrhs > 0: B (m-by-nrhs) is overwritten by Q^T B.  nb <= 256, ib <= 32. */
+int tqr_dtile_geqrf_tree(int m, int n, int nb, int ib, double *A, int lda, double *T, double *T2,
+                         int ldt, double *tau, double *tau2, int ldtau, int nrhs, double *B, int ldb,
+                         cudaStream_t stream);
+int tqr_stile_geqrf_tree(int m, int n, int nb, int ib, float *A, int lda, float *T, float *T2,
+                         int ldt, float *tau, float *tau2, int ldtau, int nrhs, float *B, int ldb,
+                         cudaStream_t stream);
+/* B := Q^T B (trans 'C'/'T') or Q B ('N') with Q from tqr_?tile_geqrf_tree. */
+int tqr_dtile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, const double *A, int lda,
+                         const double *T, const double *T2, int ldt, double *B, int ldb,
+                         cudaStream_t stream);
+int tqr_stile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, const float *A, int lda,
+                         const float *T, const float *T2, int ldt, float *B, int ldb, cudaStream_t stream);
 
 /* B (m-by-nrhs) := Q^T B (trans 'C'/'T') or Q B (trans 'N'), Q from tile_geqrf. */
 int tqr_dtile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const double *A, int lda,

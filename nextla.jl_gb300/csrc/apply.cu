@@ -72,12 +72,13 @@ static cudaError_t launch_nw(const ApplyArgs<R> &a, size_t sm, cudaStream_t st) 
 template <typename R>
 cudaError_t launch_apply(int mode, char side, char trans, int m, int n, int k, int ib,
                          R *C, int ldc, R *A1, int lda1, const R *V, int ldv,
-                         const R *T, int ldt, cudaStream_t st)
+                         const R *T, int ldt, cudaStream_t st, int tt)
 {
   if (m <= 0 || n <= 0 || k <= 0) return cudaSuccess;
   size_t sm = 0;
   ApplyArgs<R> a = make_apply_args<R>(mode, side, trans, m, n, k, ib, C, ldc, A1, lda1, V, ldv, T,
                                       ldt, &sm);
+  a.tt = (mode == 1) ? tt : -1;
   if (sm > (size_t)TQR_SMEM_MAX) return cudaErrorInvalidValue;
   switch (a.nw) {
     case 16: return launch_nw<R, 16>(a, sm, st);
@@ -88,8 +89,8 @@ cudaError_t launch_apply(int mode, char side, char trans, int m, int n, int k, i
 }
 
 template cudaError_t launch_apply<double>(int, char, char, int, int, int, int, double *, int, double *, int,
-                                          const double *, int, const double *, int, cudaStream_t);
+                                          const double *, int, const double *, int, cudaStream_t, int);
 template cudaError_t launch_apply<float>(int, char, char, int, int, int, int, float *, int, float *, int,
-                                         const float *, int, const float *, int, cudaStream_t);
+                                         const float *, int, const float *, int, cudaStream_t, int);
 
 }  // namespace tqr

@@ -46,6 +46,10 @@ struct ApplyArgs {
   int ldt;
   int nw;        // strip width (the template argument of apply_strip)
   int stage_c, stage_v, stage_t;
+  int tt = -1;   // mode 1 only, >= 0: reflector q of V (q = 0..k-1) holds rows
+                 // [0, tt + q] only (ttmqr!/parfb! with a triangular part,
+                 // src/ttmqr.jl:60-90, src/pamm.jl:104-127); rows below are
+                 // never read and region rows past tt + q are not touched
 };
 
 template <typename R>
@@ -112,7 +116,9 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
     const int i = a.fwd ? b * ib : (nblk - 1 - b) * ib;
     const int kb = min(ib, a.k - i);
     const int r0 = (a.mode == 0) ? i : 0;       // first region row this block touches
-    const int Lr = L - r0;
+    const bool ttb = (a.mode == 1 && a.tt >= 0);
+    const int Lr = ttb ? min(L, a.tt + i + kb) : L - r0;
+    auto vrows = [&](int p) { return ttb ? min(Lr, a.tt + i + p + 1) : Lr; };   // valid rows of column p
     // V block: element (rr, p) = reflector i+p at region row r0+rr
     const R *Vp;
     int ldvp;
@@ -123,7 +129,7 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
         if (a.mode == 0)
           v = (rr < p) ? R(0) : (rr == p ? R(1) : ldg_cg(a.V + ix(r0 + rr, i + p, a.ldv)));
         else
-          v = ldg_cg(a.V + ix(rr, i + p, a.ldv));
+          v = (rr < vrows(p)) ? ldg_cg(a.V + ix(rr, i + p, a.ldv)) : R(0);
         Vs[rr + (size_t)p * ldvs] = v;
       }
       Vp = Vs; ldvp = ldvs;
@@ -146,18 +152,20 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
     // Phase 1: W[p, c] = (A1 or C1 row) + sum_rr V[rr, p] * C[r0 + rr, c]
     // (mode 0 needs the unit-lower test only when V is read from global).
     const bool vtri = (a.mode == 0) && !a.stage_v;
+    const bool vtt = ttb && !a.stage_v;          // unstaged TT V: bound each column's rows
     for (int e = tid; e < kb * nwl; e += TQR_THREADS) {
       const int p = e % kb, c = e / kb;
       R acc0 = 0, acc1 = 0;
       const R *vcol = Vp + (size_t)p * ldvp;
       const R *ccol = Cp + (size_t)r0 * crs + (size_t)c * ccs;
+      const int Lp = vtt ? vrows(p) : Lr;
       int rr = vtri ? p : 0;
       if (vtri) { acc0 = ccol[(size_t)p * crs]; ++rr; }
-      for (; rr + 1 < Lr; rr += 2) {
+      for (; rr + 1 < Lp; rr += 2) {
         acc0 = fma(vcol[rr], ccol[(size_t)rr * crs], acc0);
         acc1 = fma(vcol[rr + 1], ccol[(size_t)(rr + 1) * crs], acc1);
       }
-      if (rr < Lr) acc0 = fma(vcol[rr], ccol[(size_t)rr * crs], acc0);
+      if (rr < Lp) acc0 = fma(vcol[rr], ccol[(size_t)rr * crs], acc0);
       R w = acc0 + acc1;
       if (a.mode == 1) w += ldg_cg(A1g + (size_t)(i + p) * a.a_rs + (size_t)c * a.a_cs);
       Ws[p + c * ldw] = w;
@@ -220,7 +228,8 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
 #pragma unroll
         for (int c = 0; c < NW; ++c) acc[c] = 0;
         const int pmax = vtri ? min(kb, rr + 1) : kb;
-        for (int p = 0; p < pmax; ++p) {
+        const int pmin = vtt ? max(0, rr - a.tt - i) : 0;
+        for (int p = pmin; p < pmax; ++p) {
           R v = Vp[rr + (size_t)p * ldvp];
           if (vtri && p == rr) v = R(1);
           const R *wrow = Wf + p;
@@ -237,7 +246,8 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
 #pragma unroll
         for (int c = 0; c < NW; ++c) acc[c] = 0;
         const int pmax = vtri ? min(kb, rr + 1) : kb;
-        for (int p = 0; p < pmax; ++p) {
+        const int pmin = vtt ? max(0, rr - a.tt - i) : 0;
+        for (int p = pmin; p < pmax; ++p) {
           R v = Vp[rr + (size_t)p * ldvp];
           if (vtri && p == rr) v = R(1);
           const R *wrow = Wf + p;

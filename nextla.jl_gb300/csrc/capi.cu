@@ -139,12 +139,65 @@ int parfb_impl(char side, char trans, char direct, char storev, int m1, int n1, 
   if (l < 0 || l > k) return -10;
   if (m1 == 0 || n1 == 0 || n2 == 0 || k == 0) return 0;
   if (m2 == 0) return 0;
-  // This library implements the pentagonal case l = 0 with forward,
-  // columnwise reflectors, the form tsmqr uses.
+  // Forward, columnwise reflectors (the forms tsmqr! and ttmqr! use).  A
+  // triangular part of order l makes reflector q hold rows (columns for
+  // side R) [0, mv - l + q] of V, mv = m2 (n2): pamm's trapezoid
+  // (src/pamm.jl:104-127, 153-175).
   if (direct != 'F') return -3;
   if (storev != 'C') return -4;
-  if (l != 0) return -10;
-  return rc(launch_apply<R>(1, side, trans, m2, n2, k, k, A2, lda2, A1, lda1, V, ldv, T, ldt, st));
+  const int mv = side == 'L' ? m2 : n2;
+  return rc(launch_apply<R>(1, side, trans, m2, n2, k, k, A2, lda2, A1, lda1, V, ldv, T, ldt, st,
+                            l > 0 ? mv - l : -1));
+}
+
+template <typename R>
+int ttmqr_impl(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, R *A1,
+               int lda1, R *A2, int lda2, const R *V, int ldv, const R *T, int ldt, cudaStream_t st) {
+  if (!is_side(side)) return -1;             // src/ttmqr.jl:3-37
+  if (!is_trans(trans)) return -2;
+  if (m1 < 0) return -3;
+  if (n1 < 0) return -4;
+  if (m2 < 0 || (m2 != m1 && side == 'R')) return -5;
+  if (n2 < 0 || (n2 != n1 && side == 'L')) return -6;
+  if (k < 0) return -7;
+  const int kmax = side == 'L' ? m1 : n1;
+  if (k > kmax) k = kmax;
+  if (ib < 0) return -8;
+  if (m1 == 0 || n1 == 0 || m2 == 0 || n2 == 0 || k == 0 || ib == 0) return 0;
+  if (lda1 < m1) return -10;
+  if (lda2 < m2) return -12;
+  if (ldv < (side == 'L' ? m2 : n2)) return -14;
+  if (ldt < (ib < k ? ib : k)) return -16;
+  // block i touches A2 rows (columns) [0, min(i + kb, m2)), reflector q of V
+  // rows [0, q]: the apply's triangular form with offset 0
+  return rc(launch_apply<R>(1, side, trans, m2, n2, k, ib, A2, lda2, A1, lda1, V, ldv, T, ldt, st, 0));
+}
+
+template <typename R>
+int ttqrt_impl(int m, int n, int ib, R *A1, int lda1, R *A2, int lda2, R *T, int ldt, R *tau,
+               cudaStream_t st) {
+  if (m < 0) return -1;                      // src/ttqrt.jl:86-101
+  if (n < 0) return -2;
+  if (ib < 0) return -3;
+  if (m == 0 || n == 0 || ib == 0) return 0;
+  const int k = m < n ? m : n;
+  if (lda1 < k) return -5;
+  if (lda2 < m) return -7;
+  if (ldt < (ib < k ? ib : k)) return -9;
+  for (int ii = 0; ii < k; ii += ib) {       // src/ttqrt.jl:102-117
+    const int sb = (k - ii) < ib ? (k - ii) : ib;
+    cudaError_t e = launch_tsqrt_block<R>(m, sb, A1 + ix(ii, ii, lda1), lda1, A2 + ix(0, ii, lda2),
+                                          lda2, T + ix(0, ii, ldt), ldt, tau + ii, st, ii);
+    if (e != cudaSuccess) return rc(e);
+    if (n > ii + sb) {
+      const int mi = (ii + sb) < m ? (ii + sb) : m;
+      e = launch_apply<R>(1, 'L', 'C', mi, n - ii - sb, sb, ib, A2 + ix(0, ii + sb, lda2), lda2,
+                          A1 + ix(ii, ii + sb, lda1), lda1, A2 + ix(0, ii, lda2), lda2,
+                          T + ix(0, ii, ldt), ldt, st, ii);
+      if (e != cudaSuccess) return rc(e);
+    }
+  }
+  return 0;
 }
 
 template <typename R>
@@ -213,6 +266,18 @@ extern "C" {
                      int lwork, cudaStream_t stream) {                                               \
     (void)work; (void)lwork;                                                                         \
     return tsmqr_impl<R>(side, trans, m1, n1, m2, n2, k, ib, A1, lda1, A2, lda2, V, ldv, T, ldt,     \
+                         stream);                                                                    \
+  }                                                                                                  \
+  int tqr_##P##ttqrt(int m, int n, int ib, R *A1, int lda1, R *A2, int lda2, R *T, int ldt, R *tau, \
+                     R *work, cudaStream_t stream) {                                                 \
+    (void)work;                                                                                      \
+    return ttqrt_impl<R>(m, n, ib, A1, lda1, A2, lda2, T, ldt, tau, stream);                         \
+  }                                                                                                  \
+  int tqr_##P##ttmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, R *A1,    \
+                     int lda1, R *A2, int lda2, const R *V, int ldv, const R *T, int ldt, R *work,   \
+                     int lwork, cudaStream_t stream) {                                               \
+    (void)work; (void)lwork;                                                                         \
+    return ttmqr_impl<R>(side, trans, m1, n1, m2, n2, k, ib, A1, lda1, A2, lda2, V, ldv, T, ldt,     \
                          stream);                                                                    \
   }                                                                                                  \
   int tqr_##P##parfb(char side, char trans, char direct, char storev, int m1, int n1, int m2,        \

@@ -24,10 +24,10 @@ k_panel_qr(int m, int nc, R *__restrict__ A, int lda, R *__restrict__ tau,
 template <typename R>
 __global__ void __launch_bounds__(TQR_THREADS)
 k_tsqrt_block(int m, int sb, R *__restrict__ A1, int lda1, R *__restrict__ A2, int lda2,
-              R *__restrict__ T, int ldt, R *__restrict__ tau, int staged)
+              R *__restrict__ T, int ldt, R *__restrict__ tau, int staged, int tt)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  tsqrt_block_cta<R>(m, sb, A1, lda1, A2, lda2, T, ldt, tau, staged != 0, smem_raw);
+  tsqrt_block_cta<R>(m, sb, A1, lda1, A2, lda2, T, ldt, tau, staged != 0, smem_raw, tt);
 }
 
 // ---------------------------------------------------------------------------
@@ -161,13 +161,14 @@ cudaError_t launch_panel_qr(int m, int nc, R *A, int lda, R *tau, R *T, int ldt,
 
 template <typename R>
 cudaError_t launch_tsqrt_block(int m, int sb, R *A1, int lda1, R *A2, int lda2, R *T, int ldt,
-                               R *tau, cudaStream_t st) {
-  bool staged = tsqrt_smem<R>(m, sb, true) <= (size_t)TQR_SMEM_MAX;
-  size_t sm = tsqrt_smem<R>(m, sb, staged);
+                               R *tau, cudaStream_t st, int tt) {
+  const int mrow = tt >= 0 ? (m < tt + sb ? m : tt + sb) : m;
+  bool staged = tsqrt_smem<R>(mrow, sb, true) <= (size_t)TQR_SMEM_MAX;
+  size_t sm = tsqrt_smem<R>(mrow, sb, staged);
   if (sm > (size_t)TQR_SMEM_MAX) return cudaErrorInvalidValue;
   cudaError_t e = allow_smem(k_tsqrt_block<R>, sm);
   if (e != cudaSuccess) return e;
-  k_tsqrt_block<R><<<1, TQR_THREADS, sm, st>>>(m, sb, A1, lda1, A2, lda2, T, ldt, tau, staged ? 1 : 0);
+  k_tsqrt_block<R><<<1, TQR_THREADS, sm, st>>>(m, sb, A1, lda1, A2, lda2, T, ldt, tau, staged ? 1 : 0, tt);
   count_launch();
   return cudaGetLastError();
 }
@@ -186,8 +187,8 @@ cudaError_t launch_larft(int direct_f, int storev_c, int n, int k, const R *V, i
 
 template cudaError_t launch_panel_qr<double>(int, int, double *, int, double *, double *, int, cudaStream_t);
 template cudaError_t launch_panel_qr<float>(int, int, float *, int, float *, float *, int, cudaStream_t);
-template cudaError_t launch_tsqrt_block<double>(int, int, double *, int, double *, int, double *, int, double *, cudaStream_t);
-template cudaError_t launch_tsqrt_block<float>(int, int, float *, int, float *, int, float *, int, float *, cudaStream_t);
+template cudaError_t launch_tsqrt_block<double>(int, int, double *, int, double *, int, double *, int, double *, cudaStream_t, int);
+template cudaError_t launch_tsqrt_block<float>(int, int, float *, int, float *, int, float *, int, float *, cudaStream_t, int);
 template cudaError_t launch_larft<double>(int, int, int, int, const double *, int, const double *, double *, int, cudaStream_t);
 template cudaError_t launch_larft<float>(int, int, int, int, const float *, int, const float *, float *, int, cudaStream_t);
 

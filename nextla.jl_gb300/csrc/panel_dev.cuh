@@ -41,6 +41,9 @@ struct ColumnStep {
   R *part;    // TQR_THREADS partial sums
   R *d;       // nc: -tau * (row[j] + x^T P[:, j])
   R *scal;    // 4
+  int tt = -1;  // >= 0: triangle-on-triangle form, column j of P holds rows
+                // [0, tt + j] only (NextLA src/ttqrt.jl:9); its rows below
+                // are never read
 };
 
 // One column step.  x rows are [x0, m) of P, column i.  Returns false when
@@ -95,12 +98,13 @@ __device__ bool column_step(const ColumnStep<R> &c, int i, int x0, int m, int nc
         R a0 = 0, a1 = 0;
         if (j != i) {
           const R *pc = c.P + (size_t)j * c.ldp;
+          const int mj = (c.tt >= 0 && j < i) ? min(m, c.tt + j + 1) : m;
           int r = x0 + g;
-          for (; r + G < m; r += 2 * G) {
+          for (; r + G < mj; r += 2 * G) {
             a0 = fma(pc[r], xcol[r], a0);
             a1 = fma(pc[r + G], xcol[r + G], a1);
           }
-          if (r < m) a0 = fma(pc[r], xcol[r], a0);
+          if (r < mj) a0 = fma(pc[r], xcol[r], a0);
         }
         c.part[g * nj + (j - jlo)] = a0 + a1;
       }
@@ -117,8 +121,9 @@ __device__ bool column_step(const ColumnStep<R> &c, int i, int x0, int m, int nc
       for (int j = jlo + warp; j < nc; j += TQR_WARPS) {
         if (j == i) continue;
         const R *pc = c.P + (size_t)j * c.ldp;
+        const int mj = (c.tt >= 0 && j < i) ? min(m, c.tt + j + 1) : m;
         R a = 0;
-        for (int r = x0 + lane; r < m; r += 32) a = fma(pc[r], xcol[r], a);
+        for (int r = x0 + lane; r < mj; r += 32) a = fma(pc[r], xcol[r], a);
         a = warp_sum(a);
         if (lane == 0) {
           if (j > i || (!tsqrt_form && j < i)) a += c.row[(size_t)j * c.rs];
@@ -172,6 +177,7 @@ __host__ __device__ inline size_t panel_smem(int m, int nc, bool staged, bool st
   return s;
 }
 
+// (for the ttqrt form pass m = min(m, ii + sb), the rows the block touches)
 template <typename R>
 __host__ __device__ inline size_t tsqrt_smem(int m, int sb, bool staged) {
   size_t s = rnd16(sizeof(R) * TQR_THREADS) + rnd16(sizeof(R) * sb) + rnd16(sizeof(R) * 4) +
@@ -243,10 +249,16 @@ __device__ void panel_qr_cta(int m, int nc, R *A, int lda, R *tau, R *T, int ldt
 // T at T[0, ii], tau at tau[ii].  A column whose A2 part is exactly zero gets
 // tau = 0 and leaves its T column untouched, as the reference does
 // (tsqrt.jl:61-64).
+// tt >= 0 gives the block of ttqrt instead (src/ttqrt.jl:1-80): A2 is upper
+// triangular, block column i holds rows [0, tt + i] of A2 (tt = ii), so
+// column i's reflector uses rows [0, min(tt + i + 1, m)) and nothing below
+// the diagonal is read or written.
 template <typename R>
 __device__ void tsqrt_block_cta(int m, int sb, R *A1, int lda1, R *A2, int lda2, R *T, int ldt,
-                                R *tau, bool staged, unsigned char *smem_raw)
+                                R *tau, bool staged, unsigned char *smem_raw, int tt = -1)
 {
+  const int mrow = tt >= 0 ? min(m, tt + sb) : m;     // rows of A2 the block touches
+  auto in_tri = [&](int r, int cc) { return tt < 0 || r <= tt + cc; };
   unsigned char *sp = smem_raw;
   const int tid = threadIdx.x;
   ColumnStep<R> c;
@@ -265,21 +277,22 @@ __device__ void tsqrt_block_cta(int m, int sb, R *A1, int lda1, R *A2, int lda2,
     }
   }
   if (staged) {
-    c.ldp = odd_ld(m);
+    c.ldp = odd_ld(mrow);
     c.P = carve<R>(sp, (size_t)c.ldp * sb);
-    for (int idx = tid; idx < m * sb; idx += TQR_THREADS) {
-      int r = idx % m, cc = idx / m;
-      c.P[ix(r, cc, c.ldp)] = __ldcg(A2 + ix(r, cc, lda2));
+    for (int idx = tid; idx < mrow * sb; idx += TQR_THREADS) {
+      int r = idx % mrow, cc = idx / mrow;
+      c.P[ix(r, cc, c.ldp)] = in_tri(r, cc) ? __ldcg(A2 + ix(r, cc, lda2)) : R(0);
     }
   } else {
     c.P = A2;
     c.ldp = lda2;
   }
+  c.tt = tt;
   __syncthreads();
   c.rs = ldb;
   for (int i = 0; i < sb; ++i) {
     c.row = B + i;
-    column_step<R>(c, i, 0, m, sb, true, tau + i, false);
+    column_step<R>(c, i, 0, tt >= 0 ? min(m, tt + i + 1) : m, sb, true, tau + i, false);
   }
   for (int idx = tid; idx < sb * sb; idx += TQR_THREADS) {
     int r = idx % sb, cc = idx / sb;
@@ -289,9 +302,9 @@ __device__ void tsqrt_block_cta(int m, int sb, R *A1, int lda1, R *A2, int lda2,
     }
   }
   if (staged) {
-    for (int idx = tid; idx < m * sb; idx += TQR_THREADS) {
-      int r = idx % m, cc = idx / m;
-      A2[ix(r, cc, lda2)] = c.P[ix(r, cc, c.ldp)];
+    for (int idx = tid; idx < mrow * sb; idx += TQR_THREADS) {
+      int r = idx % mrow, cc = idx / mrow;
+      if (in_tri(r, cc)) A2[ix(r, cc, lda2)] = c.P[ix(r, cc, c.ldp)];
     }
   }
   __syncthreads();

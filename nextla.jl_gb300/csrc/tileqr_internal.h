@@ -15,20 +15,23 @@ void prof_end(void *tok, cudaStream_t st, double flops);
 template <typename R>
 cudaError_t launch_panel_qr(int m, int nc, R *A, int lda, R *tau, R *T, int ldt, cudaStream_t st);
 
-// One ib-block of tsqrt (pointers already offset to the block), one CTA.
+// One ib-block of tsqrt (pointers already offset to the block), one CTA;
+// tt >= 0: the ttqrt block whose first column is column tt of the triangle.
 template <typename R>
 cudaError_t launch_tsqrt_block(int m, int sb, R *A1, int lda1, R *A2, int lda2, R *T, int ldt,
-                               R *tau, cudaStream_t st);
+                               R *tau, cudaStream_t st, int tt = -1);
 
 template <typename R>
 cudaError_t launch_larft(int direct_f, int storev_c, int n, int k, const R *V, int ldv,
                          const R *tau, R *T, int ldt, cudaStream_t st);
 
 // Block-reflector apply.  mode 0: larfb/unmqr on C (m-by-n); mode 1: tsmqr on
-// [A1; A2] (side L) or [A1 A2] (side R) with C = A2 (m-by-n).
+// [A1; A2] (side L) or [A1 A2] (side R) with C = A2 (m-by-n); mode 1 with
+// tt >= 0: reflector q of V holds rows (columns for side R) [0, tt + q] only
+// (ttmqr, parfb with a triangular part).
 template <typename R>
 cudaError_t launch_apply(int mode, char side, char trans, int m, int n, int k, int ib, R *C,
                          int ldc, R *A1, int lda1, const R *V, int ldv, const R *T, int ldt,
-                         cudaStream_t st);
+                         cudaStream_t st, int tt = -1);
 
 }  // namespace tqr

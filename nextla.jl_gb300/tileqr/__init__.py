@@ -19,7 +19,7 @@ from . import _lib
 
 __all__ = [
     "ArgumentError", "set_blocking", "empty", "zeros", "to_device", "to_numpy",
-    "geqr2", "larft", "larfb", "geqrt", "unmqr", "tsqrt", "tsmqr", "parfb",
+    "geqr2", "larft", "larfb", "geqrt", "unmqr", "tsqrt", "tsmqr", "parfb", "ttqrt", "ttmqr",
     "tile_geqrf", "tile_unmqr", "trsm_lun", "tile_gels", "tile_shapes",
 ]
 
@@ -292,6 +292,47 @@ def parfb(*args):
           m1, n1, m2, n2, k, l, p1, ld1, p2, ld2, pv, ldv, pt, ldt, None, 1)
 
 
+def ttqrt(*args):
+    """ttqrt!(m, n, ib, A1, A2, T, tau, work) | ttqrt!(A, B, T) -- src/ttqrt.jl:81-144.
+    QR of [A1; A2] with both upper triangular.  The helper returns (A1, A2, T, tau)."""
+    _arity("ttqrt", args, 8, 3)
+    if len(args) == 3:
+        A1, A2, T = args
+        m, n = A1.shape
+        if A2.shape[1] != n:
+            raise ArgumentError(f"A and B must have the same number of columns: got {n} and {A2.shape[1]}")
+        ib = T.shape[0]
+        tau = torch.zeros(min(m, n), dtype=A1.dtype, device=A1.device)
+        ttqrt(m, n, ib, A1, A2, T, tau, None)
+        return A1, A2, T, tau
+    m, n, ib, A1, A2, T, tau, work = args
+    p1, ld1 = _mat(A1)
+    p2, ld2 = _mat(A2)
+    pt, ldt = _mat(T)
+    _call(_prefix(A1, A2, T, tau), "ttqrt", m, n, ib, p1, ld1, p2, ld2, pt, ldt, _ptr(tau), None)
+
+
+def ttmqr(*args):
+    """ttmqr!(side, trans, m1, n1, m2, n2, k, ib, A1, A2, V, T, work)
+    | ttmqr!(side, trans, A1, A2, V, T) -- src/ttmqr.jl:1-134."""
+    _arity("ttmqr", args, 13, 6)
+    if len(args) == 6:
+        side, trans, A1, A2, V, T = args
+        m1, n1 = A1.shape
+        m2, n2 = A2.shape
+        ib = T.shape[0]
+        kmax = m1 if _ch(side) == b"L" else n1
+        k = min(T.shape[1], kmax, V.shape[1])      # src/ttmqr.jl:120-123
+        return ttmqr(side, trans, m1, n1, m2, n2, k, ib, A1, A2, V, T, None)
+    side, trans, m1, n1, m2, n2, k, ib, A1, A2, V, T, work = args
+    p1, ld1 = _mat(A1)
+    p2, ld2 = _mat(A2)
+    pv, ldv = _mat(V)
+    pt, ldt = _mat(T)
+    _call(_prefix(A1, A2, V, T), "ttmqr", _ch(side), _ch(trans), m1, n1, m2, n2, k, ib,
+          p1, ld1, p2, ld2, pv, ldv, pt, ldt, None, 0)
+
+
 # ---- tile QR, Q application, solve ------------------------------------------
 
 def tile_shapes(m, n, nb, ib):
@@ -403,6 +444,38 @@ def tile_geqrf(A, nb=256, ib=32, T=None, tau=None, dag=True):
         if status != 0:
             raise RuntimeError(f"tile_geqrf: schedule wait timed out at task {task} (status {status})")
     return T, tau
+
+
+def tile_geqrf_tree(A, nb=256, ib=32, B=None):
+    """Tile QR of A in place with a binary reduction tree per panel (geqrt!
+    on every tile, ttqrt!/ttmqr! merges).  Returns (T, tau, T2, tau2); with B,
+    B is overwritten by Q^T B in the same pass."""
+    m, n = A.shape
+    ts, taus = tile_shapes(m, n, nb, ib)
+    T = zeros(*ts, dtype=A.dtype, device=A.device)
+    T2 = zeros(*ts, dtype=A.dtype, device=A.device)
+    tau = zeros(*taus, dtype=A.dtype, device=A.device)
+    tau2 = zeros(*taus, dtype=A.dtype, device=A.device)
+    pa, lda = _mat(A)
+    pt, ldt = _mat(T)
+    pu, ldu = _mat(tau)
+    nrhs, pb, ldb = 0, None, 1
+    if B is not None:
+        nrhs = B.shape[1]
+        pb, ldb = _mat(B)
+    _call(_prefix(A, T, tau, B), "tile_geqrf_tree", m, n, nb, ib, pa, lda, pt, _ptr(T2), ldt, pu, _ptr(tau2),
+          ldu, nrhs, pb, ldb)
+    return T, tau, T2, tau2
+
+
+def tile_unmqr_tree(trans, A, T, T2, B, nb=256, ib=32):
+    """B := Q^T B ('C') or Q B ('N') with Q from tile_geqrf_tree."""
+    m, n = A.shape
+    pa, lda = _mat(A)
+    pt, ldt = _mat(T)
+    pb, ldb = _mat(B)
+    _call(_prefix(A, T, T2, B), "tile_unmqr_tree", _ch(trans), m, n, B.shape[1], nb, ib, pa, lda, pt,
+          _ptr(T2), ldt, pb, ldb)
 
 
 def tile_unmqr(trans, A, T, B, nb=256, ib=32):

@@ -24,10 +24,14 @@ SIGNATURES = {
     "tsqrt": [_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _P, _P],
     "tsmqr": [_C, _C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
     "parfb": [_C, _C, _C, _C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
+    "ttqrt": [_I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _P, _P],
+    "ttmqr": [_C, _C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
     "tile_geqrf": [_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P],
     "tile_unmqr": [_C, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P],
     "trsm_lun": [_I, _I, _P, _I, _P, _I, _P],
     "tile_gels": [_I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
+    "tile_geqrf_tree": [_I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P],
+    "tile_unmqr_tree": [_C, _I, _I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _I, _P],
 }
 
 # measurement hooks without a precision prefix: name -> (argtypes, restype)

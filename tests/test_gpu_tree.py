@@ -1,0 +1,95 @@
+"""Tree-reduction tile QR (geqrt! on every tile, ttqrt!/ttmqr! merges) on the
+GPU against the oracle's tree driver, which follows the same order.
+
+FP64 bar: every output (A with R and the reflectors, T, T2, tau, tau2, and Q
+applied both ways) within 1e-12 n relative of the oracle; at the tall-skinny
+benchmark size (65536 x 512) size-independent properties stand in: Q^T A = R
+through the Q application, ||A x|| = ||R x||, and |R| equal to the flat-tree
+factorisation's |R| (R is unique up to the signs of its rows).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(1024, 256, 128, 32), (1000, 300, 128, 16), (1024, 64, 32, 8), (300, 300, 128, 32),
+          (517, 130, 64, 16), (130, 130, 64, 16), (260, 129, 64, 16), (64, 200, 32, 8), (2048, 512, 256, 32),
+          (1800, 512, 256, 32)]
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.mark.parametrize("m,n,nb,ib", SHAPES)
+def test_tree_matches_oracle(tq, oracle, m, n, nb, ib):
+    import torch
+    rng = np.random.default_rng(m + 3 * n)
+    A0 = np.asfortranarray(rng.standard_normal((m, n)))
+    B0 = np.asfortranarray(rng.standard_normal((m, 5)))
+    A, B = tq.to_device(A0), tq.to_device(B0)
+    T, tau, T2, tau2 = tq.tile_geqrf_tree(A, nb, ib, B=B)
+    Ao = A0.copy(order="F")
+    To, tauo, T2o, tau2o = oracle.tile_geqrf_tree(Ao, nb, ib)
+    Bo = B0.copy(order="F")
+    oracle.tile_unmqr_tree("C", Ao, To, T2o, Bo, nb, ib)
+    tol = 1e-12 * max(n, 16)
+    assert rel(tq.to_numpy(A), Ao) < tol
+    assert rel(tq.to_numpy(T), To) < tol and rel(tq.to_numpy(T2), T2o) < tol
+    assert rel(tq.to_numpy(tau), tauo) < tol and rel(tq.to_numpy(tau2), tau2o) < tol
+    assert rel(tq.to_numpy(B), Bo) < tol
+    # Q applied both ways through the stored factors
+    for trans in "NC":
+        C0 = np.asfortranarray(rng.standard_normal((m, 19)))
+        C = tq.to_device(C0)
+        tq.tile_unmqr_tree(trans, A, T, T2, C, nb, ib)
+        Co = C0.copy(order="F")
+        oracle.tile_unmqr_tree(trans, Ao, To, T2o, Co, nb, ib)
+        assert rel(tq.to_numpy(C), Co) < tol
+    # Q^T A = [R; 0]
+    k = min(m, n)
+    QtA = tq.to_device(A0)
+    tq.tile_unmqr_tree("C", A, T, T2, QtA, nb, ib)
+    R = np.triu(tq.to_numpy(A)[:k])
+    assert np.linalg.norm(tq.to_numpy(QtA)[:k] - R) <= 1e-13 * np.linalg.norm(R) * k
+
+
+def test_tree_float(tq, oracle):
+    import torch
+    rng = np.random.default_rng(2)
+    m, n, nb, ib = 2048, 256, 256, 32
+    A0 = np.asfortranarray(rng.standard_normal((m, n)))
+    A = tq.to_device(A0, dtype=torch.float32)
+    T, tau, T2, tau2 = tq.tile_geqrf_tree(A, nb, ib)
+    Ao = np.asfortranarray(tq.to_numpy(tq.to_device(A0, dtype=torch.float32)).astype(np.float64))
+    oracle.tile_geqrf_tree(Ao, nb, ib)
+    R, Ro = np.triu(tq.to_numpy(A)[:n]).astype(np.float64), np.triu(Ao[:n])
+    assert np.linalg.norm(R - Ro) <= 1e-5 * np.linalg.norm(Ro)
+
+
+def test_tree_tall_skinny_properties(tq):
+    """65536 x 512 (the tall-skinny benchmark shape), nb = 256, ib = 32."""
+    import torch
+    m, n, nb, ib = 65536, 512, 256, 32
+    g = torch.Generator(device="cuda").manual_seed(7)
+    A0 = tq.empty(m, n)
+    A0.copy_(torch.randn(m, n, generator=g, dtype=torch.float64, device="cuda"))
+    A = tq.empty(m, n)
+    A.copy_(A0)
+    T, tau, T2, tau2 = tq.tile_geqrf_tree(A, nb, ib)
+    R = torch.triu(A[:n])
+    x = torch.randn(n, 3, generator=g, dtype=torch.float64, device="cuda")
+    ax = torch.linalg.norm(A0 @ x, dim=0)
+    rx = torch.linalg.norm(R @ x, dim=0)
+    assert ((ax - rx).abs() / ax).max().item() < 1e-13 * n
+    QtA = tq.empty(m, n)
+    QtA.copy_(A0)
+    tq.tile_unmqr_tree("C", A, T, T2, QtA, nb, ib)
+    assert (torch.linalg.norm(QtA[:n] - R) / torch.linalg.norm(R)).item() < 1e-14 * n
+    assert (torch.linalg.norm(QtA[n:]) / torch.linalg.norm(A0)).item() < 1e-14 * n
+    # |R| of the flat-tree persistent kernel
+    F = tq.empty(m, n)
+    F.copy_(A0)
+    tq.tile_geqrf(F, nb, ib)
+    Rf = torch.triu(F[:n])
+    assert (torch.linalg.norm(R.abs() - Rf.abs()) / torch.linalg.norm(Rf)).item() < 1e-12 * n
