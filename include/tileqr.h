@@ -205,6 +205,25 @@ int tqr_dtile_geqrf_tree(int m, int n, int nb, int ib, double *A, int lda, doubl
 int tqr_stile_geqrf_tree(int m, int n, int nb, int ib, float *A, int lda, float *T, float *T2,
                          int ldt, float *tau, float *tau2, int ldtau, int nrhs, float *B, int ldb,
                          cudaStream_t stream);
+/* The same tree factorisation (same arithmetic, same results) as one
+ * persistent launch over a task graph: tasks per tile / pair and 16-column
+ * strip, dependencies from the regions each task reads and writes, taken in
+ * longest-path order with bounded waits.  Needs nb and ib multiples of 16,
+ * nb <= 256, ib <= 32, nrhs <= 256.  work: 256-byte aligned,
+ * tqr_tile_tree_dag_worksize bytes (the task list, built once per shape on the
+ * host, and per-task flags); -16/-17 for an unaligned / too small work.
+ * tqr_tile_tree_dag_status: error word (0 ok, 1 a wait timed out, 2 schedule
+ * mismatch) and the task it stopped at; tqr_tile_tree_dag_check: host check
+ * that every dependency precedes its task, and the task count. */
+int tqr_tile_tree_dag_worksize(int m, int n, int nb, int ib, int nrhs, size_t *bytes);
+int tqr_tile_tree_dag_check(int m, int n, int nb, int ib, int nrhs, long long *ntasks);
+int tqr_tile_tree_dag_status(const void *work, int *error, int *item, cudaStream_t stream);
+int tqr_dtile_geqrf_tree_dag(int m, int n, int nb, int ib, double *A, int lda, double *T, double *T2,
+                             int ldt, double *tau, double *tau2, int ldtau, int nrhs, double *B, int ldb,
+                             void *work, size_t lwork, cudaStream_t stream);
+int tqr_stile_geqrf_tree_dag(int m, int n, int nb, int ib, float *A, int lda, float *T, float *T2,
+                             int ldt, float *tau, float *tau2, int ldtau, int nrhs, float *B, int ldb,
+                             void *work, size_t lwork, cudaStream_t stream);
 /* B := Q^T B (trans 'C'/'T') or Q B ('N') with Q from tqr_?tile_geqrf_tree. */
 int tqr_dtile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, const double *A, int lda,
                          const double *T, const double *T2, int ldt, double *B, int ldb,

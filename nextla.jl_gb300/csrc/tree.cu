@@ -21,6 +21,10 @@
 // ib-block panel (one CTA per tile or pair) and strip applies (one CTA per
 // 16-column strip), each a launch over all tiles or pairs of the step.
 #include <algorithm>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
 #include <vector>
 
 #include "apply_dev.cuh"
@@ -91,12 +95,12 @@ __device__ ApplyArgs<R> tree_args(int mode, int L, int k, int ib, int trans) {
   return a;
 }
 
+// One step of the tree factorisation on top tile i (and partner i + op.s for
+// the pair ops), strip y; shared by the stream driver and the persistent
+// task-graph kernel.
 template <typename R>
-__global__ void __launch_bounds__(TQR_THREADS, 2) k_tree(const TreeGeom<R> g, const TreeOp op) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int t = blockIdx.x, y = blockIdx.y;
+__device__ void tree_task(const TreeGeom<R> &g, const TreeOp &op, int i, int y, unsigned char *smem) {
   const int k = op.k, ib = g.ib, nk = g.cols(k);
-  const int i = op.i0 + t * op.istep;
   const int mi = g.rows(i);
   R *Aik = g.tile(i, k);
   switch (op.type) {
@@ -184,6 +188,12 @@ __global__ void __launch_bounds__(TQR_THREADS, 2) k_tree(const TreeGeom<R> g, co
 }
 
 template <typename R>
+__global__ void __launch_bounds__(TQR_THREADS, 2) k_tree(const TreeGeom<R> g, const TreeOp op) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  tree_task<R>(g, op, op.i0 + blockIdx.x * op.istep, blockIdx.y, smem);
+}
+
+template <typename R>
 static cudaError_t tree_launch(const TreeGeom<R> &g, const TreeOp &op, int ntask, int ny, cudaStream_t st) {
   if (ntask <= 0 || ny <= 0) return cudaSuccess;
   k_tree<R><<<dim3(ntask, ny), TQR_THREADS, kTreeSmem, st>>>(g, op);
@@ -224,11 +234,14 @@ static cudaError_t tree_factor(const TreeGeom<R> &g, cudaStream_t st) {
     const int ntile = MTt - k;
     TreeOp op{};
     op.k = k; op.i0 = k; op.istep = 1; op.a_cols = 1;
+    // reflectors of the shortest tile: its blocks end earliest, so its strips
+    // reach furthest left (the other tiles skip the strips they do not need)
+    const int kkmin = std::min(g.rows(MTt - 1), nk);
     for (int b = 0; b < nblk; ++b) {
       op.b = b;
       op.type = OP_GE_PANEL;
       if ((e = tree_launch(g, op, ntile, 1, st)) != cudaSuccess) return e;
-      const int rest = nk - std::min(nk, (b + 1) * ib);
+      const int rest = nk - std::min(nk, std::min(kkmin, (b + 1) * ib));
       op.type = OP_GE_APPLY;
       if ((e = tree_launch(g, op, ntile, (rest + kTreeNW - 1) / kTreeNW, st)) != cudaSuccess) return e;
     }
@@ -343,6 +356,419 @@ static int tree_unmqr_impl(char trans, int m, int n, int nrhs, int nb, int ib, c
   return e == cudaSuccess ? 0 : (int)e;
 }
 
+
+// ---------------------------------------------------------------------------
+// The same factorisation as one persistent launch over a task graph.
+//
+// Tasks are the steps above cut per tile / pair and per 16-column strip.  The
+// host replays the stream driver's order and records, for every task, the
+// regions it reads and writes (tile x strip x {upper triangle with diagonal,
+// strictly lower part}, and the T blocks); a task depends on the last writer
+// of each region it touches and, if it writes, on every reader since that
+// writer.  Tasks are sorted by decreasing longest path to the end (a
+// topological order); CTAs take them strictly in that order and wait on
+// per-task done flags, so the lowest unfinished task always has its inputs
+// done.  Every wait is bounded by a %globaltimer deadline that sets an error
+// word and ends the launch.  All cross-CTA data is read through L2
+// (ld.global.cg in the staged device routines) after an acquire load of the
+// flag; writers publish with __syncthreads + __threadfence + a release store.
+// ---------------------------------------------------------------------------
+static inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct TItem {
+  uint8_t type;        // TreeOpType, | 0x80 for a tsqrt/tsmqr (whole-tile) merge
+  uint8_t b;
+  uint16_t k, i, p, y;
+  uint16_t ndep;
+  uint32_t dep;        // offset of this task's dependency list (task positions)
+};
+static_assert(sizeof(TItem) == 16, "TItem layout");
+
+struct TDagHeader {
+  int head;
+  int error;           // 0 ok, 1 a wait timed out, 2 schedule / arguments mismatch
+  int err_item;
+  int nitems;
+  long long key;
+  int pad[58];
+};
+static_assert(sizeof(TDagHeader) == 256, "TDagHeader layout");
+
+template <typename R>
+struct TDagArgs {
+  TreeGeom<R> g;
+  TDagHeader *hdr;
+  int *done;
+  const TItem *items;
+  const uint32_t *deps;
+  int nitems;
+  long long key;
+  unsigned long long timeout_ns;
+};
+
+__device__ __forceinline__ int tdag_ld_acquire(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void tdag_st_release(int *p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long tdag_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(TQR_THREADS, 2) k_tree_dag(const TDagArgs<R> a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_it, s_err;
+  const int tid = threadIdx.x;
+  if (tid == 0) s_err = (a.hdr->key != a.key || a.hdr->nitems != a.nitems) ? 2 : 0;
+  __syncthreads();
+  if (s_err) {
+    if (tid == 0 && blockIdx.x == 0) atomicExch(&a.hdr->error, 2);
+    return;
+  }
+  for (;;) {
+    if (tid == 0) s_it = atomicAdd(&a.hdr->head, 1);
+    __syncthreads();
+    const int idx = s_it;
+    if (idx >= a.nitems) break;
+    const TItem it = a.items[idx];
+    if (tid == 0) {
+      int err = 0;
+      const unsigned long long t0 = tdag_ns();
+      for (int d = 0; d < (int)it.ndep && !err; ++d) {
+        const int *f = a.done + a.deps[it.dep + d];
+        while (tdag_ld_acquire(f) == 0) {
+          if (tdag_ld_acquire(&a.hdr->error) != 0) { err = 1; break; }
+          if (tdag_ns() - t0 > a.timeout_ns) {
+            if (atomicCAS(&a.hdr->error, 0, 1) == 0) a.hdr->err_item = idx;
+            err = 1;
+            break;
+          }
+          __nanosleep(64);
+        }
+      }
+      s_err = err;
+    }
+    __syncthreads();
+    if (s_err) break;
+    TreeOp op{};
+    op.type = it.type & 0x7f;
+    op.ts = (it.type & 0x80) ? 1 : 0;
+    op.k = it.k; op.b = it.b;
+    op.s = (int)it.p - (int)it.i;
+    op.trans = 0; op.a_cols = 1;
+    tree_task<R>(a.g, op, it.i, it.y, smem);
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      tdag_st_release(a.done + idx, 1);
+    }
+  }
+}
+
+// ---- host: task graph construction -----------------------------------------
+struct TreeShape {
+  int m, n, nb, ib, nrhs, MT, NT, KT;
+  int rows(int i) const { return std::min(nb, m - i * nb); }
+  int cols(int k) const { return std::min(nb, n - k * nb); }
+  int strips(int j) const { return j < NT ? (cols(j) + kTreeNW - 1) / kTreeNW : (nrhs + kTreeNW - 1) / kTreeNW; }
+  bool ragged(int k) const { int p = MT - 1; return p > k && rows(p) < cols(k); }
+};
+
+struct TreePlan {
+  TreeShape sh;
+  long long key = 0;
+  std::vector<TItem> items;
+  std::vector<uint32_t> deps;
+  unsigned char *pinned = nullptr;      // header + items + deps, page-locked
+  std::vector<unsigned char> pageable;
+  size_t off_items = 0, off_deps = 0, img_bytes = 0, done_bytes = 0, total_bytes = 0;
+  const unsigned char *image() const { return pinned ? pinned : pageable.data(); }
+  ~TreePlan() {
+    if (pinned) cudaFreeHost(pinned);
+  }
+};
+
+static double tree_cost(const TreeShape &sh, const TItem &it) {
+  const double ib = sh.ib, w = kTreeNW, nb = sh.nb;
+  const int t = it.type & 0x7f;
+  const bool ts = it.type & 0x80;
+  const double lat = 64.0 * ib * 600;          // serial column steps of a panel
+  switch (t) {
+    case OP_GE_PANEL: return 3.0 * (sh.rows(it.i) - it.b * ib) * ib * ib + lat;
+    case OP_GE_APPLY: return 4.0 * (sh.rows(it.i) - it.b * ib) * ib * w;
+    case OP_GE_TRAIL: return 4.0 * sh.rows(it.i) * std::min(sh.rows(it.i), sh.cols(it.k)) * w;
+    case OP_PR_PANEL: return 3.0 * (ts ? sh.rows(it.p) : (it.b + 1) * ib) * ib * ib + lat;
+    case OP_PR_APPLY: return 4.0 * (ts ? sh.rows(it.p) : (it.b + 1) * ib) * ib * w;
+    default: return (ts ? 4.0 * sh.rows(it.p) : 2.0 * nb) * sh.cols(it.k) * w;
+  }
+}
+
+// Builds the task list in program order with its dependencies, then sorts it.
+static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::vector<uint32_t> &out_deps) {
+  const int NS = std::max(sh.nb / kTreeNW, (sh.nrhs + kTreeNW - 1) / kTreeNW);
+  const int NJ = sh.NT + 1;                    // tile columns plus the right-hand sides
+  const int nblk = (sh.nb + sh.ib - 1) / sh.ib;
+  // regions: tile strips (upper / lower part), then T blocks of geqrt and of the merges
+  const size_t nstrip = (size_t)sh.MT * NJ * NS * 2;
+  auto rg = [&](int i, int j, int s, int lower) { return (((size_t)i * NJ + j) * NS + s) * 2 + lower; };
+  auto rt = [&](int i, int k, int b, int merge) {
+    return nstrip + (((size_t)i * sh.KT + k) * nblk + b) * 2 + merge;
+  };
+  const size_t nreg = nstrip + (size_t)sh.MT * sh.KT * nblk * 2;
+  std::vector<int> last(nreg, -1);
+  std::vector<std::vector<int>> readers(nreg);
+  std::vector<TItem> items;
+  std::vector<std::vector<int>> preds;
+  std::vector<int> cur;
+  auto rd = [&](size_t r) {
+    if (last[r] >= 0) cur.push_back(last[r]);
+    readers[r].push_back((int)items.size());
+  };
+  auto wr = [&](size_t r) {
+    if (last[r] >= 0) cur.push_back(last[r]);
+    for (int x : readers[r]) cur.push_back(x);
+    readers[r].clear();
+    last[r] = (int)items.size();
+  };
+  auto emit = [&](int type, int k, int b, int i, int p, int y) {
+    TItem it;
+    it.type = (uint8_t)type; it.b = (uint8_t)b; it.k = (uint16_t)k; it.i = (uint16_t)i;
+    it.p = (uint16_t)p; it.y = (uint16_t)y; it.ndep = 0; it.dep = 0;
+    std::sort(cur.begin(), cur.end());
+    cur.erase(std::unique(cur.begin(), cur.end()), cur.end());
+    // a task that reads and writes disjoint columns of one region (a ragged
+    // block) records itself; it never waits on itself
+    cur.erase(std::remove(cur.begin(), cur.end(), (int)items.size()), cur.end());
+    preds.push_back(cur);
+    cur.clear();
+    items.push_back(it);
+  };
+  // trailing strip y of panel k -> (tile column, strip)
+  auto trail_js = [&](int k, int y, int &j, int &s) {
+    const int ca = std::max(0, sh.n - (k + 1) * sh.nb);
+    const int sa = (ca + kTreeNW - 1) / kTreeNW;
+    if (y < sa) { const int c = y * kTreeNW; j = k + 1 + c / sh.nb; s = (c % sh.nb) / kTreeNW; }
+    else { j = sh.NT; s = y - sa; }
+  };
+  auto ntrail = [&](int k) {
+    const int ca = std::max(0, sh.n - (k + 1) * sh.nb);
+    return (ca + kTreeNW - 1) / kTreeNW + (sh.nrhs + kTreeNW - 1) / kTreeNW;
+  };
+  for (int k = 0; k < sh.KT; ++k) {
+    const int nk = sh.cols(k), NSk = sh.strips(k);   // NSk: strips of the panel's tile column
+    const bool rag = sh.ragged(k);
+    const int MTt = rag ? sh.MT - 1 : sh.MT;
+    // geqrt of every tile, block by block, then unmqr of its row
+    for (int i = k; i < MTt; ++i) {
+      const int kk = std::min(sh.rows(i), nk);
+      for (int b = 0, c = 0; c < kk; ++b, c += sh.ib) {
+        const int sb = std::min(sh.ib, kk - c);
+        const int q0 = c / kTreeNW, q1 = (c + sb + kTreeNW - 1) / kTreeNW;
+        for (int q = q0; q < q1; ++q) { wr(rg(i, k, q, 0)); wr(rg(i, k, q, 1)); }
+        wr(rt(i, k, b, 0));
+        emit(OP_GE_PANEL, k, b, i, i, 0);
+        // strip y covers columns [c + sb + 16 y, +16) clipped to nk (as in tree_task)
+        for (int y = 0; c + sb + y * kTreeNW < nk; ++y) {
+          const int c0 = c + sb + y * kTreeNW, c1 = std::min(nk, c0 + kTreeNW);
+          for (int v = q0; v < q1; ++v) rd(rg(i, k, v, 1));
+          rd(rt(i, k, b, 0));
+          for (int q = c0 / kTreeNW; q <= (c1 - 1) / kTreeNW; ++q) { wr(rg(i, k, q, 0)); wr(rg(i, k, q, 1)); }
+          emit(OP_GE_APPLY, k, b, i, i, y);
+        }
+      }
+      const int nbk = (kk + sh.ib - 1) / sh.ib;
+      for (int y = 0; y < ntrail(k); ++y) {
+        int j, s;
+        trail_js(k, y, j, s);
+        for (int q = 0; q < NSk; ++q) rd(rg(i, k, q, 1));
+        for (int b = 0; b < nbk; ++b) rd(rt(i, k, b, 0));
+        wr(rg(i, j, s, 0)); wr(rg(i, j, s, 1));
+        emit(OP_GE_TRAIL, k, 0, i, i, y);
+      }
+    }
+    auto merge = [&](int i, int p, int ts) {
+      const int kt = ts ? nk : std::min(sh.rows(p), nk);
+      const int flag = ts ? 0x80 : 0;
+      for (int b = 0, c = 0; c < kt; ++b, c += sh.ib) {
+        const int sb = std::min(sh.ib, kt - c);
+        const int q0 = c / kTreeNW, q1 = (c + sb + kTreeNW - 1) / kTreeNW;
+        for (int q = q0; q < q1; ++q) {
+          wr(rg(i, k, q, 0));
+          wr(rg(p, k, q, 0));
+          if (ts) wr(rg(p, k, q, 1));
+        }
+        wr(rt(p, k, b, 1));
+        emit(OP_PR_PANEL | flag, k, b, i, p, 0);
+        for (int y = 0; c + sb + y * kTreeNW < nk; ++y) {
+          const int c0 = c + sb + y * kTreeNW, c1 = std::min(nk, c0 + kTreeNW);
+          for (int v = q0; v < q1; ++v) {
+            rd(rg(p, k, v, 0));
+            if (ts) rd(rg(p, k, v, 1));
+          }
+          rd(rt(p, k, b, 1));
+          for (int q = c0 / kTreeNW; q <= (c1 - 1) / kTreeNW; ++q) {
+            wr(rg(i, k, q, 0));
+            wr(rg(p, k, q, 0));
+            if (ts) wr(rg(p, k, q, 1));
+          }
+          emit(OP_PR_APPLY | flag, k, b, i, p, y);
+        }
+      }
+      const int nbk = (kt + sh.ib - 1) / sh.ib;
+      for (int y = 0; y < ntrail(k); ++y) {
+        int j, s;
+        trail_js(k, y, j, s);
+        for (int q = 0; q < NSk; ++q) {
+          rd(rg(p, k, q, 0));
+          if (ts) rd(rg(p, k, q, 1));
+        }
+        for (int b = 0; b < nbk; ++b) rd(rt(p, k, b, 1));
+        wr(rg(i, j, s, 0)); wr(rg(i, j, s, 1));
+        wr(rg(p, j, s, 0)); wr(rg(p, j, s, 1));
+        emit(OP_PR_TRAIL | flag, k, 0, i, p, y);
+      }
+    };
+    if (rag) merge(sh.MT - 2, sh.MT - 1, 1);
+    for (int s = 1; k + s < MTt; s *= 2)
+      for (int i = k; i + s < MTt; i += 2 * s) merge(i, i + s, 0);
+  }
+  // longest path to the end, then a stable sort by it
+  const int N = (int)items.size();
+  std::vector<double> rank(N, 0.0);
+  for (int x = N - 1; x >= 0; --x) {
+    rank[x] += tree_cost(sh, items[x]);
+    for (int pr : preds[x]) rank[pr] = std::max(rank[pr], rank[x]);
+  }
+  std::vector<int> order(N), pos(N);
+  for (int x = 0; x < N; ++x) order[x] = x;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rank[a] > rank[b]; });
+  for (int x = 0; x < N; ++x) pos[order[x]] = x;
+  out_items.resize(N);
+  out_deps.clear();
+  for (int q = 0; q < N; ++q) {
+    const int x = order[q];
+    TItem it = items[x];
+    it.dep = (uint32_t)out_deps.size();
+    it.ndep = (uint16_t)preds[x].size();
+    for (int pr : preds[x]) out_deps.push_back((uint32_t)pos[pr]);
+    out_items[q] = it;
+  }
+}
+
+static long long tree_key(const TreeShape &sh) {
+  long long h = 7809847782465536322LL;
+  for (int v : {sh.m, sh.n, sh.nb, sh.ib, sh.nrhs, 0x7ee})
+    h = (h ^ (long long)v) * 1099511628211LL;
+  return h & 0x7fffffffffffffffLL;
+}
+
+static std::mutex g_tplan_mu;
+static std::map<long long, std::shared_ptr<TreePlan>> g_tplans;
+
+static bool tree_dag_shape(int m, int n, int nb, int ib, int nrhs, TreeShape *sh) {
+  if (m <= 0 || n <= 0 || nb <= 0 || nb > 256 || nb % kTreeNW) return false;
+  if (ib <= 0 || ib > 32 || ib % kTreeNW || nb % ib) return false;
+  if (nrhs < 0 || nrhs > 256) return false;
+  sh->m = m; sh->n = n; sh->nb = nb; sh->ib = ib; sh->nrhs = nrhs;
+  sh->MT = (m + nb - 1) / nb; sh->NT = (n + nb - 1) / nb; sh->KT = std::min(sh->MT, sh->NT);
+  if (sh->MT > 65535 || sh->NT > 65535) return false;
+  return true;
+}
+
+static std::shared_ptr<TreePlan> tree_plan(const TreeShape &sh) {
+  const long long key = tree_key(sh);
+  std::lock_guard<std::mutex> l(g_tplan_mu);
+  auto f = g_tplans.find(key);
+  if (f != g_tplans.end()) return f->second;
+  auto p = std::make_shared<TreePlan>();
+  p->sh = sh;
+  p->key = key;
+  tree_build(sh, p->items, p->deps);
+  const size_t N = p->items.size();
+  p->off_items = 256;
+  p->off_deps = align256(p->off_items + sizeof(TItem) * N);
+  p->img_bytes = p->off_deps + sizeof(uint32_t) * p->deps.size();
+  p->done_bytes = align256(sizeof(int) * N);
+  p->total_bytes = align256(p->img_bytes) + p->done_bytes;
+  unsigned char *dst = nullptr;
+  if (cudaMallocHost((void **)&p->pinned, p->img_bytes) == cudaSuccess) {
+    dst = p->pinned;
+  } else {
+    p->pinned = nullptr;
+    cudaGetLastError();
+    p->pageable.resize(p->img_bytes);
+    dst = p->pageable.data();
+  }
+  std::memset(dst, 0, p->img_bytes);
+  TDagHeader h;
+  std::memset(&h, 0, sizeof(h));
+  h.key = key;
+  h.nitems = (int)N;
+  std::memcpy(dst, &h, sizeof(h));
+  std::memcpy(dst + p->off_items, p->items.data(), sizeof(TItem) * N);
+  std::memcpy(dst + p->off_deps, p->deps.data(), sizeof(uint32_t) * p->deps.size());
+  g_tplans[key] = p;
+  return p;
+}
+
+template <typename R>
+static int tree_geqrf_dag_impl(int m, int n, int nb, int ib, R *A, int lda, R *T, R *T2, int ldt, R *tau,
+                               R *tau2, int ldtau, int nrhs, R *B, int ldb, void *work, size_t lwork,
+                               cudaStream_t st) {
+  TreeGeom<R> g;
+  int rc = tree_geom<R>(m, n, nrhs, nb, ib, A, lda, B, ldb, T, T2, ldt, tau, tau2, ldtau, &g);
+  if (rc) return rc;
+  if (m == 0 || n == 0) return 0;
+  if (!A || lda < m) return -6;
+  if (!T || !T2 || ldt < g.MT * ib) return -9;
+  if (!tau || !tau2 || ldtau < n) return -12;
+  if (nrhs < 0) return -13;
+  if (nrhs > 0 && (!B || ldb < m)) return -15;
+  TreeShape sh;
+  if (!tree_dag_shape(m, n, nb, ib, nrhs, &sh)) return -3;
+  std::shared_ptr<TreePlan> p = tree_plan(sh);
+  if (!work || ((uintptr_t)work & 255)) return -16;
+  if (lwork < p->total_bytes) return -17;
+  unsigned char *w = (unsigned char *)work;
+  int *done = (int *)(w + align256(p->img_bytes));
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(w, p->image(), p->img_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess) return (int)e;
+  if ((e = cudaMemsetAsync(done, 0, sizeof(int) * p->items.size(), st)) != cudaSuccess) return (int)e;
+  if ((e = cudaMemset2DAsync(T2, sizeof(R) * ldt, 0, sizeof(R) * g.MT * ib, n, st)) != cudaSuccess) return (int)e;
+  if ((e = cudaFuncSetAttribute(k_tree_dag<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTreeSmem)) !=
+      cudaSuccess)
+    return (int)e;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return (int)e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return (int)e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tree_dag<R>, TQR_THREADS, kTreeSmem)) !=
+      cudaSuccess)
+    return (int)e;
+  if (per_sm < 1) return (int)cudaErrorInvalidConfiguration;
+  TDagArgs<R> a;
+  a.g = g;
+  a.hdr = (TDagHeader *)w;
+  a.done = done;
+  a.items = (const TItem *)(w + p->off_items);
+  a.deps = (const uint32_t *)(w + p->off_deps);
+  a.nitems = (int)p->items.size();
+  a.key = p->key;
+  a.timeout_ns = 20000000000ull;
+  const int grid = std::min(sms * per_sm, a.nitems);
+  k_tree_dag<R><<<grid, TQR_THREADS, kTreeSmem, st>>>(a);
+  count_launch();
+  e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : (int)e;
+}
+
 }  // namespace tqr
 
 using namespace tqr;
@@ -367,6 +793,57 @@ int tqr_dtile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, con
 int tqr_stile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, const float *A, int lda,
                          const float *T, const float *T2, int ldt, float *B, int ldb, cudaStream_t stream) {
   return tree_unmqr_impl<float>(trans, m, n, nrhs, nb, ib, A, lda, T, T2, ldt, B, ldb, stream);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int tqr_tile_tree_dag_worksize(int m, int n, int nb, int ib, int nrhs, size_t *bytes) {
+  if (!bytes) return -6;
+  TreeShape sh;
+  if (!tree_dag_shape(m, n, nb, ib, nrhs, &sh)) return -1;
+  *bytes = tree_plan(sh)->total_bytes;
+  return 0;
+}
+
+int tqr_tile_tree_dag_check(int m, int n, int nb, int ib, int nrhs, long long *ntasks) {
+  TreeShape sh;
+  if (!tree_dag_shape(m, n, nb, ib, nrhs, &sh)) return -1;
+  std::shared_ptr<TreePlan> p = tree_plan(sh);
+  // every dependency points to an earlier task of the sorted order
+  for (size_t q = 0; q < p->items.size(); ++q) {
+    const TItem &it = p->items[q];
+    for (int d = 0; d < (int)it.ndep; ++d)
+      if (p->deps[it.dep + d] >= q) return 1;
+  }
+  if (ntasks) *ntasks = (long long)p->items.size();
+  return 0;
+}
+
+int tqr_tile_tree_dag_status(const void *work, int *error, int *item, cudaStream_t stream) {
+  if (!work || !error || !item) return -1;
+  int h[3];
+  cudaError_t e = cudaMemcpyAsync(h, work, sizeof(h), cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return (int)e;
+  *error = h[1];
+  *item = h[2];
+  return 0;
+}
+
+int tqr_dtile_geqrf_tree_dag(int m, int n, int nb, int ib, double *A, int lda, double *T, double *T2, int ldt,
+                             double *tau, double *tau2, int ldtau, int nrhs, double *B, int ldb, void *work,
+                             size_t lwork, cudaStream_t stream) {
+  return tree_geqrf_dag_impl<double>(m, n, nb, ib, A, lda, T, T2, ldt, tau, tau2, ldtau, nrhs, B, ldb, work,
+                                     lwork, stream);
+}
+
+int tqr_stile_geqrf_tree_dag(int m, int n, int nb, int ib, float *A, int lda, float *T, float *T2, int ldt,
+                             float *tau, float *tau2, int ldtau, int nrhs, float *B, int ldb, void *work,
+                             size_t lwork, cudaStream_t stream) {
+  return tree_geqrf_dag_impl<float>(m, n, nb, ib, A, lda, T, T2, ldt, tau, tau2, ldtau, nrhs, B, ldb, work,
+                                    lwork, stream);
 }
 
 }  // extern "C"

@@ -446,10 +446,38 @@ def tile_geqrf(A, nb=256, ib=32, T=None, tau=None, dag=True):
     return T, tau
 
 
-def tile_geqrf_tree(A, nb=256, ib=32, B=None):
+def tree_dag_workspace(m, n, nb, ib, nrhs, device):
+    """(buffer, aligned pointer, bytes) for the tree task-graph kernel, or None
+    when the shape is outside it."""
+    import ctypes
+    size = ctypes.c_size_t(0)
+    if _lib.lib().tqr_tile_tree_dag_worksize(m, n, nb, ib, nrhs, ctypes.byref(size)) != 0:
+        return None
+    key = ("tree", str(device), size.value)
+    w = _WORK.get(key)
+    if w is None:
+        w = torch.empty(size.value + 256, dtype=torch.uint8, device=device)
+        _WORK[key] = w
+    return w, w.data_ptr() + ((-w.data_ptr()) % 256), size.value
+
+
+def tree_dag_check(m, n, nb, ib, nrhs=0):
+    """Host check of the tree task graph; returns the task count."""
+    import ctypes
+    nt = ctypes.c_longlong(0)
+    rc = _lib.lib().tqr_tile_tree_dag_check(m, n, nb, ib, nrhs, ctypes.byref(nt))
+    if rc != 0:
+        raise RuntimeError(f"tree task graph check failed ({rc})")
+    return nt.value
+
+
+def tile_geqrf_tree(A, nb=256, ib=32, B=None, dag=True):
     """Tile QR of A in place with a binary reduction tree per panel (geqrt!
     on every tile, ttqrt!/ttmqr! merges).  Returns (T, tau, T2, tau2); with B,
-    B is overwritten by Q^T B in the same pass."""
+    B is overwritten by Q^T B in the same pass.  dag=True runs it as one
+    persistent launch when the shape allows (same results as the stream
+    driver)."""
+    import ctypes
     m, n = A.shape
     ts, taus = tile_shapes(m, n, nb, ib)
     T = zeros(*ts, dtype=A.dtype, device=A.device)
@@ -463,8 +491,27 @@ def tile_geqrf_tree(A, nb=256, ib=32, B=None):
     if B is not None:
         nrhs = B.shape[1]
         pb, ldb = _mat(B)
-    _call(_prefix(A, T, tau, B), "tile_geqrf_tree", m, n, nb, ib, pa, lda, pt, _ptr(T2), ldt, pu, _ptr(tau2),
-          ldu, nrhs, pb, ldb)
+    ws = tree_dag_workspace(m, n, nb, ib, nrhs, A.device) if dag else None
+    if ws is None:
+        _call(_prefix(A, T, tau, B), "tile_geqrf_tree", m, n, nb, ib, pa, lda, pt, _ptr(T2), ldt, pu,
+              _ptr(tau2), ldu, nrhs, pb, ldb)
+        return T, tau, T2, tau2
+    _, wp, size = ws
+    p = _prefix(A, T, tau, B)
+    st = torch.cuda.current_stream()
+    rc = getattr(_lib.lib(), f"tqr_{p}tile_geqrf_tree_dag")(m, n, nb, ib, pa, lda, pt, _ptr(T2), ldt, pu,
+                                                           _ptr(tau2), ldu, nrhs, pb, ldb, ctypes.c_void_p(wp),
+                                                           size, st.cuda_stream)
+    if rc < 0:
+        raise ArgumentError(f"tile_geqrf_tree: illegal value of argument {-rc}")
+    if rc > 0:
+        raise RuntimeError(f"tile_geqrf_tree: CUDA error {rc}")
+    if _BLOCKING:
+        err, item = ctypes.c_int(0), ctypes.c_int(0)
+        _lib.lib().tqr_tile_tree_dag_status(ctypes.c_void_p(wp), ctypes.byref(err), ctypes.byref(item),
+                                            st.cuda_stream)
+        if err.value != 0:
+            raise RuntimeError(f"tile_geqrf_tree: task graph stopped at task {item.value} (status {err.value})")
     return T, tau, T2, tau2
 
 

@@ -70,6 +70,13 @@ DIAG = {
     "tqr_batched_graph": ([_I, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, ctypes.POINTER(_P)], _I),
     "tqr_batched_graph_launch": ([_P, _P], _I),
     "tqr_batched_graph_destroy": ([_P], _I),
+    "tqr_tile_tree_dag_worksize": ([_I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_size_t)], _I),
+    "tqr_tile_tree_dag_check": ([_I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)], _I),
+    "tqr_tile_tree_dag_status": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I), _P], _I),
+    "tqr_dtile_geqrf_tree_dag": ([_I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P, ctypes.c_size_t,
+                                  _P], _I),
+    "tqr_stile_geqrf_tree_dag": ([_I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P, ctypes.c_size_t,
+                                  _P], _I),
     "tqr_qr_batched_worksize": ([_I, _I, _I, _I, ctypes.POINTER(ctypes.c_size_t)], _I),
     "tqr_dqr_batched_fwd": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
     "tqr_sqr_batched_fwd": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),

@@ -131,3 +131,20 @@ def test_dag_schedule_replay_with_rhs_tile(L, shape):
     """Least-squares schedules: B rides along as one extra tile column."""
     nt = ctypes.c_longlong(0)
     assert L.tqr_tile_dag_check_rhs(*shape, ctypes.byref(nt)) == 0 and nt.value > 0
+
+
+@pytest.mark.parametrize("m,n,nb,ib,nrhs", [(65536, 512, 256, 32, 0), (1000, 300, 128, 16, 5), (300, 400, 256, 32, 0),
+                                            (64, 200, 32, 16, 3), (517, 130, 64, 16, 0), (4096, 4096, 256, 32, 4)])
+def test_tree_task_graph_is_topological(L, m, n, nb, ib, nrhs):
+    """The tree task graph's dependencies all point to earlier tasks (the
+    persistent kernel's deadlock-freedom argument)."""
+    nt = ctypes.c_longlong(0)
+    assert L.tqr_tile_tree_dag_check(m, n, nb, ib, nrhs, ctypes.byref(nt)) == 0
+    assert nt.value > 0
+
+
+def test_tree_task_graph_shape_limits(L):
+    size = ctypes.c_size_t(0)
+    assert L.tqr_tile_tree_dag_worksize(100, 100, 64, 8, 0, ctypes.byref(size)) == -1      # ib not a multiple of 16
+    assert L.tqr_tile_tree_dag_worksize(100, 100, 512, 32, 0, ctypes.byref(size)) == -1    # nb > 256
+    assert L.tqr_tile_tree_dag_worksize(1024, 256, 256, 32, 0, ctypes.byref(size)) == 0 and size.value > 0

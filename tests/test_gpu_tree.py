@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 
 SHAPES = [(1024, 256, 128, 32), (1000, 300, 128, 16), (1024, 64, 32, 8), (300, 300, 128, 32),
           (517, 130, 64, 16), (130, 130, 64, 16), (260, 129, 64, 16), (64, 200, 32, 8), (2048, 512, 256, 32),
-          (1800, 512, 256, 32)]
+          (1800, 512, 256, 32), (300, 400, 256, 32), (300, 400, 256, 16), (100, 170, 64, 8)]
 
 
 def rel(a, b):
@@ -54,6 +54,31 @@ def test_tree_matches_oracle(tq, oracle, m, n, nb, ib):
     assert np.linalg.norm(tq.to_numpy(QtA)[:k] - R) <= 1e-13 * np.linalg.norm(R) * k
 
 
+@pytest.mark.parametrize("m,n,nb,ib,nrhs", [(1024, 256, 128, 32, 0), (1000, 300, 128, 16, 5), (300, 400, 256, 32, 0),
+                                            (517, 130, 64, 16, 3), (4096, 1024, 256, 32, 7), (1800, 512, 256, 32, 0),
+                                            (64, 200, 32, 16, 2)])
+def test_tree_task_graph_equals_stream_driver(tq, m, n, nb, ib, nrhs):
+    """One persistent launch over the task graph runs the same per-task
+    arithmetic as the stream driver: the results are bit-identical."""
+    import torch
+    tq.tree_dag_check(m, n, nb, ib, nrhs)
+    g = torch.Generator(device="cuda").manual_seed(m + n)
+    A0 = torch.randn(m, n, generator=g, dtype=torch.float64, device="cuda")
+    B0 = torch.randn(m, max(nrhs, 1), generator=g, dtype=torch.float64, device="cuda")[:, :nrhs]
+    outs = []
+    for dag in (False, True):
+        A = tq.empty(m, n)
+        A.copy_(A0)
+        B = None
+        if nrhs:
+            B = tq.empty(m, nrhs)
+            B.copy_(B0)
+        res = tq.tile_geqrf_tree(A, nb, ib, B=B, dag=dag)
+        outs.append((A,) + tuple(res) + ((B,) if nrhs else ()))
+    for a, b in zip(*outs):
+        assert torch.equal(a, b)
+
+
 def test_tree_float(tq, oracle):
     import torch
     rng = np.random.default_rng(2)
@@ -76,7 +101,7 @@ def test_tree_tall_skinny_properties(tq):
     A0.copy_(torch.randn(m, n, generator=g, dtype=torch.float64, device="cuda"))
     A = tq.empty(m, n)
     A.copy_(A0)
-    T, tau, T2, tau2 = tq.tile_geqrf_tree(A, nb, ib)
+    T, tau, T2, tau2 = tq.tile_geqrf_tree(A, nb, ib)        # persistent task graph
     R = torch.triu(A[:n])
     x = torch.randn(n, 3, generator=g, dtype=torch.float64, device="cuda")
     ax = torch.linalg.norm(A0 @ x, dim=0)
