@@ -44,7 +44,7 @@ def parse():
     p.add_argument("--n", type=int, default=8192, help="matrix order (default: the 8192^2 workload)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--kernel", default=None, choices=["tsmqr", "tsqrt", "geqrt"],
+    p.add_argument("--kernel", default=None, choices=["tsmqr", "tsmqr_tc", "tsqrt", "geqrt"],
                    help="time one tile kernel alone (for profiling) instead of the workload")
     p.add_argument("--dtype", default="f64", choices=["f64", "f32"], help="element type for --kernel")
     p.add_argument("--no-ls", action="store_true", help="skip the least-squares comparison")
@@ -74,7 +74,24 @@ def kernel_bench(args):
     g = torch.Generator(device="cuda").manual_seed(SEED)
     n = args.n
     res = {}
-    if args.kernel == "tsmqr":
+    if args.kernel == "tsmqr_tc":
+        # tensor-core FP32 tsmqr ('L', 'C') on the same band as --kernel tsmqr --dtype f32
+        import ctypes
+        from tileqr import _lib
+        w = ((n - NB) // 128) * 128
+        dt = torch.float32
+        A1, A2, V = tq.empty(NB, w, dtype=dt), tq.empty(NB, w, dtype=dt), tq.empty(NB, NB, dtype=dt)
+        for t in (A1, A2):
+            t.copy_(torch.randn(NB, w, generator=g, dtype=torch.float64, device="cuda"))
+        V.copy_(torch.randn(NB, NB, generator=g, dtype=torch.float64, device="cuda") / 16)
+        T = tq.empty(IB, NB, dtype=dt)
+        T.copy_(torch.triu(torch.randn(IB, NB, generator=g, dtype=torch.float64, device="cuda")) / 16)
+        err = torch.zeros(1, dtype=torch.int32, device="cuda")
+        P = lambda t: ctypes.c_void_p(t.data_ptr())
+        run = lambda: _lib.lib().tqr_stsmqr_tc(NB, w, NB, NB, P(A1), NB, P(A2), NB, P(V), NB, P(T), IB, P(err),
+                                               ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        fl = 4.0 * NB * NB * w
+    elif args.kernel == "tsmqr":
         w = n - NB
         dt = torch.float32 if args.dtype == "f32" else torch.float64
         A1, A2, V = tq.empty(NB, w, dtype=dt), tq.empty(NB, w, dtype=dt), tq.empty(NB, NB, dtype=dt)

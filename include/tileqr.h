@@ -357,6 +357,25 @@ int tqr_sqr_batched_bwd(int batch, int m, int n, int ib, const float *F, const f
                         const float *Qbar, const float *Rbar, float *Abar, void *work, size_t lwork,
                         cudaStream_t stream);
 
+/* ---- Tensor-core FP32 trailing update (no counterpart in NextLA) ----
+ * tsmqr!('L', 'C', ...) (src/tsmqr.jl:47-146, l = 0, ib = 32) on tcgen05
+ * tensor cores: [A1; A2] := Q^T [A1; A2] with Q from a tsqrt! factor V
+ * (m2-by-k) and T (32-by-k), A1 rows [0, k), m2 = 128 or 256, k a multiple of
+ * 32, n a multiple of 128.  TF32 products split three ways (hi*hi + hi*lo +
+ * lo*hi) with FP32 accumulation in TMEM: FP32-level accuracy.  *err (device)
+ * is set to 1 if a tensor-core completion wait gave up. */
+int tqr_stsmqr_tc(int m1, int n, int m2, int k, float *A1, int lda1, float *A2, int lda2, const float *V,
+                  int ldv, const float *T, int ldt, int *err, cudaStream_t stream);
+
+/* The FP32 persistent tile kernel (tqr_stile_geqrf_dag, tqr_stile_gels_dag and
+ * the mixed solve's factorisation) runs its tsmqr updates as 128-column
+ * tensor-core tasks when nb = 256, ib = 32 and A is 16-byte aligned with lda
+ * a multiple of 4; tqr_tile_dag_tensor_cores(0) switches that off (SIMT
+ * strips only), (1) back on; returns the previous setting.
+ * tqr_tile_dag_check_tc: host replay check of that schedule. */
+int tqr_tile_dag_tensor_cores(int on);
+int tqr_tile_dag_check_tc(int m, int n, int nrhs, int nb, int ib, long long *ntasks);
+
 /* ---- Measurement hooks (no counterpart in NextLA; used by the benchmark) ----
  * tqr_launch_count: kernels this library has launched since it was loaded.
  * tqr_profile_enable / tqr_profile_read: while enabled, the tile driver brackets

@@ -10,6 +10,8 @@
 //   TB(k,i,b)    tsqrt block b on [R of (k,k); tile (i,k)]               1 CTA
 //   TA(k,i,b,s)  that block applied to strip s of (k,k) and (i,k)        (tsmqr, one block)
 //   TM(k,i,j,s)  all of (i,k)'s reflectors applied to strip s of (k,j), (i,j)   (tsmqr)
+//   TC(k,i,j,c)  FP32 only: the same for the 128-column chunk c of (k,j), (i,j) on the
+//                tcgen05 tensor cores (tc_apply.cuh), in place of its 8 TM strips
 //
 // One launch with (SMs x resident CTAs) CTAs runs them all.  Each CTA takes
 // the next task index from a global counter, waits until the task's inputs
@@ -39,14 +41,17 @@
 #include <mutex>
 #include <vector>
 
+#include <type_traits>
+
 #include "apply_dev.cuh"
 #include "panel_dev.cuh"
+#include "tc_apply.cuh"
 #include "tileqr.h"
 #include "tileqr_internal.h"
 
 namespace tqr {
 
-enum : uint8_t { IT_GB = 0, IT_GA = 1, IT_UN = 2, IT_TB = 3, IT_TA = 4, IT_TM = 5 };
+enum : uint8_t { IT_GB = 0, IT_GA = 1, IT_UN = 2, IT_TB = 3, IT_TA = 4, IT_TM = 5, IT_TC = 6 };
 
 struct DagItem {
   uint8_t type, b;
@@ -62,6 +67,10 @@ struct DagGeom {
   // width nrhs that only receives trailing updates, so the factorisation also
   // forms Q^T B.  NTA is the number of tile columns of A.
   int nrhs, NTA;
+  // tc = 1: the tsmqr updates of A's tile columns run as TC tasks on NCH
+  // chunks of 128 columns (CPS strips each) per tile (FP32, nb = 256, ib = 32)
+  int tc, NCH, CPS;
+  __host__ __device__ int tm_tasks(int j) const { return (tc && j < NTA) ? NCH : strips(j); }
   __host__ __device__ int strips(int j) const { return j < NTA ? NS : (nrhs + nw - 1) / nw; }
   __host__ __device__ int width(int j) const { return j < NTA ? nb : nrhs; }
   __host__ __device__ int ver(int i, int j, int s) const { return (i * NT + j) * NS + s; }
@@ -109,6 +118,13 @@ __host__ __device__ inline int item_deps(const DagGeom &g, const DagItem &it, in
       c[n] = g.ver(k, j, s); t[n++] = i;
       c[n] = g.ver(i, j, s); t[n++] = k;
       break;
+    case IT_TC:
+      c[n] = g.done_t(k, i); t[n++] = g.panel_tasks();
+      for (int q = s * g.CPS; q < (s + 1) * g.CPS; ++q) {
+        c[n] = g.ver(k, j, q); t[n++] = i;
+        c[n] = g.ver(i, j, q); t[n++] = k;
+      }
+      break;
   }
   return n;
 }
@@ -144,6 +160,12 @@ __host__ __device__ inline int item_updates(const DagGeom &g, const DagItem &it,
     case IT_TM:
       c[n++] = g.ver(k, j, s);
       c[n++] = g.ver(i, j, s);
+      break;
+    case IT_TC:
+      for (int q = s * g.CPS; q < (s + 1) * g.CPS; ++q) {
+        c[n++] = g.ver(k, j, q);
+        c[n++] = g.ver(i, j, q);
+      }
       break;
   }
   return n;
@@ -198,8 +220,16 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
+// Per-CTA tensor-core state of the TC tasks (FP32 only).
+struct TcState {
+  uint32_t tmem;
+  uint64_t *bar;
+  uint32_t phase;
+};
+
+// Runs one task; false only if a TC task's tensor-core wait gave up.
 template <typename R, int NW>
-__device__ void run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *smem) {
+__device__ bool run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *smem, TcState *tcs) {
   const DagGeom &g = a.g;
   const int nb = g.nb, ib = g.ib;
   const int k = it.k, i = it.i, j = it.j, b = it.b, s = it.s;
@@ -213,12 +243,22 @@ __device__ void run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *
     R *Ab = tile(k, k) + ix(b * ib, b * ib, a.lda);
     panel_qr_cta<R>(nb - b * ib, ib, Ab, a.lda, tautile(k, k) + b * ib, ttile(k, k) + ix(0, b * ib, a.ldt),
                     a.ldt, true, true, smem);
-    return;
+    return true;
   }
   if (it.type == IT_TB) {
     tsqrt_block_cta<R>(nb, ib, tile(k, k) + ix(b * ib, b * ib, a.lda), a.lda, tile(i, k) + ix(0, b * ib, a.lda),
                        a.lda, ttile(i, k) + ix(0, b * ib, a.ldt), a.ldt, tautile(i, k) + b * ib, true, smem);
-    return;
+    return true;
+  }
+  if (it.type == IT_TC) {
+    if constexpr (std::is_same<R, float>::value) {
+      unsigned char *al = smem + ((1024 - (tc::saddr(smem) & 1023)) & 1023);
+      const size_t c0 = (size_t)s * tc::kChunk;
+      return tc::tsmqr_chunk(nb, nb, tile(k, j) + c0 * a.lda, a.lda, tile(i, j) + c0 * a.lda, a.lda, tile(i, k),
+                             a.lda, ttile(i, k), a.ldt, tcs->tmem, tcs->bar, &tcs->phase, al);
+    } else {
+      return false;
+    }
   }
   ApplyArgs<R> p;
   p.ib = ib;
@@ -265,6 +305,7 @@ __device__ void run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *
       break;
   }
   apply_strip<R, NW>(p, s * NW, smem);
+  return true;
 }
 
 template <typename R, int NW>
@@ -275,12 +316,34 @@ k_tile_dag(const DagArgs<R> a)
   __shared__ int s_it, s_err;
   const int tid = threadIdx.x;
   __shared__ unsigned long long s_tstart;
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ uint32_t s_tmem;
   bool first = true;
   if (tid == 0) s_err = (a.hdr->key != a.key || a.hdr->nitems != a.nitems) ? 2 : 0;
   __syncthreads();
   if (s_err) {
     if (tid == 0 && blockIdx.x == 0) atomicExch(&a.hdr->error, 2);
     return;
+  }
+  TcState tcs{0u, &s_bar, 0u};
+  bool tc_failed = false;
+  if constexpr (std::is_same<R, float>::value) {
+    if (a.g.tc) {
+      // one mbarrier and 256 TMEM columns per CTA (two CTAs per SM share TMEM)
+      if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::saddr(&s_bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      }
+      if ((tid >> 5) == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc::saddr(&s_tmem)),
+                     "r"(tc::kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      tcs.tmem = s_tmem;
+    }
   }
   for (;;) {
     if (tid == 0) s_it = atomicAdd(&a.hdr->head, 1);
@@ -315,11 +378,19 @@ k_tile_dag(const DagArgs<R> a)
     }
     __syncthreads();
     if (s_err) break;
-    run_item<R, NW>(a, it, smem_raw);
+    if (!run_item<R, NW>(a, it, smem_raw, &tcs)) {
+      // a tensor-core completion wait gave up: report, then stop this CTA
+      if (tid == 0 && atomicCAS(&a.hdr->error, 0, 3) == 0) {
+        a.hdr->err_item = idx;
+        a.hdr->err_type = it.type;
+      }
+      tc_failed = true;
+      break;
+    }
     __syncthreads();
     if (tid == 0) {
       const unsigned long long t2 = global_ns();
-      atomicAdd(&a.hdr->busy_ns[it.type], t2 - s_tstart);
+      atomicAdd(&a.hdr->busy_ns[it.type < IT_TC ? it.type : IT_TM], t2 - s_tstart);
       atomicMax(&a.hdr->t_last, t2);
       __threadfence();
       int c[kMaxDeps];
@@ -327,6 +398,18 @@ k_tile_dag(const DagArgs<R> a)
       for (int u = 0; u < nu; ++u) atomicAdd(a.cnt + c[u], 1);
     }
   }
+  if constexpr (std::is_same<R, float>::value) {
+    if (a.g.tc) {
+      // after a failed wait, one more bounded wait for the outstanding commit
+      if (tc_failed) tc::bar_wait(&s_bar, tcs.phase ^ 1u);
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if ((tid >> 5) == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tcs.tmem), "r"(tc::kTmemCols));
+    }
+  }
+  (void)tc_failed;
 }
 
 // ---------------------------------------------------------------------------
@@ -360,6 +443,7 @@ static bool dag_geom(int m, int n, int nb, int ib, DagGeom *g, int nrhs = 0) {
   if (ib % nw) return false;
   g->m = m; g->n = n; g->nb = nb; g->ib = ib; g->nw = nw;
   g->nrhs = nrhs;
+  g->tc = 0; g->NCH = nb / tc::kChunk; g->CPS = tc::kChunk / nw;
   g->NTA = n / nb;
   g->MT = m / nb; g->NT = g->NTA + (nrhs > 0 ? 1 : 0); g->KT = std::min(g->MT, g->NTA);
   g->NS = nb / nw; g->SPB = ib / nw; g->NBK = nb / ib;
@@ -372,9 +456,15 @@ static bool dag_geom(int m, int n, int nb, int ib, DagGeom *g, int nrhs = 0) {
   return true;
 }
 
+// The FP32 persistent kernel runs its tsmqr updates on the tensor cores
+// unless a caller switches that off (tqr_tile_dag_tensor_cores(0)), e.g. to
+// compare with the SIMT path.
+static int g_tc_enabled = 1;
+static bool tc_enabled() { return g_tc_enabled != 0; }
+
 static long long geom_key(const DagGeom &g) {
   long long h = 1469598103934665603LL;
-  for (int v : {g.m, g.n, g.nb, g.ib, g.nw, g.nrhs}) h = (h ^ (long long)v) * 1099511628211LL;
+  for (int v : {g.m, g.n, g.nb, g.ib, g.nw, g.nrhs, g.tc}) h = (h ^ (long long)v) * 1099511628211LL;
   return h & 0x7fffffffffffffffLL;
 }
 
@@ -382,8 +472,10 @@ static long long geom_key(const DagGeom &g) {
 // Tasks of step k in the algorithm's loop order.
 __host__ __device__ inline long long step_tasks(const DagGeom &g, int k) {
   const long long pt = g.panel_tasks();
-  const long long right = (long long)(g.NTA - k - 1) * g.NS + (g.NT > g.NTA ? g.strips(g.NTA) : 0);
-  return pt + right + (long long)(g.MT - k - 1) * (pt + right);
+  const long long rhs = g.NT > g.NTA ? g.strips(g.NTA) : 0;
+  const long long right = (long long)(g.NTA - k - 1) * g.NS + rhs;
+  const long long right_tm = (long long)(g.NTA - k - 1) * g.tm_tasks(0) + rhs;
+  return pt + right + (long long)(g.MT - k - 1) * (pt + right_tm);
 }
 
 // Writes the tasks of step k into out[] in loop order; returns their count.
@@ -406,8 +498,12 @@ __host__ __device__ inline long long gen_step(const DagGeom &g, int k, DagItem *
       push(IT_TB, i, k, b, 0);
       for (int s = (b + 1) * g.SPB; s < g.NS; ++s) push(IT_TA, i, k, b, s);
     }
-    for (int j = k + 1; j < g.NT; ++j)
-      for (int s = 0; s < g.strips(j); ++s) push(IT_TM, i, j, 0, s);
+    for (int j = k + 1; j < g.NT; ++j) {
+      if (g.tc && j < g.NTA)
+        for (int c = 0; c < g.NCH; ++c) push(IT_TC, i, j, 0, c);
+      else
+        for (int s = 0; s < g.strips(j); ++s) push(IT_TM, i, j, 0, s);
+    }
   }
   return n;
 }
@@ -431,6 +527,7 @@ static double item_cost(const DagGeom &g, const DagItem &it) {
     case IT_GA: return 4.0 * (nb - it.b * ib) * ib * nw;
     case IT_TA: return 4.0 * nb * ib * nw;
     case IT_UN: return 2.0 * nb * nb * std::min<double>(nw, g.width(it.j));
+    case IT_TC: return 4.0 * nb * nb * tc::kChunk / 6.0;     // tensor cores: ~6x a SIMT strip per column
     default: return 4.0 * nb * nb * std::min<double>(nw, g.width(it.j));
   }
 }
@@ -558,6 +655,11 @@ static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int
   if (m == 0 || n == 0) return 0;
   DagGeom g;
   if (!dag_geom(m, n, nb, ib, &g, nrhs)) return -3;   // shape outside the DAG path
+  // FP32: trailing tsmqr updates on the tensor cores when the tile shape and
+  // the float4 staging alignment allow it
+  if (std::is_same<R, float>::value && nb == 256 && ib == tc::kIb && g.nw == 16 && tc_enabled() &&
+      ((uintptr_t)A & 15) == 0 && (lda & 3) == 0)
+    g.tc = 1;
   if (lda < m) return -6;
   if (ldt < g.MT * ib) return -8;
   if (ldtau < n) return -10;
@@ -587,8 +689,9 @@ static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int
   a.nitems = (int)plan->items.size();
   a.key = plan->key;
   a.timeout_ns = 20ull * 1000ull * 1000ull * 1000ull;   // 20 s for any single wait
-  const size_t sm = std::max({apply_smem_elems(nb, ib, g.nw, true, true, true) * sizeof(R),
-                              panel_smem<R>(nb, ib, true, true), tsqrt_smem<R>(nb, ib, true)});
+  size_t sm = std::max({apply_smem_elems(nb, ib, g.nw, true, true, true) * sizeof(R),
+                        panel_smem<R>(nb, ib, true, true), tsqrt_smem<R>(nb, ib, true)});
+  if (g.tc) sm = std::max(sm, tc::kSmem);
   const double mn = (double)std::max(m, n), kn = (double)std::min(m, n);
   const double flops = 2.0 * mn * kn * kn - 2.0 * kn * kn * kn / 3.0;
   return g.nw == 16 ? launch_dag<R, 16>(a, sm, flops, st) : launch_dag<R, 8>(a, sm, flops, st);
@@ -795,6 +898,26 @@ int tqr_tile_dag_check_rhs(int m, int n, int nrhs, int nb, int ib, long long *nt
   const bool ok = build_schedule(g, items, true);
   if (ntasks) *ntasks = (long long)items.size();
   return ok ? 0 : 2;
+}
+
+int tqr_tile_dag_tensor_cores(int on) {
+  const int old = g_tc_enabled;
+  g_tc_enabled = on ? 1 : 0;
+  return old;
+}
+
+int tqr_tile_dag_check_tc(int m, int n, int nrhs, int nb, int ib, long long *ntasks) {
+  DagGeom g;
+  if (!dag_geom(m, n, nb, ib, &g, nrhs)) return 1;
+  if (nb != 256 || ib != tc::kIb || g.nw != 16) return 1;
+  g.tc = 1;
+  std::vector<DagItem> items;
+  if (!build_schedule(g, items, true)) return 2;
+  long long total = 0;
+  for (int k = 0; k < g.KT; ++k) total += step_tasks(g, k);
+  if (total != (long long)items.size()) return 3;
+  if (ntasks) *ntasks = (long long)items.size();
+  return 0;
 }
 
 int tqr_tile_dag_check(int m, int n, int nb, int ib, long long *ntasks) {

@@ -1,0 +1,82 @@
+// tc.cu -- stand-alone launcher of the tensor-core FP32 tsmqr update
+// (tc_apply.cuh): one CTA per 128-column chunk of [A1; A2].
+#include "tc_apply.cuh"
+#include "tileqr.h"
+#include "tileqr_internal.h"
+
+namespace tqr {
+
+// TMEM allocation / release and the MMA mbarrier for one CTA.
+__device__ __forceinline__ void tc_setup(uint64_t *bar, uint32_t *tmem_slot) {
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::saddr(bar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if ((threadIdx.x >> 5) == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc::saddr(tmem_slot)),
+                 "r"(tc::kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// After a failed wait: one more bounded wait for the outstanding commit, then
+// release TMEM.  After success: release TMEM.
+__device__ __forceinline__ void tc_teardown(uint64_t *bar, uint32_t phase, bool failed, uint32_t tmem) {
+  if (failed) tc::bar_wait(bar, phase);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if ((threadIdx.x >> 5) == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tc::kTmemCols));
+}
+
+__global__ void __launch_bounds__(TQR_THREADS, 1)
+k_tsmqr_tc(int m2, int k, float *A1, int lda1, float *A2, int lda2, const float *V, int ldv, const float *T, int ldt,
+           int *err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_slot;
+  unsigned char *smem = smem_raw + ((1024 - (tc::saddr(smem_raw) & 1023)) & 1023);
+  tc_setup(&bar, &tmem_slot);
+  const uint32_t tmem = tmem_slot;
+  uint32_t phase = 0;
+  const size_t c0 = (size_t)blockIdx.x * tc::kChunk;
+  const bool ok = tc::tsmqr_chunk(m2, k, A1 + c0 * lda1, lda1, A2 + c0 * lda2, lda2, V, ldv, T, ldt, tmem, &bar,
+                                  &phase, smem);
+  if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+  tc_teardown(&bar, phase ^ 1u, !ok, tmem);
+}
+
+}  // namespace tqr
+
+using namespace tqr;
+
+extern "C" {
+
+int tqr_stsmqr_tc(int m1, int n, int m2, int k, float *A1, int lda1, float *A2, int lda2, const float *V, int ldv,
+                  const float *T, int ldt, int *err, cudaStream_t stream) {
+  if (m1 < 0) return -1;
+  if (n < 0 || n % tc::kChunk) return -2;
+  if (m2 != 128 && m2 != 256) return -3;
+  if (k < 0 || k % tc::kIb || k > m1 || k > m2) return -4;
+  if (n == 0 || k == 0) return 0;
+  if (!A1 || lda1 < m1) return -6;
+  if (!A2 || lda2 < m2) return -8;
+  if (!V || ldv < m2) return -10;
+  if (!T || ldt < tc::kIb) return -12;
+  if (((uintptr_t)A2 & 15) || (lda2 & 3) || ((uintptr_t)V & 15) || (ldv & 3)) return -8;   // float4 staging
+  if (!err) return -13;
+  // two CTAs per SM at most (2 x 256 TMEM columns = all of TMEM)
+  const size_t sm = tc::kSmem;
+  cudaError_t e = cudaFuncSetAttribute(k_tsmqr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return (int)e;
+  k_tsmqr_tc<<<n / tc::kChunk, TQR_THREADS, sm, stream>>>(m2, k, A1, lda1, A2, lda2, V, ldv, T, ldt, err);
+  count_launch();
+  e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : (int)e;
+}
+
+}  // extern "C"

@@ -1,0 +1,302 @@
+// tc_apply.cuh -- FP32 tsmqr!('L','C') on the 5th-generation tensor cores.
+//
+// The trailing update of NextLA's tsmqr! (src/tsmqr.jl:47-146 with parfb!/
+// pamm!, l = 0) for one 128-column chunk of a tile pair, per ib = 32 block b:
+//
+//   W^T  = A2^T V_b              GEMM1: M = 128 (chunk columns), N = 32, K = m2
+//   W    = T_b^T (A1_b + W)      SIMT on the TMEM read-back (32 x 32 triangle)
+//   A1_b = A1_b - W
+//   A2   = A2 - V_b W            GEMM2: M = m2 (two 128-row halves), N = 128, K = 32
+//
+// Both GEMMs run as tcgen05.mma kind::tf32 with FP32 accumulators in TMEM,
+// issued by one thread and completed through an mbarrier; every operand is
+// split x = hi + lo with hi = tf32(x), lo = tf32(x - hi) and the product
+// taken as hi*hi + hi*lo + lo*hi (three MMAs into one accumulator), which
+// keeps FP32-level accuracy (the dropped lo*lo term is ~2^-22 relative).
+//
+// Shared-memory operands use the no-swizzle K-major core-matrix layout: 8
+// rows x 16 bytes per core matrix, consecutive K groups 128 bytes apart (the
+// leading byte offset), consecutive 8-row groups SBO bytes apart.
+//
+// The caller owns the TMEM allocation (kTmemCols columns at tmem) and the
+// mbarrier (initialised with count 1; *phase tracks its parity).  Every
+// mbarrier wait is bounded: on expiry the routine records the failure in
+// *err and returns (no further MMA is issued).
+#pragma once
+#include "common.cuh"
+
+namespace tqr {
+namespace tc {
+
+constexpr int kChunk = 128;            // chunk columns (GEMM1 M, GEMM2 N)
+constexpr int kIb = 32;                // reflectors per block (GEMM1 N, GEMM2 K)
+constexpr int kKc = 64;                // GEMM1 K chunk (rows of A2 staged at once)
+constexpr int kTmemCols = 256;         // D1: columns [0, 32); D2 (one 128-row half at a time): [128, 256)
+// dynamic shared memory: A operand hi/lo (2 x 32 KB), B operand hi/lo
+// (2 x 16 KB), T block (32 x 33 floats)
+constexpr size_t kBufA = 32768, kBufB = 16384;
+constexpr size_t kSmem = 2 * kBufA + 2 * kBufB + sizeof(float) * 32 * 33 + 1024;
+constexpr long kWaitLimit = 1L << 26;  // mbarrier polls before giving up
+
+__device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// tcgen05 shared-memory matrix descriptor: no swizzle, version 1.
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+// Instruction descriptor of kind::tf32: D F32, A and B TF32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_tf32(int m, int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+// Byte offset of element (row, k) in a K-major core-matrix tile.
+__device__ __forceinline__ int kmaj(int row, int k, int sbo) {
+  return (row >> 3) * sbo + (k >> 2) * 128 + (row & 7) * 16 + (k & 3) * 4;
+}
+
+__device__ __forceinline__ float tf32_round(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void put_split(unsigned char *hi, unsigned char *lo, int off, float x) {
+  const float h = tf32_round(x);
+  *reinterpret_cast<float *>(hi + off) = h;
+  *reinterpret_cast<float *>(lo + off) = tf32_round(x - h);
+}
+
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
+  asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+               "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}"
+               ::"r"(d), "l"(a), "l"(b), "r"(id), "r"(acc));
+}
+
+__device__ __forceinline__ void commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(bar)));
+}
+
+// Waits for the mbarrier phase with parity `parity`; false after kWaitLimit polls.
+__device__ __forceinline__ bool bar_wait(uint64_t *bar, uint32_t parity) {
+  for (long it = 0; it < kWaitLimit; ++it) {
+    uint32_t ok;
+    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok) : "r"(saddr(bar)), "r"(parity) : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// Shared memory written by threads -> visible to the tensor core; all threads.
+__device__ __forceinline__ void to_async_proxy() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// Issue (thread 0), commit and wait (all threads); false if the wait gave up.
+template <typename F>
+__device__ __forceinline__ bool run_mma(F issue, uint64_t *bar, uint32_t *phase) {
+  if (threadIdx.x == 0) {
+    issue();
+    commit(bar);
+  }
+  // the same verdict in every thread, so callers leave together
+  const bool ok = __syncthreads_and(bar_wait(bar, *phase)) != 0;
+  *phase ^= 1u;
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  return ok;
+}
+
+__device__ __forceinline__ void put_split4(unsigned char *hi, unsigned char *lo, int off, float4 x) {
+  float4 h, l;
+  h.x = tf32_round(x.x); l.x = tf32_round(x.x - h.x);
+  h.y = tf32_round(x.y); l.y = tf32_round(x.y - h.y);
+  h.z = tf32_round(x.z); l.z = tf32_round(x.z - h.z);
+  h.w = tf32_round(x.w); l.w = tf32_round(x.w - h.w);
+  *reinterpret_cast<float4 *>(hi + off) = h;
+  *reinterpret_cast<float4 *>(lo + off) = l;
+}
+
+// Stage rows [r0, r0 + nr) x columns [0, ncol) of a column-major matrix as
+// the K-major operand with K = row (4 consecutive rows = one 16-byte run),
+// row-of-operand = column; SBO = (nr / 4) * 128.  nr a multiple of 4, ncol a
+// multiple of 8; the source 16-byte aligned with ld a multiple of 4.
+// Lanes run over 8 columns first (conflict-free 128-byte stores), then K.
+template <int NCOL, int NR>
+__device__ __forceinline__ void stage_kmajor(const float *src, int ld, int r0, unsigned char *hi, unsigned char *lo) {
+  constexpr int NV = NCOL * NR / 4;               // float4 pieces
+  constexpr int PER = NV / TQR_THREADS;           // per thread (exact for the shapes used)
+  static_assert(NV % TQR_THREADS == 0, "staging shape");
+  float4 v[PER];
+#pragma unroll
+  for (int u = 0; u < PER; ++u) {
+    const int idx = threadIdx.x + u * TQR_THREADS;
+    const int cl = idx % 8, k4 = (idx / 8) % (NR / 4), ch = idx / (8 * (NR / 4));
+    const int c = ch * 8 + cl;
+    v[u] = __ldcg(reinterpret_cast<const float4 *>(src + (size_t)(r0 + 4 * k4) + (size_t)c * ld));
+  }
+#pragma unroll
+  for (int u = 0; u < PER; ++u) {
+    const int idx = threadIdx.x + u * TQR_THREADS;
+    const int cl = idx % 8, k4 = (idx / 8) % (NR / 4), ch = idx / (8 * (NR / 4));
+    put_split4(hi, lo, kmaj(ch * 8 + cl, 4 * k4, (NR / 4) * 128), v[u]);
+  }
+}
+
+// [A1; A2] := Q^T [A1; A2] for the 128 columns at A1, A2 (column-major):
+// A1 rows [0, k), A2 m2 rows (m2 = 128 or 256), V m2 x k, T 32 x k (blocks of
+// 32 columns), k a multiple of 32; A2, V 16-byte aligned with leading
+// dimensions multiples of 4.  256 threads; TMEM columns [0, 256) at tmem
+// (D1: [0, 32), D2: [128, 256)).  Returns false if an MMA completion wait
+// timed out.
+__device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2, int lda2, const float *V, int ldv,
+                            const float *T, int ldt, uint32_t tmem, uint64_t *bar, uint32_t *phase,
+                            unsigned char *smem) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  unsigned char *aHi = smem, *aLo = smem + kBufA, *bHi = smem + 2 * kBufA, *bLo = bHi + kBufB;
+  float *Ts = reinterpret_cast<float *>(bLo + kBufB);     // 32 x 33
+  const uint32_t id1 = idesc_tf32(128, kIb), id2 = idesc_tf32(128, kChunk);
+  const uint32_t d1 = tmem, d2 = tmem + 128;
+  const int nh = m2 / 128;
+  for (int b = 0; b < k / kIb; ++b) {
+    const float *Vb = V + (size_t)b * kIb * ldv;
+    // ---- GEMM1: D1[c][p] = sum_r A2[r][c] V_b[r][p], K chunks of 64 rows ----
+    for (int q = 0; q < m2 / kKc; ++q) {
+      stage_kmajor<kChunk, kKc>(A2, lda2, q * kKc, aHi, aLo);
+      stage_kmajor<kIb, kKc>(Vb, ldv, q * kKc, bHi, bLo);
+      to_async_proxy();
+      const bool ok = run_mma([&] {
+        for (int ks = 0; ks < kKc / 8; ++ks) {
+          const uint32_t o = ks * 256;
+          const uint64_t ah = sdesc(saddr(aHi) + o, 128, (kKc / 4) * 128), al = sdesc(saddr(aLo) + o, 128, (kKc / 4) * 128);
+          const uint64_t bh = sdesc(saddr(bHi) + o, 128, (kKc / 4) * 128), bl = sdesc(saddr(bLo) + o, 128, (kKc / 4) * 128);
+          const uint32_t first = (q == 0 && ks == 0) ? 0u : 1u;
+          mma(d1, ah, bh, id1, first);
+          mma(d1, ah, bl, id1, 1u);
+          mma(d1, al, bh, id1, 1u);
+        }
+      }, bar, phase);
+      if (!ok) return false;
+    }
+    // T block (upper triangle) to shared memory
+    for (int idx = tid; idx < kIb * kIb; idx += TQR_THREADS) {
+      const int r = idx % kIb, c = idx / kIb;
+      Ts[r + c * 33] = (r <= c) ? __ldcg(T + (size_t)r + (size_t)(b * kIb + c) * ldt) : 0.0f;
+    }
+    __syncthreads();
+    // ---- W = T^T (A1_b + D1^T); A1_b -= W; W (split) -> B operand of GEMM2 ----
+    if (warp < 4) {
+      const int c = warp * 32 + lane;
+      float w[32];
+      ld32(d1 + ((uint32_t)(warp * 32) << 16), w);
+      float *a1 = A1 + (size_t)b * kIb + (size_t)c * lda1;
+#pragma unroll
+      for (int p = 0; p < 32; ++p) w[p] += __ldcg(a1 + p);
+      // W := T^T W in place, last row first (row p reads rows q <= p, not yet overwritten)
+#pragma unroll
+      for (int p = 31; p >= 0; --p) {
+        float s = 0.0f;
+#pragma unroll
+        for (int qq = 0; qq <= p; ++qq) s = fmaf(Ts[qq + p * 33], w[qq], s);
+        w[p] = s;
+      }
+#pragma unroll
+      for (int p = 0; p < 32; ++p) a1[p] -= w[p];
+#pragma unroll
+      for (int p4 = 0; p4 < 8; ++p4)
+        put_split4(bHi, bLo, kmaj(c, 4 * p4, (kIb / 4) * 128),
+                   make_float4(w[4 * p4], w[4 * p4 + 1], w[4 * p4 + 2], w[4 * p4 + 3]));
+    }
+    // V_b as the A operand of GEMM2: row-of-operand = row r, K = p (strided in
+    // memory: four loads along r, four 4-byte stores)
+    {
+      constexpr int PER = 256 * kIb / 4 / TQR_THREADS;   // for m2 = 256; fewer active for 128
+      float4 v[PER];
+#pragma unroll
+      for (int u = 0; u < PER; ++u) {
+        const int idx = tid + u * TQR_THREADS;
+        const int r4 = idx % 64, p = idx / 64;
+        v[u] = (4 * r4 < m2) ? __ldcg(reinterpret_cast<const float4 *>(Vb + (size_t)(4 * r4) + (size_t)p * ldv))
+                             : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < PER; ++u) {
+        const int idx = tid + u * TQR_THREADS;
+        const int r4 = idx % 64, p = idx / 64;
+        if (4 * r4 < m2) {
+          put_split(aHi, aLo, kmaj(4 * r4 + 0, p, (kIb / 4) * 128), v[u].x);
+          put_split(aHi, aLo, kmaj(4 * r4 + 1, p, (kIb / 4) * 128), v[u].y);
+          put_split(aHi, aLo, kmaj(4 * r4 + 2, p, (kIb / 4) * 128), v[u].z);
+          put_split(aHi, aLo, kmaj(4 * r4 + 3, p, (kIb / 4) * 128), v[u].w);
+        }
+      }
+    }
+    to_async_proxy();
+    // ---- GEMM2 per 128-row half: D2[r][c] = sum_p V_b[128 h + r][p] W[p][c]; A2 -= D2 ----
+    for (int h = 0; h < nh; ++h) {
+      const bool ok2 = run_mma([&] {
+        const uint32_t ao = h * 128 * 128;   // 16 row groups x 1024 B per half
+        for (int ks = 0; ks < kIb / 8; ++ks) {
+          const uint32_t o = ks * 256;
+          const uint64_t ah = sdesc(saddr(aHi) + ao + o, 128, 1024), al = sdesc(saddr(aLo) + ao + o, 128, 1024);
+          const uint64_t bh = sdesc(saddr(bHi) + o, 128, 1024), bl = sdesc(saddr(bLo) + o, 128, 1024);
+          mma(d2, ah, bh, id2, ks == 0 ? 0u : 1u);
+          mma(d2, ah, bl, id2, 1u);
+          mma(d2, al, bh, id2, 1u);
+        }
+      }, bar, phase);
+      if (!ok2) return false;
+      // warps w and w + 4 share TMEM lane quarter w % 4 and split the columns
+      const int qtr = warp % 4, half_cols = warp / 4;
+      const int r = h * 128 + qtr * 32 + lane;
+#pragma unroll 1
+      for (int cc = half_cols * 4; cc < half_cols * 4 + 4; ++cc) {
+        float v[16];
+        ld16(d2 + ((uint32_t)(qtr * 32) << 16) + (uint32_t)cc * 16, v);
+        float old[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) old[j] = __ldcg(A2 + (size_t)r + (size_t)(cc * 16 + j) * lda2);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) A2[(size_t)r + (size_t)(cc * 16 + j) * lda2] = old[j] - v[j];
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    }
+  }
+  return true;
+}
+
+}  // namespace tc
+}  // namespace tqr

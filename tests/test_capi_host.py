@@ -148,3 +148,12 @@ def test_tree_task_graph_shape_limits(L):
     assert L.tqr_tile_tree_dag_worksize(100, 100, 64, 8, 0, ctypes.byref(size)) == -1      # ib not a multiple of 16
     assert L.tqr_tile_tree_dag_worksize(100, 100, 512, 32, 0, ctypes.byref(size)) == -1    # nb > 256
     assert L.tqr_tile_tree_dag_worksize(1024, 256, 256, 32, 0, ctypes.byref(size)) == 0 and size.value > 0
+
+
+@pytest.mark.parametrize("m,n,nrhs", [(1024, 1024, 0), (4096, 1024, 4), (32768, 4096, 4), (512, 1024, 0)])
+def test_tensor_core_dag_schedule_replays(L, m, n, nrhs):
+    """The FP32 schedule with 128-column tensor-core tsmqr tasks: every wait
+    target equals the number of writers before the task in program order."""
+    nt = ctypes.c_longlong(0)
+    assert L.tqr_tile_dag_check_tc(m, n, nrhs, 256, 32, ctypes.byref(nt)) == 0
+    assert nt.value > 0
