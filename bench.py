@@ -44,7 +44,7 @@ def parse():
     p.add_argument("--n", type=int, default=8192, help="matrix order (default: the 8192^2 workload)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--kernel", default=None, choices=["tsmqr", "tsmqr_tc", "tsqrt", "geqrt"],
+    p.add_argument("--kernel", default=None, choices=["tsmqr", "tsmqr_tc", "tsqrt", "geqrt", "tile"],
                    help="time one tile kernel alone (for profiling) instead of the workload")
     p.add_argument("--dtype", default="f64", choices=["f64", "f32"], help="element type for --kernel")
     p.add_argument("--no-ls", action="store_true", help="skip the least-squares comparison")
@@ -74,7 +74,19 @@ def kernel_bench(args):
     g = torch.Generator(device="cuda").manual_seed(SEED)
     n = args.n
     res = {}
-    if args.kernel == "tsmqr_tc":
+    if args.kernel == "tile":
+        # the persistent tile QR of an n x n matrix in the chosen precision
+        # (FP32: its tsmqr updates on the tensor cores)
+        dt = torch.float32 if args.dtype == "f32" else torch.float64
+        A0 = tq.empty(n, n, dtype=dt)
+        A0.copy_(torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda"))
+        A = tq.empty(n, n, dtype=dt)
+
+        def run():
+            A.copy_(A0)
+            tq.tile_geqrf(A, NB, IB)
+        fl = flops_square(n)
+    elif args.kernel == "tsmqr_tc":
         # tensor-core FP32 tsmqr ('L', 'C') on the same band as --kernel tsmqr --dtype f32
         import ctypes
         from tileqr import _lib

@@ -374,6 +374,9 @@ int tqr_stsmqr_tc(int m1, int n, int m2, int k, float *A1, int lda1, float *A2, 
  * strips only), (1) back on; returns the previous setting.
  * tqr_tile_dag_check_tc: host replay check of that schedule. */
 int tqr_tile_dag_tensor_cores(int on);
+/* Resident CTAs per SM and dynamic shared memory of the persistent tile
+ * kernel at nb = 256, ib = 32 (dtype_bytes 8 or 4; tensor_cores for FP32). */
+int tqr_tile_dag_occupancy(int dtype_bytes, int tensor_cores, int *ctas_per_sm, int *smem_bytes);
 int tqr_tile_dag_check_tc(int m, int n, int nrhs, int nb, int ib, long long *ntasks);
 
 /* ---- Measurement hooks (no counterpart in NextLA; used by the benchmark) ----

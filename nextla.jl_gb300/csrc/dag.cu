@@ -227,8 +227,9 @@ struct TcState {
   uint32_t phase;
 };
 
-// Runs one task; false only if a TC task's tensor-core wait gave up.
-template <typename R, int NW>
+// Runs one task; false only if a TC task's tensor-core wait gave up.  TC:
+// this instantiation carries the tensor-core task (FP32 only).
+template <typename R, int NW, bool TC>
 __device__ bool run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *smem, TcState *tcs) {
   const DagGeom &g = a.g;
   const int nb = g.nb, ib = g.ib;
@@ -251,7 +252,7 @@ __device__ bool run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *
     return true;
   }
   if (it.type == IT_TC) {
-    if constexpr (std::is_same<R, float>::value) {
+    if constexpr (TC && std::is_same<R, float>::value) {
       unsigned char *al = smem + ((1024 - (tc::saddr(smem) & 1023)) & 1023);
       const size_t c0 = (size_t)s * tc::kChunk;
       return tc::tsmqr_chunk(nb, nb, tile(k, j) + c0 * a.lda, a.lda, tile(i, j) + c0 * a.lda, a.lda, tile(i, k),
@@ -308,7 +309,7 @@ __device__ bool run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *
   return true;
 }
 
-template <typename R, int NW>
+template <typename R, int NW, bool TC>
 __global__ void __launch_bounds__(TQR_THREADS, 2)
 k_tile_dag(const DagArgs<R> a)
 {
@@ -327,9 +328,9 @@ k_tile_dag(const DagArgs<R> a)
   }
   TcState tcs{0u, &s_bar, 0u};
   bool tc_failed = false;
-  if constexpr (std::is_same<R, float>::value) {
+  if constexpr (TC && std::is_same<R, float>::value) {
     if (a.g.tc) {
-      // one mbarrier and 256 TMEM columns per CTA (two CTAs per SM share TMEM)
+      // one mbarrier and 256 TMEM columns per CTA
       if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::saddr(&s_bar)));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -378,7 +379,7 @@ k_tile_dag(const DagArgs<R> a)
     }
     __syncthreads();
     if (s_err) break;
-    if (!run_item<R, NW>(a, it, smem_raw, &tcs)) {
+    if (!run_item<R, NW, TC>(a, it, smem_raw, &tcs)) {
       // a tensor-core completion wait gave up: report, then stop this CTA
       if (tid == 0 && atomicCAS(&a.hdr->error, 0, 3) == 0) {
         a.hdr->err_item = idx;
@@ -398,7 +399,7 @@ k_tile_dag(const DagArgs<R> a)
       for (int u = 0; u < nu; ++u) atomicAdd(a.cnt + c[u], 1);
     }
   }
-  if constexpr (std::is_same<R, float>::value) {
+  if constexpr (TC && std::is_same<R, float>::value) {
     if (a.g.tc) {
       // after a failed wait, one more bounded wait for the outstanding commit
       if (tc_failed) tc::bar_wait(&s_bar, tcs.phase ^ 1u);
@@ -622,22 +623,22 @@ static std::shared_ptr<Plan> get_plan(const DagGeom &g) {
   return p;
 }
 
-template <typename R, int NW>
+template <typename R, int NW, bool TC = false>
 static int launch_dag(const DagArgs<R> &a, size_t sm, double flops, cudaStream_t st, bool timed = true) {
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(k_tile_dag<R, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) !=
+  if ((e = cudaFuncSetAttribute(k_tile_dag<R, NW, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) !=
       cudaSuccess)
     return (int)e;
   int dev = 0, sms = 0, per_sm = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return (int)e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return (int)e;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_dag<R, NW>, TQR_THREADS, sm)) !=
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_dag<R, NW, TC>, TQR_THREADS, sm)) !=
       cudaSuccess)
     return (int)e;
   if (per_sm < 1) return (int)cudaErrorInvalidConfiguration;
   const int grid = std::min(sms * per_sm, a.nitems);
   void *tok = timed ? prof_begin(st) : nullptr;
-  k_tile_dag<R, NW><<<grid, TQR_THREADS, sm, st>>>(a);
+  k_tile_dag<R, NW, TC><<<grid, TQR_THREADS, sm, st>>>(a);
   if (timed) prof_end(tok, st, flops);
   count_launch();
   e = cudaGetLastError();
@@ -694,6 +695,9 @@ static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int
   if (g.tc) sm = std::max(sm, tc::kSmem);
   const double mn = (double)std::max(m, n), kn = (double)std::min(m, n);
   const double flops = 2.0 * mn * kn * kn - 2.0 * kn * kn * kn / 3.0;
+  if constexpr (std::is_same<R, float>::value) {
+    if (g.tc) return launch_dag<R, 16, true>(a, sm, flops, st);
+  }
   return g.nw == 16 ? launch_dag<R, 16>(a, sm, flops, st) : launch_dag<R, 8>(a, sm, flops, st);
 }
 
@@ -898,6 +902,41 @@ int tqr_tile_dag_check_rhs(int m, int n, int nrhs, int nb, int ib, long long *nt
   const bool ok = build_schedule(g, items, true);
   if (ntasks) *ntasks = (long long)items.size();
   return ok ? 0 : 2;
+}
+
+int tqr_tile_dag_occupancy(int dtype_bytes, int tensor_cores, int *ctas_per_sm, int *smem_bytes) {
+  if ((dtype_bytes != 4 && dtype_bytes != 8) || !ctas_per_sm || !smem_bytes) return -1;
+  const int nb = 256, ib = 32;
+  size_t sm = 0;
+  cudaError_t e;
+  int per = 0;
+  if (dtype_bytes == 8) {
+    sm = std::max({apply_smem_elems(nb, ib, 16, true, true, true) * sizeof(double), panel_smem<double>(nb, ib, true, true),
+                   tsqrt_smem<double>(nb, ib, true)});
+    if ((e = cudaFuncSetAttribute(k_tile_dag<double, 16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sm)) != cudaSuccess)
+      return (int)e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tile_dag<double, 16, false>, TQR_THREADS, sm);
+  } else {
+    sm = std::max({apply_smem_elems(nb, ib, 16, true, true, true) * sizeof(float), panel_smem<float>(nb, ib, true, true),
+                   tsqrt_smem<float>(nb, ib, true)});
+    if (tensor_cores) {
+      sm = std::max(sm, tc::kSmem);
+      if ((e = cudaFuncSetAttribute(k_tile_dag<float, 16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sm)) != cudaSuccess)
+        return (int)e;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tile_dag<float, 16, true>, TQR_THREADS, sm);
+    } else {
+      if ((e = cudaFuncSetAttribute(k_tile_dag<float, 16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sm)) != cudaSuccess)
+        return (int)e;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tile_dag<float, 16, false>, TQR_THREADS, sm);
+    }
+  }
+  if (e != cudaSuccess) return (int)e;
+  *ctas_per_sm = per;
+  *smem_bytes = (int)sm;
+  return 0;
 }
 
 int tqr_tile_dag_tensor_cores(int on) {
