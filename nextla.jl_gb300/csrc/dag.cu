@@ -223,8 +223,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // Per-CTA tensor-core state of the TC tasks (FP32 only).
 struct TcState {
   uint32_t tmem;
-  uint64_t *bar;
-  uint32_t phase;
+  uint64_t *bars;                 // tc::kBars mbarriers
+  uint32_t phase[tc::kBars];
 };
 
 // Runs one task; false only if a TC task's tensor-core wait gave up.  TC:
@@ -256,7 +256,7 @@ __device__ bool run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *
       unsigned char *al = smem + ((1024 - (tc::saddr(smem) & 1023)) & 1023);
       const size_t c0 = (size_t)s * tc::kChunk;
       return tc::tsmqr_chunk(nb, nb, tile(k, j) + c0 * a.lda, a.lda, tile(i, j) + c0 * a.lda, a.lda, tile(i, k),
-                             a.lda, ttile(i, k), a.ldt, tcs->tmem, tcs->bar, &tcs->phase, al);
+                             a.lda, ttile(i, k), a.ldt, tcs->tmem, tcs->bars, tcs->phase, al);
     } else {
       return false;
     }
@@ -310,14 +310,14 @@ __device__ bool run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *
 }
 
 template <typename R, int NW, bool TC>
-__global__ void __launch_bounds__(TQR_THREADS, 2)
+__global__ void __launch_bounds__(TQR_THREADS, TC ? 1 : 2)
 k_tile_dag(const DagArgs<R> a)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_it, s_err;
   const int tid = threadIdx.x;
   __shared__ unsigned long long s_tstart;
-  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ __align__(8) uint64_t s_bars[tc::kBars];
   __shared__ uint32_t s_tmem;
   bool first = true;
   if (tid == 0) s_err = (a.hdr->key != a.key || a.hdr->nitems != a.nitems) ? 2 : 0;
@@ -326,13 +326,14 @@ k_tile_dag(const DagArgs<R> a)
     if (tid == 0 && blockIdx.x == 0) atomicExch(&a.hdr->error, 2);
     return;
   }
-  TcState tcs{0u, &s_bar, 0u};
+  TcState tcs{0u, s_bars, {0u, 0u, 0u}};
   bool tc_failed = false;
   if constexpr (TC && std::is_same<R, float>::value) {
     if (a.g.tc) {
-      // one mbarrier and 256 TMEM columns per CTA
+      // the tensor-core task's mbarriers and all TMEM columns (one CTA per SM)
       if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::saddr(&s_bar)));
+        for (int q = 0; q < tc::kBars; ++q)
+          asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::saddr(&s_bars[q])));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
       }
       if ((tid >> 5) == 0) {
@@ -401,8 +402,12 @@ k_tile_dag(const DagArgs<R> a)
   }
   if constexpr (TC && std::is_same<R, float>::value) {
     if (a.g.tc) {
-      // after a failed wait, one more bounded wait for the outstanding commit
-      if (tc_failed) tc::bar_wait(&s_bar, tcs.phase ^ 1u);
+      // after a failed wait: one more commit (it arrives once every earlier
+      // MMA has completed) and one bounded wait for it
+      if (tc_failed) {
+        if (tid == 0) tc::commit(&s_bars[2]);
+        tc::bar_wait(&s_bars[2], tcs.phase[2]);
+      }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");

@@ -6,10 +6,10 @@
 
 namespace tqr {
 
-// TMEM allocation / release and the MMA mbarrier for one CTA.
-__device__ __forceinline__ void tc_setup(uint64_t *bar, uint32_t *tmem_slot) {
+// TMEM allocation / release and the MMA mbarriers for one CTA.
+__device__ __forceinline__ void tc_setup(uint64_t *bars, uint32_t *tmem_slot) {
   if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::saddr(bar)));
+    for (int i = 0; i < tc::kBars; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::saddr(&bars[i])));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if ((threadIdx.x >> 5) == 0) {
@@ -22,10 +22,13 @@ __device__ __forceinline__ void tc_setup(uint64_t *bar, uint32_t *tmem_slot) {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// After a failed wait: one more bounded wait for the outstanding commit, then
-// release TMEM.  After success: release TMEM.
-__device__ __forceinline__ void tc_teardown(uint64_t *bar, uint32_t phase, bool failed, uint32_t tmem) {
-  if (failed) tc::bar_wait(bar, phase);
+// After a failed wait, one more commit (it arrives once every earlier MMA of
+// this thread has completed) and one bounded wait for it; then release TMEM.
+__device__ __forceinline__ void tc_teardown(uint64_t *bars, uint32_t *phase, bool failed, uint32_t tmem) {
+  if (failed) {
+    if (threadIdx.x == 0) tc::commit(&bars[2]);
+    tc::bar_wait(&bars[2], phase[2]);
+  }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -37,17 +40,17 @@ __global__ void __launch_bounds__(TQR_THREADS, 1)
 k_tsmqr_tc(int m2, int k, float *A1, int lda1, float *A2, int lda2, const float *V, int ldv, const float *T, int ldt,
            int *err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t bar;
+  __shared__ __align__(8) uint64_t bars[tc::kBars];
   __shared__ uint32_t tmem_slot;
   unsigned char *smem = smem_raw + ((1024 - (tc::saddr(smem_raw) & 1023)) & 1023);
-  tc_setup(&bar, &tmem_slot);
+  tc_setup(bars, &tmem_slot);
   const uint32_t tmem = tmem_slot;
-  uint32_t phase = 0;
+  uint32_t phase[tc::kBars] = {0u, 0u, 0u};
   const size_t c0 = (size_t)blockIdx.x * tc::kChunk;
-  const bool ok = tc::tsmqr_chunk(m2, k, A1 + c0 * lda1, lda1, A2 + c0 * lda2, lda2, V, ldv, T, ldt, tmem, &bar,
-                                  &phase, smem);
+  const bool ok = tc::tsmqr_chunk(m2, k, A1 + c0 * lda1, lda1, A2 + c0 * lda2, lda2, V, ldv, T, ldt, tmem, bars,
+                                  phase, smem);
   if (!ok && threadIdx.x == 0) atomicExch(err, 1);
-  tc_teardown(&bar, phase ^ 1u, !ok, tmem);
+  tc_teardown(bars, phase, !ok, tmem);
 }
 
 }  // namespace tqr
@@ -69,7 +72,7 @@ int tqr_stsmqr_tc(int m1, int n, int m2, int k, float *A1, int lda1, float *A2, 
   if (!T || ldt < tc::kIb) return -12;
   if (((uintptr_t)A2 & 15) || (lda2 & 3) || ((uintptr_t)V & 15) || (ldv & 3)) return -8;   // float4 staging
   if (!err) return -13;
-  // two CTAs per SM at most (2 x 256 TMEM columns = all of TMEM)
+  // kernels that use TMEM run one CTA per SM: all of TMEM and shared memory
   const size_t sm = tc::kSmem;
   cudaError_t e = cudaFuncSetAttribute(k_tsmqr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return (int)e;

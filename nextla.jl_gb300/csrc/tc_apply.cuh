@@ -18,10 +18,11 @@
 // rows x 16 bytes per core matrix, consecutive K groups 128 bytes apart (the
 // leading byte offset), consecutive 8-row groups SBO bytes apart.
 //
-// The caller owns the TMEM allocation (kTmemCols columns at tmem) and the
-// mbarrier (initialised with count 1; *phase tracks its parity).  Every
-// mbarrier wait is bounded: on expiry the routine records the failure in
-// *err and returns (no further MMA is issued).
+// The caller owns the TMEM allocation (kTmemCols columns at tmem) and kBars
+// mbarriers (initialised with count 1; phase[] tracks their parities).
+// Every mbarrier wait is bounded: on expiry the routine returns false and
+// issues no further MMA.  Kernels that use TMEM run one CTA per SM, so the
+// routine has the SM's TMEM and up to 227 KB of shared memory to itself.
 #pragma once
 #include "common.cuh"
 
@@ -31,11 +32,14 @@ namespace tc {
 constexpr int kChunk = 128;            // chunk columns (GEMM1 M, GEMM2 N)
 constexpr int kIb = 32;                // reflectors per block (GEMM1 N, GEMM2 K)
 constexpr int kKc = 64;                // GEMM1 K chunk (rows of A2 staged at once)
-constexpr int kTmemCols = 256;         // D1: columns [0, 32); D2 (one 128-row half at a time): [128, 256)
-// dynamic shared memory: A operand hi/lo (2 x 32 KB), B operand hi/lo
-// (2 x 16 KB), T block (32 x 33 floats)
-constexpr size_t kBufA = 32768, kBufB = 16384;
-constexpr size_t kSmem = 2 * kBufA + 2 * kBufB + sizeof(float) * 32 * 33 + 1024;
+constexpr int kTmemCols = 512;         // D1: columns [0, 32); D2 halves: [128, 256) and [256, 384)
+// dynamic shared memory: two GEMM1 stage buffers, each A hi/lo (2 x 32 KB) and
+// B hi/lo (2 x 8 KB); GEMM2 reuses them (V_b hi/lo in stage 0's A, W hi/lo
+// in stage 1's A); then the T block (32 x 33 floats)
+constexpr size_t kBufA = 32768, kBufB = 8192;
+constexpr size_t kStage = 2 * kBufA + 2 * kBufB;
+constexpr size_t kSmem = 2 * kStage + sizeof(float) * 32 * 33 + 1024;
+constexpr int kBars = 3;               // GEMM1 stage 0, GEMM1 stage 1, GEMM2
 constexpr long kWaitLimit = 1L << 26;  // mbarrier polls before giving up
 
 __device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -124,6 +128,15 @@ __device__ __forceinline__ void to_async_proxy() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
+// Waits (all threads) for the next phase of barrier `bar`; the same verdict
+// in every thread.
+__device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t *phase) {
+  const bool ok = __syncthreads_and(bar_wait(bar, *phase)) != 0;
+  *phase ^= 1u;
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  return ok;
+}
+
 // Issue (thread 0), commit and wait (all threads); false if the wait gave up.
 template <typename F>
 __device__ __forceinline__ bool run_mma(F issue, uint64_t *bar, uint32_t *phase) {
@@ -177,38 +190,50 @@ __device__ __forceinline__ void stage_kmajor(const float *src, int ld, int r0, u
 // [A1; A2] := Q^T [A1; A2] for the 128 columns at A1, A2 (column-major):
 // A1 rows [0, k), A2 m2 rows (m2 = 128 or 256), V m2 x k, T 32 x k (blocks of
 // 32 columns), k a multiple of 32; A2, V 16-byte aligned with leading
-// dimensions multiples of 4.  256 threads; TMEM columns [0, 256) at tmem
-// (D1: [0, 32), D2: [128, 256)).  Returns false if an MMA completion wait
-// timed out.
+// dimensions multiples of 4.  256 threads; all kTmemCols TMEM columns at
+// tmem; bars[kBars] mbarriers (count 1) with parities phase[kBars].  Returns
+// false if an MMA completion wait timed out (the caller then waits once more
+// on every barrier with a pending phase before releasing TMEM).
 __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2, int lda2, const float *V, int ldv,
-                            const float *T, int ldt, uint32_t tmem, uint64_t *bar, uint32_t *phase,
-                            unsigned char *smem) {
+                                   const float *T, int ldt, uint32_t tmem, uint64_t *bars, uint32_t *phase,
+                                   unsigned char *smem) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  unsigned char *aHi = smem, *aLo = smem + kBufA, *bHi = smem + 2 * kBufA, *bLo = bHi + kBufB;
-  float *Ts = reinterpret_cast<float *>(bLo + kBufB);     // 32 x 33
+  unsigned char *st_base[2] = {smem, smem + kStage};
+  float *Ts = reinterpret_cast<float *>(smem + 2 * kStage);     // 32 x 33
+  // GEMM2 operands in the stage buffers' A regions
+  unsigned char *vHi = smem, *vLo = smem + kBufA;                 // V_b: 256 x 32, K-major
+  unsigned char *wHi = smem + kStage, *wLo = smem + kStage + kBufA;  // W: 128 x 32, K-major
   const uint32_t id1 = idesc_tf32(128, kIb), id2 = idesc_tf32(128, kChunk);
-  const uint32_t d1 = tmem, d2 = tmem + 128;
-  const int nh = m2 / 128;
+  const uint32_t d1 = tmem;
+  const int nh = m2 / 128, nq = m2 / kKc;
+  constexpr uint32_t SB = (kKc / 4) * 128;
   for (int b = 0; b < k / kIb; ++b) {
     const float *Vb = V + (size_t)b * kIb * ldv;
-    // ---- GEMM1: D1[c][p] = sum_r A2[r][c] V_b[r][p], K chunks of 64 rows ----
-    for (int q = 0; q < m2 / kKc; ++q) {
+    // ---- GEMM1: D1[c][p] = sum_r A2[r][c] V_b[r][p], K chunks of 64 rows,
+    //      staging of chunk q + 1 overlapping the MMAs of chunk q ----
+    for (int q = 0; q < nq; ++q) {
+      const int sbuf = q & 1;
+      if (q >= 2 && !wait_phase(&bars[sbuf], &phase[sbuf])) return false;   // chunk q - 2 done with it
+      unsigned char *aHi = st_base[sbuf], *aLo = aHi + kBufA, *bHi = aHi + 2 * kBufA, *bLo = bHi + kBufB;
       stage_kmajor<kChunk, kKc>(A2, lda2, q * kKc, aHi, aLo);
       stage_kmajor<kIb, kKc>(Vb, ldv, q * kKc, bHi, bLo);
       to_async_proxy();
-      const bool ok = run_mma([&] {
+      if (tid == 0) {
         for (int ks = 0; ks < kKc / 8; ++ks) {
           const uint32_t o = ks * 256;
-          const uint64_t ah = sdesc(saddr(aHi) + o, 128, (kKc / 4) * 128), al = sdesc(saddr(aLo) + o, 128, (kKc / 4) * 128);
-          const uint64_t bh = sdesc(saddr(bHi) + o, 128, (kKc / 4) * 128), bl = sdesc(saddr(bLo) + o, 128, (kKc / 4) * 128);
+          const uint64_t ah = sdesc(saddr(aHi) + o, 128, SB), al = sdesc(saddr(aLo) + o, 128, SB);
+          const uint64_t bh = sdesc(saddr(bHi) + o, 128, SB), bl = sdesc(saddr(bLo) + o, 128, SB);
           const uint32_t first = (q == 0 && ks == 0) ? 0u : 1u;
           mma(d1, ah, bh, id1, first);
           mma(d1, ah, bl, id1, 1u);
           mma(d1, al, bh, id1, 1u);
         }
-      }, bar, phase);
-      if (!ok) return false;
+        commit(&bars[sbuf]);
+      }
     }
+    // the last two chunks' commits (one per stage buffer) are still pending
+    for (int q = (nq >= 2 ? nq - 2 : 0); q < nq; ++q)
+      if (!wait_phase(&bars[q & 1], &phase[q & 1])) return false;
     // T block (upper triangle) to shared memory
     for (int idx = tid; idx < kIb * kIb; idx += TQR_THREADS) {
       const int r = idx % kIb, c = idx / kIb;
@@ -235,13 +260,13 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
       for (int p = 0; p < 32; ++p) a1[p] -= w[p];
 #pragma unroll
       for (int p4 = 0; p4 < 8; ++p4)
-        put_split4(bHi, bLo, kmaj(c, 4 * p4, (kIb / 4) * 128),
+        put_split4(wHi, wLo, kmaj(c, 4 * p4, (kIb / 4) * 128),
                    make_float4(w[4 * p4], w[4 * p4 + 1], w[4 * p4 + 2], w[4 * p4 + 3]));
     }
     // V_b as the A operand of GEMM2: row-of-operand = row r, K = p (strided in
     // memory: four loads along r, four 4-byte stores)
     {
-      constexpr int PER = 256 * kIb / 4 / TQR_THREADS;   // for m2 = 256; fewer active for 128
+      constexpr int PER = 256 * kIb / 4 / TQR_THREADS;
       float4 v[PER];
 #pragma unroll
       for (int u = 0; u < PER; ++u) {
@@ -255,45 +280,51 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
         const int idx = tid + u * TQR_THREADS;
         const int r4 = idx % 64, p = idx / 64;
         if (4 * r4 < m2) {
-          put_split(aHi, aLo, kmaj(4 * r4 + 0, p, (kIb / 4) * 128), v[u].x);
-          put_split(aHi, aLo, kmaj(4 * r4 + 1, p, (kIb / 4) * 128), v[u].y);
-          put_split(aHi, aLo, kmaj(4 * r4 + 2, p, (kIb / 4) * 128), v[u].z);
-          put_split(aHi, aLo, kmaj(4 * r4 + 3, p, (kIb / 4) * 128), v[u].w);
+          put_split(vHi, vLo, kmaj(4 * r4 + 0, p, (kIb / 4) * 128), v[u].x);
+          put_split(vHi, vLo, kmaj(4 * r4 + 1, p, (kIb / 4) * 128), v[u].y);
+          put_split(vHi, vLo, kmaj(4 * r4 + 2, p, (kIb / 4) * 128), v[u].z);
+          put_split(vHi, vLo, kmaj(4 * r4 + 3, p, (kIb / 4) * 128), v[u].w);
         }
       }
     }
     to_async_proxy();
-    // ---- GEMM2 per 128-row half: D2[r][c] = sum_p V_b[128 h + r][p] W[p][c]; A2 -= D2 ----
-    for (int h = 0; h < nh; ++h) {
-      const bool ok2 = run_mma([&] {
+    // ---- GEMM2, both 128-row halves at once: D2_h[r][c] = sum_p V_b[128 h + r][p] W[p][c] ----
+    const bool ok2 = run_mma([&] {
+      for (int h = 0; h < nh; ++h) {
         const uint32_t ao = h * 128 * 128;   // 16 row groups x 1024 B per half
+        const uint32_t d2 = tmem + 128 + (uint32_t)h * 128;
         for (int ks = 0; ks < kIb / 8; ++ks) {
           const uint32_t o = ks * 256;
-          const uint64_t ah = sdesc(saddr(aHi) + ao + o, 128, 1024), al = sdesc(saddr(aLo) + ao + o, 128, 1024);
-          const uint64_t bh = sdesc(saddr(bHi) + o, 128, 1024), bl = sdesc(saddr(bLo) + o, 128, 1024);
+          const uint64_t ah = sdesc(saddr(vHi) + ao + o, 128, 1024), al = sdesc(saddr(vLo) + ao + o, 128, 1024);
+          const uint64_t bh = sdesc(saddr(wHi) + o, 128, 1024), bl = sdesc(saddr(wLo) + o, 128, 1024);
           mma(d2, ah, bh, id2, ks == 0 ? 0u : 1u);
           mma(d2, ah, bl, id2, 1u);
           mma(d2, al, bh, id2, 1u);
         }
-      }, bar, phase);
-      if (!ok2) return false;
-      // warps w and w + 4 share TMEM lane quarter w % 4 and split the columns
-      const int qtr = warp % 4, half_cols = warp / 4;
-      const int r = h * 128 + qtr * 32 + lane;
-#pragma unroll 1
-      for (int cc = half_cols * 4; cc < half_cols * 4 + 4; ++cc) {
-        float v[16];
-        ld16(d2 + ((uint32_t)(qtr * 32) << 16) + (uint32_t)cc * 16, v);
-        float old[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) old[j] = __ldcg(A2 + (size_t)r + (size_t)(cc * 16 + j) * lda2);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) A2[(size_t)r + (size_t)(cc * 16 + j) * lda2] = old[j] - v[j];
       }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    }, &bars[2], &phase[2]);
+    if (!ok2) return false;
+    // ---- A2 -= D2: warps 0-3 the first half, warps 4-7 the second ----
+    {
+      const int h = warp / 4, qtr = warp % 4;
+      if (h < nh) {
+        const int r = h * 128 + qtr * 32 + lane;
+        const uint32_t d2 = tmem + 128 + (uint32_t)h * 128 + ((uint32_t)(qtr * 32) << 16);
+#pragma unroll 1
+        for (int cc = 0; cc < kChunk / 16; ++cc) {
+          float v[16];
+          ld16(d2 + (uint32_t)cc * 16, v);
+          float old[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) old[j] = __ldcg(A2 + (size_t)r + (size_t)(cc * 16 + j) * lda2);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) A2[(size_t)r + (size_t)(cc * 16 + j) * lda2] = old[j] - v[j];
+        }
+      }
     }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   }
   return true;
 }
