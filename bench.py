@@ -301,9 +301,18 @@ def run_reference(args, world, rank):
 
 
 def haar(m, n, g, torch):
-    Z = torch.randn(m, n, generator=g, dtype=torch.float64, device="cuda")
-    Q, R = torch.linalg.qr(Z)
-    return Q * torch.sign(torch.diagonal(R)).unsqueeze(0)
+    """Haar-distributed m x n Q: this library's tile QR of a Gaussian matrix,
+    Q formed by the Q application, columns signed by diag(R) > 0 (no
+    dependency on torch.linalg, which cannot be loaded under the profiler)."""
+    import tileqr as tq
+    Z = tq.empty(m, n)
+    Z.copy_(torch.randn(m, n, generator=g, dtype=torch.float64, device="cuda"))
+    T, _ = tq.tile_geqrf(Z, NB, IB)
+    Q = tq.zeros(m, n)
+    Q.diagonal().fill_(1.0)
+    tq.tile_unmqr("N", Z, T, Q, NB, IB)
+    torch.cuda.synchronize()
+    return Q * torch.sign(torch.diagonal(Z)).unsqueeze(0)
 
 
 def ls_problem(m, n, k, torch, seed=SEED):

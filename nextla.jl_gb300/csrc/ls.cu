@@ -35,6 +35,21 @@ namespace tqr {
 
 constexpr int kLsMaxRhs = 16;
 
+// Exact float -> double widening with integer instructions: every FP64 warp
+// instruction occupies the SM sub-partition's FP64 pipe for ~64 cycles on
+// GB300, and a conversion is one of them; for normal numbers the IEEE fields
+// move directly (exponent rebias +896, mantissa shifted left 29).  Zeros,
+// subnormals, infinities and NaNs take the ordinary conversion.
+__device__ __forceinline__ double widen(float a) {
+  const uint32_t u = __float_as_uint(a);
+  const uint32_t e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)a;
+  const unsigned long long bits = ((unsigned long long)(u & 0x80000000u) << 32) |
+                                  ((unsigned long long)(e + 896u) << 52) |
+                                  ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
 // Y[r, c] += alpha * sum_j A[r, j] X[j, c] for K right-hand sides (a
 // compile-time count: FP64 instructions cost full pipe time even when
 // predicated off); the n columns are split over gridDim.y CTAs that add their
@@ -61,7 +76,7 @@ k_gemm_sd_n(int m, int n, const float *__restrict__ A, int lda, const double *__
     if (r < m) {
       const float *ap = A + ix(r, jb, lda);
       for (int jj = 0; jj < jn; ++jj) {
-        const double a = (double)__ldg(ap + (size_t)jj * lda);
+        const double a = widen(__ldg(ap + (size_t)jj * lda));
 #pragma unroll
         for (int c = 0; c < K; ++c) acc[c] = fma(a, Xs[jj][c], acc[c]);
       }
@@ -95,7 +110,7 @@ k_gemm_sd_t(int m, int n, const float *__restrict__ A, int lda, const double *__
     for (int c = 0; c < K; ++c) acc[c] = 0.0;
     const float *ap = A + ix(r0, j, lda);
     for (int rr = lane; rr < rn; rr += 32) {
-      const double a = (double)__ldg(ap + rr);
+      const double a = widen(__ldg(ap + rr));
 #pragma unroll
       for (int c = 0; c < K; ++c) acc[c] = fma(a, Rs[rr + c * rchunk], acc[c]);
     }
@@ -264,7 +279,7 @@ static int gemm_sd_t(int m, int n, int k, const float *A, int lda, const double 
 // Rinv_b = R_bb^-1 (FP64, upper, 256-by-256 per block, ld 256) for column
 // chunk blockIdx.y (16 columns of the identity) of block blockIdx.x.
 __global__ void __launch_bounds__(TQR_THREADS)
-k_trinv_diag(int n, const float *__restrict__ Rm, int ldr, double *__restrict__ Rinv)
+k_trinv_diag(int n, const float *__restrict__ Rm, int ldr, double *__restrict__ Rinv, double *__restrict__ RinvT)
 {
   __shared__ double x[256][17];
   __shared__ double rinv[256];
@@ -291,9 +306,12 @@ k_trinv_diag(int n, const float *__restrict__ Rm, int ldr, double *__restrict__ 
     }
     __syncthreads();
   }
+  double *outT = RinvT ? RinvT + (size_t)b * 256 * 256 : nullptr;
   for (int idx = threadIdx.x; idx < 256 * nc; idx += TQR_THREADS) {
     int r = idx % 256, c = idx / 256;
-    out[ix(r, c0 + c, 256)] = (r < nbk) ? x[r][c] : 0.0;
+    const double v = (r < nbk) ? x[r][c] : 0.0;
+    out[ix(r, c0 + c, 256)] = v;
+    if (outT) outT[ix(c0 + c, r, 256)] = v;
   }
 }
 
@@ -326,12 +344,160 @@ k_blk_solve(int trans, int nbk, int k, const double *__restrict__ Ri, const doub
   X[ix(r, c, ldx)] = s0 + s1;
 }
 
-static int trinv_diag(int n, const float *Rm, int ldr, double *Rinv, cudaStream_t st) {
+static int trinv_diag(int n, const float *Rm, int ldr, double *Rinv, double *RinvT, cudaStream_t st) {
   const int nblk = (n + 255) / 256;
-  k_trinv_diag<<<dim3(nblk, 16), TQR_THREADS, 0, st>>>(n, Rm, ldr, Rinv);
+  k_trinv_diag<<<dim3(nblk, 16), TQR_THREADS, 0, st>>>(n, Rm, ldr, Rinv, RinvT);
   count_launch();
   return (int)cudaGetLastError();
 }
+
+// ---- the same solve as one cooperative persistent launch ------------------
+// The blocked solve is a chain of 2 * n / 256 small products; launched one by
+// one they are launch- and latency-bound.  Here every CTA of one cooperative
+// grid takes rows of each step and the steps are separated by a grid
+// barrier (bounded spin, error word on timeout).
+struct GridBar {
+  int count;
+  int gen;
+  int error;
+  int pad[61];
+};
+static_assert(sizeof(GridBar) == 256, "GridBar layout");
+
+__device__ __forceinline__ int ls_ld_acquire(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// All CTAs of the grid; false (in every thread of every CTA that gets here)
+// once any wait has timed out.
+__device__ bool grid_sync(GridBar *gb, unsigned nblocks) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const int g = ls_ld_acquire(&gb->gen);
+    __threadfence();
+    if (atomicAdd(&gb->count, 1) == (int)nblocks - 1) {
+      atomicExch(&gb->count, 0);
+      __threadfence();
+      atomicAdd(&gb->gen, 1);
+    } else {
+      unsigned long long t0, t;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+      while (ls_ld_acquire(&gb->gen) == g) {
+        if (ls_ld_acquire(&gb->error)) { ok = 0; break; }
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        if (t - t0 > 2000000000ull) { atomicExch(&gb->error, 1); ok = 0; break; }
+        __nanosleep(64);
+      }
+    }
+    if (ls_ld_acquire(&gb->error)) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// X = op(R)^-1 B, op = R (trans 0, backward over the blocks) or R^T (trans
+// 1, forward).  Rinv holds R's inverted 256 x 256 diagonal blocks (ld 256)
+// and RinvT their transposes, so both directions read them along columns; B
+// is consumed.  Per step: X_b = op(Rinv_b) B_b with one warp per row (lanes
+// split the 256-term sum), then the other rows' update -- R^T: one warp per
+// row again; R: lanes over 32 consecutive rows, warps over eight 32-column
+// parts of the block, combined with FP64 atomics.
+template <int K>
+__global__ void __launch_bounds__(TQR_THREADS)
+k_trsv_coop(int trans, int n, const float *__restrict__ Rm, int ldr, const double *__restrict__ Rinv,
+            const double *__restrict__ RinvT, double *B, int ldb, double *X, int ldx, GridBar *gb) {
+  const int nblk = (n + 255) / 256;
+  const int lane = threadIdx.x & 31;
+  const int gwarp = blockIdx.x * TQR_WARPS + (threadIdx.x >> 5), nwarps = gridDim.x * TQR_WARPS;
+  for (int q = 0; q < nblk; ++q) {
+    const int b = trans ? q : nblk - 1 - q;
+    const int b0 = b * 256, nbk = min(256, n - b0);
+    // column r of M holds op(Rinv_b)[r][.]: RinvT for R (row r of Rinv_b), Rinv for R^T
+    const double *M = (trans ? Rinv : RinvT) + (size_t)b * 65536;
+    for (int r = gwarp; r < nbk; r += nwarps) {
+      double acc[K];
+#pragma unroll
+      for (int c = 0; c < K; ++c) acc[c] = 0.0;
+      const int q0 = trans ? 0 : r, q1 = trans ? r + 1 : nbk;
+      for (int qq = q0 + lane; qq < q1; qq += 32) {
+        const double a = M[ix(qq, r, 256)];
+#pragma unroll
+        for (int c = 0; c < K; ++c) acc[c] = fma(a, __ldcg(B + ix(b0 + qq, c, ldb)), acc[c]);
+      }
+#pragma unroll
+      for (int c = 0; c < K; ++c) {
+        const double v = warp_sum(acc[c]);
+        if (lane == 0) X[ix(b0 + r, c, ldx)] = v;
+      }
+    }
+    __threadfence();
+    if (!grid_sync(gb, gridDim.x)) return;
+    if (trans) {
+      // rows r >= b0 + nbk: B[r] -= sum_j R[b0 + j][r] X[b0 + j]
+      for (int r = b0 + nbk + gwarp; r < n; r += nwarps) {
+        double acc[K];
+#pragma unroll
+        for (int c = 0; c < K; ++c) acc[c] = 0.0;
+        for (int j = lane; j < nbk; j += 32) {
+          const double a = widen(Rm[ix(b0 + j, r, ldr)]);
+#pragma unroll
+          for (int c = 0; c < K; ++c) acc[c] = fma(a, __ldcg(X + ix(b0 + j, c, ldx)), acc[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < K; ++c) {
+          const double v = warp_sum(acc[c]);
+          if (lane == 0) B[ix(r, c, ldb)] -= v;
+        }
+      }
+    } else if (b0 > 0) {
+      // rows r < b0: B[r] -= sum_j R[r][b0 + j] X[b0 + j]; item = (32-row group, 32-column part)
+      const int groups = (b0 + 31) / 32, parts = (nbk + 31) / 32;
+      for (int item = gwarp; item < groups * parts; item += nwarps) {
+        const int r = (item % groups) * 32 + lane, j0 = (item / groups) * 32, j1 = min(nbk, j0 + 32);
+        if (r < b0) {
+          double acc[K];
+#pragma unroll
+          for (int c = 0; c < K; ++c) acc[c] = 0.0;
+          for (int j = j0; j < j1; ++j) {
+            const double a = widen(Rm[ix(r, b0 + j, ldr)]);
+#pragma unroll
+            for (int c = 0; c < K; ++c) acc[c] = fma(a, __ldcg(X + ix(b0 + j, c, ldx)), acc[c]);
+          }
+#pragma unroll
+          for (int c = 0; c < K; ++c) atomicAdd(B + ix(r, c, ldb), -acc[c]);
+        }
+      }
+    }
+    __threadfence();
+    if (!grid_sync(gb, gridDim.x)) return;
+  }
+}
+
+template <int K>
+static int trsv_coop_k(int trans, int n, const float *Rm, int ldr, const double *Rinv, const double *RinvT, double *B,
+                       int ldb, double *X, int ldx, GridBar *gb, cudaStream_t st) {
+  int dev = 0, sms = 0, per = 0;
+  LS_CU(cudaGetDevice(&dev));
+  LS_CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  LS_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_trsv_coop<K>, TQR_THREADS, 0));
+  if (per < 1) return (int)cudaErrorInvalidConfiguration;
+  const int grid = sms * std::min(per, 2);
+  LS_CU(cudaMemsetAsync(gb, 0, sizeof(GridBar), st));
+  void *args[] = {&trans, &n, &Rm, &ldr, &Rinv, &RinvT, &B, &ldb, &X, &ldx, &gb};
+  LS_CU(cudaLaunchCooperativeKernel((const void *)k_trsv_coop<K>, dim3(grid), dim3(TQR_THREADS), args, 0, st));
+  count_launch();
+  return 0;
+}
+
+// X = op(R)^-1 B in one cooperative launch (k = 1, 2, 4; others fall back to
+// the launch-per-step form below).
+static int trsv_coop(int trans, int n, int k, const float *Rm, int ldr, const double *Rinv, const double *RinvT,
+                     double *B, int ldb, double *X, int ldx, GridBar *gb, cudaStream_t st);
 
 // X = op(R)^-1 B for the FP32 upper R with its inverted diagonal blocks; B
 // (n-by-k) is consumed as scratch, X receives the solution.
@@ -354,6 +520,16 @@ static int trsm_sd_inv(int trans, int n, int k, const float *Rm, int ldr, const 
     }
   }
   return 0;
+}
+
+static int trsv_coop(int trans, int n, int k, const float *Rm, int ldr, const double *Rinv, const double *RinvT,
+                     double *B, int ldb, double *X, int ldx, GridBar *gb, cudaStream_t st) {
+  switch (k) {
+    case 4: return trsv_coop_k<4>(trans, n, Rm, ldr, Rinv, RinvT, B, ldb, X, ldx, gb, st);
+    case 2: return trsv_coop_k<2>(trans, n, Rm, ldr, Rinv, RinvT, B, ldb, X, ldx, gb, st);
+    case 1: return trsv_coop_k<1>(trans, n, Rm, ldr, Rinv, RinvT, B, ldb, X, ldx, gb, st);
+    default: return trsm_sd_inv(trans, n, k, Rm, ldr, Rinv, B, ldb, X, ldx, st);
+  }
 }
 
 static int colnorm2(int m, int k, const double *X, int ldx, double *out, cudaStream_t st) {
@@ -404,7 +580,7 @@ struct PhaseTimer {
 
 // Workspace layout (bytes, each piece 256-aligned)
 struct MixedWs {
-  size_t F, T, tau, dag, x32, r, s, p, t, q, sc, rinv, tmpn, total;
+  size_t F, T, tau, dag, x32, r, s, p, t, q, sc, rinv, rinvt, tmpn, gbar, total;
 };
 
 static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -427,7 +603,9 @@ static int mixed_ws(int m, int n, int k, int nb, int ib, MixedWs *w) {
   w->q = take(sizeof(double) * (size_t)m * k);
   w->sc = take(sizeof(double) * 8 * kLsMaxRhs);
   w->rinv = take(sizeof(double) * 65536 * (size_t)((n + 255) / 256));
+  w->rinvt = take(sizeof(double) * 65536 * (size_t)((n + 255) / 256));
   w->tmpn = take(sizeof(double) * (size_t)n * k);
+  w->gbar = take(sizeof(GridBar));
   w->total = off;
   return dag ? 0 : 1;
 }
@@ -516,9 +694,11 @@ int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, 
   LS_TRY(gemm_sd_n(m, n, k, A, lda, X, ldx, r, m, -1.0, 1.0, st));
   //    R's diagonal blocks inverted once; s = R^-T A^T r ; p = s ; gamma = |s|^2
   double *Rinv = (double *)(base + w.rinv), *tmpn = (double *)(base + w.tmpn);
-  LS_TRY(trinv_diag(n, F, m, Rinv, st));
+  double *RinvT = (double *)(base + w.rinvt);
+  GridBar *gbar = (GridBar *)(base + w.gbar);
+  LS_TRY(trinv_diag(n, F, m, Rinv, RinvT, st));
   LS_TRY(gemm_sd_t(m, n, k, A, lda, r, m, tmpn, n, 1.0, 0.0, st));
-  LS_TRY(trsm_sd_inv(1, n, k, F, m, Rinv, tmpn, n, s, n, st));
+  LS_TRY(trsv_coop(1, n, k, F, m, Rinv, RinvT, tmpn, n, s, n, gbar, st));
   LS_CU(cudaMemcpyAsync(p, s, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, st));
   LS_TRY(colnorm2(n, k, s, n, gamma, st));
   LS_CU(cudaMemcpyAsync(g0d, gamma, sizeof(double) * k, cudaMemcpyDeviceToDevice, st));
@@ -535,7 +715,7 @@ int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, 
   while (it < maxit && worst > 0.0) {
     // t = R^-1 p ; q = A t ; alpha = gamma / |q|^2
     LS_CU(cudaMemcpyAsync(tmpn, p, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, st));
-    LS_TRY(trsm_sd_inv(0, n, k, F, m, Rinv, tmpn, n, t, n, st));
+    LS_TRY(trsv_coop(0, n, k, F, m, Rinv, RinvT, tmpn, n, t, n, gbar, st));
     LS_TRY(gemm_sd_n(m, n, k, A, lda, t, n, q, m, 1.0, 0.0, st));
     LS_TRY(colnorm2(m, k, q, m, qq, st));
     k_cgls_alpha<<<1, 32, 0, st>>>(k, gamma, qq, g0d, tol2, alpha);
@@ -545,7 +725,7 @@ int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, 
     LS_TRY(axpy_cols(m, k, alpha, 1, q, m, r, m, st));
     //    s = R^-T A^T r ; beta = |s|^2 / gamma ; p = s + beta p
     LS_TRY(gemm_sd_t(m, n, k, A, lda, r, m, tmpn, n, 1.0, 0.0, st));
-    LS_TRY(trsm_sd_inv(1, n, k, F, m, Rinv, tmpn, n, s, n, st));
+    LS_TRY(trsv_coop(1, n, k, F, m, Rinv, RinvT, tmpn, n, s, n, gbar, st));
     LS_TRY(colnorm2(n, k, s, n, gnew, st));
     k_cgls_beta<<<1, 32, 0, st>>>(k, gamma, gnew, beta);
     count_launch();
