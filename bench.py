@@ -692,17 +692,15 @@ def main():
         print(json.dumps(res), flush=True)
         return 0
     world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        # host-only arm: rank 0 times the reference algorithm, other ranks exit
+        # without work, so no process group (and no GPU) is needed
+        return run_reference(args, world, rank)
     if world > 1:
         import torch
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    if args.impl == "reference":
-        rc = run_reference(args, world, rank)
-        if world > 1:
-            import torch.distributed as dist
-            dist.destroy_process_group()
-        return rc
 
     import torch
 
