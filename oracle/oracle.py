@@ -5,7 +5,9 @@ benchmark's CPU-baseline leg, never by the product library.
 
 The functions mirror NextLA.jl's low-level signatures (geqrt!, tsqrt!,
 tsmqr!, unmqr!, larfb!, larft!, geqr2!, parfb!) on column-major numpy
-arrays.  Views are allowed: the leading dimension is taken from the array's
+arrays, dispatching on the element type as the Julia methods do: float64
+arrays run the FP64 routines (nextla_oracle.c), complex128 arrays the
+ComplexF64 ones (nextla_oracle_z.c).  Views are allowed: the leading dimension is taken from the array's
 column stride, as Julia's `stride(A, 2)` would give it.  Argument errors
 raise ValueError (the reference raises ArgumentError).
 """
@@ -17,6 +19,7 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _SRC = os.path.join(_HERE, "nextla_oracle.c")
+_SRC_Z = os.path.join(_HERE, "nextla_oracle_z.c")     # complex elements
 _LIB_PATH = os.path.join(_HERE, "liboracle.so")
 _lib = None
 
@@ -29,8 +32,8 @@ CFLAGS = ["-O2", "-fPIC", "-shared", "-std=c11", "-ffp-contract=off", "-fopenmp"
 def build(force=False):
     """Compile liboracle.so next to this file (gcc, a second or two)."""
     if force or not os.path.exists(_LIB_PATH) or (
-            os.path.getmtime(_LIB_PATH) < os.path.getmtime(_SRC)):
-        subprocess.check_call(["gcc", *CFLAGS, "-o", _LIB_PATH, _SRC, "-lm"])
+            os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(_SRC), os.path.getmtime(_SRC_Z))):
+        subprocess.check_call(["gcc", *CFLAGS, "-o", _LIB_PATH, _SRC, _SRC_Z, "-lm"])
     return _LIB_PATH
 
 
@@ -67,6 +70,9 @@ def _declare(L):
         "ora_dtile_geqrf_tree": [_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _P],
         "ora_dtile_unmqr_tree": [_C, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _P, _I],
     }
+    for name in ("geqr2", "larft", "larfb", "geqrt", "unmqr", "parfb", "parfb_l", "tsmqr", "tsqrt", "ttqrt",
+                 "ttmqr", "tile_geqrf", "tile_unmqr"):
+        sig["ora_z" + name] = sig["ora_d" + name]
     for name, args in sig.items():
         f = getattr(L, name)
         f.argtypes = args
@@ -74,19 +80,29 @@ def _declare(L):
 
 
 def _mat(A):
-    """(pointer, ld) of a column-major float64 matrix or view."""
+    """(pointer, ld) of a column-major float64 or complex128 matrix or view."""
     if A is None:
         return None, 1
-    if A.dtype != np.float64:
-        raise TypeError("oracle works on float64 arrays")
+    if A.dtype not in (np.float64, np.complex128):
+        raise TypeError("oracle works on float64 and complex128 arrays")
+    es = A.dtype.itemsize
     if A.ndim == 1:
-        if A.size > 1 and A.strides[0] != 8:
+        if A.size > 1 and A.strides[0] != es:
             raise ValueError("vector must be contiguous")
         return A.ctypes.data, max(1, A.shape[0])
-    if A.shape[0] > 1 and A.strides[0] != 8:
+    if A.shape[0] > 1 and A.strides[0] != es:
         raise ValueError("matrix must be column-major (unit row stride)")
-    ld = A.strides[1] // 8 if A.shape[1] > 1 else A.shape[0]
+    ld = A.strides[1] // es if A.shape[1] > 1 else A.shape[0]
     return A.ctypes.data, max(1, ld)
+
+
+def _fn(name, *arrays):
+    """The oracle routine for the arrays' element type: ora_d<name> for
+    float64, ora_z<name> for complex128 (all arrays must agree)."""
+    kinds = {a.dtype for a in arrays if a is not None}
+    if len(kinds) != 1:
+        raise TypeError(f"{name}: arrays must share one element type, got {kinds}")
+    return getattr(lib(), ("ora_z" if kinds.pop() == np.complex128 else "ora_d") + name)
 
 
 def _ch(c):
@@ -114,13 +130,13 @@ def fmat(shape, rng=None, kind="uniform01"):
 
 def geqr2(m, n, A, tau, work):
     pa, lda = _mat(A)
-    return _check(lib().ora_dgeqr2(m, n, pa, lda, _mat(tau)[0], _mat(work)[0]), "geqr2")
+    return _check(_fn("geqr2", A, tau, work)(m, n, pa, lda, _mat(tau)[0], _mat(work)[0]), "geqr2")
 
 
 def larft(direct, storev, n, k, V, tau, T):
     pv, ldv = _mat(V)
     pt, ldt = _mat(T)
-    return _check(lib().ora_dlarft(_ch(direct), _ch(storev), n, k, pv, ldv,
+    return _check(_fn("larft", V, tau, T)(_ch(direct), _ch(storev), n, k, pv, ldv,
                                    _mat(tau)[0], pt, ldt), "larft")
 
 
@@ -129,14 +145,14 @@ def larfb(side, trans, direct, storev, m, n, k, V, ldv, T, C, work):
     pt, ldt = _mat(T)
     pc, ldc = _mat(C)
     pw, ldw = _mat(work)
-    return _check(lib().ora_dlarfb(_ch(side), _ch(trans), _ch(direct), _ch(storev), m, n, k,
+    return _check(_fn("larfb", V, T, C, work)(_ch(side), _ch(trans), _ch(direct), _ch(storev), m, n, k,
                                    pv, ldv, pt, ldt, pc, ldc, pw, ldw), "larfb")
 
 
 def geqrt(m, n, ib, A, T, tau, work):
     pa, lda = _mat(A)
     pt, ldt = _mat(T)
-    return _check(lib().ora_dgeqrt(m, n, ib, pa, lda, pt, ldt, _mat(tau)[0],
+    return _check(_fn("geqrt", A, T, tau, work)(m, n, ib, pa, lda, pt, ldt, _mat(tau)[0],
                                    _mat(work)[0]), "geqrt")
 
 
@@ -145,7 +161,7 @@ def unmqr(side, trans, m, n, k, ib, A, lda, T, C, work):
     pt, ldt = _mat(T)
     pc, ldc = _mat(C)
     pw, ldw = _mat(work)
-    return _check(lib().ora_dunmqr(_ch(side), _ch(trans), m, n, k, ib, pa, lda,
+    return _check(_fn("unmqr", A, T, C, work)(_ch(side), _ch(trans), m, n, k, ib, pa, lda,
                                    A.shape[0], A.shape[1], pt, ldt, pc, ldc, pw, ldw), "unmqr")
 
 
@@ -155,7 +171,7 @@ def parfb(side, trans, m1, n1, m2, n2, k, A1, A2, V, T, work):
     pv, ldv = _mat(V)
     pt, ldt = _mat(T)
     pw, ldw = _mat(work)
-    return _check(lib().ora_dparfb(_ch(side), _ch(trans), m1, n1, m2, n2, k, p1, ld1, p2, ld2,
+    return _check(_fn("parfb", A1, A2, V, T, work)(_ch(side), _ch(trans), m1, n1, m2, n2, k, p1, ld1, p2, ld2,
                                    pv, ldv, pt, ldt, pw, ldw), "parfb")
 
 
@@ -165,7 +181,7 @@ def tsmqr(side, trans, m1, n1, m2, n2, k, ib, A1, A2, V, T, work):
     pv, ldv = _mat(V)
     pt, ldt = _mat(T)
     kstored = min(V.shape[1], T.shape[1])
-    return _check(lib().ora_dtsmqr(_ch(side), _ch(trans), m1, n1, m2, n2, k, ib, kstored,
+    return _check(_fn("tsmqr", A1, A2, V, T, work)(_ch(side), _ch(trans), m1, n1, m2, n2, k, ib, kstored,
                                    p1, ld1, p2, ld2, pv, ldv, pt, ldt, _mat(work)[0]), "tsmqr")
 
 
@@ -173,7 +189,7 @@ def tsqrt(m, n, ib, A1, A2, T, tau, work):
     p1, ld1 = _mat(A1)
     p2, ld2 = _mat(A2)
     pt, ldt = _mat(T)
-    return _check(lib().ora_dtsqrt(m, n, ib, A1.shape[0], p1, ld1, p2, ld2, pt, ldt,
+    return _check(_fn("tsqrt", A1, A2, T, tau, work)(m, n, ib, A1.shape[0], p1, ld1, p2, ld2, pt, ldt,
                                    _mat(tau)[0], _mat(work)[0]), "tsqrt")
 
 
@@ -181,10 +197,10 @@ def tile_geqrf(A, nb, ib):
     """Flat-tree tile QR of A in place; returns (T, tau) in the tile layouts."""
     m, n = A.shape
     MT = (m + nb - 1) // nb
-    T = np.zeros((MT * ib, n), order="F")
-    tau = np.zeros((n, MT), order="F")
+    T = np.zeros((MT * ib, n), order="F", dtype=A.dtype)
+    tau = np.zeros((n, MT), order="F", dtype=A.dtype)
     pa, lda = _mat(A)
-    _check(lib().ora_dtile_geqrf(m, n, nb, ib, pa, lda, T.ctypes.data, MT * ib,
+    _check(_fn("tile_geqrf", A, T, tau)(m, n, nb, ib, pa, lda, T.ctypes.data, MT * ib,
                                  tau.ctypes.data, n), "tile_geqrf")
     return T, tau
 
@@ -194,7 +210,7 @@ def tile_unmqr(trans, A, T, B, nb, ib):
     pa, lda = _mat(A)
     pt, ldt = _mat(T)
     pb, ldb = _mat(B)
-    return _check(lib().ora_dtile_unmqr(_ch(trans), m, n, B.shape[1], nb, ib, pa, lda, pt, ldt,
+    return _check(_fn("tile_unmqr", A, T, B)(_ch(trans), m, n, B.shape[1], nb, ib, pa, lda, pt, ldt,
                                         pb, ldb), "tile_unmqr")
 
 
@@ -210,7 +226,7 @@ def parfb_l(side, trans, m1, n1, m2, n2, k, l, A1, A2, V, T, work):
     pv, ldv = _mat(V)
     pt, ldt = _mat(T)
     pw, ldw = _mat(work)
-    return _check(lib().ora_dparfb_l(_ch(side), _ch(trans), m1, n1, m2, n2, k, l, p1, ld1, p2, ld2,
+    return _check(_fn("parfb_l", A1, A2, V, T, work)(_ch(side), _ch(trans), m1, n1, m2, n2, k, l, p1, ld1, p2, ld2,
                                      pv, ldv, pt, ldt, pw, ldw), "parfb")
 
 
@@ -218,7 +234,7 @@ def ttqrt(m, n, ib, A1, A2, T, tau, work):
     p1, ld1 = _mat(A1)
     p2, ld2 = _mat(A2)
     pt, ldt = _mat(T)
-    return _check(lib().ora_dttqrt(m, n, ib, p1, ld1, p2, ld2, pt, ldt, _mat(tau)[0],
+    return _check(_fn("ttqrt", A1, A2, T, tau, work)(m, n, ib, p1, ld1, p2, ld2, pt, ldt, _mat(tau)[0],
                                    _mat(work)[0]), "ttqrt")
 
 
@@ -227,7 +243,7 @@ def ttmqr(side, trans, m1, n1, m2, n2, k, ib, A1, A2, V, T, work):
     p2, ld2 = _mat(A2)
     pv, ldv = _mat(V)
     pt, ldt = _mat(T)
-    return _check(lib().ora_dttmqr(_ch(side), _ch(trans), m1, n1, m2, n2, k, ib, p1, ld1, p2, ld2,
+    return _check(_fn("ttmqr", A1, A2, V, T, work)(_ch(side), _ch(trans), m1, n1, m2, n2, k, ib, p1, ld1, p2, ld2,
                                    pv, ldv, pt, ldt, _mat(work)[0]), "ttmqr")
 
 

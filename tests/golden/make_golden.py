@@ -28,6 +28,114 @@ def Q24(a):
     return F(np.ldexp(np.round(np.ldexp(a, 24)), -24))
 
 
+def Z(a):
+    return np.asfortranarray(a, dtype=np.complex128)
+
+
+def QZ(re, im):
+    """Complex input with both parts rounded to 24 significant bits."""
+    return Z(Q24(re) + 1j * Q24(im))
+
+
+def crand(rng, shape):
+    """rand(ComplexF64, shape): real and imaginary parts uniform in [0, 1)."""
+    return QZ(rng.random(shape), rng.random(shape))
+
+
+def crandn(rng, shape):
+    return QZ(rng.standard_normal(shape), rng.standard_normal(shape))
+
+
+def complex_vectors(rng, g):
+    """ComplexF64 vectors (every reference kernel test runs ComplexF64 too,
+    test/lapack_helpers.jl:11) against zgeqrt / ztpqrt / ztpmqrt / zgemqrt /
+    zlarfg, at the reference's test shapes plus one 128 x 128, ib = 32 tile.
+    Keys start with "z_"."""
+    # geqrt (test/geqrt.jl:6-11) vs zgeqrt
+    for (m, n, ib) in [(20, 15, 4), (32, 32, 8), (64, 32, 16), (32, 64, 8), (128, 128, 32)]:
+        A = crand(rng, (m, n))
+        a, t, info = lapack.zgeqrt(ib, A.copy(order="F"))
+        assert info == 0
+        key = f"z_geqrt_{m}_{n}_{ib}"
+        g[key + "_A"], g[key + "_outA"], g[key + "_outT"] = A, Z(a), Z(t[:, : min(m, n)])
+    # tsqrt (test/tsqrt.jl:8-13, A1 = triu(rand) + 2I) vs ztpqrt(l = 0)
+    for (m, n, ib) in [(32, 24, 8), (48, 32, 16), (20, 20, 10), (128, 128, 32)]:
+        A1 = Z(np.triu(crand(rng, (n, n))) + 2.0 * np.eye(n))
+        A2 = crand(rng, (m, n))
+        a1, a2, t, info = lapack.ztpqrt(0, ib, A1.copy(order="F"), A2.copy(order="F"))
+        assert info == 0
+        key = f"z_tsqrt_{m}_{n}_{ib}"
+        g[key + "_A1"], g[key + "_A2"] = A1, A2
+        g[key + "_outA1"], g[key + "_outA2"], g[key + "_outT"] = Z(a1), Z(a2), Z(t)
+    # tsmqr (test/tsmqr.jl:6-40) and ttmqr (test/ttmqr.jl:6-37, V = triu) vs
+    # ztpmqrt(l = 0), all side x trans forms
+    for kind in ("tsmqr", "ttmqr"):
+        for side in "LR":
+            for trans in "NC":
+                if kind == "tsmqr":
+                    if side == "L":
+                        m1, n1, m2, k, ib = 32, 24, 20, 16, 8
+                        n2 = n1
+                    else:
+                        m1, n1, n2, k, ib = 24, 32, 20, 16, 8
+                        m2 = m1
+                    V = crand(rng, (m2, k) if side == "L" else (n2, k))
+                else:
+                    m1 = n1 = m2 = n2 = 24
+                    k, ib = 16, 8
+                    V = Z(np.triu(crandn(rng, (24, k))))
+                A1 = crand(rng, (m1, n1))
+                A2 = crand(rng, (m2, n2))
+                T = Z(np.triu(crand(rng, (ib, k))))
+                out1 = A1.copy(order="F")
+                sub = out1[:k] if side == "L" else out1[:, :k]
+                a1, a2, info = lapack.ztpmqrt(0, V, T, Z(sub), A2.copy(order="F"), side=side, trans=trans)
+                assert info == 0
+                if side == "L":
+                    out1[:k] = a1
+                else:
+                    out1[:, :k] = a1
+                key = f"z_{kind}_{side}{trans}"
+                g[key + "_A1"], g[key + "_A2"], g[key + "_V"], g[key + "_T"] = A1, A2, V, T
+                g[key + "_outA1"], g[key + "_outA2"] = Z(out1), Z(a2)
+                g[key + "_dims"] = np.array([m1, n1, m2, n2, k, ib])
+    # unmqr (test/unmqr.jl:1-79) vs zgemqrt
+    m, n, k, ib = 64, 48, 32, 8
+    Aq = crand(rng, (m, k))
+    aq, tq, info = lapack.zgeqrt(ib, Aq.copy(order="F"))
+    assert info == 0
+    g["z_unmqr_Aqr"], g["z_unmqr_T"] = Z(aq), Z(tq)
+    for side in "LR":
+        for trans in "NC":
+            C = crand(rng, (m, n) if side == "L" else (n, m))
+            c, info = lapack.zgemqrt(aq, tq, C.copy(order="F"), side=side, trans=trans)
+            assert info == 0
+            g[f"z_unmqr_{side}{trans}_C"], g[f"z_unmqr_{side}{trans}_out"] = C, Z(c)
+    # larfg (test/larfg.jl) vs zlarfg
+    for n in (2, 7, 33, 256):
+        x = crandn(rng, (n,))
+        alpha, xo, tau = lapack.zlarfg(n, x[0], x[1:].copy())
+        g[f"z_larfg_{n}_x"] = x
+        g[f"z_larfg_{n}_out"] = np.concatenate([[alpha], xo, [tau]])
+    # ttqrt (test/ttqrt.jl:6-11) vs ztpqrt(l = n), with its Q applied both
+    # ways (ttmqr 'L') vs ztpmqrt(l = n)
+    for (n, ib) in [(16, 4), (24, 8), (48, 16)]:
+        A1 = Z(np.triu(crandn(rng, (n, n))) + 2.0 * np.eye(n))
+        A2 = Z(np.triu(crandn(rng, (n, n))) + 2.0 * np.eye(n))
+        a1, a2, t, info = lapack.ztpqrt(n, ib, A1.copy(order="F"), A2.copy(order="F"))
+        assert info == 0
+        key = f"z_ttqrt_{n}_{ib}"
+        g[key + "_A1"], g[key + "_A2"] = A1, A2
+        g[key + "_outA1"], g[key + "_outA2"], g[key + "_outT"] = Z(a1), Z(a2), Z(t)
+        for trans in "NC":
+            C1, C2 = crandn(rng, (n, 40)), crandn(rng, (n, 40))
+            c1, c2, info = lapack.ztpmqrt(n, Z(a2), Z(t), C1.copy(order="F"), C2.copy(order="F"),
+                                          side="L", trans=trans)
+            assert info == 0
+            g[f"{key}_L{trans}_C1"], g[f"{key}_L{trans}_C2"] = C1, C2
+            g[f"{key}_L{trans}_out1"], g[f"{key}_L{trans}_out2"] = Z(c1), Z(c2)
+
+
 def main():
     rng = np.random.default_rng(20240611)
     g = {}
@@ -146,6 +254,7 @@ def main():
             key = f"ttmqr_{side}{trans}"
             g[key + "_A1"], g[key + "_A2"], g[key + "_V"], g[key + "_T"] = A1, A2, V, T
             g[key + "_outA1"], g[key + "_outA2"] = F(out1), F(a2)
+    complex_vectors(rng, g)
     np.savez_compressed(OUT, **g)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")
 
