@@ -16,7 +16,9 @@
  *     a binding that keeps that behaviour synchronises the stream afterwards.
  *   - Flags are the ASCII characters NextLA uses ('L'/'R', 'N'/'C'/'T',
  *     'F'/'B', 'C'/'R').  'T' means the same as 'C' for real types.
- *   - Each routine exists for double (tqr_d...) and float (tqr_s...).
+ *   - Each routine exists for double (tqr_d...) and float (tqr_s...); the
+ *     tile kernels and the flat tile QR also for ComplexF64 (tqr_z...) and
+ *     ComplexF32 (tqr_c...), declared together further down.
  */
 #ifndef TILEQR_H
 #define TILEQR_H
@@ -26,6 +28,12 @@
 #ifdef __cplusplus
 extern "C" {
 #endif
+
+/* Complex elements: real part first, the layout of Julia's ComplexF64 /
+ * ComplexF32 and of C99's double _Complex / float _Complex.  Pointers to them
+ * must be aligned to the element size (16 / 8 bytes; a CuArray's are). */
+typedef struct { double re, im; } tqr_zcomplex;
+typedef struct { float re, im; } tqr_ccomplex;
 
 /* geqr2!(m, n, A, tau, work) -- src/geqr2.jl:107-121.
  * Unblocked Householder QR of the m-by-n A; tau has min(m, n) entries. */
@@ -120,6 +128,88 @@ int tqr_dttmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int
 int tqr_sttmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, float *A1,
                int lda1, float *A2, int lda2, const float *V, int ldv, const float *T, int ldt,
                float *work, int lwork, cudaStream_t stream);
+
+/* ---- Complex elements (every reference kernel test runs ComplexF32 and
+ * ComplexF64, test/lapack_helpers.jl:11).  Same arguments and semantics as
+ * the real routines above, with the reference's complex conventions:
+ * beta = -copysign(|(alpha, x)|, re(alpha)) is real, tau = ((beta - re)/beta,
+ * -im/beta), a column gets tau = 0 only when x = 0 and im(alpha) = 0
+ * (src/geqr2.jl:37-68), the updates apply H^H = I - conj(tau) v v^H, op(Q)
+ * for trans 'C' is Q^H, and 'T' acts as 'C' (src/tsmqr.jl:20).  As in the
+ * reference, geqr2 leaves a one-row column (the last of an m <= n panel)
+ * with tau = 0, so R's last diagonal entry may stay complex there.  A
+ * pointer not aligned to the element size returns -(its position). ---- */
+int tqr_zgeqr2(int m, int n, tqr_zcomplex *A, int lda, tqr_zcomplex *tau, tqr_zcomplex *work,
+               cudaStream_t stream);
+int tqr_zlarft(char direct, char storev, int n, int k, const tqr_zcomplex *V, int ldv,
+               const tqr_zcomplex *tau, tqr_zcomplex *T, int ldt, cudaStream_t stream);
+int tqr_zlarfb(char side, char trans, char direct, char storev, int m, int n, int k,
+               const tqr_zcomplex *V, int ldv, const tqr_zcomplex *T, int ldt, tqr_zcomplex *C,
+               int ldc, tqr_zcomplex *work, int ldwork, cudaStream_t stream);
+int tqr_zgeqrt(int m, int n, int ib, tqr_zcomplex *A, int lda, tqr_zcomplex *T, int ldt,
+               tqr_zcomplex *tau, tqr_zcomplex *work, cudaStream_t stream);
+int tqr_zunmqr(char side, char trans, int m, int n, int k, int ib, const tqr_zcomplex *A, int lda,
+               const tqr_zcomplex *T, int ldt, tqr_zcomplex *C, int ldc, tqr_zcomplex *work,
+               int ldwork, cudaStream_t stream);
+int tqr_ztsqrt(int m, int n, int ib, int m1, tqr_zcomplex *A1, int lda1, tqr_zcomplex *A2, int lda2,
+               tqr_zcomplex *T, int ldt, tqr_zcomplex *tau, tqr_zcomplex *work,
+               cudaStream_t stream);
+int tqr_ztsmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib,
+               tqr_zcomplex *A1, int lda1, tqr_zcomplex *A2, int lda2, const tqr_zcomplex *V,
+               int ldv, const tqr_zcomplex *T, int ldt, tqr_zcomplex *work, int lwork,
+               cudaStream_t stream);
+int tqr_zparfb(char side, char trans, char direct, char storev, int m1, int n1, int m2, int n2,
+               int k, int l, tqr_zcomplex *A1, int lda1, tqr_zcomplex *A2, int lda2,
+               const tqr_zcomplex *V, int ldv, const tqr_zcomplex *T, int ldt, tqr_zcomplex *work,
+               int ldwork, cudaStream_t stream);
+int tqr_zttqrt(int m, int n, int ib, tqr_zcomplex *A1, int lda1, tqr_zcomplex *A2, int lda2,
+               tqr_zcomplex *T, int ldt, tqr_zcomplex *tau, tqr_zcomplex *work,
+               cudaStream_t stream);
+int tqr_zttmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib,
+               tqr_zcomplex *A1, int lda1, tqr_zcomplex *A2, int lda2, const tqr_zcomplex *V,
+               int ldv, const tqr_zcomplex *T, int ldt, tqr_zcomplex *work, int lwork,
+               cudaStream_t stream);
+int tqr_ztile_geqrf(int m, int n, int nb, int ib, tqr_zcomplex *A, int lda, tqr_zcomplex *T,
+                    int ldt, tqr_zcomplex *tau, int ldtau, cudaStream_t stream);
+int tqr_ztile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const tqr_zcomplex *A,
+                    int lda, const tqr_zcomplex *T, int ldt, tqr_zcomplex *B, int ldb,
+                    cudaStream_t stream);
+
+int tqr_cgeqr2(int m, int n, tqr_ccomplex *A, int lda, tqr_ccomplex *tau, tqr_ccomplex *work,
+               cudaStream_t stream);
+int tqr_clarft(char direct, char storev, int n, int k, const tqr_ccomplex *V, int ldv,
+               const tqr_ccomplex *tau, tqr_ccomplex *T, int ldt, cudaStream_t stream);
+int tqr_clarfb(char side, char trans, char direct, char storev, int m, int n, int k,
+               const tqr_ccomplex *V, int ldv, const tqr_ccomplex *T, int ldt, tqr_ccomplex *C,
+               int ldc, tqr_ccomplex *work, int ldwork, cudaStream_t stream);
+int tqr_cgeqrt(int m, int n, int ib, tqr_ccomplex *A, int lda, tqr_ccomplex *T, int ldt,
+               tqr_ccomplex *tau, tqr_ccomplex *work, cudaStream_t stream);
+int tqr_cunmqr(char side, char trans, int m, int n, int k, int ib, const tqr_ccomplex *A, int lda,
+               const tqr_ccomplex *T, int ldt, tqr_ccomplex *C, int ldc, tqr_ccomplex *work,
+               int ldwork, cudaStream_t stream);
+int tqr_ctsqrt(int m, int n, int ib, int m1, tqr_ccomplex *A1, int lda1, tqr_ccomplex *A2, int lda2,
+               tqr_ccomplex *T, int ldt, tqr_ccomplex *tau, tqr_ccomplex *work,
+               cudaStream_t stream);
+int tqr_ctsmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib,
+               tqr_ccomplex *A1, int lda1, tqr_ccomplex *A2, int lda2, const tqr_ccomplex *V,
+               int ldv, const tqr_ccomplex *T, int ldt, tqr_ccomplex *work, int lwork,
+               cudaStream_t stream);
+int tqr_cparfb(char side, char trans, char direct, char storev, int m1, int n1, int m2, int n2,
+               int k, int l, tqr_ccomplex *A1, int lda1, tqr_ccomplex *A2, int lda2,
+               const tqr_ccomplex *V, int ldv, const tqr_ccomplex *T, int ldt, tqr_ccomplex *work,
+               int ldwork, cudaStream_t stream);
+int tqr_cttqrt(int m, int n, int ib, tqr_ccomplex *A1, int lda1, tqr_ccomplex *A2, int lda2,
+               tqr_ccomplex *T, int ldt, tqr_ccomplex *tau, tqr_ccomplex *work,
+               cudaStream_t stream);
+int tqr_cttmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib,
+               tqr_ccomplex *A1, int lda1, tqr_ccomplex *A2, int lda2, const tqr_ccomplex *V,
+               int ldv, const tqr_ccomplex *T, int ldt, tqr_ccomplex *work, int lwork,
+               cudaStream_t stream);
+int tqr_ctile_geqrf(int m, int n, int nb, int ib, tqr_ccomplex *A, int lda, tqr_ccomplex *T,
+                    int ldt, tqr_ccomplex *tau, int ldtau, cudaStream_t stream);
+int tqr_ctile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const tqr_ccomplex *A,
+                    int lda, const tqr_ccomplex *T, int ldt, tqr_ccomplex *B, int ldb,
+                    cudaStream_t stream);
 
 /* ---- Tile QR built from the kernels above (no counterpart in NextLA, which
  * ships only the tile kernels; the composition is the flat-tree order its

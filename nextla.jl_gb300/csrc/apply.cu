@@ -27,6 +27,7 @@ ApplyArgs<R> make_apply_args(int mode, char side, char trans, int m, int n, int 
   a.ib = ib;
   a.fwd = (left && trans != 'N') || (!left && trans == 'N');
   a.transT = left ? (trans != 'N') : (trans == 'N');
+  a.conj_c = is_cx<R> && !left;      // right side: the view is C^H
   a.C = C;
   a.A1 = A1;
   a.V = V; a.ldv = ldv;
@@ -92,5 +93,9 @@ template cudaError_t launch_apply<double>(int, char, char, int, int, int, int, d
                                           const double *, int, const double *, int, cudaStream_t, int);
 template cudaError_t launch_apply<float>(int, char, char, int, int, int, int, float *, int, float *, int,
                                          const float *, int, const float *, int, cudaStream_t, int);
+template cudaError_t launch_apply<cx<double>>(int, char, char, int, int, int, int, cx<double> *, int, cx<double> *,
+                                              int, const cx<double> *, int, const cx<double> *, int, cudaStream_t, int);
+template cudaError_t launch_apply<cx<float>>(int, char, char, int, int, int, int, cx<float> *, int, cx<float> *, int,
+                                             const cx<float> *, int, const cx<float> *, int, cudaStream_t, int);
 
 }  // namespace tqr

@@ -11,10 +11,13 @@
 //   mode 1 (tsmqr): V1 = I over a separate A1 (rows [i, i+kb)), V2 = V[0:L, i:i+kb]
 //          over all L rows of A2.
 //
-// For every block, in the reference's order:  W = A1/C1 rows + V^T C2,
+// For every block, in the reference's order:  W = A1/C1 rows + V^H C2,
 // W = op(T) W, A1/C1 rows -= W, C2 -= V W.  Right-side applies run the same
-// code on the transposed view (row stride ld, column stride 1): C op(Q) is
-// (op(Q)^T C^T)^T, which only swaps strides and whether T is transposed.
+// code on the conjugate-transposed view (row stride ld, column stride 1):
+// C op(Q) is (op(Q)^H C^H)^H, which swaps the strides and whether T is
+// conjugate-transposed and, for complex elements, conjugates C (and A1) on
+// the way in and out (conj_c).  Element types as in panel_dev.cuh; for
+// complex ones op(T) is T or T^H and 'T' means 'C' (src/tsmqr.jl:20).
 //
 // GB300 mapping: FP64 runs at ~7.9 GFLOP/s per SM through the SIMT DFMA pipe
 // (the FP64 MMA path is slower on sm_103a) and every FP64 warp instruction
@@ -32,6 +35,7 @@ namespace tqr {
 
 template <typename R>
 struct ApplyArgs {
+  int conj_c = 0;  // complex elements, right side: the view holds conj(C), conj(A1)
   int mode;      // 0: larfb/unmqr, 1: tsmqr
   int L;         // rows of the region (C rows for mode 0, A2 rows for mode 1), transposed view
   int ncols;     // extent split into strips (columns of the transposed view)
@@ -51,9 +55,6 @@ struct ApplyArgs {
                  // src/ttmqr.jl:60-90, src/pamm.jl:104-127); rows below are
                  // never read and region rows past tt + q are not touched
 };
-
-template <typename R>
-__device__ __forceinline__ R ldg_cg(const R *p) { return __ldcg(p); }
 
 // Phase 2 keeps op(T) W in registers (up to kW2Regs entries per thread) and
 // only needs a second W buffer beyond that.
@@ -93,23 +94,25 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
   R *const Cg = a.C + (size_t)c0 * a.c_cs;
   R *Cp;
   int crs, ccs;
+  const bool cjc = a.conj_c != 0;
   if (a.stage_c) {
     Cp = Cs; crs = 1; ccs = ldcs;
     if (a.c_rs == 1) {
       for (int idx = tid; idx < L * nwl; idx += TQR_THREADS) {
         int r = idx % L, c = idx / L;
-        Cs[r + (size_t)c * ldcs] = ldg_cg(Cg + (size_t)r + (size_t)c * a.c_cs);
+        Cs[r + (size_t)c * ldcs] = conj_if(ldg_cg(Cg + (size_t)r + (size_t)c * a.c_cs), cjc);
       }
     } else {
       for (int idx = tid; idx < L * nwl; idx += TQR_THREADS) {
         int c = idx % nwl, r = idx / nwl;
-        Cs[r + (size_t)c * ldcs] = ldg_cg(Cg + (size_t)r * a.c_rs + c);
+        Cs[r + (size_t)c * ldcs] = conj_if(ldg_cg(Cg + (size_t)r * a.c_rs + c), cjc);
       }
     }
   } else {
     Cp = Cg; crs = a.c_rs; ccs = a.c_cs;
   }
   R *const A1g = (a.mode == 1) ? a.A1 + (size_t)c0 * a.a_cs : nullptr;
+  const bool cjg = cjc && !a.stage_c;          // C read and written in global memory
 
   const int nblk = (a.k + ib - 1) / ib;
   for (int b = 0; b < nblk; ++b) {
@@ -149,7 +152,7 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
     }
     __syncthreads();
 
-    // Phase 1: W[p, c] = (A1 or C1 row) + sum_rr V[rr, p] * C[r0 + rr, c]
+    // Phase 1: W[p, c] = (A1 or C1 row) + sum_rr conj(V[rr, p]) * C[r0 + rr, c]
     // (mode 0 needs the unit-lower test only when V is read from global).
     const bool vtri = (a.mode == 0) && !a.stage_v;
     const bool vtt = ttb && !a.stage_v;          // unstaged TT V: bound each column's rows
@@ -160,19 +163,19 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
       const R *ccol = Cp + (size_t)r0 * crs + (size_t)c * ccs;
       const int Lp = vtt ? vrows(p) : Lr;
       int rr = vtri ? p : 0;
-      if (vtri) { acc0 = ccol[(size_t)p * crs]; ++rr; }
+      if (vtri) { acc0 = conj_if(ccol[(size_t)p * crs], cjg); ++rr; }
       for (; rr + 1 < Lp; rr += 2) {
-        acc0 = fma(vcol[rr], ccol[(size_t)rr * crs], acc0);
-        acc1 = fma(vcol[rr + 1], ccol[(size_t)(rr + 1) * crs], acc1);
+        acc0 = madc(vcol[rr], conj_if(ccol[(size_t)rr * crs], cjg), acc0);
+        acc1 = madc(vcol[rr + 1], conj_if(ccol[(size_t)(rr + 1) * crs], cjg), acc1);
       }
-      if (rr < Lp) acc0 = fma(vcol[rr], ccol[(size_t)rr * crs], acc0);
+      if (rr < Lp) acc0 = madc(vcol[rr], conj_if(ccol[(size_t)rr * crs], cjg), acc0);
       R w = acc0 + acc1;
-      if (a.mode == 1) w += ldg_cg(A1g + (size_t)(i + p) * a.a_rs + (size_t)c * a.a_cs);
+      if (a.mode == 1) w += conj_if(ldg_cg(A1g + (size_t)(i + p) * a.a_rs + (size_t)c * a.a_cs), cjc);
       Ws[p + c * ldw] = w;
     }
     __syncthreads();
-    // Phase 2: W := op(T) W, T upper triangular kb-by-kb (two partial sums per
-    // entry to halve the dependent FMA chain)
+    // Phase 2: W := op(T) W, T upper triangular kb-by-kb, op(T) = T^H when
+    // transT (two partial sums per entry to halve the dependent FMA chain)
     auto t_entry = [&](int e) -> R {
       const int p = e % kb, c = e / kb;
       const R *wc = Ws + c * ldw;
@@ -180,17 +183,17 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
       if (a.transT) {
         int q = 0;
         for (; q + 1 <= p; q += 2) {
-          s0 = fma(Tp[q + (size_t)p * ldtp], wc[q], s0);
-          s1 = fma(Tp[q + 1 + (size_t)p * ldtp], wc[q + 1], s1);
+          s0 = madc(Tp[q + (size_t)p * ldtp], wc[q], s0);
+          s1 = madc(Tp[q + 1 + (size_t)p * ldtp], wc[q + 1], s1);
         }
-        if (q <= p) s0 = fma(Tp[q + (size_t)p * ldtp], wc[q], s0);
+        if (q <= p) s0 = madc(Tp[q + (size_t)p * ldtp], wc[q], s0);
       } else {
         int q = p;
         for (; q + 1 < kb; q += 2) {
-          s0 = fma(Tp[p + (size_t)q * ldtp], wc[q], s0);
-          s1 = fma(Tp[p + (size_t)(q + 1) * ldtp], wc[q + 1], s1);
+          s0 = mad(Tp[p + (size_t)q * ldtp], wc[q], s0);
+          s1 = mad(Tp[p + (size_t)(q + 1) * ldtp], wc[q + 1], s1);
         }
-        if (q < kb) s0 = fma(Tp[p + (size_t)q * ldtp], wc[q], s0);
+        if (q < kb) s0 = mad(Tp[p + (size_t)q * ldtp], wc[q], s0);
       }
       return s0 + s1;
     };
@@ -215,11 +218,12 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
     }
     const R *Wf = w2buf ? W2 : Ws;
     // Phase 3: C[r0 + rr, c] -= sum_p V[rr, p] W[p, c];  mode 1: A1 rows -= W
+    // (through the conjugated view when conj_c)
     if (a.mode == 1) {
       for (int e = tid; e < ne; e += TQR_THREADS) {
         const int p = e % kb, c = e / kb;
         R *dst = A1g + (size_t)(i + p) * a.a_rs + (size_t)c * a.a_cs;
-        *dst = ldg_cg(dst) - Wf[p + c * ldw];
+        *dst = ldg_cg(dst) - conj_if(Wf[p + c * ldw], cjc);
       }
     }
     if (nwl == NW) {
@@ -234,11 +238,11 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
           if (vtri && p == rr) v = R(1);
           const R *wrow = Wf + p;
 #pragma unroll
-          for (int c = 0; c < NW; ++c) acc[c] = fma(v, wrow[c * ldw], acc[c]);
+          for (int c = 0; c < NW; ++c) acc[c] = mad(v, wrow[c * ldw], acc[c]);
         }
         R *crow = Cp + (size_t)(r0 + rr) * crs;
 #pragma unroll
-        for (int c = 0; c < NW; ++c) crow[(size_t)c * ccs] -= acc[c];
+        for (int c = 0; c < NW; ++c) crow[(size_t)c * ccs] -= conj_if(acc[c], cjg);
       }
     } else {
       for (int rr = tid; rr < Lr; rr += TQR_THREADS) {
@@ -253,12 +257,12 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
           const R *wrow = Wf + p;
 #pragma unroll
           for (int c = 0; c < NW; ++c)
-            if (c < nwl) acc[c] = fma(v, wrow[c * ldw], acc[c]);
+            if (c < nwl) acc[c] = mad(v, wrow[c * ldw], acc[c]);
         }
         R *crow = Cp + (size_t)(r0 + rr) * crs;
 #pragma unroll
         for (int c = 0; c < NW; ++c)
-          if (c < nwl) crow[(size_t)c * ccs] -= acc[c];
+          if (c < nwl) crow[(size_t)c * ccs] -= conj_if(acc[c], cjg);
       }
     }
     __syncthreads();
@@ -267,12 +271,12 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
     if (a.c_rs == 1) {
       for (int idx = tid; idx < L * nwl; idx += TQR_THREADS) {
         int r = idx % L, c = idx / L;
-        Cg[(size_t)r + (size_t)c * a.c_cs] = Cs[r + (size_t)c * ldcs];
+        Cg[(size_t)r + (size_t)c * a.c_cs] = conj_if(Cs[r + (size_t)c * ldcs], cjc);
       }
     } else {
       for (int idx = tid; idx < L * nwl; idx += TQR_THREADS) {
         int c = idx % nwl, r = idx / nwl;
-        Cg[(size_t)r * a.c_rs + c] = Cs[r + (size_t)c * ldcs];
+        Cg[(size_t)r * a.c_rs + c] = conj_if(Cs[r + (size_t)c * ldcs], cjc);
       }
     }
   }

@@ -22,6 +22,11 @@ inline bool is_side(char c) { return c == 'L' || c == 'R'; }
 inline bool is_trans(char c) { return c == 'N' || c == 'C' || c == 'T'; }
 inline int rc(cudaError_t e) { return e == cudaSuccess ? 0 : (int)e; }
 
+// C-ABI element pointer -> device element pointer (same layout)
+template <typename R, typename C> inline R *dp(C *p) { return reinterpret_cast<R *>(p); }
+template <typename R, typename C> inline const R *dp(const C *p) { return reinterpret_cast<const R *>(p); }
+template <typename R> inline bool al(const void *p) { return ((uintptr_t)p % alignof(R)) == 0; }
+
 template <typename R>
 int geqr2_impl(int m, int n, R *A, int lda, R *tau, cudaStream_t st) {
   if (m < 0) return -1;                      // src/geqr2.jl:108-113
@@ -231,65 +236,111 @@ int tsqrt_impl(int m, int n, int ib, int m1, R *A1, int lda1, R *A2, int lda2, R
 
 extern "C" {
 
-#define TQR_INSTANTIATE(P, R)                                                                        \
-  int tqr_##P##geqr2(int m, int n, R *A, int lda, R *tau, R *work, cudaStream_t stream) {            \
+// P: the BLAS-style prefix; CT: the element type of the C signature
+// (tileqr.h); R: the device element type (the same type for real elements,
+// cx<double> / cx<float> for tqr_zcomplex / tqr_ccomplex, which share their
+// layout).  A pointer not aligned to the element size (16 bytes for
+// ComplexF64, 8 for ComplexF32) is an illegal argument.
+#define TQR_INSTANTIATE(P, CT, R)                                                                    \
+  int tqr_##P##geqr2(int m, int n, CT *A, int lda, CT *tau, CT *work, cudaStream_t stream) {         \
     (void)work;                                                                                      \
-    return geqr2_impl<R>(m, n, A, lda, tau, stream);                                                 \
+    if (!al<R>(A)) return -3;                                                                        \
+    if (!al<R>(tau)) return -5;                                                                      \
+    return geqr2_impl<R>(m, n, dp<R>(A), lda, dp<R>(tau), stream);                                   \
   }                                                                                                  \
-  int tqr_##P##larft(char direct, char storev, int n, int k, const R *V, int ldv, const R *tau,      \
-                     R *T, int ldt, cudaStream_t stream) {                                           \
-    return larft_impl<R>(direct, storev, n, k, V, ldv, tau, T, ldt, stream);                         \
+  int tqr_##P##larft(char direct, char storev, int n, int k, const CT *V, int ldv, const CT *tau,    \
+                     CT *T, int ldt, cudaStream_t stream) {                                          \
+    if (!al<R>(V)) return -5;                                                                        \
+    if (!al<R>(tau)) return -7;                                                                      \
+    if (!al<R>(T)) return -8;                                                                        \
+    return larft_impl<R>(direct, storev, n, k, dp<R>(V), ldv, dp<R>(tau), dp<R>(T), ldt, stream);    \
   }                                                                                                  \
   int tqr_##P##larfb(char side, char trans, char direct, char storev, int m, int n, int k,           \
-                     const R *V, int ldv, const R *T, int ldt, R *C, int ldc, R *work, int ldwork,   \
+                     const CT *V, int ldv, const CT *T, int ldt, CT *C, int ldc, CT *work,           \
+                     int ldwork, cudaStream_t stream) {                                              \
+    (void)work; (void)ldwork;                                                                        \
+    if (!al<R>(V)) return -8;                                                                        \
+    if (!al<R>(T)) return -10;                                                                       \
+    if (!al<R>(C)) return -12;                                                                       \
+    return larfb_impl<R>(side, trans, direct, storev, m, n, k, dp<R>(V), ldv, dp<R>(T), ldt,         \
+                         dp<R>(C), ldc, stream);                                                     \
+  }                                                                                                  \
+  int tqr_##P##geqrt(int m, int n, int ib, CT *A, int lda, CT *T, int ldt, CT *tau, CT *work,        \
+                     cudaStream_t stream) {                                                          \
+    (void)work;                                                                                      \
+    if (!al<R>(A)) return -4;                                                                        \
+    if (!al<R>(T)) return -6;                                                                        \
+    if (!al<R>(tau)) return -8;                                                                      \
+    return geqrt_impl<R>(m, n, ib, dp<R>(A), lda, dp<R>(T), ldt, dp<R>(tau), stream);                \
+  }                                                                                                  \
+  int tqr_##P##unmqr(char side, char trans, int m, int n, int k, int ib, const CT *A, int lda,       \
+                     const CT *T, int ldt, CT *C, int ldc, CT *work, int ldwork,                     \
                      cudaStream_t stream) {                                                          \
     (void)work; (void)ldwork;                                                                        \
-    return larfb_impl<R>(side, trans, direct, storev, m, n, k, V, ldv, T, ldt, C, ldc, stream);      \
-  }                                                                                                  \
-  int tqr_##P##geqrt(int m, int n, int ib, R *A, int lda, R *T, int ldt, R *tau, R *work,            \
-                     cudaStream_t stream) {                                                          \
-    (void)work;                                                                                      \
-    return geqrt_impl<R>(m, n, ib, A, lda, T, ldt, tau, stream);                                     \
-  }                                                                                                  \
-  int tqr_##P##unmqr(char side, char trans, int m, int n, int k, int ib, const R *A, int lda,        \
-                     const R *T, int ldt, R *C, int ldc, R *work, int ldwork, cudaStream_t stream) { \
-    (void)work; (void)ldwork;                                                                        \
-    return unmqr_impl<R>(side, trans, m, n, k, ib, A, lda, T, ldt, C, ldc, stream);                  \
-  }                                                                                                  \
-  int tqr_##P##tsqrt(int m, int n, int ib, int m1, R *A1, int lda1, R *A2, int lda2, R *T, int ldt,  \
-                     R *tau, R *work, cudaStream_t stream) {                                         \
-    (void)work;                                                                                      \
-    return tsqrt_impl<R>(m, n, ib, m1, A1, lda1, A2, lda2, T, ldt, tau, stream);                     \
-  }                                                                                                  \
-  int tqr_##P##tsmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, R *A1,    \
-                     int lda1, R *A2, int lda2, const R *V, int ldv, const R *T, int ldt, R *work,   \
-                     int lwork, cudaStream_t stream) {                                               \
-    (void)work; (void)lwork;                                                                         \
-    return tsmqr_impl<R>(side, trans, m1, n1, m2, n2, k, ib, A1, lda1, A2, lda2, V, ldv, T, ldt,     \
+    if (!al<R>(A)) return -7;                                                                        \
+    if (!al<R>(T)) return -9;                                                                        \
+    if (!al<R>(C)) return -11;                                                                       \
+    return unmqr_impl<R>(side, trans, m, n, k, ib, dp<R>(A), lda, dp<R>(T), ldt, dp<R>(C), ldc,      \
                          stream);                                                                    \
   }                                                                                                  \
-  int tqr_##P##ttqrt(int m, int n, int ib, R *A1, int lda1, R *A2, int lda2, R *T, int ldt, R *tau, \
-                     R *work, cudaStream_t stream) {                                                 \
+  int tqr_##P##tsqrt(int m, int n, int ib, int m1, CT *A1, int lda1, CT *A2, int lda2, CT *T,        \
+                     int ldt, CT *tau, CT *work, cudaStream_t stream) {                              \
     (void)work;                                                                                      \
-    return ttqrt_impl<R>(m, n, ib, A1, lda1, A2, lda2, T, ldt, tau, stream);                         \
-  }                                                                                                  \
-  int tqr_##P##ttmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, R *A1,    \
-                     int lda1, R *A2, int lda2, const R *V, int ldv, const R *T, int ldt, R *work,   \
-                     int lwork, cudaStream_t stream) {                                               \
-    (void)work; (void)lwork;                                                                         \
-    return ttmqr_impl<R>(side, trans, m1, n1, m2, n2, k, ib, A1, lda1, A2, lda2, V, ldv, T, ldt,     \
+    if (!al<R>(A1)) return -5;                                                                       \
+    if (!al<R>(A2)) return -7;                                                                       \
+    if (!al<R>(T)) return -9;                                                                        \
+    if (!al<R>(tau)) return -11;                                                                     \
+    return tsqrt_impl<R>(m, n, ib, m1, dp<R>(A1), lda1, dp<R>(A2), lda2, dp<R>(T), ldt, dp<R>(tau),  \
                          stream);                                                                    \
+  }                                                                                                  \
+  int tqr_##P##tsmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, CT *A1,   \
+                     int lda1, CT *A2, int lda2, const CT *V, int ldv, const CT *T, int ldt,         \
+                     CT *work, int lwork, cudaStream_t stream) {                                     \
+    (void)work; (void)lwork;                                                                         \
+    if (!al<R>(A1)) return -9;                                                                       \
+    if (!al<R>(A2)) return -11;                                                                      \
+    if (!al<R>(V)) return -13;                                                                       \
+    if (!al<R>(T)) return -15;                                                                       \
+    return tsmqr_impl<R>(side, trans, m1, n1, m2, n2, k, ib, dp<R>(A1), lda1, dp<R>(A2), lda2,       \
+                         dp<R>(V), ldv, dp<R>(T), ldt, stream);                                      \
+  }                                                                                                  \
+  int tqr_##P##ttqrt(int m, int n, int ib, CT *A1, int lda1, CT *A2, int lda2, CT *T, int ldt,       \
+                     CT *tau, CT *work, cudaStream_t stream) {                                       \
+    (void)work;                                                                                      \
+    if (!al<R>(A1)) return -4;                                                                       \
+    if (!al<R>(A2)) return -6;                                                                       \
+    if (!al<R>(T)) return -8;                                                                        \
+    if (!al<R>(tau)) return -10;                                                                     \
+    return ttqrt_impl<R>(m, n, ib, dp<R>(A1), lda1, dp<R>(A2), lda2, dp<R>(T), ldt, dp<R>(tau),      \
+                         stream);                                                                    \
+  }                                                                                                  \
+  int tqr_##P##ttmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, CT *A1,   \
+                     int lda1, CT *A2, int lda2, const CT *V, int ldv, const CT *T, int ldt,         \
+                     CT *work, int lwork, cudaStream_t stream) {                                     \
+    (void)work; (void)lwork;                                                                         \
+    if (!al<R>(A1)) return -9;                                                                       \
+    if (!al<R>(A2)) return -11;                                                                      \
+    if (!al<R>(V)) return -13;                                                                       \
+    if (!al<R>(T)) return -15;                                                                       \
+    return ttmqr_impl<R>(side, trans, m1, n1, m2, n2, k, ib, dp<R>(A1), lda1, dp<R>(A2), lda2,       \
+                         dp<R>(V), ldv, dp<R>(T), ldt, stream);                                      \
   }                                                                                                  \
   int tqr_##P##parfb(char side, char trans, char direct, char storev, int m1, int n1, int m2,        \
-                     int n2, int k, int l, R *A1, int lda1, R *A2, int lda2, const R *V, int ldv,    \
-                     const R *T, int ldt, R *work, int ldwork, cudaStream_t stream) {                \
+                     int n2, int k, int l, CT *A1, int lda1, CT *A2, int lda2, const CT *V,          \
+                     int ldv, const CT *T, int ldt, CT *work, int ldwork, cudaStream_t stream) {     \
     (void)work; (void)ldwork;                                                                        \
-    return parfb_impl<R>(side, trans, direct, storev, m1, n1, m2, n2, k, l, A1, lda1, A2, lda2, V,   \
-                         ldv, T, ldt, stream);                                                       \
+    if (!al<R>(A1)) return -11;                                                                      \
+    if (!al<R>(A2)) return -13;                                                                      \
+    if (!al<R>(V)) return -15;                                                                       \
+    if (!al<R>(T)) return -17;                                                                       \
+    return parfb_impl<R>(side, trans, direct, storev, m1, n1, m2, n2, k, l, dp<R>(A1), lda1,         \
+                         dp<R>(A2), lda2, dp<R>(V), ldv, dp<R>(T), ldt, stream);                     \
   }
 
-TQR_INSTANTIATE(d, double)
-TQR_INSTANTIATE(s, float)
+TQR_INSTANTIATE(d, double, double)
+TQR_INSTANTIATE(s, float, float)
+TQR_INSTANTIATE(z, tqr_zcomplex, cx<double>)
+TQR_INSTANTIATE(c, tqr_ccomplex, cx<float>)
 
 #undef TQR_INSTANTIATE
 

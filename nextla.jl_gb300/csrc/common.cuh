@@ -54,15 +54,112 @@ template <typename R> __device__ inline R dev_copysign(R a, R b);
 template <> __device__ inline double dev_copysign<double>(double a, double b) { return copysign(a, b); }
 template <> __device__ inline float dev_copysign<float>(float a, float b) { return copysignf(a, b); }
 
-// Householder scalars in NextLA's convention (src/geqr2.jl:48-68,
-// src/tsqrt.jl:61-70): beta = -copysign(sqrt(alpha^2 + |x|^2), alpha),
-// tau = (beta - alpha) / beta, scale = 1 / (alpha - beta).  xnorm_sq == 0
-// means "no reflector" (tau = 0).
+// ---------------------------------------------------------------------------
+// Element types.  The tile kernels are written once over an element type E:
+// double, float, cx<double> (Julia's ComplexF64) or cx<float> (ComplexF32).
+// cx<R> is two R's, real part first -- the layout of Julia's Complex{R}, of
+// C99's R _Complex and of the C-ABI's tqr_zcomplex / tqr_ccomplex -- aligned
+// to its size so a load or store is one 16-byte (8-byte) access.
+//
+// The helpers below make the real instantiations compile to exactly the
+// arithmetic the real-only kernels had: conj_ is the identity, mad / madc are
+// one fma, abs2_add is fma(v, v, s).
+// ---------------------------------------------------------------------------
 template <typename R>
-__device__ inline void householder(R alpha, R xnorm_sq, R &beta, R &tau, R &scale) {
+struct __align__(2 * sizeof(R)) cx {
+  R x, y;   // real, imaginary
+  cx() = default;
+  __host__ __device__ constexpr cx(R re, R im = R(0)) : x(re), y(im) {}
+};
+
+template <typename E> struct elem_traits { using real = E; static constexpr bool complex = false; };
+template <typename R> struct elem_traits<cx<R>> { using real = R; static constexpr bool complex = true; };
+template <typename E> using real_t = typename elem_traits<E>::real;
+template <typename E> constexpr bool is_cx = elem_traits<E>::complex;
+
+template <typename R> __host__ __device__ __forceinline__ cx<R> operator+(cx<R> a, cx<R> b) { return cx<R>(a.x + b.x, a.y + b.y); }
+template <typename R> __host__ __device__ __forceinline__ cx<R> operator-(cx<R> a, cx<R> b) { return cx<R>(a.x - b.x, a.y - b.y); }
+template <typename R> __host__ __device__ __forceinline__ cx<R> operator-(cx<R> a) { return cx<R>(-a.x, -a.y); }
+template <typename R> __host__ __device__ __forceinline__ cx<R> operator*(cx<R> a, cx<R> b) {
+  return cx<R>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename R> __host__ __device__ __forceinline__ cx<R> &operator+=(cx<R> &a, cx<R> b) { a = a + b; return a; }
+template <typename R> __host__ __device__ __forceinline__ cx<R> &operator-=(cx<R> &a, cx<R> b) { a = a - b; return a; }
+template <typename R> __host__ __device__ __forceinline__ cx<R> &operator*=(cx<R> &a, cx<R> b) { a = a * b; return a; }
+template <typename R> __host__ __device__ __forceinline__ bool operator==(cx<R> a, cx<R> b) { return a.x == b.x && a.y == b.y; }
+template <typename R> __host__ __device__ __forceinline__ bool operator!=(cx<R> a, cx<R> b) { return !(a == b); }
+
+__device__ __forceinline__ double conj_(double a) { return a; }
+__device__ __forceinline__ float conj_(float a) { return a; }
+template <typename R> __device__ __forceinline__ cx<R> conj_(cx<R> a) { return cx<R>(a.x, -a.y); }
+
+// conj_ only when c holds (complex elements; the identity for real ones)
+template <typename E> __device__ __forceinline__ E conj_if(E a, bool c) {
+  if constexpr (is_cx<E>) { return c ? conj_(a) : a; } else { (void)c; return a; }
+}
+
+// mad(a, b, c) = a b + c
+__device__ __forceinline__ double mad(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float mad(float a, float b, float c) { return fmaf(a, b, c); }
+template <typename R> __device__ __forceinline__ cx<R> mad(cx<R> a, cx<R> b, cx<R> c) {
+  return cx<R>(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
+}
+// madc(a, b, c) = conj(a) b + c
+__device__ __forceinline__ double madc(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float madc(float a, float b, float c) { return fmaf(a, b, c); }
+template <typename R> __device__ __forceinline__ cx<R> madc(cx<R> a, cx<R> b, cx<R> c) {
+  return cx<R>(fma(a.x, b.x, fma(a.y, b.y, c.x)), fma(a.x, b.y, fma(-a.y, b.x, c.y)));
+}
+// |v|^2 + s
+__device__ __forceinline__ double abs2_add(double v, double s) { return fma(v, v, s); }
+__device__ __forceinline__ float abs2_add(float v, float s) { return fmaf(v, v, s); }
+template <typename R> __device__ __forceinline__ R abs2_add(cx<R> v, R s) { return fma(v.x, v.x, fma(v.y, v.y, s)); }
+
+template <typename R>
+__device__ inline cx<R> warp_sum(cx<R> v) {
+  return cx<R>(warp_sum(v.x), warp_sum(v.y));
+}
+
+// Loads through L2 only (ld.global.cg): in the persistent kernels other SMs
+// write the same tiles between tasks and L1 is not coherent with them.
+__device__ __forceinline__ double ldg_cg(const double *p) { return __ldcg(p); }
+__device__ __forceinline__ float ldg_cg(const float *p) { return __ldcg(p); }
+__device__ __forceinline__ cx<double> ldg_cg(const cx<double> *p) {
+  const double2 v = __ldcg(reinterpret_cast<const double2 *>(p));
+  return cx<double>(v.x, v.y);
+}
+__device__ __forceinline__ cx<float> ldg_cg(const cx<float> *p) {
+  const float2 v = __ldcg(reinterpret_cast<const float2 *>(p));
+  return cx<float>(v.x, v.y);
+}
+
+// Householder scalars in NextLA's convention (src/geqr2.jl:37-68,
+// src/tsqrt.jl:52-73): beta = -copysign(sqrt(|alpha|^2 + |x|^2), re(alpha))
+// (real), tau = (beta - alpha) / beta -- for complex elements
+// ((beta - re)/beta, -im/beta) -- and scale = 1 / (alpha - beta), formed for
+// complex elements as conj(alpha - beta) / |alpha - beta|^2 without a complex
+// division.  Returns false for "no reflector" (tau = 0): |x| == 0, and for
+// complex elements also im(alpha) == 0.
+template <typename R>
+__device__ inline bool householder(R alpha, R xnorm_sq, R &beta, R &tau, R &scale) {
+  if (xnorm_sq == R(0)) return false;
   beta = -dev_copysign(dev_sqrt(alpha * alpha + xnorm_sq), alpha);
   tau = (beta - alpha) / beta;
   scale = R(1) / (alpha - beta);
+  return true;
+}
+
+template <typename R>
+__device__ inline bool householder(cx<R> alpha, R xnorm_sq, cx<R> &beta, cx<R> &tau, cx<R> &scale) {
+  const R ar = alpha.x, ai = alpha.y;
+  if (xnorm_sq == R(0) && ai == R(0)) return false;
+  const R b = -dev_copysign(dev_sqrt(ar * ar + ai * ai + xnorm_sq), ar);
+  beta = cx<R>(b);
+  tau = cx<R>((b - ar) / b, -ai / b);
+  const R dr = ar - b, di = ai;
+  const R a2 = dr * dr + di * di;
+  scale = cx<R>(dr / a2, -di / a2);
+  return true;
 }
 
 }  // namespace tqr

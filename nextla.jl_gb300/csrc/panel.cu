@@ -34,7 +34,9 @@ k_tsqrt_block(int m, int sb, R *__restrict__ A1, int lda1, R *__restrict__ A2, i
 // Stand-alone larft (all four direct/storev variants), one CTA.  The outer
 // loop over reflectors stays serial as in the reference; the trailing-zero
 // scan, the V^H v products and the triangular mat-vec are spread over the
-// CTA.  Variant B keeps the reference's indexing (larft.jl:125-202).
+// CTA.  Variant B keeps the reference's indexing (larft.jl:125-202).  For
+// complex elements the conjugates sit where the reference puts them
+// (larft.jl:71-84, 98-108, 146-158, 171-180).
 // ---------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(TQR_THREADS)
@@ -70,11 +72,11 @@ k_larft(int direct_f, int storev_c, int n, int k, const R *__restrict__ V, int l
         R acc = 0;
         if (storev_c) {
           if (i + 1 <= j)
-            for (int r = i + 1; r <= j; ++r) acc += Vc(r, p) * Vc(r, i);
-          work[p] = -ti * Vc(i, p) + (-ti) * acc;
+            for (int r = i + 1; r <= j; ++r) acc += conj_(Vc(r, p)) * Vc(r, i);
+          work[p] = -ti * conj_(Vc(i, p)) + (-ti) * acc;
         } else {
           if (i > 0 && i + 1 <= j)
-            for (int r = i + 1; r <= j; ++r) acc += Vc(p, r) * Vc(i, r);
+            for (int r = i + 1; r <= j; ++r) acc += Vc(p, r) * conj_(Vc(i, r));
           work[p] = -ti * Vc(p, i) + (-ti) * acc;
         }
       }
@@ -112,13 +114,13 @@ k_larft(int direct_f, int storev_c, int n, int k, const R *__restrict__ V, int l
           R acc = 0;
           R base;
           if (storev_c) {
-            base = -ti * Vc(n - k + i, p);
+            base = -ti * conj_(Vc(n - k + i, p));
             if (j <= n - k + i)
-              for (int r = j; r <= n - k + i; ++r) acc += Vc(r, p) * Vc(r, k - 1);
+              for (int r = j; r <= n - k + i; ++r) acc += conj_(Vc(r, p)) * Vc(r, k - 1);
           } else {
             base = -ti * Vc(p, n - k + i);
             if (j <= n - k + i - 1)
-              for (int r = j; r <= n - k + i - 1; ++r) acc += Vc(p, r) * Vc(i, r);
+              for (int r = j; r <= n - k + i - 1; ++r) acc += Vc(p, r) * conj_(Vc(i, r));
           }
           work[p] = base + (-ti) * acc;
         }
@@ -191,5 +193,13 @@ template cudaError_t launch_tsqrt_block<double>(int, int, double *, int, double 
 template cudaError_t launch_tsqrt_block<float>(int, int, float *, int, float *, int, float *, int, float *, cudaStream_t, int);
 template cudaError_t launch_larft<double>(int, int, int, int, const double *, int, const double *, double *, int, cudaStream_t);
 template cudaError_t launch_larft<float>(int, int, int, int, const float *, int, const float *, float *, int, cudaStream_t);
+
+#define TQR_PANEL_INST(E)                                                                                         \
+  template cudaError_t launch_panel_qr<E>(int, int, E *, int, E *, E *, int, cudaStream_t);                       \
+  template cudaError_t launch_tsqrt_block<E>(int, int, E *, int, E *, int, E *, int, E *, cudaStream_t, int);     \
+  template cudaError_t launch_larft<E>(int, int, int, int, const E *, int, const E *, E *, int, cudaStream_t);
+TQR_PANEL_INST(cx<double>)
+TQR_PANEL_INST(cx<float>)
+#undef TQR_PANEL_INST
 
 }  // namespace tqr

@@ -12,12 +12,18 @@
 //   geqr2 at column i:  alpha = P[i,i], x = P[i+1:m, i], "row" = P[i, :]
 //   tsqrt at column i:  alpha = A1[i,i], x = A2[0:m, i], "row" = A1[i, :]
 //
-//   xnorm^2 = sum x^2; beta, tau, scale (one thread, broadcast); x *= scale;
-//   d_j = -tau (row[j] + x^T P[x rows, j]) for every other column j (j > i:
-//   the w of the rank-1 apply; j < i: the V^H v of the T column -- geqr2 keeps
-//   the row term there because row i of column j < i is part of v_j, tsqrt
-//   drops it because the A1 part of v_j is e_j);  row[j] += d_j and
-//   P[x rows, j] += x d_j for j > i;  T[0:i, i] = T[0:i, 0:i] d[0:i].
+//   xnorm^2 = sum |x|^2; beta, tau, scale (one thread, broadcast); x *= scale;
+//   S_j = row[j] + x^H P[x rows, j] for every other column j;
+//   j > i: d_j = -conj(tau) S_j, the update of H^H = I - conj(tau) v v^H
+//          (row[j] += d_j, P[x rows, j] += x d_j);
+//   j < i: d_j = -tau conj(S_j) = -tau v_j^H v_i, the T column's V^H v
+//          (geqr2 keeps the row term there because row i of column j < i is
+//          part of v_j; tsqrt drops it because the A1 part of v_j is e_j);
+//   T[0:i, i] = T[0:i, 0:i] d[0:i].
+// For real elements conj is the identity and both d's are -tau S_j.  The
+// element type E is double, float, cx<double> or cx<float> (common.cuh); the
+// complex forms follow the reference's complex branches (src/geqr2.jl:38-99,
+// src/tsqrt.jl:52-122, src/larft.jl:71-84).
 //
 // On GB300 every FP64 warp instruction holds an SM sub-partition's FP64 pipe
 // for ~64 cycles whatever its active-lane count, and sqrt/div cost ~600 cycles.
@@ -30,17 +36,17 @@
 
 namespace tqr {
 
-template <typename R>
+template <typename E>
 struct ColumnStep {
-  R *P;       // x region rows live here (geqr2: the panel; tsqrt: A2)
+  E *P;       // x region rows live here (geqr2: the panel; tsqrt: A2)
   int ldp;
-  R *row;     // row i of the factored matrix: row[j * rs]
+  E *row;     // row i of the factored matrix: row[j * rs]
   int rs;
-  R *Ts;      // T (nc-by-nc upper), ld = ldts, or nullptr
+  E *Ts;      // T (nc-by-nc upper), ld = ldts, or nullptr
   int ldts;
-  R *part;    // TQR_THREADS partial sums
-  R *d;       // nc: -tau * (row[j] + x^T P[:, j])
-  R *scal;    // 4
+  E *part;    // TQR_THREADS partial sums
+  E *d;       // nc: d_j above
+  E *scal;    // 4
   int tt = -1;  // >= 0: triangle-on-triangle form, column j of P holds rows
                 // [0, tt + j] only (NextLA src/ttqrt.jl:9); its rows below
                 // are never read
@@ -49,42 +55,42 @@ struct ColumnStep {
 // One column step.  x rows are [x0, m) of P, column i.  Returns false when
 // the reflector is the identity (tau = 0).  Contains the syncs it needs; all
 // threads call it with identical arguments.
-template <typename R>
-__device__ bool column_step(const ColumnStep<R> &c, int i, int x0, int m, int nc, bool tsqrt_form,
-                            R *tau_out, bool zero_t_on_skip)
+template <typename E>
+__device__ bool column_step(const ColumnStep<E> &c, int i, int x0, int m, int nc, bool tsqrt_form,
+                            E *tau_out, bool zero_t_on_skip)
 {
+  using S = real_t<E>;
   const int tid = threadIdx.x;
-  R *xcol = c.P + (size_t)i * c.ldp;
+  E *xcol = c.P + (size_t)i * c.ldp;
   // ---- norm of x ----
-  R s = 0;
-  for (int r = x0 + tid; r < m; r += TQR_THREADS) {
-    R v = xcol[r];
-    s = fma(v, v, s);
-  }
+  S s = 0;
+  for (int r = x0 + tid; r < m; r += TQR_THREADS) s = abs2_add(xcol[r], s);
   s = warp_sum(s);
-  if ((tid & 31) == 0) c.part[tid >> 5] = s;
+  S *rpart = reinterpret_cast<S *>(c.part);
+  if ((tid & 31) == 0) rpart[tid >> 5] = s;
   __syncthreads();
   if (tid == 0) {
-    R t = 0;
+    S t = 0;
 #pragma unroll
-    for (int w = 0; w < TQR_WARPS; ++w) t += c.part[w];
-    if (t != R(0)) {
-      R beta, tv, sc;
-      householder(c.row[(size_t)i * c.rs], t, beta, tv, sc);
-      c.scal[0] = beta; c.scal[1] = tv; c.scal[2] = sc; c.scal[3] = R(1);
+    for (int w = 0; w < TQR_WARPS; ++w) t += rpart[w];
+    E beta, tv, sc;
+    if (householder(c.row[(size_t)i * c.rs], t, beta, tv, sc)) {
+      c.scal[0] = beta; c.scal[1] = tv; c.scal[2] = sc; c.scal[3] = E(1);
     } else {
-      c.scal[3] = R(0);
+      c.scal[3] = E(0);
     }
   }
   __syncthreads();
-  if (c.scal[3] == R(0)) {
-    if (tid == 0) *tau_out = R(0);
+  if (c.scal[3] == E(0)) {
+    if (tid == 0) *tau_out = E(0);
     if (zero_t_on_skip && c.Ts)
-      for (int p = tid; p <= i; p += TQR_THREADS) c.Ts[p + (size_t)i * c.ldts] = R(0);
+      for (int p = tid; p <= i; p += TQR_THREADS) c.Ts[p + (size_t)i * c.ldts] = E(0);
     __syncthreads();
     return false;
   }
-  const R beta = c.scal[0], tv = c.scal[1], sc = c.scal[2];
+  const E beta = c.scal[0], tv = c.scal[1], sc = c.scal[2];
+  // d_j = -conj(tau) S_j (j > i), -tau conj(S_j) (j < i)
+  auto dval = [&](int j, E acc) -> E { return j > i ? -(conj_(tv) * acc) : -(tv * conj_(acc)); };
   for (int r = x0 + tid; r < m; r += TQR_THREADS) xcol[r] *= sc;
   __syncthreads();
   // ---- d_j for all j != i (j < i only when T is built) ----
@@ -95,39 +101,39 @@ __device__ bool column_step(const ColumnStep<R> &c, int i, int x0, int m, int nc
       const int G = TQR_THREADS / nj;          // row groups
       const int j = jlo + tid % nj, g = tid / nj;
       if (g < G) {
-        R a0 = 0, a1 = 0;
+        E a0 = 0, a1 = 0;
         if (j != i) {
-          const R *pc = c.P + (size_t)j * c.ldp;
+          const E *pc = c.P + (size_t)j * c.ldp;
           const int mj = (c.tt >= 0 && j < i) ? min(m, c.tt + j + 1) : m;
           int r = x0 + g;
           for (; r + G < mj; r += 2 * G) {
-            a0 = fma(pc[r], xcol[r], a0);
-            a1 = fma(pc[r + G], xcol[r + G], a1);
+            a0 = madc(xcol[r], pc[r], a0);
+            a1 = madc(xcol[r + G], pc[r + G], a1);
           }
-          if (r < mj) a0 = fma(pc[r], xcol[r], a0);
+          if (r < mj) a0 = madc(xcol[r], pc[r], a0);
         }
         c.part[g * nj + (j - jlo)] = a0 + a1;
       }
       __syncthreads();
       if (tid < nj) {
         const int jj = jlo + tid;
-        R acc = 0;
+        E acc = 0;
         for (int gg = 0; gg < G; ++gg) acc += c.part[gg * nj + tid];
         if (jj > i || (!tsqrt_form && jj < i)) acc += c.row[(size_t)jj * c.rs];
-        c.d[jj] = -tv * acc;
+        c.d[jj] = dval(jj, acc);
       }
     } else {
       const int lane = tid & 31, warp = tid >> 5;
       for (int j = jlo + warp; j < nc; j += TQR_WARPS) {
         if (j == i) continue;
-        const R *pc = c.P + (size_t)j * c.ldp;
+        const E *pc = c.P + (size_t)j * c.ldp;
         const int mj = (c.tt >= 0 && j < i) ? min(m, c.tt + j + 1) : m;
-        R a = 0;
-        for (int r = x0 + lane; r < mj; r += 32) a = fma(pc[r], xcol[r], a);
+        E a = 0;
+        for (int r = x0 + lane; r < mj; r += 32) a = madc(xcol[r], pc[r], a);
         a = warp_sum(a);
         if (lane == 0) {
           if (j > i || (!tsqrt_form && j < i)) a += c.row[(size_t)j * c.rs];
-          c.d[j] = -tv * a;
+          c.d[j] = dval(j, a);
         }
       }
     }
@@ -139,15 +145,15 @@ __device__ bool column_step(const ColumnStep<R> &c, int i, int x0, int m, int nc
     for (int j = i + 1 + tid; j < nc; j += TQR_THREADS) c.row[(size_t)j * c.rs] += c.d[j];
     for (int idx = tid; idx < ncol * rows; idx += TQR_THREADS) {
       const int rr = idx % rows, j = i + 1 + idx / rows;
-      R *pc = c.P + (size_t)j * c.ldp;
-      pc[x0 + rr] = fma(c.d[j], xcol[x0 + rr], pc[x0 + rr]);
+      E *pc = c.P + (size_t)j * c.ldp;
+      pc[x0 + rr] = mad(xcol[x0 + rr], c.d[j], pc[x0 + rr]);
     }
   }
   // ---- T column i ----
   if (c.Ts) {
     for (int p = tid; p < i; p += TQR_THREADS) {
-      R acc = 0;
-      for (int q = p; q < i; ++q) acc = fma(c.Ts[p + (size_t)q * c.ldts], c.d[q], acc);
+      E acc = 0;
+      for (int q = p; q < i; ++q) acc = mad(c.Ts[p + (size_t)q * c.ldts], c.d[q], acc);
       c.Ts[p + (size_t)i * c.ldts] = acc;
     }
     if (tid == 0) c.Ts[i + (size_t)i * c.ldts] = tv;
@@ -209,7 +215,7 @@ __device__ void panel_qr_cta(int m, int nc, R *A, int lda, R *tau, R *T, int ldt
     c.P = carve<R>(sp, (size_t)c.ldp * nc);
     for (int idx = tid; idx < m * nc; idx += TQR_THREADS) {
       int r = idx % m, cc = idx / m;
-      c.P[ix(r, cc, c.ldp)] = __ldcg(A + ix(r, cc, lda));
+      c.P[ix(r, cc, c.ldp)] = ldg_cg(A + ix(r, cc, lda));
     }
   } else {
     c.P = A;
@@ -272,8 +278,8 @@ __device__ void tsqrt_block_cta(int m, int sb, R *A1, int lda1, R *A2, int lda2,
   for (int idx = tid; idx < sb * sb; idx += TQR_THREADS) {
     int r = idx % sb, cc = idx / sb;
     if (r <= cc) {
-      B[ix(r, cc, ldb)] = __ldcg(A1 + ix(r, cc, lda1));
-      c.Ts[r + (size_t)cc * c.ldts] = __ldcg(T + ix(r, cc, ldt));   // skipped columns keep T
+      B[ix(r, cc, ldb)] = ldg_cg(A1 + ix(r, cc, lda1));
+      c.Ts[r + (size_t)cc * c.ldts] = ldg_cg(T + ix(r, cc, ldt));   // skipped columns keep T
     }
   }
   if (staged) {
@@ -281,7 +287,7 @@ __device__ void tsqrt_block_cta(int m, int sb, R *A1, int lda1, R *A2, int lda2,
     c.P = carve<R>(sp, (size_t)c.ldp * sb);
     for (int idx = tid; idx < mrow * sb; idx += TQR_THREADS) {
       int r = idx % mrow, cc = idx / mrow;
-      c.P[ix(r, cc, c.ldp)] = in_tri(r, cc) ? __ldcg(A2 + ix(r, cc, lda2)) : R(0);
+      c.P[ix(r, cc, c.ldp)] = in_tri(r, cc) ? ldg_cg(A2 + ix(r, cc, lda2)) : R(0);
     }
   } else {
     c.P = A2;

@@ -63,6 +63,33 @@ template <> struct K<float> {
   }
 };
 
+// Complex elements: the C-ABI takes tqr_zcomplex / tqr_ccomplex, the same
+// layout as cx<double> / cx<float>.
+#define TQR_K_COMPLEX(P, CT, E)                                                                                  \
+  template <> struct K<E> {                                                                                      \
+    static CT *c(E *p) { return reinterpret_cast<CT *>(p); }                                                      \
+    static const CT *c(const E *p) { return reinterpret_cast<const CT *>(p); }                                    \
+    static int geqrt(int m, int n, int ib, E *A, int lda, E *T, int ldt, E *tau, cudaStream_t s) {               \
+      return tqr_##P##geqrt(m, n, ib, c(A), lda, c(T), ldt, c(tau), nullptr, s);                                 \
+    }                                                                                                            \
+    static int tsqrt(int m, int n, int ib, int m1, E *A1, int lda1, E *A2, int lda2, E *T, int ldt, E *tau,      \
+                     cudaStream_t s) {                                                                           \
+      return tqr_##P##tsqrt(m, n, ib, m1, c(A1), lda1, c(A2), lda2, c(T), ldt, c(tau), nullptr, s);              \
+    }                                                                                                            \
+    static int unmqr(char side, char trans, int m, int n, int k, int ib, const E *A, int lda, const E *T,        \
+                     int ldt, E *C, int ldc, cudaStream_t s) {                                                   \
+      return tqr_##P##unmqr(side, trans, m, n, k, ib, c(A), lda, c(T), ldt, c(C), ldc, nullptr, 0, s);           \
+    }                                                                                                            \
+    static int tsmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, E *A1, int lda1,      \
+                     E *A2, int lda2, const E *V, int ldv, const E *T, int ldt, cudaStream_t s) {                \
+      return tqr_##P##tsmqr(side, trans, m1, n1, m2, n2, k, ib, c(A1), lda1, c(A2), lda2, c(V), ldv, c(T), ldt, \
+                            nullptr, 0, s);                                                                      \
+    }                                                                                                            \
+  };
+TQR_K_COMPLEX(z, tqr_zcomplex, cx<double>)
+TQR_K_COMPLEX(c, tqr_ccomplex, cx<float>)
+#undef TQR_K_COMPLEX
+
 // Internal streams of one device: a high-priority panel stream and a
 // low-priority update stream, plus the events that order them.
 struct DevStreams {
@@ -329,6 +356,30 @@ int tqr_dtile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const do
 int tqr_stile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const float *A, int lda,
                     const float *T, int ldt, float *B, int ldb, cudaStream_t stream) {
   return tile_unmqr<float>(trans, m, n, nrhs, nb, ib, A, lda, T, ldt, B, ldb, stream);
+}
+int tqr_ztile_geqrf(int m, int n, int nb, int ib, tqr_zcomplex *A, int lda, tqr_zcomplex *T, int ldt,
+                    tqr_zcomplex *tau, int ldtau, cudaStream_t stream) {
+  using E = cx<double>;
+  if (((uintptr_t)A | (uintptr_t)T | (uintptr_t)tau) % alignof(E)) return -5;
+  return tile_geqrf<E>(m, n, nb, ib, (E *)A, lda, (E *)T, ldt, (E *)tau, ldtau, stream);
+}
+int tqr_ctile_geqrf(int m, int n, int nb, int ib, tqr_ccomplex *A, int lda, tqr_ccomplex *T, int ldt,
+                    tqr_ccomplex *tau, int ldtau, cudaStream_t stream) {
+  using E = cx<float>;
+  if (((uintptr_t)A | (uintptr_t)T | (uintptr_t)tau) % alignof(E)) return -5;
+  return tile_geqrf<E>(m, n, nb, ib, (E *)A, lda, (E *)T, ldt, (E *)tau, ldtau, stream);
+}
+int tqr_ztile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const tqr_zcomplex *A, int lda,
+                    const tqr_zcomplex *T, int ldt, tqr_zcomplex *B, int ldb, cudaStream_t stream) {
+  using E = cx<double>;
+  if (((uintptr_t)A | (uintptr_t)T | (uintptr_t)B) % alignof(E)) return -7;
+  return tile_unmqr<E>(trans, m, n, nrhs, nb, ib, (const E *)A, lda, (const E *)T, ldt, (E *)B, ldb, stream);
+}
+int tqr_ctile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const tqr_ccomplex *A, int lda,
+                    const tqr_ccomplex *T, int ldt, tqr_ccomplex *B, int ldb, cudaStream_t stream) {
+  using E = cx<float>;
+  if (((uintptr_t)A | (uintptr_t)T | (uintptr_t)B) % alignof(E)) return -7;
+  return tile_unmqr<E>(trans, m, n, nrhs, nb, ib, (const E *)A, lda, (const E *)T, ldt, (E *)B, ldb, stream);
 }
 int tqr_dtrsm_lun(int n, int nrhs, const double *R, int ldr, double *B, int ldb, cudaStream_t stream) {
   return trsm_lun<double>(n, nrhs, R, ldr, B, ldb, stream);

@@ -4,7 +4,9 @@ Function names and argument lists follow NextLA's in-place kernels
 (`geqrt!`, `tsqrt!`, `tsmqr!`, `unmqr!`, `larfb!`, `larft!`, `geqr2!`,
 `parfb!`) and their allocating helper methods, dispatched on the number of
 arguments the way Julia dispatches on the method signature.  Arrays are
-column-major CUDA tensors (float64 or float32): build them with `empty`,
+column-major CUDA tensors -- float64, float32, complex128 (ComplexF64) or
+complex64 (ComplexF32), the element types the reference tests; the complex
+types cover the tile kernels and the flat tile QR -- built with `empty`,
 `zeros` or `to_device`, and pass slices of them as NextLA passes `@view`s; the
 leading dimension is read from the column stride.
 
@@ -78,6 +80,10 @@ def _prefix(*ts):
         return "d"
     if dt == torch.float32:
         return "s"
+    if dt == torch.complex128:
+        return "z"
+    if dt == torch.complex64:
+        return "c"
     raise TypeError(f"unsupported element type {dt}")
 
 
@@ -423,7 +429,8 @@ def tile_geqrf(A, nb=256, ib=32, T=None, tau=None, dag=True):
     pa, lda = _mat(A)
     pt, ldt = _mat(T)
     pu, ldu = _mat(tau)
-    ws = dag_workspace(m, n, nb, ib, A.device) if dag else None
+    real = _prefix(A, T, tau) in ("d", "s")
+    ws = dag_workspace(m, n, nb, ib, A.device) if dag and real else None
     if ws is None:
         _call(_prefix(A, T, tau), "tile_geqrf", m, n, nb, ib, pa, lda, pt, ldt, pu, ldu)
         return T, tau

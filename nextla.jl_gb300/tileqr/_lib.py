@@ -34,6 +34,15 @@ SIGNATURES = {
     "tile_unmqr_tree": [_C, _I, _I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _I, _P],
 }
 
+# routines that also exist for ComplexF64 (prefix z) and ComplexF32 (prefix c)
+COMPLEX = ("geqr2", "larft", "larfb", "geqrt", "unmqr", "tsqrt", "tsmqr", "parfb", "ttqrt", "ttmqr",
+           "tile_geqrf", "tile_unmqr")
+
+
+def prefixes(name):
+    return ("d", "s", "z", "c") if name in COMPLEX else ("d", "s")
+
+
 # measurement hooks without a precision prefix: name -> (argtypes, restype)
 DIAG = {
     "tqr_launch_count": ([], ctypes.c_ulonglong),
@@ -103,7 +112,7 @@ def lib():
                 f"{LIB_PATH} is not built; run nextla.jl_gb300/tileqr_build.py (no CPU fallback exists)")
         L = ctypes.CDLL(LIB_PATH)
         for name, args in SIGNATURES.items():
-            for p in ("d", "s"):
+            for p in prefixes(name):
                 f = getattr(L, f"tqr_{p}{name}")
                 f.argtypes = args
                 f.restype = _I
@@ -135,6 +144,8 @@ def profile_read():
 
 
 def fn(prefix, name):
+    if prefix not in prefixes(name) and name in SIGNATURES:
+        raise TypeError(f"{name} has no {'complex' if prefix in 'zc' else prefix} form")
     return getattr(lib(), f"tqr_{prefix}{name}")
 
 
@@ -143,6 +154,6 @@ def exported_symbols():
     L = lib()
     out = []
     for name in SIGNATURES:
-        for p in ("d", "s"):
+        for p in prefixes(name):
             out.append((f"tqr_{p}{name}", hasattr(L, f"tqr_{p}{name}")))
     return out

@@ -37,7 +37,7 @@ def test_exports_every_header_symbol(L):
 
 def test_python_signatures_cover_header():
     from tileqr import _lib
-    declared = {f"tqr_{p}{n}" for n in _lib.SIGNATURES for p in "ds"} | set(_lib.DIAG)
+    declared = {f"tqr_{p}{n}" for n in _lib.SIGNATURES for p in _lib.prefixes(n)} | set(_lib.DIAG)
     assert set(header_symbols()) <= declared
 
 
@@ -157,3 +157,25 @@ def test_tensor_core_dag_schedule_replays(L, m, n, nrhs):
     nt = ctypes.c_longlong(0)
     assert L.tqr_tile_dag_check_tc(m, n, nrhs, 256, 32, ctypes.byref(nt)) == 0
     assert nt.value > 0
+
+
+def test_complex_entry_points_exported(L):
+    """ComplexF64 / ComplexF32 forms of every tile kernel and of the tile QR."""
+    from tileqr import _lib
+    for name in _lib.COMPLEX:
+        for p in "zc":
+            assert hasattr(L, f"tqr_{p}{name}"), (p, name)
+
+
+def test_complex_argument_errors(L):
+    """Same argument checks as the real forms, plus element alignment."""
+    import ctypes
+    z = ctypes.c_void_p(16)       # aligned; never dereferenced: the calls fail their checks first
+    assert L.tqr_zgeqrt(-1, 4, 2, z, 4, z, 2, z, None, None) == -1
+    assert L.tqr_zgeqrt(4, 4, 0, z, 4, z, 2, z, None, None) == -3
+    assert L.tqr_zgeqrt(4, 4, 2, ctypes.c_void_p(8), 4, z, 2, z, None, None) == -4    # 8-byte aligned A
+    assert L.tqr_cgeqrt(4, 4, 2, ctypes.c_void_p(4), 4, z, 2, z, None, None) == -4    # 4-byte aligned A
+    assert L.tqr_ztsmqr(b"X", b"N", 8, 8, 8, 8, 4, 2, z, 8, z, 8, z, 8, z, 2, None, 0, None) == -1
+    assert L.tqr_ztsmqr(b"L", b"Q", 8, 8, 8, 8, 4, 2, z, 8, z, 8, z, 8, z, 2, None, 0, None) == -2
+    assert L.tqr_zunmqr(b"L", b"C", 8, 8, 4, 2, z, 8, z, 2, ctypes.c_void_p(24), 8, None, 0, None) == -11
+    assert L.tqr_ztile_geqrf(8, 8, 4, 8, z, 8, z, 8, z, 8, None) == -4                  # ib > nb
