@@ -59,6 +59,9 @@ def parse():
     p.add_argument("--adjoint-only", action="store_true", help="run only the differentiable QR")
     p.add_argument("--no-tall", action="store_true", help="skip the tall-skinny flat vs tree comparison")
     p.add_argument("--tall-only", action="store_true", help="run only the tall-skinny flat vs tree comparison")
+    p.add_argument("--no-complex", action="store_true", help="skip the complex tile QR")
+    p.add_argument("--complex-only", action="store_true", help="run only the complex tile QR")
+    p.add_argument("--complex-n", type=int, default=4096, help="order of the complex matrix")
     return p.parse_args()
 
 
@@ -514,6 +517,41 @@ def tall_bench(tq, torch, m=65536, n=512, steps=3, warmup=2, peak=None, dtype="f
     return out
 
 
+def complex_bench(tq, torch, n=4096, steps=3, warmup=3, peak=None):
+    """ComplexF64 and ComplexF32 tile QR of an n x n matrix (real and
+    imaginary parts N(0,1), nb = 256, ib = 32) through the persistent kernel,
+    against the stream driver.  Flops in real arithmetic: 4 x (4/3 n^3), the
+    complex multiply-add being 8 real flops (4 fused multiply-adds)."""
+    flops = 4.0 * 4.0 / 3.0 * n ** 3
+    st = torch.cuda.current_stream()
+    out = {"workload": f"complex tile QR {n}x{n}, N(0,1) real and imaginary parts, nb={NB}, ib={IB}",
+           "flops": flops}
+    for name, dt in (("c128", torch.complex128), ("c64", torch.complex64)):
+        g = torch.Generator(device="cuda").manual_seed(SEED)
+        A0 = tq.empty(n, n, dtype=dt)
+        A0.copy_(torch.complex(torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda"),
+                               torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda")).to(dt))
+        A = tq.empty(n, n, dtype=dt)
+        for mode, dag in (("dag", True), ("stream", False)):
+            ts = []
+            for rep in range(warmup + steps):
+                A.copy_(A0)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                tq.tile_geqrf(A, NB, IB, dag=dag)
+                e1.record(st)
+                torch.cuda.synchronize()
+                if rep >= warmup:
+                    ts.append(e0.elapsed_time(e1))
+            t = min(ts)
+            out[f"{name}_{mode}_ms"] = t
+            out[f"{name}_{mode}_tflops"] = flops / t / 1e9
+        if peak and name == "c128":
+            out["c128_dag_frac_of_fp64_simt_peak"] = flops / out["c128_dag_ms"] / 1e9 / peak
+    return out
+
+
 def adjoint_bench(torch, batch=256, m=2048, n=256, steps=3, warmup=3, peak=None):
     """Differentiable QR: (Q, R) = qr(A) for a batch of 256 Float64 2048x256
     N(0,1) matrices, loss 1/2||R^-1 Q^T b - y||^2 + <dQ, Q> + <dR, R> with
@@ -669,6 +707,18 @@ def main():
         tq.set_blocking(False)
         peak = fp64_peak(_lib, torch)
         res = {"f64": tall_bench(tq, torch, peak=peak), "f32": tall_bench(tq, torch, dtype="f32")}
+        print(json.dumps(res), flush=True)
+        return 0
+    if args.complex_only:
+        import torch
+
+        import tileqr as tq
+        import tileqr_build
+        from tileqr import _lib
+        tileqr_build.build()
+        tq.set_blocking(False)
+        res = complex_bench(tq, torch, args.complex_n, max(1, args.steps), max(3, args.warmup),
+                            peak=fp64_peak(_lib, torch))
         print(json.dumps(res), flush=True)
         return 0
     if args.adjoint_only:
@@ -831,6 +881,10 @@ def main():
     if rank == 0 and world == 1 and not args.no_adjoint:
         adj = adjoint_bench(torch, 256, 2048, 256, 3, 3, peak=peak)
 
+    cplx = None
+    if rank == 0 and world == 1 and not args.no_complex:
+        cplx = complex_bench(tq, torch, args.complex_n, 3, 3, peak=peak)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -844,6 +898,7 @@ def main():
             "batched_uneven_gels": bat,
             "differentiable_qr": adj,
             "tall_skinny_65536x512": tall,
+            "complex_tile_qr": cplx,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

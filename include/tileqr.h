@@ -236,6 +236,14 @@ int tqr_dtile_geqrf_dag(int m, int n, int nb, int ib, double *A, int lda, double
                         double *tau, int ldtau, void *work, size_t lwork, cudaStream_t stream);
 int tqr_stile_geqrf_dag(int m, int n, int nb, int ib, float *A, int lda, float *T, int ldt,
                         float *tau, int ldtau, void *work, size_t lwork, cudaStream_t stream);
+/* ComplexF64 / ComplexF32 forms (bit-identical to tqr_ztile_geqrf / tqr_ctile_geqrf).
+ * tqr_tile_dag_worksize covers every element type. */
+int tqr_ztile_geqrf_dag(int m, int n, int nb, int ib, tqr_zcomplex *A, int lda, tqr_zcomplex *T,
+                        int ldt, tqr_zcomplex *tau, int ldtau, void *work, size_t lwork,
+                        cudaStream_t stream);
+int tqr_ctile_geqrf_dag(int m, int n, int nb, int ib, tqr_ccomplex *A, int lda, tqr_ccomplex *T,
+                        int ldt, tqr_ccomplex *tau, int ldtau, void *work, size_t lwork,
+                        cudaStream_t stream);
 int tqr_tile_dag_status(const void *work, int *status, int *task, cudaStream_t stream);
 /* Statistics of the last run in `work` (synchronises `stream`), nanoseconds
  * summed over CTAs: out[0..5] time running each task type (GB, GA, UN, TB,

@@ -436,14 +436,27 @@ struct Plan {
   }
 };
 
-static bool dag_geom(int m, int n, int nb, int ib, DagGeom *g, int nrhs = 0) {
+// Largest shared-memory need of any task, for elements of esize bytes (8: the
+// real types, checked for the wider one; 16: ComplexF64).
+static size_t dag_task_smem(int nb, int ib, int nw, int esize) {
+  if (esize == 16)
+    return std::max({apply_smem_elems(nb, ib, nw, true, true, true) * sizeof(cx<double>),
+                     panel_smem<cx<double>>(nb, ib, true, true), tsqrt_smem<cx<double>>(nb, ib, true)});
+  return std::max({apply_smem_elems(nb, ib, nw, true, true, true) * sizeof(double),
+                   panel_smem<double>(nb, ib, true, true), tsqrt_smem<double>(nb, ib, true)});
+}
+
+// esize: bytes per element of the factorised matrix, rounded up to 8 (double,
+// float and ComplexF32 share one geometry; ComplexF64 gets its own).
+static bool dag_geom(int m, int n, int nb, int ib, DagGeom *g, int nrhs = 0, int esize = 8) {
   if (m <= 0 || n <= 0 || nb <= 0 || ib <= 0 || nrhs < 0 || nrhs > nb) return false;
   if (m % nb || n % nb || nb % ib) return false;
   if (nrhs > 0 && m < n) return false;         // the RHS tile column is never a panel
   if (nb > 256) return false;                  // one tile column of V per CTA in shared memory
+  esize = esize > 8 ? 16 : 8;
   // 16-wide strips when two CTAs still fit per SM, else 8 (ib must be a multiple)
   int nw = 16;
-  if (ib % 16 || 2 * (apply_smem_elems(nb, ib, 16, true, true, true) * sizeof(double) + 1024) >
+  if (ib % 16 || 2 * (apply_smem_elems(nb, ib, 16, true, true, true) * esize + 1024) >
                      (size_t)TQR_SMEM_MAX + 1024)
     nw = 8;
   if (ib % nw) return false;
@@ -455,10 +468,8 @@ static bool dag_geom(int m, int n, int nb, int ib, DagGeom *g, int nrhs = 0) {
   g->NS = nb / nw; g->SPB = ib / nw; g->NBK = nb / ib;
   if (2 * g->SPB + 1 > kMaxDeps) return false;
   if (g->MT > 65535 || g->NT > 65535 || g->NBK > 255) return false;
-  // every task's shared memory (checked for the wider type) must fit one CTA
-  const size_t sm = std::max({apply_smem_elems(nb, ib, nw, true, true, true) * sizeof(double),
-                              panel_smem<double>(nb, ib, true, true), tsqrt_smem<double>(nb, ib, true)});
-  if (sm > (size_t)TQR_SMEM_MAX) return false;
+  // every task's shared memory must fit one CTA
+  if (dag_task_smem(nb, ib, nw, esize) > (size_t)TQR_SMEM_MAX) return false;
   return true;
 }
 
@@ -660,7 +671,7 @@ static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int
   if (ib <= 0 || ib > nb) return -4;
   if (m == 0 || n == 0) return 0;
   DagGeom g;
-  if (!dag_geom(m, n, nb, ib, &g, nrhs)) return -3;   // shape outside the DAG path
+  if (!dag_geom(m, n, nb, ib, &g, nrhs, (int)sizeof(R))) return -3;   // shape outside the DAG path
   // FP32: trailing tsmqr updates on the tensor cores when the tile shape and
   // the float4 staging alignment allow it
   if (std::is_same<R, float>::value && nb == 256 && ib == tc::kIb && g.nw == 16 && tc_enabled() &&
@@ -825,7 +836,12 @@ int tqr_tile_dag_worksize(int m, int n, int nb, int ib, size_t *bytes) {
     *bytes = 0;
     return 1;    // not eligible: use tqr_?tile_geqrf (stream driver, no workspace)
   }
-  *bytes = get_plan(g)->bytes_total;
+  // one size for every element type: ComplexF64 may schedule narrower strips
+  // (more tasks) than the real types
+  size_t b = get_plan(g)->bytes_total;
+  DagGeom gz;
+  if (dag_geom(m, n, nb, ib, &gz, 0, 16)) b = std::max(b, get_plan(gz)->bytes_total);
+  *bytes = b;
   return 0;
 }
 
@@ -869,6 +885,20 @@ int tqr_dtile_geqrf_dag(int m, int n, int nb, int ib, double *A, int lda, double
 int tqr_stile_geqrf_dag(int m, int n, int nb, int ib, float *A, int lda, float *T, int ldt,
                         float *tau, int ldtau, void *work, size_t lwork, cudaStream_t stream) {
   return tile_geqrf_dag<float>(m, n, nb, ib, A, lda, T, ldt, tau, ldtau, work, lwork, stream);
+}
+
+int tqr_ztile_geqrf_dag(int m, int n, int nb, int ib, tqr_zcomplex *A, int lda, tqr_zcomplex *T, int ldt,
+                        tqr_zcomplex *tau, int ldtau, void *work, size_t lwork, cudaStream_t stream) {
+  using E = cx<double>;
+  if (((uintptr_t)A | (uintptr_t)T | (uintptr_t)tau) % alignof(E)) return -5;
+  return tile_geqrf_dag<E>(m, n, nb, ib, (E *)A, lda, (E *)T, ldt, (E *)tau, ldtau, work, lwork, stream);
+}
+
+int tqr_ctile_geqrf_dag(int m, int n, int nb, int ib, tqr_ccomplex *A, int lda, tqr_ccomplex *T, int ldt,
+                        tqr_ccomplex *tau, int ldtau, void *work, size_t lwork, cudaStream_t stream) {
+  using E = cx<float>;
+  if (((uintptr_t)A | (uintptr_t)T | (uintptr_t)tau) % alignof(E)) return -5;
+  return tile_geqrf_dag<E>(m, n, nb, ib, (E *)A, lda, (E *)T, ldt, (E *)tau, ldtau, work, lwork, stream);
 }
 
 int tqr_tile_dag_status(const void *work, int *status, int *task, cudaStream_t stream) {

@@ -429,8 +429,7 @@ def tile_geqrf(A, nb=256, ib=32, T=None, tau=None, dag=True):
     pa, lda = _mat(A)
     pt, ldt = _mat(T)
     pu, ldu = _mat(tau)
-    real = _prefix(A, T, tau) in ("d", "s")
-    ws = dag_workspace(m, n, nb, ib, A.device) if dag and real else None
+    ws = dag_workspace(m, n, nb, ib, A.device) if dag else None
     if ws is None:
         _call(_prefix(A, T, tau), "tile_geqrf", m, n, nb, ib, pa, lda, pt, ldt, pu, ldu)
         return T, tau
@@ -442,6 +441,11 @@ def tile_geqrf(A, nb=256, ib=32, T=None, tau=None, dag=True):
     st = torch.cuda.current_stream()
     rc = getattr(_lib.lib(), f"tqr_{p}tile_geqrf_dag")(m, n, nb, ib, pa, lda, pt, ldt, pu, ldu,
                                                       ctypes.c_void_p(wp), size, st.cuda_stream)
+    if rc == -3:
+        # outside the persistent path for this element type (ComplexF64's
+        # tasks need twice the shared memory): the stream driver
+        _call(p, "tile_geqrf", m, n, nb, ib, pa, lda, pt, ldt, pu, ldu)
+        return T, tau
     if rc < 0:
         raise ArgumentError(f"tile_geqrf: illegal value of argument {-rc}")
     if rc > 0:

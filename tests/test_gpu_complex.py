@@ -369,12 +369,32 @@ def test_ztile_qr(tq, oracle, dt, m, n, nb, ib):
     assert np.linalg.norm(host(tq, QhA)[:k] - R) <= bar * np.linalg.norm(R) * k
 
 
+@pytest.mark.parametrize("dt", DTYPES)
+@pytest.mark.parametrize("m,n,nb,ib", [(1024, 512, 256, 32), (512, 1024, 256, 32), (768, 768, 128, 16),
+                                       (1024, 1024, 256, 32)])
+def test_ztile_qr_task_graph_equals_stream_driver(tq, dt, m, n, nb, ib):
+    """The persistent task-graph kernel runs the same per-task arithmetic as
+    the stream driver on complex tiles too: bit-identical A, T, tau."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(m + n)
+    re = torch.randn(m, n, generator=g, dtype=torch.float64, device="cuda")
+    im = torch.randn(m, n, generator=g, dtype=torch.float64, device="cuda")
+    A0 = torch.complex(re, im).to(tdt(dt))
+    outs = []
+    for dag in (False, True):
+        A = tq.empty(m, n, dtype=tdt(dt))
+        A.copy_(A0)
+        T, tau = tq.tile_geqrf(A, nb, ib, dag=dag)
+        outs.append((A, T, tau))
+    for a, b in zip(*outs):
+        assert torch.equal(a, b)
+
+
 def test_zcomplex_has_no_real_only_paths(tq):
-    """The persistent task-graph schedule and the solves are real-only: a
-    complex tile QR takes the stream driver, and the real-only routines say
-    so instead of running on reinterpreted data."""
+    """The solves are real-only: they say so instead of running on
+    reinterpreted complex data."""
     A = tq.to_device(crand(np.random.default_rng(0), (512, 256)), dtype=tdt("complex128"))
-    T, tau = tq.tile_geqrf(A, 256, 32, dag=True)          # falls back to the stream driver
+    T, tau = tq.tile_geqrf(A, 256, 32, dag=True)
     assert T.dtype == tdt("complex128")
     with pytest.raises(TypeError):
         tq.trsm_lun(A[:256, :256], tq.zeros(256, 1, dtype=tdt("complex128")))
