@@ -137,8 +137,9 @@ int tqr_sttmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int
  * (src/geqr2.jl:37-68), the updates apply H^H = I - conj(tau) v v^H, op(Q)
  * for trans 'C' is Q^H, and 'T' acts as 'C' (src/tsmqr.jl:20).  As in the
  * reference, geqr2 leaves a one-row column (the last of an m <= n panel)
- * with tau = 0, so R's last diagonal entry may stay complex there.  A
- * pointer not aligned to the element size returns -(its position). ---- */
+ * with tau = 0, so R's last diagonal entry may stay complex there.  The
+ * triangular solve divides in Smith's scaled form.  A pointer not aligned to
+ * the element size returns an argument error. ---- */
 int tqr_zgeqr2(int m, int n, tqr_zcomplex *A, int lda, tqr_zcomplex *tau, tqr_zcomplex *work,
                cudaStream_t stream);
 int tqr_zlarft(char direct, char storev, int n, int k, const tqr_zcomplex *V, int ldv,
@@ -174,6 +175,10 @@ int tqr_ztile_geqrf(int m, int n, int nb, int ib, tqr_zcomplex *A, int lda, tqr_
 int tqr_ztile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const tqr_zcomplex *A,
                     int lda, const tqr_zcomplex *T, int ldt, tqr_zcomplex *B, int ldb,
                     cudaStream_t stream);
+int tqr_ztrsm_lun(int n, int nrhs, const tqr_zcomplex *R, int ldr, tqr_zcomplex *B, int ldb,
+                  cudaStream_t stream);
+int tqr_ztile_gels(int m, int n, int nrhs, int nb, int ib, tqr_zcomplex *A, int lda, tqr_zcomplex *T,
+                   int ldt, tqr_zcomplex *tau, int ldtau, tqr_zcomplex *B, int ldb, cudaStream_t stream);
 
 int tqr_cgeqr2(int m, int n, tqr_ccomplex *A, int lda, tqr_ccomplex *tau, tqr_ccomplex *work,
                cudaStream_t stream);
@@ -210,6 +215,10 @@ int tqr_ctile_geqrf(int m, int n, int nb, int ib, tqr_ccomplex *A, int lda, tqr_
 int tqr_ctile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const tqr_ccomplex *A,
                     int lda, const tqr_ccomplex *T, int ldt, tqr_ccomplex *B, int ldb,
                     cudaStream_t stream);
+int tqr_ctrsm_lun(int n, int nrhs, const tqr_ccomplex *R, int ldr, tqr_ccomplex *B, int ldb,
+                  cudaStream_t stream);
+int tqr_ctile_gels(int m, int n, int nrhs, int nb, int ib, tqr_ccomplex *A, int lda, tqr_ccomplex *T,
+                   int ldt, tqr_ccomplex *tau, int ldtau, tqr_ccomplex *B, int ldb, cudaStream_t stream);
 
 /* ---- Tile QR built from the kernels above (no counterpart in NextLA, which
  * ships only the tile kernels; the composition is the flat-tree order its

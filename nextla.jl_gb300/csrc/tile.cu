@@ -244,6 +244,21 @@ int tile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const R *A, i
 // diagonal, then b[r] -= (R[r,i] / R[r,r]) b[i]); the rows above are updated
 // with C -= R_blk X_blk.  No size limit (the reference kernel stops at 1024).
 // ---------------------------------------------------------------------------
+// a / b: the division itself for real elements; for complex elements Smith's
+// algorithm (R. L. Smith, "Algorithm 116: Complex division", CACM 5(8), 1962),
+// which scales by the larger part of b so |b|^2 is never formed.
+__device__ __forceinline__ double div_(double a, double b) { return a / b; }
+__device__ __forceinline__ float div_(float a, float b) { return a / b; }
+template <typename R>
+__device__ __forceinline__ cx<R> div_(cx<R> a, cx<R> b) {
+  if (fabs(b.x) >= fabs(b.y)) {
+    const R r = b.y / b.x, d = b.x + b.y * r;
+    return cx<R>((a.x + a.y * r) / d, (a.y - a.x * r) / d);
+  }
+  const R r = b.x / b.y, d = b.y + b.x * r;
+  return cx<R>((a.x * r + a.y) / d, (a.y * r - a.x) / d);
+}
+
 template <typename R>
 __global__ void __launch_bounds__(TQR_THREADS)
 k_trsv_block(int nb, const R *__restrict__ Rm, int ldr, R *__restrict__ B, int ldb)
@@ -254,12 +269,12 @@ k_trsv_block(int nb, const R *__restrict__ Rm, int ldr, R *__restrict__ B, int l
   R *col = B + (size_t)blockIdx.x * ldb;
   for (int r = threadIdx.x; r < nb; r += TQR_THREADS) {
     dg[r] = Rm[ix(r, r, ldr)];
-    b[r] = col[r] / dg[r];
+    b[r] = div_(col[r], dg[r]);
   }
   __syncthreads();
   for (int i = nb - 1; i > 0; --i) {
     const R bi = b[i];
-    for (int r = threadIdx.x; r < i; r += TQR_THREADS) b[r] -= (Rm[ix(r, i, ldr)] / dg[r]) * bi;
+    for (int r = threadIdx.x; r < i; r += TQR_THREADS) b[r] -= div_(Rm[ix(r, i, ldr)], dg[r]) * bi;
     __syncthreads();
   }
   for (int r = threadIdx.x; r < nb; r += TQR_THREADS) col[r] = b[r];
@@ -380,6 +395,28 @@ int tqr_ctile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const tq
   using E = cx<float>;
   if (((uintptr_t)A | (uintptr_t)T | (uintptr_t)B) % alignof(E)) return -7;
   return tile_unmqr<E>(trans, m, n, nrhs, nb, ib, (const E *)A, lda, (const E *)T, ldt, (E *)B, ldb, stream);
+}
+int tqr_ztrsm_lun(int n, int nrhs, const tqr_zcomplex *R, int ldr, tqr_zcomplex *B, int ldb, cudaStream_t stream) {
+  using E = cx<double>;
+  if (((uintptr_t)R | (uintptr_t)B) % alignof(E)) return -3;
+  return trsm_lun<E>(n, nrhs, (const E *)R, ldr, (E *)B, ldb, stream);
+}
+int tqr_ctrsm_lun(int n, int nrhs, const tqr_ccomplex *R, int ldr, tqr_ccomplex *B, int ldb, cudaStream_t stream) {
+  using E = cx<float>;
+  if (((uintptr_t)R | (uintptr_t)B) % alignof(E)) return -3;
+  return trsm_lun<E>(n, nrhs, (const E *)R, ldr, (E *)B, ldb, stream);
+}
+int tqr_ztile_gels(int m, int n, int nrhs, int nb, int ib, tqr_zcomplex *A, int lda, tqr_zcomplex *T, int ldt,
+                   tqr_zcomplex *tau, int ldtau, tqr_zcomplex *B, int ldb, cudaStream_t stream) {
+  using E = cx<double>;
+  if (((uintptr_t)A | (uintptr_t)T | (uintptr_t)tau | (uintptr_t)B) % alignof(E)) return -6;
+  return tile_gels<E>(m, n, nrhs, nb, ib, (E *)A, lda, (E *)T, ldt, (E *)tau, ldtau, (E *)B, ldb, stream);
+}
+int tqr_ctile_gels(int m, int n, int nrhs, int nb, int ib, tqr_ccomplex *A, int lda, tqr_ccomplex *T, int ldt,
+                   tqr_ccomplex *tau, int ldtau, tqr_ccomplex *B, int ldb, cudaStream_t stream) {
+  using E = cx<float>;
+  if (((uintptr_t)A | (uintptr_t)T | (uintptr_t)tau | (uintptr_t)B) % alignof(E)) return -6;
+  return tile_gels<E>(m, n, nrhs, nb, ib, (E *)A, lda, (E *)T, ldt, (E *)tau, ldtau, (E *)B, ldb, stream);
 }
 int tqr_dtrsm_lun(int n, int nrhs, const double *R, int ldr, double *B, int ldb, cudaStream_t stream) {
   return trsm_lun<double>(n, nrhs, R, ldr, B, ldb, stream);

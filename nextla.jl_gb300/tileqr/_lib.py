@@ -36,7 +36,7 @@ SIGNATURES = {
 
 # routines that also exist for ComplexF64 (prefix z) and ComplexF32 (prefix c)
 COMPLEX = ("geqr2", "larft", "larfb", "geqrt", "unmqr", "tsqrt", "tsmqr", "parfb", "ttqrt", "ttmqr",
-           "tile_geqrf", "tile_unmqr")
+           "tile_geqrf", "tile_unmqr", "trsm_lun", "tile_gels")
 
 
 def prefixes(name):

@@ -734,3 +734,33 @@ int ora_ztile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const zc
     free(work);
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Upper-triangular solve R X = B with LeftUpperTRSM!'s arithmetic           */
+/* (src/trsm.jl:38-63): B scaled by the diagonal first, then                 */
+/* b[r] -= (A[r,i] / A[r,r]) b[i].  Complex division in Smith's scaled form  */
+/* (R. L. Smith, "Algorithm 116: Complex division", CACM 5(8), 1962).        */
+/* ------------------------------------------------------------------------ */
+static zc zdiv(zc a, zc b)
+{
+    double ar = creal(a), ai = cimag(a), br = creal(b), bi = cimag(b);
+    if (fabs(br) >= fabs(bi)) {
+        double r = bi / br, d = br + bi * r;
+        return CMPLX((ar + ai * r) / d, (ai - ar * r) / d);
+    }
+    double r = br / bi, d = bi + br * r;
+    return CMPLX((ar * r + ai) / d, (ai * r - ar) / d);
+}
+
+int ora_ztrsm_lun(int n, int nrhs, const zc *A, int lda, zc *B, int ldb)
+{
+    if (n < 0) return -1;
+    if (nrhs < 0) return -2;
+    for (int c = 0; c < nrhs; ++c) {
+        zc *b = B + IDX(0, c, ldb);
+        for (int r = 0; r < n; ++r) b[r] = zdiv(b[r], A[IDX(r, r, lda)]);
+        for (int i = n - 1; i >= 0; --i)
+            for (int r = 0; r < i; ++r) b[r] -= zmul(zdiv(A[IDX(r, i, lda)], A[IDX(r, r, lda)]), b[i]);
+    }
+    return 0;
+}

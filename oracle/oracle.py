@@ -71,7 +71,7 @@ def _declare(L):
         "ora_dtile_unmqr_tree": [_C, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _P, _I],
     }
     for name in ("geqr2", "larft", "larfb", "geqrt", "unmqr", "parfb", "parfb_l", "tsmqr", "tsqrt", "ttqrt",
-                 "ttmqr", "tile_geqrf", "tile_unmqr"):
+                 "ttmqr", "tile_geqrf", "tile_unmqr", "trsm_lun"):
         sig["ora_z" + name] = sig["ora_d" + name]
     for name, args in sig.items():
         f = getattr(L, name)
@@ -217,7 +217,7 @@ def tile_unmqr(trans, A, T, B, nb, ib):
 def trsm_lun(R, B):
     pr, ldr = _mat(R)
     pb, ldb = _mat(B)
-    return _check(lib().ora_dtrsm_lun(R.shape[1], B.shape[1], pr, ldr, pb, ldb), "trsm")
+    return _check(_fn("trsm_lun", R, B)(R.shape[1], B.shape[1], pr, ldr, pb, ldb), "trsm")
 
 
 def parfb_l(side, trans, m1, n1, m2, n2, k, l, A1, A2, V, T, work):
@@ -272,8 +272,9 @@ def tile_unmqr_tree(trans, A, T, T2, B, nb, ib):
 
 def tile_lstsq(A, B, nb, ib):
     """min ||A X - B|| by tile QR: returns X (n-by-nrhs); A and B are copied."""
-    A = np.array(A, order="F", dtype=np.float64)
-    B = np.array(B, order="F", dtype=np.float64)
+    dt = np.complex128 if np.iscomplexobj(A) or np.iscomplexobj(B) else np.float64
+    A = np.array(A, order="F", dtype=dt)
+    B = np.array(B, order="F", dtype=dt)
     n = A.shape[1]
     T, _ = tile_geqrf(A, nb, ib)
     tile_unmqr("C", A, T, B, nb, ib)

@@ -390,11 +390,46 @@ def test_ztile_qr_task_graph_equals_stream_driver(tq, dt, m, n, nb, ib):
         assert torch.equal(a, b)
 
 
-def test_zcomplex_has_no_real_only_paths(tq):
-    """The solves are real-only: they say so instead of running on
-    reinterpreted complex data."""
+@pytest.mark.parametrize("dt", DTYPES)
+@pytest.mark.parametrize("n,nrhs", [(40, 3), (300, 5), (600, 1)])
+def test_ztrsm_lun(tq, oracle, dt, n, nrhs):
+    """LeftUpperTRSM!'s arithmetic on complex R (diagonal scaling, then
+    b[r] -= (R[r,i]/R[r,r]) b[i]), blocked beyond 256 rows."""
+    rng = np.random.default_rng(n + nrhs)
+    R0 = np.triu(crand(rng, (n, n))) / np.sqrt(n)
+    R0[np.diag_indices(n)] = (2 + rng.random(n)) * np.exp(1j * rng.uniform(0, 2 * np.pi, n))
+    R0, B0 = rnd(R0, dt), rnd(crand(rng, (n, nrhs)), dt)
+    B = dev(tq, B0, dt)
+    tq.trsm_lun(dev(tq, R0, dt), B)
+    Xo = B0.copy(order="F")
+    oracle.trsm_lun(R0, Xo)
+    assert rel(host(tq, B), Xo) < tol(dt, 10 * n)
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+def test_ztile_gels(tq, oracle, dt):
+    """Complex least squares (tile QR, Q^H B, back-substitution) against the
+    oracle's and against the planted solution."""
+    rng = np.random.default_rng(12)
+    m, n, k = 600, 300, 2
+    A0 = rnd(crand(rng, (m, n)), dt)
+    x = crand(rng, (n, k))
+    B0 = rnd(A0 @ x, dt)
+    A, B = dev(tq, A0, dt), dev(tq, B0, dt)
+    X, T, tau = tq.tile_gels(A, B, 128, 32)
+    Xo = oracle.tile_lstsq(A0, B0, 128, 32)
+    assert rel(host(tq, X), Xo) < tol(dt, 1000)
+    bar = 1e-9 if dt == "complex128" else 1e-3
+    assert np.abs(host(tq, X) - x).max() < bar
+
+
+def test_zcomplex_real_only_paths_refuse(tq):
+    """The tree driver and the mixed-precision solve are real-only: they say
+    so instead of running on reinterpreted complex data."""
     A = tq.to_device(crand(np.random.default_rng(0), (512, 256)), dtype=tdt("complex128"))
     T, tau = tq.tile_geqrf(A, 256, 32, dag=True)
     assert T.dtype == tdt("complex128")
     with pytest.raises(TypeError):
-        tq.trsm_lun(A[:256, :256], tq.zeros(256, 1, dtype=tdt("complex128")))
+        tq.tile_unmqr_tree("C", A, T, T, tq.zeros(512, 1, dtype=tdt("complex128")), 256, 32)
+    with pytest.raises(TypeError):
+        tq.lstsq_mixed(A, tq.zeros(512, 1, dtype=tdt("complex128")))

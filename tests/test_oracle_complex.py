@@ -247,3 +247,28 @@ def test_ztile_qr_backward_error(oracle, m, n, nb, ib):
     B = A0.copy(order="F")
     oracle.tile_unmqr("C", A, T, B, nb, ib)
     assert np.linalg.norm(B[:n] - R) <= 1e-13 * n * np.linalg.norm(R)
+
+
+def test_ztile_lstsq(oracle):
+    """Complex least squares through the tile QR and LeftUpperTRSM!'s solve."""
+    rng = np.random.default_rng(3)
+    A = Z(rng.standard_normal((600, 300)) + 1j * rng.standard_normal((600, 300)))
+    x = rng.standard_normal((300, 2)) + 1j * rng.standard_normal((300, 2))
+    X = oracle.tile_lstsq(A, A @ x, 128, 32)
+    assert X.dtype == np.complex128
+    assert np.abs(X - x).max() < 1e-10
+
+
+def test_ztrsm_smith_division(oracle):
+    """The back-substitution against numpy's solve on a well-conditioned R,
+    including diagonal entries with a dominant imaginary part (the second
+    branch of Smith's division)."""
+    rng = np.random.default_rng(4)
+    n = 40
+    R = np.triu(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(n)
+    R[np.diag_indices(n)] = (2 + rng.random(n)) * np.exp(1j * rng.uniform(0, 2 * np.pi, n))
+    R = Z(R)
+    B = Z(rng.standard_normal((n, 3)) + 1j * rng.standard_normal((n, 3)))
+    X = B.copy(order="F")
+    oracle.trsm_lun(R, X)
+    assert np.abs(R @ X - B).max() < 1e-13
