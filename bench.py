@@ -60,6 +60,7 @@ def parse():
     p.add_argument("--no-tall", action="store_true", help="skip the tall-skinny flat vs tree comparison")
     p.add_argument("--tall-only", action="store_true", help="run only the tall-skinny flat vs tree comparison")
     p.add_argument("--no-complex", action="store_true", help="skip the complex tile QR")
+    p.add_argument("--no-extras", action="store_true", help="skip the 1024^2 latency and the tiling sweep")
     p.add_argument("--complex-only", action="store_true", help="run only the complex tile QR")
     p.add_argument("--complex-n", type=int, default=4096, help="order of the complex matrix")
     return p.parse_args()
@@ -460,10 +461,15 @@ def batched_bench(torch, nprob=4096, steps=5, warmup=3, peak=None):
         esz = A0.element_size()
         ms = statistics.median(times)
         fl = bg.flops()
+        # algorithmic bytes: read A and B, write R and X: sum(mn + mk + n^2 + nk) elements
+        abytes = esz * sum(m_ * n_ + m_ * k_ + n_ * n_ + n_ * k_ for m_, n_, k_ in zip(ms_, ns_, ks_))
+        hbm, hsrc = hbm_peak_gbs()
         out[tag] = {
             "problems_per_s": nprob / (ms / 1e3), "ms_per_batch": ms, "ms_min": min(times),
             "tflops": fl / (ms / 1e3) / 1e12, "algorithmic_flops_per_batch": fl,
             "frac_of_fp64_simt_peak": (fl / (ms / 1e3) / 1e12 / peak) if (peak and tag == "f64") else None,
+            "algorithmic_bytes_per_batch": abytes, "hbm_gbs": abytes / ms / 1e6,
+            "frac_of_hbm": abytes / ms / 1e6 / hbm, "hbm_peak_source": hsrc,
             "gpu_launches_per_batch": launches / (warmup + steps),
             "rejected_descriptors": bad[0],
             "residual_max": float(res.max().item()), "residual_median": float(res.median().item()),
@@ -514,6 +520,15 @@ def tall_bench(tq, torch, m=65536, n=512, steps=3, warmup=2, peak=None, dtype="f
            "tree": "binary reduction tree, one persistent launch over its task graph"}
     if peak and dtype == "f64":
         out["tree_frac_of_fp64_simt_peak"] = flops / t_tree / 1e9 / peak
+    # the HBM view: A must be read and written at least once per pass, and the
+    # factorisation needs two passes over it (panel reduction, then the update)
+    hbm, src = hbm_peak_gbs()
+    min_bytes = 2 * 2 * m * n * A.element_size()
+    out["hbm_min_bytes"] = min_bytes
+    out["tree_hbm_gbs_at_min_bytes"] = min_bytes / t_tree / 1e6
+    out["tree_frac_of_hbm"] = min_bytes / t_tree / 1e6 / hbm
+    out["hbm_peak_gbs"] = hbm
+    out["hbm_peak_source"] = src
     return out
 
 
@@ -550,6 +565,120 @@ def complex_bench(tq, torch, n=4096, steps=3, warmup=3, peak=None):
         if peak and name == "c128":
             out["c128_dag_frac_of_fp64_simt_peak"] = flops / out["c128_dag_ms"] / 1e9 / peak
     return out
+
+
+def hbm_peak_gbs():
+    """The measured copy bandwidth of the GB300s (MEASURED_PEAKS.json)."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(path))["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback"
+
+
+def latency_bench(tq, torch, n=1024, nrhs=16, reps=20, warmup=5):
+    """1024 x 1024 FP64 tile QR (U[-1,1], seeded, nb = 256, ib = 32: 4 x 4
+    tiles) followed by Q^T applied to 1024 x 16 right-hand sides -- a
+    latency-bound size, reported as latency: device time with the inputs
+    resident, and end to end through the API from pinned host buffers (A and
+    B in, R/V, T and Q^T B out)."""
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    A0 = tq.empty(n, n)
+    A0.copy_(torch.rand(n, n, generator=g, dtype=torch.float64, device="cuda") * 2 - 1)
+    B0 = tq.empty(n, nrhs)
+    B0.copy_(torch.rand(n, nrhs, generator=g, dtype=torch.float64, device="cuda") * 2 - 1)
+    A, B = tq.empty(n, n), tq.empty(n, nrhs)
+    ts, taus = tq.tile_shapes(n, n, NB, IB)
+    T, tau = tq.zeros(*ts), tq.zeros(*taus)
+    st = torch.cuda.current_stream()
+
+    def run():
+        tq.tile_geqrf(A, NB, IB, T, tau)
+        tq.tile_unmqr("C", A, T, B, NB, IB)
+
+    qr_ms, all_ms = [], []
+    for rep in range(warmup + reps):
+        A.copy_(A0)
+        B.copy_(B0)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record(st)
+        tq.tile_geqrf(A, NB, IB, T, tau)
+        ev[1].record(st)
+        tq.tile_unmqr("C", A, T, B, NB, IB)
+        ev[2].record(st)
+        torch.cuda.synchronize()
+        if rep >= warmup:
+            qr_ms.append(ev[0].elapsed_time(ev[1]))
+            all_ms.append(ev[0].elapsed_time(ev[2]))
+    hA = A0.t().cpu().pin_memory()
+    hB = B0.t().cpu().pin_memory()
+    hOut, hBo = torch.empty_like(hA).pin_memory(), torch.empty_like(hB).pin_memory()
+    hT = torch.empty((ts[1], ts[0]), dtype=torch.float64).pin_memory()
+    e2e = []
+    for rep in range(warmup + reps):
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(st)
+        A.t().copy_(hA, non_blocking=True)
+        B.t().copy_(hB, non_blocking=True)
+        run()
+        hOut.copy_(A.t(), non_blocking=True)
+        hT.copy_(T.t(), non_blocking=True)
+        hBo.copy_(B.t(), non_blocking=True)
+        f1.record(st)
+        torch.cuda.synchronize()
+        if rep >= warmup:
+            e2e.append(f0.elapsed_time(f1))
+    fl = flops_square(n) + 4.0 * n * n * nrhs - 2.0 * n * n * nrhs
+    return {"workload": f"tile QR of a {n}x{n} U[-1,1] FP64 matrix (nb={NB}, ib={IB}) + Q^T on {n}x{nrhs}",
+            "qr_ms_median": statistics.median(qr_ms), "qr_plus_apply_ms_median": statistics.median(all_ms),
+            "qr_plus_apply_ms_min": min(all_ms), "e2e_ms_median": statistics.median(e2e),
+            "flops": fl, "tflops_at_median": fl / statistics.median(all_ms) / 1e9,
+            "h2d_bytes": 8 * (n * n + n * nrhs), "d2h_bytes": 8 * (n * n + ts[0] * ts[1] + n * nrhs),
+            "bound": "latency (16 tiles: the panel chain of 4 geqrt + 6 tsqrt is the critical path)"}
+
+
+def autotune_square(tq, torch, n, candidates=((256, 32), (256, 16), (256, 64), (128, 32), (128, 16)),
+                    steps=2, warmup=1):
+    """The square FP64 tile QR over a few (nb, ib) tilings: ms and TFLOP/s of
+    each (persistent kernel where the tiling allows it), and the best."""
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    A0 = tq.empty(n, n)
+    A0.copy_(torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda"))
+    A = tq.empty(n, n)
+    st = torch.cuda.current_stream()
+    res = {}
+    for nb, ib in candidates:
+        ts, taus = tq.tile_shapes(n, n, nb, ib)
+        T, tau = tq.zeros(*ts), tq.zeros(*taus)
+        times = []
+        for rep in range(warmup + steps):
+            A.copy_(A0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            tq.tile_geqrf(A, nb, ib, T, tau)
+            e1.record(st)
+            torch.cuda.synchronize()
+            if rep >= warmup:
+                times.append(e0.elapsed_time(e1))
+        t = min(times)
+        res[f"nb{nb}_ib{ib}"] = {"ms": t, "tflops": flops_square(n) / t / 1e9,
+                                 "persistent": tq.dag_worksize(n, n, nb, ib) is not None}
+        del T, tau
+    best = max(res, key=lambda k: res[k]["tflops"])
+    return {"workload": f"tile QR {n}x{n} FP64 N(0,1), (nb, ib) sweep", "results": res, "best": best}
+
+
+def lapack_dgeqrf_tflops(n):
+    """scipy's LAPACK dgeqrf (OpenBLAS, all host threads) on an n x n N(0,1)
+    matrix: the library CPU QR beside the restated reference algorithm."""
+    import numpy as np
+    from scipy.linalg import lapack
+    rng = np.random.default_rng(SEED)
+    A = np.asfortranarray(rng.standard_normal((n, n)))
+    t0 = time.perf_counter()
+    _, _, _, info = lapack.dgeqrf(A, overwrite_a=1)
+    dt = time.perf_counter() - t0
+    return flops_square(n) / dt / 1e12, dt
 
 
 def adjoint_bench(torch, batch=256, m=2048, n=256, steps=3, warmup=3, peak=None):
@@ -864,6 +993,12 @@ def main():
                "sample": (f"oracle (C restatement of NextLA's kernels, OpenMP over tile columns) "
                           f"flat-tree tile QR of a {CPU_SAMPLE_N}x{CPU_SAMPLE_N} N(0,1) matrix, "
                           f"nb={NB}, ib={IB}; best of {len(times)} runs of {min(times):.1f} s")}
+        try:
+            lv, lt = lapack_dgeqrf_tflops(n)
+            cpu["lapack_dgeqrf"] = {"value": lv, "unit": UNIT, "seconds": lt,
+                                    "sample": f"scipy LAPACK dgeqrf (OpenBLAS, all host threads) on the {n}x{n} matrix"}
+        except Exception as ex:       # scipy missing on the host: report why
+            cpu["lapack_dgeqrf"] = {"unavailable": str(ex)[:200]}
 
     ls = None
     if rank == 0 and world == 1 and not args.no_ls:
@@ -885,6 +1020,12 @@ def main():
     if rank == 0 and world == 1 and not args.no_complex:
         cplx = complex_bench(tq, torch, args.complex_n, 3, 3, peak=peak)
 
+    lat = None
+    tune = None
+    if rank == 0 and world == 1 and not args.no_extras:
+        lat = latency_bench(tq, torch)
+        tune = autotune_square(tq, torch, n)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -899,6 +1040,8 @@ def main():
             "differentiable_qr": adj,
             "tall_skinny_65536x512": tall,
             "complex_tile_qr": cplx,
+            "latency_1024": lat,
+            "tiling_sweep": tune,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
