@@ -462,7 +462,8 @@ def batched_bench(torch, nprob=4096, steps=5, warmup=3, peak=None):
         ms = statistics.median(times)
         fl = bg.flops()
         # algorithmic bytes: read A and B, write R and X: sum(mn + mk + n^2 + nk) elements
-        abytes = esz * sum(m_ * n_ + m_ * k_ + n_ * n_ + n_ * k_ for m_, n_, k_ in zip(ms_, ns_, ks_))
+        abytes = esz * sum(int(m_) * int(n_) + int(m_) * int(k_) + int(n_) * int(n_) + int(n_) * int(k_)
+                           for m_, n_, k_ in zip(ms_, ns_, ks_))
         hbm, hsrc = hbm_peak_gbs()
         out[tag] = {
             "problems_per_s": nprob / (ms / 1e3), "ms_per_batch": ms, "ms_min": min(times),
