@@ -61,6 +61,7 @@ def parse():
     p.add_argument("--tall-only", action="store_true", help="run only the tall-skinny flat vs tree comparison")
     p.add_argument("--no-complex", action="store_true", help="skip the complex tile QR")
     p.add_argument("--no-extras", action="store_true", help="skip the 1024^2 latency and the tiling sweep")
+    p.add_argument("--latency-only", action="store_true", help="run only the 1024^2 latency line")
     p.add_argument("--complex-only", action="store_true", help="run only the complex tile QR")
     p.add_argument("--complex-n", type=int, default=4096, help="order of the complex matrix")
     return p.parse_args()
@@ -838,6 +839,15 @@ def main():
         peak = fp64_peak(_lib, torch)
         res = {"f64": tall_bench(tq, torch, peak=peak), "f32": tall_bench(tq, torch, dtype="f32")}
         print(json.dumps(res), flush=True)
+        return 0
+    if args.latency_only:
+        import torch
+
+        import tileqr as tq
+        import tileqr_build
+        tileqr_build.build()
+        tq.set_blocking(False)
+        print(json.dumps(latency_bench(tq, torch)), flush=True)
         return 0
     if args.complex_only:
         import torch

@@ -15,6 +15,9 @@ k_apply(const ApplyArgs<R> a)
   apply_strip<R, NW>(a, blockIdx.x * NW, smem_raw);
 }
 
+// Fewest CTAs a stand-alone apply should run on before narrower strips are used.
+constexpr int kMinStripCtas = 32;
+
 template <typename R>
 ApplyArgs<R> make_apply_args(int mode, char side, char trans, int m, int n, int k, int ib, R *C,
                              int ldc, R *A1, int lda1, const R *V, int ldv, const R *T, int ldt,
@@ -50,6 +53,11 @@ ApplyArgs<R> make_apply_args(int mode, char side, char trans, int m, int n, int 
   if (bytes(nw) > cap) sv = false;
   if (bytes(nw) > cap) sc = false;
   while (bytes(nw) > cap && nw > 1) nw = (nw == 16) ? 8 : (nw == 8 ? 4 : 1);
+  // A narrow operand (a few right-hand sides) would leave all but a CTA or
+  // two idle, each CTA working through every block at one SM's FP64 rate:
+  // narrower strips spread it over more SMs.  The per-column arithmetic does
+  // not depend on the strip width, so results are unchanged bit for bit.
+  while (nw > 1 && (a.ncols + nw - 1) / nw < kMinStripCtas) nw = (nw == 16) ? 8 : (nw == 8 ? 4 : 1);
   a.nw = nw;
   a.stage_c = sc; a.stage_v = sv; a.stage_t = stt;
   *smem_bytes = bytes(nw);
