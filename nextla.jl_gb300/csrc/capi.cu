@@ -33,7 +33,7 @@ int geqr2_impl(int m, int n, R *A, int lda, R *tau, cudaStream_t st) {
   if (n < 0) return -2;
   if (lda < (m > 1 ? m : 1)) return -4;
   if (m == 0 || n == 0) return 0;
-  return rc(launch_panel_qr<R>(m, n, A, lda, tau, (R *)nullptr, 1, st));
+  return rc(launch_panel_qr<R>(m, n, A, lda, tau, (R *)nullptr, 1, st, true));
 }
 
 template <typename R>
@@ -64,8 +64,12 @@ int larfb_impl(char side, char trans, char direct, char storev, int m, int n, in
   return rc(launch_apply<R>(0, side, trans, m, n, k, k, C, ldc, (R *)nullptr, 0, V, ldv, T, ldt, st));
 }
 
+}  // namespace
+
+namespace tqr {
+
 template <typename R>
-int geqrt_impl(int m, int n, int ib, R *A, int lda, R *T, int ldt, R *tau, cudaStream_t st) {
+int geqrt_impl(int m, int n, int ib, R *A, int lda, R *T, int ldt, R *tau, cudaStream_t st, bool cluster) {
   if (m < 0) return -1;                      // src/geqrt.jl:24-34
   if (n < 0) return -2;
   if (ib < 0 || (ib == 0 && m > 0 && n > 0)) return -3;
@@ -77,7 +81,7 @@ int geqrt_impl(int m, int n, int ib, R *A, int lda, R *T, int ldt, R *tau, cudaS
     const int sb = ib < k - i ? ib : k - i;
     R *av = A + ix(i, i, lda);
     R *tv = T + ix(0, i, ldt);
-    cudaError_t e = launch_panel_qr<R>(m - i, sb, av, lda, tau + i, tv, ldt, st);
+    cudaError_t e = launch_panel_qr<R>(m - i, sb, av, lda, tau + i, tv, ldt, st, cluster);
     if (e != cudaSuccess) return rc(e);
     if (n > i + sb) {
       e = launch_apply<R>(0, 'L', 'C', m - i, n - i - sb, sb, sb, A + ix(i, i + sb, lda), lda,
@@ -127,6 +131,10 @@ int tsmqr_impl(char side, char trans, int m1, int n1, int m2, int n2, int k, int
   if (ldt < (ib < k ? ib : k)) return -16;
   return rc(launch_apply<R>(1, side, trans, m2, n2, k, ib, A2, lda2, A1, lda1, V, ldv, T, ldt, st));
 }
+
+}  // namespace tqr
+
+namespace {
 
 template <typename R>
 int parfb_impl(char side, char trans, char direct, char storev, int m1, int n1, int m2, int n2,
@@ -192,7 +200,7 @@ int ttqrt_impl(int m, int n, int ib, R *A1, int lda1, R *A2, int lda2, R *T, int
   for (int ii = 0; ii < k; ii += ib) {       // src/ttqrt.jl:102-117
     const int sb = (k - ii) < ib ? (k - ii) : ib;
     cudaError_t e = launch_tsqrt_block<R>(m, sb, A1 + ix(ii, ii, lda1), lda1, A2 + ix(0, ii, lda2),
-                                          lda2, T + ix(0, ii, ldt), ldt, tau + ii, st, ii);
+                                          lda2, T + ix(0, ii, ldt), ldt, tau + ii, st, ii, true);
     if (e != cudaSuccess) return rc(e);
     if (n > ii + sb) {
       const int mi = (ii + sb) < m ? (ii + sb) : m;
@@ -205,9 +213,13 @@ int ttqrt_impl(int m, int n, int ib, R *A1, int lda1, R *A2, int lda2, R *T, int
   return 0;
 }
 
+}  // namespace
+
+namespace tqr {
+
 template <typename R>
 int tsqrt_impl(int m, int n, int ib, int m1, R *A1, int lda1, R *A2, int lda2, R *T, int ldt,
-               R *tau, cudaStream_t st) {
+               R *tau, cudaStream_t st, bool cluster) {
   if (m < 0) return -1;                      // src/tsqrt.jl:129-144
   if (n < 0) return -2;
   if (ib < 0) return -3;
@@ -220,7 +232,7 @@ int tsqrt_impl(int m, int n, int ib, int m1, R *A1, int lda1, R *A2, int lda2, R
   for (int ii = 0; ii < k; ii += ib) {       // src/tsqrt.jl:146-155
     const int sb = (k - ii) < ib ? (k - ii) : ib;
     cudaError_t e = launch_tsqrt_block<R>(m, sb, A1 + ix(ii, ii, lda1), lda1, A2 + ix(0, ii, lda2),
-                                          lda2, T + ix(0, ii, ldt), ldt, tau + ii, st);
+                                          lda2, T + ix(0, ii, ldt), ldt, tau + ii, st, -1, cluster);
     if (e != cudaSuccess) return rc(e);
     if (n > ii + sb) {
       e = launch_apply<R>(1, 'L', 'C', m, n - ii - sb, sb, ib, A2 + ix(0, ii + sb, lda2), lda2,
@@ -232,7 +244,20 @@ int tsqrt_impl(int m, int n, int ib, int m1, R *A1, int lda1, R *A2, int lda2, R
   return 0;
 }
 
-}  // namespace
+#define TQR_IMPL_INST(R)                                                                                  \
+  template int geqrt_impl<R>(int, int, int, R *, int, R *, int, R *, cudaStream_t, bool);                \
+  template int tsqrt_impl<R>(int, int, int, int, R *, int, R *, int, R *, int, R *, cudaStream_t, bool); \
+  template int unmqr_impl<R>(char, char, int, int, int, int, const R *, int, const R *, int, R *, int,   \
+                             cudaStream_t);                                                              \
+  template int tsmqr_impl<R>(char, char, int, int, int, int, int, int, R *, int, R *, int, const R *, int, \
+                             const R *, int, cudaStream_t);
+TQR_IMPL_INST(double)
+TQR_IMPL_INST(float)
+TQR_IMPL_INST(cx<double>)
+TQR_IMPL_INST(cx<float>)
+#undef TQR_IMPL_INST
+
+}  // namespace tqr
 
 extern "C" {
 
@@ -271,7 +296,7 @@ extern "C" {
     if (!al<R>(A)) return -4;                                                                        \
     if (!al<R>(T)) return -6;                                                                        \
     if (!al<R>(tau)) return -8;                                                                      \
-    return geqrt_impl<R>(m, n, ib, dp<R>(A), lda, dp<R>(T), ldt, dp<R>(tau), stream);                \
+    return geqrt_impl<R>(m, n, ib, dp<R>(A), lda, dp<R>(T), ldt, dp<R>(tau), stream, true);          \
   }                                                                                                  \
   int tqr_##P##unmqr(char side, char trans, int m, int n, int k, int ib, const CT *A, int lda,       \
                      const CT *T, int ldt, CT *C, int ldc, CT *work, int ldwork,                     \
@@ -291,7 +316,7 @@ extern "C" {
     if (!al<R>(T)) return -9;                                                                        \
     if (!al<R>(tau)) return -11;                                                                     \
     return tsqrt_impl<R>(m, n, ib, m1, dp<R>(A1), lda1, dp<R>(A2), lda2, dp<R>(T), ldt, dp<R>(tau),  \
-                         stream);                                                                    \
+                         stream, true);                                                              \
   }                                                                                                  \
   int tqr_##P##tsmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, CT *A1,   \
                      int lda1, CT *A2, int lda2, const CT *V, int ldv, const CT *T, int ldt,         \

@@ -7,7 +7,7 @@
 //                 (NextLA src/larft.jl:48-203).
 //
 // The per-panel algorithms are panel_qr_cta / tsqrt_block_cta (panel_dev.cuh).
-#include "panel_dev.cuh"
+#include "panel_cluster.cuh"
 #include "tileqr_internal.h"
 
 namespace tqr {
@@ -28,6 +28,14 @@ k_tsqrt_block(int m, int sb, R *__restrict__ A1, int lda1, R *__restrict__ A2, i
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   tsqrt_block_cta<R>(m, sb, A1, lda1, A2, lda2, T, ldt, tau, staged != 0, smem_raw, tt);
+}
+
+template <typename E>
+__global__ void __launch_bounds__(TQR_THREADS)
+k_panel_cluster(const ClusterPanelArgs<E> a, int C)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cluster_panel<E>(a, C, smem_raw);
 }
 
 // ---------------------------------------------------------------------------
@@ -148,8 +156,50 @@ static cudaError_t allow_smem(K kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+// Cluster size for a panel touching mrow rows: 0 when one CTA is the better
+// choice (too few rows to split) or the columns exceed the cluster kernel's.
+static int cluster_size_for(int mrow, int nc) {
+  if (nc > 64) return 0;
+  return mrow >= 192 ? 8 : (mrow >= 96 ? 4 : (mrow >= 64 ? 2 : 0));
+}
+
+// Launches the cluster panel; *used = false (and nothing launched) when the
+// shape is better left to one CTA or its rows do not fit a cluster of 8.
+template <typename E>
+static cudaError_t launch_cluster(const ClusterPanelArgs<E> &a, int mrow, cudaStream_t st, bool *used) {
+  *used = false;
+  const int C = cluster_size_for(mrow, a.nc);
+  if (!C) return cudaSuccess;
+  const size_t sm = cluster_panel_smem<E>(mrow, a.nc, C);
+  if (sm > (size_t)TQR_SMEM_MAX) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(k_panel_cluster<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(C, 1, 1);
+  cfg.blockDim = dim3(TQR_THREADS, 1, 1);
+  cfg.dynamicSmemBytes = sm;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, k_panel_cluster<E>, a, C);
+  count_launch();
+  *used = true;
+  return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
 template <typename R>
-cudaError_t launch_panel_qr(int m, int nc, R *A, int lda, R *tau, R *T, int ldt, cudaStream_t st) {
+cudaError_t launch_panel_qr(int m, int nc, R *A, int lda, R *tau, R *T, int ldt, cudaStream_t st, bool cluster) {
+  if (cluster) {
+    ClusterPanelArgs<R> a{0, m, nc, A, lda, nullptr, 1, T, ldt, tau, -1};
+    bool used = false;
+    cudaError_t e = launch_cluster<R>(a, m, st, &used);
+    if (used || e != cudaSuccess) return e;
+  }
   const bool stage_t = (T != nullptr) && nc <= 64;
   bool staged = panel_smem<R>(m, nc, true, stage_t) <= (size_t)TQR_SMEM_MAX;
   size_t sm = panel_smem<R>(m, nc, staged, stage_t);
@@ -163,8 +213,14 @@ cudaError_t launch_panel_qr(int m, int nc, R *A, int lda, R *tau, R *T, int ldt,
 
 template <typename R>
 cudaError_t launch_tsqrt_block(int m, int sb, R *A1, int lda1, R *A2, int lda2, R *T, int ldt,
-                               R *tau, cudaStream_t st, int tt) {
+                               R *tau, cudaStream_t st, int tt, bool cluster) {
   const int mrow = tt >= 0 ? (m < tt + sb ? m : tt + sb) : m;
+  if (cluster) {
+    ClusterPanelArgs<R> a{1, m, sb, A2, lda2, A1, lda1, T, ldt, tau, tt};
+    bool used = false;
+    cudaError_t e = launch_cluster<R>(a, mrow, st, &used);
+    if (used || e != cudaSuccess) return e;
+  }
   bool staged = tsqrt_smem<R>(mrow, sb, true) <= (size_t)TQR_SMEM_MAX;
   size_t sm = tsqrt_smem<R>(mrow, sb, staged);
   if (sm > (size_t)TQR_SMEM_MAX) return cudaErrorInvalidValue;
@@ -187,16 +243,16 @@ cudaError_t launch_larft(int direct_f, int storev_c, int n, int k, const R *V, i
   return cudaGetLastError();
 }
 
-template cudaError_t launch_panel_qr<double>(int, int, double *, int, double *, double *, int, cudaStream_t);
-template cudaError_t launch_panel_qr<float>(int, int, float *, int, float *, float *, int, cudaStream_t);
-template cudaError_t launch_tsqrt_block<double>(int, int, double *, int, double *, int, double *, int, double *, cudaStream_t, int);
-template cudaError_t launch_tsqrt_block<float>(int, int, float *, int, float *, int, float *, int, float *, cudaStream_t, int);
+template cudaError_t launch_panel_qr<double>(int, int, double *, int, double *, double *, int, cudaStream_t, bool);
+template cudaError_t launch_panel_qr<float>(int, int, float *, int, float *, float *, int, cudaStream_t, bool);
+template cudaError_t launch_tsqrt_block<double>(int, int, double *, int, double *, int, double *, int, double *, cudaStream_t, int, bool);
+template cudaError_t launch_tsqrt_block<float>(int, int, float *, int, float *, int, float *, int, float *, cudaStream_t, int, bool);
 template cudaError_t launch_larft<double>(int, int, int, int, const double *, int, const double *, double *, int, cudaStream_t);
 template cudaError_t launch_larft<float>(int, int, int, int, const float *, int, const float *, float *, int, cudaStream_t);
 
 #define TQR_PANEL_INST(E)                                                                                         \
-  template cudaError_t launch_panel_qr<E>(int, int, E *, int, E *, E *, int, cudaStream_t);                       \
-  template cudaError_t launch_tsqrt_block<E>(int, int, E *, int, E *, int, E *, int, E *, cudaStream_t, int);     \
+  template cudaError_t launch_panel_qr<E>(int, int, E *, int, E *, E *, int, cudaStream_t, bool);                       \
+  template cudaError_t launch_tsqrt_block<E>(int, int, E *, int, E *, int, E *, int, E *, cudaStream_t, int, bool);     \
   template cudaError_t launch_larft<E>(int, int, int, int, const E *, int, const E *, E *, int, cudaStream_t);
 TQR_PANEL_INST(cx<double>)
 TQR_PANEL_INST(cx<float>)

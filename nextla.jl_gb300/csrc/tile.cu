@@ -27,68 +27,26 @@ using namespace tqr;
 
 namespace {
 
-template <typename R> struct K;
-template <> struct K<double> {
-  static int geqrt(int m, int n, int ib, double *A, int lda, double *T, int ldt, double *tau, cudaStream_t s) {
-    return tqr_dgeqrt(m, n, ib, A, lda, T, ldt, tau, nullptr, s);
+// The kernels the driver composes: the C-ABI routines' bodies with the
+// one-CTA panels, whose per-task arithmetic is the persistent schedule's, so
+// the two drivers give the same bits.
+template <typename R> struct K {
+  static int geqrt(int m, int n, int ib, R *A, int lda, R *T, int ldt, R *tau, cudaStream_t s) {
+    return geqrt_impl<R>(m, n, ib, A, lda, T, ldt, tau, s, false);
   }
-  static int tsqrt(int m, int n, int ib, int m1, double *A1, int lda1, double *A2, int lda2, double *T, int ldt,
-                   double *tau, cudaStream_t s) {
-    return tqr_dtsqrt(m, n, ib, m1, A1, lda1, A2, lda2, T, ldt, tau, nullptr, s);
+  static int tsqrt(int m, int n, int ib, int m1, R *A1, int lda1, R *A2, int lda2, R *T, int ldt, R *tau,
+                   cudaStream_t s) {
+    return tsqrt_impl<R>(m, n, ib, m1, A1, lda1, A2, lda2, T, ldt, tau, s, false);
   }
-  static int unmqr(char side, char trans, int m, int n, int k, int ib, const double *A, int lda, const double *T,
-                   int ldt, double *C, int ldc, cudaStream_t s) {
-    return tqr_dunmqr(side, trans, m, n, k, ib, A, lda, T, ldt, C, ldc, nullptr, 0, s);
+  static int unmqr(char side, char trans, int m, int n, int k, int ib, const R *A, int lda, const R *T, int ldt,
+                   R *C, int ldc, cudaStream_t s) {
+    return unmqr_impl<R>(side, trans, m, n, k, ib, A, lda, T, ldt, C, ldc, s);
   }
-  static int tsmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, double *A1, int lda1,
-                   double *A2, int lda2, const double *V, int ldv, const double *T, int ldt, cudaStream_t s) {
-    return tqr_dtsmqr(side, trans, m1, n1, m2, n2, k, ib, A1, lda1, A2, lda2, V, ldv, T, ldt, nullptr, 0, s);
-  }
-};
-template <> struct K<float> {
-  static int geqrt(int m, int n, int ib, float *A, int lda, float *T, int ldt, float *tau, cudaStream_t s) {
-    return tqr_sgeqrt(m, n, ib, A, lda, T, ldt, tau, nullptr, s);
-  }
-  static int tsqrt(int m, int n, int ib, int m1, float *A1, int lda1, float *A2, int lda2, float *T, int ldt,
-                   float *tau, cudaStream_t s) {
-    return tqr_stsqrt(m, n, ib, m1, A1, lda1, A2, lda2, T, ldt, tau, nullptr, s);
-  }
-  static int unmqr(char side, char trans, int m, int n, int k, int ib, const float *A, int lda, const float *T,
-                   int ldt, float *C, int ldc, cudaStream_t s) {
-    return tqr_sunmqr(side, trans, m, n, k, ib, A, lda, T, ldt, C, ldc, nullptr, 0, s);
-  }
-  static int tsmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, float *A1, int lda1,
-                   float *A2, int lda2, const float *V, int ldv, const float *T, int ldt, cudaStream_t s) {
-    return tqr_stsmqr(side, trans, m1, n1, m2, n2, k, ib, A1, lda1, A2, lda2, V, ldv, T, ldt, nullptr, 0, s);
+  static int tsmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, R *A1, int lda1,
+                   R *A2, int lda2, const R *V, int ldv, const R *T, int ldt, cudaStream_t s) {
+    return tsmqr_impl<R>(side, trans, m1, n1, m2, n2, k, ib, A1, lda1, A2, lda2, V, ldv, T, ldt, s);
   }
 };
-
-// Complex elements: the C-ABI takes tqr_zcomplex / tqr_ccomplex, the same
-// layout as cx<double> / cx<float>.
-#define TQR_K_COMPLEX(P, CT, E)                                                                                  \
-  template <> struct K<E> {                                                                                      \
-    static CT *c(E *p) { return reinterpret_cast<CT *>(p); }                                                      \
-    static const CT *c(const E *p) { return reinterpret_cast<const CT *>(p); }                                    \
-    static int geqrt(int m, int n, int ib, E *A, int lda, E *T, int ldt, E *tau, cudaStream_t s) {               \
-      return tqr_##P##geqrt(m, n, ib, c(A), lda, c(T), ldt, c(tau), nullptr, s);                                 \
-    }                                                                                                            \
-    static int tsqrt(int m, int n, int ib, int m1, E *A1, int lda1, E *A2, int lda2, E *T, int ldt, E *tau,      \
-                     cudaStream_t s) {                                                                           \
-      return tqr_##P##tsqrt(m, n, ib, m1, c(A1), lda1, c(A2), lda2, c(T), ldt, c(tau), nullptr, s);              \
-    }                                                                                                            \
-    static int unmqr(char side, char trans, int m, int n, int k, int ib, const E *A, int lda, const E *T,        \
-                     int ldt, E *C, int ldc, cudaStream_t s) {                                                   \
-      return tqr_##P##unmqr(side, trans, m, n, k, ib, c(A), lda, c(T), ldt, c(C), ldc, nullptr, 0, s);           \
-    }                                                                                                            \
-    static int tsmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, E *A1, int lda1,      \
-                     E *A2, int lda2, const E *V, int ldv, const E *T, int ldt, cudaStream_t s) {                \
-      return tqr_##P##tsmqr(side, trans, m1, n1, m2, n2, k, ib, c(A1), lda1, c(A2), lda2, c(V), ldv, c(T), ldt, \
-                            nullptr, 0, s);                                                                      \
-    }                                                                                                            \
-  };
-TQR_K_COMPLEX(z, tqr_zcomplex, cx<double>)
-TQR_K_COMPLEX(c, tqr_ccomplex, cx<float>)
-#undef TQR_K_COMPLEX
 
 // Internal streams of one device: a high-priority panel stream and a
 // low-priority update stream, plus the events that order them.

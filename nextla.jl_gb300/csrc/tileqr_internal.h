@@ -11,15 +11,34 @@ bool profiling();
 void *prof_begin(cudaStream_t st);
 void prof_end(void *tok, cudaStream_t st, double flops);
 
-// geqr2 (+ T when T != nullptr) on an m-by-nc panel, one CTA.
+// geqr2 (+ T when T != nullptr) on an m-by-nc panel: one CTA, or with
+// cluster = true a thread-block cluster splitting the rows when the panel is
+// tall enough (panel_cluster.cuh; different summation order, same bar).
 template <typename R>
-cudaError_t launch_panel_qr(int m, int nc, R *A, int lda, R *tau, R *T, int ldt, cudaStream_t st);
+cudaError_t launch_panel_qr(int m, int nc, R *A, int lda, R *tau, R *T, int ldt, cudaStream_t st,
+                            bool cluster = false);
 
-// One ib-block of tsqrt (pointers already offset to the block), one CTA;
-// tt >= 0: the ttqrt block whose first column is column tt of the triangle.
+// One ib-block of tsqrt (pointers already offset to the block), one CTA or
+// (cluster = true) a cluster; tt >= 0: the ttqrt block whose first column is
+// column tt of the triangle.
 template <typename R>
 cudaError_t launch_tsqrt_block(int m, int sb, R *A1, int lda1, R *A2, int lda2, R *T, int ldt,
-                               R *tau, cudaStream_t st, int tt = -1);
+                               R *tau, cudaStream_t st, int tt = -1, bool cluster = false);
+
+// The C-ABI routines' bodies (capi.cu).  `cluster` selects the cluster panel
+// for the panel steps: the entry points use it; the stream tile driver does
+// not, so that it stays bit-identical to the persistent schedule.
+template <typename R>
+int geqrt_impl(int m, int n, int ib, R *A, int lda, R *T, int ldt, R *tau, cudaStream_t st, bool cluster);
+template <typename R>
+int tsqrt_impl(int m, int n, int ib, int m1, R *A1, int lda1, R *A2, int lda2, R *T, int ldt, R *tau,
+               cudaStream_t st, bool cluster);
+template <typename R>
+int unmqr_impl(char side, char trans, int m, int n, int k, int ib, const R *A, int lda, const R *T, int ldt,
+               R *C, int ldc, cudaStream_t st);
+template <typename R>
+int tsmqr_impl(char side, char trans, int m1, int n1, int m2, int n2, int k, int ib, R *A1, int lda1, R *A2,
+               int lda2, const R *V, int ldv, const R *T, int ldt, cudaStream_t st);
 
 template <typename R>
 cudaError_t launch_larft(int direct_f, int storev_c, int n, int k, const R *V, int ldv,
