@@ -331,6 +331,35 @@ int tqr_dtile_geqrf_tree_dag(int m, int n, int nb, int ib, double *A, int lda, d
 int tqr_stile_geqrf_tree_dag(int m, int n, int nb, int ib, float *A, int lda, float *T, float *T2,
                              int ldt, float *tau, float *tau2, int ldtau, int nrhs, float *B, int ldb,
                              void *work, size_t lwork, cudaStream_t stream);
+/* Hierarchical form (PLASMA's HQR): the tiles of each panel form groups of
+ * grp consecutive tiles, each reduced flat into its first tile (geqrt! on the
+ * leader, tsqrt!/tsmqr! of the others into it -- their reflectors in the whole
+ * tile, with T2 / tau2), then the leaders by the binary ttqrt!/ttmqr! tree at
+ * distances grp, 2 grp, ...; a ragged last tile joins the last group.
+ * grp = 1 is tqr_?tile_geqrf_tree; a panel's serial chain is grp + log2 of its
+ * leader count tile steps.  Same layouts as the tree form; the Q application
+ * takes the same grp. */
+int tqr_dtile_geqrf_hqr(int m, int n, int nb, int ib, int grp, double *A, int lda, double *T, double *T2,
+                        int ldt, double *tau, double *tau2, int ldtau, int nrhs, double *B, int ldb,
+                        cudaStream_t stream);
+int tqr_stile_geqrf_hqr(int m, int n, int nb, int ib, int grp, float *A, int lda, float *T, float *T2,
+                        int ldt, float *tau, float *tau2, int ldtau, int nrhs, float *B, int ldb,
+                        cudaStream_t stream);
+int tqr_tile_hqr_dag_worksize(int m, int n, int nb, int ib, int grp, int nrhs, size_t *bytes);
+int tqr_tile_hqr_dag_check(int m, int n, int nb, int ib, int grp, int nrhs, long long *ntasks);
+int tqr_dtile_geqrf_hqr_dag(int m, int n, int nb, int ib, int grp, double *A, int lda, double *T,
+                            double *T2, int ldt, double *tau, double *tau2, int ldtau, int nrhs, double *B,
+                            int ldb, void *work, size_t lwork, cudaStream_t stream);
+int tqr_stile_geqrf_hqr_dag(int m, int n, int nb, int ib, int grp, float *A, int lda, float *T, float *T2,
+                            int ldt, float *tau, float *tau2, int ldtau, int nrhs, float *B, int ldb,
+                            void *work, size_t lwork, cudaStream_t stream);
+int tqr_dtile_unmqr_hqr(char trans, int m, int n, int nrhs, int nb, int ib, int grp, const double *A,
+                        int lda, const double *T, const double *T2, int ldt, double *B, int ldb,
+                        cudaStream_t stream);
+int tqr_stile_unmqr_hqr(char trans, int m, int n, int nrhs, int nb, int ib, int grp, const float *A,
+                        int lda, const float *T, const float *T2, int ldt, float *B, int ldb,
+                        cudaStream_t stream);
+
 /* B := Q^T B (trans 'C'/'T') or Q B ('N') with Q from tqr_?tile_geqrf_tree. */
 int tqr_dtile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, const double *A, int lda,
                          const double *T, const double *T2, int ldt, double *B, int ldb,

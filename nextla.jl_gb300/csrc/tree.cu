@@ -6,7 +6,12 @@
 // For panel k the flat tree chains MT - k tsqrt! calls; here every tile of the
 // panel is factored at once (geqrt!), then pairs at distance s = 1, 2, 4, ...
 // are merged by ttqrt!, so the serial chain per panel is 1 + ceil(log2(MT - k))
-// tile steps.  A last row tile with fewer rows than the panel has columns
+// tile steps.  The hierarchical form (group size grp > 1, PLASMA's HQR) first
+// reduces groups of grp consecutive tiles flat into their first tile (geqrt!
+// on that leader, tsqrt!/tsmqr! of each other tile into it -- the flat tree's
+// arithmetic), then the leaders by the binary tree at distances grp, 2 grp,
+// ...: a chain of grp + log2 of the leader count per panel with the flat
+// tree's update flops inside the groups.  A last row tile with fewer rows than the panel has columns
 // would become a wide trapezoid that ttqrt! (min(m, n) reflectors) cannot
 // reduce; it is merged whole into the tile above it by tsqrt!/tsmqr! first.
 //
@@ -40,6 +45,7 @@ constexpr size_t kTreeSmem = 110976;
 template <typename R>
 struct TreeGeom {
   int m, n, nb, ib, MT, NT, KT, nrhs;
+  int grp;           // tiles per flat group (1: the binary tree)
   R *A; int lda;
   R *B; int ldb;
   R *T, *T2; int ldt;
@@ -221,35 +227,40 @@ static int tree_pairs(int k, int MTt, int s) {
   return c;
 }
 
+// Leaders of panel k: tiles k, k + grp, ... below MTt; the last one takes
+// the ragged tile.
+static inline int tree_nlead(int k, int MTt, int grp) { return (MTt - k + grp - 1) / grp; }
+
 template <typename R>
 static cudaError_t tree_factor(const TreeGeom<R> &g, cudaStream_t st) {
   cudaError_t e = cudaFuncSetAttribute(k_tree<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTreeSmem);
   if (e != cudaSuccess) return e;
-  const int ib = g.ib;
+  const int ib = g.ib, G = g.grp;
   for (int k = 0; k < g.KT; ++k) {
     const int nk = g.cols(k);
     const bool rag = tree_ragged(g, k);
     const int MTt = rag ? g.MT - 1 : g.MT;
     const int nblk = (nk + ib - 1) / ib;
-    const int ntile = MTt - k;
+    const int nlead = tree_nlead(k, MTt, G);
+    const int last = k + (nlead - 1) * G;
     TreeOp op{};
-    op.k = k; op.i0 = k; op.istep = 1; op.a_cols = 1;
-    // reflectors of the shortest tile: its blocks end earliest, so its strips
-    // reach furthest left (the other tiles skip the strips they do not need)
-    const int kkmin = std::min(g.rows(MTt - 1), nk);
+    op.k = k; op.i0 = k; op.istep = G; op.a_cols = 1;
+    // reflectors of the shortest leader: its blocks end earliest, so its
+    // strips reach furthest left (the other tiles skip the strips they do not need)
+    const int kkmin = std::min(g.rows(last), nk);
     for (int b = 0; b < nblk; ++b) {
       op.b = b;
       op.type = OP_GE_PANEL;
-      if ((e = tree_launch(g, op, ntile, 1, st)) != cudaSuccess) return e;
+      if ((e = tree_launch(g, op, nlead, 1, st)) != cudaSuccess) return e;
       const int rest = nk - std::min(nk, std::min(kkmin, (b + 1) * ib));
       op.type = OP_GE_APPLY;
-      if ((e = tree_launch(g, op, ntile, (rest + kTreeNW - 1) / kTreeNW, st)) != cudaSuccess) return e;
+      if ((e = tree_launch(g, op, nlead, (rest + kTreeNW - 1) / kTreeNW, st)) != cudaSuccess) return e;
     }
     op.type = OP_GE_TRAIL; op.trans = 0;
-    if ((e = tree_launch(g, op, ntile, trail_strips(g, k, 1), st)) != cudaSuccess) return e;
-    auto merge = [&](int i0, int s, int npair, int ts) -> cudaError_t {
+    if ((e = tree_launch(g, op, nlead, trail_strips(g, k, 1), st)) != cudaSuccess) return e;
+    auto merge = [&](int i0, int s, int istep, int npair, int ts) -> cudaError_t {
       TreeOp q{};
-      q.k = k; q.i0 = i0; q.istep = 2 * s; q.s = s; q.ts = ts; q.a_cols = 1;
+      q.k = k; q.i0 = i0; q.istep = istep; q.s = s; q.ts = ts; q.a_cols = 1;
       const int kt = ts ? nk : std::min(g.rows(i0 + s), nk);
       const int nb2 = (kt + ib - 1) / ib;
       cudaError_t e2;
@@ -264,9 +275,15 @@ static cudaError_t tree_factor(const TreeGeom<R> &g, cudaStream_t st) {
       q.type = OP_PR_TRAIL; q.trans = 0;
       return tree_launch(g, q, npair, trail_strips(g, k, 1), st);
     };
-    if (rag && (e = merge(g.MT - 2, 1, 1, 1)) != cudaSuccess) return e;
-    for (int s = 1; k + s < MTt; s *= 2)
-      if ((e = merge(k, s, tree_pairs(k, MTt, s), 0)) != cudaSuccess) return e;
+    // flat reduction inside the groups (tile i + d into leader i), then the
+    // ragged tile into the last leader
+    for (int d = 1; d < G; ++d) {
+      const int npair = (MTt - 1 - d - k) >= 0 ? (MTt - 1 - d - k) / G + 1 : 0;
+      if (npair > 0 && (e = merge(k, d, G, npair, 1)) != cudaSuccess) return e;
+    }
+    if (rag && (e = merge(last, g.MT - 1 - last, 1, 1, 1)) != cudaSuccess) return e;
+    for (int s = G; k + s < MTt; s *= 2)
+      if ((e = merge(k, s, 2 * s, tree_pairs(k, MTt, s), 0)) != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
@@ -276,31 +293,41 @@ template <typename R>
 static cudaError_t tree_apply_q(const TreeGeom<R> &g, int trans, cudaStream_t st) {
   cudaError_t e = cudaFuncSetAttribute(k_tree<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTreeSmem);
   if (e != cudaSuccess) return e;
-  const int ny = (g.nrhs + kTreeNW - 1) / kTreeNW;
+  const int ny = (g.nrhs + kTreeNW - 1) / kTreeNW, G = g.grp;
   for (int kx = 0; kx < g.KT; ++kx) {
     const int k = trans ? g.KT - 1 - kx : kx;
     const bool rag = tree_ragged(g, k);
     const int MTt = rag ? g.MT - 1 : g.MT;
+    const int nlead = tree_nlead(k, MTt, G);
+    const int last = k + (nlead - 1) * G;
     TreeOp ge{};
-    ge.type = OP_GE_TRAIL; ge.k = k; ge.i0 = k; ge.istep = 1; ge.trans = trans; ge.a_cols = 0;
-    auto pair = [&](int i0, int s, int npair, int ts) {
+    ge.type = OP_GE_TRAIL; ge.k = k; ge.i0 = k; ge.istep = G; ge.trans = trans; ge.a_cols = 0;
+    auto pair = [&](int i0, int s, int istep, int npair, int ts) {
       TreeOp q{};
-      q.type = OP_PR_TRAIL; q.k = k; q.i0 = i0; q.istep = 2 * s; q.s = s; q.ts = ts; q.trans = trans;
+      q.type = OP_PR_TRAIL; q.k = k; q.i0 = i0; q.istep = istep; q.s = s; q.ts = ts; q.trans = trans;
       q.a_cols = 0;
       return tree_launch(g, q, npair, ny, st);
     };
+    auto group = [&](int d) {
+      const int npair = (MTt - 1 - d - k) >= 0 ? (MTt - 1 - d - k) / G + 1 : 0;
+      return npair > 0 ? pair(k, d, G, npair, 1) : cudaSuccess;
+    };
     if (!trans) {
-      if ((e = tree_launch(g, ge, MTt - k, ny, st)) != cudaSuccess) return e;
-      if (rag && (e = pair(g.MT - 2, 1, 1, 1)) != cudaSuccess) return e;
-      for (int s = 1; k + s < MTt; s *= 2)
-        if ((e = pair(k, s, tree_pairs(k, MTt, s), 0)) != cudaSuccess) return e;
+      if ((e = tree_launch(g, ge, nlead, ny, st)) != cudaSuccess) return e;
+      for (int d = 1; d < G; ++d)
+        if ((e = group(d)) != cudaSuccess) return e;
+      if (rag && (e = pair(last, g.MT - 1 - last, 1, 1, 1)) != cudaSuccess) return e;
+      for (int s = G; k + s < MTt; s *= 2)
+        if ((e = pair(k, s, 2 * s, tree_pairs(k, MTt, s), 0)) != cudaSuccess) return e;
     } else {
-      int smax = 1;
+      int smax = G;
       while (k + smax < MTt) smax *= 2;
-      for (int s = smax / 2; s >= 1; s /= 2)
-        if ((e = pair(k, s, tree_pairs(k, MTt, s), 0)) != cudaSuccess) return e;
-      if (rag && (e = pair(g.MT - 2, 1, 1, 1)) != cudaSuccess) return e;
-      if ((e = tree_launch(g, ge, MTt - k, ny, st)) != cudaSuccess) return e;
+      for (int s = smax / 2; s >= G; s /= 2)
+        if ((e = pair(k, s, 2 * s, tree_pairs(k, MTt, s), 0)) != cudaSuccess) return e;
+      if (rag && (e = pair(last, g.MT - 1 - last, 1, 1, 1)) != cudaSuccess) return e;
+      for (int d = G - 1; d >= 1; --d)
+        if ((e = group(d)) != cudaSuccess) return e;
+      if ((e = tree_launch(g, ge, nlead, ny, st)) != cudaSuccess) return e;
     }
   }
   return cudaSuccess;
@@ -308,12 +335,12 @@ static cudaError_t tree_apply_q(const TreeGeom<R> &g, int trans, cudaStream_t st
 
 template <typename R>
 static int tree_geom(int m, int n, int nrhs, int nb, int ib, R *A, int lda, R *B, int ldb, R *T, R *T2, int ldt,
-                     R *tau, R *tau2, int ldtau, TreeGeom<R> *g) {
+                     R *tau, R *tau2, int ldtau, TreeGeom<R> *g, int grp = 1) {
   if (m < 0) return -1;
   if (n < 0) return -2;
   if (nb <= 0 || nb > 256) return -3;
   if (ib <= 0 || ib > nb || ib > 32) return -4;
-  g->m = m; g->n = n; g->nb = nb; g->ib = ib; g->nrhs = nrhs;
+  g->m = m; g->n = n; g->nb = nb; g->ib = ib; g->nrhs = nrhs; g->grp = grp;
   g->MT = (m + nb - 1) / nb; g->NT = (n + nb - 1) / nb; g->KT = std::min(g->MT, g->NT);
   g->A = A; g->lda = lda; g->B = B; g->ldb = ldb;
   g->T = T; g->T2 = T2; g->ldt = ldt;
@@ -323,9 +350,10 @@ static int tree_geom(int m, int n, int nrhs, int nb, int ib, R *A, int lda, R *B
 
 template <typename R>
 static int tree_geqrf_impl(int m, int n, int nb, int ib, R *A, int lda, R *T, R *T2, int ldt, R *tau, R *tau2,
-                           int ldtau, int nrhs, R *B, int ldb, cudaStream_t st) {
+                           int ldtau, int nrhs, R *B, int ldb, cudaStream_t st, int grp = 1) {
+  if (grp <= 0) return -5;
   TreeGeom<R> g;
-  int rc = tree_geom<R>(m, n, nrhs, nb, ib, A, lda, B, ldb, T, T2, ldt, tau, tau2, ldtau, &g);
+  int rc = tree_geom<R>(m, n, nrhs, nb, ib, A, lda, B, ldb, T, T2, ldt, tau, tau2, ldtau, &g, grp);
   if (rc) return rc;
   if (m == 0 || n == 0) return 0;
   if (!A || lda < m) return -6;
@@ -341,11 +369,12 @@ static int tree_geqrf_impl(int m, int n, int nb, int ib, R *A, int lda, R *T, R 
 
 template <typename R>
 static int tree_unmqr_impl(char trans, int m, int n, int nrhs, int nb, int ib, const R *A, int lda, const R *T,
-                           const R *T2, int ldt, R *B, int ldb, cudaStream_t st) {
+                           const R *T2, int ldt, R *B, int ldb, cudaStream_t st, int grp = 1) {
   if (trans != 'N' && trans != 'C' && trans != 'T') return -1;
+  if (grp <= 0) return -7;
   TreeGeom<R> g;
   int rc = tree_geom<R>(m, n, nrhs, nb, ib, const_cast<R *>(A), lda, B, ldb, const_cast<R *>(T),
-                        const_cast<R *>(T2), ldt, nullptr, nullptr, 1, &g);
+                        const_cast<R *>(T2), ldt, nullptr, nullptr, 1, &g, grp);
   if (rc) return rc == -1 ? -2 : rc == -2 ? -3 : rc == -3 ? -5 : -6;
   if (nrhs < 0) return -4;
   if (m == 0 || n == 0 || nrhs == 0) return 0;
@@ -476,6 +505,7 @@ __global__ void __launch_bounds__(TQR_THREADS, 2) k_tree_dag(const TDagArgs<R> a
 // ---- host: task graph construction -----------------------------------------
 struct TreeShape {
   int m, n, nb, ib, nrhs, MT, NT, KT;
+  int grp = 1;
   int rows(int i) const { return std::min(nb, m - i * nb); }
   int cols(int k) const { return std::min(nb, n - k * nb); }
   int strips(int j) const { return j < NT ? (cols(j) + kTreeNW - 1) / kTreeNW : (nrhs + kTreeNW - 1) / kTreeNW; }
@@ -562,12 +592,14 @@ static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::
     const int ca = std::max(0, sh.n - (k + 1) * sh.nb);
     return (ca + kTreeNW - 1) / kTreeNW + (sh.nrhs + kTreeNW - 1) / kTreeNW;
   };
+  const int G = sh.grp;
   for (int k = 0; k < sh.KT; ++k) {
     const int nk = sh.cols(k), NSk = sh.strips(k);   // NSk: strips of the panel's tile column
     const bool rag = sh.ragged(k);
     const int MTt = rag ? sh.MT - 1 : sh.MT;
-    // geqrt of every tile, block by block, then unmqr of its row
-    for (int i = k; i < MTt; ++i) {
+    const int last = k + ((MTt - 1 - k) / G) * G;    // last group leader
+    // geqrt of every group leader, block by block, then unmqr of its row
+    for (int i = k; i < MTt; i += G) {
       const int kk = std::min(sh.rows(i), nk);
       for (int b = 0, c = 0; c < kk; ++b, c += sh.ib) {
         const int sb = std::min(sh.ib, kk - c);
@@ -636,8 +668,10 @@ static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::
         emit(OP_PR_TRAIL | flag, k, 0, i, p, y);
       }
     };
-    if (rag) merge(sh.MT - 2, sh.MT - 1, 1);
-    for (int s = 1; k + s < MTt; s *= 2)
+    for (int d = 1; d < G; ++d)
+      for (int i = k; i + d < MTt; i += G) merge(i, i + d, 1);
+    if (rag) merge(last, sh.MT - 1, 1);
+    for (int s = G; k + s < MTt; s *= 2)
       for (int i = k; i + s < MTt; i += 2 * s) merge(i, i + s, 0);
   }
   // longest path to the end, then a stable sort by it
@@ -665,7 +699,7 @@ static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::
 
 static long long tree_key(const TreeShape &sh) {
   long long h = 7809847782465536322LL;
-  for (int v : {sh.m, sh.n, sh.nb, sh.ib, sh.nrhs, 0x7ee})
+  for (int v : {sh.m, sh.n, sh.nb, sh.ib, sh.nrhs, sh.grp, 0x7ee})
     h = (h ^ (long long)v) * 1099511628211LL;
   return h & 0x7fffffffffffffffLL;
 }
@@ -673,8 +707,10 @@ static long long tree_key(const TreeShape &sh) {
 static std::mutex g_tplan_mu;
 static std::map<long long, std::shared_ptr<TreePlan>> g_tplans;
 
-static bool tree_dag_shape(int m, int n, int nb, int ib, int nrhs, TreeShape *sh) {
+static bool tree_dag_shape(int m, int n, int nb, int ib, int nrhs, TreeShape *sh, int grp = 1) {
   if (m <= 0 || n <= 0 || nb <= 0 || nb > 256 || nb % kTreeNW) return false;
+  if (grp <= 0) return false;
+  sh->grp = grp;
   if (ib <= 0 || ib > 32 || ib % kTreeNW || nb % ib) return false;
   if (nrhs < 0 || nrhs > 256) return false;
   sh->m = m; sh->n = n; sh->nb = nb; sh->ib = ib; sh->nrhs = nrhs;
@@ -722,9 +758,10 @@ static std::shared_ptr<TreePlan> tree_plan(const TreeShape &sh) {
 template <typename R>
 static int tree_geqrf_dag_impl(int m, int n, int nb, int ib, R *A, int lda, R *T, R *T2, int ldt, R *tau,
                                R *tau2, int ldtau, int nrhs, R *B, int ldb, void *work, size_t lwork,
-                               cudaStream_t st) {
+                               cudaStream_t st, int grp = 1) {
+  if (grp <= 0) return -5;
   TreeGeom<R> g;
-  int rc = tree_geom<R>(m, n, nrhs, nb, ib, A, lda, B, ldb, T, T2, ldt, tau, tau2, ldtau, &g);
+  int rc = tree_geom<R>(m, n, nrhs, nb, ib, A, lda, B, ldb, T, T2, ldt, tau, tau2, ldtau, &g, grp);
   if (rc) return rc;
   if (m == 0 || n == 0) return 0;
   if (!A || lda < m) return -6;
@@ -733,7 +770,7 @@ static int tree_geqrf_dag_impl(int m, int n, int nb, int ib, R *A, int lda, R *T
   if (nrhs < 0) return -13;
   if (nrhs > 0 && (!B || ldb < m)) return -15;
   TreeShape sh;
-  if (!tree_dag_shape(m, n, nb, ib, nrhs, &sh)) return -3;
+  if (!tree_dag_shape(m, n, nb, ib, nrhs, &sh, grp)) return -3;
   std::shared_ptr<TreePlan> p = tree_plan(sh);
   if (!work || ((uintptr_t)work & 255)) return -16;
   if (lwork < p->total_bytes) return -17;
@@ -785,6 +822,25 @@ int tqr_stile_geqrf_tree(int m, int n, int nb, int ib, float *A, int lda, float 
   return tree_geqrf_impl<float>(m, n, nb, ib, A, lda, T, T2, ldt, tau, tau2, ldtau, nrhs, B, ldb, stream);
 }
 
+#define TQR_HQR(P, R)                                                                                          \
+  int tqr_##P##tile_geqrf_hqr(int m, int n, int nb, int ib, int grp, R *A, int lda, R *T, R *T2, int ldt, R *tau, \
+                              R *tau2, int ldtau, int nrhs, R *B, int ldb, cudaStream_t stream) {                \
+    return tree_geqrf_impl<R>(m, n, nb, ib, A, lda, T, T2, ldt, tau, tau2, ldtau, nrhs, B, ldb, stream, grp);    \
+  }                                                                                                              \
+  int tqr_##P##tile_unmqr_hqr(char trans, int m, int n, int nrhs, int nb, int ib, int grp, const R *A, int lda,  \
+                              const R *T, const R *T2, int ldt, R *B, int ldb, cudaStream_t stream) {            \
+    return tree_unmqr_impl<R>(trans, m, n, nrhs, nb, ib, A, lda, T, T2, ldt, B, ldb, stream, grp);               \
+  }                                                                                                              \
+  int tqr_##P##tile_geqrf_hqr_dag(int m, int n, int nb, int ib, int grp, R *A, int lda, R *T, R *T2, int ldt,    \
+                                  R *tau, R *tau2, int ldtau, int nrhs, R *B, int ldb, void *work, size_t lwork, \
+                                  cudaStream_t stream) {                                                         \
+    return tree_geqrf_dag_impl<R>(m, n, nb, ib, A, lda, T, T2, ldt, tau, tau2, ldtau, nrhs, B, ldb, work, lwork, \
+                                  stream, grp);                                                                  \
+  }
+TQR_HQR(d, double)
+TQR_HQR(s, float)
+#undef TQR_HQR
+
 int tqr_dtile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, const double *A, int lda,
                          const double *T, const double *T2, int ldt, double *B, int ldb, cudaStream_t stream) {
   return tree_unmqr_impl<double>(trans, m, n, nrhs, nb, ib, A, lda, T, T2, ldt, B, ldb, stream);
@@ -812,6 +868,27 @@ int tqr_tile_tree_dag_check(int m, int n, int nb, int ib, int nrhs, long long *n
   if (!tree_dag_shape(m, n, nb, ib, nrhs, &sh)) return -1;
   std::shared_ptr<TreePlan> p = tree_plan(sh);
   // every dependency points to an earlier task of the sorted order
+  for (size_t q = 0; q < p->items.size(); ++q) {
+    const TItem &it = p->items[q];
+    for (int d = 0; d < (int)it.ndep; ++d)
+      if (p->deps[it.dep + d] >= q) return 1;
+  }
+  if (ntasks) *ntasks = (long long)p->items.size();
+  return 0;
+}
+
+int tqr_tile_hqr_dag_worksize(int m, int n, int nb, int ib, int grp, int nrhs, size_t *bytes) {
+  if (!bytes) return -7;
+  TreeShape sh;
+  if (!tree_dag_shape(m, n, nb, ib, nrhs, &sh, grp)) return -1;
+  *bytes = tree_plan(sh)->total_bytes;
+  return 0;
+}
+
+int tqr_tile_hqr_dag_check(int m, int n, int nb, int ib, int grp, int nrhs, long long *ntasks) {
+  TreeShape sh;
+  if (!tree_dag_shape(m, n, nb, ib, nrhs, &sh, grp)) return -1;
+  std::shared_ptr<TreePlan> p = tree_plan(sh);
   for (size_t q = 0; q < p->items.size(); ++q) {
     const TItem &it = p->items[q];
     for (int d = 0; d < (int)it.ndep; ++d)

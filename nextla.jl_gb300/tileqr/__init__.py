@@ -457,12 +457,12 @@ def tile_geqrf(A, nb=256, ib=32, T=None, tau=None, dag=True):
     return T, tau
 
 
-def tree_dag_workspace(m, n, nb, ib, nrhs, device):
+def tree_dag_workspace(m, n, nb, ib, nrhs, device, grp=1):
     """(buffer, aligned pointer, bytes) for the tree task-graph kernel, or None
     when the shape is outside it."""
     import ctypes
     size = ctypes.c_size_t(0)
-    if _lib.lib().tqr_tile_tree_dag_worksize(m, n, nb, ib, nrhs, ctypes.byref(size)) != 0:
+    if _lib.lib().tqr_tile_hqr_dag_worksize(m, n, nb, ib, grp, nrhs, ctypes.byref(size)) != 0:
         return None
     key = ("tree", str(device), size.value)
     w = _WORK.get(key)
@@ -472,22 +472,24 @@ def tree_dag_workspace(m, n, nb, ib, nrhs, device):
     return w, w.data_ptr() + ((-w.data_ptr()) % 256), size.value
 
 
-def tree_dag_check(m, n, nb, ib, nrhs=0):
+def tree_dag_check(m, n, nb, ib, nrhs=0, grp=1):
     """Host check of the tree task graph; returns the task count."""
     import ctypes
     nt = ctypes.c_longlong(0)
-    rc = _lib.lib().tqr_tile_tree_dag_check(m, n, nb, ib, nrhs, ctypes.byref(nt))
+    rc = _lib.lib().tqr_tile_hqr_dag_check(m, n, nb, ib, grp, nrhs, ctypes.byref(nt))
     if rc != 0:
         raise RuntimeError(f"tree task graph check failed ({rc})")
     return nt.value
 
 
-def tile_geqrf_tree(A, nb=256, ib=32, B=None, dag=True):
+def tile_geqrf_tree(A, nb=256, ib=32, B=None, dag=True, grp=1):
     """Tile QR of A in place with a binary reduction tree per panel (geqrt!
     on every tile, ttqrt!/ttmqr! merges).  Returns (T, tau, T2, tau2); with B,
     B is overwritten by Q^T B in the same pass.  dag=True runs it as one
     persistent launch when the shape allows (same results as the stream
-    driver)."""
+    driver).  grp > 1: the hierarchical form -- groups of grp tiles reduced
+    flat into their first tile (tsqrt!/tsmqr!), the group leaders by the
+    binary tree."""
     import ctypes
     m, n = A.shape
     ts, taus = tile_shapes(m, n, nb, ib)
@@ -502,17 +504,17 @@ def tile_geqrf_tree(A, nb=256, ib=32, B=None, dag=True):
     if B is not None:
         nrhs = B.shape[1]
         pb, ldb = _mat(B)
-    ws = tree_dag_workspace(m, n, nb, ib, nrhs, A.device) if dag else None
+    ws = tree_dag_workspace(m, n, nb, ib, nrhs, A.device, grp) if dag else None
     if ws is None:
-        _call(_prefix(A, T, tau, B), "tile_geqrf_tree", m, n, nb, ib, pa, lda, pt, _ptr(T2), ldt, pu,
+        _call(_prefix(A, T, tau, B), "tile_geqrf_hqr", m, n, nb, ib, grp, pa, lda, pt, _ptr(T2), ldt, pu,
               _ptr(tau2), ldu, nrhs, pb, ldb)
         return T, tau, T2, tau2
     _, wp, size = ws
     p = _prefix(A, T, tau, B)
     st = torch.cuda.current_stream()
-    rc = getattr(_lib.lib(), f"tqr_{p}tile_geqrf_tree_dag")(m, n, nb, ib, pa, lda, pt, _ptr(T2), ldt, pu,
-                                                           _ptr(tau2), ldu, nrhs, pb, ldb, ctypes.c_void_p(wp),
-                                                           size, st.cuda_stream)
+    rc = getattr(_lib.lib(), f"tqr_{p}tile_geqrf_hqr_dag")(m, n, nb, ib, grp, pa, lda, pt, _ptr(T2), ldt, pu,
+                                                          _ptr(tau2), ldu, nrhs, pb, ldb, ctypes.c_void_p(wp),
+                                                          size, st.cuda_stream)
     if rc < 0:
         raise ArgumentError(f"tile_geqrf_tree: illegal value of argument {-rc}")
     if rc > 0:
@@ -526,13 +528,13 @@ def tile_geqrf_tree(A, nb=256, ib=32, B=None, dag=True):
     return T, tau, T2, tau2
 
 
-def tile_unmqr_tree(trans, A, T, T2, B, nb=256, ib=32):
-    """B := Q^T B ('C') or Q B ('N') with Q from tile_geqrf_tree."""
+def tile_unmqr_tree(trans, A, T, T2, B, nb=256, ib=32, grp=1):
+    """B := Q^T B ('C') or Q B ('N') with Q from tile_geqrf_tree (same grp)."""
     m, n = A.shape
     pa, lda = _mat(A)
     pt, ldt = _mat(T)
     pb, ldb = _mat(B)
-    _call(_prefix(A, T, T2, B), "tile_unmqr_tree", _ch(trans), m, n, B.shape[1], nb, ib, pa, lda, pt,
+    _call(_prefix(A, T, T2, B), "tile_unmqr_hqr", _ch(trans), m, n, B.shape[1], nb, ib, grp, pa, lda, pt,
           _ptr(T2), ldt, pb, ldb)
 
 

@@ -32,6 +32,8 @@ SIGNATURES = {
     "tile_gels": [_I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
     "tile_geqrf_tree": [_I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P],
     "tile_unmqr_tree": [_C, _I, _I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _I, _P],
+    "tile_geqrf_hqr": [_I, _I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P],
+    "tile_unmqr_hqr": [_C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _I, _P],
 }
 
 # routines that also exist for ComplexF64 (prefix z) and ComplexF32 (prefix c)
@@ -82,6 +84,12 @@ DIAG = {
     "tqr_batched_graph_launch": ([_P, _P], _I),
     "tqr_batched_graph_destroy": ([_P], _I),
     "tqr_tile_tree_dag_worksize": ([_I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_size_t)], _I),
+    "tqr_tile_hqr_dag_worksize": ([_I, _I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_size_t)], _I),
+    "tqr_tile_hqr_dag_check": ([_I, _I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)], _I),
+    "tqr_dtile_geqrf_hqr_dag": ([_I, _I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P, ctypes.c_size_t,
+                                 _P], _I),
+    "tqr_stile_geqrf_hqr_dag": ([_I, _I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P, ctypes.c_size_t,
+                                 _P], _I),
     "tqr_tile_tree_dag_check": ([_I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)], _I),
     "tqr_tile_tree_dag_status": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I), _P], _I),
     "tqr_dtile_geqrf_tree_dag": ([_I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P, ctypes.c_size_t,

@@ -843,24 +843,34 @@ static int tree_ragged(int m, int nb, int MT, int k, int nk)
     return p > k && imin(nb, m - p * nb) < nk;
 }
 
-int ora_dtile_geqrf_tree(int m, int n, int nb, int ib, double *A, int lda, double *T, int ldt,
-                         double *tau, int ldtau, double *T2, double *tau2)
+/* Hierarchical variant (PLASMA's HQR): the panel's tiles form groups of    */
+/* grp consecutive tiles; each group is reduced flat into its first tile     */
+/* (geqrt on the group leader, tsqrt/tsmqr of each other tile into it), then */
+/* the leaders by the binary ttqrt/ttmqr tree at distances grp, 2 grp, ...   */
+/* A ragged last tile joins the last group (tsqrt into its leader).  grp = 1 */
+/* is the binary tree above; grp >= MT the flat tree (with the flat tiles'   */
+/* reflectors stored as merges: T2, tau2).                                   */
+int ora_dtile_geqrf_hqr(int m, int n, int nb, int ib, int grp, double *A, int lda, double *T, int ldt,
+                        double *tau, int ldtau, double *T2, double *tau2)
 {
     if (m < 0) return -1;
     if (n < 0) return -2;
     if (nb <= 0) return -3;
     if (ib <= 0 || ib > nb) return -4;
+    if (grp <= 0) return -5;
     if (m == 0 || n == 0) return 0;
     int MT = (m + nb - 1) / nb, NT = (n + nb - 1) / nb, KT = imin(MT, NT);
-    if (lda < m) return -6;
-    if (ldt < MT * ib) return -8;
-    if (ldtau < n) return -10;
+    if (lda < m) return -7;
+    if (ldt < MT * ib) return -9;
+    if (ldtau < n) return -11;
     for (int k = 0; k < KT; ++k) {
         int nk = imin(nb, n - k * nb);
         int rag = tree_ragged(m, nb, MT, k, nk);
-        int MTt = rag ? MT - 1 : MT;             /* tiles the tree reduces */
+        int MTt = rag ? MT - 1 : MT;             /* tiles the groups hold */
+        int last = k + ((MTt - 1 - k) / grp) * grp;   /* last group leader */
+        /* geqrt of every leader and unmqr of its row */
 #pragma omp parallel for schedule(dynamic)
-        for (int i = k; i < MTt; ++i) {
+        for (int i = k; i < MTt; i += grp) {
             int mi = imin(nb, m - i * nb), kk = imin(mi, nk);
             double *w = (double *)malloc(sizeof(double) * (size_t)nb * (size_t)nb);
             double *tv = (double *)malloc(sizeof(double) * (size_t)nb);
@@ -876,26 +886,32 @@ int ora_dtile_geqrf_tree(int m, int n, int nb, int ib, double *A, int lda, doubl
             free(w);
             free(tv);
         }
-        if (rag) {
-            int p = MT - 1, q = p - 1, mp = imin(nb, m - p * nb);
-            double *w = (double *)malloc(sizeof(double) * (size_t)nb * (size_t)nb);
-            double *tv = (double *)malloc(sizeof(double) * (size_t)nb);
-            double *Apk = A + IDX(p * nb, k * nb, lda);
-            double *T2p = T2 + IDX(p * ib, k * nb, ldt);
-            ora_dtsqrt(mp, nk, ib, nb, A + IDX(q * nb, k * nb, lda), lda, Apk, lda, T2p, ldt, tv, w);
-            for (int c = 0; c < nk; ++c) tau2[IDX(k * nb + c, p, ldtau)] = tv[c];
+        /* flat reduction inside each group: tile i + d into leader i; the
+           ragged tile after the others, into the last leader */
+        for (int d = 1; d <= grp; ++d) {
 #pragma omp parallel for schedule(dynamic)
-            for (int j = k + 1; j < NT; ++j) {
-                int nj = imin(nb, n - j * nb);
-                double *wj = (double *)malloc(sizeof(double) * (size_t)nb * (size_t)nb);
-                ora_dtsmqr('L', 'C', nb, nj, mp, nj, nk, ib, nk, A + IDX(q * nb, j * nb, lda), lda,
-                           A + IDX(p * nb, j * nb, lda), lda, Apk, lda, T2p, ldt, wj);
-                free(wj);
+            for (int i = k; i < MTt; i += grp) {
+                int p = (d < grp) ? i + d : (rag && i == last ? MT - 1 : -1);
+                if (p < 0 || (d < grp && p >= MTt)) continue;
+                int mp = imin(nb, m - p * nb), mi = imin(nb, m - i * nb);
+                double *w = (double *)malloc(sizeof(double) * (size_t)nb * (size_t)nb);
+                double *tv = (double *)malloc(sizeof(double) * (size_t)nb);
+                double *Apk = A + IDX(p * nb, k * nb, lda);
+                double *T2p = T2 + IDX(p * ib, k * nb, ldt);
+                ora_dtsqrt(mp, nk, ib, mi, A + IDX(i * nb, k * nb, lda), lda, Apk, lda, T2p, ldt, tv, w);
+                for (int c = 0; c < imin(mi, nk); ++c) tau2[IDX(k * nb + c, p, ldtau)] = tv[c];
+                for (int j = k + 1; j < NT; ++j) {
+                    int nj = imin(nb, n - j * nb);
+                    ora_dtsmqr('L', 'C', mi, nj, mp, nj, imin(mi, nk), ib, imin(mi, nk),
+                               A + IDX(i * nb, j * nb, lda), lda, A + IDX(p * nb, j * nb, lda), lda, Apk, lda,
+                               T2p, ldt, w);
+                }
+                free(w);
+                free(tv);
             }
-            free(w);
-            free(tv);
         }
-        for (int s = 1; k + s < MTt; s *= 2) {
+        /* binary tree over the leaders */
+        for (int s = grp; k + s < MTt; s *= 2) {
 #pragma omp parallel for schedule(dynamic)
             for (int i = k; i < MTt - s; i += 2 * s) {
                 int p = i + s;
@@ -919,9 +935,16 @@ int ora_dtile_geqrf_tree(int m, int n, int nb, int ib, double *A, int lda, doubl
     return 0;
 }
 
-/* B := Q^T B (trans 'C'/'T') or Q B ('N') for Q of ora_dtile_geqrf_tree.   */
-int ora_dtile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, const double *A,
-                         int lda, const double *T, int ldt, const double *T2, double *B, int ldb)
+int ora_dtile_geqrf_tree(int m, int n, int nb, int ib, double *A, int lda, double *T, int ldt,
+                         double *tau, int ldtau, double *T2, double *tau2)
+{
+    int rc = ora_dtile_geqrf_hqr(m, n, nb, ib, 1, A, lda, T, ldt, tau, ldtau, T2, tau2);
+    return rc < -4 ? rc + 1 : rc;
+}
+
+/* B := Q^T B (trans 'C'/'T') or Q B ('N') for Q of ora_dtile_geqrf_hqr.    */
+int ora_dtile_unmqr_hqr(char trans, int m, int n, int nrhs, int nb, int ib, int grp, const double *A,
+                        int lda, const double *T, int ldt, const double *T2, double *B, int ldb)
 {
     if (trans != 'N' && trans != 'C' && trans != 'T') return -1;
     if (m < 0) return -2;
@@ -929,6 +952,7 @@ int ora_dtile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, con
     if (nrhs < 0) return -4;
     if (nb <= 0) return -5;
     if (ib <= 0 || ib > nb) return -6;
+    if (grp <= 0) return -7;
     if (m == 0 || n == 0 || nrhs == 0) return 0;
     int MT = (m + nb - 1) / nb, NT = (n + nb - 1) / nb, KT = imin(MT, NT);
     double *work = (double *)malloc(sizeof(double) * (size_t)nrhs * (size_t)nb);
@@ -939,45 +963,58 @@ int ora_dtile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, con
         int nk = imin(nb, n - k * nb);
         int rag = tree_ragged(m, nb, MT, k, nk);
         int MTt = rag ? MT - 1 : MT;
-        int smax = 1;
+        int last = k + ((MTt - 1 - k) / grp) * grp;
+        int smax = grp;
         while (k + smax < MTt) smax *= 2;
-        int p = MT - 1, q = p - 1, mp = imin(nb, m - p * nb);
+        /* merge (leader i, tile p) of the flat group step, or of the tree */
+#define GRP_MERGE(i, p, op)                                                                        \
+        do {                                                                                       \
+            int mi_ = imin(nb, m - (i) * nb), mp_ = imin(nb, m - (p) * nb);                        \
+            ora_dtsmqr('L', op, mi_, nrhs, mp_, nrhs, imin(mi_, nk), ib, imin(mi_, nk),            \
+                       B + IDX((i) * nb, 0, ldb), ldb, B + IDX((p) * nb, 0, ldb), ldb,             \
+                       A + IDX((p) * nb, k * nb, lda), lda, T2 + IDX((p) * ib, k * nb, ldt), ldt,   \
+                       work);                                                                      \
+        } while (0)
+#define TREE_MERGE(i, p, op)                                                                       \
+        do {                                                                                       \
+            int mp_ = imin(nb, m - (p) * nb);                                                      \
+            ora_dttmqr('L', op, nb, nrhs, mp_, nrhs, imin(mp_, nk), ib, B + IDX((i) * nb, 0, ldb),  \
+                       ldb, B + IDX((p) * nb, 0, ldb), ldb, A + IDX((p) * nb, k * nb, lda), lda,    \
+                       T2 + IDX((p) * ib, k * nb, ldt), ldt, work);                                \
+        } while (0)
         if (tr) {
-            for (int i = k; i < MTt; ++i) {
+            for (int i = k; i < MTt; i += grp) {
                 int mi = imin(nb, m - i * nb);
                 ora_dunmqr('L', 'C', mi, nrhs, imin(mi, nk), ib, A + IDX(i * nb, k * nb, lda), lda, mi,
                            nk, T + IDX(i * ib, k * nb, ldt), ldt, B + IDX(i * nb, 0, ldb), ldb, work, nrhs);
             }
-            if (rag)
-                ora_dtsmqr('L', 'C', nb, nrhs, mp, nrhs, nk, ib, nk, B + IDX(q * nb, 0, ldb), ldb,
-                           B + IDX(p * nb, 0, ldb), ldb, A + IDX(p * nb, k * nb, lda), lda,
-                           T2 + IDX(p * ib, k * nb, ldt), ldt, work);
-            for (int s = 1; k + s < MTt; s *= 2)
-                for (int i = k; i < MTt - s; i += 2 * s) {
-                    int pp = i + s, mpp = imin(nb, m - pp * nb);
-                    ora_dttmqr('L', 'C', nb, nrhs, mpp, nrhs, imin(mpp, nk), ib, B + IDX(i * nb, 0, ldb),
-                               ldb, B + IDX(pp * nb, 0, ldb), ldb, A + IDX(pp * nb, k * nb, lda), lda,
-                               T2 + IDX(pp * ib, k * nb, ldt), ldt, work);
-                }
+            for (int d = 1; d < grp; ++d)
+                for (int i = k; i + d < MTt; i += grp) GRP_MERGE(i, i + d, 'C');
+            if (rag) GRP_MERGE(last, MT - 1, 'C');
+            for (int s = grp; k + s < MTt; s *= 2)
+                for (int i = k; i < MTt - s; i += 2 * s) TREE_MERGE(i, i + s, 'C');
         } else {
-            for (int s = smax / 2; s >= 1; s /= 2)
-                for (int i = k; i < MTt - s; i += 2 * s) {
-                    int pp = i + s, mpp = imin(nb, m - pp * nb);
-                    ora_dttmqr('L', 'N', nb, nrhs, mpp, nrhs, imin(mpp, nk), ib, B + IDX(i * nb, 0, ldb),
-                               ldb, B + IDX(pp * nb, 0, ldb), ldb, A + IDX(pp * nb, k * nb, lda), lda,
-                               T2 + IDX(pp * ib, k * nb, ldt), ldt, work);
-                }
-            if (rag)
-                ora_dtsmqr('L', 'N', nb, nrhs, mp, nrhs, nk, ib, nk, B + IDX(q * nb, 0, ldb), ldb,
-                           B + IDX(p * nb, 0, ldb), ldb, A + IDX(p * nb, k * nb, lda), lda,
-                           T2 + IDX(p * ib, k * nb, ldt), ldt, work);
-            for (int i = k; i < MTt; ++i) {
+            for (int s = smax / 2; s >= grp; s /= 2)
+                for (int i = k; i < MTt - s; i += 2 * s) TREE_MERGE(i, i + s, 'N');
+            if (rag) GRP_MERGE(last, MT - 1, 'N');
+            for (int d = grp - 1; d >= 1; --d)
+                for (int i = k; i + d < MTt; i += grp) GRP_MERGE(i, i + d, 'N');
+            for (int i = k; i < MTt; i += grp) {
                 int mi = imin(nb, m - i * nb);
                 ora_dunmqr('L', 'N', mi, nrhs, imin(mi, nk), ib, A + IDX(i * nb, k * nb, lda), lda, mi,
                            nk, T + IDX(i * ib, k * nb, ldt), ldt, B + IDX(i * nb, 0, ldb), ldb, work, nrhs);
             }
         }
+#undef GRP_MERGE
+#undef TREE_MERGE
     }
     free(work);
     return 0;
+}
+
+int ora_dtile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, const double *A,
+                         int lda, const double *T, int ldt, const double *T2, double *B, int ldb)
+{
+    int rc = ora_dtile_unmqr_hqr(trans, m, n, nrhs, nb, ib, 1, A, lda, T, ldt, T2, B, ldb);
+    return rc < -6 ? rc + 1 : rc;
 }

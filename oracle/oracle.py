@@ -69,6 +69,8 @@ def _declare(L):
         "ora_dttmqr": [_C, _C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
         "ora_dtile_geqrf_tree": [_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _P],
         "ora_dtile_unmqr_tree": [_C, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _P, _I],
+        "ora_dtile_geqrf_hqr": [_I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _P],
+        "ora_dtile_unmqr_hqr": [_C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _P, _I],
     }
     for name in ("geqr2", "larft", "larfb", "geqrt", "unmqr", "parfb", "parfb_l", "tsmqr", "tsqrt", "ttqrt",
                  "ttmqr", "tile_geqrf", "tile_unmqr", "trsm_lun"):
@@ -260,6 +262,30 @@ def tile_geqrf_tree(A, nb, ib):
     _check(lib().ora_dtile_geqrf_tree(m, n, nb, ib, pa, lda, T.ctypes.data, MT * ib, tau.ctypes.data, n,
                                       T2.ctypes.data, tau2.ctypes.data), "tile_geqrf_tree")
     return T, tau, T2, tau2
+
+
+def tile_geqrf_hqr(A, nb, ib, grp):
+    """Hierarchical tile QR in place: groups of grp tiles reduced flat into
+    their first tile, the group leaders by the binary tree.  Returns
+    (T, tau, T2, tau2) as tile_geqrf_tree does."""
+    m, n = A.shape
+    MT = (m + nb - 1) // nb
+    T = np.zeros((MT * ib, n), order="F")
+    T2 = np.zeros((MT * ib, n), order="F")
+    tau = np.zeros((n, MT), order="F")
+    tau2 = np.zeros((n, MT), order="F")
+    pa, lda = _mat(A)
+    _check(lib().ora_dtile_geqrf_hqr(m, n, nb, ib, grp, pa, lda, T.ctypes.data, MT * ib, tau.ctypes.data, n,
+                                     T2.ctypes.data, tau2.ctypes.data), "tile_geqrf_hqr")
+    return T, tau, T2, tau2
+
+
+def tile_unmqr_hqr(trans, A, T, T2, B, nb, ib, grp):
+    m, n = A.shape
+    pa, lda = _mat(A)
+    pb, ldb = _mat(B)
+    return _check(lib().ora_dtile_unmqr_hqr(_ch(trans), m, n, B.shape[1], nb, ib, grp, pa, lda, T.ctypes.data,
+                                            T.shape[0], T2.ctypes.data, pb, ldb), "tile_unmqr_hqr")
 
 
 def tile_unmqr_tree(trans, A, T, T2, B, nb, ib):

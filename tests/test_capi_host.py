@@ -179,3 +179,19 @@ def test_complex_argument_errors(L):
     assert L.tqr_ztsmqr(b"L", b"Q", 8, 8, 8, 8, 4, 2, z, 8, z, 8, z, 8, z, 2, None, 0, None) == -2
     assert L.tqr_zunmqr(b"L", b"C", 8, 8, 4, 2, z, 8, z, 2, ctypes.c_void_p(24), 8, None, 0, None) == -11
     assert L.tqr_ztile_geqrf(8, 8, 4, 8, z, 8, z, 8, z, 8, None) == -4                  # ib > nb
+
+
+@pytest.mark.parametrize("m,n,nb,ib,grp,nrhs", [(2048, 512, 128, 32, 4, 3), (4096, 1024, 256, 32, 8, 5),
+                                                (517, 130, 64, 16, 3, 2), (32768, 4096, 256, 32, 16, 4),
+                                                (65536, 512, 256, 32, 8, 0)])
+def test_hqr_task_graph_is_topological(L, m, n, nb, ib, grp, nrhs):
+    """The hierarchical schedule: every dependency precedes its task; more
+    groups than tiles degenerates to the flat tree, grp = 1 to the binary tree."""
+    import ctypes
+    nt = ctypes.c_longlong(0)
+    assert L.tqr_tile_hqr_dag_check(m, n, nb, ib, grp, nrhs, ctypes.byref(nt)) == 0
+    assert nt.value > 0
+    one, tree = ctypes.c_longlong(0), ctypes.c_longlong(0)
+    assert L.tqr_tile_hqr_dag_check(m, n, nb, ib, 1, nrhs, ctypes.byref(one)) == 0
+    assert L.tqr_tile_tree_dag_check(m, n, nb, ib, nrhs, ctypes.byref(tree)) == 0
+    assert one.value == tree.value

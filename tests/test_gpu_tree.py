@@ -118,3 +118,78 @@ def test_tree_tall_skinny_properties(tq):
     tq.tile_geqrf(F, nb, ib)
     Rf = torch.triu(F[:n])
     assert (torch.linalg.norm(R.abs() - Rf.abs()) / torch.linalg.norm(Rf)).item() < 1e-12 * n
+
+
+HQR_SHAPES = [(1024, 256, 128, 32, 2), (1000, 300, 128, 16, 3), (2048, 256, 128, 32, 4), (1800, 512, 256, 32, 2),
+              (517, 130, 64, 16, 3), (300, 400, 256, 32, 2), (2048, 512, 128, 32, 8), (1024, 256, 128, 32, 100)]
+
+
+@pytest.mark.parametrize("m,n,nb,ib,grp", HQR_SHAPES)
+def test_hqr_matches_oracle(tq, oracle, m, n, nb, ib, grp):
+    """Hierarchical form (groups of grp tiles reduced flat, leaders by the
+    binary tree) against the oracle's driver, which follows the same order."""
+    rng = np.random.default_rng(m + 5 * n + grp)
+    A0 = np.asfortranarray(rng.standard_normal((m, n)))
+    B0 = np.asfortranarray(rng.standard_normal((m, 3)))
+    A, B = tq.to_device(A0), tq.to_device(B0)
+    T, tau, T2, tau2 = tq.tile_geqrf_tree(A, nb, ib, B=B, grp=grp)
+    Ao = A0.copy(order="F")
+    To, tauo, T2o, tau2o = oracle.tile_geqrf_hqr(Ao, nb, ib, grp)
+    Bo = B0.copy(order="F")
+    oracle.tile_unmqr_hqr("C", Ao, To, T2o, Bo, nb, ib, grp)
+    tol = 1e-12 * max(n, 16)
+    assert rel(tq.to_numpy(A), Ao) < tol
+    assert rel(tq.to_numpy(T), To) < tol and rel(tq.to_numpy(T2), T2o) < tol
+    assert rel(tq.to_numpy(tau), tauo) < tol and rel(tq.to_numpy(tau2), tau2o) < tol
+    assert rel(tq.to_numpy(B), Bo) < tol
+    for trans in "NC":
+        C0 = np.asfortranarray(rng.standard_normal((m, 11)))
+        C = tq.to_device(C0)
+        tq.tile_unmqr_tree(trans, A, T, T2, C, nb, ib, grp=grp)
+        Co = C0.copy(order="F")
+        oracle.tile_unmqr_hqr(trans, Ao, To, T2o, Co, nb, ib, grp)
+        assert rel(tq.to_numpy(C), Co) < tol
+
+
+@pytest.mark.parametrize("m,n,nb,ib,grp,nrhs", [(2048, 512, 128, 32, 4, 3), (1800, 512, 256, 32, 2, 0),
+                                                (4096, 1024, 256, 32, 8, 5), (517, 130, 64, 16, 3, 2)])
+def test_hqr_task_graph_equals_stream_driver(tq, m, n, nb, ib, grp, nrhs):
+    import torch
+    tq.tree_dag_check(m, n, nb, ib, nrhs, grp=grp)
+    g = torch.Generator(device="cuda").manual_seed(m + n + grp)
+    A0 = torch.randn(m, n, generator=g, dtype=torch.float64, device="cuda")
+    B0 = torch.randn(m, max(nrhs, 1), generator=g, dtype=torch.float64, device="cuda")[:, :nrhs]
+    outs = []
+    for dag in (False, True):
+        A = tq.empty(m, n)
+        A.copy_(A0)
+        B = None
+        if nrhs:
+            B = tq.empty(m, nrhs)
+            B.copy_(B0)
+        res = tq.tile_geqrf_tree(A, nb, ib, B=B, dag=dag, grp=grp)
+        outs.append((A,) + tuple(res) + ((B,) if nrhs else ()))
+    for a, b in zip(*outs):
+        assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("grp", [4, 16])
+def test_hqr_float_properties(tq, grp):
+    """FP32 hierarchical QR at the mixed solve's tall shape class:
+    ||A x|| = ||R x|| and Q^T A = R through the stored factors."""
+    import torch
+    m, n, nb, ib = 8192, 1024, 256, 32
+    g = torch.Generator(device="cuda").manual_seed(grp)
+    A0 = tq.empty(m, n, dtype=torch.float32)
+    A0.copy_(torch.randn(m, n, generator=g, dtype=torch.float64, device="cuda"))
+    A = tq.empty(m, n, dtype=torch.float32)
+    A.copy_(A0)
+    T, tau, T2, tau2 = tq.tile_geqrf_tree(A, nb, ib, grp=grp)
+    R = torch.triu(A[:n]).double()
+    x = torch.randn(n, 2, generator=g, dtype=torch.float64, device="cuda")
+    ax = torch.linalg.norm(A0.double() @ x, dim=0)
+    assert ((ax - torch.linalg.norm(R @ x, dim=0)).abs() / ax).max().item() < 1e-5
+    QtA = tq.empty(m, n, dtype=torch.float32)
+    QtA.copy_(A0)
+    tq.tile_unmqr_tree("C", A, T, T2, QtA, nb, ib, grp=grp)
+    assert (torch.linalg.norm(QtA[:n].double() - R) / torch.linalg.norm(R)).item() < 1e-5

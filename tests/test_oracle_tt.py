@@ -143,3 +143,41 @@ def test_tree_tile_qr_properties(oracle, m, n, nb, ib):
     # R is unique up to the signs of its rows
     Rl = np.linalg.qr(A0, mode="r")
     assert np.linalg.norm(np.abs(R) - np.abs(Rl)) <= 1e-12 * np.linalg.norm(Rl) * k
+
+
+# ---- hierarchical tree (groups reduced flat, leaders by the binary tree) ----
+@pytest.mark.parametrize("m,n,nb,ib,grp", [(1024, 256, 128, 32, 2), (1000, 300, 128, 16, 3), (2048, 256, 128, 32, 4),
+                                           (1800, 512, 256, 32, 2), (517, 130, 64, 16, 3), (300, 400, 256, 32, 2),
+                                           (1024, 256, 128, 32, 8), (1024, 256, 128, 32, 100)])
+def test_hqr_properties(oracle, m, n, nb, ib, grp):
+    """Q^T A = [R; 0], Q Q^T = I through the stored factors, |R| equal to the
+    flat tree's, and grp = 1 identical to the binary tree."""
+    rng = np.random.default_rng(m + n + grp)
+    A0 = np.asfortranarray(rng.standard_normal((m, n)))
+    A = A0.copy(order="F")
+    T, tau, T2, tau2 = oracle.tile_geqrf_hqr(A, nb, ib, grp)
+    k = min(m, n)
+    R = np.triu(A[:k])
+    B = A0.copy(order="F")
+    oracle.tile_unmqr_hqr("C", A, T, T2, B, nb, ib, grp)
+    assert np.linalg.norm(B[:k] - R) <= 1e-13 * np.linalg.norm(R) * k
+    assert np.linalg.norm(B[k:]) <= 1e-13 * np.linalg.norm(A0) * k
+    C0 = np.asfortranarray(rng.standard_normal((m, 5)))
+    C = C0.copy(order="F")
+    oracle.tile_unmqr_hqr("N", A, T, T2, C, nb, ib, grp)
+    oracle.tile_unmqr_hqr("C", A, T, T2, C, nb, ib, grp)
+    assert np.abs(C - C0).max() < 1e-13 * m
+    F = A0.copy(order="F")
+    oracle.tile_geqrf(F, nb, ib)
+    assert np.allclose(np.abs(R), np.abs(np.triu(F[:k])), atol=1e-11 * np.abs(R).max())
+
+
+def test_hqr_group_one_is_the_binary_tree(oracle):
+    rng = np.random.default_rng(9)
+    A0 = np.asfortranarray(rng.standard_normal((1000, 300)))
+    A1, A2 = A0.copy(order="F"), A0.copy(order="F")
+    r1 = oracle.tile_geqrf_tree(A1, 128, 16)
+    r2 = oracle.tile_geqrf_hqr(A2, 128, 16, 1)
+    assert np.array_equal(A1, A2)
+    for a, b in zip(r1, r2):
+        assert np.array_equal(a, b)
