@@ -108,13 +108,15 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
   if (a.stage_c) {
     Cp = Cs; crs = 1; ccs = ldcs;
     if (a.c_rs == 1) {
-      stage_batched<R>(L * nwl,
-                       [&](int idx) { return conj_if(ldg_cg(Cg + (size_t)(idx % L) + (size_t)(idx / L) * a.c_cs), cjc); },
-                       [&](int idx, R v) { Cs[(idx % L) + (size_t)(idx / L) * ldcs] = v; });
+      for (int idx = tid; idx < L * nwl; idx += TQR_THREADS) {
+        int r = idx % L, c = idx / L;
+        Cs[r + (size_t)c * ldcs] = conj_if(ldg_cg(Cg + (size_t)r + (size_t)c * a.c_cs), cjc);
+      }
     } else {
-      stage_batched<R>(L * nwl,
-                       [&](int idx) { return conj_if(ldg_cg(Cg + (size_t)(idx / nwl) * a.c_rs + (idx % nwl)), cjc); },
-                       [&](int idx, R v) { Cs[(idx / nwl) + (size_t)(idx % nwl) * ldcs] = v; });
+      for (int idx = tid; idx < L * nwl; idx += TQR_THREADS) {
+        int c = idx % nwl, r = idx / nwl;
+        Cs[r + (size_t)c * ldcs] = conj_if(ldg_cg(Cg + (size_t)r * a.c_rs + c), cjc);
+      }
     }
   } else {
     Cp = Cg; crs = a.c_rs; ccs = a.c_cs;
@@ -134,14 +136,15 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
     const R *Vp;
     int ldvp;
     if (a.stage_v) {
-      stage_batched<R>(
-          Lr * kb,
-          [&](int idx) {
-            const int rr = idx % Lr, p = idx / Lr;
-            if (a.mode == 0) return (rr < p) ? R(0) : (rr == p ? R(1) : ldg_cg(a.V + ix(r0 + rr, i + p, a.ldv)));
-            return (rr < vrows(p)) ? ldg_cg(a.V + ix(rr, i + p, a.ldv)) : R(0);
-          },
-          [&](int idx, R v) { Vs[(idx % Lr) + (size_t)(idx / Lr) * ldvs] = v; });
+      for (int idx = tid; idx < Lr * kb; idx += TQR_THREADS) {
+        int rr = idx % Lr, p = idx / Lr;
+        R v;
+        if (a.mode == 0)
+          v = (rr < p) ? R(0) : (rr == p ? R(1) : ldg_cg(a.V + ix(r0 + rr, i + p, a.ldv)));
+        else
+          v = (rr < vrows(p)) ? ldg_cg(a.V + ix(rr, i + p, a.ldv)) : R(0);
+        Vs[rr + (size_t)p * ldvs] = v;
+      }
       Vp = Vs; ldvp = ldvs;
     } else {
       Vp = a.V + ix(r0, i, a.ldv); ldvp = a.ldv;
@@ -149,12 +152,10 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
     const R *Tp;
     int ldtp;
     if (a.stage_t) {
-      stage_batched<R>(kb * kb,
-                       [&](int idx) {
-                         const int p = idx % kb, q = idx / kb;
-                         return (p <= q) ? ldg_cg(a.T + ix(p, i + q, a.ldt)) : R(0);
-                       },
-                       [&](int idx, R v) { Ts[(idx % kb) + (idx / kb) * ib] = v; });
+      for (int idx = tid; idx < kb * kb; idx += TQR_THREADS) {
+        int p = idx % kb, q = idx / kb;
+        Ts[p + q * ib] = (p <= q) ? ldg_cg(a.T + ix(p, i + q, a.ldt)) : R(0);
+      }
       Tp = Ts; ldtp = ib;
     } else {
       Tp = a.T + ix(0, i, a.ldt); ldtp = a.ldt;
@@ -178,20 +179,22 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
           for (int c = 0; c < 4; ++c) acc[u][c] = 0.f;
         const float *cb = Cp + (size_t)r0 + (size_t)(4 * cg) * ccs;
         for (int q = rs; 4 * q < Lr; q += 8) {
+          float v[4][4], cv[4][4];
 #pragma unroll
           for (int t = 0; t < 4; ++t) {
             const int r = 4 * q + t;
             const bool ok = r < Lr;
-            float v[4], cv[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) v[u] = (ok && pb + u < kb) ? Vp[r + (size_t)(pb + u) * ldvp] : 0.f;
+            for (int u = 0; u < 4; ++u) v[t][u] = (ok && pb + u < kb) ? Vp[r + (size_t)(pb + u) * ldvp] : 0.f;
 #pragma unroll
-            for (int c = 0; c < 4; ++c) cv[c] = ok ? cb[r + (size_t)c * ccs] : 0.f;
+            for (int c = 0; c < 4; ++c) cv[t][c] = ok ? cb[r + (size_t)c * ccs] : 0.f;
+          }
+#pragma unroll
+          for (int t = 0; t < 4; ++t)
 #pragma unroll
             for (int u = 0; u < 4; ++u)
 #pragma unroll
-              for (int c = 0; c < 4; ++c) acc[u][c] = fmaf(v[u], cv[c], acc[u][c]);
-          }
+              for (int c = 0; c < 4; ++c) acc[u][c] = fmaf(v[t][u], cv[t][c], acc[u][c]);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u)

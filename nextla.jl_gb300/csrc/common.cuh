@@ -8,8 +8,6 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <type_traits>
-
 #define TQR_THREADS 256
 #define TQR_WARPS (TQR_THREADS / 32)
 
@@ -133,35 +131,6 @@ __device__ __forceinline__ cx<double> ldg_cg(const cx<double> *p) {
 __device__ __forceinline__ cx<float> ldg_cg(const cx<float> *p) {
   const float2 v = __ldcg(reinterpret_cast<const float2 *>(p));
   return cx<float>(v.x, v.y);
-}
-
-// Gathers n elements into shared memory: get(idx) loads one (from global,
-// through L2), put(idx, v) stores it.  Each thread issues kStageBatch
-// independent loads before its first store: with one load and one store per
-// iteration a warp would wait out the full L2 latency once per element, since
-// the compiler cannot move a global load above a store it might alias.
-// Batched for FP32 only: there a block's staging is a large part of its time;
-// an FP64 block's arithmetic takes ~30x longer than its loads, the other CTA
-// on the SM hides them, and the extra live registers would make the FP64
-// kernels spill.
-template <typename E>
-constexpr int kStageBatch = std::is_same<E, float>::value ? 4 : 1;
-template <typename E, typename Get, typename Put>
-__device__ __forceinline__ void stage_batched(int n, Get get, Put put) {
-  constexpr int K = kStageBatch<E>;
-  for (int base = threadIdx.x; base < n; base += K * TQR_THREADS) {
-    E v[K];
-#pragma unroll
-    for (int u = 0; u < K; ++u) {
-      const int idx = base + u * TQR_THREADS;
-      if (idx < n) v[u] = get(idx);
-    }
-#pragma unroll
-    for (int u = 0; u < K; ++u) {
-      const int idx = base + u * TQR_THREADS;
-      if (idx < n) put(idx, v[u]);
-    }
-  }
 }
 
 // Householder scalars in NextLA's convention (src/geqr2.jl:37-68,

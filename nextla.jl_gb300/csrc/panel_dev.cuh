@@ -213,8 +213,10 @@ __device__ void panel_qr_cta(int m, int nc, R *A, int lda, R *tau, R *T, int ldt
   if (staged) {
     c.ldp = odd_ld(m);
     c.P = carve<R>(sp, (size_t)c.ldp * nc);
-    stage_batched<R>(m * nc, [&](int idx) { return ldg_cg(A + ix(idx % m, idx / m, lda)); },
-                     [&](int idx, R v) { c.P[ix(idx % m, idx / m, c.ldp)] = v; });
+    for (int idx = tid; idx < m * nc; idx += TQR_THREADS) {
+      int r = idx % m, cc = idx / m;
+      c.P[ix(r, cc, c.ldp)] = ldg_cg(A + ix(r, cc, lda));
+    }
   } else {
     c.P = A;
     c.ldp = lda;
@@ -283,12 +285,10 @@ __device__ void tsqrt_block_cta(int m, int sb, R *A1, int lda1, R *A2, int lda2,
   if (staged) {
     c.ldp = odd_ld(mrow);
     c.P = carve<R>(sp, (size_t)c.ldp * sb);
-    stage_batched<R>(mrow * sb,
-                     [&](int idx) {
-                       const int r = idx % mrow, cc = idx / mrow;
-                       return in_tri(r, cc) ? ldg_cg(A2 + ix(r, cc, lda2)) : R(0);
-                     },
-                     [&](int idx, R v) { c.P[ix(idx % mrow, idx / mrow, c.ldp)] = v; });
+    for (int idx = tid; idx < mrow * sb; idx += TQR_THREADS) {
+      int r = idx % mrow, cc = idx / mrow;
+      c.P[ix(r, cc, c.ldp)] = in_tri(r, cc) ? ldg_cg(A2 + ix(r, cc, lda2)) : R(0);
+    }
   } else {
     c.P = A2;
     c.ldp = lda2;
