@@ -80,8 +80,12 @@ template <typename E> constexpr bool is_cx = elem_traits<E>::complex;
 template <typename R> __host__ __device__ __forceinline__ cx<R> operator+(cx<R> a, cx<R> b) { return cx<R>(a.x + b.x, a.y + b.y); }
 template <typename R> __host__ __device__ __forceinline__ cx<R> operator-(cx<R> a, cx<R> b) { return cx<R>(a.x - b.x, a.y - b.y); }
 template <typename R> __host__ __device__ __forceinline__ cx<R> operator-(cx<R> a) { return cx<R>(-a.x, -a.y); }
+// The product with its fused multiply-adds spelled out: left as
+// a.x * b.x - a.y * b.y the compiler may fuse either product, and may choose
+// differently in different kernels, which would make two drivers that run
+// the same arithmetic round differently.
 template <typename R> __host__ __device__ __forceinline__ cx<R> operator*(cx<R> a, cx<R> b) {
-  return cx<R>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  return cx<R>(fma(a.x, b.x, -(a.y * b.y)), fma(a.x, b.y, a.y * b.x));
 }
 template <typename R> __host__ __device__ __forceinline__ cx<R> &operator+=(cx<R> &a, cx<R> b) { a = a + b; return a; }
 template <typename R> __host__ __device__ __forceinline__ cx<R> &operator-=(cx<R> &a, cx<R> b) { a = a - b; return a; }
@@ -167,11 +171,11 @@ template <typename R>
 __device__ inline bool householder(cx<R> alpha, R xnorm_sq, cx<R> &beta, cx<R> &tau, cx<R> &scale) {
   const R ar = alpha.x, ai = alpha.y;
   if (xnorm_sq == R(0) && ai == R(0)) return false;
-  const R b = -dev_copysign(dev_sqrt(ar * ar + ai * ai + xnorm_sq), ar);
+  const R b = -dev_copysign(dev_sqrt(fma(ar, ar, ai * ai) + xnorm_sq), ar);   // fusions spelled out
   beta = cx<R>(b);
   tau = cx<R>((b - ar) / b, -ai / b);
   const R dr = ar - b, di = ai;
-  const R a2 = dr * dr + di * di;
+  const R a2 = fma(dr, dr, di * di);
   scale = cx<R>(dr / a2, -di / a2);
   return true;
 }
