@@ -108,9 +108,10 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
   if (a.stage_c) {
     Cp = Cs; crs = 1; ccs = ldcs;
     if (a.c_rs == 1) {
-      for_block(L, nwl, [&](int r, int c) {
+      for (int idx = tid; idx < L * nwl; idx += TQR_THREADS) {
+        int r = idx % L, c = idx / L;
         Cs[r + (size_t)c * ldcs] = conj_if(ldg_cg(Cg + (size_t)r + (size_t)c * a.c_cs), cjc);
-      });
+      }
     } else {
       for (int idx = tid; idx < L * nwl; idx += TQR_THREADS) {
         int c = idx % nwl, r = idx / nwl;
@@ -135,14 +136,15 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
     const R *Vp;
     int ldvp;
     if (a.stage_v) {
-      for_block(Lr, kb, [&](int rr, int p) {
+      for (int idx = tid; idx < Lr * kb; idx += TQR_THREADS) {
+        int rr = idx % Lr, p = idx / Lr;
         R v;
         if (a.mode == 0)
           v = (rr < p) ? R(0) : (rr == p ? R(1) : ldg_cg(a.V + ix(r0 + rr, i + p, a.ldv)));
         else
           v = (rr < vrows(p)) ? ldg_cg(a.V + ix(rr, i + p, a.ldv)) : R(0);
         Vs[rr + (size_t)p * ldvs] = v;
-      });
+      }
       Vp = Vs; ldvp = ldvs;
     } else {
       Vp = a.V + ix(r0, i, a.ldv); ldvp = a.ldv;
@@ -150,7 +152,10 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
     const R *Tp;
     int ldtp;
     if (a.stage_t) {
-      for_block(kb, kb, [&](int p, int q) { Ts[p + q * ib] = (p <= q) ? ldg_cg(a.T + ix(p, i + q, a.ldt)) : R(0); });
+      for (int idx = tid; idx < kb * kb; idx += TQR_THREADS) {
+        int p = idx % kb, q = idx / kb;
+        Ts[p + q * ib] = (p <= q) ? ldg_cg(a.T + ix(p, i + q, a.ldt)) : R(0);
+      }
       Tp = Ts; ldtp = ib;
     } else {
       Tp = a.T + ix(0, i, a.ldt); ldtp = a.ldt;
@@ -359,7 +364,10 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
   }
   if (a.stage_c) {
     if (a.c_rs == 1) {
-      for_block(L, nwl, [&](int r, int c) { Cg[(size_t)r + (size_t)c * a.c_cs] = conj_if(Cs[r + (size_t)c * ldcs], cjc); });
+      for (int idx = tid; idx < L * nwl; idx += TQR_THREADS) {
+        int r = idx % L, c = idx / L;
+        Cg[(size_t)r + (size_t)c * a.c_cs] = conj_if(Cs[r + (size_t)c * ldcs], cjc);
+      }
     } else {
       for (int idx = tid; idx < L * nwl; idx += TQR_THREADS) {
         int c = idx % nwl, r = idx / nwl;

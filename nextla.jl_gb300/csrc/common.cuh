@@ -137,20 +137,6 @@ __device__ __forceinline__ cx<float> ldg_cg(const cx<float> *p) {
   return cx<float>(v.x, v.y);
 }
 
-// Visits every (r, c) of an nr-by-nc block once: each warp takes 32-row
-// chunks of one column at a time, its lanes the rows, so consecutive lanes
-// touch consecutive rows (coalesced global access, conflict-free column-major
-// shared access) and no index is divided per element.
-template <typename F>
-__device__ __forceinline__ void for_block(int nr, int nc, F f) {
-  const int lane = threadIdx.x & 31;
-  const int nrc = (nr + 31) >> 5;               // 32-row chunks per column
-  for (int t = threadIdx.x >> 5; t < nc * nrc; t += TQR_WARPS) {
-    const int c = t / nrc, r = ((t - c * nrc) << 5) + lane;
-    if (r < nr) f(r, c);
-  }
-}
-
 // Householder scalars in NextLA's convention (src/geqr2.jl:37-68,
 // src/tsqrt.jl:52-73): beta = -copysign(sqrt(|alpha|^2 + |x|^2), re(alpha))
 // (real), tau = (beta - alpha) / beta -- for complex elements

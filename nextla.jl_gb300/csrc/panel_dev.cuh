@@ -143,12 +143,11 @@ __device__ bool column_step(const ColumnStep<E> &c, int i, int x0, int m, int nc
   {
     const int ncol = nc - i - 1, rows = m - x0;
     for (int j = i + 1 + tid; j < nc; j += TQR_THREADS) c.row[(size_t)j * c.rs] += c.d[j];
-    if (rows > 0)
-      for_block(rows, ncol, [&](int rr, int jj) {
-        const int j = i + 1 + jj;
-        E *pc = c.P + (size_t)j * c.ldp;
-        pc[x0 + rr] = mad(xcol[x0 + rr], c.d[j], pc[x0 + rr]);
-      });
+    for (int idx = tid; idx < ncol * rows; idx += TQR_THREADS) {
+      const int rr = idx % rows, j = i + 1 + idx / rows;
+      E *pc = c.P + (size_t)j * c.ldp;
+      pc[x0 + rr] = mad(xcol[x0 + rr], c.d[j], pc[x0 + rr]);
+    }
   }
   // ---- T column i ----
   if (c.Ts) {
@@ -214,7 +213,10 @@ __device__ void panel_qr_cta(int m, int nc, R *A, int lda, R *tau, R *T, int ldt
   if (staged) {
     c.ldp = odd_ld(m);
     c.P = carve<R>(sp, (size_t)c.ldp * nc);
-    for_block(m, nc, [&](int r, int cc) { c.P[ix(r, cc, c.ldp)] = ldg_cg(A + ix(r, cc, lda)); });
+    for (int idx = tid; idx < m * nc; idx += TQR_THREADS) {
+      int r = idx % m, cc = idx / m;
+      c.P[ix(r, cc, c.ldp)] = ldg_cg(A + ix(r, cc, lda));
+    }
   } else {
     c.P = A;
     c.ldp = lda;
@@ -234,7 +236,10 @@ __device__ void panel_qr_cta(int m, int nc, R *A, int lda, R *tau, R *T, int ldt
     column_step<R>(c, i, i + 1, m, nc, false, tau + i, true);
   }
   if (staged) {
-    for_block(m, nc, [&](int r, int cc) { A[ix(r, cc, lda)] = c.P[ix(r, cc, c.ldp)]; });
+    for (int idx = tid; idx < m * nc; idx += TQR_THREADS) {
+      int r = idx % m, cc = idx / m;
+      A[ix(r, cc, lda)] = c.P[ix(r, cc, c.ldp)];
+    }
   }
   if (T && stage_t) {
     for (int idx = tid; idx < k * k; idx += TQR_THREADS) {
@@ -280,9 +285,10 @@ __device__ void tsqrt_block_cta(int m, int sb, R *A1, int lda1, R *A2, int lda2,
   if (staged) {
     c.ldp = odd_ld(mrow);
     c.P = carve<R>(sp, (size_t)c.ldp * sb);
-    for_block(mrow, sb, [&](int r, int cc) {
+    for (int idx = tid; idx < mrow * sb; idx += TQR_THREADS) {
+      int r = idx % mrow, cc = idx / mrow;
       c.P[ix(r, cc, c.ldp)] = in_tri(r, cc) ? ldg_cg(A2 + ix(r, cc, lda2)) : R(0);
-    });
+    }
   } else {
     c.P = A2;
     c.ldp = lda2;
@@ -302,9 +308,10 @@ __device__ void tsqrt_block_cta(int m, int sb, R *A1, int lda1, R *A2, int lda2,
     }
   }
   if (staged) {
-    for_block(mrow, sb, [&](int r, int cc) {
+    for (int idx = tid; idx < mrow * sb; idx += TQR_THREADS) {
+      int r = idx % mrow, cc = idx / mrow;
       if (in_tri(r, cc)) A2[ix(r, cc, lda2)] = c.P[ix(r, cc, c.ldp)];
-    });
+    }
   }
   __syncthreads();
 }
