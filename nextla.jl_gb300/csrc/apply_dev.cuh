@@ -77,8 +77,7 @@ __host__ __device__ inline size_t apply_smem_elems(int L, int ib, int nw, bool s
 // FP32 strips of 16 columns take register-tiled phases 1 and 3 (each thread a
 // 4 x 4 block of outputs, so one shared-memory load feeds two FMAs instead of
 // one): the FP32 pipe is 64x the FP64 one and the FP64 layout would leave it
-// waiting on shared memory.  Needs C, V and T staged, ib <= 32 and at least
-// 128 rows.
+// waiting on shared memory.  Needs C, V and T staged and ib <= 32.
 template <typename R, int NW>
 constexpr bool kTiledF32 = std::is_same<R, float>::value && NW == 16;
 
@@ -88,9 +87,7 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
   const int tid = threadIdx.x;
   const int nwl = min(NW, a.ncols - c0);
   if (nwl <= 0) return;
-  // (short regions -- small independent problems -- keep the one-row-per-thread
-  // form, which measured faster there)
-  const bool f32_tiled = kTiledF32<R, NW> && a.stage_c && a.stage_v && a.stage_t && a.ib <= 32 && a.L >= 128;
+  const bool f32_tiled = kTiledF32<R, NW> && a.stage_c && a.stage_v && a.stage_t && a.ib <= 32;
   const int L = a.L, ib = a.ib;
   const int ldw = ib;
   const int ldcs = odd_ld(L), ldvs = odd_ld(L);
