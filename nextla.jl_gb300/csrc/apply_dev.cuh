@@ -29,8 +29,6 @@
 // (ld.global.cg): in the persistent kernel other SMs write the same tiles
 // between tasks, and L1 is not coherent with them.
 #pragma once
-#include <type_traits>
-
 #include "common.cuh"
 
 namespace tqr {
@@ -74,20 +72,12 @@ __host__ __device__ inline size_t apply_smem_elems(int L, int ib, int nw, bool s
 }
 
 // Apply to the strip of columns [c0, c0 + NW) (clamped to ncols).
-// FP32 strips of 16 columns take register-tiled phases 1 and 3 (each thread a
-// 4 x 4 block of outputs, so one shared-memory load feeds two FMAs instead of
-// one): the FP32 pipe is 64x the FP64 one and the FP64 layout would leave it
-// waiting on shared memory.  Needs C, V and T staged and ib <= 32.
-template <typename R, int NW>
-constexpr bool kTiledF32 = std::is_same<R, float>::value && NW == 16;
-
 template <typename R, int NW>
 __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_raw)
 {
   const int tid = threadIdx.x;
   const int nwl = min(NW, a.ncols - c0);
   if (nwl <= 0) return;
-  const bool f32_tiled = kTiledF32<R, NW> && a.stage_c && a.stage_v && a.stage_t && a.ib <= 32;
   const int L = a.L, ib = a.ib;
   const int ldw = ib;
   const int ldcs = odd_ld(L), ldvs = odd_ld(L);
@@ -166,58 +156,7 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
     // (mode 0 needs the unit-lower test only when V is read from global).
     const bool vtri = (a.mode == 0) && !a.stage_v;
     const bool vtt = ttb && !a.stage_v;          // unstaged TT V: bound each column's rows
-    if constexpr (kTiledF32<R, NW>) {
-      if (f32_tiled) {
-        // warp w: reflectors [4w, 4w + 4); lane: columns [4 (lane & 3), +4) and
-        // every 8th 4-row chunk from chunk lane >> 2; staged V holds explicit
-        // zeros / ones, so the product is dense over the block's rows
-        const int lane = tid & 31, cg = lane & 3, rs = lane >> 2, pb = 4 * (tid >> 5);
-        float acc[4][4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int c = 0; c < 4; ++c) acc[u][c] = 0.f;
-        const float *cb = Cp + (size_t)r0 + (size_t)(4 * cg) * ccs;
-        for (int q = rs; 4 * q < Lr; q += 8) {
-          float v[4][4], cv[4][4];
-#pragma unroll
-          for (int t = 0; t < 4; ++t) {
-            const int r = 4 * q + t;
-            const bool ok = r < Lr;
-#pragma unroll
-            for (int u = 0; u < 4; ++u) v[t][u] = (ok && pb + u < kb) ? Vp[r + (size_t)(pb + u) * ldvp] : 0.f;
-#pragma unroll
-            for (int c = 0; c < 4; ++c) cv[t][c] = ok ? cb[r + (size_t)c * ccs] : 0.f;
-          }
-#pragma unroll
-          for (int t = 0; t < 4; ++t)
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-#pragma unroll
-              for (int c = 0; c < 4; ++c) acc[u][c] = fmaf(v[t][u], cv[t][c], acc[u][c]);
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int c = 0; c < 4; ++c)
-#pragma unroll
-            for (int o = 4; o < 32; o <<= 1) acc[u][c] += __shfl_xor_sync(0xffffffffu, acc[u][c], o);
-        if (rs == 0) {
-#pragma unroll
-          for (int u = 0; u < 4; ++u)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-              const int pp = pb + u, cc = 4 * cg + c;
-              if (pp < kb && cc < nwl) {
-                float w = acc[u][c];
-                if (a.mode == 1) w += ldg_cg(A1g + (size_t)(i + pp) * a.a_rs + (size_t)cc * a.a_cs);
-                Ws[pp + cc * ldw] = w;
-              }
-            }
-        }
-      }
-    }
-    for (int e = tid; e < (f32_tiled ? 0 : kb * nwl); e += TQR_THREADS) {
+    for (int e = tid; e < kb * nwl; e += TQR_THREADS) {
       const int p = e % kb, c = e / kb;
       R acc0 = 0, acc1 = 0;
       const R *vcol = Vp + (size_t)p * ldvp;
@@ -287,41 +226,7 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
         *dst = ldg_cg(dst) - conj_if(Wf[p + c * ldw], cjc);
       }
     }
-    if constexpr (kTiledF32<R, NW>) {
-      if (f32_tiled) {
-        // thread: rows [4 (tid >> 2), +4) of every 256-row sweep, columns [4 (tid & 3), +4)
-        const int cg = tid & 3;
-        for (int rb = 4 * (tid >> 2); rb < Lr; rb += 4 * (TQR_THREADS / 4)) {
-          float acc[4][4];
-#pragma unroll
-          for (int t = 0; t < 4; ++t)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) acc[t][c] = 0.f;
-          for (int p = 0; p < kb; ++p) {
-            float v[4], w[4];
-#pragma unroll
-            for (int t = 0; t < 4; ++t) v[t] = (rb + t < Lr) ? Vp[rb + t + (size_t)p * ldvp] : 0.f;
-#pragma unroll
-            for (int c = 0; c < 4; ++c) w[c] = Wf[p + (4 * cg + c) * ldw];
-#pragma unroll
-            for (int t = 0; t < 4; ++t)
-#pragma unroll
-              for (int c = 0; c < 4; ++c) acc[t][c] = fmaf(v[t], w[c], acc[t][c]);
-          }
-#pragma unroll
-          for (int t = 0; t < 4; ++t) {
-            if (rb + t >= Lr) continue;
-            float *crow = Cp + (size_t)(r0 + rb + t);
-#pragma unroll
-            for (int c = 0; c < 4; ++c)
-              if (4 * cg + c < nwl) crow[(size_t)(4 * cg + c) * ccs] -= acc[t][c];
-          }
-        }
-      }
-    }
-    if (f32_tiled) {
-      // done above
-    } else if (nwl == NW) {
+    if (nwl == NW) {
       for (int rr = tid; rr < Lr; rr += TQR_THREADS) {
         R acc[NW];
 #pragma unroll
