@@ -254,6 +254,14 @@ int tqr_ctile_geqrf_dag(int m, int n, int nb, int ib, tqr_ccomplex *A, int lda, 
                         int ldt, tqr_ccomplex *tau, int ldtau, void *work, size_t lwork,
                         cudaStream_t stream);
 int tqr_tile_dag_status(const void *work, int *status, int *task, cudaStream_t stream);
+/* Failure-detection self-test: the FP64 persistent tile QR with task 0 also
+ * waiting for a word nothing writes and every wait bounded by wait_ms
+ * (1..5000): the launch ends by itself with status 1 (a wait timed out) and
+ * task 0 reported, the CUDA context stays usable.  Arguments as
+ * tqr_dtile_geqrf_dag; A, T, tau are left partly factored. */
+int tqr_tile_dag_wait_selftest(int m, int n, int nb, int ib, double *A, int lda, double *T, int ldt,
+                               double *tau, int ldtau, void *work, size_t lwork, int wait_ms,
+                               cudaStream_t stream);
 /* Statistics of the last run in `work` (synchronises `stream`), nanoseconds
  * summed over CTAs: out[0..5] time running each task type (GB, GA, UN, TB,
  * TA, TM), out[6] time waiting for inputs, out[7]/out[8] first and last

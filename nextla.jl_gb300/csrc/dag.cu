@@ -206,6 +206,7 @@ struct DagArgs {
   int nitems;
   long long key;
   unsigned long long timeout_ns;
+  int hold = 0;     // failure-detection test: task 0 also waits for a header word nothing writes
 };
 
 __device__ __forceinline__ int ld_acquire(const int *p) {
@@ -358,6 +359,20 @@ k_tile_dag(const DagArgs<R> a)
       const int nd = item_deps(a.g, it, c, t);
       const unsigned long long t0 = global_ns();
       int err = 0;
+      // test hook (tqr_tile_dag_wait_selftest): a wait that can only run out
+      if (a.hold && idx == 0) {
+        while (ld_acquire(reinterpret_cast<const int *>(&a.hdr->pad1[0])) == 0) {
+          if (global_ns() - t0 > a.timeout_ns) {
+            if (atomicCAS(&a.hdr->error, 0, 1) == 0) {
+              a.hdr->err_item = idx;
+              a.hdr->err_type = it.type;
+            }
+            err = 1;
+            break;
+          }
+          __nanosleep(128);
+        }
+      }
       for (int d = 0; d < nd && !err; ++d) {
         while (ld_acquire(a.cnt + c[d]) < t[d]) {
           if (ld_acquire(&a.hdr->error) != 0) { err = 1; break; }
@@ -664,7 +679,7 @@ static int launch_dag(const DagArgs<R> &a, size_t sm, double flops, cudaStream_t
 template <typename R>
 static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int ldt, R *tau,
                           int ldtau, void *work, size_t lwork, cudaStream_t st, int nrhs = 0,
-                          R *B = nullptr, int ldb = 1) {
+                          R *B = nullptr, int ldb = 1, unsigned long long hold_ns = 0) {
   if (m < 0) return -1;
   if (n < 0) return -2;
   if (nb <= 0) return -3;
@@ -706,6 +721,10 @@ static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int
   a.nitems = (int)plan->items.size();
   a.key = plan->key;
   a.timeout_ns = 20ull * 1000ull * 1000ull * 1000ull;   // 20 s for any single wait
+  if (hold_ns) {
+    a.timeout_ns = hold_ns;
+    a.hold = 1;
+  }
   size_t sm = std::max({apply_smem_elems(nb, ib, g.nw, true, true, true) * sizeof(R),
                         panel_smem<R>(nb, ib, true, true), tsqrt_smem<R>(nb, ib, true)});
   if (g.tc) sm = std::max(sm, tc::kSmem);
@@ -899,6 +918,13 @@ int tqr_ctile_geqrf_dag(int m, int n, int nb, int ib, tqr_ccomplex *A, int lda, 
   using E = cx<float>;
   if (((uintptr_t)A | (uintptr_t)T | (uintptr_t)tau) % alignof(E)) return -5;
   return tile_geqrf_dag<E>(m, n, nb, ib, (E *)A, lda, (E *)T, ldt, (E *)tau, ldtau, work, lwork, stream);
+}
+
+int tqr_tile_dag_wait_selftest(int m, int n, int nb, int ib, double *A, int lda, double *T, int ldt, double *tau,
+                               int ldtau, void *work, size_t lwork, int wait_ms, cudaStream_t stream) {
+  if (wait_ms <= 0 || wait_ms > 5000) return -13;
+  return tile_geqrf_dag<double>(m, n, nb, ib, A, lda, T, ldt, tau, ldtau, work, lwork, stream, 0, nullptr, 1,
+                                (unsigned long long)wait_ms * 1000000ull);
 }
 
 int tqr_tile_dag_status(const void *work, int *status, int *task, cudaStream_t stream) {

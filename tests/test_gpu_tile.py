@@ -153,3 +153,43 @@ def test_full_size_properties(tq, m, n):
     assert rel(Bh[:n], Rh) < 1e-12 * n
     if m > n:
         assert np.max(np.abs(Bh[n:])) < 1e-12 * n * np.max(np.abs(Rh))
+
+
+def test_dag_bounded_wait_reports_and_context_survives(tq):
+    """Failure detection without a fault: task 0 of the persistent kernel also
+    waits for a word nothing writes.  Every wait is bounded (100 ms here), so
+    the launch ends by itself with status 1 (a wait timed out) and the CUDA
+    context stays usable: a normal factorisation afterwards is correct."""
+    import ctypes
+    import time
+    import torch
+    from tileqr import _lib
+    L = _lib.lib()
+    m = n = 512
+    nb, ib = 256, 32
+    rng = np.random.default_rng(5)
+    A0 = np.asfortranarray(rng.standard_normal((m, n)))
+    A = tq.to_device(A0)
+    ts, taus = tq.tile_shapes(m, n, nb, ib)
+    T, tau = tq.zeros(*ts), tq.zeros(*taus)
+    w, off, size = tq.dag_workspace(m, n, nb, ib, A.device)
+    wp = w.data_ptr() + off
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    st = torch.cuda.current_stream()
+    t0 = time.time()
+    rc = L.tqr_tile_dag_wait_selftest(m, n, nb, ib, P(A), m, P(T), ts[0], P(tau), taus[0], ctypes.c_void_p(wp), size,
+                                      100, ctypes.c_void_p(st.cuda_stream))
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert time.time() - t0 < 10
+    status, task = tq.dag_status(wp)
+    assert status == 1, (status, task)
+    assert L.tqr_tile_dag_wait_selftest(m, n, nb, ib, P(A), m, P(T), ts[0], P(tau), taus[0], ctypes.c_void_p(wp),
+                                        size, 0, None) == -13
+    # the context still works: a full factorisation is right
+    B = tq.to_device(A0)
+    tq.tile_geqrf(B, nb, ib)
+    R = np.triu(tq.to_numpy(B)[:n])
+    x = rng.standard_normal((n, 2))
+    ax = np.linalg.norm(A0 @ x, axis=0)
+    assert np.max(np.abs(ax - np.linalg.norm(R @ x, axis=0)) / ax) < 1e-13 * n
