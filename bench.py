@@ -55,6 +55,8 @@ def parse():
     p.add_argument("--no-batched", action="store_true", help="skip the batched uneven QR + solve")
     p.add_argument("--batched-only", action="store_true", help="run only the batched uneven QR + solve")
     p.add_argument("--batched-n", type=int, default=4096, help="problems per batch")
+    p.add_argument("--batched-no-tune", action="store_true",
+                   help="default (ib, strip) per size class instead of the autotuner's choice")
     p.add_argument("--no-adjoint", action="store_true", help="skip the differentiable QR")
     p.add_argument("--adjoint-only", action="store_true", help="run only the differentiable QR")
     p.add_argument("--no-tall", action="store_true", help="skip the tall-skinny flat vs tree comparison")
@@ -408,7 +410,7 @@ def ls_bench(tq, torch, m=32768, n=4096, k=4, steps=2, warmup=1, orth=True):
     return res
 
 
-def batched_bench(torch, nprob=4096, steps=5, warmup=3, peak=None):
+def batched_bench(torch, nprob=4096, steps=5, warmup=3, peak=None, tune=True):
     """Batched uneven QR + least squares: nprob problems, m ~ U[32,512],
     n ~ U[16,m], k ~ U[1,8], N(0,1) entries, one persistent launch replayed
     from a CUDA graph.  Per precision: problems/s with inputs resident
@@ -424,7 +426,7 @@ def batched_bench(torch, nprob=4096, steps=5, warmup=3, peak=None):
            "unit": "problems/s"}
     ms_, ns_, ks_ = Bt.random_sizes(nprob, seed=SEED % 1000)
     for tag, dt in (("f64", torch.float64), ("f32", torch.float32)):
-        bg = Bt.BatchedGels(ms_, ns_, ks_, dtype=dt, tune=True)
+        bg = Bt.BatchedGels(ms_, ns_, ks_, dtype=dt, tune=tune)
         g = torch.Generator(device="cuda").manual_seed(SEED)
         A0 = torch.randn(bg.A.shape, generator=g, device="cuda", dtype=torch.float64).to(dt)
         B0 = torch.randn(bg.B.shape, generator=g, device="cuda", dtype=torch.float64).to(dt)
@@ -887,7 +889,7 @@ def main():
         import tileqr_build
         from tileqr import _lib
         tileqr_build.build()
-        res = batched_bench(torch, args.batched_n, max(1, args.steps), max(3, args.warmup),
+        res = batched_bench(torch, args.batched_n, max(1, args.steps), max(3, args.warmup), tune=not args.batched_no_tune,
                             peak=fp64_peak(_lib, torch))
         print(json.dumps(res), flush=True)
         return 0
