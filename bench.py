@@ -59,6 +59,8 @@ def parse():
                    help="default (ib, strip) per size class instead of the autotuner's choice")
     p.add_argument("--no-adjoint", action="store_true", help="skip the differentiable QR")
     p.add_argument("--adjoint-only", action="store_true", help="run only the differentiable QR")
+    p.add_argument("--adjoint-kernels", action="store_true",
+                   help="with --adjoint-only: the forward and adjoint kernels alone, seeded cotangents")
     p.add_argument("--no-tall", action="store_true", help="skip the tall-skinny flat vs tree comparison")
     p.add_argument("--tall-only", action="store_true", help="run only the tall-skinny flat vs tree comparison")
     p.add_argument("--no-complex", action="store_true", help="skip the complex tile QR")
@@ -695,7 +697,7 @@ def lapack_dgeqrf_tflops(n):
     return flops_square(n) / dt / 1e12, dt
 
 
-def adjoint_bench(torch, batch=256, m=2048, n=256, steps=3, warmup=3, peak=None):
+def adjoint_bench(torch, batch=256, m=2048, n=256, steps=3, warmup=3, peak=None, kernels_only=False):
     """Differentiable QR: (Q, R) = qr(A) for a batch of 256 Float64 2048x256
     N(0,1) matrices, loss 1/2||R^-1 Q^T b - y||^2 + <dQ, Q> + <dR, R> with
     seeded b, y, dQ, dR, backward through the adjoint kernel.  Times the
@@ -730,9 +732,13 @@ def adjoint_bench(torch, batch=256, m=2048, n=256, steps=3, warmup=3, peak=None)
         e0.record(st)
         Q, R, F, tau = AD.qr_forward(A)
         e1.record(st)
-        Ql = Q.requires_grad_(True)
-        Rl = R.requires_grad_(True)
-        Qb, Rb = torch.autograd.grad(loss(Ql, Rl), (Ql, Rl))
+        if kernels_only:
+            # the kernels alone (profiling): seeded cotangents instead of the loss's
+            Qb, Rb = dQ, torch.triu(dR)
+        else:
+            Ql = Q.requires_grad_(True)
+            Rl = R.requires_grad_(True)
+            Qb, Rb = torch.autograd.grad(loss(Ql, Rl), (Ql, Rl))
         e2.record(st)
         Ab = AD.qr_backward(F, tau, Qb, Rb)
         e3.record(st)
@@ -742,6 +748,9 @@ def adjoint_bench(torch, batch=256, m=2048, n=256, steps=3, warmup=3, peak=None)
             bwd_ms.append(e2.elapsed_time(e3))
             step_ms.append(e0.elapsed_time(e3))
     launches = (_lib.launch_count() - launches0) / (warmup + steps)
+    if kernels_only:
+        return {"workload": f"QR forward and adjoint kernels, batch of {batch} Float64 {m}x{n}, seeded cotangents",
+                "fwd_ms": statistics.median(fwd_ms), "bwd_ms": statistics.median(bwd_ms)}
     # the autograd path end to end (rule's backward) must give the same gradient
     Ar = A.detach().clone().requires_grad_(True)
     Q, R = AD.qr(Ar)
@@ -880,6 +889,7 @@ def main():
         from tileqr import _lib
         tileqr_build.build()
         res = adjoint_bench(torch, 256, 2048, 256, max(1, args.steps), max(3, args.warmup),
+                            kernels_only=args.adjoint_kernels,
                             peak=fp64_peak(_lib, torch))
         print(json.dumps(res), flush=True)
         return 0
