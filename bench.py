@@ -493,6 +493,46 @@ def batched_bench(torch, nprob=4096, steps=5, warmup=3, peak=None, tune=True):
     return out
 
 
+def batched_sharded_bench(torch, nprob, world, rank, steps=5, warmup=3):
+    """The FP64 batch of batched_bench split across the ranks by cost
+    (tileqr.batched.shard): each rank solves its part in one persistent
+    launch; time = max over ranks of the timed replays; no collective on the
+    data path (results would be gathered on the host)."""
+    from tileqr import batched as Bt
+    ms_, ns_, ks_ = Bt.random_sizes(nprob, seed=SEED % 1000)
+    mine = Bt.shard(ms_, ns_, ks_, world, rank)
+    bg = Bt.BatchedGels(ms_[mine], ns_[mine], ks_[mine], dtype=torch.float64, tune=True)
+    g = torch.Generator(device="cuda").manual_seed(SEED + rank)
+    A0 = torch.randn(bg.A.shape, generator=g, device="cuda", dtype=torch.float64)
+    B0 = torch.randn(bg.B.shape, generator=g, device="cuda", dtype=torch.float64)
+    bg.capture()
+    st = torch.cuda.current_stream()
+    for _ in range(warmup):
+        bg.A.copy_(A0)
+        bg.B.copy_(B0)
+        bg.replay(sync=True)
+    total = 0.0
+    for _ in range(steps):
+        bg.A.copy_(A0)
+        bg.B.copy_(B0)
+        torch.cuda.synchronize()
+        barrier(world)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        bg.replay(sync=False)
+        e1.record(st)
+        torch.cuda.synchronize()
+        total += reduce_max(e0.elapsed_time(e1), world)
+    ms = total / steps
+    cost = Bt.problem_cost(ms_, ns_, ks_)
+    bad = bg.status()
+    bg.close()
+    return {"workload": f"{nprob} FP64 least-squares problems (the batched_uneven_gels batch) split by cost over "
+                        f"{world} ranks", "problems_per_s": nprob / (ms / 1e3), "ms_per_batch": ms,
+            "rank0_problems": int(mine.size), "rank0_cost_share": float(cost[mine].sum() / cost.sum()),
+            "rejected_descriptors_rank0": bad[0], "scaling": "strong (fixed batch)"}
+
+
 def tall_bench(tq, torch, m=65536, n=512, steps=3, warmup=2, peak=None, dtype="f64"):
     """Tall-skinny tile QR (m x n, N(0,1), nb = 256, ib = 32): the flat-tree
     persistent kernel against the binary-tree driver (geqrt on every tile,
@@ -1049,6 +1089,10 @@ def main():
     if rank == 0 and world == 1 and not args.no_adjoint:
         adj = adjoint_bench(torch, 256, 2048, 256, 3, 3, peak=peak)
 
+    sharded = None
+    if world > 1 and not args.no_batched:
+        sharded = batched_sharded_bench(torch, args.batched_n, world, rank)
+
     cplx = None
     if rank == 0 and world == 1 and not args.no_complex:
         cplx = complex_bench(tq, torch, args.complex_n, 3, 3, peak=peak)
@@ -1070,6 +1114,7 @@ def main():
             "dag_stats_last_step": dag,
             "least_squares_mixed_vs_fp64": ls,
             "batched_uneven_gels": bat,
+            "batched_uneven_gels_sharded": sharded,
             "differentiable_qr": adj,
             "tall_skinny_65536x512": tall,
             "complex_tile_qr": cplx,

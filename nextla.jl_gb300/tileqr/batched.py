@@ -217,3 +217,30 @@ def random_sizes(nprob, seed=0, max_m=MAX_M, min_m=32, min_n=16, max_k=MAX_K):
     ns = np.array([rng.integers(min(min_n, m), m + 1) for m in ms])
     ks = rng.integers(1, max_k + 1, size=nprob)
     return ms.astype(np.int32), ns.astype(np.int32), ks.astype(np.int32)
+
+
+def problem_cost(ms, ns, ks):
+    """Flops of each problem: 2 m n^2 - 2 n^3 / 3 (QR) + 4 m n k (Q^T B) + n^2 k (solve)."""
+    m = np.asarray(ms, dtype=np.float64)
+    n = np.asarray(ns, dtype=np.float64)
+    k = np.asarray(ks, dtype=np.float64)
+    return 2 * m * n * n - 2 * n ** 3 / 3 + 4 * m * n * k + n * n * k
+
+
+def shard(ms, ns, ks, world, rank):
+    """Indices of the problems rank `rank` of `world` solves: the batch split by
+    cost, largest problem first onto the least-loaded rank (ties to the lower
+    rank), so every rank computes the same partition without communication.
+    The ranks' results are gathered on the host afterwards; the solves need no
+    collective."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("need 0 <= rank < world")
+    cost = problem_cost(ms, ns, ks)
+    order = np.lexsort((np.arange(cost.size), -cost))       # cost descending, index ascending
+    load = np.zeros(world)
+    owner = np.empty(cost.size, dtype=np.int64)
+    for q in order:
+        r = int(np.argmin(load))
+        owner[q] = r
+        load[r] += cost[q]
+    return np.nonzero(owner == rank)[0]

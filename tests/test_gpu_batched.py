@@ -165,3 +165,17 @@ def test_batched_rejects_corrupt_descriptor(tq):
     assert res[ok].max() < 1e-14
     # the rejected problem's data is untouched
     assert torch.equal(bg.a_view(17), bg.a_view(17, A0))
+
+
+def test_sharded_batch_one_rank(tq):
+    """The multi-rank batched measurement with a single rank: the whole batch,
+    all of its cost, no rejected descriptors."""
+    import os
+    import sys
+    import torch
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    import bench
+    r = bench.batched_sharded_bench(torch, 512, 1, 0, steps=1, warmup=1)
+    assert r["rank0_problems"] == 512 and abs(r["rank0_cost_share"] - 1.0) < 1e-12
+    assert r["rejected_descriptors_rank0"] == 0 and r["problems_per_s"] > 0
