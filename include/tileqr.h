@@ -106,6 +106,26 @@ int tqr_sparfb(char side, char trans, char direct, char storev, int m1, int n1, 
                int k, int l, float *A1, int lda1, float *A2, int lda2, const float *V, int ldv,
                const float *T, int ldt, float *work, int ldwork, cudaStream_t stream);
 
+/* pamm!(op, side, storev, direct, m, n, k, l, A1, A2, V, W) -- src/pamm.jl:49-473.
+ * Every op / side / storev / direct form.  Ve, the reflector block in its
+ * canonical orientation (mv x k, mv = m for side 'L', n for 'R'), is V
+ * (storev 'C') or V^T ('R'), with a trapezoid of order l: direct 'F' keeps
+ * only the upper triangle of the last l rows of the first l columns, 'B' only
+ * the lower triangle of the first l rows of the last l columns.
+ *   op 'W': W = A1 + f(Ve)^T A2 ('L', W k x n) or A1 + A2 f(Ve) ('R', W m x k),
+ *           f = conjugation for (L, C) and (R, R);
+ *   op 'A': A2 -= g(Ve) W ('L') or W g(Ve)^T ('R'), g = conjugation for
+ *           (L, R) and (R, C); W's first ('F') or last ('B') l rows ('L') /
+ *           columns ('R') are left holding the trapezoid's triangle times W,
+ *           as the reference's in-place triangular product leaves them.
+ *           A1 is not used (may be NULL).
+ * Requires 0 <= l <= min(k, mv) (-8 otherwise). */
+int tqr_dpamm(char op, char side, char storev, char direct, int m, int n, int k, int l, const double *A1,
+              int lda1, double *A2, int lda2, const double *V, int ldv, double *W, int ldw,
+              cudaStream_t stream);
+int tqr_spamm(char op, char side, char storev, char direct, int m, int n, int k, int l, const float *A1,
+              int lda1, float *A2, int lda2, const float *V, int ldv, float *W, int ldw, cudaStream_t stream);
+
 /* ttqrt!(m, n, ib, A1, A2, T, tau, work) -- src/ttqrt.jl:81-119.
  * QR of [A1 (upper triangular); A2 (upper triangular, m-by-n)], k = min(m, n)
  * reflectors; column r's reflector occupies A2 rows [0, min(r + 1, m)).
@@ -175,6 +195,9 @@ int tqr_ztile_geqrf(int m, int n, int nb, int ib, tqr_zcomplex *A, int lda, tqr_
 int tqr_ztile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const tqr_zcomplex *A,
                     int lda, const tqr_zcomplex *T, int ldt, tqr_zcomplex *B, int ldb,
                     cudaStream_t stream);
+int tqr_zpamm(char op, char side, char storev, char direct, int m, int n, int k, int l,
+              const tqr_zcomplex *A1, int lda1, tqr_zcomplex *A2, int lda2, const tqr_zcomplex *V,
+              int ldv, tqr_zcomplex *W, int ldw, cudaStream_t stream);
 int tqr_ztrsm_lun(int n, int nrhs, const tqr_zcomplex *R, int ldr, tqr_zcomplex *B, int ldb,
                   cudaStream_t stream);
 int tqr_ztile_gels(int m, int n, int nrhs, int nb, int ib, tqr_zcomplex *A, int lda, tqr_zcomplex *T,
@@ -215,6 +238,9 @@ int tqr_ctile_geqrf(int m, int n, int nb, int ib, tqr_ccomplex *A, int lda, tqr_
 int tqr_ctile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const tqr_ccomplex *A,
                     int lda, const tqr_ccomplex *T, int ldt, tqr_ccomplex *B, int ldb,
                     cudaStream_t stream);
+int tqr_cpamm(char op, char side, char storev, char direct, int m, int n, int k, int l,
+              const tqr_ccomplex *A1, int lda1, tqr_ccomplex *A2, int lda2, const tqr_ccomplex *V,
+              int ldv, tqr_ccomplex *W, int ldw, cudaStream_t stream);
 int tqr_ctrsm_lun(int n, int nrhs, const tqr_ccomplex *R, int ldr, tqr_ccomplex *B, int ldb,
                   cudaStream_t stream);
 int tqr_ctile_gels(int m, int n, int nrhs, int nb, int ib, tqr_ccomplex *A, int lda, tqr_ccomplex *T,

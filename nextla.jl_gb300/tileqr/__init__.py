@@ -21,7 +21,7 @@ from . import _lib
 
 __all__ = [
     "ArgumentError", "set_blocking", "empty", "zeros", "to_device", "to_numpy",
-    "geqr2", "larft", "larfb", "geqrt", "unmqr", "tsqrt", "tsmqr", "parfb", "ttqrt", "ttmqr",
+    "geqr2", "larft", "larfb", "geqrt", "unmqr", "tsqrt", "tsmqr", "parfb", "pamm", "ttqrt", "ttmqr",
     "tile_geqrf", "tile_unmqr", "trsm_lun", "tile_gels", "tile_shapes",
 ]
 
@@ -296,6 +296,18 @@ def parfb(*args):
     pt, ldt = _mat(T)
     _call(_prefix(A1, A2, V, T), "parfb", _ch(side), _ch(trans), _ch(direct), _ch(storev),
           m1, n1, m2, n2, k, l, p1, ld1, p2, ld2, pv, ldv, pt, ldt, None, 1)
+
+
+def pamm(op, side, storev, direct, m, n, k, l, A1, A2, V, W):
+    """pamm!(op, side, storev, direct, m, n, k, l, A1, A2, V, W) -- src/pamm.jl:49-473
+    (op 'W': W = A1 + op(V) A2 or A1 + A2 op(V); op 'A': A2 -= op(V) W or W op(V),
+    every storev / direct form, V's trapezoid of order l)."""
+    p1, ld1 = _mat(A1)
+    p2, ld2 = _mat(A2)
+    pv, ldv = _mat(V)
+    pw, ldw = _mat(W)
+    _call(_prefix(A1, A2, V, W), "pamm", _ch(op), _ch(side), _ch(storev), _ch(direct), m, n, k, l,
+          p1, ld1, p2, ld2, pv, ldv, pw, ldw)
 
 
 def ttqrt(*args):

@@ -25,6 +25,7 @@ SIGNATURES = {
     "tsmqr": [_C, _C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
     "parfb": [_C, _C, _C, _C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
     "ttqrt": [_I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _P, _P],
+    "pamm": [_C, _C, _C, _C, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
     "ttmqr": [_C, _C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P],
     "tile_geqrf": [_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P],
     "tile_unmqr": [_C, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P],
@@ -38,7 +39,7 @@ SIGNATURES = {
 
 # routines that also exist for ComplexF64 (prefix z) and ComplexF32 (prefix c)
 COMPLEX = ("geqr2", "larft", "larfb", "geqrt", "unmqr", "tsqrt", "tsmqr", "parfb", "ttqrt", "ttmqr",
-           "tile_geqrf", "tile_unmqr", "trsm_lun", "tile_gels")
+           "tile_geqrf", "tile_unmqr", "trsm_lun", "tile_gels", "pamm")
 
 
 def prefixes(name):

@@ -1018,3 +1018,102 @@ int ora_dtile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, con
     int rc = ora_dtile_unmqr_hqr(trans, m, n, nrhs, nb, ib, 1, A, lda, T, ldt, T2, B, ldb);
     return rc < -6 ? rc + 1 : rc;
 }
+
+/* ------------------------------------------------------------------------ */
+/* pamm (src/pamm.jl:49-473), every op / side / storev / direct form.        */
+/* The reflector block, in its canonical orientation Ve (mv x k, mv = m for  */
+/* side L, n for R), is V (storev 'C') or V^T ('R'); its trapezoid of order  */
+/* l holds, for direct 'F', only the upper triangle of the last l rows of    */
+/* the first l columns (pamm.jl:104-127) and, for 'B', only the lower        */
+/* triangle of the first l rows of the last l columns (pamm.jl:197-222).     */
+/*   op 'W': W = A1 + f(Ve)^T A2 (L) or A1 + A2 f(Ve) (R), f = conj for     */
+/*           (L, C) and (R, R) (pamm.jl:97-298);                             */
+/*   op 'A': A2 -= g(Ve) W (L) or W g(Ve)^T (R), g = conj for (L, R) and     */
+/*           (R, C); the reference also leaves the trapezoid's triangle      */
+/*           times W in W's first ('F') or last ('B') l rows (L) / columns   */
+/*           (R) (pamm.jl:317-319 and the other forms' trimatmul), which is  */
+/*           reproduced here.                                                */
+/* Requires 0 <= l <= min(k, mv).                                            */
+/* ------------------------------------------------------------------------ */
+static int pamm_valid(int fwd, int r, int p, int mv, int k, int l)
+{
+    if (fwd) return !(p < l && r >= mv - l && r - (mv - l) > p);
+    return !(p >= k - l && r < l && r < p - (k - l));
+}
+
+int ora_dpamm(char op, char side, char storev, char direct, int m, int n, int k, int l,
+              const double *A1, int lda1, double *A2, int lda2, const double *V, int ldv,
+              double *W, int ldw)
+{
+    if (op != 'W' && op != 'A') return -1;
+    if (side != 'L' && side != 'R') return -2;
+    if (storev != 'C' && storev != 'R') return -3;
+    if (direct != 'F' && direct != 'B') return -4;
+    if (m < 0) return -5;
+    if (n < 0) return -6;
+    if (k < 0) return -7;
+    if (l < 0) return -8;
+    if (m == 0 || n == 0 || k == 0) return 0;
+    int L = (side == 'L'), C = (storev == 'C'), fwd = (direct == 'F');
+    int mv = L ? m : n;
+    if (l > k || l > mv) return -8;
+#define VE(r, p) (C ? V[IDX(r, p, ldv)] : V[IDX(p, r, ldv)])
+    if (op == 'W') {
+        if (L) {
+            for (int c = 0; c < n; ++c)
+                for (int p = 0; p < k; ++p) {
+                    double acc = 0.0;
+                    for (int r = 0; r < m; ++r)
+                        if (pamm_valid(fwd, r, p, mv, k, l)) acc += VE(r, p) * A2[IDX(r, c, lda2)];
+                    W[IDX(p, c, ldw)] = A1[IDX(p, c, lda1)] + acc;
+                }
+        } else {
+            for (int p = 0; p < k; ++p)
+                for (int i = 0; i < m; ++i) {
+                    double acc = 0.0;
+                    for (int c = 0; c < n; ++c)
+                        if (pamm_valid(fwd, c, p, mv, k, l)) acc += A2[IDX(i, c, lda2)] * VE(c, p);
+                    W[IDX(i, p, ldw)] = A1[IDX(i, p, lda1)] + acc;
+                }
+        }
+        return 0;
+    }
+    /* op 'A': A2 first, from the incoming W */
+    if (L) {
+        for (int c = 0; c < n; ++c)
+            for (int r = 0; r < m; ++r) {
+                double acc = 0.0;
+                for (int p = 0; p < k; ++p)
+                    if (pamm_valid(fwd, r, p, mv, k, l)) acc += VE(r, p) * W[IDX(p, c, ldw)];
+                A2[IDX(r, c, lda2)] -= acc;
+            }
+    } else {
+        for (int c = 0; c < n; ++c)
+            for (int i = 0; i < m; ++i) {
+                double acc = 0.0;
+                for (int p = 0; p < k; ++p)
+                    if (pamm_valid(fwd, c, p, mv, k, l)) acc += W[IDX(i, p, ldw)] * VE(c, p);
+                A2[IDX(i, c, lda2)] -= acc;
+            }
+    }
+    /* then the triangle times W in W's block of l rows (L) / columns (R) */
+    int b0 = fwd ? 0 : k - l;
+    int cnt = L ? n : m;
+    double *tmp = (double *)malloc(sizeof(double) * (size_t)(l > 0 ? l : 1));
+    for (int x = 0; x < cnt; ++x) {
+        for (int t = 0; t < l; ++t) {
+            int rt = fwd ? mv - l + t : t;                  /* the A2 row (column) of triangle row t */
+            double acc = 0.0;
+            for (int p = b0; p < b0 + l; ++p)
+                if (pamm_valid(fwd, rt, p, mv, k, l))
+                    acc += VE(rt, p) * (L ? W[IDX(p, x, ldw)] : W[IDX(x, p, ldw)]);
+            tmp[t] = acc;
+        }
+        for (int t = 0; t < l; ++t) {
+            if (L) W[IDX(b0 + t, x, ldw)] = tmp[t]; else W[IDX(x, b0 + t, ldw)] = tmp[t];
+        }
+    }
+    free(tmp);
+#undef VE
+    return 0;
+}

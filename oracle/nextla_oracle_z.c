@@ -764,3 +764,96 @@ int ora_ztrsm_lun(int n, int nrhs, const zc *A, int lda, zc *B, int ldb)
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* pamm for complex elements: the forms of ora_dpamm (nextla_oracle.c) with */
+/* the reference's conjugations -- op 'W' conjugates Ve for (L, C) and      */
+/* (R, R) (pamm.jl:120,139-153,...: 'C' / adjoint), op 'A' for (L, R) and   */
+/* (R, C) (pamm.jl:330-343, 351-365, ...).                                  */
+/* ------------------------------------------------------------------------ */
+static int zpamm_valid(int fwd, int r, int p, int mv, int k, int l)
+{
+    if (fwd) return !(p < l && r >= mv - l && r - (mv - l) > p);
+    return !(p >= k - l && r < l && r < p - (k - l));
+}
+
+int ora_zpamm(char op, char side, char storev, char direct, int m, int n, int k, int l,
+              const zc *A1, int lda1, zc *A2, int lda2, const zc *V, int ldv, zc *W, int ldw)
+{
+    if (op != 'W' && op != 'A') return -1;
+    if (side != 'L' && side != 'R') return -2;
+    if (storev != 'C' && storev != 'R') return -3;
+    if (direct != 'F' && direct != 'B') return -4;
+    if (m < 0) return -5;
+    if (n < 0) return -6;
+    if (k < 0) return -7;
+    if (l < 0) return -8;
+    if (m == 0 || n == 0 || k == 0) return 0;
+    int L = (side == 'L'), C = (storev == 'C'), fwd = (direct == 'F');
+    int mv = L ? m : n;
+    if (l > k || l > mv) return -8;
+    int cjw = (L && C) || (!L && !C), cja = (L && !C) || (!L && C);
+#define VE(r, p) (C ? V[IDX(r, p, ldv)] : V[IDX(p, r, ldv)])
+    if (op == 'W') {
+        if (L) {
+            for (int c = 0; c < n; ++c)
+                for (int p = 0; p < k; ++p) {
+                    zc acc = 0.0;
+                    for (int r = 0; r < m; ++r)
+                        if (zpamm_valid(fwd, r, p, mv, k, l))
+                            acc += zmul(cjw ? conj(VE(r, p)) : VE(r, p), A2[IDX(r, c, lda2)]);
+                    W[IDX(p, c, ldw)] = A1[IDX(p, c, lda1)] + acc;
+                }
+        } else {
+            for (int p = 0; p < k; ++p)
+                for (int i = 0; i < m; ++i) {
+                    zc acc = 0.0;
+                    for (int c = 0; c < n; ++c)
+                        if (zpamm_valid(fwd, c, p, mv, k, l))
+                            acc += zmul(A2[IDX(i, c, lda2)], cjw ? conj(VE(c, p)) : VE(c, p));
+                    W[IDX(i, p, ldw)] = A1[IDX(i, p, lda1)] + acc;
+                }
+        }
+        return 0;
+    }
+    if (L) {
+        for (int c = 0; c < n; ++c)
+            for (int r = 0; r < m; ++r) {
+                zc acc = 0.0;
+                for (int p = 0; p < k; ++p)
+                    if (zpamm_valid(fwd, r, p, mv, k, l))
+                        acc += zmul(cja ? conj(VE(r, p)) : VE(r, p), W[IDX(p, c, ldw)]);
+                A2[IDX(r, c, lda2)] -= acc;
+            }
+    } else {
+        for (int c = 0; c < n; ++c)
+            for (int i = 0; i < m; ++i) {
+                zc acc = 0.0;
+                for (int p = 0; p < k; ++p)
+                    if (zpamm_valid(fwd, c, p, mv, k, l))
+                        acc += zmul(W[IDX(i, p, ldw)], cja ? conj(VE(c, p)) : VE(c, p));
+                A2[IDX(i, c, lda2)] -= acc;
+            }
+    }
+    int b0 = fwd ? 0 : k - l;
+    int cnt = L ? n : m;
+    zc *tmp = (zc *)malloc(sizeof(zc) * (size_t)(l > 0 ? l : 1));
+    for (int x = 0; x < cnt; ++x) {
+        for (int t = 0; t < l; ++t) {
+            int rt = fwd ? mv - l + t : t;
+            zc acc = 0.0;
+            for (int p = b0; p < b0 + l; ++p)
+                if (zpamm_valid(fwd, rt, p, mv, k, l)) {
+                    zc v = cja ? conj(VE(rt, p)) : VE(rt, p);
+                    acc += L ? zmul(v, W[IDX(p, x, ldw)]) : zmul(W[IDX(x, p, ldw)], v);
+                }
+            tmp[t] = acc;
+        }
+        for (int t = 0; t < l; ++t) {
+            if (L) W[IDX(b0 + t, x, ldw)] = tmp[t]; else W[IDX(x, b0 + t, ldw)] = tmp[t];
+        }
+    }
+    free(tmp);
+#undef VE
+    return 0;
+}

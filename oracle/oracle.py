@@ -70,10 +70,11 @@ def _declare(L):
         "ora_dtile_geqrf_tree": [_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _P],
         "ora_dtile_unmqr_tree": [_C, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _P, _I],
         "ora_dtile_geqrf_hqr": [_I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _P],
+        "ora_dpamm": [_C, _C, _C, _C, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I],
         "ora_dtile_unmqr_hqr": [_C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _P, _I],
     }
     for name in ("geqr2", "larft", "larfb", "geqrt", "unmqr", "parfb", "parfb_l", "tsmqr", "tsqrt", "ttqrt",
-                 "ttmqr", "tile_geqrf", "tile_unmqr", "trsm_lun"):
+                 "ttmqr", "tile_geqrf", "tile_unmqr", "trsm_lun", "pamm"):
         sig["ora_z" + name] = sig["ora_d" + name]
     for name, args in sig.items():
         f = getattr(L, name)
@@ -262,6 +263,16 @@ def tile_geqrf_tree(A, nb, ib):
     _check(lib().ora_dtile_geqrf_tree(m, n, nb, ib, pa, lda, T.ctypes.data, MT * ib, tau.ctypes.data, n,
                                       T2.ctypes.data, tau2.ctypes.data), "tile_geqrf_tree")
     return T, tau, T2, tau2
+
+
+def pamm(op, side, storev, direct, m, n, k, l, A1, A2, V, W):
+    """pamm!(op, side, storev, direct, m, n, k, l, A1, A2, V, W) -- src/pamm.jl:49."""
+    p1, ld1 = _mat(A1)
+    p2, ld2 = _mat(A2)
+    pv, ldv = _mat(V)
+    pw, ldw = _mat(W)
+    return _check(_fn("pamm", A1, A2, V, W)(_ch(op), _ch(side), _ch(storev), _ch(direct), m, n, k, l, p1, ld1,
+                                            p2, ld2, pv, ldv, pw, ldw), "pamm")
 
 
 def tile_geqrf_hqr(A, nb, ib, grp):
