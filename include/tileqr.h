@@ -94,11 +94,11 @@ int tqr_stsmqr(char side, char trans, int m1, int n1, int m2, int n2, int k, int
                float *work, int lwork, cudaStream_t stream);
 
 /* parfb!(side, trans, direct, storev, m1, n1, m2, n2, k, l, A1, A2, V, T, work)
- * -- src/parfb.jl:44-191 with pamm! (src/pamm.jl:49-473).  Implemented for
- * forward, columnwise reflectors (direct 'B' returns -3, storev 'R' -4) with
- * any triangular order 0 <= l <= k: V's first l columns hold, over the last
- * l of the m2 (side 'R': n2) rows, only an upper triangle, whose strictly
- * lower part is not read. */
+ * -- src/parfb.jl:44-191 with pamm! (src/pamm.jl:49-473), every side x trans x
+ * direct x storev form, triangular order 0 <= l <= k (V's trapezoid as in
+ * tqr_?pamm).  The forward columnwise form (the one tsmqr! and ttmqr! use) runs
+ * fused and ignores work; the backward and rowwise forms go through pamm! and
+ * need work (k x n2 for side 'L', m2 x k for 'R', ldwork; -20 if missing). */
 int tqr_dparfb(char side, char trans, char direct, char storev, int m1, int n1, int m2, int n2,
                int k, int l, double *A1, int lda1, double *A2, int lda2, const double *V, int ldv,
                const double *T, int ldt, double *work, int ldwork, cudaStream_t stream);

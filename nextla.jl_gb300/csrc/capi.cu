@@ -139,7 +139,7 @@ namespace {
 template <typename R>
 int parfb_impl(char side, char trans, char direct, char storev, int m1, int n1, int m2, int n2,
                int k, int l, R *A1, int lda1, R *A2, int lda2, const R *V, int ldv, const R *T,
-               int ldt, cudaStream_t st) {
+               int ldt, R *work, int ldwork, cudaStream_t st) {
   if (!is_side(side)) return -1;             // src/parfb.jl:47-85
   if (!is_trans(trans)) return -2;
   if (direct != 'F' && direct != 'B') return -3;
@@ -152,13 +152,17 @@ int parfb_impl(char side, char trans, char direct, char storev, int m1, int n1, 
   if (l < 0 || l > k) return -10;
   if (m1 == 0 || n1 == 0 || n2 == 0 || k == 0) return 0;
   if (m2 == 0) return 0;
-  // Forward, columnwise reflectors (the forms tsmqr! and ttmqr! use).  A
-  // triangular part of order l makes reflector q hold rows (columns for
-  // side R) [0, mv - l + q] of V, mv = m2 (n2): pamm's trapezoid
-  // (src/pamm.jl:104-127, 153-175).
-  if (direct != 'F') return -3;
-  if (storev != 'C') return -4;
+  // Forward, columnwise reflectors (the forms tsmqr! and ttmqr! use) run in
+  // the fused apply: a triangular part of order l makes reflector q hold rows
+  // (columns for side R) [0, mv - l + q] of V, mv = m2 (n2): pamm's trapezoid
+  // (src/pamm.jl:104-127, 153-175).  The other forms go through pamm with the
+  // caller's work (k x n2 for side L, m2 x k for R).
   const int mv = side == 'L' ? m2 : n2;
+  if (direct != 'F' || storev != 'C') {
+    if (!work || ldwork < (side == 'L' ? k : m2)) return -20;
+    return parfb_general<R>(side, trans, direct, storev, m2, n2, k, l, A1, lda1, A2, lda2, V, ldv, T, ldt, work,
+                            ldwork, st);
+  }
   return rc(launch_apply<R>(1, side, trans, m2, n2, k, k, A2, lda2, A1, lda1, V, ldv, T, ldt, st,
                             l > 0 ? mv - l : -1));
 }
@@ -353,13 +357,13 @@ extern "C" {
   int tqr_##P##parfb(char side, char trans, char direct, char storev, int m1, int n1, int m2,        \
                      int n2, int k, int l, CT *A1, int lda1, CT *A2, int lda2, const CT *V,          \
                      int ldv, const CT *T, int ldt, CT *work, int ldwork, cudaStream_t stream) {     \
-    (void)work; (void)ldwork;                                                                        \
     if (!al<R>(A1)) return -11;                                                                      \
     if (!al<R>(A2)) return -13;                                                                      \
     if (!al<R>(V)) return -15;                                                                       \
     if (!al<R>(T)) return -17;                                                                       \
+    if (!al<R>(work)) return -19;                                                                    \
     return parfb_impl<R>(side, trans, direct, storev, m1, n1, m2, n2, k, l, dp<R>(A1), lda1,         \
-                         dp<R>(A2), lda2, dp<R>(V), ldv, dp<R>(T), ldt, stream);                     \
+                         dp<R>(A2), lda2, dp<R>(V), ldv, dp<R>(T), ldt, dp<R>(work), ldwork, stream); \
   }
 
 TQR_INSTANTIATE(d, double, double)

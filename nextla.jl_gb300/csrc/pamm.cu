@@ -153,6 +153,82 @@ int pamm_impl(char op, char side, char storev, char direct, int m, int n, int k,
   return 0;
 }
 
+// W := M W (side L, W k x cnt) or W M (side R, W cnt x k), M = tfun(T's upper
+// ('F') or lower ('B') triangle), in place: one thread per W column (row),
+// walking the outputs in the order that reads only entries not yet rewritten.
+template <typename E>
+__global__ void __launch_bounds__(TQR_THREADS)
+k_parfb_tmul(int left, int upper, int adj, int k, int cnt, const E *__restrict__ T, int ldt, E *__restrict__ W,
+             int ldw)
+{
+  const int x = blockIdx.x * TQR_THREADS + threadIdx.x;
+  if (x >= cnt) return;
+  auto m = [&](int i, int j) -> E {            // M[i, j]
+    const int r = adj ? j : i, c = adj ? i : j;
+    if (upper ? r > c : r < c) return E(0);
+    return conj_if(T[ix(r, c, ldt)], adj != 0);
+  };
+  auto w = [&](int i) -> E & { return left ? W[ix(i, x, ldw)] : W[ix(x, i, ldw)]; };
+  // effective triangle of M: upper when (upper, no adjoint) or (lower, adjoint)
+  const bool mup = (upper != 0) != (adj != 0);
+  // left: out[i] = sum_j M[i,j] w[j]; M upper -> reads j >= i -> ascending i.
+  // right: out[j] = sum_i w[i] M[i,j]; M upper -> reads i <= j -> descending j.
+  const bool ascend = left ? mup : !mup;
+  for (int s = 0; s < k; ++s) {
+    const int i = ascend ? s : k - 1 - s;
+    // only the triangle's entries: the rest of w is already rewritten
+    const bool hi = left ? mup : !mup;          // the nonzero j lie at or above i
+    const int j0 = hi ? i : 0, j1 = hi ? k : i + 1;
+    E acc = 0;
+    if (left) {
+      for (int j = j0; j < j1; ++j) acc = mad(m(i, j), w(j), acc);
+    } else {
+      for (int j = j0; j < j1; ++j) acc = mad(w(j), m(j, i), acc);
+    }
+    w(i) = acc;
+  }
+}
+
+template <typename E>
+__global__ void __launch_bounds__(TQR_THREADS)
+k_sub_block(int rows, int cols, E *__restrict__ A, int lda, const E *__restrict__ W, int ldw)
+{
+  const long long id = (long long)blockIdx.x * TQR_THREADS + threadIdx.x;
+  if (id >= (long long)rows * cols) return;
+  const int r = (int)(id % rows), c = (int)(id / rows);
+  A[ix(r, c, lda)] = A[ix(r, c, lda)] - W[ix(r, c, ldw)];
+}
+
+template <typename E>
+int parfb_general(char side, char trans, char direct, char storev, int m2, int n2, int k, int l, E *A1, int lda1,
+                  E *A2, int lda2, const E *V, int ldv, const E *T, int ldt, E *W, int ldw, cudaStream_t st) {
+  const bool left = side == 'L';
+  int rc = pamm_impl<E>('W', side, storev, direct, m2, n2, k, l, A1, lda1, A2, lda2, V, ldv, W, ldw, st);
+  if (rc) return rc;
+  const int cnt = left ? n2 : m2;
+  k_parfb_tmul<E><<<(cnt + TQR_THREADS - 1) / TQR_THREADS, TQR_THREADS, 0, st>>>(
+      left ? 1 : 0, direct == 'F' ? 1 : 0, trans != 'N' ? 1 : 0, k, cnt, T, ldt, W, ldw);
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return (int)e;
+  const int rows = left ? k : m2, cols = left ? n2 : k;
+  const long long nt = (long long)rows * cols;
+  k_sub_block<E><<<(unsigned)((nt + TQR_THREADS - 1) / TQR_THREADS), TQR_THREADS, 0, st>>>(rows, cols, A1, lda1, W,
+                                                                                          ldw);
+  count_launch();
+  if ((e = cudaGetLastError()) != cudaSuccess) return (int)e;
+  return pamm_impl<E>('A', side, storev, direct, m2, n2, k, l, A1, lda1, A2, lda2, V, ldv, W, ldw, st);
+}
+
+#define TQR_PARFB_INST(E)                                                                                     \
+  template int parfb_general<E>(char, char, char, char, int, int, int, int, E *, int, E *, int, const E *, int, \
+                                const E *, int, E *, int, cudaStream_t);
+TQR_PARFB_INST(double)
+TQR_PARFB_INST(float)
+TQR_PARFB_INST(cx<double>)
+TQR_PARFB_INST(cx<float>)
+#undef TQR_PARFB_INST
+
 }  // namespace tqr
 
 using namespace tqr;

@@ -53,4 +53,11 @@ cudaError_t launch_apply(int mode, char side, char trans, int m, int n, int k, i
                          int ldc, R *A1, int lda1, const R *V, int ldv, const R *T, int ldt,
                          cudaStream_t st, int tt = -1);
 
+// parfb! in the forms the fused apply does not cover (direct 'B' or storev
+// 'R', pamm.cu): pamm 'W' into the caller's work W, the T product, A1 -= W,
+// pamm 'A' (src/parfb.jl:121-189).
+template <typename R>
+int parfb_general(char side, char trans, char direct, char storev, int m2, int n2, int k, int l, R *A1, int lda1,
+                  R *A2, int lda2, const R *V, int ldv, const R *T, int ldt, R *W, int ldw, cudaStream_t st);
+
 }  // namespace tqr

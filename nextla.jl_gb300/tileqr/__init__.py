@@ -294,8 +294,15 @@ def parfb(*args):
     p2, ld2 = _mat(A2)
     pv, ldv = _mat(V)
     pt, ldt = _mat(T)
+    pw, ldw = None, 1
+    if _ch(direct) != b"F" or _ch(storev) != b"C":
+        # backward or rowwise forms run through pamm! and need the work block
+        # (k x n2 for side 'L', m2 x k for 'R'), as the reference's parfb! does
+        if work is None or work.dim() != 2:
+            work = zeros(*((k, n2) if _ch(side) == b"L" else (m2, k)), dtype=A1.dtype, device=A1.device)
+        pw, ldw = _mat(work)
     _call(_prefix(A1, A2, V, T), "parfb", _ch(side), _ch(trans), _ch(direct), _ch(storev),
-          m1, n1, m2, n2, k, l, p1, ld1, p2, ld2, pv, ldv, pt, ldt, None, 1)
+          m1, n1, m2, n2, k, l, p1, ld1, p2, ld2, pv, ldv, pt, ldt, pw, ldw)
 
 
 def pamm(op, side, storev, direct, m, n, k, l, A1, A2, V, W):

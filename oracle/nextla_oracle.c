@@ -1117,3 +1117,54 @@ int ora_dpamm(char op, char side, char storev, char direct, int m, int n, int k,
 #undef VE
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* parfb in every direct / storev form (src/parfb.jl:44-191): pamm 'W',     */
+/* W := tfun(T) W (side L) or W tfun(T) (R) with T's upper ('F') or lower    */
+/* ('B') triangle and tfun the adjoint for trans != 'N' (parfb.jl:95-99,     */
+/* 121-189), A1 -= W, pamm 'A'.  W is the caller's work (k x n2 for side L,  */
+/* m2 x k for R).                                                            */
+/* ------------------------------------------------------------------------ */
+int ora_dparfb_full(char side, char trans, char direct, char storev, int m1, int n1, int m2, int n2,
+                    int k, int l, double *A1, int lda1, double *A2, int lda2, const double *V, int ldv,
+                    const double *T, int ldt, double *W, int ldw)
+{
+    if (side != 'L' && side != 'R') return -1;
+    if (trans != 'N' && trans != 'C' && trans != 'T') return -2;
+    if (direct != 'F' && direct != 'B') return -3;
+    if (storev != 'C' && storev != 'R') return -4;
+    if (m1 < 0) return -5;
+    if (n1 < 0) return -6;
+    if (m2 < 0 || (side == 'R' && m1 != m2)) return -7;
+    if (n2 < 0 || (side == 'L' && n1 != n2)) return -8;
+    if (k < 0) return -9;
+    if (l < 0 || l > k) return -10;
+    if (m1 == 0 || n1 == 0 || n2 == 0 || k == 0 || m2 == 0) return 0;
+    int L = (side == 'L'), up = (direct == 'F'), adj = (trans != 'N');
+    int rc = ora_dpamm('W', side, storev, direct, m2, n2, k, l, A1, lda1, A2, lda2, V, ldv, W, ldw);
+    if (rc) return rc;
+    /* M = tfun(triangle of T); left: W = M W, right: W = W M */
+#define TRI(i, j) ((up ? (i) <= (j) : (i) >= (j)) ? T[IDX(i, j, ldt)] : 0.0)
+#define M(i, j) (adj ? TRI(j, i) : TRI(i, j))
+    int cnt = L ? n2 : m2;
+    double *tmp = (double *)malloc(sizeof(double) * (size_t)k);
+    for (int x = 0; x < cnt; ++x) {
+        for (int i = 0; i < k; ++i) {
+            double acc = 0.0;
+            for (int j = 0; j < k; ++j)
+                acc += L ? M(i, j) * W[IDX(j, x, ldw)] : W[IDX(x, j, ldw)] * M(j, i);
+            tmp[i] = acc;
+        }
+        for (int i = 0; i < k; ++i) {
+            if (L) W[IDX(i, x, ldw)] = tmp[i]; else W[IDX(x, i, ldw)] = tmp[i];
+        }
+    }
+    free(tmp);
+#undef TRI
+#undef M
+    for (int x = 0; x < cnt; ++x)
+        for (int i = 0; i < k; ++i) {
+            if (L) A1[IDX(i, x, lda1)] -= W[IDX(i, x, ldw)]; else A1[IDX(x, i, lda1)] -= W[IDX(x, i, ldw)];
+        }
+    return ora_dpamm('A', side, storev, direct, m2, n2, k, l, A1, lda1, A2, lda2, V, ldv, W, ldw);
+}

@@ -857,3 +857,48 @@ int ora_zpamm(char op, char side, char storev, char direct, int m, int n, int k,
 #undef VE
     return 0;
 }
+
+/* parfb in every direct / storev form for complex elements: the sequence of */
+/* ora_dparfb_full (nextla_oracle.c) with the adjoint conjugating T.         */
+int ora_zparfb_full(char side, char trans, char direct, char storev, int m1, int n1, int m2, int n2,
+                    int k, int l, zc *A1, int lda1, zc *A2, int lda2, const zc *V, int ldv,
+                    const zc *T, int ldt, zc *W, int ldw)
+{
+    if (side != 'L' && side != 'R') return -1;
+    if (trans != 'N' && trans != 'C' && trans != 'T') return -2;
+    if (direct != 'F' && direct != 'B') return -3;
+    if (storev != 'C' && storev != 'R') return -4;
+    if (m1 < 0) return -5;
+    if (n1 < 0) return -6;
+    if (m2 < 0 || (side == 'R' && m1 != m2)) return -7;
+    if (n2 < 0 || (side == 'L' && n1 != n2)) return -8;
+    if (k < 0) return -9;
+    if (l < 0 || l > k) return -10;
+    if (m1 == 0 || n1 == 0 || n2 == 0 || k == 0 || m2 == 0) return 0;
+    int L = (side == 'L'), up = (direct == 'F'), adj = (trans != 'N');
+    int rc = ora_zpamm('W', side, storev, direct, m2, n2, k, l, A1, lda1, A2, lda2, V, ldv, W, ldw);
+    if (rc) return rc;
+#define TRI(i, j) ((up ? (i) <= (j) : (i) >= (j)) ? T[IDX(i, j, ldt)] : (zc)0.0)
+#define M(i, j) (adj ? conj(TRI(j, i)) : TRI(i, j))
+    int cnt = L ? n2 : m2;
+    zc *tmp = (zc *)malloc(sizeof(zc) * (size_t)k);
+    for (int x = 0; x < cnt; ++x) {
+        for (int i = 0; i < k; ++i) {
+            zc acc = 0.0;
+            for (int j = 0; j < k; ++j)
+                acc += L ? zmul(M(i, j), W[IDX(j, x, ldw)]) : zmul(W[IDX(x, j, ldw)], M(j, i));
+            tmp[i] = acc;
+        }
+        for (int i = 0; i < k; ++i) {
+            if (L) W[IDX(i, x, ldw)] = tmp[i]; else W[IDX(x, i, ldw)] = tmp[i];
+        }
+    }
+    free(tmp);
+#undef TRI
+#undef M
+    for (int x = 0; x < cnt; ++x)
+        for (int i = 0; i < k; ++i) {
+            if (L) A1[IDX(i, x, lda1)] -= W[IDX(i, x, ldw)]; else A1[IDX(x, i, lda1)] -= W[IDX(x, i, ldw)];
+        }
+    return ora_zpamm('A', side, storev, direct, m2, n2, k, l, A1, lda1, A2, lda2, V, ldv, W, ldw);
+}

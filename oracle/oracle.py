@@ -71,10 +71,11 @@ def _declare(L):
         "ora_dtile_unmqr_tree": [_C, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _P, _I],
         "ora_dtile_geqrf_hqr": [_I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _P],
         "ora_dpamm": [_C, _C, _C, _C, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I],
+        "ora_dparfb_full": [_C, _C, _C, _C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, _I],
         "ora_dtile_unmqr_hqr": [_C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _P, _I],
     }
     for name in ("geqr2", "larft", "larfb", "geqrt", "unmqr", "parfb", "parfb_l", "tsmqr", "tsqrt", "ttqrt",
-                 "ttmqr", "tile_geqrf", "tile_unmqr", "trsm_lun", "pamm"):
+                 "ttmqr", "tile_geqrf", "tile_unmqr", "trsm_lun", "pamm", "parfb_full"):
         sig["ora_z" + name] = sig["ora_d" + name]
     for name, args in sig.items():
         f = getattr(L, name)
@@ -273,6 +274,19 @@ def pamm(op, side, storev, direct, m, n, k, l, A1, A2, V, W):
     pw, ldw = _mat(W)
     return _check(_fn("pamm", A1, A2, V, W)(_ch(op), _ch(side), _ch(storev), _ch(direct), m, n, k, l, p1, ld1,
                                             p2, ld2, pv, ldv, pw, ldw), "pamm")
+
+
+def parfb_full(side, trans, direct, storev, m1, n1, m2, n2, k, l, A1, A2, V, T, W):
+    """parfb! in every direct / storev form (src/parfb.jl:44-191); W is work
+    (k x n2 for side 'L', m2 x k for 'R')."""
+    p1, ld1 = _mat(A1)
+    p2, ld2 = _mat(A2)
+    pv, ldv = _mat(V)
+    pt, ldt = _mat(T)
+    pw, ldw = _mat(W)
+    return _check(_fn("parfb_full", A1, A2, V, T, W)(_ch(side), _ch(trans), _ch(direct), _ch(storev), m1, n1, m2,
+                                                      n2, k, l, p1, ld1, p2, ld2, pv, ldv, pt, ldt, pw, ldw),
+                  "parfb")
 
 
 def tile_geqrf_hqr(A, nb, ib, grp):

@@ -87,10 +87,14 @@ def test_larfb_larft_edge_cases(L):
     assert L.tqr_dlarft(b"F", b"C", 0, 2, NULL, 1, NULL, NULL, 2, NULL) == 0
 
 
-def test_parfb_unsupported_forms_are_reported(L):
+def test_parfb_argument_checks(L):
+    """Bad flags are argument errors; the backward and rowwise forms need the
+    work block (its position, -20, when it is missing); l > k is illegal."""
     a = (4, 6, 4, 6, 3, 0, NULL, 4, NULL, 4, NULL, 4, NULL, 3, NULL, 3, NULL)
-    assert L.tqr_dparfb(b"L", b"N", b"F", b"R", *a) == -4
-    assert L.tqr_dparfb(b"L", b"N", b"B", b"C", *a) == -3
+    assert L.tqr_dparfb(b"L", b"N", b"X", b"C", *a) == -3
+    assert L.tqr_dparfb(b"L", b"N", b"F", b"X", *a) == -4
+    assert L.tqr_dparfb(b"L", b"N", b"F", b"R", *a) == -20
+    assert L.tqr_dparfb(b"L", b"N", b"B", b"C", *a) == -20
     assert L.tqr_dparfb(b"L", b"N", b"F", b"C", 4, 6, 4, 6, 3, 4, NULL, 4, NULL, 4, NULL, 4, NULL, 3,
                         NULL, 3, NULL) == -10   # l > k
 

@@ -127,3 +127,50 @@ def test_pamm_quick_return_and_errors(oracle):
                  ("W", "L", "C", "F", 10, 5, 5, 6)]:
         with pytest.raises(ValueError):
             oracle.pamm(*args, A1, A2, V, W)
+
+
+def explicit_tprfb(side, trans, direct, storev, k, l, V, T, A1, A2):
+    """[A1; A2] := op(H) [A1; A2] (side L) or [A1 A2] op(H) (R) with the
+    pentagonal block reflector H = I - Vf T Vf^H (columnwise: Vf = [I; Ve]) or
+    I - Vf^H T Vf (rowwise: Vf = [I Ve^T]), T's upper ('F') or lower ('B')
+    triangle, V's trapezoid of order l -- LAPACK's tprfb, which the reference
+    tests parfb! against (test/parfb.jl:44-51)."""
+    L = side == "L"
+    mv = A2.shape[0] if L else A2.shape[1]
+    Ve = masked_ve(V, storev, direct, mv, k, l)
+    Tt = np.triu(T[:k, :k]) if direct == "F" else np.tril(T[:k, :k])
+    Vc = np.vstack([np.eye(k, dtype=Ve.dtype), Ve])           # columnwise reflectors
+    if storev == "C":
+        H = np.eye(k + mv, dtype=Ve.dtype) - Vc @ Tt @ Vc.conj().T
+    else:
+        Vr = Vc.T                                               # rows [I V]: V is stored rowwise
+        H = np.eye(k + mv, dtype=Ve.dtype) - Vr.conj().T @ Tt @ Vr
+    op = H if trans == "N" else H.conj().T
+    if L:
+        X = op @ np.vstack([A1[:k], A2])
+        return X[:k], X[k:]
+    X = np.hstack([A1[:, :k], A2]) @ op
+    return X[:, :k], X[:, k:]
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+@pytest.mark.parametrize("side", "LR")
+@pytest.mark.parametrize("trans", "NC")
+@pytest.mark.parametrize("direct", "FB")
+@pytest.mark.parametrize("storev", "CR")
+def test_parfb_every_form_vs_explicit_reflector(oracle, dt, side, trans, direct, storev):
+    """test/parfb.jl's shapes (m2, n2, k, l = 20, 24, 8, 4, T = rand(k, k))."""
+    rng = np.random.default_rng(hash((side, trans, direct, storev)) % 2**32)
+    cplx = np.iscomplexobj(np.zeros(1, dt))
+    R = lambda *s: F(rng.random(s) + (1j * rng.random(s) if cplx else 0), dt)
+    m2, n2, k, l = 20, 24, 8, 4
+    m1, n1 = (k, n2) if side == "L" else (m2, k)
+    A1, A2 = R(m1, n1), R(m2, n2)
+    mv = m2 if side == "L" else n2
+    V = R(mv, k) if storev == "C" else R(k, mv)
+    T = R(k, k)
+    W = np.zeros((k, n2) if side == "L" else (m2, k), dt, order="F")
+    X1, X2 = explicit_tprfb(side, trans, direct, storev, k, l, V, T, A1, A2)
+    oracle.parfb_full(side, trans, direct, storev, m1, n1, m2, n2, k, l, A1, A2, V, T, W)
+    assert np.abs(A1 - X1).max() <= 1e-12 * np.abs(X1).max()
+    assert np.abs(A2 - X2).max() <= 1e-12 * np.abs(X2).max()
