@@ -533,6 +533,39 @@ def batched_sharded_bench(torch, nprob, world, rank, steps=5, warmup=3):
             "rejected_descriptors_rank0": bad[0], "scaling": "strong (fixed batch)"}
 
 
+def adjoint_sharded_bench(torch, world, rank, batch=256, m=2048, n=256, steps=3, warmup=3):
+    """The differentiable-QR batch split across the ranks (equal problems:
+    tileqr.batched.shard gives each rank batch/world of them); forward and
+    adjoint kernels with seeded cotangents, time = max over ranks."""
+    import numpy as np
+    from tileqr import autodiff as AD
+    from tileqr import batched as Bt
+    ones = np.ones(batch, dtype=np.int32)
+    mine = Bt.shard(ones * m, ones * n, ones, world, rank)
+    g = torch.Generator(device="cuda").manual_seed(SEED + rank)
+    A = torch.randn((batch, m, n), generator=g, dtype=torch.float64, device="cuda")[torch.as_tensor(mine)]
+    dQ = torch.randn((len(mine), m, n), generator=g, dtype=torch.float64, device="cuda")
+    dR = torch.triu(torch.randn((len(mine), n, n), generator=g, dtype=torch.float64, device="cuda"))
+    st = torch.cuda.current_stream()
+    total = 0.0
+    for rep in range(warmup + steps):
+        torch.cuda.synchronize()
+        barrier(world)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        Q, R, F, tau = AD.qr_forward(A)
+        AD.qr_backward(F, tau, dQ, dR)
+        e1.record(st)
+        torch.cuda.synchronize()
+        t = reduce_max(e0.elapsed_time(e1), world)
+        if rep >= warmup:
+            total += t
+    ms = total / steps
+    return {"workload": f"differentiable QR forward + adjoint kernels, {batch} Float64 {m}x{n} problems split over "
+                        f"{world} ranks", "problems_per_s": batch / (ms / 1e3), "ms_per_step": ms,
+            "rank0_problems": int(len(mine)), "scaling": "strong (fixed batch)"}
+
+
 def tall_bench(tq, torch, m=65536, n=512, steps=3, warmup=2, peak=None, dtype="f64"):
     """Tall-skinny tile QR (m x n, N(0,1), nb = 256, ib = 32): the flat-tree
     persistent kernel against the binary-tree driver (geqrt on every tile,
@@ -1092,6 +1125,9 @@ def main():
     sharded = None
     if world > 1 and not args.no_batched:
         sharded = batched_sharded_bench(torch, args.batched_n, world, rank)
+    adj_sharded = None
+    if world > 1 and not args.no_adjoint:
+        adj_sharded = adjoint_sharded_bench(torch, world, rank)
 
     cplx = None
     if rank == 0 and world == 1 and not args.no_complex:
@@ -1115,6 +1151,7 @@ def main():
             "least_squares_mixed_vs_fp64": ls,
             "batched_uneven_gels": bat,
             "batched_uneven_gels_sharded": sharded,
+            "differentiable_qr_sharded": adj_sharded,
             "differentiable_qr": adj,
             "tall_skinny_65536x512": tall,
             "complex_tile_qr": cplx,

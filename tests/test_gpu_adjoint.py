@@ -152,3 +152,17 @@ def test_full_configuration_256_x_2048x256(tq, oracle):
         fd = (loss_torch(Qp, Rp, b, y, dQ, dR, torch) - loss_torch(Qm, Rm, b, y, dQ, dR, torch)).item() / (2 * h)
     an = (G * E).sum().item()
     assert abs(fd - an) <= 1e-6 * max(1.0, abs(an)), (fd, an)
+
+
+def test_sharded_adjoint_one_rank():
+    """The multi-rank differentiable-QR measurement with a single rank."""
+    import os
+    import sys
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    import bench
+    r = bench.adjoint_sharded_bench(torch, 1, 0, batch=8, m=512, n=64, steps=1, warmup=1)
+    assert r["rank0_problems"] == 8 and r["problems_per_s"] > 0
