@@ -3,7 +3,7 @@
 Multi-GPU runs of this path are replicas: each rank factors its own matrix and
 the only cross-rank operations are the timing barrier and a MAX reduction of
 the elapsed time.  Those helpers are checked here with two gloo ranks, and the
-reference arm is launched the way the driver launches it (torchrun, 2 ranks):
+reference arm is launched as a multi-GPU bench run launches it (torchrun, 2 ranks):
 rank 0 prints the one JSON line, rank 1 exits 0 without work.
 """
 import json
