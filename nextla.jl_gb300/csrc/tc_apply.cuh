@@ -6,7 +6,8 @@
 //   W^T  = A2^T V_b              GEMM1: M = 128 (chunk columns), N = 32, K = m2
 //   W    = T_b^T (A1_b + W)      SIMT on the TMEM read-back (32 x 32 triangle)
 //   A1_b = A1_b - W
-//   A2   = A2 - V_b W            GEMM2: M = m2 (two 128-row halves), N = 128, K = 32
+//   D2   = W^T V_b^T             GEMM2: M = 128, N = 128 per half of A2's rows
+//   A2^T = A2^T - D2             SIMT, IEEE FP32, on A2^T kept in TMEM
 //
 // Both GEMMs run as tcgen05.mma kind::tf32 with FP32 accumulators in TMEM,
 // issued by one thread and completed through an mbarrier; every operand is
@@ -32,13 +33,23 @@ namespace tc {
 constexpr int kChunk = 128;            // chunk columns (GEMM1 M, GEMM2 N)
 constexpr int kIb = 32;                // reflectors per block (GEMM1 N, GEMM2 K)
 constexpr int kKc = 64;                // GEMM1 K chunk (rows of A2 staged at once)
-constexpr int kTmemCols = 512;         // D1: columns [0, 32); D2 halves: [128, 256) and [256, 384)
+// TMEM columns: A2^T in [128, 128 + m2); D2 of A2's rows [0, 128) in [0, 128)
+// (D1, in [0, 32), is consumed before GEMM2 overwrites it) and of rows
+// [128, 256) in [384, 512)
+constexpr int kTmemCols = 512;
+constexpr uint32_t kA2Col = 128;
+__device__ __forceinline__ uint32_t d2col(int r) { return r < 128 ? (uint32_t)r : (uint32_t)(256 + r); }
 // dynamic shared memory: two GEMM1 stage buffers, each A hi/lo (2 x 32 KB) and
-// B hi/lo (2 x 8 KB); GEMM2 reuses them (V_b hi/lo in stage 0's A, W hi/lo
-// in stage 1's A); then the T block (32 x 33 floats)
+// B hi/lo (2 x 8 KB); GEMM2 reuses them (V_b^T hi/lo in stage 0's A, W^T
+// hi/lo in stage 1's A); then the raw V_b and the T block (32 x 33 floats)
 constexpr size_t kBufA = 32768, kBufB = 8192;
 constexpr size_t kStage = 2 * kBufA + 2 * kBufB;
-constexpr size_t kSmem = 2 * kStage + sizeof(float) * 32 * 33 + 1024;
+// the raw FP32 V_b (32 columns of up to 256 rows, column stride 260: the 16
+// extra bytes make both operand builds from it bank-conflict free), fetched
+// with cp.async one block ahead
+constexpr int kVrawLd = 260;
+constexpr size_t kVraw = sizeof(float) * 32 * kVrawLd;
+constexpr size_t kSmem = 2 * kStage + kVraw + sizeof(float) * 32 * 33 + 1024;
 constexpr int kBars = 3;               // GEMM1 stage 0, GEMM1 stage 1, GEMM2
 constexpr long kWaitLimit = 1L << 26;  // mbarrier polls before giving up
 
@@ -187,6 +198,59 @@ __device__ __forceinline__ void stage_kmajor(const float *src, int ld, int r0, u
   }
 }
 
+// 32 consecutive TMEM columns of this warp's lane quarter <- v (one column per
+// register); the caller waits (wait_st) before the values are read.
+__device__ __forceinline__ void st16(uint32_t taddr, const float (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
+      ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+        "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+        "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
+        "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+        "r"(__float_as_uint(v[15]))
+      : "memory");
+}
+
+__device__ __forceinline__ void wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// TMEM writes of every thread -> visible to every thread and to the MMAs.
+__device__ __forceinline__ void tmem_sync() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// V_b (m2 x 32, column-major, 16-byte aligned, ldv a multiple of 4) ->
+// Vraw (column stride kVrawLd) by 16-byte cp.async copies; one commit group.
+__device__ __forceinline__ void prefetch_vb(const float *Vb, int ldv, int m2, float *Vraw) {
+  const int per_col = m2 / 4;
+  for (int idx = threadIdx.x; idx < kIb * per_col; idx += TQR_THREADS) {
+    const int p = idx / per_col, r4 = idx % per_col;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr(Vraw + p * kVrawLd + 4 * r4)),
+                 "l"(Vb + (size_t)p * ldv + 4 * r4)
+                 : "memory");
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ void prefetch_wait() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// GEMM1's B operand for rows [r0, r0 + kKc) from Vraw: row-of-operand p, K =
+// r.  Lanes take 8 p by 4 K runs, so the 16-byte reads (column stride
+// kVrawLd) and the core-matrix stores each spread over all banks.
+__device__ __forceinline__ void stage_vb1(const float *Vraw, int r0, unsigned char *hi, unsigned char *lo) {
+  constexpr uint32_t SB = (kKc / 4) * 128;
+#pragma unroll
+  for (int u = 0; u < kIb * kKc / 4 / TQR_THREADS; ++u) {
+    const int idx = threadIdx.x + u * TQR_THREADS;
+    const int rest = idx >> 5;
+    const int p = 8 * (rest & 3) + (idx & 7), k4 = 4 * (rest >> 2) + ((idx >> 3) & 3);
+    const float4 x = *reinterpret_cast<const float4 *>(Vraw + p * kVrawLd + r0 + 4 * k4);
+    put_split4(hi, lo, kmaj(p, 4 * k4, SB), x);
+  }
+}
+
 // [A1; A2] := Q^T [A1; A2] for the 128 columns at A1, A2 (column-major):
 // A1 rows [0, k), A2 m2 rows (m2 = 128 or 256), V m2 x k, T 32 x k (blocks of
 // 32 columns), k a multiple of 32; A2, V 16-byte aligned with leading
@@ -194,29 +258,108 @@ __device__ __forceinline__ void stage_kmajor(const float *src, int ld, int r0, u
 // tmem; bars[kBars] mbarriers (count 1) with parities phase[kBars].  Returns
 // false if an MMA completion wait timed out (the caller then waits once more
 // on every barrier with a pending phase before releasing TMEM).
+//
+// A2 stays in TMEM for the whole chunk, transposed: TMEM lane c (the chunk
+// column) holds A2[0:m2, c] in columns [kA2Col, kA2Col + m2).  So GEMM2 is
+// taken transposed, D2 = W^T V_b^T (M = 128 columns, N = 128 rows per half,
+// K = 32), and GEMM1's K-major operand A2^T (row c, K = r) is read back from
+// TMEM one lane per thread: 16 consecutive r of one c are four 16-byte K
+// runs, stored without any transpose.  The subtraction A2^T -= D2 is fused
+// into the next block's staging pass (and into the final write-back) and runs
+// on the FP32 pipe: the tensor core's own accumulation is not IEEE
+// round-to-nearest, so accumulating A2 through it, block after block and tile
+// after tile, lets its rounding drift build up; D2 starts from zero every
+// block, as the product alone.  A2 moves through global memory once per chunk
+// (in at the start, out at the end) instead of twice per block.
 __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2, int lda2, const float *V, int ldv,
                                    const float *T, int ldt, uint32_t tmem, uint64_t *bars, uint32_t *phase,
                                    unsigned char *smem) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // warps w and w + 4 reach TMEM lanes [32 (w % 4), 32 (w % 4) + 32): this
+  // thread's lane is chunk column c; the two warp sets split A2's rows
+  const int c = (warp & 3) * 32 + lane, wset = warp >> 2;
+  const uint32_t d2t = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+  const uint32_t a2t = d2t + kA2Col;
   unsigned char *st_base[2] = {smem, smem + kStage};
-  float *Ts = reinterpret_cast<float *>(smem + 2 * kStage);     // 32 x 33
+  float *Vraw = reinterpret_cast<float *>(smem + 2 * kStage);              // 32 x kVrawLd
+  float *Ts = reinterpret_cast<float *>(smem + 2 * kStage + kVraw);        // 32 x 33
   // GEMM2 operands in the stage buffers' A regions
-  unsigned char *vHi = smem, *vLo = smem + kBufA;                 // V_b: 256 x 32, K-major
-  unsigned char *wHi = smem + kStage, *wLo = smem + kStage + kBufA;  // W: 128 x 32, K-major
-  const uint32_t id1 = idesc_tf32(128, kIb), id2 = idesc_tf32(128, kChunk);
+  unsigned char *vHi = smem, *vLo = smem + kBufA;                    // V_b^T: m2 x 32, K-major (B)
+  unsigned char *wHi = smem + kStage, *wLo = smem + kStage + kBufA;  // -W^T: 128 x 32, K-major (A)
+  const uint32_t id1 = idesc_tf32(128, kIb), id2 = idesc_tf32(128, 128);
   const uint32_t d1 = tmem;
-  const int nh = m2 / 128, nq = m2 / kKc;
+  const int nq = m2 / kKc, half = m2 / 2;
   constexpr uint32_t SB = (kKc / 4) * 128;
+  if (k >= kIb) prefetch_vb(V, ldv, m2, Vraw);
+  // ---- A2^T into TMEM: thread c reads its column (16-byte runs along r) ----
+  {
+    const float *src = A2 + (size_t)c * lda2;
+#pragma unroll 1
+    for (int r0 = wset * half; r0 < (wset + 1) * half; r0 += 32) {
+      float4 x[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) x[u] = __ldcg(reinterpret_cast<const float4 *>(src + r0 + 4 * u));
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        float v[16];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          v[4 * u] = x[4 * g + u].x; v[4 * u + 1] = x[4 * g + u].y;
+          v[4 * u + 2] = x[4 * g + u].z; v[4 * u + 3] = x[4 * g + u].w;
+        }
+        st16(a2t + (uint32_t)(r0 + 16 * g), v);
+      }
+    }
+    wait_st();
+  }
+  tmem_sync();
   for (int b = 0; b < k / kIb; ++b) {
-    const float *Vb = V + (size_t)b * kIb * ldv;
-    // ---- GEMM1: D1[c][p] = sum_r A2[r][c] V_b[r][p], K chunks of 64 rows,
+    // this block's T (upper triangle) and A1 rows, fetched now and used after GEMM1
+    float tv[kIb * kIb / TQR_THREADS];
+#pragma unroll
+    for (int u = 0; u < kIb * kIb / TQR_THREADS; ++u) {
+      const int idx = tid + u * TQR_THREADS, r = idx % kIb, cc = idx / kIb;
+      tv[u] = (r <= cc) ? __ldcg(T + (size_t)r + (size_t)(b * kIb + cc) * ldt) : 0.0f;
+    }
+    float *a1 = A1 + (size_t)b * kIb + (size_t)c * lda1;
+    float a1v[kIb];
+    if (warp < 4) {
+#pragma unroll
+      for (int p = 0; p < kIb; ++p) a1v[p] = __ldcg(a1 + p);
+    }
+    prefetch_wait();
+    __syncthreads();   // V_b in Vraw
+    // ---- GEMM1: D1[c][p] = sum_r A2^T[c][r] V_b[r][p], K chunks of 64 rows,
     //      staging of chunk q + 1 overlapping the MMAs of chunk q ----
     for (int q = 0; q < nq; ++q) {
       const int sbuf = q & 1;
-      if (q >= 2 && !wait_phase(&bars[sbuf], &phase[sbuf])) return false;   // chunk q - 2 done with it
+      if (q >= 2 && !wait_phase(&bars[sbuf], &phase[sbuf])) {   // chunk q - 2 done with it
+        prefetch_wait();
+        return false;
+      }
       unsigned char *aHi = st_base[sbuf], *aLo = aHi + kBufA, *bHi = aHi + 2 * kBufA, *bLo = bHi + kBufB;
-      stage_kmajor<kChunk, kKc>(A2, lda2, q * kKc, aHi, aLo);
-      stage_kmajor<kIb, kKc>(Vb, ldv, q * kKc, bHi, bLo);
+      // A operand from TMEM: warp set s takes rows [32 s, 32 s + 32) of the
+      // chunk, first finishing the previous block's A2^T -= D2 on them (chunk
+      // 0's D2 columns are read before this block's GEMM1 overwrites D1)
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const int r = q * kKc + wset * 32 + g * 16;
+        float v[16];
+        ld16(a2t + (uint32_t)r, v);
+        if (b > 0) {
+          float d[16];
+          ld16(d2t + d2col(r), d);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] -= d[j];
+          st16(a2t + (uint32_t)r, v);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          put_split4(aHi, aLo, kmaj(c, r - q * kKc + 4 * u, SB),
+                     make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]));
+      }
+      if (b > 0) wait_st();
+      stage_vb1(Vraw, q * kKc, bHi, bLo);
       to_async_proxy();
       if (tid == 0) {
         for (int ks = 0; ks < kKc / 8; ++ks) {
@@ -233,21 +376,23 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
     }
     // the last two chunks' commits (one per stage buffer) are still pending
     for (int q = (nq >= 2 ? nq - 2 : 0); q < nq; ++q)
-      if (!wait_phase(&bars[q & 1], &phase[q & 1])) return false;
+      if (!wait_phase(&bars[q & 1], &phase[q & 1])) {
+        prefetch_wait();
+        return false;
+      }
     // T block (upper triangle) to shared memory
-    for (int idx = tid; idx < kIb * kIb; idx += TQR_THREADS) {
-      const int r = idx % kIb, c = idx / kIb;
-      Ts[r + c * 33] = (r <= c) ? __ldcg(T + (size_t)r + (size_t)(b * kIb + c) * ldt) : 0.0f;
+#pragma unroll
+    for (int u = 0; u < kIb * kIb / TQR_THREADS; ++u) {
+      const int idx = tid + u * TQR_THREADS, r = idx % kIb, cc = idx / kIb;
+      Ts[r + cc * 33] = tv[u];
     }
     __syncthreads();
-    // ---- W = T^T (A1_b + D1^T); A1_b -= W; W (split) -> B operand of GEMM2 ----
     if (warp < 4) {
-      const int c = warp * 32 + lane;
+      // ---- W = T^T (A1_b + D1^T); A1_b -= W; W (split) -> A operand of GEMM2 ----
       float w[32];
       ld32(d1 + ((uint32_t)(warp * 32) << 16), w);
-      float *a1 = A1 + (size_t)b * kIb + (size_t)c * lda1;
 #pragma unroll
-      for (int p = 0; p < 32; ++p) w[p] += __ldcg(a1 + p);
+      for (int p = 0; p < 32; ++p) w[p] += a1v[p];
       // W := T^T W in place, last row first (row p reads rows q <= p, not yet overwritten)
 #pragma unroll
       for (int p = 31; p >= 0; --p) {
@@ -262,70 +407,61 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
       for (int p4 = 0; p4 < 8; ++p4)
         put_split4(wHi, wLo, kmaj(c, 4 * p4, (kIb / 4) * 128),
                    make_float4(w[4 * p4], w[4 * p4 + 1], w[4 * p4 + 2], w[4 * p4 + 3]));
-    }
-    // V_b as the A operand of GEMM2: row-of-operand = row r, K = p (strided in
-    // memory: four loads along r, four 4-byte stores)
-    {
-      constexpr int PER = 256 * kIb / 4 / TQR_THREADS;
-      float4 v[PER];
-#pragma unroll
-      for (int u = 0; u < PER; ++u) {
-        const int idx = tid + u * TQR_THREADS;
-        const int r4 = idx % 64, p = idx / 64;
-        v[u] = (4 * r4 < m2) ? __ldcg(reinterpret_cast<const float4 *>(Vb + (size_t)(4 * r4) + (size_t)p * ldv))
-                             : make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-#pragma unroll
-      for (int u = 0; u < PER; ++u) {
-        const int idx = tid + u * TQR_THREADS;
-        const int r4 = idx % 64, p = idx / 64;
-        if (4 * r4 < m2) {
-          put_split(vHi, vLo, kmaj(4 * r4 + 0, p, (kIb / 4) * 128), v[u].x);
-          put_split(vHi, vLo, kmaj(4 * r4 + 1, p, (kIb / 4) * 128), v[u].y);
-          put_split(vHi, vLo, kmaj(4 * r4 + 2, p, (kIb / 4) * 128), v[u].z);
-          put_split(vHi, vLo, kmaj(4 * r4 + 3, p, (kIb / 4) * 128), v[u].w);
-        }
+    } else {
+      // ---- meanwhile V_b^T as the B operand of GEMM2 from Vraw: row r, K = p;
+      //      four reads along p (consecutive r across the warp), one 16-byte store ----
+      const int t = tid - 128;
+#pragma unroll 4
+      for (int idx = t; idx < m2 * (kIb / 4); idx += 128) {
+        const int r = idx % m2, p4 = idx / m2;
+        const float *vp = Vraw + (4 * p4) * kVrawLd + r;
+        put_split4(vHi, vLo, kmaj(r, 4 * p4, (kIb / 4) * 128),
+                   make_float4(vp[0], vp[kVrawLd], vp[2 * kVrawLd], vp[3 * kVrawLd]));
       }
     }
     to_async_proxy();
-    // ---- GEMM2, both 128-row halves at once: D2_h[r][c] = sum_p V_b[128 h + r][p] W[p][c] ----
+    // Vraw is free: the next block's V_b flies during GEMM2
+    if (b + 1 < k / kIb) prefetch_vb(V + (size_t)(b + 1) * kIb * ldv, ldv, m2, Vraw);
+    // ---- GEMM2, both 128-row halves: D2[c][r] = sum_p W[p][c] V_b[r][p] ----
     const bool ok2 = run_mma([&] {
-      for (int h = 0; h < nh; ++h) {
-        const uint32_t ao = h * 128 * 128;   // 16 row groups x 1024 B per half
-        const uint32_t d2 = tmem + 128 + (uint32_t)h * 128;
+      for (int h = 0; h < m2 / 128; ++h) {
+        const uint32_t bo = h * 16 * 1024;   // 16 row groups of V_b^T per half
         for (int ks = 0; ks < kIb / 8; ++ks) {
           const uint32_t o = ks * 256;
-          const uint64_t ah = sdesc(saddr(vHi) + ao + o, 128, 1024), al = sdesc(saddr(vLo) + ao + o, 128, 1024);
-          const uint64_t bh = sdesc(saddr(wHi) + o, 128, 1024), bl = sdesc(saddr(wLo) + o, 128, 1024);
+          const uint64_t ah = sdesc(saddr(wHi) + o, 128, 1024), al = sdesc(saddr(wLo) + o, 128, 1024);
+          const uint64_t bh = sdesc(saddr(vHi) + bo + o, 128, 1024), bl = sdesc(saddr(vLo) + bo + o, 128, 1024);
+          const uint32_t d2 = tmem + d2col(128 * h);
           mma(d2, ah, bh, id2, ks == 0 ? 0u : 1u);
           mma(d2, ah, bl, id2, 1u);
           mma(d2, al, bh, id2, 1u);
         }
       }
     }, &bars[2], &phase[2]);
-    if (!ok2) return false;
-    // ---- A2 -= D2: warps 0-3 the first half, warps 4-7 the second ----
-    {
-      const int h = warp / 4, qtr = warp % 4;
-      if (h < nh) {
-        const int r = h * 128 + qtr * 32 + lane;
-        const uint32_t d2 = tmem + 128 + (uint32_t)h * 128 + ((uint32_t)(qtr * 32) << 16);
-#pragma unroll 1
-        for (int cc = 0; cc < kChunk / 16; ++cc) {
-          float v[16];
-          ld16(d2 + (uint32_t)cc * 16, v);
-          float old[16];
-#pragma unroll
-          for (int j = 0; j < 16; ++j) old[j] = __ldcg(A2 + (size_t)r + (size_t)(cc * 16 + j) * lda2);
-#pragma unroll
-          for (int j = 0; j < 16; ++j) A2[(size_t)r + (size_t)(cc * 16 + j) * lda2] = old[j] - v[j];
-        }
-      }
+    if (!ok2) {
+      prefetch_wait();   // no copy into shared memory outlives the routine
+      return false;
     }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   }
+  // ---- A2 = A2^T - D2 out of TMEM: thread c writes its column ----
+  {
+    float *dst = A2 + (size_t)c * lda2;
+#pragma unroll 1
+    for (int r0 = wset * half; r0 < (wset + 1) * half; r0 += 16) {
+      float v[16];
+      ld16(a2t + (uint32_t)r0, v);
+      if (k >= kIb) {   // the last block's D2 is pending
+        float d[16];
+        ld16(d2t + d2col(r0), d);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] -= d[j];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        *reinterpret_cast<float4 *>(dst + r0 + 4 * u) =
+            make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]);
+    }
+  }
+  tmem_sync();
   return true;
 }
 
