@@ -531,9 +531,11 @@ int tqr_sqr_batched_bwd(int batch, int m, int n, int ib, const float *F, const f
  * tsmqr!('L', 'C', ...) (src/tsmqr.jl:47-146, l = 0, ib = 32) on tcgen05
  * tensor cores: [A1; A2] := Q^T [A1; A2] with Q from a tsqrt! factor V
  * (m2-by-k) and T (32-by-k), A1 rows [0, k), m2 = 128 or 256, k a multiple of
- * 32, n a multiple of 128.  TF32 products split three ways (hi*hi + hi*lo +
- * lo*hi) with FP32 accumulation in TMEM: FP32-level accuracy.  *err (device)
- * is set to 1 if a tensor-core completion wait gave up. */
+ * 32, n a multiple of 128; A1, A2 and V 16-byte aligned with leading
+ * dimensions multiples of 4 (-6, -8 otherwise).  TF32 products split three
+ * ways (hi*hi + hi*lo + lo*hi) with FP32 accumulation in TMEM: FP32-level
+ * accuracy.  *err (device) is set to 1 if a tensor-core completion wait gave
+ * up. */
 int tqr_stsmqr_tc(int m1, int n, int m2, int k, float *A1, int lda1, float *A2, int lda2, const float *V,
                   int ldv, const float *T, int ldt, int *err, cudaStream_t stream);
 

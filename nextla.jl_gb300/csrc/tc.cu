@@ -70,7 +70,9 @@ int tqr_stsmqr_tc(int m1, int n, int m2, int k, float *A1, int lda1, float *A2, 
   if (!A2 || lda2 < m2) return -8;
   if (!V || ldv < m2) return -10;
   if (!T || ldt < tc::kIb) return -12;
-  if (((uintptr_t)A2 & 15) || (lda2 & 3) || ((uintptr_t)V & 15) || (ldv & 3)) return -8;   // float4 staging
+  // 16-byte copies and loads
+  if (((uintptr_t)A1 & 15) || (lda1 & 3)) return -6;
+  if (((uintptr_t)A2 & 15) || (lda2 & 3) || ((uintptr_t)V & 15) || (ldv & 3)) return -8;
   if (!err) return -13;
   // kernels that use TMEM run one CTA per SM: all of TMEM and shared memory
   const size_t sm = tc::kSmem;

@@ -41,15 +41,20 @@ constexpr uint32_t kA2Col = 128;
 __device__ __forceinline__ uint32_t d2col(int r) { return r < 128 ? (uint32_t)r : (uint32_t)(256 + r); }
 // dynamic shared memory: two GEMM1 stage buffers, each A hi/lo (2 x 32 KB) and
 // B hi/lo (2 x 8 KB); GEMM2 reuses them (V_b^T hi/lo in stage 0's A, W^T
-// hi/lo in stage 1's A); then the raw V_b and the T block (32 x 33 floats)
+// hi/lo in stage 1's A), and A2 passes through them (column stride kRawLd)
+// on its way into and out of TMEM; then the raw V_b and A1_b of the current
+// block (fetched with cp.async one block ahead) and the T block.  The raw
+// strides (260 and 36 floats) put consecutive columns 16 bytes apart modulo
+// 128, so a warp reading one 16-byte run per column, or 8 columns by 4 runs,
+// spreads over all banks.
 constexpr size_t kBufA = 32768, kBufB = 8192;
 constexpr size_t kStage = 2 * kBufA + 2 * kBufB;
-// the raw FP32 V_b (32 columns of up to 256 rows, column stride 260: the 16
-// extra bytes make both operand builds from it bank-conflict free), fetched
-// with cp.async one block ahead
-constexpr int kVrawLd = 260;
-constexpr size_t kVraw = sizeof(float) * 32 * kVrawLd;
-constexpr size_t kSmem = 2 * kStage + kVraw + sizeof(float) * 32 * 33 + 1024;
+constexpr int kRawLd = 260, kA1Ld = 36, kTLd = 36;
+constexpr size_t kVraw = sizeof(float) * 32 * kRawLd;     // V_b: 32 columns of m2 rows
+constexpr size_t kA1s = sizeof(float) * 128 * kA1Ld;      // A1_b: 128 columns of 32 rows
+constexpr size_t kTs = sizeof(float) * 32 * kTLd;         // T_b: 32 x 32
+constexpr size_t kSmem = 2 * kStage + kVraw + kA1s + kTs + 1024;
+static_assert(sizeof(float) * 128 * kRawLd <= 2 * kStage, "A2 staging fits the stage buffers");
 constexpr int kBars = 3;               // GEMM1 stage 0, GEMM1 stage 1, GEMM2
 constexpr long kWaitLimit = 1L << 26;  // mbarrier polls before giving up
 
@@ -77,12 +82,6 @@ __device__ __forceinline__ float tf32_round(float x) {
   return __uint_as_float(r);
 }
 
-__device__ __forceinline__ void put_split(unsigned char *hi, unsigned char *lo, int off, float x) {
-  const float h = tf32_round(x);
-  *reinterpret_cast<float *>(hi + off) = h;
-  *reinterpret_cast<float *>(lo + off) = tf32_round(x - h);
-}
-
 __device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
   asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
                "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}"
@@ -104,31 +103,22 @@ __device__ __forceinline__ bool bar_wait(uint64_t *bar, uint32_t parity) {
   return false;
 }
 
+// 32 TMEM columns of this warp's lane quarter; the load and its wait are one
+// asm statement, so no use of the registers can be scheduled before the wait.
 __device__ __forceinline__ void ld32(uint32_t taddr, float (&v)[32]) {
   uint32_t r[32];
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+      "tcgen05.wait::ld.sync.aligned;"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
         "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
         "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
         "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      : "r"(taddr)
+      : "memory");
 #pragma unroll
   for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
-}
-
-__device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
 // Shared memory written by threads -> visible to the tensor core; all threads.
@@ -148,20 +138,6 @@ __device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t *phase) {
   return ok;
 }
 
-// Issue (thread 0), commit and wait (all threads); false if the wait gave up.
-template <typename F>
-__device__ __forceinline__ bool run_mma(F issue, uint64_t *bar, uint32_t *phase) {
-  if (threadIdx.x == 0) {
-    issue();
-    commit(bar);
-  }
-  // the same verdict in every thread, so callers leave together
-  const bool ok = __syncthreads_and(bar_wait(bar, *phase)) != 0;
-  *phase ^= 1u;
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  return ok;
-}
-
 __device__ __forceinline__ void put_split4(unsigned char *hi, unsigned char *lo, int off, float4 x) {
   float4 h, l;
   h.x = tf32_round(x.x); l.x = tf32_round(x.x - h.x);
@@ -170,46 +146,6 @@ __device__ __forceinline__ void put_split4(unsigned char *hi, unsigned char *lo,
   h.w = tf32_round(x.w); l.w = tf32_round(x.w - h.w);
   *reinterpret_cast<float4 *>(hi + off) = h;
   *reinterpret_cast<float4 *>(lo + off) = l;
-}
-
-// Stage rows [r0, r0 + nr) x columns [0, ncol) of a column-major matrix as
-// the K-major operand with K = row (4 consecutive rows = one 16-byte run),
-// row-of-operand = column; SBO = (nr / 4) * 128.  nr a multiple of 4, ncol a
-// multiple of 8; the source 16-byte aligned with ld a multiple of 4.
-// Lanes run over 8 columns first (conflict-free 128-byte stores), then K.
-template <int NCOL, int NR>
-__device__ __forceinline__ void stage_kmajor(const float *src, int ld, int r0, unsigned char *hi, unsigned char *lo) {
-  constexpr int NV = NCOL * NR / 4;               // float4 pieces
-  constexpr int PER = NV / TQR_THREADS;           // per thread (exact for the shapes used)
-  static_assert(NV % TQR_THREADS == 0, "staging shape");
-  float4 v[PER];
-#pragma unroll
-  for (int u = 0; u < PER; ++u) {
-    const int idx = threadIdx.x + u * TQR_THREADS;
-    const int cl = idx % 8, k4 = (idx / 8) % (NR / 4), ch = idx / (8 * (NR / 4));
-    const int c = ch * 8 + cl;
-    v[u] = __ldcg(reinterpret_cast<const float4 *>(src + (size_t)(r0 + 4 * k4) + (size_t)c * ld));
-  }
-#pragma unroll
-  for (int u = 0; u < PER; ++u) {
-    const int idx = threadIdx.x + u * TQR_THREADS;
-    const int cl = idx % 8, k4 = (idx / 8) % (NR / 4), ch = idx / (8 * (NR / 4));
-    put_split4(hi, lo, kmaj(ch * 8 + cl, 4 * k4, (NR / 4) * 128), v[u]);
-  }
-}
-
-// 32 consecutive TMEM columns of this warp's lane quarter <- v (one column per
-// register); the caller waits (wait_st) before the values are read.
-__device__ __forceinline__ void st16(uint32_t taddr, const float (&v)[16]) {
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
-      ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
-        "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
-        "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
-        "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
-        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
-        "r"(__float_as_uint(v[15]))
-      : "memory");
 }
 
 __device__ __forceinline__ void wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
@@ -221,24 +157,35 @@ __device__ __forceinline__ void tmem_sync() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// V_b (m2 x 32, column-major, 16-byte aligned, ldv a multiple of 4) ->
-// Vraw (column stride kVrawLd) by 16-byte cp.async copies; one commit group.
-__device__ __forceinline__ void prefetch_vb(const float *Vb, int ldv, int m2, float *Vraw) {
-  const int per_col = m2 / 4;
-  for (int idx = threadIdx.x; idx < kIb * per_col; idx += TQR_THREADS) {
-    const int p = idx / per_col, r4 = idx % per_col;
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr(Vraw + p * kVrawLd + 4 * r4)),
-                 "l"(Vb + (size_t)p * ldv + 4 * r4)
-                 : "memory");
-  }
-  asm volatile("cp.async.commit_group;" ::: "memory");
+__device__ __forceinline__ void cp16(void *sdst, const void *gsrc) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr(sdst)), "l"(gsrc) : "memory");
 }
+
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 
 __device__ __forceinline__ void prefetch_wait() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
+// Block b's raw operands by 16-byte cp.async copies, one commit group:
+// V_b (m2 x 32) -> Vraw (column stride kRawLd), A1_b (32 x 128) -> A1s
+// (column stride kA1Ld).  Sources 16-byte aligned, leading dimensions
+// multiples of 4; consecutive threads copy consecutive 16 bytes of a column.
+__device__ __forceinline__ void prefetch_block(const float *Vb, int ldv, int m2, float *Vraw, const float *A1b,
+                                               int lda1, float *A1s) {
+  const int per_col = m2 / 4;
+  for (int idx = threadIdx.x; idx < kIb * per_col; idx += TQR_THREADS) {
+    const int p = idx / per_col, r4 = idx % per_col;
+    cp16(Vraw + p * kRawLd + 4 * r4, Vb + (size_t)p * ldv + 4 * r4);
+  }
+  for (int idx = threadIdx.x; idx < kChunk * (kIb / 4); idx += TQR_THREADS) {
+    const int cc = idx / (kIb / 4), p4 = idx % (kIb / 4);
+    cp16(A1s + cc * kA1Ld + 4 * p4, A1b + (size_t)cc * lda1 + 4 * p4);
+  }
+  cp_commit();
+}
+
 // GEMM1's B operand for rows [r0, r0 + kKc) from Vraw: row-of-operand p, K =
 // r.  Lanes take 8 p by 4 K runs, so the 16-byte reads (column stride
-// kVrawLd) and the core-matrix stores each spread over all banks.
+// kRawLd) and the core-matrix stores each spread over all banks.
 __device__ __forceinline__ void stage_vb1(const float *Vraw, int r0, unsigned char *hi, unsigned char *lo) {
   constexpr uint32_t SB = (kKc / 4) * 128;
 #pragma unroll
@@ -246,14 +193,58 @@ __device__ __forceinline__ void stage_vb1(const float *Vraw, int r0, unsigned ch
     const int idx = threadIdx.x + u * TQR_THREADS;
     const int rest = idx >> 5;
     const int p = 8 * (rest & 3) + (idx & 7), k4 = 4 * (rest >> 2) + ((idx >> 3) & 3);
-    const float4 x = *reinterpret_cast<const float4 *>(Vraw + p * kVrawLd + r0 + 4 * k4);
+    const float4 x = *reinterpret_cast<const float4 *>(Vraw + p * kRawLd + r0 + 4 * k4);
     put_split4(hi, lo, kmaj(p, 4 * k4, SB), x);
   }
 }
 
+// Two 32-column TMEM reads of this warp's lane quarter, one wait.
+__device__ __forceinline__ void ld32x2(uint32_t ta, uint32_t tb, float (&a)[32], float (&b)[32]) {
+  uint32_t r[64];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%64];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,"
+      "%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%65];\n"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
+        "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
+        "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
+        "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
+        "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+      : "r"(ta), "r"(tb)
+      : "memory");
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    a[j] = __uint_as_float(r[j]);
+    b[j] = __uint_as_float(r[32 + j]);
+  }
+}
+
+__device__ __forceinline__ void st32(uint32_t taddr, const float (&v)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};"
+      ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+        "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+        "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
+        "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+        "r"(__float_as_uint(v[15])), "r"(__float_as_uint(v[16])), "r"(__float_as_uint(v[17])),
+        "r"(__float_as_uint(v[18])), "r"(__float_as_uint(v[19])), "r"(__float_as_uint(v[20])),
+        "r"(__float_as_uint(v[21])), "r"(__float_as_uint(v[22])), "r"(__float_as_uint(v[23])),
+        "r"(__float_as_uint(v[24])), "r"(__float_as_uint(v[25])), "r"(__float_as_uint(v[26])),
+        "r"(__float_as_uint(v[27])), "r"(__float_as_uint(v[28])), "r"(__float_as_uint(v[29])),
+        "r"(__float_as_uint(v[30])), "r"(__float_as_uint(v[31]))
+      : "memory");
+}
+
 // [A1; A2] := Q^T [A1; A2] for the 128 columns at A1, A2 (column-major):
 // A1 rows [0, k), A2 m2 rows (m2 = 128 or 256), V m2 x k, T 32 x k (blocks of
-// 32 columns), k a multiple of 32; A2, V 16-byte aligned with leading
+// 32 columns), k a multiple of 32; A1, A2, V 16-byte aligned with leading
 // dimensions multiples of 4.  256 threads; all kTmemCols TMEM columns at
 // tmem; bars[kBars] mbarriers (count 1) with parities phase[kBars].  Returns
 // false if an MMA completion wait timed out (the caller then waits once more
@@ -281,84 +272,82 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
   const uint32_t d2t = tmem + ((uint32_t)((warp & 3) * 32) << 16);
   const uint32_t a2t = d2t + kA2Col;
   unsigned char *st_base[2] = {smem, smem + kStage};
-  float *Vraw = reinterpret_cast<float *>(smem + 2 * kStage);              // 32 x kVrawLd
-  float *Ts = reinterpret_cast<float *>(smem + 2 * kStage + kVraw);        // 32 x 33
+  float *A2raw = reinterpret_cast<float *>(smem);                                  // 128 x kRawLd
+  float *Vraw = reinterpret_cast<float *>(smem + 2 * kStage);                      // 32 x kRawLd
+  float *A1s = reinterpret_cast<float *>(smem + 2 * kStage + kVraw);               // 128 x kA1Ld
+  float *Ts = reinterpret_cast<float *>(smem + 2 * kStage + kVraw + kA1s);         // 32 x kTLd
   // GEMM2 operands in the stage buffers' A regions
   unsigned char *vHi = smem, *vLo = smem + kBufA;                    // V_b^T: m2 x 32, K-major (B)
-  unsigned char *wHi = smem + kStage, *wLo = smem + kStage + kBufA;  // -W^T: 128 x 32, K-major (A)
+  unsigned char *wHi = smem + kStage, *wLo = smem + kStage + kBufA;  // W^T: 128 x 32, K-major (A)
   const uint32_t id1 = idesc_tf32(128, kIb), id2 = idesc_tf32(128, 128);
   const uint32_t d1 = tmem;
-  const int nq = m2 / kKc, half = m2 / 2;
+  const int nq = m2 / kKc, half = m2 / 2, per_col = m2 / 4, nblk = k / kIb;
   constexpr uint32_t SB = (kKc / 4) * 128;
-  if (k >= kIb) prefetch_vb(V, ldv, m2, Vraw);
-  // ---- A2^T into TMEM: thread c reads its column (16-byte runs along r) ----
-  {
-    const float *src = A2 + (size_t)c * lda2;
-#pragma unroll 1
-    for (int r0 = wset * half; r0 < (wset + 1) * half; r0 += 32) {
-      float4 x[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) x[u] = __ldcg(reinterpret_cast<const float4 *>(src + r0 + 4 * u));
-#pragma unroll
-      for (int g = 0; g < 2; ++g) {
-        float v[16];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          v[4 * u] = x[4 * g + u].x; v[4 * u + 1] = x[4 * g + u].y;
-          v[4 * u + 2] = x[4 * g + u].z; v[4 * u + 3] = x[4 * g + u].w;
-        }
-        st16(a2t + (uint32_t)(r0 + 16 * g), v);
-      }
-    }
-    wait_st();
+  auto fail = [&]() {
+    prefetch_wait();   // no copy into shared memory outlives the routine
+    return false;
+  };
+  // ---- A2 into TMEM as A2^T: coalesced cp.async into the stage buffers, then
+  //      thread c moves its column (16-byte runs along r) with tcgen05.st ----
+  for (int idx = tid; idx < kChunk * per_col; idx += TQR_THREADS) {
+    const int cc = idx / per_col, r4 = idx % per_col;
+    cp16(A2raw + cc * kRawLd + 4 * r4, A2 + (size_t)cc * lda2 + 4 * r4);
   }
+  cp_commit();
+  if (nblk > 0) prefetch_block(V, ldv, m2, Vraw, A1, lda1, A1s);
+  prefetch_wait();
+  __syncthreads();
+#pragma unroll 1
+  for (int r0 = wset * half; r0 < (wset + 1) * half; r0 += 32) {
+    float v[32];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const float4 x = *reinterpret_cast<const float4 *>(A2raw + c * kRawLd + r0 + 4 * u);
+      v[4 * u] = x.x; v[4 * u + 1] = x.y; v[4 * u + 2] = x.z; v[4 * u + 3] = x.w;
+    }
+    st32(a2t + (uint32_t)r0, v);
+  }
+  wait_st();
   tmem_sync();
-  for (int b = 0; b < k / kIb; ++b) {
-    // this block's T (upper triangle) and A1 rows, fetched now and used after GEMM1
+  for (int b = 0; b < nblk; ++b) {
+    // this block's T (upper triangle), fetched now and used after GEMM1
     float tv[kIb * kIb / TQR_THREADS];
 #pragma unroll
     for (int u = 0; u < kIb * kIb / TQR_THREADS; ++u) {
       const int idx = tid + u * TQR_THREADS, r = idx % kIb, cc = idx / kIb;
       tv[u] = (r <= cc) ? __ldcg(T + (size_t)r + (size_t)(b * kIb + cc) * ldt) : 0.0f;
     }
-    float *a1 = A1 + (size_t)b * kIb + (size_t)c * lda1;
-    float a1v[kIb];
-    if (warp < 4) {
-#pragma unroll
-      for (int p = 0; p < kIb; ++p) a1v[p] = __ldcg(a1 + p);
+    if (b > 0) {
+      prefetch_wait();
+      __syncthreads();   // V_b, A1_b in Vraw, A1s
     }
-    prefetch_wait();
-    __syncthreads();   // V_b in Vraw
     // ---- GEMM1: D1[c][p] = sum_r A2^T[c][r] V_b[r][p], K chunks of 64 rows,
     //      staging of chunk q + 1 overlapping the MMAs of chunk q ----
     for (int q = 0; q < nq; ++q) {
       const int sbuf = q & 1;
-      if (q >= 2 && !wait_phase(&bars[sbuf], &phase[sbuf])) {   // chunk q - 2 done with it
-        prefetch_wait();
-        return false;
-      }
+      if (q >= 2 && !wait_phase(&bars[sbuf], &phase[sbuf])) return fail();   // chunk q - 2 done with it
       unsigned char *aHi = st_base[sbuf], *aLo = aHi + kBufA, *bHi = aHi + 2 * kBufA, *bLo = bHi + kBufB;
       // A operand from TMEM: warp set s takes rows [32 s, 32 s + 32) of the
       // chunk, first finishing the previous block's A2^T -= D2 on them (chunk
       // 0's D2 columns are read before this block's GEMM1 overwrites D1)
-#pragma unroll
-      for (int g = 0; g < 2; ++g) {
-        const int r = q * kKc + wset * 32 + g * 16;
-        float v[16];
-        ld16(a2t + (uint32_t)r, v);
+      {
+        const int r = q * kKc + wset * 32;
+        float v[32];
         if (b > 0) {
-          float d[16];
-          ld16(d2t + d2col(r), d);
+          float d[32];
+          ld32x2(a2t + (uint32_t)r, d2t + d2col(r), v, d);
 #pragma unroll
-          for (int j = 0; j < 16; ++j) v[j] -= d[j];
-          st16(a2t + (uint32_t)r, v);
+          for (int j = 0; j < 32; ++j) v[j] -= d[j];
+          st32(a2t + (uint32_t)r, v);
+        } else {
+          ld32(a2t + (uint32_t)r, v);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-          put_split4(aHi, aLo, kmaj(c, r - q * kKc + 4 * u, SB),
+        for (int u = 0; u < 8; ++u)
+          put_split4(aHi, aLo, kmaj(c, wset * 32 + 4 * u, SB),
                      make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]));
+        if (b > 0) wait_st();
       }
-      if (b > 0) wait_st();
       stage_vb1(Vraw, q * kKc, bHi, bLo);
       to_async_proxy();
       if (tid == 0) {
@@ -376,37 +365,48 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
     }
     // the last two chunks' commits (one per stage buffer) are still pending
     for (int q = (nq >= 2 ? nq - 2 : 0); q < nq; ++q)
-      if (!wait_phase(&bars[q & 1], &phase[q & 1])) {
-        prefetch_wait();
-        return false;
-      }
-    // T block (upper triangle) to shared memory
+      if (!wait_phase(&bars[q & 1], &phase[q & 1])) return fail();
+    // T block (upper triangle, zeros below) to shared memory
 #pragma unroll
     for (int u = 0; u < kIb * kIb / TQR_THREADS; ++u) {
       const int idx = tid + u * TQR_THREADS, r = idx % kIb, cc = idx / kIb;
-      Ts[r + cc * 33] = tv[u];
+      Ts[r + cc * kTLd] = tv[u];
     }
     __syncthreads();
     if (warp < 4) {
-      // ---- W = T^T (A1_b + D1^T); A1_b -= W; W (split) -> A operand of GEMM2 ----
+      // ---- W = T^T (A1_b + D1^T); A1_b -= W (in A1s); W (split) -> A operand of GEMM2 ----
       float w[32];
       ld32(d1 + ((uint32_t)(warp * 32) << 16), w);
+      float *a1s = A1s + c * kA1Ld;
 #pragma unroll
-      for (int p = 0; p < 32; ++p) w[p] += a1v[p];
-      // W := T^T W in place, last row first (row p reads rows q <= p, not yet overwritten)
+      for (int p4 = 0; p4 < 8; ++p4) {
+        const float4 x = *reinterpret_cast<const float4 *>(a1s + 4 * p4);
+        w[4 * p4] += x.x; w[4 * p4 + 1] += x.y; w[4 * p4 + 2] += x.z; w[4 * p4 + 3] += x.w;
+      }
+      // W := T^T W in place, last row first (row p reads rows q <= p, not yet
+      // overwritten; the zeros of T below its diagonal cover the rest of the
+      // 16-byte group)
 #pragma unroll
       for (int p = 31; p >= 0; --p) {
         float s = 0.0f;
 #pragma unroll
-        for (int qq = 0; qq <= p; ++qq) s = fmaf(Ts[qq + p * 33], w[qq], s);
+        for (int q4 = 0; q4 <= p / 4; ++q4) {
+          const float4 t = *reinterpret_cast<const float4 *>(Ts + p * kTLd + 4 * q4);
+          s = fmaf(t.x, w[4 * q4], s);
+          s = fmaf(t.y, w[4 * q4 + 1], s);
+          s = fmaf(t.z, w[4 * q4 + 2], s);
+          s = fmaf(t.w, w[4 * q4 + 3], s);
+        }
         w[p] = s;
       }
 #pragma unroll
-      for (int p = 0; p < 32; ++p) a1[p] -= w[p];
-#pragma unroll
-      for (int p4 = 0; p4 < 8; ++p4)
-        put_split4(wHi, wLo, kmaj(c, 4 * p4, (kIb / 4) * 128),
-                   make_float4(w[4 * p4], w[4 * p4 + 1], w[4 * p4 + 2], w[4 * p4 + 3]));
+      for (int p4 = 0; p4 < 8; ++p4) {
+        float4 x = *reinterpret_cast<const float4 *>(a1s + 4 * p4);
+        x.x -= w[4 * p4]; x.y -= w[4 * p4 + 1]; x.z -= w[4 * p4 + 2]; x.w -= w[4 * p4 + 3];
+        *reinterpret_cast<float4 *>(a1s + 4 * p4) = x;
+        put_split4(wHi, wLo, kmaj(c, 4 * p4, (kIb / 4) * 128), make_float4(w[4 * p4], w[4 * p4 + 1],
+                                                                          w[4 * p4 + 2], w[4 * p4 + 3]));
+      }
     } else {
       // ---- meanwhile V_b^T as the B operand of GEMM2 from Vraw: row r, K = p;
       //      four reads along p (consecutive r across the warp), one 16-byte store ----
@@ -414,16 +414,14 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
 #pragma unroll 4
       for (int idx = t; idx < m2 * (kIb / 4); idx += 128) {
         const int r = idx % m2, p4 = idx / m2;
-        const float *vp = Vraw + (4 * p4) * kVrawLd + r;
+        const float *vp = Vraw + (4 * p4) * kRawLd + r;
         put_split4(vHi, vLo, kmaj(r, 4 * p4, (kIb / 4) * 128),
-                   make_float4(vp[0], vp[kVrawLd], vp[2 * kVrawLd], vp[3 * kVrawLd]));
+                   make_float4(vp[0], vp[kRawLd], vp[2 * kRawLd], vp[3 * kRawLd]));
       }
     }
     to_async_proxy();
-    // Vraw is free: the next block's V_b flies during GEMM2
-    if (b + 1 < k / kIb) prefetch_vb(V + (size_t)(b + 1) * kIb * ldv, ldv, m2, Vraw);
     // ---- GEMM2, both 128-row halves: D2[c][r] = sum_p W[p][c] V_b[r][p] ----
-    const bool ok2 = run_mma([&] {
+    if (tid == 0) {
       for (int h = 0; h < m2 / 128; ++h) {
         const uint32_t bo = h * 16 * 1024;   // 16 row groups of V_b^T per half
         for (int ks = 0; ks < kIb / 8; ++ks) {
@@ -436,30 +434,45 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
           mma(d2, al, bh, id2, 1u);
         }
       }
-    }, &bars[2], &phase[2]);
-    if (!ok2) {
-      prefetch_wait();   // no copy into shared memory outlives the routine
-      return false;
+      commit(&bars[2]);
     }
-  }
-  // ---- A2 = A2^T - D2 out of TMEM: thread c writes its column ----
-  {
-    float *dst = A2 + (size_t)c * lda2;
-#pragma unroll 1
-    for (int r0 = wset * half; r0 < (wset + 1) * half; r0 += 16) {
-      float v[16];
-      ld16(a2t + (uint32_t)r0, v);
-      if (k >= kIb) {   // the last block's D2 is pending
-        float d[16];
-        ld16(d2t + d2col(r0), d);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) v[j] -= d[j];
+    // while the MMAs run: the updated A1_b back to global (coalesced), then
+    // the next block's V_b and A1_b into Vraw, A1s
+    {
+      float *A1b = A1 + (size_t)b * kIb;
+      for (int idx = tid; idx < kChunk * (kIb / 4); idx += TQR_THREADS) {
+        const int cc = idx / (kIb / 4), p4 = idx % (kIb / 4);
+        *reinterpret_cast<float4 *>(A1b + (size_t)cc * lda1 + 4 * p4) =
+            *reinterpret_cast<const float4 *>(A1s + cc * kA1Ld + 4 * p4);
       }
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        *reinterpret_cast<float4 *>(dst + r0 + 4 * u) =
-            make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]);
     }
+    __syncthreads();
+    if (b + 1 < nblk)
+      prefetch_block(V + (size_t)(b + 1) * kIb * ldv, ldv, m2, Vraw, A1 + (size_t)(b + 1) * kIb, lda1, A1s);
+    if (!wait_phase(&bars[2], &phase[2])) return fail();
+  }
+  // ---- A2 = A2^T - D2 out of TMEM through the stage buffers (coalesced) ----
+#pragma unroll 1
+  for (int r0 = wset * half; r0 < (wset + 1) * half; r0 += 32) {
+    float v[32];
+    if (nblk > 0) {   // the last block's D2 is pending
+      float d[32];
+      ld32x2(a2t + (uint32_t)r0, d2t + d2col(r0), v, d);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) v[j] -= d[j];
+    } else {
+      ld32(a2t + (uint32_t)r0, v);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      *reinterpret_cast<float4 *>(A2raw + c * kRawLd + r0 + 4 * u) =
+          make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]);
+  }
+  __syncthreads();
+  for (int idx = tid; idx < kChunk * per_col; idx += TQR_THREADS) {
+    const int cc = idx / per_col, r4 = idx % per_col;
+    *reinterpret_cast<float4 *>(A2 + (size_t)cc * lda2 + 4 * r4) =
+        *reinterpret_cast<const float4 *>(A2raw + cc * kRawLd + 4 * r4);
   }
   tmem_sync();
   return true;
