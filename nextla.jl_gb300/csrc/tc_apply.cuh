@@ -6,14 +6,18 @@
 //   W^T  = A2^T V_b              GEMM1: M = 128 (chunk columns), N = 32, K = m2
 //   W    = T_b^T (A1_b + W)      SIMT on the TMEM read-back (32 x 32 triangle)
 //   A1_b = A1_b - W
-//   D2   = W^T V_b^T             GEMM2: M = 128, N = 128 per half of A2's rows
+//   D2   = W^T V_b^T             GEMM2: M = 128, N = m2, K = 32
 //   A2^T = A2^T - D2             SIMT, IEEE FP32, on A2^T kept in TMEM
 //
 // Both GEMMs run as tcgen05.mma kind::tf32 with FP32 accumulators in TMEM,
 // issued by one thread and completed through an mbarrier; every operand is
-// split x = hi + lo with hi = tf32(x), lo = tf32(x - hi) and the product
-// taken as hi*hi + hi*lo + lo*hi (three MMAs into one accumulator), which
-// keeps FP32-level accuracy (the dropped lo*lo term is ~2^-22 relative).
+// split x = hi + lo with hi = tf32(x), lo = tf32(x - hi), which keeps
+// FP32-level accuracy.  GEMM2 takes hi*hi + hi*lo + lo*hi (three MMAs into
+// one accumulator; the dropped lo*lo term is ~2^-22 relative).  GEMM1's N =
+// 32 is too narrow to keep the tensor core busy, so its B operand is [V_hi;
+// V_lo] (N = 64) and two MMAs per K step, A_hi [V_hi; V_lo] + A_lo [V_hi;
+// V_lo], leave W's two halves side by side (the read-back adds them): the
+// MMA count of a K step drops from three to two.
 //
 // Shared-memory operands use the no-swizzle K-major core-matrix layout: 8
 // rows x 16 bytes per core matrix, consecutive K groups 128 bytes apart (the
@@ -33,12 +37,11 @@ namespace tc {
 constexpr int kChunk = 128;            // chunk columns (GEMM1 M, GEMM2 N)
 constexpr int kIb = 32;                // reflectors per block (GEMM1 N, GEMM2 K)
 constexpr int kKc = 64;                // GEMM1 K chunk (rows of A2 staged at once)
-// TMEM columns: A2^T in [128, 128 + m2); D2 of A2's rows [0, 128) in [0, 128)
-// (D1, in [0, 32), is consumed before GEMM2 overwrites it) and of rows
-// [128, 256) in [384, 512)
+// TMEM columns: D2 (row r of A2 in column r) in [0, m2), A2^T in [256,
+// 256 + m2); D1 (64 columns, W's two halves) in [0, 64), consumed before
+// GEMM2 overwrites it
 constexpr int kTmemCols = 512;
-constexpr uint32_t kA2Col = 128;
-__device__ __forceinline__ uint32_t d2col(int r) { return r < 128 ? (uint32_t)r : (uint32_t)(256 + r); }
+constexpr uint32_t kA2Col = 256;
 // dynamic shared memory: two GEMM1 stage buffers, each A hi/lo (2 x 32 KB) and
 // B hi/lo (2 x 8 KB); GEMM2 reuses them (V_b^T hi/lo in stage 0's A, W^T
 // hi/lo in stage 1's A), and A2 passes through them (column stride kRawLd)
@@ -252,8 +255,8 @@ __device__ __forceinline__ void st32(uint32_t taddr, const float (&v)[32]) {
 //
 // A2 stays in TMEM for the whole chunk, transposed: TMEM lane c (the chunk
 // column) holds A2[0:m2, c] in columns [kA2Col, kA2Col + m2).  So GEMM2 is
-// taken transposed, D2 = W^T V_b^T (M = 128 columns, N = 128 rows per half,
-// K = 32), and GEMM1's K-major operand A2^T (row c, K = r) is read back from
+// taken transposed, D2 = W^T V_b^T (M = 128 columns, N = m2 rows, K = 32),
+// and GEMM1's K-major operand A2^T (row c, K = r) is read back from
 // TMEM one lane per thread: 16 consecutive r of one c are four 16-byte K
 // runs, stored without any transpose.  The subtraction A2^T -= D2 is fused
 // into the next block's staging pass (and into the final write-back) and runs
@@ -279,7 +282,7 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
   // GEMM2 operands in the stage buffers' A regions
   unsigned char *vHi = smem, *vLo = smem + kBufA;                    // V_b^T: m2 x 32, K-major (B)
   unsigned char *wHi = smem + kStage, *wLo = smem + kStage + kBufA;  // W^T: 128 x 32, K-major (A)
-  const uint32_t id1 = idesc_tf32(128, kIb), id2 = idesc_tf32(128, 128);
+  const uint32_t id1 = idesc_tf32(128, 2 * kIb), id2 = idesc_tf32(128, m2);
   const uint32_t d1 = tmem;
   const int nq = m2 / kKc, half = m2 / 2, per_col = m2 / 4, nblk = k / kIb;
   constexpr uint32_t SB = (kKc / 4) * 128;
@@ -329,13 +332,14 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
       unsigned char *aHi = st_base[sbuf], *aLo = aHi + kBufA, *bHi = aHi + 2 * kBufA, *bLo = bHi + kBufB;
       // A operand from TMEM: warp set s takes rows [32 s, 32 s + 32) of the
       // chunk, first finishing the previous block's A2^T -= D2 on them (chunk
-      // 0's D2 columns are read before this block's GEMM1 overwrites D1)
+      // 0's D2 columns, [0, 64), are read before this block's GEMM1 writes D1
+      // there; chunk 1's, [64, 128), are disjoint from D1)
       {
         const int r = q * kKc + wset * 32;
         float v[32];
         if (b > 0) {
           float d[32];
-          ld32x2(a2t + (uint32_t)r, d2t + d2col(r), v, d);
+          ld32x2(a2t + (uint32_t)r, d2t + (uint32_t)r, v, d);
 #pragma unroll
           for (int j = 0; j < 32; ++j) v[j] -= d[j];
           st32(a2t + (uint32_t)r, v);
@@ -354,11 +358,10 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
         for (int ks = 0; ks < kKc / 8; ++ks) {
           const uint32_t o = ks * 256;
           const uint64_t ah = sdesc(saddr(aHi) + o, 128, SB), al = sdesc(saddr(aLo) + o, 128, SB);
-          const uint64_t bh = sdesc(saddr(bHi) + o, 128, SB), bl = sdesc(saddr(bLo) + o, 128, SB);
-          const uint32_t first = (q == 0 && ks == 0) ? 0u : 1u;
-          mma(d1, ah, bh, id1, first);
-          mma(d1, ah, bl, id1, 1u);
-          mma(d1, al, bh, id1, 1u);
+          // rows 32..63 of this N = 64 operand are V_lo: bLo sits 4 row groups after bHi
+          const uint64_t bb = sdesc(saddr(bHi) + o, 128, SB);
+          mma(d1, ah, bb, id1, (q == 0 && ks == 0) ? 0u : 1u);
+          mma(d1, al, bb, id1, 1u);
         }
         commit(&bars[sbuf]);
       }
@@ -376,7 +379,12 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
     if (warp < 4) {
       // ---- W = T^T (A1_b + D1^T); A1_b -= W (in A1s); W (split) -> A operand of GEMM2 ----
       float w[32];
-      ld32(d1 + ((uint32_t)(warp * 32) << 16), w);
+      {
+        float wl[32];
+        ld32x2(d1 + ((uint32_t)(warp * 32) << 16), d1 + ((uint32_t)(warp * 32) << 16) + kIb, w, wl);
+#pragma unroll
+        for (int p = 0; p < 32; ++p) w[p] += wl[p];   // (A_hi + A_lo) V_hi + (A_hi + A_lo) V_lo
+      }
       float *a1s = A1s + c * kA1Ld;
 #pragma unroll
       for (int p4 = 0; p4 < 8; ++p4) {
@@ -420,19 +428,15 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
       }
     }
     to_async_proxy();
-    // ---- GEMM2, both 128-row halves: D2[c][r] = sum_p W[p][c] V_b[r][p] ----
+    // ---- GEMM2 over all m2 rows at once: D2[c][r] = sum_p W[p][c] V_b[r][p] ----
     if (tid == 0) {
-      for (int h = 0; h < m2 / 128; ++h) {
-        const uint32_t bo = h * 16 * 1024;   // 16 row groups of V_b^T per half
-        for (int ks = 0; ks < kIb / 8; ++ks) {
-          const uint32_t o = ks * 256;
-          const uint64_t ah = sdesc(saddr(wHi) + o, 128, 1024), al = sdesc(saddr(wLo) + o, 128, 1024);
-          const uint64_t bh = sdesc(saddr(vHi) + bo + o, 128, 1024), bl = sdesc(saddr(vLo) + bo + o, 128, 1024);
-          const uint32_t d2 = tmem + d2col(128 * h);
-          mma(d2, ah, bh, id2, ks == 0 ? 0u : 1u);
-          mma(d2, ah, bl, id2, 1u);
-          mma(d2, al, bh, id2, 1u);
-        }
+      for (int ks = 0; ks < kIb / 8; ++ks) {
+        const uint32_t o = ks * 256;
+        const uint64_t ah = sdesc(saddr(wHi) + o, 128, 1024), al = sdesc(saddr(wLo) + o, 128, 1024);
+        const uint64_t bh = sdesc(saddr(vHi) + o, 128, 1024), bl = sdesc(saddr(vLo) + o, 128, 1024);
+        mma(tmem, ah, bh, id2, ks == 0 ? 0u : 1u);
+        mma(tmem, ah, bl, id2, 1u);
+        mma(tmem, al, bh, id2, 1u);
       }
       commit(&bars[2]);
     }
@@ -457,7 +461,7 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
     float v[32];
     if (nblk > 0) {   // the last block's D2 is pending
       float d[32];
-      ld32x2(a2t + (uint32_t)r0, d2t + d2col(r0), v, d);
+      ld32x2(a2t + (uint32_t)r0, d2t + (uint32_t)r0, v, d);
 #pragma unroll
       for (int j = 0; j < 32; ++j) v[j] -= d[j];
     } else {
