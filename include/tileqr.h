@@ -296,6 +296,20 @@ int tqr_tile_dag_stats(const void *work, unsigned long long *out, cudaStream_t s
 /* Host-only self check of the schedule for a shape: replays the task list and
  * confirms every closed-form wait target and the topological sort (0 = ok). */
 int tqr_tile_dag_check(int m, int n, int nb, int ib, long long *ntasks);
+/* (nb, ib) autotuner of the tile QR (no counterpart in NextLA, whose callers
+ * pass nb and ib).  Times the tile QR of a seeded m-by-n matrix (uniform
+ * [-1, 1) entries) for each candidate (nb, ib): (256, 32), (256, 16),
+ * (256, 64); (128, 32), (128, 16) when max(m, n) <= 16384; (64, 16), (64, 32)
+ * when max(m, n) <= 2048 -- through the persistent kernel where m and n are
+ * multiples of nb, else the stream driver -- and returns the fastest in
+ * *nb, *ib.  The result is cached per (dtype_bytes, m, n); force = 1 times
+ * again.  dtype_bytes 8 (Float64) or 4 (Float32).  Allocates, synchronises
+ * `stream` and frees before it returns: call it outside any stream capture.
+ * Returns TQR_ERR_WAIT_TIMEOUT if a persistent-kernel wait ran out.
+ * tqr_tile_tuning reads the cache: 0 and the entry, or 1 if not tuned. */
+#define TQR_ERR_WAIT_TIMEOUT (-1001)
+int tqr_tile_autotune(int dtype_bytes, int m, int n, int force, int *nb, int *ib, cudaStream_t stream);
+int tqr_tile_tuning(int dtype_bytes, int m, int n, int *nb, int *ib);
 int tqr_tile_dag_check_rhs(int m, int n, int nrhs, int nb, int ib, long long *ntasks);
 
 /* Least squares in one persistent launch plus a triangular solve (m >= n,

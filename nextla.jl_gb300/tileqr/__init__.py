@@ -23,6 +23,7 @@ __all__ = [
     "ArgumentError", "set_blocking", "empty", "zeros", "to_device", "to_numpy",
     "geqr2", "larft", "larfb", "geqrt", "unmqr", "tsqrt", "tsmqr", "parfb", "pamm", "ttqrt", "ttmqr",
     "tile_geqrf", "tile_unmqr", "trsm_lun", "tile_gels", "tile_shapes",
+    "autotune_tiling", "tile_geqrf_tuned",
 ]
 
 _BLOCKING = True
@@ -474,6 +475,36 @@ def tile_geqrf(A, nb=256, ib=32, T=None, tau=None, dag=True):
         if status != 0:
             raise RuntimeError(f"tile_geqrf: schedule wait timed out at task {task} (status {status})")
     return T, tau
+
+
+def autotune_tiling(m, n, dtype=torch.float64, force=False):
+    """(nb, ib) for the tile QR of an m x n matrix of `dtype` (float64 or
+    float32), chosen by timing every candidate tiling on a seeded matrix of
+    that shape (libtileqr's tqr_tile_autotune).  Cached per (dtype, m, n):
+    the first call for a shape allocates and synchronises, later calls return
+    the cached pair; force=True times again."""
+    import ctypes
+    if dtype not in (torch.float64, torch.float32):
+        raise ArgumentError("autotune_tiling: dtype must be float64 or float32")
+    nb, ib = ctypes.c_int(0), ctypes.c_int(0)
+    st = torch.cuda.current_stream()
+    rc = _lib.lib().tqr_tile_autotune(8 if dtype == torch.float64 else 4, m, n, 1 if force else 0,
+                                      ctypes.byref(nb), ctypes.byref(ib), st.cuda_stream)
+    if rc < 0 and rc > -1000:
+        raise ArgumentError(f"autotune_tiling: illegal value of argument {-rc}")
+    if rc != 0:
+        raise RuntimeError(f"autotune_tiling: error {rc}")
+    return nb.value, ib.value
+
+
+def tile_geqrf_tuned(A, T=None, tau=None):
+    """Tile QR of A in place with the autotuned (nb, ib) for its shape and
+    element type; returns (T, tau, nb, ib) -- T and tau in the layout of that
+    tiling, which later calls (tile_unmqr, tile_gels) must use."""
+    m, n = A.shape
+    nb, ib = autotune_tiling(m, n, A.dtype)
+    T, tau = tile_geqrf(A, nb, ib, T, tau)
+    return T, tau, nb, ib
 
 
 def tree_dag_workspace(m, n, nb, ib, nrhs, device, grp=1):

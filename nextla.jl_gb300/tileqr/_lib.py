@@ -61,6 +61,8 @@ DIAG = {
     "tqr_tile_dag_status": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I), _P], _I),
     "tqr_tile_dag_wait_selftest": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, ctypes.c_size_t, _I, _P], _I),
     "tqr_tile_dag_check": ([_I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)], _I),
+    "tqr_tile_autotune": ([_I, _I, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), _P], _I),
+    "tqr_tile_tuning": ([_I, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
     "tqr_tile_dag_stats": ([_P, ctypes.POINTER(ctypes.c_ulonglong), _P], _I),
     "tqr_dtile_geqrf_noalloc": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P], _I),
     "tqr_tile_dag_check_rhs": ([_I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)], _I),

@@ -199,3 +199,15 @@ def test_hqr_task_graph_is_topological(L, m, n, nb, ib, grp, nrhs):
     assert L.tqr_tile_hqr_dag_check(m, n, nb, ib, 1, nrhs, ctypes.byref(one)) == 0
     assert L.tqr_tile_tree_dag_check(m, n, nb, ib, nrhs, ctypes.byref(tree)) == 0
     assert one.value == tree.value
+
+
+def test_tile_autotune_argument_errors(L):
+    nb, ib = ctypes.c_int(0), ctypes.c_int(0)
+    assert L.tqr_tile_autotune(3, 64, 64, 0, ctypes.byref(nb), ctypes.byref(ib), NULL) == -1
+    assert L.tqr_tile_autotune(8, 0, 64, 0, ctypes.byref(nb), ctypes.byref(ib), NULL) == -2
+    assert L.tqr_tile_autotune(8, 64, -1, 0, ctypes.byref(nb), ctypes.byref(ib), NULL) == -3
+    assert L.tqr_tile_autotune(8, 64, 64, 0, NULL, ctypes.byref(ib), NULL) == -5
+    assert L.tqr_tile_autotune(4, 64, 64, 0, ctypes.byref(nb), NULL, NULL) == -6
+    # nothing tuned for this shape yet
+    assert L.tqr_tile_tuning(8, 12345, 77, ctypes.byref(nb), ctypes.byref(ib)) == 1
+    assert L.tqr_tile_tuning(8, 64, 64, NULL, ctypes.byref(ib)) == -4
