@@ -29,6 +29,8 @@
 // (ld.global.cg): in the persistent kernel other SMs write the same tiles
 // between tasks, and L1 is not coherent with them.
 #pragma once
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace tqr {
@@ -69,6 +71,32 @@ __host__ __device__ inline size_t apply_smem_elems(int L, int ib, int nw, bool s
   if (sc) s += (size_t)odd_ld(L) * nw;
   if (sv) s += (size_t)odd_ld(L) * ib;
   return s;
+}
+
+// acc[c] += v * w[c], c < NW, reading w (16-byte aligned) in 16-byte pieces
+// for FP64 / FP32 elements; the FMAs are the scalar loop's, in its order.
+template <typename R, int NW>
+__device__ __forceinline__ void wrow_mad(R v, const R *w, R (&acc)[NW]) {
+  if constexpr (std::is_same<R, double>::value && NW % 2 == 0) {
+#pragma unroll
+    for (int c = 0; c < NW; c += 2) {
+      const double2 x = *reinterpret_cast<const double2 *>(w + c);
+      acc[c] = mad(v, x.x, acc[c]);
+      acc[c + 1] = mad(v, x.y, acc[c + 1]);
+    }
+  } else if constexpr (std::is_same<R, float>::value && NW % 4 == 0) {
+#pragma unroll
+    for (int c = 0; c < NW; c += 4) {
+      const float4 x = *reinterpret_cast<const float4 *>(w + c);
+      acc[c] = mad(v, x.x, acc[c]);
+      acc[c + 1] = mad(v, x.y, acc[c + 1]);
+      acc[c + 2] = mad(v, x.z, acc[c + 2]);
+      acc[c + 3] = mad(v, x.w, acc[c + 3]);
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < NW; ++c) acc[c] = mad(v, w[c], acc[c]);
+  }
 }
 
 // Apply to the strip of columns [c0, c0 + NW) (clamped to ncols).
@@ -154,24 +182,57 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
 
     // Phase 1: W[p, c] = (A1 or C1 row) + sum_rr conj(V[rr, p]) * C[r0 + rr, c]
     // (mode 0 needs the unit-lower test only when V is read from global).
+    // Entries e and e + TQR_THREADS have the same p when kb divides
+    // TQR_THREADS: one pass computes both, reading V's column once and
+    // running four independent FMA chains; each entry keeps its own two-chain
+    // summation order, so the result does not depend on the pairing.
     const bool vtri = (a.mode == 0) && !a.stage_v;
     const bool vtt = ttb && !a.stage_v;          // unstaged TT V: bound each column's rows
-    for (int e = tid; e < kb * nwl; e += TQR_THREADS) {
+    const int ne1 = kb * nwl;
+    const bool pair = (TQR_THREADS % kb) == 0;
+    auto finish_w = [&](int p, int c, R w) {
+      if (a.mode == 1) w += conj_if(ldg_cg(A1g + (size_t)(i + p) * a.a_rs + (size_t)c * a.a_cs), cjc);
+      Ws[p + c * ldw] = w;
+    };
+    for (int e = tid; e < ne1; e += (pair ? 2 : 1) * TQR_THREADS) {
       const int p = e % kb, c = e / kb;
-      R acc0 = 0, acc1 = 0;
       const R *vcol = Vp + (size_t)p * ldvp;
       const R *ccol = Cp + (size_t)r0 * crs + (size_t)c * ccs;
       const int Lp = vtt ? vrows(p) : Lr;
       int rr = vtri ? p : 0;
-      if (vtri) { acc0 = conj_if(ccol[(size_t)p * crs], cjg); ++rr; }
-      for (; rr + 1 < Lp; rr += 2) {
-        acc0 = madc(vcol[rr], conj_if(ccol[(size_t)rr * crs], cjg), acc0);
-        acc1 = madc(vcol[rr + 1], conj_if(ccol[(size_t)(rr + 1) * crs], cjg), acc1);
+      if (pair && e + TQR_THREADS < ne1) {
+        const int c2 = (e + TQR_THREADS) / kb;
+        const R *ccol2 = Cp + (size_t)r0 * crs + (size_t)c2 * ccs;
+        R acc0 = 0, acc1 = 0, bcc0 = 0, bcc1 = 0;
+        if (vtri) {
+          acc0 = conj_if(ccol[(size_t)p * crs], cjg);
+          bcc0 = conj_if(ccol2[(size_t)p * crs], cjg);
+          ++rr;
+        }
+        for (; rr + 1 < Lp; rr += 2) {
+          const R v0 = vcol[rr], v1 = vcol[rr + 1];
+          acc0 = madc(v0, conj_if(ccol[(size_t)rr * crs], cjg), acc0);
+          acc1 = madc(v1, conj_if(ccol[(size_t)(rr + 1) * crs], cjg), acc1);
+          bcc0 = madc(v0, conj_if(ccol2[(size_t)rr * crs], cjg), bcc0);
+          bcc1 = madc(v1, conj_if(ccol2[(size_t)(rr + 1) * crs], cjg), bcc1);
+        }
+        if (rr < Lp) {
+          const R v0 = vcol[rr];
+          acc0 = madc(v0, conj_if(ccol[(size_t)rr * crs], cjg), acc0);
+          bcc0 = madc(v0, conj_if(ccol2[(size_t)rr * crs], cjg), bcc0);
+        }
+        finish_w(p, c, acc0 + acc1);
+        finish_w(p, c2, bcc0 + bcc1);
+      } else {
+        R acc0 = 0, acc1 = 0;
+        if (vtri) { acc0 = conj_if(ccol[(size_t)p * crs], cjg); ++rr; }
+        for (; rr + 1 < Lp; rr += 2) {
+          acc0 = madc(vcol[rr], conj_if(ccol[(size_t)rr * crs], cjg), acc0);
+          acc1 = madc(vcol[rr + 1], conj_if(ccol[(size_t)(rr + 1) * crs], cjg), acc1);
+        }
+        if (rr < Lp) acc0 = madc(vcol[rr], conj_if(ccol[(size_t)rr * crs], cjg), acc0);
+        finish_w(p, c, acc0 + acc1);
       }
-      if (rr < Lp) acc0 = madc(vcol[rr], conj_if(ccol[(size_t)rr * crs], cjg), acc0);
-      R w = acc0 + acc1;
-      if (a.mode == 1) w += conj_if(ldg_cg(A1g + (size_t)(i + p) * a.a_rs + (size_t)c * a.a_cs), cjc);
-      Ws[p + c * ldw] = w;
     }
     __syncthreads();
     // Phase 2: W := op(T) W, T upper triangular kb-by-kb, op(T) = T^H when
@@ -197,9 +258,11 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
       }
       return s0 + s1;
     };
+    // op(T) W is written back transposed, W^T[c, p] at c + p * NW, so that
+    // phase 3 reads the NW entries of one p contiguously
     const int ne = kb * nwl;
     if (w2buf) {
-      for (int e = tid; e < ne; e += TQR_THREADS) W2[(e % kb) + (e / kb) * ldw] = t_entry(e);
+      for (int e = tid; e < ne; e += TQR_THREADS) W2[(e / kb) + (e % kb) * NW] = t_entry(e);
       __syncthreads();
     } else {
       R reg[kW2Regs];
@@ -212,21 +275,23 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
 #pragma unroll
       for (int u = 0; u < kW2Regs; ++u) {
         const int e = tid + u * TQR_THREADS;
-        if (e < ne) Ws[(e % kb) + (e / kb) * ldw] = reg[u];
+        if (e < ne) Ws[(e / kb) + (e % kb) * NW] = reg[u];
       }
       __syncthreads();
     }
-    const R *Wf = w2buf ? W2 : Ws;
+    const R *Wf = w2buf ? W2 : Ws;     // W^T: entry (p, c) at c + p * NW
     // Phase 3: C[r0 + rr, c] -= sum_p V[rr, p] W[p, c];  mode 1: A1 rows -= W
     // (through the conjugated view when conj_c)
     if (a.mode == 1) {
       for (int e = tid; e < ne; e += TQR_THREADS) {
         const int p = e % kb, c = e / kb;
         R *dst = A1g + (size_t)(i + p) * a.a_rs + (size_t)c * a.a_cs;
-        *dst = ldg_cg(dst) - conj_if(Wf[p + c * ldw], cjc);
+        *dst = ldg_cg(dst) - conj_if(Wf[c + p * NW], cjc);
       }
     }
     if (nwl == NW) {
+      // 16-byte loads of W^T rows where the element type and alignment allow
+      const bool wvec = ((uintptr_t)Wf & 15) == 0;
       for (int rr = tid; rr < Lr; rr += TQR_THREADS) {
         R acc[NW];
 #pragma unroll
@@ -236,9 +301,13 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
         for (int p = pmin; p < pmax; ++p) {
           R v = Vp[rr + (size_t)p * ldvp];
           if (vtri && p == rr) v = R(1);
-          const R *wrow = Wf + p;
+          const R *wrow = Wf + (size_t)p * NW;
+          if (wvec) {
+            wrow_mad<R, NW>(v, wrow, acc);
+          } else {
 #pragma unroll
-          for (int c = 0; c < NW; ++c) acc[c] = mad(v, wrow[c * ldw], acc[c]);
+            for (int c = 0; c < NW; ++c) acc[c] = mad(v, wrow[c], acc[c]);
+          }
         }
         R *crow = Cp + (size_t)(r0 + rr) * crs;
 #pragma unroll
@@ -254,10 +323,10 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
         for (int p = pmin; p < pmax; ++p) {
           R v = Vp[rr + (size_t)p * ldvp];
           if (vtri && p == rr) v = R(1);
-          const R *wrow = Wf + p;
+          const R *wrow = Wf + (size_t)p * NW;
 #pragma unroll
           for (int c = 0; c < NW; ++c)
-            if (c < nwl) acc[c] = mad(v, wrow[c * ldw], acc[c]);
+            if (c < nwl) acc[c] = mad(v, wrow[c], acc[c]);
         }
         R *crow = Cp + (size_t)(r0 + rr) * crs;
 #pragma unroll
