@@ -139,22 +139,33 @@ __device__ bool column_step(const ColumnStep<E> &c, int i, int x0, int m, int nc
     }
   }
   __syncthreads();
-  // ---- rank-1 update of the columns right of i ----
+  // ---- rank-1 update of the columns right of i: one row per thread, its x
+  //      entry held in a register, the columns in order (no index division) ----
   {
-    const int ncol = nc - i - 1, rows = m - x0;
+    const int rows = m - x0;
     for (int j = i + 1 + tid; j < nc; j += TQR_THREADS) c.row[(size_t)j * c.rs] += c.d[j];
-    for (int idx = tid; idx < ncol * rows; idx += TQR_THREADS) {
-      const int rr = idx % rows, j = i + 1 + idx / rows;
-      E *pc = c.P + (size_t)j * c.ldp;
-      pc[x0 + rr] = mad(xcol[x0 + rr], c.d[j], pc[x0 + rr]);
+    for (int rr = tid; rr < rows; rr += TQR_THREADS) {
+      const E xv = xcol[x0 + rr];
+      E *pr = c.P + x0 + rr;
+#pragma unroll 4
+      for (int j = i + 1; j < nc; ++j) pr[(size_t)j * c.ldp] = mad(xv, c.d[j], pr[(size_t)j * c.ldp]);
     }
   }
-  // ---- T column i ----
+  // ---- T column i: T[p, i] = sum_{q = p}^{i-1} T[p, q] d[q], four partial
+  //      sums over q (mod 4) to shorten the dependent chain ----
   if (c.Ts) {
     for (int p = tid; p < i; p += TQR_THREADS) {
-      E acc = 0;
-      for (int q = p; q < i; ++q) acc = mad(c.Ts[p + (size_t)q * c.ldts], c.d[q], acc);
-      c.Ts[p + (size_t)i * c.ldts] = acc;
+      E a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+      const E *tp = c.Ts + p;
+      int q = p;
+      for (; q + 3 < i; q += 4) {
+        a0 = mad(tp[(size_t)q * c.ldts], c.d[q], a0);
+        a1 = mad(tp[(size_t)(q + 1) * c.ldts], c.d[q + 1], a1);
+        a2 = mad(tp[(size_t)(q + 2) * c.ldts], c.d[q + 2], a2);
+        a3 = mad(tp[(size_t)(q + 3) * c.ldts], c.d[q + 3], a3);
+      }
+      for (; q < i; ++q) a0 = mad(tp[(size_t)q * c.ldts], c.d[q], a0);
+      c.Ts[p + (size_t)i * c.ldts] = (a0 + a1) + (a2 + a3);
     }
     if (tid == 0) c.Ts[i + (size_t)i * c.ldts] = tv;
   }
