@@ -96,7 +96,44 @@ __device__ bool column_step(const ColumnStep<E> &c, int i, int x0, int m, int nc
   // ---- d_j for all j != i (j < i only when T is built) ----
   const int jlo = c.Ts ? 0 : i + 1;
   const int nj = nc - jlo;
-  if (nj > 0) {
+  if (nj > 0 && sizeof(S) == 4) {
+    // single precision: a warp per four columns, lanes over rows (stride 32),
+    // one shuffle reduction per column -- no shared-memory partials and one
+    // barrier less; the FP32 pipe makes the reduction's adds cheap
+    const int lane = tid & 31, warp = tid >> 5;
+    for (int jb = jlo + 4 * warp; jb < nc; jb += 4 * TQR_WARPS) {
+      E a[4];
+      const E *pcs[4];
+      int mjs[4];
+      int mmax = x0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int j = jb + u;
+        a[u] = E(0);
+        pcs[u] = c.P + (size_t)j * c.ldp;
+        mjs[u] = (j < nc && j != i) ? ((c.tt >= 0 && j < i) ? min(m, c.tt + j + 1) : m) : x0;
+        mmax = max(mmax, mjs[u]);
+      }
+      for (int r = x0 + lane; r < mmax; r += 32) {
+        const E xv = xcol[r];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (r < mjs[u]) a[u] = madc(xv, pcs[u][r], a[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = warp_sum(a[u]);
+      if (lane == 0) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int j = jb + u;
+          if (j >= nc || j == i) continue;
+          E acc = a[u];
+          if (j > i || (!tsqrt_form && j < i)) acc += c.row[(size_t)j * c.rs];
+          c.d[j] = dval(j, acc);
+        }
+      }
+    }
+  } else if (nj > 0) {
     if (nj <= TQR_THREADS) {
       const int G = TQR_THREADS / nj;          // row groups
       const int j = jlo + tid % nj, g = tid / nj;
