@@ -99,8 +99,10 @@ __device__ __forceinline__ void wrow_mad(R v, const R *w, R (&acc)[NW]) {
   }
 }
 
-// Apply to the strip of columns [c0, c0 + NW) (clamped to ncols).
-template <typename R, int NW>
+// Apply to the strip of columns [c0, c0 + NW) (clamped to ncols).  VEC:
+// 16-byte staging of C and V for FP32 elements (kernels with registers to
+// spare: the tensor-core tile kernel runs one CTA per SM).
+template <typename R, int NW, bool VEC = false>
 __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_raw)
 {
   const int tid = threadIdx.x;
@@ -125,7 +127,9 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
   const bool cjc = a.conj_c != 0;
   if (a.stage_c) {
     Cp = Cs; crs = 1; ccs = ldcs;
-    if (a.c_rs == 1) {
+    if (VEC && a.c_rs == 1 && cols16_ok(Cg, (size_t)a.c_cs, L)) {
+      stage_cols16_f32(Cg, (size_t)a.c_cs, L, nwl, Cs, ldcs, cjc);
+    } else if (a.c_rs == 1) {
       for (int idx = tid; idx < L * nwl; idx += TQR_THREADS) {
         int r = idx % L, c = idx / L;
         Cs[r + (size_t)c * ldcs] = conj_if(ldg_cg(Cg + (size_t)r + (size_t)c * a.c_cs), cjc);
@@ -153,7 +157,11 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
     // V block: element (rr, p) = reflector i+p at region row r0+rr
     const R *Vp;
     int ldvp;
-    if (a.stage_v) {
+    if (VEC && a.stage_v && a.mode == 1 && !ttb && cols16_ok(a.V + ix(0, i, a.ldv), (size_t)a.ldv, Lr)) {
+      // every row of every reflector is stored: a plain column-block copy
+      stage_cols16_f32(a.V + ix(0, i, a.ldv), (size_t)a.ldv, Lr, kb, Vs, ldvs, false);
+      Vp = Vs; ldvp = ldvs;
+    } else if (a.stage_v) {
       for (int idx = tid; idx < Lr * kb; idx += TQR_THREADS) {
         int rr = idx % Lr, p = idx / Lr;
         R v;
@@ -337,7 +345,9 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
     __syncthreads();
   }
   if (a.stage_c) {
-    if (a.c_rs == 1) {
+    if (VEC && a.c_rs == 1 && cols16_ok(Cg, (size_t)a.c_cs, L)) {
+      unstage_cols16_f32(Cs, ldcs, L, nwl, Cg, (size_t)a.c_cs, cjc);
+    } else if (a.c_rs == 1) {
       for (int idx = tid; idx < L * nwl; idx += TQR_THREADS) {
         int r = idx % L, c = idx / L;
         Cg[(size_t)r + (size_t)c * a.c_cs] = conj_if(Cs[r + (size_t)c * ldcs], cjc);

@@ -7,6 +7,9 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
+
+#include <type_traits>
 
 #define TQR_THREADS 256
 #define TQR_WARPS (TQR_THREADS / 32)
@@ -135,6 +138,87 @@ __device__ __forceinline__ cx<double> ldg_cg(const cx<double> *p) {
 __device__ __forceinline__ cx<float> ldg_cg(const cx<float> *p) {
   const float2 v = __ldcg(reinterpret_cast<const float2 *>(p));
   return cx<float>(v.x, v.y);
+}
+
+// ---------------------------------------------------------------------------
+// 16-byte staging of column blocks between global and shared memory.
+// A strided scalar loop (one load, one store per element) lets a warp wait out
+// the L2 latency once per element: the compiler cannot move a global load
+// above a shared store it cannot prove disjoint.  These copy an nr-by-ncl
+// column-major block with 16-byte global accesses, each thread issuing up to
+// kStageVec loads before its first store.  Preconditions (checked by
+// cols16_ok): the global block and its column stride are 16-byte aligned and
+// nr is a multiple of 16 / sizeof(E).  The shared side keeps any column
+// stride (odd strides avoid bank conflicts) and is written element by element.
+// ---------------------------------------------------------------------------
+constexpr int kStageVec = 4;
+
+// Used for FP32 elements only: an FP32 task is latency-bound on the one CTA a
+// TMEM kernel gets per SM, while the FP64 kernels run two CTAs per SM whose
+// DFMA work hides the scalar loop's waits (and have no registers to spare).
+template <typename E>
+__device__ __forceinline__ bool cols16_ok(const E *g, size_t ldg, int nr) {
+  constexpr int VE = 16 / sizeof(E);
+  return std::is_same<E, float>::value && ((uintptr_t)g & 15) == 0 && ((ldg * sizeof(E)) & 15) == 0 &&
+         nr % VE == 0;
+}
+
+// dst[r + c * ldd] = conj_if(src[r + c * lds], cj), r < nr, c < ncl
+template <typename E>
+__device__ __forceinline__ void stage_cols16(const E *src, size_t lds, int nr, int ncl, E *dst, int ldd, bool cj) {
+  constexpr int VE = 16 / sizeof(E);
+  const int per_col = nr / VE, nvec = per_col * ncl;
+  for (int base = threadIdx.x; base < nvec; base += kStageVec * TQR_THREADS) {
+    uint4 buf[kStageVec];
+#pragma unroll
+    for (int u = 0; u < kStageVec; ++u) {
+      const int idx = base + u * TQR_THREADS;
+      if (idx < nvec) {
+        const int c = idx / per_col, q = idx - c * per_col;
+        buf[u] = __ldcg(reinterpret_cast<const uint4 *>(src + (size_t)c * lds) + q);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kStageVec; ++u) {
+      const int idx = base + u * TQR_THREADS;
+      if (idx < nvec) {
+        const int c = idx / per_col, q = idx - c * per_col;
+        E e[VE];
+        memcpy(e, &buf[u], 16);
+        E *d = dst + (size_t)c * ldd + q * VE;
+#pragma unroll
+        for (int t = 0; t < VE; ++t) d[t] = conj_if(e[t], cj);
+      }
+    }
+  }
+}
+
+// dst[r + c * ldd] = conj_if(src[r + c * lds], cj) from shared src to global dst
+template <typename E>
+__device__ __forceinline__ void unstage_cols16(const E *src, int lds, int nr, int ncl, E *dst, size_t ldd, bool cj) {
+  constexpr int VE = 16 / sizeof(E);
+  const int per_col = nr / VE, nvec = per_col * ncl;
+  for (int idx = threadIdx.x; idx < nvec; idx += TQR_THREADS) {
+    const int c = idx / per_col, q = idx - c * per_col;
+    const E *s = src + (size_t)c * lds + q * VE;
+    E e[VE];
+#pragma unroll
+    for (int t = 0; t < VE; ++t) e[t] = conj_if(s[t], cj);
+    uint4 v;
+    memcpy(&v, e, 16);
+    reinterpret_cast<uint4 *>(dst + (size_t)c * ldd)[q] = v;
+  }
+}
+
+// The call sites: the 16-byte copies for FP32 elements (cols16_ok is false
+// for every other type, so these are never reached with one).
+template <typename E>
+__device__ __forceinline__ void stage_cols16_f32(const E *src, size_t lds, int nr, int ncl, E *dst, int ldd, bool cj) {
+  if constexpr (std::is_same<E, float>::value) stage_cols16(src, lds, nr, ncl, dst, ldd, cj);
+}
+template <typename E>
+__device__ __forceinline__ void unstage_cols16_f32(const E *src, int lds, int nr, int ncl, E *dst, size_t ldd, bool cj) {
+  if constexpr (std::is_same<E, float>::value) unstage_cols16(src, lds, nr, ncl, dst, ldd, cj);
 }
 
 // Householder scalars in NextLA's convention (src/geqr2.jl:37-68,

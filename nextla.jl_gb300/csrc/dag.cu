@@ -243,12 +243,12 @@ __device__ bool run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *
   auto tautile = [&](int r, int c) { return a.tau + ix(c * nb, r, a.ldtau); };
   if (it.type == IT_GB) {
     R *Ab = tile(k, k) + ix(b * ib, b * ib, a.lda);
-    panel_qr_cta<R>(nb - b * ib, ib, Ab, a.lda, tautile(k, k) + b * ib, ttile(k, k) + ix(0, b * ib, a.ldt),
+    panel_qr_cta<R, TC>(nb - b * ib, ib, Ab, a.lda, tautile(k, k) + b * ib, ttile(k, k) + ix(0, b * ib, a.ldt),
                     a.ldt, true, true, smem);
     return true;
   }
   if (it.type == IT_TB) {
-    tsqrt_block_cta<R>(nb, ib, tile(k, k) + ix(b * ib, b * ib, a.lda), a.lda, tile(i, k) + ix(0, b * ib, a.lda),
+    tsqrt_block_cta<R, TC>(nb, ib, tile(k, k) + ix(b * ib, b * ib, a.lda), a.lda, tile(i, k) + ix(0, b * ib, a.lda),
                        a.lda, ttile(i, k) + ix(0, b * ib, a.ldt), a.ldt, tautile(i, k) + b * ib, true, smem);
     return true;
   }
@@ -306,7 +306,7 @@ __device__ bool run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *
       p.T = ttile(i, k);
       break;
   }
-  apply_strip<R, NW>(p, s * NW, smem);
+  apply_strip<R, NW, TC>(p, s * NW, smem);
   return true;
 }
 

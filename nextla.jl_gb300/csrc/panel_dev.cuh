@@ -241,7 +241,8 @@ __host__ __device__ inline size_t tsqrt_smem(int m, int sb, bool staged) {
 }
 
 // geqr2 (+ T) on the m-by-nc panel A; T (nc-by-nc, ldt) may be nullptr.
-template <typename R>
+// VEC: 16-byte staging for FP32 elements (as apply_strip).
+template <typename R, bool VEC = false>
 __device__ void panel_qr_cta(int m, int nc, R *A, int lda, R *tau, R *T, int ldt, bool staged,
                              bool stage_t, unsigned char *smem_raw)
 {
@@ -261,9 +262,13 @@ __device__ void panel_qr_cta(int m, int nc, R *A, int lda, R *tau, R *T, int ldt
   if (staged) {
     c.ldp = odd_ld(m);
     c.P = carve<R>(sp, (size_t)c.ldp * nc);
-    for (int idx = tid; idx < m * nc; idx += TQR_THREADS) {
-      int r = idx % m, cc = idx / m;
-      c.P[ix(r, cc, c.ldp)] = ldg_cg(A + ix(r, cc, lda));
+    if (VEC && cols16_ok(A, (size_t)lda, m)) {
+      stage_cols16_f32(A, (size_t)lda, m, nc, c.P, c.ldp, false);
+    } else {
+      for (int idx = tid; idx < m * nc; idx += TQR_THREADS) {
+        int r = idx % m, cc = idx / m;
+        c.P[ix(r, cc, c.ldp)] = ldg_cg(A + ix(r, cc, lda));
+      }
     }
   } else {
     c.P = A;
@@ -284,9 +289,13 @@ __device__ void panel_qr_cta(int m, int nc, R *A, int lda, R *tau, R *T, int ldt
     column_step<R>(c, i, i + 1, m, nc, false, tau + i, true);
   }
   if (staged) {
-    for (int idx = tid; idx < m * nc; idx += TQR_THREADS) {
-      int r = idx % m, cc = idx / m;
-      A[ix(r, cc, lda)] = c.P[ix(r, cc, c.ldp)];
+    if (VEC && cols16_ok(A, (size_t)lda, m)) {
+      unstage_cols16_f32(c.P, c.ldp, m, nc, A, (size_t)lda, false);
+    } else {
+      for (int idx = tid; idx < m * nc; idx += TQR_THREADS) {
+        int r = idx % m, cc = idx / m;
+        A[ix(r, cc, lda)] = c.P[ix(r, cc, c.ldp)];
+      }
     }
   }
   if (T && stage_t) {
@@ -307,7 +316,7 @@ __device__ void panel_qr_cta(int m, int nc, R *A, int lda, R *tau, R *T, int ldt
 // triangular, block column i holds rows [0, tt + i] of A2 (tt = ii), so
 // column i's reflector uses rows [0, min(tt + i + 1, m)) and nothing below
 // the diagonal is read or written.
-template <typename R>
+template <typename R, bool VEC = false>
 __device__ void tsqrt_block_cta(int m, int sb, R *A1, int lda1, R *A2, int lda2, R *T, int ldt,
                                 R *tau, bool staged, unsigned char *smem_raw, int tt = -1)
 {
@@ -333,9 +342,13 @@ __device__ void tsqrt_block_cta(int m, int sb, R *A1, int lda1, R *A2, int lda2,
   if (staged) {
     c.ldp = odd_ld(mrow);
     c.P = carve<R>(sp, (size_t)c.ldp * sb);
-    for (int idx = tid; idx < mrow * sb; idx += TQR_THREADS) {
-      int r = idx % mrow, cc = idx / mrow;
-      c.P[ix(r, cc, c.ldp)] = in_tri(r, cc) ? ldg_cg(A2 + ix(r, cc, lda2)) : R(0);
+    if (VEC && tt < 0 && cols16_ok(A2, (size_t)lda2, mrow)) {
+      stage_cols16_f32(A2, (size_t)lda2, mrow, sb, c.P, c.ldp, false);
+    } else {
+      for (int idx = tid; idx < mrow * sb; idx += TQR_THREADS) {
+        int r = idx % mrow, cc = idx / mrow;
+        c.P[ix(r, cc, c.ldp)] = in_tri(r, cc) ? ldg_cg(A2 + ix(r, cc, lda2)) : R(0);
+      }
     }
   } else {
     c.P = A2;
@@ -356,9 +369,13 @@ __device__ void tsqrt_block_cta(int m, int sb, R *A1, int lda1, R *A2, int lda2,
     }
   }
   if (staged) {
-    for (int idx = tid; idx < mrow * sb; idx += TQR_THREADS) {
-      int r = idx % mrow, cc = idx / mrow;
-      if (in_tri(r, cc)) A2[ix(r, cc, lda2)] = c.P[ix(r, cc, c.ldp)];
+    if (VEC && tt < 0 && cols16_ok(A2, (size_t)lda2, mrow)) {
+      unstage_cols16_f32(c.P, c.ldp, mrow, sb, A2, (size_t)lda2, false);
+    } else {
+      for (int idx = tid; idx < mrow * sb; idx += TQR_THREADS) {
+        int r = idx % mrow, cc = idx / mrow;
+        if (in_tri(r, cc)) A2[ix(r, cc, lda2)] = c.P[ix(r, cc, c.ldp)];
+      }
     }
   }
   __syncthreads();
