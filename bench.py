@@ -1054,27 +1054,48 @@ def main():
         hT = torch.empty((ts[1], ts[0]), dtype=torch.float64).pin_memory()
         Ad = tq.empty(n, n)
 
-        def e2e_step():
+        phase_ev = []
+
+        def e2e_step(record=False):
+            evs = [torch.cuda.Event(enable_timing=True) for _ in range(4)] if record else None
+            if record:
+                evs[0].record(st)
             Ad.t().copy_(hA, non_blocking=True)         # H2D of the input matrix
+            if record:
+                evs[1].record(st)
             tq.tile_geqrf(Ad, NB, IB, T, tau)
+            if record:
+                evs[2].record(st)
             hOut.copy_(Ad.t(), non_blocking=True)       # D2H of R and V
             hT.copy_(T.t(), non_blocking=True)          # D2H of T
+            if record:
+                evs[3].record(st)
+                phase_ev.append(evs)
         for _ in range(2):
             e2e_step()
         torch.cuda.synchronize()
         ks = max(1, min(args.steps, 3))
+        eclk = Clocks(torch.cuda.current_device())
+        eclk.start()
         barrier(world)
         f0 = torch.cuda.Event(enable_timing=True)
         f1 = torch.cuda.Event(enable_timing=True)
         f0.record(st)
+        marks = []
         for _ in range(ks):
-            e2e_step()
+            e2e_step(record=True)
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record(st)
+            marks.append(ev)
         f1.record(st)
         torch.cuda.synchronize()
         ems = reduce_max(f0.elapsed_time(f1), world)
+        steps_ms = [f0.elapsed_time(marks[0])] + [marks[q].elapsed_time(marks[q + 1]) for q in range(ks - 1)]
         e2e = {"value": flops * world * ks / (ems / 1e3) / 1e12, "unit": UNIT,
                "h2d_bytes_per_step": 8 * n * n, "d2h_bytes_per_step": 8 * n * n + 8 * ts[0] * ts[1],
-               "steps": ks, "ms_per_step": ems / ks}
+               "steps": ks, "ms_per_step": ems / ks, "step_ms": steps_ms, "clocks": eclk.stop(),
+               "phase_ms_median": {nm: statistics.median(e[q].elapsed_time(e[q + 1]) for e in phase_ev)
+                                   for q, nm in enumerate(("h2d", "factor", "d2h"))}}
 
     # roofline of the dominant kernel (the trailing update: band tsmqr/unmqr)
     peak = fp64_peak(_lib, torch)

@@ -119,7 +119,17 @@ k_gemm_sd_n(int m, int n, const float *__restrict__ A, int lda, const double *__
         float sh[K], sl[K];
 #pragma unroll
         for (int c = 0; c < K; ++c) sh[c] = sl[c] = 0.0f;
-        for (int jj = g0; jj < g1; ++jj) {
+        int jj = g0;
+        for (; jj + 8 <= g1; jj += 8) {    // eight loads of A in flight, then their terms in order
+          float av[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) av[u] = __ldg(ap + (size_t)(jj + u) * lda);
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+#pragma unroll
+            for (int c = 0; c < K; ++c) df_mad(av[u], Xh[jj + u][c], Xl[jj + u][c], sh[c], sl[c]);
+        }
+        for (; jj < g1; ++jj) {
           const float a = __ldg(ap + (size_t)jj * lda);
 #pragma unroll
           for (int c = 0; c < K; ++c) df_mad(a, Xh[jj][c], Xl[jj][c], sh[c], sl[c]);
@@ -162,7 +172,18 @@ k_gemm_sd_t(int m, int n, const float *__restrict__ A, int lda, const double *__
       float sh[K], sl[K];
 #pragma unroll
       for (int c = 0; c < K; ++c) sh[c] = sl[c] = 0.0f;
-      for (int rr = g0 + lane; rr < g1; rr += 32) {
+      int rr = g0 + lane;
+      for (; rr + 7 * 32 < g1; rr += 8 * 32) {    // eight loads of A in flight, then their terms in order
+        float av[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) av[u] = __ldg(ap + rr + 32 * u);
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+#pragma unroll
+          for (int c = 0; c < K; ++c)
+            df_mad(av[u], Rh[rr + 32 * u + c * rchunk], Rl[rr + 32 * u + c * rchunk], sh[c], sl[c]);
+      }
+      for (; rr < g1; rr += 32) {
         const float a = __ldg(ap + rr);
 #pragma unroll
         for (int c = 0; c < K; ++c) df_mad(a, Rh[rr + c * rchunk], Rl[rr + c * rchunk], sh[c], sl[c]);
@@ -265,7 +286,7 @@ template <int K>
 static int gemm_sd_n_k(int m, int n, const float *A, int lda, const double *X, int ldx, double *Y, int ldy,
                        double alpha, cudaStream_t st) {
   const int gx = (m + TQR_THREADS - 1) / TQR_THREADS;
-  int gy = std::max(1, std::min((n + 255) / 256, (4 * 152 + gx - 1) / gx));
+  int gy = std::max(1, std::min((n + 255) / 256, (8 * 152 + gx - 1) / gx));
   const int jchunk = ((n + gy - 1) / gy + 255) / 256 * 256;
   gy = (n + jchunk - 1) / jchunk;
   k_gemm_sd_n<K><<<dim3(gx, gy), TQR_THREADS, 0, st>>>(m, n, A, lda, X, ldx, Y, ldy, alpha, jchunk);
