@@ -440,9 +440,11 @@ int tqr_stile_gels(int m, int n, int nrhs, int nb, int ib, float *A, int lda, fl
  * mixed precision as future work) ----
  * min ||A X - B|| for a Float32 A (m-by-n, m >= n, lda) and Float64 B
  * (m-by-nrhs, nrhs <= 16): tile QR of a copy of A in FP32 (persistent kernel
- * when m, n are multiples of nb), X0 = R^-1 (Q^T B)[0:n] in FP32, then CGLS in
- * FP64 on the right-preconditioned problem min ||A R^-1 Y - B|| (X = R^-1 Y),
- * every product with A in FP64 on A's FP32 entries.  Stops when the
+ * when m, n are multiples of nb), X0 = R^-1 (Q^T B)[0:n] in FP32, then CGLS
+ * with FP64 iterates on the right-preconditioned problem min ||A R^-1 Y - B||
+ * (X = R^-1 Y): every product with A uses A's FP32 entries exactly and sums in
+ * double-float on the FP32 pipe (~2^-48 relative per 32 terms, flushed to
+ * FP64), every solve with R runs in FP64.  Stops when the
  * preconditioned normal-equation residual of every column has dropped by
  * `tol` or after `maxit` iterations; `iters` and `relres` (that ratio) report
  * where it stopped.  A and B are not modified.  `work` (256-byte aligned) holds

@@ -624,9 +624,10 @@ def tile_gels(A, B, nb=256, ib=32):
 # ---- mixed-precision least squares -----------------------------------------
 
 def lstsq_mixed(A32, B, nb=256, ib=32, maxit=50, tol=1e-13):
-    """min ||A X - B|| for a float32 A and float64 B: FP32 tile QR, FP64 CGLS
-    refinement preconditioned by R (tqr_dsgels).  Returns (X, iterations,
-    relative preconditioned residual reached).  A and B are left unchanged."""
+    """min ||A X - B|| for a float32 A and float64 B: FP32 tile QR, then CGLS
+    with FP64 iterates preconditioned by R, its products with A summed in
+    double-float (tqr_dsgels).  Returns (X, iterations, relative
+    preconditioned residual reached).  A and B are left unchanged."""
     import ctypes
     if A32.dtype != torch.float32 or B.dtype != torch.float64:
         raise TypeError("lstsq_mixed wants a float32 A and a float64 B")
