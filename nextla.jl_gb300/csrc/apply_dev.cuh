@@ -177,10 +177,15 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
     }
     const R *Tp;
     int ldtp;
+    // Staged T is column-major for op(T) = T and row-major for op(T) = T^H:
+    // phase 2 then reads, for fixed q, entries that are consecutive across the
+    // lanes (p), free of shared-memory bank conflicts.
     if (a.stage_t) {
       for (int idx = tid; idx < kb * kb; idx += TQR_THREADS) {
         int p = idx % kb, q = idx / kb;
-        Ts[p + q * ib] = (p <= q) ? ldg_cg(a.T + ix(p, i + q, a.ldt)) : R(0);
+        const R t = (p <= q) ? ldg_cg(a.T + ix(p, i + q, a.ldt)) : R(0);
+        if (a.transT) Ts[q + p * ib] = t;
+        else Ts[p + q * ib] = t;
       }
       Tp = Ts; ldtp = ib;
     } else {
@@ -250,12 +255,14 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
       const R *wc = Ws + c * ldw;
       R s0 = 0, s1 = 0;
       if (a.transT) {
+        // T(q, p): row-major when staged, column-major in global memory
+        const size_t rs = a.stage_t ? (size_t)ib : 1, cs = a.stage_t ? 1 : (size_t)ldtp;
         int q = 0;
         for (; q + 1 <= p; q += 2) {
-          s0 = madc(Tp[q + (size_t)p * ldtp], wc[q], s0);
-          s1 = madc(Tp[q + 1 + (size_t)p * ldtp], wc[q + 1], s1);
+          s0 = madc(Tp[q * rs + p * cs], wc[q], s0);
+          s1 = madc(Tp[(q + 1) * rs + p * cs], wc[q + 1], s1);
         }
-        if (q <= p) s0 = madc(Tp[q + (size_t)p * ldtp], wc[q], s0);
+        if (q <= p) s0 = madc(Tp[q * rs + p * cs], wc[q], s0);
       } else {
         int q = p;
         for (; q + 1 < kb; q += 2) {
