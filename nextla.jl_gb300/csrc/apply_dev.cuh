@@ -99,6 +99,41 @@ __device__ __forceinline__ void wrow_mad(R v, const R *w, R (&acc)[NW]) {
   }
 }
 
+// Phase 1 of a full FP32 block (256 staged rows, 32 reflectors, 16 columns)
+// with register blocking: warp g takes rows [32 g, 32 g + 32), lane t a 4 x 4
+// block of W (reflectors 4 (t % 8) .., columns 4 (t / 8) ..), so each shared
+// load feeds four FMAs; part[g * 512 + p + 32 c] receives the row group's sum.
+// Used by the tensor-core instantiation, whose one CTA per SM leaves phase 1
+// bound by shared-memory load throughput.
+__device__ __forceinline__ void phase1_blocked_f32(const float *Vp, int ldvp, const float *Cp, int ccs, float *part) {
+  const int g = threadIdx.x >> 5, t = threadIdx.x & 31;
+  const int p0 = 4 * (t & 7), c0 = 4 * (t >> 3);
+  float acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int w = 0; w < 4; ++w) acc[u][w] = 0.0f;
+  const float *v0 = Vp + (size_t)p0 * ldvp, *cp0 = Cp + (size_t)c0 * ccs;
+#pragma unroll 4
+  for (int rr = 32 * g; rr < 32 * g + 32; ++rr) {
+    float v[4], c[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      v[u] = v0[rr + (size_t)u * ldvp];
+      c[u] = cp0[rr + (size_t)u * ccs];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int w = 0; w < 4; ++w) acc[u][w] = fmaf(v[u], c[w], acc[u][w]);
+  }
+  float *pg = part + (size_t)g * 512;
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int w = 0; w < 4; ++w) pg[(p0 + u) + 32 * (c0 + w)] = acc[u][w];
+}
+
 // Apply to the strip of columns [c0, c0 + NW) (clamped to ncols).  VEC:
 // 16-byte staging of C and V for FP32 elements (kernels with registers to
 // spare: the tensor-core tile kernel runs one CTA per SM).
@@ -207,7 +242,24 @@ __device__ void apply_strip(const ApplyArgs<R> &a, int c0, unsigned char *smem_r
       if (a.mode == 1) w += conj_if(ldg_cg(A1g + (size_t)(i + p) * a.a_rs + (size_t)c * a.a_cs), cjc);
       Ws[p + c * ldw] = w;
     };
-    for (int e = tid; e < ne1; e += (pair ? 2 : 1) * TQR_THREADS) {
+    bool blocked = false;
+    if constexpr (VEC && std::is_same<R, float>::value && NW == 16) {
+      // tensor-core instantiation: 16 x 32 W of a full 256-row block through
+      // 4 x 4 register blocks; the eight row-group sums are added in order
+      if (a.mode == 1 && !ttb && kb == 32 && nwl == 16 && Lr == 256 && a.stage_v && a.stage_c && !cjg) {
+        float *part = Vs + (size_t)ldvs * ib;     // 8 x 512 partial sums after the staged V
+        phase1_blocked_f32(Vp, ldvp, Cp, ccs, part);
+        __syncthreads();
+        for (int e = tid; e < 512; e += TQR_THREADS) {
+          float w = 0.0f;
+#pragma unroll
+          for (int g = 0; g < 8; ++g) w += part[g * 512 + e];
+          finish_w(e % 32, e / 32, w);
+        }
+        blocked = true;
+      }
+    }
+    for (int e = blocked ? ne1 : tid; e < ne1; e += (pair ? 2 : 1) * TQR_THREADS) {
       const int p = e % kb, c = e / kb;
       const R *vcol = Vp + (size_t)p * ldvp;
       const R *ccol = Cp + (size_t)r0 * crs + (size_t)c * ccs;
