@@ -120,12 +120,12 @@ k_gemm_sd_n(int m, int n, const float *__restrict__ A, int lda, const double *__
 #pragma unroll
         for (int c = 0; c < K; ++c) sh[c] = sl[c] = 0.0f;
         int jj = g0;
-        for (; jj + 8 <= g1; jj += 8) {    // eight loads of A in flight, then their terms in order
-          float av[8];
+        for (; jj + 16 <= g1; jj += 16) {    // sixteen loads of A in flight, then their terms in order
+          float av[16];
 #pragma unroll
-          for (int u = 0; u < 8; ++u) av[u] = __ldg(ap + (size_t)(jj + u) * lda);
+          for (int u = 0; u < 16; ++u) av[u] = __ldg(ap + (size_t)(jj + u) * lda);
 #pragma unroll
-          for (int u = 0; u < 8; ++u)
+          for (int u = 0; u < 16; ++u)
 #pragma unroll
             for (int c = 0; c < K; ++c) df_mad(av[u], Xh[jj + u][c], Xl[jj + u][c], sh[c], sl[c]);
         }
@@ -318,9 +318,10 @@ static int gemm_sd_n(int m, int n, int k, const float *A, int lda, const double 
 template <int K>
 static int gemm_sd_t_k(int m, int n, const float *A, int lda, const double *R, int ldr, double *Z, int ldz,
                        double alpha, cudaStream_t st) {
-  const int rchunk = 1024, cols = 64;
+  const int rchunk = 2048, cols = 64;
   dim3 grid((m + rchunk - 1) / rchunk, (n + cols - 1) / cols);
-  const size_t sm = 2 * sizeof(float) * rchunk * K;
+  const size_t sm = 2 * sizeof(float) * rchunk * K;   // 64 KB at K = 4: above the default limit
+  LS_CU(cudaFuncSetAttribute(k_gemm_sd_t<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   k_gemm_sd_t<K><<<grid, TQR_THREADS, sm, st>>>(m, n, A, lda, R, ldr, Z, ldz, alpha, rchunk, cols);
   count_launch();
   return (int)cudaGetLastError();
