@@ -30,6 +30,61 @@ static int imin(int a, int b) { return a < b ? a : b; }
 static int imax(int a, int b) { return a > b ? a : b; }
 
 /* ------------------------------------------------------------------------ */
+/* Host BLAS (optional).  NextLA's larfb! forms its products with           */
+/* LinearAlgebra.mul! / trmm (src/larfb.jl:66-98), which run in the host    */
+/* BLAS on CPU arrays, and pamm!/parfb!'s products (src/pamm.jl:120-126,    */
+/* 310-312; src/parfb.jl:125) are the same GEMM/TRMM shapes.  When a caller  */
+/* registers the Fortran-ABI dgemm/dtrmm of a host BLAS (the Python front    */
+/* end takes them from scipy.linalg.cython_blas), larfb and the l = 0      */
+/* forward parfb run those steps in that BLAS and the flat tile driver     */
+/* applies each panel's reflectors to the whole trailing row block in one  */
+/* call (tsmqr!/unmqr! on a wider A1/A2: column by column the same         */
+/* operations), letting the BLAS use every host thread.  Only the order of  */
+/* the sums inside a product changes.  With nothing registered (the         */
+/* default, used by the golden-vector tests) every routine runs its plain  */
+/* loops.                                                                   */
+/* ------------------------------------------------------------------------ */
+typedef void (*ora_dgemm_fn)(const char *, const char *, const int *, const int *, const int *,
+                             const double *, const double *, const int *, const double *,
+                             const int *, const double *, double *, const int *);
+typedef void (*ora_dtrmm_fn)(const char *, const char *, const char *, const char *, const int *,
+                             const int *, const double *, const double *, const int *, double *,
+                             const int *);
+static ora_dgemm_fn g_dgemm = NULL;
+static ora_dtrmm_fn g_dtrmm = NULL;
+
+/* Registers (both non-NULL) or clears (both NULL) the host BLAS. */
+int ora_set_host_blas(void *dgemm, void *dtrmm)
+{
+    if ((dgemm == NULL) != (dtrmm == NULL)) return -1;
+    g_dgemm = (ora_dgemm_fn)dgemm;
+    g_dtrmm = (ora_dtrmm_fn)dtrmm;
+    return 0;
+}
+
+int ora_host_blas_on(void) { return g_dgemm != NULL; }
+
+static void bgemm(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
+                  const double *B, int ldb, double beta, double *C, int ldc)
+{
+    if (m <= 0 || n <= 0) return;
+    if (k <= 0) {
+        if (beta == 0.0)
+            for (int c = 0; c < n; ++c) for (int r = 0; r < m; ++r) C[IDX(r, c, ldc)] = 0.0;
+        return;
+    }
+    g_dgemm(&ta, &tb, &m, &n, &k, &alpha, A, &lda, B, &ldb, &beta, C, &ldc);
+}
+
+static void btrmm(char side, char uplo, char ta, char diag, int m, int n, const double *A, int lda,
+                  double *B, int ldb)
+{
+    if (m <= 0 || n <= 0) return;
+    const double one = 1.0;
+    g_dtrmm(&side, &uplo, &ta, &diag, &m, &n, &one, A, &lda, B, &ldb);
+}
+
+/* ------------------------------------------------------------------------ */
 /* geqr2: unblocked Householder QR (src/geqr2.jl:23-105)                      */
 /* ------------------------------------------------------------------------ */
 int ora_dgeqr2(int m, int n, double *A, int lda, double *tau, double *work)
@@ -202,6 +257,33 @@ int ora_dlarfb(char side, char trans, char direct, char storev, int m, int n, in
 #define Wm(r, c) W[IDX(r, c, ldw)]
     int rows = (side == 'L') ? n : m;                       /* W rows */
     int len = (side == 'L') ? m : n;                        /* order of H */
+    if (g_dgemm) {
+        /* the same seven steps (larfb.jl:66-98 for 'L', :107-141 for 'R')
+           with the products in the host BLAS */
+        int useTH = (side == 'L') ? (trans == 'N') : (trans != 'N');
+        for (int p = 0; p < k; ++p)
+            for (int r = 0; r < rows; ++r) Wm(r, p) = (side == 'L') ? Cm(p, r) : Cm(r, p);
+        btrmm('R', 'L', 'N', 'U', rows, k, V, ldv, W, ldw);              /* W V1 */
+        if (len > k) {
+            if (side == 'L')
+                bgemm('T', 'N', rows, k, len - k, 1.0, C + k, ldc, V + k, ldv, 1.0, W, ldw);
+            else
+                bgemm('N', 'N', rows, k, len - k, 1.0, C + IDX(0, k, ldc), ldc, V + k, ldv, 1.0, W, ldw);
+        }
+        btrmm('R', 'U', useTH ? 'T' : 'N', 'N', rows, k, T, ldt, W, ldw); /* W op(T) */
+        if (len > k) {
+            if (side == 'L')
+                bgemm('N', 'T', len - k, rows, k, -1.0, V + k, ldv, W, ldw, 1.0, C + k, ldc);
+            else
+                bgemm('N', 'T', rows, len - k, k, -1.0, W, ldw, V + k, ldv, 1.0, C + IDX(0, k, ldc), ldc);
+        }
+        btrmm('R', 'L', 'T', 'U', rows, k, V, ldv, W, ldw);              /* W V1^H */
+        for (int p = 0; p < k; ++p)
+            for (int r = 0; r < rows; ++r) {
+                if (side == 'L') Cm(p, r) -= Wm(r, p); else Cm(r, p) -= Wm(r, p);
+            }
+        return 0;
+    }
     double *tmp = (double *)malloc(sizeof(double) * (size_t)k);
     if (!tmp) return -100;
     /* W := C1^H (L) or C1 (R) */
@@ -353,6 +435,27 @@ static void parfb_lv(char side, char trans, int m2, int n2, int k, int l,
 #define Tm(r, c) T[IDX(r, c, ldt)]
 #define Wm(r, c) W[IDX(r, c, ldw)]
     int tr = (trans != 'N');                                /* tfun = adjoint */
+    if (g_dgemm && l == 0) {
+        /* the same four steps with the products in the host BLAS */
+        if (side == 'L') {
+            bgemm('T', 'N', k, n2, m2, 1.0, V, ldv, A2, lda2, 0.0, W, ldw);   /* W = V^H A2 */
+            for (int c = 0; c < n2; ++c)
+                for (int p = 0; p < k; ++p) Wm(p, c) += A1m(p, c);
+            btrmm('L', 'U', tr ? 'T' : 'N', 'N', k, n2, T, ldt, W, ldw);      /* W = op(T) W */
+            for (int c = 0; c < n2; ++c)
+                for (int p = 0; p < k; ++p) A1m(p, c) -= Wm(p, c);
+            bgemm('N', 'N', m2, n2, k, -1.0, V, ldv, W, ldw, 1.0, A2, lda2);  /* A2 -= V W */
+        } else {
+            bgemm('N', 'N', m2, k, n2, 1.0, A2, lda2, V, ldv, 0.0, W, ldw);   /* W = A2 V */
+            for (int p = 0; p < k; ++p)
+                for (int r = 0; r < m2; ++r) Wm(r, p) += A1m(r, p);
+            btrmm('R', 'U', tr ? 'T' : 'N', 'N', m2, k, T, ldt, W, ldw);      /* W = W op(T) */
+            for (int p = 0; p < k; ++p)
+                for (int r = 0; r < m2; ++r) A1m(r, p) -= Wm(r, p);
+            bgemm('N', 'T', m2, n2, k, -1.0, W, ldw, V, ldv, 1.0, A2, lda2);  /* A2 -= W V^H */
+        }
+        return;
+    }
     if (side == 'L') {
         /* pamm 'W': W[1:k,1:n2] = V^H A2; W[i,:] += A1[i,:]  (pamm.jl:120-126) */
         for (int c = 0; c < n2; ++c)
@@ -595,7 +698,10 @@ int ora_dtile_geqrf(int m, int n, int nb, int ib, double *A, int lda, double *T,
     if (lda < m) return -6;
     if (ldt < MT * ib) return -8;
     if (ldtau < n) return -10;
-    double *work = (double *)malloc(sizeof(double) * (size_t)nb * (size_t)nb);
+    const int wide = (g_dgemm != NULL);
+    size_t wsize = (size_t)nb * (size_t)nb;
+    if (wide && (size_t)ib * (size_t)n > wsize) wsize = (size_t)ib * (size_t)n;
+    double *work = (double *)malloc(sizeof(double) * wsize);
     double *tv = (double *)malloc(sizeof(double) * (size_t)nb);
     if (!work || !tv) { free(work); free(tv); return -100; }
     int KT = imin(MT, NT);
@@ -605,10 +711,31 @@ int ora_dtile_geqrf(int m, int n, int nb, int ib, double *A, int lda, double *T,
         double *Tkk = T + IDX(k * ib, k * nb, ldt);
         ora_dgeqrt(mk, nk, ib, Akk, lda, Tkk, ldt, tv, work);
         for (int c = 0; c < imin(mk, nk); ++c) tau[IDX(k * nb + c, k, ldtau)] = tv[c];
+        if (wide) {
+            /* host BLAS registered: one unmqr!/tsmqr! per panel tile over the
+               whole trailing row block (every column sees the same steps as
+               in the per-tile calls below; the BLAS threads over columns) */
+            int nt = n - (k + 1) * nb;
+            if (nt > 0)
+                ora_dunmqr('L', 'C', mk, nt, imin(mk, nk), ib, Akk, lda, mk, nk, Tkk, ldt,
+                           A + IDX(k * nb, (k + 1) * nb, lda), lda, work, nt);
+            for (int i = k + 1; i < MT; ++i) {
+                int mi = imin(nb, m - i * nb);
+                double *Aik = A + IDX(i * nb, k * nb, lda);
+                double *Tik = T + IDX(i * ib, k * nb, ldt);
+                ora_dtsqrt(mi, nk, ib, mk, Akk, lda, Aik, lda, Tik, ldt, tv, work);
+                for (int c = 0; c < imin(mk, nk); ++c) tau[IDX(k * nb + c, i, ldtau)] = tv[c];
+                if (nt > 0)
+                    ora_dtsmqr('L', 'C', mk, nt, mi, nt, imin(mk, nk), ib, imin(mk, nk),
+                               A + IDX(k * nb, (k + 1) * nb, lda), lda, A + IDX(i * nb, (k + 1) * nb, lda),
+                               lda, Aik, lda, Tik, ldt, work);
+            }
+            continue;
+        }
         /* Tiles of different columns are independent: with OpenMP the column
            loops run on all host threads (each call keeps its serial order, so
            the result does not depend on the thread count). */
-#pragma omp parallel for schedule(dynamic)
+#pragma omp parallel for schedule(dynamic) if (!g_dgemm)
         for (int j = k + 1; j < NT; ++j) {
             int nj = imin(nb, n - j * nb);
             double *w = (double *)malloc(sizeof(double) * (size_t)nb * (size_t)nb);
@@ -622,7 +749,7 @@ int ora_dtile_geqrf(int m, int n, int nb, int ib, double *A, int lda, double *T,
             double *Tik = T + IDX(i * ib, k * nb, ldt);
             ora_dtsqrt(mi, nk, ib, mk, Akk, lda, Aik, lda, Tik, ldt, tv, work);
             for (int c = 0; c < imin(mk, nk); ++c) tau[IDX(k * nb + c, i, ldtau)] = tv[c];
-#pragma omp parallel for schedule(dynamic)
+#pragma omp parallel for schedule(dynamic) if (!g_dgemm)
             for (int j = k + 1; j < NT; ++j) {
                 int nj = imin(nb, n - j * nb);
                 double *w = (double *)malloc(sizeof(double) * (size_t)nb * (size_t)nb);
@@ -869,7 +996,7 @@ int ora_dtile_geqrf_hqr(int m, int n, int nb, int ib, int grp, double *A, int ld
         int MTt = rag ? MT - 1 : MT;             /* tiles the groups hold */
         int last = k + ((MTt - 1 - k) / grp) * grp;   /* last group leader */
         /* geqrt of every leader and unmqr of its row */
-#pragma omp parallel for schedule(dynamic)
+#pragma omp parallel for schedule(dynamic) if (!g_dgemm)
         for (int i = k; i < MTt; i += grp) {
             int mi = imin(nb, m - i * nb), kk = imin(mi, nk);
             double *w = (double *)malloc(sizeof(double) * (size_t)nb * (size_t)nb);
@@ -889,7 +1016,7 @@ int ora_dtile_geqrf_hqr(int m, int n, int nb, int ib, int grp, double *A, int ld
         /* flat reduction inside each group: tile i + d into leader i; the
            ragged tile after the others, into the last leader */
         for (int d = 1; d <= grp; ++d) {
-#pragma omp parallel for schedule(dynamic)
+#pragma omp parallel for schedule(dynamic) if (!g_dgemm)
             for (int i = k; i < MTt; i += grp) {
                 int p = (d < grp) ? i + d : (rag && i == last ? MT - 1 : -1);
                 if (p < 0 || (d < grp && p >= MTt)) continue;
@@ -912,7 +1039,7 @@ int ora_dtile_geqrf_hqr(int m, int n, int nb, int ib, int grp, double *A, int ld
         }
         /* binary tree over the leaders */
         for (int s = grp; k + s < MTt; s *= 2) {
-#pragma omp parallel for schedule(dynamic)
+#pragma omp parallel for schedule(dynamic) if (!g_dgemm)
             for (int i = k; i < MTt - s; i += 2 * s) {
                 int p = i + s;
                 int mp = imin(nb, m - p * nb), kt = imin(mp, nk);

@@ -73,6 +73,8 @@ def _declare(L):
         "ora_dpamm": [_C, _C, _C, _C, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I],
         "ora_dparfb_full": [_C, _C, _C, _C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, _I],
         "ora_dtile_unmqr_hqr": [_C, _I, _I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _P, _I],
+        "ora_set_host_blas": [_P, _P],
+        "ora_host_blas_on": [],
     }
     for name in ("geqr2", "larft", "larfb", "geqrt", "unmqr", "parfb", "parfb_l", "tsmqr", "tsqrt", "ttqrt",
                  "ttmqr", "tile_geqrf", "tile_unmqr", "trsm_lun", "pamm", "parfb_full"):
@@ -81,6 +83,88 @@ def _declare(L):
         f = getattr(L, name)
         f.argtypes = args
         f.restype = _I
+
+
+# ---------------------------------------------------------------------------
+# Host BLAS for the oracle's products (see the note above ora_set_host_blas in
+# nextla_oracle.c): NextLA's larfb! runs them through LinearAlgebra.mul!, i.e.
+# the host BLAS on CPU arrays.  The Fortran-ABI dgemm/dtrmm are taken from
+# scipy.linalg.cython_blas (scipy's bundled OpenBLAS, every host thread).
+# ---------------------------------------------------------------------------
+
+def _blas_pointers():
+    import scipy.linalg.cython_blas as cb
+    get_name = ctypes.pythonapi.PyCapsule_GetName
+    get_name.restype = ctypes.c_char_p
+    get_name.argtypes = [ctypes.py_object]
+    get_ptr = ctypes.pythonapi.PyCapsule_GetPointer
+    get_ptr.restype = ctypes.c_void_p
+    get_ptr.argtypes = [ctypes.py_object, ctypes.c_char_p]
+    out = []
+    for name in ("dgemm", "dtrmm"):
+        cap = cb.__pyx_capi__[name]
+        out.append(get_ptr(cap, get_name(cap)))
+    return out
+
+
+def set_host_blas(on):
+    """Route the oracle's GEMM/TRMM steps through the host BLAS (on=True) or
+    back to its plain loops (on=False, the default).  Returns the old state."""
+    L = lib()
+    old = bool(L.ora_host_blas_on())
+    if on:
+        g, t = _blas_pointers()
+        rc = L.ora_set_host_blas(ctypes.c_void_p(g), ctypes.c_void_p(t))
+    else:
+        rc = L.ora_set_host_blas(None, None)
+    if rc != 0:
+        raise RuntimeError("ora_set_host_blas failed")
+    return old
+
+
+class host_blas:
+    """Context manager: the oracle's products run in the host BLAS inside."""
+
+    def __enter__(self):
+        self._old = set_host_blas(True)
+        return self
+
+    def __exit__(self, *exc):
+        set_host_blas(self._old)
+        return False
+
+
+def blas_threads():
+    """Threads the host BLAS uses (None when it cannot be queried)."""
+    try:
+        import scipy.linalg.cython_blas  # noqa: F401  (loads the BLAS)
+        for name in ("scipy_openblas_get_num_threads64_", "scipy_openblas_get_num_threads",
+                     "openblas_get_num_threads64_", "openblas_get_num_threads"):
+            for lib_ in _loaded_blas_libs():
+                f = getattr(lib_, name, None)
+                if f is not None:
+                    f.restype = ctypes.c_int
+                    return int(f())
+    except Exception:
+        return None
+    return None
+
+
+def _loaded_blas_libs():
+    out = []
+    try:
+        with open("/proc/self/maps") as fh:
+            paths = {ln.split()[-1] for ln in fh if "openblas" in ln.lower() and ln.rstrip().endswith(".so")
+                     or ("openblas" in ln.lower() and ".so" in ln)}
+    except OSError:
+        return out
+    for pth in sorted(paths):
+        if os.path.exists(pth):
+            try:
+                out.append(ctypes.CDLL(pth))
+            except OSError:
+                pass
+    return out
 
 
 def _mat(A):
