@@ -168,31 +168,42 @@ def config(n, N):
 
 
 # ---------------------------------------------------------------------------
-# CPU side: the oracle (C restatement of NextLA's kernels, flat-tree driver,
-# OpenMP over independent tile columns) on a bounded sample of the workload.
+# CPU side: the oracle (C restatement of NextLA's kernels, flat-tree driver)
+# with its products in the host BLAS, as NextLA's larfb! runs them through
+# LinearAlgebra.mul! on CPU arrays; the BLAS threads over the trailing
+# columns of each panel (every host thread).  One step is the whole
+# 8192^2 workload.
 # ---------------------------------------------------------------------------
-CPU_SAMPLE_N = 2048
 # tiles per flat group of the hierarchical tall-skinny QR (a sweep at 65536 x 512
 # over 1, 2, 4, 8, 16, 32 measured 50.7, 45.2, 42.1, 42.2, 43.0, 50.7 ms)
 HQR_GRP = 4
 
 
-def cpu_sample_tflops(n=CPU_SAMPLE_N, reps=1):
+def cpu_sample_tflops(n, reps=1):
+    """The oracle's flat-tree tile QR of the n x n N(0,1) workload (host BLAS
+    products), timed on the host; returns (best TFLOP/s, seconds per run)."""
     import numpy as np
     import oracle
     oracle.build()
     rng = np.random.default_rng(SEED)
     A0 = np.asfortranarray(rng.standard_normal((n, n)))
-    best = None
+    A = np.empty_like(A0, order="F")
     times = []
-    for _ in range(reps):
-        A = A0.copy(order="F")
-        t0 = time.perf_counter()
-        oracle.tile_geqrf(A, NB, IB)
-        dt = time.perf_counter() - t0
-        times.append(dt)
-        best = dt if best is None else min(best, dt)
-    return flops_square(n) / best / 1e12, times
+    with oracle.host_blas():
+        for _ in range(reps):
+            A[...] = A0
+            t0 = time.perf_counter()
+            oracle.tile_geqrf(A, NB, IB)
+            times.append(time.perf_counter() - t0)
+    return flops_square(n) / min(times) / 1e12, times
+
+
+def cpu_cores_line():
+    """Host cores and the BLAS thread count the CPU leg runs with."""
+    import oracle
+    threads = oracle.blas_threads() or cpu_threads()
+    return threads, (f"{cpu_threads()} host cores, {threads} BLAS threads (scipy's OpenBLAS); the serial "
+                     f"panel steps (NextLA's single-work-item geqr2/tsqrt block kernels) on one thread")
 
 
 def cpu_threads():
@@ -283,19 +294,30 @@ def run_reference(args, world, rank):
     all host threads) on a bounded sample of the same workload."""
     if rank != 0:
         return 0
-    threads = cpu_threads()
-    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-    n = CPU_SAMPLE_N
-    for _ in range(args.warmup):
-        cpu_sample_tflops(n)
+    import numpy as np
+    import oracle
+    oracle.build()
+    threads, cores_note = cpu_cores_line()
+    n = args.n
+    rng = np.random.default_rng(SEED)
+    A0 = np.asfortranarray(rng.standard_normal((n, n)))
+    A = np.empty_like(A0, order="F")
     times = []
-    for _ in range(args.steps):
-        _, t = cpu_sample_tflops(n)
-        times.append(t[0])
+    with oracle.host_blas():
+        # one untimed run loads the BLAS and pages the matrices in (a CPU run
+        # has nothing else to warm up; more would only lengthen the arm)
+        for _ in range(min(args.warmup, 1)):
+            A[...] = A0
+            oracle.tile_geqrf(A, NB, IB)
+        for _ in range(args.steps):
+            A[...] = A0
+            t0 = time.perf_counter()
+            oracle.tile_geqrf(A, NB, IB)
+            times.append(time.perf_counter() - t0)
     total = sum(times)
     value = flops_square(n) * len(times) / total / 1e12
-    sample = (f"flat-tree tile QR of a {n}x{n} N(0,1) float64 matrix (nb={NB}, ib={IB}), the "
-              f"leading {n}x{n} block of the {args.n}^2 workload, per step")
+    sample = (f"the whole workload each step: flat-tree tile QR of the {n}x{n} N(0,1) float64 matrix "
+              f"(nb={NB}, ib={IB}); {cores_note}")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
@@ -305,8 +327,8 @@ def run_reference(args, world, rank):
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": ("Julia (the reference's language) is not installed on this host; the reference "
-                 "arm runs the C restatement of NextLA's kernels (oracle/nextla_oracle.c) with "
-                 "OpenMP over independent tile columns"),
+                 "arm runs the C restatement of NextLA's kernels (oracle/nextla_oracle.c) with its "
+                 "larfb!/parfb! products in the host BLAS, as NextLA's mul! runs them on CPU arrays"),
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -397,18 +419,41 @@ def ls_bench(tq, torch, m=32768, n=4096, k=4, steps=2, warmup=1, orth=True):
            "rel_diff_mixed_vs_fp64": (torch.linalg.norm(Xm - X64) / torch.linalg.norm(X64)).item(),
            "note": ("normwise backward error ||b - Ax||/(||A|| ||x|| + ||b||) is bounded below by the "
                     "1e-10 noise for any least-squares solution; both forms reach the same value")}
+    # the same solve with the FP32 panels, for comparison (time, iterations)
+    old = tq.dsgels_fp64_panels(False)
+    try:
+        t32 = []
+        for rep in range(warmup + steps):
+            (Xp, it32, rr32), ms = timed(lambda: tq.lstsq_mixed(Ac, bc, NB, IB, maxit=60, tol=1e-13))
+            if rep >= warmup:
+                t32.append(ms)
+        res["fp32_panels"] = {"mixed_ms": min(t32), "iterations": it32,
+                              "rel_diff_vs_fp64": (torch.linalg.norm(Xp - X64) / torch.linalg.norm(X64)).item()}
+    finally:
+        tq.dsgels_fp64_panels(old)
     if orth:
-        for tag, dt, src in (("mixed", torch.float32, A32), ("fp64", torch.float64, A64)):
+        # ||I - Q^T Q||_F of each stored factor, Q formed in FP64 from its V and T
+        # (widened), so the figure is the factor's own, not an FP32 Q formation's
+        def orth_of(F, T):
+            Fd, Td = tq.empty(m, n), tq.empty(*T.shape)
+            Fd.copy_(F.double())
+            Td.copy_(T.double())
+            Q = tq.zeros(m, n)
+            Q.diagonal().fill_(1.0)
+            tq.tile_unmqr("N", Fd, Td, Q, NB, IB)
+            o = torch.linalg.norm(Q.t() @ Q - torch.eye(n, dtype=torch.float64, device="cuda")).item()
+            del Fd, Td, Q
+            return o
+        for tag in ("mixed", "mixed_fp32_panels", "fp64"):
+            dt = torch.float64 if tag == "fp64" else torch.float32
             F = tq.empty(m, n, dtype=dt)
-            F.copy_(src)
-            T, _ = tq.tile_geqrf(F, NB, IB)
-            Q = tq.empty(m, n, dtype=dt)
-            Q.copy_(torch.eye(m, n, dtype=dt, device="cuda"))
-            tq.tile_unmqr("N", F, T, Q, NB, IB)
-            Qd = Q.double()
-            res[f"orth_I_minus_QtQ_fro_{tag}"] = torch.linalg.norm(
-                Qd.t() @ Qd - torch.eye(n, dtype=torch.float64, device="cuda")).item()
-            del F, Q, Qd, T
+            F.copy_(A32 if dt == torch.float32 else A64)
+            if tag == "mixed":
+                T, _ = tq.tile_geqrf_f64p(F, NB, IB)
+            else:
+                T, _ = tq.tile_geqrf(F, NB, IB)
+            res[f"orth_I_minus_QtQ_fro_{tag}"] = orth_of(F, T)
+            del F, T
     return res
 
 
@@ -898,6 +943,128 @@ def fp64_peak(tq_lib, torch):
     return best
 
 
+def fp64_mma_peak(tq_lib, torch):
+    """FP64 tensor-core (DMMA, mma.sync.m8n8k4.f64) rate of this GPU, and
+    the DMMA/DFMA split when some warps of each CTA run one and the rest the
+    other (tqr_fp64_mma_probe): whether the two FP64 paths add up."""
+    import ctypes
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, iters = sms * 2, 4000
+    out = torch.empty(blocks * 256, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream()
+    fa, fb = ctypes.c_double(0), ctypes.c_double(0)
+    mix = {}
+    for dw in (8, 0, 2, 4, 6, 8):
+        best = None
+        for _ in range(3):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            rc = tq_lib.lib().tqr_fp64_mma_probe(blocks, iters, dw, ctypes.c_void_p(out.data_ptr()),
+                                                ctypes.byref(fa), ctypes.byref(fb),
+                                                ctypes.c_void_p(st.cuda_stream))
+            e1.record(st)
+            st.synchronize()
+            if rc != 0:
+                raise RuntimeError(f"fp64 mma probe failed: {rc}")
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        mix[f"dmma_warps_{dw}_of_8"] = {"dmma_tflops": fa.value / best / 1e9, "dfma_tflops": fb.value / best / 1e9,
+                                        "total_tflops": (fa.value + fb.value) / best / 1e9}
+    return mix["dmma_warps_8_of_8"]["dmma_tflops"], mix
+
+
+def noalloc_vs_workspace(tq, torch, sizes=(4096, 8192), reps=3):
+    """The allocation-free tile QR (tqr_dtile_geqrf_noalloc: schedule in a
+    fixed device array, tasks in loop order) against the workspace entry
+    point (critical-path order) on the same matrix."""
+    import ctypes
+    from tileqr import _lib
+    st = torch.cuda.current_stream()
+    out = {}
+    for n in sizes:
+        g = torch.Generator(device="cuda").manual_seed(SEED + n)
+        A0 = tq.empty(n, n)
+        A0.copy_(torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda"))
+        A = tq.empty(n, n)
+        ts, taus = tq.tile_shapes(n, n, NB, IB)
+        T, tau = tq.zeros(*ts), tq.zeros(*taus)
+        P = lambda t: ctypes.c_void_p(t.data_ptr())
+
+        def noalloc():
+            rc = _lib.lib().tqr_dtile_geqrf_noalloc(n, n, NB, IB, P(A), n, P(T), ts[0], P(tau), taus[0],
+                                                   ctypes.c_void_p(st.cuda_stream))
+            if rc != 0:
+                raise RuntimeError(f"noalloc: {rc}")
+
+        def workspace():
+            tq.tile_geqrf(A, NB, IB, T, tau)
+
+        res = {}
+        for name, fn in (("workspace_ms", workspace), ("noalloc_ms", noalloc)):
+            ts_ = []
+            for rep in range(reps + 1):
+                A.copy_(A0)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                fn()
+                e1.record(st)
+                torch.cuda.synchronize()
+                if rep:
+                    ts_.append(e0.elapsed_time(e1))
+            res[name] = min(ts_)
+        status = ctypes.c_int(-1)
+        _lib.lib().tqr_tile_noalloc_status(ctypes.byref(status), None, ctypes.c_void_p(st.cuda_stream))
+        res["noalloc_status"] = status.value
+        res["noalloc_over_workspace"] = res["noalloc_ms"] / res["workspace_ms"]
+        out[f"{n}x{n}"] = res
+        del A0, A, T, tau
+    return out
+
+
+def summaries(ls, bat, adj, tall, noalloc):
+    """Short figures of the other configurations, placed last on the JSON line."""
+    out = {}
+    if ls:
+        out["mixed_ls_32768x4096"] = {
+            "speedup_vs_fp64": round(ls["speedup"], 2), "fp64_ms": round(ls["fp64_ms"], 1),
+            "mixed_ms": round(ls["mixed_ms"], 1), "iters": ls["mixed_iterations"],
+            "ls_berr_mixed": float(f"{ls['ls_backward_error_mixed']:.3e}"),
+            "ls_berr_fp64": float(f"{ls['ls_backward_error_fp64']:.3e}"),
+            "nw_berr_mixed": float(f"{ls['normwise_backward_error_mixed']:.4e}"),
+            "nw_berr_fp64": float(f"{ls['normwise_backward_error_fp64']:.4e}"),
+            "x_rel_to_fp64": float(f"{ls['rel_diff_mixed_vs_fp64']:.2e}")}
+        if "orth_I_minus_QtQ_fro_mixed" in ls:
+            out["mixed_ls_32768x4096"]["orth_mixed"] = float(f"{ls['orth_I_minus_QtQ_fro_mixed']:.2e}")
+            out["mixed_ls_32768x4096"]["orth_fp32_panels"] = float(
+                f"{ls['orth_I_minus_QtQ_fro_mixed_fp32_panels']:.2e}")
+        if ls.get("fp32_panels"):
+            out["mixed_ls_32768x4096"]["fp32_panels_ms_iters"] = [round(ls["fp32_panels"]["mixed_ms"], 1),
+                                                                  ls["fp32_panels"]["iterations"]]
+    if bat:
+        for tag in ("f64", "f32"):
+            b = bat.get(tag)
+            if b:
+                out[f"batched_{tag}"] = {"problems_per_s": round(b["problems_per_s"]),
+                                         "e2e_problems_per_s": round(b["e2e"]["value"]),
+                                         "tflops": round(b["tflops"], 3), "residual_max": float(f"{b['residual_max']:.2e}")}
+                if b.get("frac_of_fp64_simt_peak"):
+                    out[f"batched_{tag}"]["frac_fp64_simt"] = round(b["frac_of_fp64_simt_peak"], 3)
+    if adj and "fwd_ms" in adj:
+        out["adjoint_256x2048x256"] = {"fwd_ms": round(adj["fwd_ms"], 1), "bwd_ms": round(adj["bwd_ms"], 1)}
+        if adj.get("central_difference"):
+            out["adjoint_256x2048x256"]["fd_rel_err"] = float(f"{adj['central_difference']['rel_err']:.2e}")
+        if adj.get("rel_err_vs_cpu_fp64_adjoint_problem0") is not None:
+            out["adjoint_256x2048x256"]["cpu_adjoint_rel_err"] = float(
+                f"{adj['rel_err_vs_cpu_fp64_adjoint_problem0']:.2e}")
+    if tall:
+        out["tall_65536x512"] = {"hqr_ms": round(tall["hqr_ms"], 1), "flat_ms": round(tall["flat_dag_ms"], 1),
+                                 "hqr_tflops": round(tall["hqr_tflops"], 3)}
+    if noalloc:
+        out["noalloc_over_workspace"] = {k: round(v["noalloc_over_workspace"], 3) for k, v in noalloc.items()}
+    return out
+
+
 def cublas_dgemm_tflops(torch, n=4096):
     a = torch.randn(n, n, dtype=torch.float64, device="cuda")
     b = torch.randn(n, n, dtype=torch.float64, device="cuda")
@@ -1097,8 +1264,9 @@ def main():
                "phase_ms_median": {nm: statistics.median(e[q].elapsed_time(e[q + 1]) for e in phase_ev)
                                    for q, nm in enumerate(("h2d", "factor", "d2h"))}}
 
-    # roofline of the dominant kernel (the trailing update: band tsmqr/unmqr)
+    # roofline of the dominant kernel (the one persistent launch per step)
     peak = fp64_peak(_lib, torch)
+    mma_peak, mma_mix = fp64_mma_peak(_lib, torch)
     dgemm = cublas_dgemm_tflops(torch)
     achieved = (prof_flops / prof_n) / (prof_ms / prof_n) / 1e9 if prof_n else None
     traffic = None
@@ -1108,25 +1276,30 @@ def main():
             traffic = json.load(open(tpath)).get("bytes_per_launch")
         except (OSError, ValueError):
             traffic = None
-    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+    roofline = {"bound": "fp64_simt", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "fp64_mma_tflops": mma_peak,
+                "frac_of_fp64_mma": (achieved / mma_peak) if (achieved and mma_peak) else None,
+                "cublas_dgemm_tflops": dgemm,
+                "fp64_mma_dfma_mix": mma_mix,
                 "kernel": ("k_tile_dag (one persistent launch per factorisation: panel, unmqr and "
                            "tsmqr tasks), FP64 SIMT DFMA; algorithmic flops 4/3 n^3 per launch"),
-                "peak_source": ("measured: DFMA-chain probe on this GPU (SIMT FP64 ceiling; "
-                                f"cuBLAS DGEMM measured alongside at {dgemm:.3f} TFLOP/s; the "
-                                "FP64 MMA path measured slower than SIMT on sm_103a)"),
+                "peak_source": ("measured live: DFMA-chain probe (tqr_fp64_peak_probe), the FP64 ceiling "
+                                "on this GPU; the FP64 tensor-core rate (tqr_fp64_mma_probe, "
+                                "mma.sync.m8n8k4.f64) and cuBLAS DGEMM measured alongside; "
+                                "MEASURED_PEAKS.json has no FP64 figure"),
                 "timed_launches": prof_n, "algorithmic_flops_per_launch": (prof_flops / prof_n) if prof_n else None,
                 "ms_per_launch": (prof_ms / prof_n) if prof_n else None}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        threads = cpu_threads()
-        os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-        v, times = cpu_sample_tflops(CPU_SAMPLE_N, reps=2)
+        threads, cores_note = cpu_cores_line()
+        v, times = cpu_sample_tflops(n, reps=2)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": (f"oracle (C restatement of NextLA's kernels, OpenMP over tile columns) "
-                          f"flat-tree tile QR of a {CPU_SAMPLE_N}x{CPU_SAMPLE_N} N(0,1) matrix, "
-                          f"nb={NB}, ib={IB}; best of {len(times)} runs of {min(times):.1f} s")}
+               "sample": (f"the workload itself: oracle (C restatement of NextLA's kernels, larfb!/parfb! "
+                          f"products in the host BLAS as NextLA's mul! does) flat-tree tile QR of the "
+                          f"{n}x{n} N(0,1) matrix, nb={NB}, ib={IB}; best of {len(times)} runs "
+                          f"({', '.join(f'{t:.1f}' for t in times)} s); {cores_note}")}
         try:
             lv, lt = lapack_dgeqrf_tflops(n)
             cpu["lapack_dgeqrf"] = {"value": lv, "unit": UNIT, "seconds": lt,
@@ -1163,9 +1336,11 @@ def main():
 
     lat = None
     tune = None
+    noalloc = None
     if rank == 0 and world == 1 and not args.no_extras:
         lat = latency_bench(tq, torch)
         tune = autotune_square(tq, torch, n)
+        noalloc = noalloc_vs_workspace(tq, torch)
 
     if rank == 0:
         line = {
@@ -1176,15 +1351,18 @@ def main():
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": launches,
             "dag_stats_last_step": dag,
-            "least_squares_mixed_vs_fp64": ls,
-            "batched_uneven_gels": bat,
-            "batched_uneven_gels_sharded": sharded,
-            "differentiable_qr_sharded": adj_sharded,
-            "differentiable_qr": adj,
-            "tall_skinny_65536x512": tall,
             "complex_tile_qr": cplx,
             "latency_1024": lat,
             "tiling_sweep": tune,
+            "noalloc_vs_workspace": noalloc,
+            "batched_uneven_gels_sharded": sharded,
+            "differentiable_qr_sharded": adj_sharded,
+            "tall_skinny_65536x512": tall,
+            "differentiable_qr": adj,
+            "batched_uneven_gels": bat,
+            "least_squares_mixed_vs_fp64": ls,
+            # last on the line, so that a record keeping only the tail still has them
+            "summary_other_configs": summaries(ls, bat, adj, tall, noalloc),
         }
         print(json.dumps(line), flush=True)
     if world > 1:

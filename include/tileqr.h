@@ -6,7 +6,20 @@
  *   - Matrices are column-major with an explicit leading dimension; indices are
  *     0-based.  A Julia caller passes pointer(A) and stride(A, 2) of its (view
  *     of a) CuArray, exactly the storage NextLA's kernels index.
- *   - All pointers are device pointers; nothing is allocated by the library.
+ *   - All pointers are device pointers.  The tile kernels, the stream tile
+ *     driver and the solves allocate no device memory per call; scratch is
+ *     the caller's `work`.  What the library does allocate:
+ *       * the autotuners (tqr_tile_autotune, tqr_batched_autotune) cudaMalloc
+ *         their timing matrices and free them before returning;
+ *       * tqr_batched_graph creates a stream and instantiates a CUDA graph;
+ *       * the persistent drivers (tqr_?tile_geqrf_dag, tqr_?tile_gels_dag,
+ *         tqr_?tile_geqrf_{tree,hqr}_dag, tqr_dsgels) keep a pinned host
+ *         image of each shape's schedule (cudaMallocHost on the first call
+ *         for that shape, cached until exit);
+ *       * the stream tile driver creates two streams and four events per
+ *         device on its first call (kept until exit); tqr_dsgels creates
+ *         four timing events per call.
+ *     tqr_dtile_geqrf_noalloc allocates nothing, on the host or the device.
  *   - `work` / `lwork` / `ldwork` arguments exist for signature parity with
  *     NextLA and may be NULL: the W blocks live in on-chip shared memory.
  *   - Return value: 0 on success; -i when argument i (1-based position in the
@@ -326,7 +339,10 @@ int tqr_stile_gels_dag(int m, int n, int nrhs, int nb, int ib, float *A, int lda
                        cudaStream_t stream);
 
 /* Allocation-free tile QR (no counterpart in NextLA).  Same factorisation and
- * the same bits as tqr_dtile_geqrf_dag, but it needs no `work` argument: for
+ * the same bits as tqr_dtile_geqrf_dag (each tile strip sees the same
+ * operations in the same order; only the order in which CTAs pick up tasks
+ * differs: loop order here, longest path first there), but it needs no
+ * `work` argument: for
  * callers that cannot hand the library device memory -- code running while a
  * framework's caching allocator owns the device, host code that must not
  * take the implicit synchronisation of cudaMalloc/cudaFree mid-pipeline, or
@@ -339,10 +355,21 @@ int tqr_stile_gels_dag(int m, int n, int nrhs, int nb, int ib, float *A, int lda
  * that first call before any stream capture.  Each call clears the counters
  * it needs; all calls share the one array, so calls whose kernels overlap on
  * the GPU (different streams, several host threads) race and must be
- * serialised by the caller.  No cudaMalloc, cudaFree or other allocation. */
+ * serialised by the caller.  No cudaMalloc, cudaFree or other allocation.
+ * The array's device address is cached per device for the life of its
+ * primary context: do not call this entry point (or its status reader) after
+ * a cudaDeviceReset in the same process.
+ *
+ * tqr_tile_noalloc_status reads the error word of the last launch on the
+ * current device, as tqr_tile_dag_status does for a caller's `work`: *status
+ * 0 = ok, 1 = a dependency wait ran out (20 s), 2 = the schedule in the array
+ * did not match the launch (another call overwrote it); *task is the task
+ * index that reported it.  A non-zero status means A, T and tau are only
+ * partly factorised.  It synchronises `stream`. */
 #define TQR_ERR_SCRATCH_TOO_SMALL (-1000)
 int tqr_dtile_geqrf_noalloc(int m, int n, int nb, int ib, double *A, int lda, double *T, int ldt,
                             double *tau, int ldtau, cudaStream_t stream);
+int tqr_tile_noalloc_status(int *status, int *task, cudaStream_t stream);
 
 /* Tile QR with a binary reduction tree per panel (no counterpart in NextLA;
  * the composition its TT kernels exist for).  Panel k: geqrt! on every tile
@@ -439,8 +466,12 @@ int tqr_stile_gels(int m, int n, int nrhs, int nb, int ib, float *A, int lda, fl
 /* ---- Mixed-precision least squares (no counterpart in NextLA; its poster lists
  * mixed precision as future work) ----
  * min ||A X - B|| for a Float32 A (m-by-n, m >= n, lda) and Float64 B
- * (m-by-nrhs, nrhs <= 16): tile QR of a copy of A in FP32 (persistent kernel
- * when m, n are multiples of nb), X0 = R^-1 (Q^T B)[0:n] in FP32, then CGLS
+ * (m-by-nrhs, nrhs <= 16): tile QR of a copy of A (persistent kernel when m,
+ * n are multiples of nb) with the trailing tsmqr/unmqr updates in FP32 (TF32x3
+ * on the tensor cores) and the panel tasks in FP64 -- the larfg norm and
+ * reflector scaling, the larft T build, the tsqrt blocks and the diagonal R
+ * triangles they update, on a widened copy of each panel block, V / T / tau
+ * rounded to FP32 once for the updates; X0 = R^-1 (Q^T B)[0:n] in FP32, then CGLS
  * with FP64 iterates on the right-preconditioned problem min ||A R^-1 Y - B||
  * (X = R^-1 Y): every product with A uses A's FP32 entries exactly and sums in
  * double-float on the FP32 pipe (~2^-48 relative per 32 terms, flushed to
@@ -457,6 +488,15 @@ int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, 
 /* Device time (ms) of the last tqr_dsgels call's phases: ms[0] FP32 tile QR,
  * ms[1] X0 = R^-1 Q^T B, ms[2] FP64 CGLS refinement; iters its iterations. */
 int tqr_dsgels_phases(double *ms, int *iters);
+/* tqr_dsgels_fp64_panels(0) makes later tqr_dsgels calls factor with FP32
+ * panels instead (for comparison); 1 restores the default.  Returns the
+ * previous setting.  Process-wide. */
+int tqr_dsgels_fp64_panels(int on);
+/* The FP32 tile QR with FP64 panels on its own (the factorisation of
+ * tqr_dsgels, without B): as tqr_stile_geqrf_dag, same T/tau layouts; `work`
+ * from tqr_tile_dag_worksize (which covers this form). */
+int tqr_stile_geqrf_dag_f64p(int m, int n, int nb, int ib, float *A, int lda, float *T, int ldt, float *tau,
+                             int ldtau, void *work, size_t lwork, cudaStream_t stream);
 
 /* ---- Batched uneven QR + least squares (no counterpart in NextLA, which
  * factors one matrix at a time) ----
@@ -575,11 +615,19 @@ int tqr_tile_dag_check_tc(int m, int n, int nrhs, int nb, int ib, long long *nta
  * and summed algorithmic flops (4 m2 k n per tsmqr, 2 n k (2 m - k) per
  * unmqr), then forgets them.
  * tqr_fp64_peak_probe: independent DFMA chains, 16 * iters * blocks * 256
- * flops, writing blocks * 256 doubles to out -- the SIMT FP64 ceiling. */
+ * flops, writing blocks * 256 doubles to out -- the SIMT FP64 ceiling.
+ * tqr_fp64_mma_probe: the FP64 tensor-core counterpart.  CTAs of 256 threads;
+ * in each, warps 0 .. dmma_warps-1 run 4 independent mma.sync.m8n8k4.f64
+ * accumulator chains for iters steps, the other warps 8 DFMA chains per
+ * thread; *dmma_flops / *dfma_flops receive the flops of each part
+ * (dmma_warps = 8: DMMA alone, 0: DFMA alone).  out takes blocks * 256
+ * doubles. */
 unsigned long long tqr_launch_count(void);
 void tqr_profile_enable(int on);
 int tqr_profile_read(long long *launches, double *device_ms, double *flops);
 int tqr_fp64_peak_probe(int blocks, int iters, double *out, cudaStream_t stream);
+int tqr_fp64_mma_probe(int blocks, int iters, int dmma_warps, double *out, double *dmma_flops,
+                       double *dfma_flops, cudaStream_t stream);
 
 #ifdef __cplusplus
 }

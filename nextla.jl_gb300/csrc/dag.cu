@@ -70,6 +70,10 @@ struct DagGeom {
   // tc = 1: the tsmqr updates of A's tile columns run as TC tasks on NCH
   // chunks of 128 columns (CPS strips each) per tile (FP32, nb = 256, ib = 32)
   int tc, NCH, CPS;
+  // f64p = 1 (FP32 only): the panel tasks GB and TB compute in FP64
+  // (panel_qr_cta_f64 / tsqrt_block_cta_f64) with the diagonal R triangles
+  // kept in an FP64 array after the schedule in the workspace
+  int f64p;
   __host__ __device__ int tm_tasks(int j) const { return (tc && j < NTA) ? NCH : strips(j); }
   __host__ __device__ int strips(int j) const { return j < NTA ? NS : (nrhs + nw - 1) / nw; }
   __host__ __device__ int width(int j) const { return j < NTA ? nb : nrhs; }
@@ -207,6 +211,7 @@ struct DagArgs {
   long long key;
   unsigned long long timeout_ns;
   int hold = 0;     // failure-detection test: task 0 also waits for a header word nothing writes
+  double *D = nullptr;   // g.f64p: FP64 diagonal R triangles, ib x (KT nb), ld ib
 };
 
 __device__ __forceinline__ int ld_acquire(const int *p) {
@@ -243,11 +248,26 @@ __device__ bool run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *
   auto tautile = [&](int r, int c) { return a.tau + ix(c * nb, r, a.ldtau); };
   if (it.type == IT_GB) {
     R *Ab = tile(k, k) + ix(b * ib, b * ib, a.lda);
+    if constexpr (std::is_same<R, float>::value) {
+      if (a.D) {
+        panel_qr_cta_f64(nb - b * ib, ib, Ab, a.lda, tautile(k, k) + b * ib, ttile(k, k) + ix(0, b * ib, a.ldt),
+                         a.ldt, a.D + (size_t)(k * nb + b * ib) * ib, ib, smem);
+        return true;
+      }
+    }
     panel_qr_cta<R, TC>(nb - b * ib, ib, Ab, a.lda, tautile(k, k) + b * ib, ttile(k, k) + ix(0, b * ib, a.ldt),
                     a.ldt, true, true, smem);
     return true;
   }
   if (it.type == IT_TB) {
+    if constexpr (std::is_same<R, float>::value) {
+      if (a.D) {
+        tsqrt_block_cta_f64(nb, ib, a.D + (size_t)(k * nb + b * ib) * ib, ib, tile(k, k) + ix(b * ib, b * ib, a.lda),
+                            a.lda, tile(i, k) + ix(0, b * ib, a.lda), a.lda, ttile(i, k) + ix(0, b * ib, a.ldt),
+                            a.ldt, tautile(i, k) + b * ib, smem);
+        return true;
+      }
+    }
     tsqrt_block_cta<R, TC>(nb, ib, tile(k, k) + ix(b * ib, b * ib, a.lda), a.lda, tile(i, k) + ix(0, b * ib, a.lda),
                        a.lda, ttile(i, k) + ix(0, b * ib, a.ldt), a.ldt, tautile(i, k) + b * ib, true, smem);
     return true;
@@ -444,7 +464,7 @@ struct Plan {
   // the copies stay asynchronous); falls back to pageable memory
   unsigned char *pinned = nullptr;
   std::vector<unsigned char> pageable;
-  size_t bytes_counters = 0, bytes_items = 0, bytes_total = 0;
+  size_t bytes_counters = 0, bytes_items = 0, bytes_d = 0, bytes_total = 0;
   const unsigned char *image() const { return pinned ? pinned : pageable.data(); }
   ~Plan() {
     if (pinned) cudaFreeHost(pinned);
@@ -478,6 +498,7 @@ static bool dag_geom(int m, int n, int nb, int ib, DagGeom *g, int nrhs = 0, int
   g->m = m; g->n = n; g->nb = nb; g->ib = ib; g->nw = nw;
   g->nrhs = nrhs;
   g->tc = 0; g->NCH = nb / tc::kChunk; g->CPS = tc::kChunk / nw;
+  g->f64p = 0;
   g->NTA = n / nb;
   g->MT = m / nb; g->NT = g->NTA + (nrhs > 0 ? 1 : 0); g->KT = std::min(g->MT, g->NTA);
   g->NS = nb / nw; g->SPB = ib / nw; g->NBK = nb / ib;
@@ -496,7 +517,7 @@ static bool tc_enabled() { return g_tc_enabled != 0; }
 
 static long long geom_key(const DagGeom &g) {
   long long h = 1469598103934665603LL;
-  for (int v : {g.m, g.n, g.nb, g.ib, g.nw, g.nrhs, g.tc}) h = (h ^ (long long)v) * 1099511628211LL;
+  for (int v : {g.m, g.n, g.nb, g.ib, g.nw, g.nrhs, g.tc, g.f64p}) h = (h ^ (long long)v) * 1099511628211LL;
   return h & 0x7fffffffffffffffLL;
 }
 
@@ -631,7 +652,8 @@ static std::shared_ptr<Plan> get_plan(const DagGeom &g) {
   build_schedule(g, p->items, false);
   p->bytes_counters = align256(sizeof(int) * (size_t)g.ncounters());
   p->bytes_items = align256(sizeof(DagItem) * p->items.size());
-  p->bytes_total = 256 + p->bytes_counters + p->bytes_items;
+  p->bytes_d = g.f64p ? align256(sizeof(double) * (size_t)g.ib * g.KT * g.nb) : 0;
+  p->bytes_total = 256 + p->bytes_counters + p->bytes_items + p->bytes_d;
   const size_t img = 256 + sizeof(DagItem) * p->items.size();
   unsigned char *dst = nullptr;
   if (cudaMallocHost((void **)&p->pinned, img) == cudaSuccess) {
@@ -679,7 +701,7 @@ static int launch_dag(const DagArgs<R> &a, size_t sm, double flops, cudaStream_t
 template <typename R>
 static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int ldt, R *tau,
                           int ldtau, void *work, size_t lwork, cudaStream_t st, int nrhs = 0,
-                          R *B = nullptr, int ldb = 1, unsigned long long hold_ns = 0) {
+                          R *B = nullptr, int ldb = 1, unsigned long long hold_ns = 0, bool f64p = false) {
   if (m < 0) return -1;
   if (n < 0) return -2;
   if (nb <= 0) return -3;
@@ -692,6 +714,10 @@ static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int
   if (std::is_same<R, float>::value && nb == 256 && ib == tc::kIb && g.nw == 16 && tc_enabled() &&
       ((uintptr_t)A & 15) == 0 && (lda & 3) == 0)
     g.tc = 1;
+  if (f64p) {
+    if (!std::is_same<R, float>::value) return -3;
+    g.f64p = 1;
+  }
   if (lda < m) return -6;
   if (ldt < g.MT * ib) return -8;
   if (ldtau < n) return -10;
@@ -720,6 +746,7 @@ static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int
   a.items = (const DagItem *)(w + 256 + plan->bytes_counters);
   a.nitems = (int)plan->items.size();
   a.key = plan->key;
+  if (g.f64p) a.D = (double *)(w + 256 + plan->bytes_counters + plan->bytes_items);
   a.timeout_ns = 20ull * 1000ull * 1000ull * 1000ull;   // 20 s for any single wait
   if (hold_ns) {
     a.timeout_ns = hold_ns;
@@ -728,6 +755,7 @@ static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int
   size_t sm = std::max({apply_smem_elems(nb, ib, g.nw, true, true, true) * sizeof(R),
                         panel_smem<R>(nb, ib, true, true), tsqrt_smem<R>(nb, ib, true)});
   if (g.tc) sm = std::max(sm, tc::kSmem);
+  if (g.f64p) sm = std::max({sm, panel_f64_smem(nb, ib), tsqrt_f64_smem(nb, ib)});
   const double mn = (double)std::max(m, n), kn = (double)std::min(m, n);
   const double flops = 2.0 * mn * kn * kn - 2.0 * kn * kn * kn / 3.0;
   if constexpr (std::is_same<R, float>::value) {
@@ -756,6 +784,9 @@ static void *g_static_ptr[64];
 
 // Device address of g_tile_scratch on the current device (set-up on the
 // first call per device; in host code the symbol itself is only a stand-in).
+// The address is cached for the life of the device's primary context: after
+// a cudaDeviceReset the cached address is stale, so the entry points that use
+// it must not be called after a reset in the same process.
 static cudaError_t static_scratch(void **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -842,11 +873,42 @@ static int tile_geqrf_noalloc(int m, int n, int nb, int ib, double *A, int lda, 
                     : launch_dag<double, 8>(a, sm, 0.0, st, false);
 }
 
+// Workspace of the FP64-panel form of geometry g: the same schedule plus the
+// FP64 diagonal triangles (the task list and counters do not depend on it).
+static size_t f64p_bytes(const DagGeom &g) {
+  return get_plan(g)->bytes_total + align256(sizeof(double) * (size_t)g.ib * g.KT * g.nb);
+}
+
+// tqr_dsgels factors with FP64 panels unless a caller switches that off
+// (tqr_dsgels_fp64_panels(0)), e.g. to compare with the all-FP32 panels.
+static int g_f64p_enabled = 1;
+
+int stile_gels_dag_mixed(int m, int n, int nrhs, int nb, int ib, float *A, int lda, float *T, int ldt,
+                         float *tau, int ldtau, float *B, int ldb, void *work, size_t lwork, cudaStream_t stream) {
+  if (nrhs < 0 || nrhs > nb) return -3;
+  int rc = tile_geqrf_dag<float>(m, n, nb, ib, A, lda, T, ldt, tau, ldtau, work, lwork, stream, nrhs, B, ldb, 0,
+                                 g_f64p_enabled != 0);
+  if (rc != 0) return rc;
+  return nrhs > 0 ? tqr_strsm_lun(n, nrhs, A, lda, B, ldb, stream) : 0;
+}
+
 }  // namespace tqr
 
 using namespace tqr;
 
 extern "C" {
+
+int tqr_dsgels_fp64_panels(int on) {
+  const int old = g_f64p_enabled;
+  g_f64p_enabled = on ? 1 : 0;
+  return old;
+}
+
+int tqr_stile_geqrf_dag_f64p(int m, int n, int nb, int ib, float *A, int lda, float *T, int ldt, float *tau,
+                             int ldtau, void *work, size_t lwork, cudaStream_t stream) {
+  return tile_geqrf_dag<float>(m, n, nb, ib, A, lda, T, ldt, tau, ldtau, work, lwork, stream, 0, nullptr, 1, 0,
+                               true);
+}
 
 int tqr_tile_dag_worksize(int m, int n, int nb, int ib, size_t *bytes) {
   if (!bytes) return -5;
@@ -860,6 +922,7 @@ int tqr_tile_dag_worksize(int m, int n, int nb, int ib, size_t *bytes) {
   size_t b = get_plan(g)->bytes_total;
   DagGeom gz;
   if (dag_geom(m, n, nb, ib, &gz, 0, 16)) b = std::max(b, get_plan(gz)->bytes_total);
+  b = std::max(b, f64p_bytes(g));
   *bytes = b;
   return 0;
 }
@@ -871,7 +934,7 @@ int tqr_tile_gels_worksize(int m, int n, int nrhs, int nb, int ib, size_t *bytes
     *bytes = 0;
     return 1;
   }
-  *bytes = get_plan(g)->bytes_total;
+  *bytes = std::max(get_plan(g)->bytes_total, f64p_bytes(g));
   return 0;
 }
 
@@ -941,6 +1004,23 @@ int tqr_tile_dag_status(const void *work, int *status, int *task, cudaStream_t s
 int tqr_dtile_geqrf_noalloc(int m, int n, int nb, int ib, double *A, int lda, double *T, int ldt,
                             double *tau, int ldtau, cudaStream_t stream) {
   return tile_geqrf_noalloc(m, n, nb, ib, A, lda, T, ldt, tau, ldtau, stream);
+}
+
+// Error word of the last tqr_dtile_geqrf_noalloc launch on this device: the
+// header sits at the start of the static array, which no caller can address,
+// so this reads it for them (a copy from the symbol, then a stream
+// synchronisation; nothing is allocated).
+int tqr_tile_noalloc_status(int *status, int *task, cudaStream_t stream) {
+  void *wv = nullptr;
+  cudaError_t e = static_scratch(&wv);
+  if (e != cudaSuccess) return (int)e;
+  DagHeader h;
+  e = cudaMemcpyFromSymbolAsync(&h, g_tile_scratch, sizeof(h), 0, cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return (int)e;
+  if (status) *status = h.error;
+  if (task) *task = h.err_item;
+  return 0;
 }
 
 int tqr_tile_dag_stats(const void *work, unsigned long long *out, cudaStream_t stream) {

@@ -10,6 +10,11 @@
 //   tqr_fp64_peak_probe     a DFMA throughput kernel: 16 * iters * blocks *
 //                           threads flops of independent FMA chains, the FP64
 //                           ceiling a SIMT kernel can reach on this GPU
+//   tqr_fp64_mma_probe      the FP64 tensor-core (DMMA) counterpart: warps
+//                           issue independent mma.sync.m8n8k4.f64 chains, or a
+//                           chosen number of warps per CTA run DMMA while the
+//                           others run DFMA chains, to show whether the two
+//                           paths add up
 #include <atomic>
 #include <mutex>
 #include <vector>
@@ -72,6 +77,38 @@ __global__ void __launch_bounds__(256) k_fp64_probe(double *out, int iters, doub
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+// 256 threads = 8 warps per CTA.  Warps below dmma_warps run 4 independent
+// accumulator chains of mma.sync.m8n8k4.f64 (512 flops per warp and MMA);
+// the others run 8 independent DFMA chains per thread (2 flops per lane and
+// FMA).  Each warp writes its accumulators so nothing is dead code.
+__global__ void __launch_bounds__(256) k_fp64_mma_probe(double *out, int iters, int dmma_warps, double a,
+                                                         double b) {
+  const int warp = threadIdx.x >> 5;
+  const size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (warp < dmma_warps) {
+    double d[4][2];
+    for (int c = 0; c < 4; ++c) { d[c][0] = threadIdx.x + c; d[c][1] = threadIdx.x - c; }
+    const double fa = a * (1 + (threadIdx.x & 3)), fb = b;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        asm volatile(
+            "mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+            : "+d"(d[c][0]), "+d"(d[c][1])
+            : "d"(fa), "d"(fb));
+    }
+    out[o] = d[0][0] + d[0][1] + d[1][0] + d[1][1] + d[2][0] + d[2][1] + d[3][0] + d[3][1];
+  } else {
+    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5,
+           x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+      x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+      x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    out[o] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  }
+}
+
 }  // namespace tqr
 
 extern "C" {
@@ -116,3 +153,18 @@ int tqr_fp64_peak_probe(int blocks, int iters, double *out, cudaStream_t stream)
 }
 
 }  // extern "C"
+
+extern "C" int tqr_fp64_mma_probe(int blocks, int iters, int dmma_warps, double *out, double *dmma_flops,
+                                  double *dfma_flops, cudaStream_t stream) {
+  if (blocks <= 0) return -1;
+  if (iters <= 0) return -2;
+  if (dmma_warps < 0 || dmma_warps > 8) return -3;
+  if (!out) return -4;
+  // scale factors of magnitude one keep the chains finite for any iters
+  tqr::k_fp64_mma_probe<<<blocks, 256, 0, stream>>>(out, iters, dmma_warps, 0.999999999, 1e-12);
+  tqr::count_launch(1);
+  if (dmma_flops) *dmma_flops = (double)blocks * dmma_warps * 4.0 * iters * 512.0;
+  if (dfma_flops) *dfma_flops = (double)blocks * (8 - dmma_warps) * 32.0 * 8.0 * iters * 2.0;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : (int)e;
+}

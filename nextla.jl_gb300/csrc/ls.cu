@@ -4,8 +4,12 @@
 // mixed-precision solver as future work.  min ||A X - B||_2 for a Float32-stored
 // A (m >= n) and Float64 right-hand sides:
 //
-//   1. copy A into the factor workspace F and tile-QR it in FP32 (the same
-//      persistent kernel as the FP64 form, float instantiation);
+//   1. copy A into the factor workspace F and tile-QR it (the same persistent
+//      kernel as the FP64 form, float instantiation): the trailing tsmqr
+//      updates in FP32 (TF32x3 on the tensor cores), the panel tasks -- the
+//      larfg norm and reflector scaling, the larft T build and the tsqrt
+//      blocks with their diagonal R triangles -- in FP64 on a widened copy of
+//      the panel block, V / T / tau rounded to FP32 once for the updates;
 //   2. X0 = R^-1 (Q^T B)[0:n] in FP32 (tile Q application + triangular solve);
 //   3. refine with CGLS on the right-preconditioned problem
 //      min || (A R^-1) Y - B ||, X = R^-1 Y, with FP64 iterates: every product
@@ -741,7 +745,7 @@ int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, 
   const int MT = (m + nb - 1) / nb, k = nrhs;
   cudaStream_t st = stream;
   PhaseTimer pt(st);
-  // 1. FP32 tile QR of a copy of A
+  // 1. tile QR of a copy of A: FP32 updates, FP64 panels
   k_copy_f32_mat<<<blocks_for((long long)m * n), TQR_THREADS, 0, st>>>(m, n, A, lda, F, m);
   count_launch();
   LS_CU(cudaGetLastError());
@@ -752,7 +756,7 @@ int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, 
   if (tqr_tile_gels_worksize(m, n, k, nb, ib, &dagb) == 0) {
     // 1+2 in one persistent launch: B (in FP32) rides along as an extra tile
     // column, so the factorisation leaves Q^T B behind; then R X0 = (Q^T B)[0:n]
-    LS_TRY(tqr_stile_gels_dag(m, n, k, nb, ib, F, m, T, MT * ib, tau, n, x32, m, base + w.dag, dagb, st));
+    LS_TRY(stile_gels_dag_mixed(m, n, k, nb, ib, F, m, T, MT * ib, tau, n, x32, m, base + w.dag, dagb, st));
     pt.mark(1);
   } else {
     LS_TRY(tqr_stile_geqrf(m, n, nb, ib, F, m, T, MT * ib, tau, n, st));

@@ -50,6 +50,11 @@ struct ColumnStep {
   int tt = -1;  // >= 0: triangle-on-triangle form, column j of P holds rows
                 // [0, tt + j] only (NextLA src/ttqrt.jl:9); its rows below
                 // are never read
+  bool round32 = false;   // FP64 panels of an FP32 matrix: each reflector and
+                          // its tau are rounded to FP32 as soon as they are
+                          // formed, so every later use -- the rest of the
+                          // block, the T build, the FP32 updates -- applies
+                          // the reflector that is stored
 };
 
 // One column step.  x rows are [x0, m) of P, column i.  Returns false when
@@ -75,6 +80,9 @@ __device__ bool column_step(const ColumnStep<E> &c, int i, int x0, int m, int nc
     for (int w = 0; w < TQR_WARPS; ++w) t += rpart[w];
     E beta, tv, sc;
     if (householder(c.row[(size_t)i * c.rs], t, beta, tv, sc)) {
+      if constexpr (std::is_same<E, double>::value) {
+        if (c.round32) tv = (double)(float)tv;
+      }
       c.scal[0] = beta; c.scal[1] = tv; c.scal[2] = sc; c.scal[3] = E(1);
     } else {
       c.scal[3] = E(0);
@@ -91,7 +99,15 @@ __device__ bool column_step(const ColumnStep<E> &c, int i, int x0, int m, int nc
   const E beta = c.scal[0], tv = c.scal[1], sc = c.scal[2];
   // d_j = -conj(tau) S_j (j > i), -tau conj(S_j) (j < i)
   auto dval = [&](int j, E acc) -> E { return j > i ? -(conj_(tv) * acc) : -(tv * conj_(acc)); };
-  for (int r = x0 + tid; r < m; r += TQR_THREADS) xcol[r] *= sc;
+  if constexpr (std::is_same<E, double>::value) {
+    if (c.round32) {
+      for (int r = x0 + tid; r < m; r += TQR_THREADS) xcol[r] = (double)(float)(xcol[r] * sc);
+    } else {
+      for (int r = x0 + tid; r < m; r += TQR_THREADS) xcol[r] *= sc;
+    }
+  } else {
+    for (int r = x0 + tid; r < m; r += TQR_THREADS) xcol[r] *= sc;
+  }
   __syncthreads();
   // ---- d_j for all j != i (j < i only when T is built) ----
   const int jlo = c.Ts ? 0 : i + 1;
@@ -378,6 +394,128 @@ __device__ void tsqrt_block_cta(int m, int sb, R *A1, int lda1, R *A2, int lda2,
       }
     }
   }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Panels of an FP32 matrix computed in FP64 (the mixed-precision tile QR).
+// The block is widened into shared memory as doubles (exact), the Householder
+// norms and scalars, the in-block updates and the T build run in FP64
+// (column_step<double>).  Each reflector v and its tau are rounded to FP32
+// the moment they are formed (ColumnStep::round32), so the rest of the block,
+// the FP64 T build and the FP32 trailing updates all apply the reflector that
+// is stored; T is rounded once, on the way out.  The R triangle on
+// the panel's diagonal -- geqrt's ib x ib block, which every tsqrt block of
+// the panel then updates as its A1 -- also goes to an FP64 copy D; the tsqrt
+// blocks read and write D instead of the rounded A1, so the chain of tsqrt
+// blocks down a panel never rounds it (A1 receives each result rounded, and
+// holds the final R after the last one).
+// ---------------------------------------------------------------------------
+__host__ __device__ inline size_t panel_f64_smem(int m, int nc) {
+  return panel_smem<double>(m, nc, true, true) + rnd16(sizeof(double) * nc);
+}
+__host__ __device__ inline size_t tsqrt_f64_smem(int m, int sb) {
+  return tsqrt_smem<double>(m, sb, true) + rnd16(sizeof(double) * sb);
+}
+
+// geqr2 + T of the m-by-nc FP32 panel A in FP64.  D (ldd) receives the upper
+// triangle of the first min(m, nc) rows in FP64.
+__device__ inline void panel_qr_cta_f64(int m, int nc, float *A, int lda, float *tau, float *T, int ldt,
+                                        double *D, int ldd, unsigned char *smem_raw)
+{
+  unsigned char *sp = smem_raw;
+  const int tid = threadIdx.x;
+  ColumnStep<double> c;
+  c.round32 = true;
+  c.part = carve<double>(sp, TQR_THREADS);
+  c.d = carve<double>(sp, nc);
+  c.scal = carve<double>(sp, 4);
+  c.ldts = odd_ld(nc);
+  c.Ts = carve<double>(sp, (size_t)c.ldts * nc);
+  c.ldp = odd_ld(m);
+  c.P = carve<double>(sp, (size_t)c.ldp * nc);
+  double *taus = carve<double>(sp, nc);
+  for (int idx = tid; idx < m * nc; idx += TQR_THREADS) {
+    const int r = idx % m, cc = idx / m;
+    c.P[ix(r, cc, c.ldp)] = (double)ldg_cg(A + ix(r, cc, lda));
+  }
+  __syncthreads();
+  const int k = min(m, nc);
+  for (int i = 0; i < k; ++i) {
+    c.row = c.P + i;
+    c.rs = c.ldp;
+    if (m - i <= 1) {                                  // geqr2.jl:32-35
+      if (tid == 0) taus[i] = 0.0;
+      for (int p = tid; p <= i; p += TQR_THREADS) c.Ts[p + (size_t)i * c.ldts] = 0.0;
+      __syncthreads();
+      continue;
+    }
+    column_step<double>(c, i, i + 1, m, nc, false, taus + i, true);
+  }
+  for (int idx = tid; idx < m * nc; idx += TQR_THREADS) {
+    const int r = idx % m, cc = idx / m;
+    const double v = c.P[ix(r, cc, c.ldp)];
+    A[ix(r, cc, lda)] = (float)v;
+    if (r <= cc && r < k) D[ix(r, cc, ldd)] = v;
+  }
+  for (int idx = tid; idx < k * k; idx += TQR_THREADS) {
+    const int p = idx % k, q = idx / k;
+    if (p <= q) T[ix(p, q, ldt)] = (float)c.Ts[p + (size_t)q * c.ldts];
+  }
+  for (int i = tid; i < k; i += TQR_THREADS) tau[i] = (float)taus[i];
+  __syncthreads();
+}
+
+// One ib-block of tsqrt on an FP32 A2 (m-by-sb) in FP64; its A1 triangle is
+// read from and written to the FP64 copy D (ldd), and written rounded to A1.
+__device__ inline void tsqrt_block_cta_f64(int m, int sb, double *D, int ldd, float *A1, int lda1, float *A2,
+                                           int lda2, float *T, int ldt, float *tau, unsigned char *smem_raw)
+{
+  unsigned char *sp = smem_raw;
+  const int tid = threadIdx.x;
+  ColumnStep<double> c;
+  c.round32 = true;
+  c.part = carve<double>(sp, TQR_THREADS);
+  c.d = carve<double>(sp, sb);
+  c.scal = carve<double>(sp, 4);
+  const int ldb = odd_ld(sb);
+  double *B = carve<double>(sp, (size_t)ldb * sb);
+  c.ldts = odd_ld(sb);
+  c.Ts = carve<double>(sp, (size_t)c.ldts * sb);
+  c.ldp = odd_ld(m);
+  c.P = carve<double>(sp, (size_t)c.ldp * sb);
+  double *taus = carve<double>(sp, sb);
+  for (int idx = tid; idx < sb * sb; idx += TQR_THREADS) {
+    const int r = idx % sb, cc = idx / sb;
+    if (r <= cc) {
+      B[ix(r, cc, ldb)] = ldg_cg(D + ix(r, cc, ldd));
+      c.Ts[r + (size_t)cc * c.ldts] = (double)ldg_cg(T + ix(r, cc, ldt));   // skipped columns keep T
+    }
+  }
+  for (int idx = tid; idx < m * sb; idx += TQR_THREADS) {
+    const int r = idx % m, cc = idx / m;
+    c.P[ix(r, cc, c.ldp)] = (double)ldg_cg(A2 + ix(r, cc, lda2));
+  }
+  __syncthreads();
+  c.rs = ldb;
+  for (int i = 0; i < sb; ++i) {
+    c.row = B + i;
+    column_step<double>(c, i, 0, m, sb, true, taus + i, false);
+  }
+  for (int idx = tid; idx < sb * sb; idx += TQR_THREADS) {
+    const int r = idx % sb, cc = idx / sb;
+    if (r <= cc) {
+      const double v = B[ix(r, cc, ldb)];
+      D[ix(r, cc, ldd)] = v;
+      A1[ix(r, cc, lda1)] = (float)v;
+      T[ix(r, cc, ldt)] = (float)c.Ts[r + (size_t)cc * c.ldts];
+    }
+  }
+  for (int idx = tid; idx < m * sb; idx += TQR_THREADS) {
+    const int r = idx % m, cc = idx / m;
+    A2[ix(r, cc, lda2)] = (float)c.P[ix(r, cc, c.ldp)];
+  }
+  for (int i = tid; i < sb; i += TQR_THREADS) tau[i] = (float)taus[i];
   __syncthreads();
 }
 

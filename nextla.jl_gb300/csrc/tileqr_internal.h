@@ -60,4 +60,11 @@ template <typename R>
 int parfb_general(char side, char trans, char direct, char storev, int m2, int n2, int k, int l, R *A1, int lda1,
                   R *A2, int lda2, const R *V, int ldv, const R *T, int ldt, R *W, int ldw, cudaStream_t st);
 
+// The FP32 least-squares factorisation of the mixed solve (dag.cu): as
+// tqr_stile_gels_dag, with the panel tasks (geqr2/larfg, larft, the tsqrt
+// blocks and their diagonal triangles) in FP64 unless tqr_dsgels_fp64_panels(0)
+// switched that off.  Workspace: tqr_tile_gels_worksize covers it.
+int stile_gels_dag_mixed(int m, int n, int nrhs, int nb, int ib, float *A, int lda, float *T, int ldt,
+                         float *tau, int ldtau, float *B, int ldb, void *work, size_t lwork, cudaStream_t stream);
+
 }  // namespace tqr

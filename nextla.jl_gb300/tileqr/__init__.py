@@ -477,6 +477,50 @@ def tile_geqrf(A, nb=256, ib=32, T=None, tau=None, dag=True):
     return T, tau
 
 
+def tile_geqrf_f64p(A, nb=256, ib=32, T=None, tau=None):
+    """The FP32 tile QR of the mixed solve on its own: A float32, trailing
+    updates in FP32, panel tasks (larfg, larft, tsqrt blocks and diagonal R
+    triangles) in FP64, V/T/tau rounded to FP32 (tqr_stile_geqrf_dag_f64p).
+    Needs the persistent-kernel shape (m, n multiples of nb).  Returns (T, tau)."""
+    import ctypes
+    if A.dtype != torch.float32:
+        raise TypeError("tile_geqrf_f64p factors a float32 matrix")
+    m, n = A.shape
+    ts, taus = tile_shapes(m, n, nb, ib)
+    if T is None:
+        T = zeros(*ts, dtype=A.dtype, device=A.device)
+    if tau is None:
+        tau = zeros(*taus, dtype=A.dtype, device=A.device)
+    ws = dag_workspace(m, n, nb, ib, A.device)
+    if ws is None:
+        raise ArgumentError("tile_geqrf_f64p: shape outside the persistent path")
+    global _LAST_DAG_WORK
+    w, off, size = ws
+    wp = w.data_ptr() + off
+    _LAST_DAG_WORK = wp
+    pa, lda = _mat(A)
+    pt, ldt = _mat(T)
+    pu, ldu = _mat(tau)
+    st = torch.cuda.current_stream()
+    rc = _lib.lib().tqr_stile_geqrf_dag_f64p(m, n, nb, ib, pa, lda, pt, ldt, pu, ldu, ctypes.c_void_p(wp), size,
+                                            st.cuda_stream)
+    if rc < 0:
+        raise ArgumentError(f"tile_geqrf_f64p: illegal value of argument {-rc}")
+    if rc > 0:
+        raise RuntimeError(f"tile_geqrf_f64p: CUDA error {rc}")
+    if _BLOCKING:
+        status, task = dag_status(wp)
+        if status != 0:
+            raise RuntimeError(f"tile_geqrf_f64p: schedule wait timed out at task {task} (status {status})")
+    return T, tau
+
+
+def dsgels_fp64_panels(on):
+    """Whether lstsq_mixed factors with FP64 panels (default True); returns
+    the previous setting."""
+    return bool(_lib.lib().tqr_dsgels_fp64_panels(1 if on else 0))
+
+
 def autotune_tiling(m, n, dtype=torch.float64, force=False):
     """(nb, ib) for the tile QR of an m x n matrix of `dtype` (float64 or
     float32), chosen by timing every candidate tiling on a seeded matrix of

@@ -53,6 +53,8 @@ DIAG = {
     "tqr_profile_read": ([ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double),
                           ctypes.POINTER(ctypes.c_double)], _I),
     "tqr_fp64_peak_probe": ([_I, _I, _P, _P], _I),
+    "tqr_fp64_mma_probe": ([_I, _I, _I, _P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _P],
+                           _I),
     "tqr_tile_dag_worksize": ([_I, _I, _I, _I, ctypes.POINTER(ctypes.c_size_t)], _I),
     "tqr_dtile_geqrf_dag": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, ctypes.c_size_t, _P], _I),
     "tqr_stile_geqrf_dag": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, ctypes.c_size_t, _P], _I),
@@ -65,12 +67,15 @@ DIAG = {
     "tqr_tile_tuning": ([_I, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
     "tqr_tile_dag_stats": ([_P, ctypes.POINTER(ctypes.c_ulonglong), _P], _I),
     "tqr_dtile_geqrf_noalloc": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P], _I),
+    "tqr_tile_noalloc_status": ([ctypes.POINTER(_I), ctypes.POINTER(_I), _P], _I),
     "tqr_tile_dag_check_rhs": ([_I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)], _I),
     "tqr_tile_gels_worksize": ([_I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_size_t)], _I),
     "tqr_dtile_gels_dag": ([_I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, ctypes.c_size_t, _P], _I),
     "tqr_stile_gels_dag": ([_I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, ctypes.c_size_t, _P], _I),
     "tqr_dsgels_worksize": ([_I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_size_t)], _I),
     "tqr_dsgels_phases": ([ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I)], _I),
+    "tqr_dsgels_fp64_panels": ([_I], _I),
+    "tqr_stile_geqrf_dag_f64p": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, ctypes.c_size_t, _P], _I),
     "tqr_dsgels": ([_I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _I, ctypes.c_double, _P, ctypes.c_size_t,
                     ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_double), _P], _I),
     "tqr_batched_problem_bytes": ([], _I),

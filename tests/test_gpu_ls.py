@@ -85,3 +85,87 @@ def test_mixed_factor_orthogonality(tq):
         out[dt] = torch.linalg.norm(Qd.t() @ Qd - torch.eye(n, dtype=torch.float64, device="cuda")).item()
     assert out[torch.float64] < 1e-13 * n ** 0.5
     assert out[torch.float32] < 1e-4
+
+
+def _factor_error(tq, A32, nb, ib, f64p):
+    """(||I - Q^T Q||_F, ||A - Q R||_F / ||A||_F) of the stored FP32 factor,
+    with Q formed in FP64 from the FP32 V and T (widened): the factor's own
+    orthogonality and backward error, not those of an FP32 Q formation."""
+    import torch
+    m, n = A32.shape
+    A = tq.empty(m, n, dtype=torch.float32)
+    A.copy_(A32)
+    if f64p:
+        T, _ = tq.tile_geqrf_f64p(A, nb, ib)
+    else:
+        T, _ = tq.tile_geqrf(A, nb, ib)
+    Fd, Td = tq.empty(m, n), tq.empty(*T.shape)
+    Fd.copy_(A.double())
+    Td.copy_(T.double())
+    Q = tq.zeros(m, n)
+    Q.diagonal().fill_(1.0)
+    tq.tile_unmqr("N", Fd, Td, Q, nb, ib)
+    orth = torch.linalg.norm(Q.t() @ Q - torch.eye(n, dtype=torch.float64, device="cuda")).item()
+    A64 = A32.double()
+    berr = (torch.linalg.norm(A64 - Q @ torch.triu(Fd[:n])) / torch.linalg.norm(A64)).item()
+    return orth, berr
+
+
+@pytest.mark.parametrize("m,n", [(4096, 1024), (8192, 512)])
+def test_fp64_panels_improve_the_mixed_factor(tq, m, n):
+    """The mixed solve's factorisation keeps the larfg norm and scaling, the
+    larft T build and the tsqrt diagonal triangles in FP64 (FP32 updates):
+    on the mixed configuration's matrix family (condition number 1e6) its
+    stored factor is closer to orthogonal than with FP32 panels, and its
+    backward error stays at the FP32 level the updates set."""
+    import torch
+    A32, _ = make_problem(m, n, 1, 23 + n, torch)
+    o32, b32 = _factor_error(tq, A32, 256, 32, False)
+    o64, b64 = _factor_error(tq, A32, 256, 32, True)
+    print(f"\n{m}x{n}: ||I - Q^T Q||_F FP32 panels {o32:.3e}, FP64 panels {o64:.3e}; "
+          f"||A - QR|| / ||A|| {b32:.3e} -> {b64:.3e}")
+    assert o64 < 0.75 * o32
+    assert o64 < 1e-4 and b64 <= 1.05 * b32 and b64 < 1e-5
+
+
+def test_fp64_panel_factor_matches_the_oracle(tq, oracle):
+    """Parity of the FP64-panel factorisation with the FP64 oracle on the
+    same FP32-valued input, at the FP32 bar (the updates are FP32)."""
+    import torch
+    rng = np.random.default_rng(31)
+    m, n, nb, ib = 1024, 512, 256, 32
+    A0 = rng.standard_normal((m, n)).astype(np.float32).astype(np.float64)
+    A = tq.to_device(A0, dtype=torch.float32)
+    T, tau = tq.tile_geqrf_f64p(A, nb, ib)
+    Ao = np.asfortranarray(A0)
+    To, tauo = oracle.tile_geqrf(Ao, nb, ib)
+    rel = lambda a, b: float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+    assert rel(tq.to_numpy(A).astype(np.float64), Ao) < 1e-5
+    assert rel(tq.to_numpy(T).astype(np.float64), To) < 1e-5
+    assert rel(tq.to_numpy(tau).astype(np.float64), tauo) < 1e-5
+
+
+def test_mixed_solve_with_either_panel_precision(tq, oracle):
+    """The mixed solve reaches the FP64 least-squares solution with FP64
+    panels (the default) and with FP32 panels (tqr_dsgels_fp64_panels(0));
+    the FP64-panel factor needs no more CGLS iterations."""
+    import torch
+    m, n, k = 4096, 1024, 2
+    A32, b = make_problem(m, n, k, 41, torch)
+    Xo = torch.from_numpy(oracle.tile_lstsq(A32.double().cpu().numpy(), b.cpu().numpy(), 256, 32)).cuda()
+    Ac = tq.empty(m, n, dtype=torch.float32)
+    Ac.copy_(A32)
+    bc = tq.empty(m, k)
+    bc.copy_(b)
+    res = {}
+    old = tq.dsgels_fp64_panels(True)
+    try:
+        for on in (True, False):
+            tq.dsgels_fp64_panels(on)
+            Xm, iters, relres = tq.lstsq_mixed(Ac, bc, 256, 32, maxit=60, tol=1e-13)
+            res[on] = (iters, (torch.linalg.norm(Xm - Xo) / torch.linalg.norm(Xo)).item())
+    finally:
+        tq.dsgels_fp64_panels(old)
+    print(f"\nmixed solve: FP64 panels {res[True]}, FP32 panels {res[False]} (iterations, rel. to oracle)")
+    assert res[True][1] < 1e-8 and res[False][1] < 1e-8
+    assert res[True][0] <= res[False][0]
