@@ -44,9 +44,11 @@ def parse():
     p.add_argument("--n", type=int, default=8192, help="matrix order (default: the 8192^2 workload)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--kernel", default=None, choices=["tsmqr", "tsmqr_tc", "tsqrt", "geqrt", "tile"],
+    p.add_argument("--kernel", default=None,
+                   choices=["tsmqr", "tsmqr_tc", "tsqrt", "geqrt", "tile", "tile_f64p", "hqr", "larft", "trsm"],
                    help="time one tile kernel alone (for profiling) instead of the workload")
-    p.add_argument("--dtype", default="f64", choices=["f64", "f32"], help="element type for --kernel")
+    p.add_argument("--dtype", default="f64", choices=["f64", "f32", "c64", "c128"],
+                   help="element type for --kernel (complex: tile only)")
     p.add_argument("--no-ls", action="store_true", help="skip the least-squares comparison")
     p.add_argument("--ls-only", action="store_true", help="run only the least-squares comparison")
     p.add_argument("--ls-m", type=int, default=32768)
@@ -83,18 +85,63 @@ def kernel_bench(args):
     g = torch.Generator(device="cuda").manual_seed(SEED)
     n = args.n
     res = {}
-    if args.kernel == "tile":
+    if args.kernel in ("tile", "tile_f64p"):
         # the persistent tile QR of an n x n matrix in the chosen precision
-        # (FP32: its tsmqr updates on the tensor cores)
-        dt = torch.float32 if args.dtype == "f32" else torch.float64
+        # (FP32: its tsmqr updates on the tensor cores; tile_f64p: FP32 with
+        # the mixed solve's FP64 panels; complex: 4 real flops per complex one)
+        dt = {"f32": torch.float32, "f64": torch.float64, "c64": torch.complex64,
+              "c128": torch.complex128}[args.dtype]
+        if args.kernel == "tile_f64p":
+            dt = torch.float32
         A0 = tq.empty(n, n, dtype=dt)
-        A0.copy_(torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda"))
+        if dt.is_complex:
+            A0.copy_(torch.complex(torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda"),
+                                   torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda")))
+        else:
+            A0.copy_(torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda"))
         A = tq.empty(n, n, dtype=dt)
 
         def run():
             A.copy_(A0)
-            tq.tile_geqrf(A, NB, IB)
-        fl = flops_square(n)
+            if args.kernel == "tile_f64p":
+                tq.tile_geqrf_f64p(A, NB, IB)
+            else:
+                tq.tile_geqrf(A, NB, IB)
+        fl = flops_square(n) * (4 if dt.is_complex else 1)
+    elif args.kernel == "hqr":
+        # the hierarchical tall-skinny QR (groups of HQR_GRP tiles) of an
+        # n x 512 matrix, one persistent launch over its task graph
+        dt = torch.float32 if args.dtype == "f32" else torch.float64
+        A0 = tq.empty(n, 512, dtype=dt)
+        A0.copy_(torch.randn(n, 512, generator=g, dtype=torch.float64, device="cuda"))
+        A = tq.empty(n, 512, dtype=dt)
+
+        def run():
+            A.copy_(A0)
+            tq.tile_geqrf_tree(A, NB, IB, dag=True, grp=HQR_GRP)
+        fl = 2.0 * n * 512 ** 2 - 2.0 * 512 ** 3 / 3
+    elif args.kernel == "larft":
+        # stand-alone larft!('F', 'C') on an n x 32 block of reflectors
+        dt = torch.float32 if args.dtype == "f32" else torch.float64
+        V = tq.empty(n, IB, dtype=dt)
+        V.copy_(torch.randn(n, IB, generator=g, dtype=torch.float64, device="cuda") / 16)
+        tau = torch.rand(IB, generator=g, dtype=torch.float64, device="cuda").to(dt) + 1
+        T = tq.zeros(IB, IB, dtype=dt)
+        run = lambda: tq.larft("F", "C", n, IB, V, tau, T)
+        fl = 1.0 * n * IB * IB
+    elif args.kernel == "trsm":
+        # the least-squares back-solve R X = B, n x n upper R, 4 right-hand sides
+        R = tq.empty(n, n)
+        R.copy_(torch.triu(torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda")) +
+                4 * torch.eye(n, dtype=torch.float64, device="cuda"))
+        B0 = tq.empty(n, 4)
+        B0.copy_(torch.randn(n, 4, generator=g, dtype=torch.float64, device="cuda"))
+        B = tq.empty(n, 4)
+
+        def run():
+            B.copy_(B0)
+            tq.trsm_lun(R, B)
+        fl = 4.0 * n * n
     elif args.kernel == "tsmqr_tc":
         # tensor-core FP32 tsmqr ('L', 'C') on the same band as --kernel tsmqr --dtype f32
         import ctypes
