@@ -421,6 +421,22 @@ int tqr_stile_geqrf_hqr(int m, int n, int nb, int ib, int grp, float *A, int lda
                         int ldt, float *tau, float *tau2, int ldtau, int nrhs, float *B, int ldb,
                         cudaStream_t stream);
 int tqr_tile_hqr_dag_worksize(int m, int n, int nb, int ib, int grp, int nrhs, size_t *bytes);
+/* The FP32 hierarchical tree of the mixed solve (no counterpart in NextLA):
+ * as tqr_stile_geqrf_hqr_dag, with the panel steps -- geqrt! blocks, the
+ * tsqrt! merges into a group leader and the ttqrt! merges of leaders -- in
+ * FP64 on widened copies (the leaders' diagonal R triangles kept in FP64 in
+ * `work`, reflectors and tau rounded to FP32 as formed).  For 256 x 256 tiles
+ * with ib = 32 every trailing update of A (the leaders' unmqr!, the merges'
+ * tsmqr! and ttmqr!) runs on the tensor cores (TF32x3, 128-column chunks), as
+ * it does in the plain FP32 task graph unless tqr_tile_dag_tensor_cores(0).
+ * m and n multiples of nb, ib <= 32.  `work` from tqr_tile_hqr_dag_worksize
+ * (it covers this form).  tqr_tile_hqr_dag_check_tc verifies the
+ * tensor-core task graph's order on the host and returns its number of
+ * tensor-core tasks in *ntasks. */
+int tqr_stile_geqrf_hqr_dag_f64p(int m, int n, int nb, int ib, int grp, float *A, int lda, float *T, float *T2,
+                                 int ldt, float *tau, float *tau2, int ldtau, int nrhs, float *B, int ldb, void *work,
+                                 size_t lwork, cudaStream_t stream);
+int tqr_tile_hqr_dag_check_tc(int m, int n, int nb, int ib, int grp, int nrhs, long long *ntasks);
 int tqr_tile_hqr_dag_check(int m, int n, int nb, int ib, int grp, int nrhs, long long *ntasks);
 int tqr_dtile_geqrf_hqr_dag(int m, int n, int nb, int ib, int grp, double *A, int lda, double *T,
                             double *T2, int ldt, double *tau, double *tau2, int ldtau, int nrhs, double *B,
@@ -492,6 +508,12 @@ int tqr_dsgels_phases(double *ms, int *iters);
  * panels instead (for comparison); 1 restores the default.  Returns the
  * previous setting.  Process-wide. */
 int tqr_dsgels_fp64_panels(int on);
+/* tqr_dsgels_hqr_group(grp): grp > 0 makes later tqr_dsgels calls factor with
+ * the hierarchical tree (groups of grp tiles reduced flat, leaders by the
+ * binary tree; tqr_stile_geqrf_hqr_dag_f64p) when m and n are multiples of
+ * nb; 0 restores the flat tree.  Returns the previous setting.  Process-wide;
+ * tqr_dsgels_worksize depends on it. */
+int tqr_dsgels_hqr_group(int grp);
 /* The FP32 tile QR with FP64 panels on its own (the factorisation of
  * tqr_dsgels, without B): as tqr_stile_geqrf_dag, same T/tau layouts; `work`
  * from tqr_tile_dag_worksize (which covers this form). */

@@ -262,9 +262,13 @@ __device__ bool run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *
   if (it.type == IT_TB) {
     if constexpr (std::is_same<R, float>::value) {
       if (a.D) {
-        tsqrt_block_cta_f64(nb, ib, a.D + (size_t)(k * nb + b * ib) * ib, ib, tile(k, k) + ix(b * ib, b * ib, a.lda),
-                            a.lda, tile(i, k) + ix(0, b * ib, a.lda), a.lda, ttile(i, k) + ix(0, b * ib, a.ldt),
-                            a.ldt, tautile(i, k) + b * ib, smem);
+        double *Dk = a.D + (size_t)(k * nb + b * ib) * ib;
+        float *A1 = tile(k, k) + ix(b * ib, b * ib, a.lda), *A2 = tile(i, k) + ix(0, b * ib, a.lda);
+        float *Tb = ttile(i, k) + ix(0, b * ib, a.ldt), *tb = tautile(i, k) + b * ib;
+        if (ib <= 32)
+          tsqrt_block_f64x(nb, ib, Dk, ib, A1, a.lda, A2, a.lda, Tb, a.ldt, tb, smem);
+        else
+          tsqrt_block_cta_f64(nb, ib, Dk, ib, A1, a.lda, A2, a.lda, Tb, a.ldt, tb, smem);
         return true;
       }
     }
@@ -514,6 +518,7 @@ static bool dag_geom(int m, int n, int nb, int ib, DagGeom *g, int nrhs = 0, int
 // compare with the SIMT path.
 static int g_tc_enabled = 1;
 static bool tc_enabled() { return g_tc_enabled != 0; }
+bool tile_tc_enabled() { return g_tc_enabled != 0; }
 
 static long long geom_key(const DagGeom &g) {
   long long h = 1469598103934665603LL;
@@ -755,7 +760,7 @@ static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int
   size_t sm = std::max({apply_smem_elems(nb, ib, g.nw, true, true, true) * sizeof(R),
                         panel_smem<R>(nb, ib, true, true), tsqrt_smem<R>(nb, ib, true)});
   if (g.tc) sm = std::max(sm, tc::kSmem);
-  if (g.f64p) sm = std::max({sm, panel_f64_smem(nb, ib), tsqrt_f64_smem(nb, ib)});
+  if (g.f64p) sm = std::max({sm, panel_f64_smem(nb, ib), tsqrt_f64_smem(nb, ib), tsqrt_f64x_smem(nb, ib)});
   const double mn = (double)std::max(m, n), kn = (double)std::min(m, n);
   const double flops = 2.0 * mn * kn * kn - 2.0 * kn * kn * kn / 3.0;
   if constexpr (std::is_same<R, float>::value) {

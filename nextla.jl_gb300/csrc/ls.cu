@@ -662,8 +662,13 @@ struct PhaseTimer {
 
 // Workspace layout (bytes, each piece 256-aligned)
 struct MixedWs {
-  size_t F, T, tau, dag, x32, r, s, p, t, q, sc, rinv, rinvt, tmpn, gbar, total;
+  size_t F, T, tau, T2, tau2, dag, x32, r, s, p, t, q, sc, rinv, rinvt, tmpn, gbar, total;
 };
+
+// Factorisation schedule of tqr_dsgels: 0 = the flat tree (one tsqrt chain
+// per panel), grp > 0 = the hierarchical tree with groups of grp tiles
+// (tqr_dsgels_hqr_group).
+static int g_dsgels_grp = 0;
 
 static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -674,8 +679,11 @@ static int mixed_ws(int m, int n, int k, int nb, int ib, MixedWs *w) {
   w->F = take(sizeof(float) * (size_t)m * n);
   w->T = take(sizeof(float) * (size_t)MT * ib * n);
   w->tau = take(sizeof(float) * (size_t)n * MT);
+  w->T2 = take(sizeof(float) * (size_t)MT * ib * n);
+  w->tau2 = take(sizeof(float) * (size_t)n * MT);
   size_t dag = 0;
   if (tqr_tile_gels_worksize(m, n, k, nb, ib, &dag) != 0) dag = 0;
+  if (g_dsgels_grp > 0) dag = std::max(dag, tree_dag_work_bytes(m, n, nb, ib, g_dsgels_grp, k));
   w->dag = take(dag ? dag : 256);
   w->x32 = take(sizeof(float) * (size_t)m * k);
   w->r = take(sizeof(double) * (size_t)m * k);
@@ -703,6 +711,12 @@ int tqr_dsgels_phases(double *ms, int *iters) {
     for (int i = 0; i < 3; ++i) ms[i] = g_phase_ms[i];
   if (iters) *iters = g_phase_iters;
   return 0;
+}
+
+int tqr_dsgels_hqr_group(int grp) {
+  const int old = g_dsgels_grp;
+  g_dsgels_grp = grp > 0 ? grp : 0;
+  return old;
 }
 
 int tqr_dsgels_worksize(int m, int n, int nrhs, int nb, int ib, size_t *bytes) {
@@ -753,7 +767,14 @@ int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, 
   count_launch();
   LS_CU(cudaGetLastError());
   size_t dagb = 0;
-  if (tqr_tile_gels_worksize(m, n, k, nb, ib, &dagb) == 0) {
+  float *T2 = (float *)(base + w.T2), *tau2 = (float *)(base + w.tau2);
+  const size_t hqrb = g_dsgels_grp > 0 ? tree_dag_work_bytes(m, n, nb, ib, g_dsgels_grp, k) : 0;
+  if (hqrb > 0 && m % nb == 0 && n % nb == 0 && ib <= 32) {
+    // the hierarchical tree: B rides along as extra trailing columns
+    LS_TRY(stile_gels_hqr_mixed(m, n, k, nb, ib, g_dsgels_grp, F, m, T, T2, MT * ib, tau, tau2, n, x32, m,
+                                base + w.dag, w.x32 - w.dag, st));
+    pt.mark(1);
+  } else if (tqr_tile_gels_worksize(m, n, k, nb, ib, &dagb) == 0) {
     // 1+2 in one persistent launch: B (in FP32) rides along as an extra tile
     // column, so the factorisation leaves Q^T B behind; then R X0 = (Q^T B)[0:n]
     LS_TRY(stile_gels_dag_mixed(m, n, k, nb, ib, F, m, T, MT * ib, tau, n, x32, m, base + w.dag, dagb, st));

@@ -519,4 +519,243 @@ __device__ inline void tsqrt_block_cta_f64(int m, int sb, double *D, int ldd, fl
   __syncthreads();
 }
 
+// One ib-block of ttqrt (src/ttqrt.jl:1-80) in FP64 for the mixed form of the
+// hierarchical tree: A1's triangle is read from and written to its FP64 copy
+// D1 (ldd1) and written rounded to A1; A2 holds the block's columns of the
+// upper-triangular partner R, rows [0, tt + sb): rows [0, tt) come from the
+// FP32 A2, the partner's diagonal triangle (rows [tt, tt + sb)) from its FP64
+// copy D2 (ldd2).  Reflector q uses rows [0, tt + q] (the tt form of
+// column_step).  The merge reflectors go back to A2 rounded; D2 is consumed.
+__host__ __device__ inline size_t ttqrt_f64_smem(int m, int sb) {
+  return tsqrt_smem<double>(m, sb, true) + rnd16(sizeof(double) * sb);
+}
+
+__device__ inline void ttqrt_block_cta_f64(int m, int sb, int tt, double *D1, int ldd1, float *A1, int lda1,
+                                           const double *D2, int ldd2, float *A2, int lda2, float *T, int ldt,
+                                           float *tau, unsigned char *smem_raw)
+{
+  const int mrow = min(m, tt + sb);
+  unsigned char *sp = smem_raw;
+  const int tid = threadIdx.x;
+  ColumnStep<double> c;
+  c.round32 = true;
+  c.part = carve<double>(sp, TQR_THREADS);
+  c.d = carve<double>(sp, sb);
+  c.scal = carve<double>(sp, 4);
+  const int ldb = odd_ld(sb);
+  double *B = carve<double>(sp, (size_t)ldb * sb);
+  c.ldts = odd_ld(sb);
+  c.Ts = carve<double>(sp, (size_t)c.ldts * sb);
+  c.ldp = odd_ld(mrow);
+  c.P = carve<double>(sp, (size_t)c.ldp * sb);
+  double *taus = carve<double>(sp, sb);
+  for (int idx = tid; idx < sb * sb; idx += TQR_THREADS) {
+    const int r = idx % sb, cc = idx / sb;
+    if (r <= cc) {
+      B[ix(r, cc, ldb)] = ldg_cg(D1 + ix(r, cc, ldd1));
+      c.Ts[r + (size_t)cc * c.ldts] = (double)ldg_cg(T + ix(r, cc, ldt));   // skipped columns keep T
+    }
+  }
+  for (int idx = tid; idx < mrow * sb; idx += TQR_THREADS) {
+    const int r = idx % mrow, cc = idx / mrow;
+    double v = 0.0;
+    if (r <= tt + cc) v = r < tt ? (double)ldg_cg(A2 + ix(r, cc, lda2)) : ldg_cg(D2 + ix(r - tt, cc, ldd2));
+    c.P[ix(r, cc, c.ldp)] = v;
+  }
+  c.tt = tt;
+  __syncthreads();
+  c.rs = ldb;
+  for (int i = 0; i < sb; ++i) {
+    c.row = B + i;
+    column_step<double>(c, i, 0, min(m, tt + i + 1), sb, true, taus + i, false);
+  }
+  for (int idx = tid; idx < sb * sb; idx += TQR_THREADS) {
+    const int r = idx % sb, cc = idx / sb;
+    if (r <= cc) {
+      const double v = B[ix(r, cc, ldb)];
+      D1[ix(r, cc, ldd1)] = v;
+      A1[ix(r, cc, lda1)] = (float)v;
+      T[ix(r, cc, ldt)] = (float)c.Ts[r + (size_t)cc * c.ldts];
+    }
+  }
+  for (int idx = tid; idx < mrow * sb; idx += TQR_THREADS) {
+    const int r = idx % mrow, cc = idx / mrow;
+    if (r <= tt + cc) A2[ix(r, cc, lda2)] = (float)c.P[ix(r, cc, c.ldp)];
+  }
+  for (int i = tid; i < sb; i += TQR_THREADS) tau[i] = (float)taus[i];
+  __syncthreads();
+}
+
+// The tsqrt block of the mixed form laid out for latency (sb <= 32, m <= 256,
+// 256 threads).  Same arithmetic as tsqrt_block_cta_f64 (column_step<double>
+// with round32 in the tsqrt form) except the order of some sums, reorganised
+// because a dependent FP64 instruction costs ~64 cycles on GB300 and the
+// block runs on the serial tsqrt chain of a panel:
+//   * the dot products S_j = x^T P_j are laid out as (column j = tid / 8, row
+//     group g = tid % 8), so each column's eight partial sums meet in eight
+//     consecutive lanes and reduce by three shuffles -- no shared-memory pass
+//     and no barrier;
+//   * the update P_j += x d_j runs one row per thread, and each thread first
+//     updates its entry of column i + 1 and squares it, so the next column's
+//     norm is summed while the rest of the update proceeds (look-ahead);
+//   * the eight warp partials of the norm reduce by three shuffles in warp 0,
+//     which then forms the Householder scalars;
+// four barriers per column.  Columns with a zero A2 part are skipped as in the
+// reference (tau = 0, T column untouched, src/tsqrt.jl:61-64).
+__host__ __device__ inline size_t tsqrt_f64x_smem(int m, int sb) {
+  return rnd16(sizeof(double) * (size_t)odd_ld(m) * sb) + 2 * rnd16(sizeof(double) * (size_t)odd_ld(sb) * sb) +
+         rnd16(sizeof(double) * 32) + rnd16(sizeof(double) * TQR_WARPS) + rnd16(sizeof(double) * 4) +
+         rnd16(sizeof(double) * 32);
+}
+
+__device__ inline void tsqrt_block_f64x(int m, int sb, double *D, int ldd, float *A1, int lda1, float *A2, int lda2,
+                                        float *T, int ldt, float *tau, unsigned char *smem_raw)
+{
+  unsigned char *sp = smem_raw;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ldp = odd_ld(m), ldb = odd_ld(sb), ldts = odd_ld(sb);
+  double *P = carve<double>(sp, (size_t)ldp * sb);
+  double *B = carve<double>(sp, (size_t)ldb * sb);
+  double *Ts = carve<double>(sp, (size_t)ldts * sb);
+  double *d = carve<double>(sp, 32);
+  double *part = carve<double>(sp, TQR_WARPS);
+  double *scal = carve<double>(sp, 4);
+  double *taus = carve<double>(sp, 32);
+  for (int idx = tid; idx < sb * sb; idx += TQR_THREADS) {
+    const int r = idx % sb, cc = idx / sb;
+    if (r <= cc) {
+      B[ix(r, cc, ldb)] = ldg_cg(D + ix(r, cc, ldd));
+      Ts[r + (size_t)cc * ldts] = (double)ldg_cg(T + ix(r, cc, ldt));   // skipped columns keep T
+    }
+  }
+  for (int idx = tid; idx < m * sb; idx += TQR_THREADS) {
+    const int r = idx % m, cc = idx / m;
+    P[ix(r, cc, ldp)] = (double)ldg_cg(A2 + ix(r, cc, lda2));
+  }
+  __syncthreads();
+  // norm partials of column 0
+  {
+    double s = 0.0;
+    for (int r = tid; r < m; r += TQR_THREADS) s = fma(P[r], P[r], s);
+    s = warp_sum(s);
+    if (lane == 0) part[warp] = s;
+  }
+  __syncthreads();
+  const int jd = tid >> 3, gd = tid & 7;
+  for (int i = 0; i < sb; ++i) {
+    double *xi = P + (size_t)i * ldp;
+    // ---- Householder scalars (warp 0) ----
+    if (warp == 0) {
+      double t = lane < TQR_WARPS ? part[lane] : 0.0;
+      t += __shfl_xor_sync(0xffffffffu, t, 4);
+      t += __shfl_xor_sync(0xffffffffu, t, 2);
+      t += __shfl_xor_sync(0xffffffffu, t, 1);
+      if (lane == 0) {
+        double beta, tv, sc;
+        if (householder(B[ix(i, i, ldb)], t, beta, tv, sc)) {
+          scal[0] = beta; scal[1] = (double)(float)tv; scal[2] = sc; scal[3] = 1.0;
+        } else {
+          scal[3] = 0.0;
+        }
+      }
+    }
+    __syncthreads();
+    if (scal[3] == 0.0) {
+      // no reflector: tau = 0, T column and the block's columns untouched
+      if (tid == 0) taus[i] = 0.0;
+      if (i + 1 < sb) {
+        const double *xn = P + (size_t)(i + 1) * ldp;
+        double s = 0.0;
+        for (int r = tid; r < m; r += TQR_THREADS) s = fma(xn[r], xn[r], s);
+        s = warp_sum(s);
+        if (lane == 0) part[warp] = s;
+      }
+      __syncthreads();
+      continue;
+    }
+    const double tv = scal[1], sc = scal[2];
+    // ---- x *= scale, rounded to the stored FP32 reflector ----
+    for (int r = tid; r < m; r += TQR_THREADS) xi[r] = (double)(float)(xi[r] * sc);
+    __syncthreads();
+    // ---- d_j = -tau (row_j [j > i] + x^T P_j), j != i ----
+    {
+      double a0 = 0.0, a1 = 0.0;
+      if (jd < sb && jd != i) {
+        const double *pj = P + (size_t)jd * ldp;
+        int r = gd;
+        for (; r + 8 < m; r += 16) {
+          a0 = fma(xi[r], pj[r], a0);
+          a1 = fma(xi[r + 8], pj[r + 8], a1);
+        }
+        if (r < m) a0 = fma(xi[r], pj[r], a0);
+      }
+      double a = a0 + a1;
+      a += __shfl_xor_sync(0xffffffffu, a, 4);
+      a += __shfl_xor_sync(0xffffffffu, a, 2);
+      a += __shfl_xor_sync(0xffffffffu, a, 1);
+      if (gd == 0 && jd < sb && jd != i) {
+        if (jd > i) a += B[ix(i, jd, ldb)];
+        d[jd] = -(tv * a);
+      }
+    }
+    __syncthreads();
+    // ---- rank-1 update of columns j > i (one row per thread, column i + 1
+    //      first and its square summed for the next norm), row i of the
+    //      triangle, T column i ----
+    {
+      double snext = 0.0;
+      for (int r = tid; r < m; r += TQR_THREADS) {
+        const double xv = xi[r];
+        double *pr = P + r;
+        if (i + 1 < sb) {
+          const double v = fma(xv, d[i + 1], pr[(size_t)(i + 1) * ldp]);
+          pr[(size_t)(i + 1) * ldp] = v;
+          snext = fma(v, v, snext);
+        }
+#pragma unroll 4
+        for (int j = i + 2; j < sb; ++j) pr[(size_t)j * ldp] = fma(xv, d[j], pr[(size_t)j * ldp]);
+      }
+      if (i + 1 < sb) {
+        snext = warp_sum(snext);
+        if (lane == 0) part[warp] = snext;
+      }
+      for (int j = i + 1 + tid; j < sb; j += TQR_THREADS) B[ix(i, j, ldb)] += d[j];
+      for (int p = tid; p < i; p += TQR_THREADS) {
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        const double *tp = Ts + p;
+        int q = p;
+        for (; q + 3 < i; q += 4) {
+          a0 = fma(tp[(size_t)q * ldts], d[q], a0);
+          a1 = fma(tp[(size_t)(q + 1) * ldts], d[q + 1], a1);
+          a2 = fma(tp[(size_t)(q + 2) * ldts], d[q + 2], a2);
+          a3 = fma(tp[(size_t)(q + 3) * ldts], d[q + 3], a3);
+        }
+        for (; q < i; ++q) a0 = fma(tp[(size_t)q * ldts], d[q], a0);
+        Ts[p + (size_t)i * ldts] = (a0 + a1) + (a2 + a3);
+      }
+      if (tid == 0) {
+        Ts[i + (size_t)i * ldts] = tv;
+        B[ix(i, i, ldb)] = scal[0];
+        taus[i] = tv;
+      }
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < sb * sb; idx += TQR_THREADS) {
+    const int r = idx % sb, cc = idx / sb;
+    if (r <= cc) {
+      const double v = B[ix(r, cc, ldb)];
+      D[ix(r, cc, ldd)] = v;
+      A1[ix(r, cc, lda1)] = (float)v;
+      T[ix(r, cc, ldt)] = (float)Ts[r + (size_t)cc * ldts];
+    }
+  }
+  for (int idx = tid; idx < m * sb; idx += TQR_THREADS) {
+    const int r = idx % m, cc = idx / m;
+    A2[ix(r, cc, lda2)] = (float)P[ix(r, cc, ldp)];
+  }
+  for (int i = tid; i < sb; i += TQR_THREADS) tau[i] = (float)taus[i];
+  __syncthreads();
+}
+
 }  // namespace tqr

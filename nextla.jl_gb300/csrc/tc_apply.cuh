@@ -23,6 +23,12 @@
 // rows x 16 bytes per core matrix, consecutive K groups 128 bytes apart (the
 // leading byte offset), consecutive 8-row groups SBO bytes apart.
 //
+// The same routine serves the other two trailing updates of the tile QR by
+// masking V while it is staged (VMode): unmqr! of a geqrt! factor (V unit
+// lower triangular in the tile, no A1: W = V_b^T C, C -= V_b W over the whole
+// tile, src/unmqr.jl:99-148) and ttmqr! (V upper triangular: reflector p of
+// the block at column d0 holds rows [0, d0 + p] only, src/ttmqr.jl:1-95).
+//
 // The caller owns the TMEM allocation (kTmemCols columns at tmem) and kBars
 // mbarriers (initialised with count 1; phase[] tracks their parities).
 // Every mbarrier wait is bounded: on expiry the routine returns false and
@@ -168,10 +174,25 @@ __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_grou
 
 __device__ __forceinline__ void prefetch_wait() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
+// How V is read: as stored (tsmqr!), unit lower triangular within the tile
+// (the V of geqrt!, for unmqr!: zeros above the diagonal, ones on it, the R
+// stored there is not read), or upper triangular (the V of ttqrt!, for
+// ttmqr!: zeros below the diagonal, where the tile keeps geqrt!'s V).
+enum VMode : int { kVFull = 0, kVUnitLower = 1, kVUpper = 2 };
+
+// Row r of a reflector under the mode; diag is the reflector's diagonal row
+// (the row of its implicit or stored leading entry).
+__device__ __forceinline__ float vmask(int vmode, int r, int diag, float v) {
+  if (vmode == kVUnitLower) return r < diag ? 0.0f : (r == diag ? 1.0f : v);
+  if (vmode == kVUpper) return r <= diag ? v : 0.0f;
+  return v;
+}
+
 // Block b's raw operands by 16-byte cp.async copies, one commit group:
 // V_b (m2 x 32) -> Vraw (column stride kRawLd), A1_b (32 x 128) -> A1s
-// (column stride kA1Ld).  Sources 16-byte aligned, leading dimensions
-// multiples of 4; consecutive threads copy consecutive 16 bytes of a column.
+// (column stride kA1Ld; skipped when A1b is null).  Sources 16-byte aligned,
+// leading dimensions multiples of 4; consecutive threads copy consecutive 16
+// bytes of a column.
 __device__ __forceinline__ void prefetch_block(const float *Vb, int ldv, int m2, float *Vraw, const float *A1b,
                                                int lda1, float *A1s) {
   const int per_col = m2 / 4;
@@ -179,7 +200,7 @@ __device__ __forceinline__ void prefetch_block(const float *Vb, int ldv, int m2,
     const int p = idx / per_col, r4 = idx % per_col;
     cp16(Vraw + p * kRawLd + 4 * r4, Vb + (size_t)p * ldv + 4 * r4);
   }
-  for (int idx = threadIdx.x; idx < kChunk * (kIb / 4); idx += TQR_THREADS) {
+  for (int idx = threadIdx.x; A1b && idx < kChunk * (kIb / 4); idx += TQR_THREADS) {
     const int cc = idx / (kIb / 4), p4 = idx % (kIb / 4);
     cp16(A1s + cc * kA1Ld + 4 * p4, A1b + (size_t)cc * lda1 + 4 * p4);
   }
@@ -189,14 +210,20 @@ __device__ __forceinline__ void prefetch_block(const float *Vb, int ldv, int m2,
 // GEMM1's B operand for rows [r0, r0 + kKc) from Vraw: row-of-operand p, K =
 // r.  Lanes take 8 p by 4 K runs, so the 16-byte reads (column stride
 // kRawLd) and the core-matrix stores each spread over all banks.
-__device__ __forceinline__ void stage_vb1(const float *Vraw, int r0, unsigned char *hi, unsigned char *lo) {
+__device__ __forceinline__ void stage_vb1(const float *Vraw, int r0, unsigned char *hi, unsigned char *lo, int vmode,
+                                          int d0) {
   constexpr uint32_t SB = (kKc / 4) * 128;
 #pragma unroll
   for (int u = 0; u < kIb * kKc / 4 / TQR_THREADS; ++u) {
     const int idx = threadIdx.x + u * TQR_THREADS;
     const int rest = idx >> 5;
     const int p = 8 * (rest & 3) + (idx & 7), k4 = 4 * (rest >> 2) + ((idx >> 3) & 3);
-    const float4 x = *reinterpret_cast<const float4 *>(Vraw + p * kRawLd + r0 + 4 * k4);
+    float4 x = *reinterpret_cast<const float4 *>(Vraw + p * kRawLd + r0 + 4 * k4);
+    if (vmode != kVFull) {
+      const int r = r0 + 4 * k4, dg = d0 + p;
+      x.x = vmask(vmode, r, dg, x.x); x.y = vmask(vmode, r + 1, dg, x.y);
+      x.z = vmask(vmode, r + 2, dg, x.z); x.w = vmask(vmode, r + 3, dg, x.w);
+    }
     put_split4(hi, lo, kmaj(p, 4 * k4, SB), x);
   }
 }
@@ -248,7 +275,8 @@ __device__ __forceinline__ void st32(uint32_t taddr, const float (&v)[32]) {
 // [A1; A2] := Q^T [A1; A2] for the 128 columns at A1, A2 (column-major):
 // A1 rows [0, k), A2 m2 rows (m2 = 128 or 256), V m2 x k, T 32 x k (blocks of
 // 32 columns), k a multiple of 32; A1, A2, V 16-byte aligned with leading
-// dimensions multiples of 4.  256 threads; all kTmemCols TMEM columns at
+// dimensions multiples of 4.  vmode kVUnitLower: A1 is null and A2 := Q^T A2
+// with geqrt!'s V (unmqr!); kVUpper: ttmqr!'s V.  256 threads; all kTmemCols TMEM columns at
 // tmem; bars[kBars] mbarriers (count 1) with parities phase[kBars].  Returns
 // false if an MMA completion wait timed out (the caller then waits once more
 // on every barrier with a pending phase before releasing TMEM).
@@ -267,7 +295,7 @@ __device__ __forceinline__ void st32(uint32_t taddr, const float (&v)[32]) {
 // (in at the start, out at the end) instead of twice per block.
 __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2, int lda2, const float *V, int ldv,
                                    const float *T, int ldt, uint32_t tmem, uint64_t *bars, uint32_t *phase,
-                                   unsigned char *smem) {
+                                   unsigned char *smem, int vmode = kVFull) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // warps w and w + 4 reach TMEM lanes [32 (w % 4), 32 (w % 4) + 32): this
   // thread's lane is chunk column c; the two warp sets split A2's rows
@@ -352,7 +380,7 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
                      make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]));
         if (b > 0) wait_st();
       }
-      stage_vb1(Vraw, q * kKc, bHi, bLo);
+      stage_vb1(Vraw, q * kKc, bHi, bLo, vmode, b * kIb);
       to_async_proxy();
       if (tid == 0) {
         for (int ks = 0; ks < kKc / 8; ++ks) {
@@ -386,10 +414,12 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
         for (int p = 0; p < 32; ++p) w[p] += wl[p];   // (A_hi + A_lo) V_hi + (A_hi + A_lo) V_lo
       }
       float *a1s = A1s + c * kA1Ld;
+      if (A1) {
 #pragma unroll
-      for (int p4 = 0; p4 < 8; ++p4) {
-        const float4 x = *reinterpret_cast<const float4 *>(a1s + 4 * p4);
-        w[4 * p4] += x.x; w[4 * p4 + 1] += x.y; w[4 * p4 + 2] += x.z; w[4 * p4 + 3] += x.w;
+        for (int p4 = 0; p4 < 8; ++p4) {
+          const float4 x = *reinterpret_cast<const float4 *>(a1s + 4 * p4);
+          w[4 * p4] += x.x; w[4 * p4 + 1] += x.y; w[4 * p4 + 2] += x.z; w[4 * p4 + 3] += x.w;
+        }
       }
       // W := T^T W in place, last row first (row p reads rows q <= p, not yet
       // overwritten; the zeros of T below its diagonal cover the rest of the
@@ -409,9 +439,11 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
       }
 #pragma unroll
       for (int p4 = 0; p4 < 8; ++p4) {
-        float4 x = *reinterpret_cast<const float4 *>(a1s + 4 * p4);
-        x.x -= w[4 * p4]; x.y -= w[4 * p4 + 1]; x.z -= w[4 * p4 + 2]; x.w -= w[4 * p4 + 3];
-        *reinterpret_cast<float4 *>(a1s + 4 * p4) = x;
+        if (A1) {
+          float4 x = *reinterpret_cast<const float4 *>(a1s + 4 * p4);
+          x.x -= w[4 * p4]; x.y -= w[4 * p4 + 1]; x.z -= w[4 * p4 + 2]; x.w -= w[4 * p4 + 3];
+          *reinterpret_cast<float4 *>(a1s + 4 * p4) = x;
+        }
         put_split4(wHi, wLo, kmaj(c, 4 * p4, (kIb / 4) * 128), make_float4(w[4 * p4], w[4 * p4 + 1],
                                                                           w[4 * p4 + 2], w[4 * p4 + 3]));
       }
@@ -423,8 +455,13 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
       for (int idx = t; idx < m2 * (kIb / 4); idx += 128) {
         const int r = idx % m2, p4 = idx / m2;
         const float *vp = Vraw + (4 * p4) * kRawLd + r;
-        put_split4(vHi, vLo, kmaj(r, 4 * p4, (kIb / 4) * 128),
-                   make_float4(vp[0], vp[kRawLd], vp[2 * kRawLd], vp[3 * kRawLd]));
+        float4 x = make_float4(vp[0], vp[kRawLd], vp[2 * kRawLd], vp[3 * kRawLd]);
+        if (vmode != kVFull) {
+          const int dg = b * kIb + 4 * p4;
+          x.x = vmask(vmode, r, dg, x.x); x.y = vmask(vmode, r, dg + 1, x.y);
+          x.z = vmask(vmode, r, dg + 2, x.z); x.w = vmask(vmode, r, dg + 3, x.w);
+        }
+        put_split4(vHi, vLo, kmaj(r, 4 * p4, (kIb / 4) * 128), x);
       }
     }
     to_async_proxy();
@@ -442,7 +479,7 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
     }
     // while the MMAs run: the updated A1_b back to global (coalesced), then
     // the next block's V_b and A1_b into Vraw, A1s
-    {
+    if (A1) {
       float *A1b = A1 + (size_t)b * kIb;
       for (int idx = tid; idx < kChunk * (kIb / 4); idx += TQR_THREADS) {
         const int cc = idx / (kIb / 4), p4 = idx % (kIb / 4);
@@ -452,7 +489,8 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
     }
     __syncthreads();
     if (b + 1 < nblk)
-      prefetch_block(V + (size_t)(b + 1) * kIb * ldv, ldv, m2, Vraw, A1 + (size_t)(b + 1) * kIb, lda1, A1s);
+      prefetch_block(V + (size_t)(b + 1) * kIb * ldv, ldv, m2, Vraw, A1 ? A1 + (size_t)(b + 1) * kIb : nullptr,
+                     lda1, A1s);
     if (!wait_phase(&bars[2], &phase[2])) return fail();
   }
   // ---- A2 = A2^T - D2 out of TMEM through the stage buffers (coalesced) ----

@@ -67,4 +67,18 @@ int parfb_general(char side, char trans, char direct, char storev, int m2, int n
 int stile_gels_dag_mixed(int m, int n, int nrhs, int nb, int ib, float *A, int lda, float *T, int ldt,
                          float *tau, int ldtau, float *B, int ldb, void *work, size_t lwork, cudaStream_t stream);
 
+// Whether FP32 persistent schedules may use the tensor cores
+// (tqr_tile_dag_tensor_cores; dag.cu).
+bool tile_tc_enabled();
+
+// The mixed solve's factorisation as the hierarchical tree (tree.cu): groups
+// of grp tiles reduced flat, the leaders by the binary tree, FP64 panel steps,
+// tensor-core trailing updates; B rides along as extra trailing columns, then
+// R X = (Q^T B)[0:n].  T2, tau2 as for tqr_stile_geqrf_hqr_dag; work from
+// tree_dag_work_bytes.
+int stile_gels_hqr_mixed(int m, int n, int nrhs, int nb, int ib, int grp, float *A, int lda, float *T, float *T2,
+                         int ldt, float *tau, float *tau2, int ldtau, float *B, int ldb, void *work, size_t lwork,
+                         cudaStream_t stream);
+size_t tree_dag_work_bytes(int m, int n, int nb, int ib, int grp, int nrhs);
+
 }  // namespace tqr

@@ -34,6 +34,7 @@
 
 #include "apply_dev.cuh"
 #include "panel_dev.cuh"
+#include "tc_apply.cuh"
 #include "tileqr.h"
 #include "tileqr_internal.h"
 
@@ -58,7 +59,12 @@ struct TreeGeom {
 };
 
 enum TreeOpType { OP_GE_PANEL = 0, OP_GE_APPLY = 1, OP_GE_TRAIL = 2, OP_PR_PANEL = 3, OP_PR_APPLY = 4,
-                  OP_PR_TRAIL = 5 };
+                  OP_PR_TRAIL = 5,
+                  // task graph only, FP32, on the tensor cores, one 128-column
+                  // chunk of A per task: the trailing update of a merge
+                  // (tsmqr! for a tsqrt merge, ttmqr! for a ttqrt merge) and
+                  // of a geqrt! (unmqr!)
+                  OP_PR_TRAIL_TC = 6, OP_GE_TRAIL_TC = 7 };
 
 struct TreeOp {
   int type;
@@ -433,7 +439,42 @@ struct TDagArgs {
   int nitems;
   long long key;
   unsigned long long timeout_ns;
+  // mixed form (FP32 matrix): FP64 diagonal R triangles of the panel steps,
+  // ib x nb per (tile row i, panel k) at D + ((k MT + i) nb) ib, ld ib
+  double *D = nullptr;
+  __device__ double *Dtri(int i, int k, int c) const {
+    return D + ((size_t)k * g.MT + i) * (size_t)g.nb * g.ib + (size_t)c * g.ib;
+  }
 };
+
+// Panel steps of the mixed form: geqrt blocks, tsqrt merges (into a group
+// leader) and ttqrt merges (of two leaders) in FP64 with the leaders'
+// diagonal triangles kept in D (panel_dev.cuh).
+__device__ inline void tree_panel_f64(const TDagArgs<float> &a, const TreeOp &op, int i, unsigned char *smem) {
+  const TreeGeom<float> &g = a.g;
+  const int k = op.k, ib = g.ib, nk = g.cols(k), mi = g.rows(i), c = op.b * ib;
+  float *Aik = g.tile(i, k);
+  if (op.type == OP_GE_PANEL) {
+    const int kk = min(mi, nk);
+    if (c >= kk) return;
+    const int sb = min(ib, kk - c);
+    panel_qr_cta_f64(mi - c, sb, Aik + ix(c, c, g.lda), g.lda, g.tautile(g.tau, i, k) + c,
+                     g.ttile(g.T, i, k) + ix(0, c, g.ldt), g.ldt, a.Dtri(i, k, c), ib, smem);
+    return;
+  }
+  const int p = i + op.s, mp = g.rows(p);
+  float *Apk = g.tile(p, k);
+  const int kt = op.ts ? nk : min(mp, nk);
+  if (c >= kt) return;
+  const int sb = min(ib, kt - c);
+  float *T2b = g.ttile(g.T2, p, k) + ix(0, c, g.ldt), *t2b = g.tautile(g.tau2, p, k) + c;
+  if (op.ts)
+    tsqrt_block_f64x(mp, sb, a.Dtri(i, k, c), ib, Aik + ix(c, c, g.lda), g.lda, Apk + ix(0, c, g.lda), g.lda, T2b,
+                     g.ldt, t2b, smem);
+  else
+    ttqrt_block_cta_f64(mp, sb, c, a.Dtri(i, k, c), ib, Aik + ix(c, c, g.lda), g.lda, a.Dtri(p, k, c), ib,
+                        Apk + ix(0, c, g.lda), g.lda, T2b, g.ldt, t2b, smem);
+}
 
 __device__ __forceinline__ int tdag_ld_acquire(const int *p) {
   int v;
@@ -451,16 +492,39 @@ __device__ __forceinline__ unsigned long long tdag_ns() {
   return t;
 }
 
-template <typename R>
-__global__ void __launch_bounds__(TQR_THREADS, 2) k_tree_dag(const TDagArgs<R> a) {
+// TC: this instantiation owns the SM's TMEM and runs the tensor-core chunk
+// tasks (FP32, one CTA per SM); the other instantiations never meet one.
+template <typename R, bool TC>
+__global__ void __launch_bounds__(TQR_THREADS, TC ? 1 : 2) k_tree_dag(const TDagArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_it, s_err;
+  __shared__ __align__(8) uint64_t s_bars[tc::kBars];
+  __shared__ uint32_t s_tmem;
   const int tid = threadIdx.x;
   if (tid == 0) s_err = (a.hdr->key != a.key || a.hdr->nitems != a.nitems) ? 2 : 0;
   __syncthreads();
   if (s_err) {
     if (tid == 0 && blockIdx.x == 0) atomicExch(&a.hdr->error, 2);
     return;
+  }
+  uint32_t phase[tc::kBars] = {0u, 0u, 0u};
+  uint32_t tmem = 0;
+  bool tc_failed = false;
+  if constexpr (TC) {
+    if (tid == 0) {
+      for (int q = 0; q < tc::kBars; ++q)
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::saddr(&s_bars[q])));
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if ((tid >> 5) == 0) {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc::saddr(&s_tmem)),
+                   "r"(tc::kTmemCols));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    tmem = s_tmem;
   }
   for (;;) {
     if (tid == 0) s_it = atomicAdd(&a.hdr->head, 1);
@@ -493,19 +557,71 @@ __global__ void __launch_bounds__(TQR_THREADS, 2) k_tree_dag(const TDagArgs<R> a
     op.k = it.k; op.b = it.b;
     op.s = (int)it.p - (int)it.i;
     op.trans = 0; op.a_cols = 1;
-    tree_task<R>(a.g, op, it.i, it.y, smem);
+    bool ok = true;
+    if constexpr (std::is_same<R, float>::value) {
+      if (op.type == OP_PR_TRAIL_TC || op.type == OP_GE_TRAIL_TC) {
+        if constexpr (TC) {
+          const TreeGeom<R> &g = a.g;
+          const int k = it.k;
+          const int col = (k + 1) * g.nb + (int)it.y * tc::kChunk;
+          const int j = col / g.nb, off = col % g.nb;
+          unsigned char *al = smem + ((1024 - (tc::saddr(smem) & 1023)) & 1023);
+          if (op.type == OP_GE_TRAIL_TC) {
+            // unmqr! of geqrt!'s factor of tile (i, k) on the chunk of tile (i, j)
+            ok = tc::tsmqr_chunk(g.rows(it.i), min(g.rows(it.i), g.cols(k)), nullptr, g.lda,
+                                 g.tile(it.i, j) + (size_t)off * g.lda, g.lda, g.tile(it.i, k), g.lda,
+                                 g.ttile(g.T, it.i, k), g.ldt, tmem, s_bars, phase, al, tc::kVUnitLower);
+          } else {
+            const int p = it.p;
+            ok = tc::tsmqr_chunk(g.rows(p), op.ts ? g.cols(k) : min(g.rows(p), g.cols(k)),
+                                 g.tile(it.i, j) + (size_t)off * g.lda, g.lda, g.tile(p, j) + (size_t)off * g.lda,
+                                 g.lda, g.tile(p, k), g.lda, g.ttile(g.T2, p, k), g.ldt, tmem, s_bars, phase, al,
+                                 op.ts ? tc::kVFull : tc::kVUpper);
+          }
+        } else {
+          ok = false;   // never scheduled without the tensor-core instantiation
+        }
+      } else if (a.D && (op.type == OP_GE_PANEL || op.type == OP_PR_PANEL)) {
+        tree_panel_f64(a, op, it.i, smem);
+      } else {
+        tree_task<R>(a.g, op, it.i, it.y, smem);
+      }
+    } else {
+      tree_task<R>(a.g, op, it.i, it.y, smem);
+    }
+    if (!ok) {
+      if (tid == 0 && atomicCAS(&a.hdr->error, 0, 3) == 0) a.hdr->err_item = idx;
+      tc_failed = true;
+      break;
+    }
     __syncthreads();
     if (tid == 0) {
       __threadfence();
       tdag_st_release(a.done + idx, 1);
     }
   }
+  if constexpr (TC) {
+    // after a failed wait: one more commit (it arrives once every earlier MMA
+    // has completed) and one bounded wait for it, then release TMEM
+    if (tc_failed) {
+      if (tid == 0) tc::commit(&s_bars[2]);
+      tc::bar_wait(&s_bars[2], phase[2]);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if ((tid >> 5) == 0)
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tc::kTmemCols));
+  }
+  (void)tc_failed;
 }
 
 // ---- host: task graph construction -----------------------------------------
 struct TreeShape {
   int m, n, nb, ib, nrhs, MT, NT, KT;
   int grp = 1;
+  int tc = 0;       // FP32: trailing updates of A as tensor-core chunk tasks
+  int f64p = 0;     // FP32: panel steps in FP64 (the mixed form)
   int rows(int i) const { return std::min(nb, m - i * nb); }
   int cols(int k) const { return std::min(nb, n - k * nb); }
   int strips(int j) const { return j < NT ? (cols(j) + kTreeNW - 1) / kTreeNW : (nrhs + kTreeNW - 1) / kTreeNW; }
@@ -537,6 +653,8 @@ static double tree_cost(const TreeShape &sh, const TItem &it) {
     case OP_GE_TRAIL: return 4.0 * sh.rows(it.i) * std::min(sh.rows(it.i), sh.cols(it.k)) * w;
     case OP_PR_PANEL: return 3.0 * (ts ? sh.rows(it.p) : (it.b + 1) * ib) * ib * ib + lat;
     case OP_PR_APPLY: return 4.0 * (ts ? sh.rows(it.p) : (it.b + 1) * ib) * ib * w;
+    case OP_PR_TRAIL_TC: return 4.0 * sh.rows(it.p) * sh.cols(it.k) * tc::kChunk / 6.0;   // ~6x a SIMT strip
+    case OP_GE_TRAIL_TC: return 4.0 * sh.rows(it.i) * sh.cols(it.k) * tc::kChunk / 6.0;
     default: return (ts ? 4.0 * sh.rows(it.p) : 2.0 * nb) * sh.cols(it.k) * w;
   }
 }
@@ -617,7 +735,21 @@ static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::
         }
       }
       const int nbk = (kk + sh.ib - 1) / sh.ib;
-      for (int y = 0; y < ntrail(k); ++y) {
+      // tensor-core chunks of A's trailing columns for a full tile, then
+      // strips for the rest (B's columns)
+      int y0 = 0;
+      const int ca = std::max(0, sh.n - (k + 1) * sh.nb);
+      if (sh.tc && sh.rows(i) == sh.nb && kk == sh.nb && ca % tc::kChunk == 0) {
+        for (int ch = 0; ch < ca / tc::kChunk; ++ch) {
+          for (int q = 0; q < NSk; ++q) rd(rg(i, k, q, 1));
+          for (int b = 0; b < nbk; ++b) rd(rt(i, k, b, 0));
+          const int c0 = ch * tc::kChunk, j = k + 1 + c0 / sh.nb, s0 = (c0 % sh.nb) / kTreeNW;
+          for (int s = s0; s < s0 + tc::kChunk / kTreeNW; ++s) { wr(rg(i, j, s, 0)); wr(rg(i, j, s, 1)); }
+          emit(OP_GE_TRAIL_TC, k, 0, i, i, ch);
+        }
+        y0 = (ca + kTreeNW - 1) / kTreeNW;
+      }
+      for (int y = y0; y < ntrail(k); ++y) {
         int j, s;
         trail_js(k, y, j, s);
         for (int q = 0; q < NSk; ++q) rd(rg(i, k, q, 1));
@@ -655,7 +787,27 @@ static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::
         }
       }
       const int nbk = (kt + sh.ib - 1) / sh.ib;
-      for (int y = 0; y < ntrail(k); ++y) {
+      // tensor-core chunks of A's trailing columns for a merge of full tiles,
+      // then strips for the rest (B's columns)
+      int y0 = 0;
+      const int ca = std::max(0, sh.n - (k + 1) * sh.nb);
+      if (sh.tc && sh.rows(p) == sh.nb && sh.rows(i) == sh.nb && kt == sh.nb && ca % tc::kChunk == 0) {
+        for (int ch = 0; ch < ca / tc::kChunk; ++ch) {
+          for (int q = 0; q < NSk; ++q) {
+            rd(rg(p, k, q, 0));
+            if (ts) rd(rg(p, k, q, 1));
+          }
+          for (int b = 0; b < nbk; ++b) rd(rt(p, k, b, 1));
+          const int c0 = ch * tc::kChunk, j = k + 1 + c0 / sh.nb, s0 = (c0 % sh.nb) / kTreeNW;
+          for (int s = s0; s < s0 + tc::kChunk / kTreeNW; ++s) {
+            wr(rg(i, j, s, 0)); wr(rg(i, j, s, 1));
+            wr(rg(p, j, s, 0)); wr(rg(p, j, s, 1));
+          }
+          emit(OP_PR_TRAIL_TC | flag, k, 0, i, p, ch);
+        }
+        y0 = (ca + kTreeNW - 1) / kTreeNW;
+      }
+      for (int y = y0; y < ntrail(k); ++y) {
         int j, s;
         trail_js(k, y, j, s);
         for (int q = 0; q < NSk; ++q) {
@@ -699,7 +851,9 @@ static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::
 
 static long long tree_key(const TreeShape &sh) {
   long long h = 7809847782465536322LL;
-  for (int v : {sh.m, sh.n, sh.nb, sh.ib, sh.nrhs, sh.grp, 0x7ee})
+  // f64p changes no task or dependency (only the device routines of the
+  // panel tasks), so it shares the plan
+  for (int v : {sh.m, sh.n, sh.nb, sh.ib, sh.nrhs, sh.grp, sh.tc, 0x7ee})
     h = (h ^ (long long)v) * 1099511628211LL;
   return h & 0x7fffffffffffffffLL;
 }
@@ -755,10 +909,60 @@ static std::shared_ptr<TreePlan> tree_plan(const TreeShape &sh) {
   return p;
 }
 
+// The tensor-core and FP64-panel options of an FP32 task graph: tensor-core
+// chunks need full 256 x 256 tiles with ib = 32, a 16-byte aligned A and a
+// leading dimension that keeps every column 16-byte aligned; the FP64 panels
+// (mixed form) need full tiles and ib <= 32.
+static bool tree_tc_ok(const TreeShape &sh, const void *A, int lda) {
+  return sh.nb == 256 && sh.ib == tc::kIb && sh.m % sh.nb == 0 && sh.n % sh.nb == 0 && ((uintptr_t)A & 15) == 0 &&
+         (lda & 3) == 0;
+}
+static bool tree_f64p_ok(const TreeShape &sh) { return sh.m % sh.nb == 0 && sh.n % sh.nb == 0 && sh.ib <= 32; }
+
+// Bytes of the FP64 triangles of the mixed form (after the plan's bytes).
+static size_t tree_d_bytes(const TreeShape &sh) {
+  return align256(sizeof(double) * (size_t)sh.MT * sh.KT * sh.nb * sh.ib);
+}
+
+// Workspace covering the plain plan and, for FP32-eligible shapes, the
+// tensor-core plan (another task list) and the FP64 triangles.
+static size_t tree_work_bytes(TreeShape sh) {
+  size_t b = tree_plan(sh)->total_bytes;
+  const size_t d = tree_f64p_ok(sh) ? tree_d_bytes(sh) : 0;
+  b += d;
+  if (sh.nb == 256 && sh.ib == tc::kIb && sh.m % sh.nb == 0 && sh.n % sh.nb == 0) {
+    sh.tc = 1;
+    b = std::max(b, tree_plan(sh)->total_bytes + d);
+  }
+  return b;
+}
+
+template <typename R, bool TC>
+static cudaError_t tree_dag_launch(const TDagArgs<R> &a, size_t sm, cudaStream_t st) {
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_tree_dag<R, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) !=
+      cudaSuccess)
+    return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tree_dag<R, TC>, TQR_THREADS, sm)) !=
+      cudaSuccess)
+    return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const int grid = std::min(sms * per_sm, a.nitems);
+  k_tree_dag<R, TC><<<grid, TQR_THREADS, sm, st>>>(a);
+  count_launch();
+  return cudaGetLastError();
+}
+
+// mixed: FP32 only -- FP64 panel steps (and tensor-core updates where the
+// shape allows), the factorisation of the mixed-precision solve.  Plain FP32
+// graphs use the tensor cores too unless tqr_tile_dag_tensor_cores(0).
 template <typename R>
 static int tree_geqrf_dag_impl(int m, int n, int nb, int ib, R *A, int lda, R *T, R *T2, int ldt, R *tau,
                                R *tau2, int ldtau, int nrhs, R *B, int ldb, void *work, size_t lwork,
-                               cudaStream_t st, int grp = 1) {
+                               cudaStream_t st, int grp = 1, bool mixed = false) {
   if (grp <= 0) return -5;
   TreeGeom<R> g;
   int rc = tree_geom<R>(m, n, nrhs, nb, ib, A, lda, B, ldb, T, T2, ldt, tau, tau2, ldtau, &g, grp);
@@ -771,25 +975,25 @@ static int tree_geqrf_dag_impl(int m, int n, int nb, int ib, R *A, int lda, R *T
   if (nrhs > 0 && (!B || ldb < m)) return -15;
   TreeShape sh;
   if (!tree_dag_shape(m, n, nb, ib, nrhs, &sh, grp)) return -3;
+  if constexpr (std::is_same<R, float>::value) {
+    if (tree_tc_ok(sh, A, lda) && (mixed || tile_tc_enabled())) sh.tc = 1;
+    if (mixed) {
+      if (!tree_f64p_ok(sh)) return -3;
+      sh.f64p = 1;
+    }
+  } else {
+    if (mixed) return -3;
+  }
   std::shared_ptr<TreePlan> p = tree_plan(sh);
+  const size_t dbytes = sh.f64p ? tree_d_bytes(sh) : 0;
   if (!work || ((uintptr_t)work & 255)) return -16;
-  if (lwork < p->total_bytes) return -17;
+  if (lwork < p->total_bytes + dbytes) return -17;
   unsigned char *w = (unsigned char *)work;
   int *done = (int *)(w + align256(p->img_bytes));
   cudaError_t e;
   if ((e = cudaMemcpyAsync(w, p->image(), p->img_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess) return (int)e;
   if ((e = cudaMemsetAsync(done, 0, sizeof(int) * p->items.size(), st)) != cudaSuccess) return (int)e;
   if ((e = cudaMemset2DAsync(T2, sizeof(R) * ldt, 0, sizeof(R) * g.MT * ib, n, st)) != cudaSuccess) return (int)e;
-  if ((e = cudaFuncSetAttribute(k_tree_dag<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTreeSmem)) !=
-      cudaSuccess)
-    return (int)e;
-  int dev = 0, sms = 0, per_sm = 0;
-  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return (int)e;
-  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return (int)e;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tree_dag<R>, TQR_THREADS, kTreeSmem)) !=
-      cudaSuccess)
-    return (int)e;
-  if (per_sm < 1) return (int)cudaErrorInvalidConfiguration;
   TDagArgs<R> a;
   a.g = g;
   a.hdr = (TDagHeader *)w;
@@ -799,11 +1003,34 @@ static int tree_geqrf_dag_impl(int m, int n, int nb, int ib, R *A, int lda, R *T
   a.nitems = (int)p->items.size();
   a.key = p->key;
   a.timeout_ns = 20000000000ull;
-  const int grid = std::min(sms * per_sm, a.nitems);
-  k_tree_dag<R><<<grid, TQR_THREADS, kTreeSmem, st>>>(a);
-  count_launch();
-  e = cudaGetLastError();
+  if (sh.f64p) a.D = (double *)(w + p->total_bytes);
+  size_t sm = kTreeSmem;
+  if (sh.f64p)
+    sm = std::max({sm, panel_f64_smem(nb, ib), tsqrt_f64x_smem(nb, ib), ttqrt_f64_smem(nb, ib)});
+  if constexpr (std::is_same<R, float>::value) {
+    if (sh.tc) {
+      e = tree_dag_launch<R, true>(a, std::max(sm, tc::kSmem), st);
+      return e == cudaSuccess ? 0 : (int)e;
+    }
+  }
+  e = tree_dag_launch<R, false>(a, sm, st);
   return e == cudaSuccess ? 0 : (int)e;
+}
+
+int stile_gels_hqr_mixed(int m, int n, int nrhs, int nb, int ib, int grp, float *A, int lda, float *T, float *T2,
+                         int ldt, float *tau, float *tau2, int ldtau, float *B, int ldb, void *work, size_t lwork,
+                         cudaStream_t stream) {
+  if (nrhs < 0) return -3;
+  int rc = tree_geqrf_dag_impl<float>(m, n, nb, ib, A, lda, T, T2, ldt, tau, tau2, ldtau, nrhs, B, ldb, work, lwork,
+                                      stream, grp, true);
+  if (rc != 0) return rc;
+  return nrhs > 0 ? tqr_strsm_lun(n, nrhs, A, lda, B, ldb, stream) : 0;
+}
+
+size_t tree_dag_work_bytes(int m, int n, int nb, int ib, int grp, int nrhs) {
+  TreeShape sh;
+  if (!tree_dag_shape(m, n, nb, ib, nrhs, &sh, grp)) return 0;
+  return tree_work_bytes(sh);
 }
 
 }  // namespace tqr
@@ -859,7 +1086,7 @@ int tqr_tile_tree_dag_worksize(int m, int n, int nb, int ib, int nrhs, size_t *b
   if (!bytes) return -6;
   TreeShape sh;
   if (!tree_dag_shape(m, n, nb, ib, nrhs, &sh)) return -1;
-  *bytes = tree_plan(sh)->total_bytes;
+  *bytes = tree_work_bytes(sh);
   return 0;
 }
 
@@ -881,7 +1108,31 @@ int tqr_tile_hqr_dag_worksize(int m, int n, int nb, int ib, int grp, int nrhs, s
   if (!bytes) return -7;
   TreeShape sh;
   if (!tree_dag_shape(m, n, nb, ib, nrhs, &sh, grp)) return -1;
-  *bytes = tree_plan(sh)->total_bytes;
+  *bytes = tree_work_bytes(sh);
+  return 0;
+}
+
+int tqr_stile_geqrf_hqr_dag_f64p(int m, int n, int nb, int ib, int grp, float *A, int lda, float *T, float *T2,
+                                 int ldt, float *tau, float *tau2, int ldtau, int nrhs, float *B, int ldb, void *work,
+                                 size_t lwork, cudaStream_t stream) {
+  return tree_geqrf_dag_impl<float>(m, n, nb, ib, A, lda, T, T2, ldt, tau, tau2, ldtau, nrhs, B, ldb, work, lwork,
+                                    stream, grp, true);
+}
+
+int tqr_tile_hqr_dag_check_tc(int m, int n, int nb, int ib, int grp, int nrhs, long long *ntasks) {
+  TreeShape sh;
+  if (!tree_dag_shape(m, n, nb, ib, nrhs, &sh, grp)) return -1;
+  if (nb != 256 || ib != tc::kIb || m % nb || n % nb) return -1;
+  sh.tc = 1;
+  std::shared_ptr<TreePlan> p = tree_plan(sh);
+  long long ntc = 0;
+  for (size_t q = 0; q < p->items.size(); ++q) {
+    const TItem &it = p->items[q];
+    if ((it.type & 0x7f) == OP_PR_TRAIL_TC || (it.type & 0x7f) == OP_GE_TRAIL_TC) ++ntc;
+    for (int d = 0; d < (int)it.ndep; ++d)
+      if (p->deps[it.dep + d] >= q) return 1;
+  }
+  if (ntasks) *ntasks = ntc;
   return 0;
 }
 

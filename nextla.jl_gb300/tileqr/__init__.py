@@ -515,6 +515,12 @@ def tile_geqrf_f64p(A, nb=256, ib=32, T=None, tau=None):
     return T, tau
 
 
+def dsgels_hqr_group(grp):
+    """Factorisation schedule of lstsq_mixed: 0 = the flat tree, grp > 0 = the
+    hierarchical tree with groups of grp tiles; returns the previous setting."""
+    return int(_lib.lib().tqr_dsgels_hqr_group(int(grp)))
+
+
 def dsgels_fp64_panels(on):
     """Whether lstsq_mixed factors with FP64 panels (default True); returns
     the previous setting."""
@@ -576,14 +582,15 @@ def tree_dag_check(m, n, nb, ib, nrhs=0, grp=1):
     return nt.value
 
 
-def tile_geqrf_tree(A, nb=256, ib=32, B=None, dag=True, grp=1):
+def tile_geqrf_tree(A, nb=256, ib=32, B=None, dag=True, grp=1, f64p=False):
     """Tile QR of A in place with a binary reduction tree per panel (geqrt!
     on every tile, ttqrt!/ttmqr! merges).  Returns (T, tau, T2, tau2); with B,
     B is overwritten by Q^T B in the same pass.  dag=True runs it as one
     persistent launch when the shape allows (same results as the stream
-    driver).  grp > 1: the hierarchical form -- groups of grp tiles reduced
-    flat into their first tile (tsqrt!/tsmqr!), the group leaders by the
-    binary tree."""
+    driver for FP64).  grp > 1: the hierarchical form -- groups of grp tiles
+    reduced flat into their first tile (tsqrt!/tsmqr!), the group leaders by
+    the binary tree.  f64p=True (float32 A, task graph only): the mixed
+    solve's form, panel steps in FP64 (tqr_stile_geqrf_hqr_dag_f64p)."""
     import ctypes
     m, n = A.shape
     ts, taus = tile_shapes(m, n, nb, ib)
@@ -599,6 +606,8 @@ def tile_geqrf_tree(A, nb=256, ib=32, B=None, dag=True, grp=1):
         nrhs = B.shape[1]
         pb, ldb = _mat(B)
     ws = tree_dag_workspace(m, n, nb, ib, nrhs, A.device, grp) if dag else None
+    if ws is None and f64p:
+        raise ArgumentError("tile_geqrf_tree: f64p needs the persistent task graph's shape")
     if ws is None:
         _call(_prefix(A, T, tau, B), "tile_geqrf_hqr", m, n, nb, ib, grp, pa, lda, pt, _ptr(T2), ldt, pu,
               _ptr(tau2), ldu, nrhs, pb, ldb)
@@ -606,9 +615,11 @@ def tile_geqrf_tree(A, nb=256, ib=32, B=None, dag=True, grp=1):
     _, wp, size = ws
     p = _prefix(A, T, tau, B)
     st = torch.cuda.current_stream()
-    rc = getattr(_lib.lib(), f"tqr_{p}tile_geqrf_hqr_dag")(m, n, nb, ib, grp, pa, lda, pt, _ptr(T2), ldt, pu,
-                                                          _ptr(tau2), ldu, nrhs, pb, ldb, ctypes.c_void_p(wp),
-                                                          size, st.cuda_stream)
+    if f64p and p != "s":
+        raise TypeError("tile_geqrf_tree: f64p needs a float32 matrix")
+    fn = "tqr_stile_geqrf_hqr_dag_f64p" if f64p else f"tqr_{p}tile_geqrf_hqr_dag"
+    rc = getattr(_lib.lib(), fn)(m, n, nb, ib, grp, pa, lda, pt, _ptr(T2), ldt, pu, _ptr(tau2), ldu, nrhs, pb, ldb,
+                                 ctypes.c_void_p(wp), size, st.cuda_stream)
     if rc < 0:
         raise ArgumentError(f"tile_geqrf_tree: illegal value of argument {-rc}")
     if rc > 0:

@@ -201,6 +201,26 @@ def test_hqr_task_graph_is_topological(L, m, n, nb, ib, grp, nrhs):
     assert one.value == tree.value
 
 
+@pytest.mark.parametrize("m,n,grp,nrhs", [(4096, 1024, 4, 3), (8192, 512, 8, 0), (32768, 4096, 16, 4),
+                                        (2048, 2048, 2, 1)])
+def test_hqr_tensor_core_task_graph_is_topological(L, m, n, grp, nrhs):
+    """The FP32 hierarchical schedule with every trailing update of A (the
+    leaders' unmqr!, the tsqrt merges' tsmqr!, the ttqrt merges' ttmqr!) as
+    tensor-core chunk tasks: still topological, and one chunk task per 128
+    trailing columns of A per geqrt and per merge."""
+    import ctypes
+    nt = ctypes.c_longlong(0)
+    assert L.tqr_tile_hqr_dag_check_tc(m, n, 256, 32, grp, nrhs, ctypes.byref(nt)) == 0
+    MT, NT = m // 256, n // 256
+    expect = 0
+    for k in range(min(MT, NT)):
+        leaders = len(range(k, MT, grp))     # one geqrt! each
+        merges = (MT - k) - 1                # every tile but tile k is merged once
+        expect += (leaders + merges) * (n - (k + 1) * 256) // 128
+    assert nt.value == expect
+    assert L.tqr_tile_hqr_dag_check_tc(m + 100, n, 256, 32, grp, nrhs, ctypes.byref(nt)) == -1   # ragged
+
+
 def test_tile_autotune_argument_errors(L):
     nb, ib = ctypes.c_int(0), ctypes.c_int(0)
     assert L.tqr_tile_autotune(3, 64, 64, 0, ctypes.byref(nb), ctypes.byref(ib), NULL) == -1

@@ -193,3 +193,59 @@ def test_hqr_float_properties(tq, grp):
     QtA.copy_(A0)
     tq.tile_unmqr_tree("C", A, T, T2, QtA, nb, ib, grp=grp)
     assert (torch.linalg.norm(QtA[:n].double() - R) / torch.linalg.norm(R)).item() < 1e-5
+
+
+@pytest.mark.parametrize("m,n,grp", [(4096, 1024, 4), (8192, 512, 8), (2048, 768, 2)])
+def test_mixed_hqr_matches_oracle(tq, oracle, m, n, grp):
+    """The mixed solve's hierarchical factorisation (FP32 matrix; geqrt
+    blocks, tsqrt and ttqrt merges in FP64; the trailing updates on the
+    tensor cores) against the FP64 oracle's hierarchical tree on the same
+    FP32-valued input, at the FP32 bar; the stored factors apply Q^T to A
+    back to R."""
+    import torch
+    nb, ib = 256, 32
+    rng = np.random.default_rng(m + grp)
+    A0 = rng.standard_normal((m, n)).astype(np.float32).astype(np.float64)
+    A = tq.to_device(A0, dtype=torch.float32)
+    T, tau, T2, tau2 = tq.tile_geqrf_tree(A, nb, ib, grp=grp, f64p=True)
+    Ao = np.asfortranarray(A0)
+    To, tauo, T2o, tau2o = oracle.tile_geqrf_hqr(Ao, nb, ib, grp)
+    # the reference's Float32 pin is normwise isapprox at rtol 1e-5 for one
+    # kernel call (test/lapack_helpers.jl:14); a whole factorisation adds one
+    # FP32 update per tile row below, so the bar grows with sqrt(m / nb);
+    # entrywise against the largest entry at ten times that
+    bar = 1e-5 * np.sqrt(m / nb)
+    for x, y in ((A, Ao), (T, To), (tau, tauo), (T2, T2o), (tau2, tau2o)):
+        xg = tq.to_numpy(x).astype(np.float64)
+        assert np.linalg.norm(xg - y) <= bar * np.linalg.norm(y)
+        assert rel(xg, y) < 10 * bar
+    QtA = tq.to_device(A0, dtype=torch.float32)
+    tq.tile_unmqr_tree("C", A, T, T2, QtA, nb, ib, grp=grp)
+    R = np.triu(tq.to_numpy(A)[:n]).astype(np.float64)
+    assert np.linalg.norm(tq.to_numpy(QtA)[:n].astype(np.float64) - R) <= 1e-5 * np.linalg.norm(R)
+
+
+def test_mixed_hqr_is_more_orthogonal_than_fp32_panels(tq):
+    """FP64 panel steps in the hierarchical tree: the stored factor (Q formed
+    in FP64 from the FP32 V, T, T2) is closer to orthogonal than the same
+    tree with FP32 panels."""
+    import torch
+    m, n, nb, ib, grp = 8192, 1024, 256, 32, 8
+    g = torch.Generator(device="cuda").manual_seed(3)
+    A0 = tq.empty(m, n, dtype=torch.float32)
+    A0.copy_(torch.randn(m, n, generator=g, dtype=torch.float64, device="cuda"))
+    orth = {}
+    for f64p in (False, True):
+        A = A0.clone()
+        T, tau, T2, tau2 = tq.tile_geqrf_tree(A, nb, ib, grp=grp, f64p=f64p)
+        Fd = tq.empty(m, n)
+        Fd.copy_(A.double())
+        Td, T2d = tq.empty(*T.shape), tq.empty(*T2.shape)
+        Td.copy_(T.double())
+        T2d.copy_(T2.double())
+        Q = tq.zeros(m, n)
+        Q.diagonal().fill_(1.0)
+        tq.tile_unmqr_tree("N", Fd, Td, T2d, Q, nb, ib, grp=grp)
+        orth[f64p] = torch.linalg.norm(Q.t() @ Q - torch.eye(n, dtype=torch.float64, device="cuda")).item()
+    print(f"\nhqr {m}x{n} grp {grp}: ||I - Q^T Q||_F FP32 panels {orth[False]:.3e}, FP64 panels {orth[True]:.3e}")
+    assert orth[True] < 0.75 * orth[False]
