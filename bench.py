@@ -466,6 +466,21 @@ def ls_bench(tq, torch, m=32768, n=4096, k=4, steps=2, warmup=1, orth=True):
            "rel_diff_mixed_vs_fp64": (torch.linalg.norm(Xm - X64) / torch.linalg.norm(X64)).item(),
            "note": ("normwise backward error ||b - Ax||/(||A|| ||x|| + ||b||) is bounded below by the "
                     "1e-10 noise for any least-squares solution; both forms reach the same value")}
+    # the same solve on the flat tree (FP64 panels), for comparison
+    oldg = tq.dsgels_hqr_group(0)
+    try:
+        tfl = []
+        for rep in range(warmup + steps):
+            (Xf, itf, _), ms = timed(lambda: tq.lstsq_mixed(Ac, bc, NB, IB, maxit=60, tol=1e-13))
+            if rep >= warmup:
+                tfl.append(ms)
+                phf = tq.dsgels_phases()
+        res["flat_tree"] = {"mixed_ms": min(tfl), "iterations": itf, "qr32_ms": phf["qr32_ms"],
+                            "rel_diff_vs_fp64": (torch.linalg.norm(Xf - X64) / torch.linalg.norm(X64)).item()}
+    finally:
+        tq.dsgels_hqr_group(oldg)
+    res["schedule"] = (f"hierarchical tree, groups of {oldg} tiles" if oldg and m // NB >= 2 * oldg
+                       else "flat tree")
     # the same solve with the FP32 panels, for comparison (time, iterations)
     old = tq.dsgels_fp64_panels(False)
     try:
@@ -491,16 +506,35 @@ def ls_bench(tq, torch, m=32768, n=4096, k=4, steps=2, warmup=1, orth=True):
             o = torch.linalg.norm(Q.t() @ Q - torch.eye(n, dtype=torch.float64, device="cuda")).item()
             del Fd, Td, Q
             return o
-        for tag in ("mixed", "mixed_fp32_panels", "fp64"):
+        for tag in ("mixed_flat", "mixed_fp32_panels", "fp64"):
             dt = torch.float64 if tag == "fp64" else torch.float32
             F = tq.empty(m, n, dtype=dt)
             F.copy_(A32 if dt == torch.float32 else A64)
-            if tag == "mixed":
+            if tag == "mixed_flat":
                 T, _ = tq.tile_geqrf_f64p(F, NB, IB)
             else:
                 T, _ = tq.tile_geqrf(F, NB, IB)
             res[f"orth_I_minus_QtQ_fro_{tag}"] = orth_of(F, T)
             del F, T
+        # the factor the default mixed solve uses: the hierarchical tree
+        grp = tq.dsgels_hqr_group(0)
+        tq.dsgels_hqr_group(grp)
+        if grp and m // NB >= 2 * grp:
+            F = tq.empty(m, n, dtype=torch.float32)
+            F.copy_(A32)
+            T, _, T2, _ = tq.tile_geqrf_tree(F, NB, IB, grp=grp, f64p=True)
+            Fd, Td, T2d = tq.empty(m, n), tq.empty(*T.shape), tq.empty(*T2.shape)
+            Fd.copy_(F.double())
+            Td.copy_(T.double())
+            T2d.copy_(T2.double())
+            Q = tq.zeros(m, n)
+            Q.diagonal().fill_(1.0)
+            tq.tile_unmqr_tree("N", Fd, Td, T2d, Q, NB, IB, grp=grp)
+            res["orth_I_minus_QtQ_fro_mixed"] = torch.linalg.norm(
+                Q.t() @ Q - torch.eye(n, dtype=torch.float64, device="cuda")).item()
+            del F, T, T2, Fd, Td, T2d, Q
+        else:
+            res["orth_I_minus_QtQ_fro_mixed"] = res["orth_I_minus_QtQ_fro_mixed_flat"]
     return res
 
 
@@ -1085,6 +1119,10 @@ def summaries(ls, bat, adj, tall, noalloc):
             out["mixed_ls_32768x4096"]["orth_mixed"] = float(f"{ls['orth_I_minus_QtQ_fro_mixed']:.2e}")
             out["mixed_ls_32768x4096"]["orth_fp32_panels"] = float(
                 f"{ls['orth_I_minus_QtQ_fro_mixed_fp32_panels']:.2e}")
+        if ls.get("flat_tree"):
+            out["mixed_ls_32768x4096"]["flat_tree_ms_iters"] = [round(ls["flat_tree"]["mixed_ms"], 1),
+                                                                ls["flat_tree"]["iterations"]]
+            out["mixed_ls_32768x4096"]["schedule"] = ls.get("schedule")
         if ls.get("fp32_panels"):
             out["mixed_ls_32768x4096"]["fp32_panels_ms_iters"] = [round(ls["fp32_panels"]["mixed_ms"], 1),
                                                                   ls["fp32_panels"]["iterations"]]

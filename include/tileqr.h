@@ -508,11 +508,12 @@ int tqr_dsgels_phases(double *ms, int *iters);
  * panels instead (for comparison); 1 restores the default.  Returns the
  * previous setting.  Process-wide. */
 int tqr_dsgels_fp64_panels(int on);
-/* tqr_dsgels_hqr_group(grp): grp > 0 makes later tqr_dsgels calls factor with
- * the hierarchical tree (groups of grp tiles reduced flat, leaders by the
- * binary tree; tqr_stile_geqrf_hqr_dag_f64p) when m and n are multiples of
- * nb; 0 restores the flat tree.  Returns the previous setting.  Process-wide;
- * tqr_dsgels_worksize depends on it. */
+/* tqr_dsgels_hqr_group(grp): grp > 0 (default 16) makes tqr_dsgels factor
+ * with the hierarchical tree (groups of grp tiles reduced flat, leaders by
+ * the binary tree; tqr_stile_geqrf_hqr_dag_f64p) when m and n are multiples
+ * of nb and A has at least 2 grp tile rows; 0 selects the flat tree always.
+ * Returns the previous setting.  Process-wide; tqr_dsgels_worksize depends
+ * on it. */
 int tqr_dsgels_hqr_group(int grp);
 /* The FP32 tile QR with FP64 panels on its own (the factorisation of
  * tqr_dsgels, without B): as tqr_stile_geqrf_dag, same T/tau layouts; `work`

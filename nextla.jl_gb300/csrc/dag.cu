@@ -887,6 +887,7 @@ static size_t f64p_bytes(const DagGeom &g) {
 // tqr_dsgels factors with FP64 panels unless a caller switches that off
 // (tqr_dsgels_fp64_panels(0)), e.g. to compare with the all-FP32 panels.
 static int g_f64p_enabled = 1;
+bool dsgels_f64p_enabled() { return g_f64p_enabled != 0; }
 
 int stile_gels_dag_mixed(int m, int n, int nrhs, int nb, int ib, float *A, int lda, float *T, int ldt,
                          float *tau, int ldtau, float *B, int ldb, void *work, size_t lwork, cudaStream_t stream) {

@@ -665,10 +665,18 @@ struct MixedWs {
   size_t F, T, tau, T2, tau2, dag, x32, r, s, p, t, q, sc, rinv, rinvt, tmpn, gbar, total;
 };
 
-// Factorisation schedule of tqr_dsgels: 0 = the flat tree (one tsqrt chain
-// per panel), grp > 0 = the hierarchical tree with groups of grp tiles
-// (tqr_dsgels_hqr_group).
-static int g_dsgels_grp = 0;
+// Factorisation schedule of tqr_dsgels: grp > 0 = the hierarchical tree with
+// groups of grp tiles for matrices of at least 2 grp tile rows (the FP64
+// panel steps make the flat tree's tsqrt chain per panel the critical path:
+// 32768 x 4096 factors in 86.8 ms with groups of 16 against 109.4 ms flat);
+// 0 = always the flat tree (tqr_dsgels_hqr_group).
+static int g_dsgels_grp = 16;
+
+// (the hierarchical form exists with FP64 panel steps only: with
+// tqr_dsgels_fp64_panels(0) the solve uses the flat tree)
+static bool use_hqr(int m, int n, int nb, int ib) {
+  return g_dsgels_grp > 0 && dsgels_f64p_enabled() && m % nb == 0 && n % nb == 0 && ib <= 32 && m / nb >= 2 * g_dsgels_grp;
+}
 
 static size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -683,7 +691,7 @@ static int mixed_ws(int m, int n, int k, int nb, int ib, MixedWs *w) {
   w->tau2 = take(sizeof(float) * (size_t)n * MT);
   size_t dag = 0;
   if (tqr_tile_gels_worksize(m, n, k, nb, ib, &dag) != 0) dag = 0;
-  if (g_dsgels_grp > 0) dag = std::max(dag, tree_dag_work_bytes(m, n, nb, ib, g_dsgels_grp, k));
+  if (use_hqr(m, n, nb, ib)) dag = std::max(dag, tree_dag_work_bytes(m, n, nb, ib, g_dsgels_grp, k));
   w->dag = take(dag ? dag : 256);
   w->x32 = take(sizeof(float) * (size_t)m * k);
   w->r = take(sizeof(double) * (size_t)m * k);
@@ -768,8 +776,7 @@ int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, 
   LS_CU(cudaGetLastError());
   size_t dagb = 0;
   float *T2 = (float *)(base + w.T2), *tau2 = (float *)(base + w.tau2);
-  const size_t hqrb = g_dsgels_grp > 0 ? tree_dag_work_bytes(m, n, nb, ib, g_dsgels_grp, k) : 0;
-  if (hqrb > 0 && m % nb == 0 && n % nb == 0 && ib <= 32) {
+  if (use_hqr(m, n, nb, ib) && tree_dag_work_bytes(m, n, nb, ib, g_dsgels_grp, k) > 0) {
     // the hierarchical tree: B rides along as extra trailing columns
     LS_TRY(stile_gels_hqr_mixed(m, n, k, nb, ib, g_dsgels_grp, F, m, T, T2, MT * ib, tau, tau2, n, x32, m,
                                 base + w.dag, w.x32 - w.dag, st));

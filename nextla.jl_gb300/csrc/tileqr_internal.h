@@ -70,6 +70,8 @@ int stile_gels_dag_mixed(int m, int n, int nrhs, int nb, int ib, float *A, int l
 // Whether FP32 persistent schedules may use the tensor cores
 // (tqr_tile_dag_tensor_cores; dag.cu).
 bool tile_tc_enabled();
+// Whether tqr_dsgels factors with FP64 panel steps (tqr_dsgels_fp64_panels).
+bool dsgels_f64p_enabled();
 
 // The mixed solve's factorisation as the hierarchical tree (tree.cu): groups
 // of grp tiles reduced flat, the leaders by the binary tree, FP64 panel steps,

@@ -516,8 +516,9 @@ def tile_geqrf_f64p(A, nb=256, ib=32, T=None, tau=None):
 
 
 def dsgels_hqr_group(grp):
-    """Factorisation schedule of lstsq_mixed: 0 = the flat tree, grp > 0 = the
-    hierarchical tree with groups of grp tiles; returns the previous setting."""
+    """Factorisation schedule of lstsq_mixed: grp > 0 = the hierarchical tree
+    with groups of grp tiles when A has at least 2 grp tile rows (default
+    16), 0 = the flat tree always; returns the previous setting."""
     return int(_lib.lib().tqr_dsgels_hqr_group(int(grp)))
 
 
