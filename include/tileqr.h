@@ -625,6 +625,13 @@ int tqr_stsmqr_tc(int m1, int n, int m2, int k, float *A1, int lda1, float *A2, 
  * strips only), (1) back on; returns the previous setting.
  * tqr_tile_dag_check_tc: host replay check of that schedule. */
 int tqr_tile_dag_tensor_cores(int on);
+/* The tensor-core updates (tqr_stsmqr_tc and the tensor-core tasks of the
+ * FP32 persistent kernels) load A2, A1 and V with the tensor memory
+ * accelerator (cp.async.bulk.tensor, 128-byte swizzle, tensor maps encoded on
+ * the host per launch); tqr_tile_tc_tma(0) makes them use 16-byte cp.async
+ * copies into the same layout instead (the same results bit for bit), (1)
+ * restores TMA.  Returns the previous setting.  Process-wide. */
+int tqr_tile_tc_tma(int on);
 /* Resident CTAs per SM and dynamic shared memory of the persistent tile
  * kernel at nb = 256, ib = 32 (dtype_bytes 8 or 4; tensor_cores for FP32). */
 int tqr_tile_dag_occupancy(int dtype_bytes, int tensor_cores, int *ctas_per_sm, int *smem_bytes);

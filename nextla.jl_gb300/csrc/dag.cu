@@ -212,6 +212,11 @@ struct DagArgs {
   unsigned long long timeout_ns;
   int hold = 0;     // failure-detection test: task 0 also waits for a header word nothing writes
   double *D = nullptr;   // g.f64p: FP64 diagonal R triangles, ib x (KT nb), ld ib
+  // g.tc with tma: tensor maps of A for the TC tasks' TMA loads (32 x 128 and
+  // 32 x 32 boxes); the kernel takes DagArgs as a __grid_constant__ parameter
+  // so their addresses are valid operands
+  CUtensorMap tmw, tmn;
+  int tma = 0;
 };
 
 __device__ __forceinline__ int ld_acquire(const int *p) {
@@ -280,8 +285,10 @@ __device__ bool run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *
     if constexpr (TC && std::is_same<R, float>::value) {
       unsigned char *al = smem + ((1024 - (tc::saddr(smem) & 1023)) & 1023);
       const size_t c0 = (size_t)s * tc::kChunk;
+      const tc::TcMaps mp{&a.tmw, &a.tmw, &a.tmn, k * nb, j * nb + (int)c0, i * nb, j * nb + (int)c0, i * nb, k * nb};
       return tc::tsmqr_chunk(nb, nb, tile(k, j) + c0 * a.lda, a.lda, tile(i, j) + c0 * a.lda, a.lda, tile(i, k),
-                             a.lda, ttile(i, k), a.ldt, tcs->tmem, tcs->bars, tcs->phase, al);
+                             a.lda, ttile(i, k), a.ldt, tcs->tmem, tcs->bars, tcs->phase, al, tc::kVFull,
+                             a.tma ? &mp : nullptr);
     } else {
       return false;
     }
@@ -336,7 +343,7 @@ __device__ bool run_item(const DagArgs<R> &a, const DagItem &it, unsigned char *
 
 template <typename R, int NW, bool TC>
 __global__ void __launch_bounds__(TQR_THREADS, TC ? 1 : 2)
-k_tile_dag(const DagArgs<R> a)
+k_tile_dag(const __grid_constant__ DagArgs<R> a)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_it, s_err;
@@ -351,7 +358,7 @@ k_tile_dag(const DagArgs<R> a)
     if (tid == 0 && blockIdx.x == 0) atomicExch(&a.hdr->error, 2);
     return;
   }
-  TcState tcs{0u, s_bars, {0u, 0u, 0u}};
+  TcState tcs{0u, s_bars, {0u, 0u, 0u, 0u}};
   bool tc_failed = false;
   if constexpr (TC && std::is_same<R, float>::value) {
     if (a.g.tc) {
@@ -752,6 +759,11 @@ static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int
   a.nitems = (int)plan->items.size();
   a.key = plan->key;
   if (g.f64p) a.D = (double *)(w + 256 + plan->bytes_counters + plan->bytes_items);
+  if constexpr (std::is_same<R, float>::value) {
+    if (g.tc && tc_tma_enabled())
+      a.tma = make_tmap_f32(&a.tmw, A, m, (long long)g.NTA * nb, lda, 32, tc::kChunk) == cudaSuccess &&
+              make_tmap_f32(&a.tmn, A, m, (long long)g.NTA * nb, lda, 32, tc::kIb) == cudaSuccess;
+  }
   a.timeout_ns = 20ull * 1000ull * 1000ull * 1000ull;   // 20 s for any single wait
   if (hold_ns) {
     a.timeout_ns = hold_ns;

@@ -1,10 +1,62 @@
 // tc.cu -- stand-alone launcher of the tensor-core FP32 tsmqr update
 // (tc_apply.cuh): one CTA per 128-column chunk of [A1; A2].
+#include <mutex>
+
 #include "tc_apply.cuh"
 #include "tileqr.h"
 #include "tileqr_internal.h"
 
 namespace tqr {
+
+// ---- tensor maps for the tensor-core chunk routine's TMA loads -------------
+// cuTensorMapEncodeTiled is a driver entry point; it is looked up once through
+// the runtime (no link against the driver library).
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn tmap_encoder() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+cudaError_t make_tmap_f32(void *tm, const float *base, long long rows, long long cols, long long ld, int box_rows,
+                          int box_cols) {
+  // 16-byte aligned base and column stride; the inner box spans at most the
+  // 128-byte swizzle; FP32 inner extent a multiple of 16 bytes
+  if (!tm || !base || ((uintptr_t)base & 15) || ((ld * 4) & 15) || rows <= 0 || cols <= 0 || ld < rows ||
+      box_rows <= 0 || box_rows * 4 > 128 || (box_rows * 4) % 16 || box_cols <= 0 || box_cols > 256)
+    return cudaErrorInvalidValue;
+  EncodeTiledFn f = tmap_encoder();
+  if (!f) return cudaErrorNotSupported;
+  const cuuint64_t dims[2] = {(cuuint64_t)rows, (cuuint64_t)cols};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * 4};
+  const cuuint32_t box[2] = {(cuuint32_t)box_rows, (cuuint32_t)box_cols};
+  const cuuint32_t es[2] = {1, 1};
+  const CUresult r = f(static_cast<CUtensorMap *>(tm), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base),
+                       dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+static int g_tma_enabled = 1;
+bool tc_tma_enabled() { return g_tma_enabled != 0; }
+
+// The stand-alone launch's maps of A1, A2 and V (kernel parameter space).
+struct TcLaunchMaps {
+  CUtensorMap a1, a2, v;
+  int tma;
+};
 
 // TMEM allocation / release and the MMA mbarriers for one CTA.
 __device__ __forceinline__ void tc_setup(uint64_t *bars, uint32_t *tmem_slot) {
@@ -38,17 +90,18 @@ __device__ __forceinline__ void tc_teardown(uint64_t *bars, uint32_t *phase, boo
 
 __global__ void __launch_bounds__(TQR_THREADS, 1)
 k_tsmqr_tc(int m2, int k, float *A1, int lda1, float *A2, int lda2, const float *V, int ldv, const float *T, int ldt,
-           int *err) {
+           int *err, const __grid_constant__ TcLaunchMaps maps) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bars[tc::kBars];
   __shared__ uint32_t tmem_slot;
   unsigned char *smem = smem_raw + ((1024 - (tc::saddr(smem_raw) & 1023)) & 1023);
   tc_setup(bars, &tmem_slot);
   const uint32_t tmem = tmem_slot;
-  uint32_t phase[tc::kBars] = {0u, 0u, 0u};
+  uint32_t phase[tc::kBars] = {0u, 0u, 0u, 0u};
   const size_t c0 = (size_t)blockIdx.x * tc::kChunk;
+  const tc::TcMaps mp{&maps.a1, &maps.a2, &maps.v, 0, (int)c0, 0, (int)c0, 0, 0};
   const bool ok = tc::tsmqr_chunk(m2, k, A1 + c0 * lda1, lda1, A2 + c0 * lda2, lda2, V, ldv, T, ldt, tmem, bars,
-                                  phase, smem);
+                                  phase, smem, tc::kVFull, maps.tma ? &mp : nullptr);
   if (!ok && threadIdx.x == 0) atomicExch(err, 1);
   tc_teardown(bars, phase, !ok, tmem);
 }
@@ -78,10 +131,20 @@ int tqr_stsmqr_tc(int m1, int n, int m2, int k, float *A1, int lda1, float *A2, 
   const size_t sm = tc::kSmem;
   cudaError_t e = cudaFuncSetAttribute(k_tsmqr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return (int)e;
-  k_tsmqr_tc<<<n / tc::kChunk, TQR_THREADS, sm, stream>>>(m2, k, A1, lda1, A2, lda2, V, ldv, T, ldt, err);
+  TcLaunchMaps maps;
+  maps.tma = tc_tma_enabled() && make_tmap_f32(&maps.a1, A1, m1, n, lda1, 32, tc::kChunk) == cudaSuccess &&
+             make_tmap_f32(&maps.a2, A2, m2, n, lda2, 32, tc::kChunk) == cudaSuccess &&
+             make_tmap_f32(&maps.v, V, m2, k, ldv, 32, tc::kIb) == cudaSuccess;
+  k_tsmqr_tc<<<n / tc::kChunk, TQR_THREADS, sm, stream>>>(m2, k, A1, lda1, A2, lda2, V, ldv, T, ldt, err, maps);
   count_launch();
   e = cudaGetLastError();
   return e == cudaSuccess ? 0 : (int)e;
+}
+
+int tqr_tile_tc_tma(int on) {
+  const int old = tqr::g_tma_enabled;
+  tqr::g_tma_enabled = on ? 1 : 0;
+  return old;
 }
 
 }  // extern "C"

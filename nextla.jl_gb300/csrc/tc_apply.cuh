@@ -35,6 +35,8 @@
 // issues no further MMA.  Kernels that use TMEM run one CTA per SM, so the
 // routine has the SM's TMEM and up to 227 KB of shared memory to itself.
 #pragma once
+#include <cuda.h>   // CUtensorMap (the tensor maps are encoded on the host)
+
 #include "common.cuh"
 
 namespace tqr {
@@ -50,24 +52,62 @@ constexpr int kTmemCols = 512;
 constexpr uint32_t kA2Col = 256;
 // dynamic shared memory: two GEMM1 stage buffers, each A hi/lo (2 x 32 KB) and
 // B hi/lo (2 x 8 KB); GEMM2 reuses them (V_b^T hi/lo in stage 0's A, W^T
-// hi/lo in stage 1's A), and A2 passes through them (column stride kRawLd)
-// on its way into and out of TMEM; then the raw V_b and A1_b of the current
-// block (fetched with cp.async one block ahead) and the T block.  The raw
-// strides (260 and 36 floats) put consecutive columns 16 bytes apart modulo
-// 128, so a warp reading one 16-byte run per column, or 8 columns by 4 runs,
-// spreads over all banks.
+// hi/lo in stage 1's A), and A2 passes through them on its way into and out
+// of TMEM as m2 / 32 boxes of 32 rows x 128 columns; then V_b (m2 / 32 boxes
+// of 32 rows x 32 columns) and A1_b (one box of 32 rows x 128 columns) of the
+// current block, fetched one block ahead, and the T block.  The raw buffers
+// use the 128-byte swizzle of the tensor memory accelerator's tiled loads:
+// a box is stored as 128-byte rows (32 consecutive matrix rows of one
+// column), and in row y the 16-byte chunk c sits at position c ^ (y % 8).
+// The TMA loads write them so, the cp.async fallback writes the same layout,
+// and every reader (one 16-byte run per column, 8 columns by 4 runs, or 32
+// consecutive rows of a column per warp) spreads over all banks.
 constexpr size_t kBufA = 32768, kBufB = 8192;
 constexpr size_t kStage = 2 * kBufA + 2 * kBufB;
-constexpr int kRawLd = 260, kA1Ld = 36, kTLd = 36;
-constexpr size_t kVraw = sizeof(float) * 32 * kRawLd;     // V_b: 32 columns of m2 rows
-constexpr size_t kA1s = sizeof(float) * 128 * kA1Ld;      // A1_b: 128 columns of 32 rows
-constexpr size_t kTs = sizeof(float) * 32 * kTLd;         // T_b: 32 x 32
+constexpr uint32_t kA2Box = 32 * kChunk * 4;               // 32 rows x 128 columns
+constexpr uint32_t kVBox = 32 * kIb * 4;                   // 32 rows x 32 columns
+constexpr int kTLd = 36;
+constexpr size_t kVraw = 8 * (size_t)kVBox;                // V_b: up to 256 rows
+constexpr size_t kA1s = kA2Box;                            // A1_b: 32 rows x 128 columns
+constexpr size_t kTs = sizeof(float) * 32 * kTLd;          // T_b: 32 x 32
 constexpr size_t kSmem = 2 * kStage + kVraw + kA1s + kTs + 1024;
-static_assert(sizeof(float) * 128 * kRawLd <= 2 * kStage, "A2 staging fits the stage buffers");
-constexpr int kBars = 3;               // GEMM1 stage 0, GEMM1 stage 1, GEMM2
+static_assert(8 * (size_t)kA2Box <= 2 * kStage, "A2 staging fits the stage buffers");
+static_assert((2 * kStage) % 1024 == 0 && kVraw % 1024 == 0, "swizzled boxes start 1024-byte aligned");
+constexpr int kBars = 4;               // GEMM1 stage 0, GEMM1 stage 1, GEMM2, operand loads
 constexpr long kWaitLimit = 1L << 26;  // mbarrier polls before giving up
 
 __device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Byte offset of element (r, c) -- matrix row r, column c -- in a stack of
+// 128-byte-swizzled boxes of 32 rows each, box_bytes apart (see above).
+__device__ __forceinline__ uint32_t swz(int r, int c, uint32_t box_bytes) {
+  return (uint32_t)(r >> 5) * box_bytes + (uint32_t)c * 128u +
+         ((uint32_t)(((r & 31) >> 2) ^ (c & 7)) << 4) + ((uint32_t)(r & 3) << 2);
+}
+
+// Where the operands come from: tensor maps of the FP32 matrices (128-byte
+// swizzle; a1 and a2 with 32 x 128 boxes, v with 32 x 32 boxes) and the
+// element coordinates (row, column) of A1, A2 and V.  Loads then go through
+// the tensor memory accelerator; a null TcMaps uses 16-byte cp.async copies
+// into the same layout.
+struct TcMaps {
+  const CUtensorMap *a1, *a2, *v;
+  int a1r, a1c, a2r, a2c, vr, vc;
+};
+
+// One tiled TMA load of a 2-D box at element coordinates (x = row, y =
+// column), completing on the mbarrier with its byte count.  x is a multiple
+// of 32 here (16-byte aligned start for FP32).
+__device__ __forceinline__ void tma_load2d(void *sdst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(saddr(sdst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(saddr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void arm_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
+}
 
 // tcgen05 shared-memory matrix descriptor: no swizzle, version 1.
 __device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
@@ -188,37 +228,69 @@ __device__ __forceinline__ float vmask(int vmode, int r, int diag, float v) {
   return v;
 }
 
-// Block b's raw operands by 16-byte cp.async copies, one commit group:
-// V_b (m2 x 32) -> Vraw (column stride kRawLd), A1_b (32 x 128) -> A1s
-// (column stride kA1Ld; skipped when A1b is null).  Sources 16-byte aligned,
-// leading dimensions multiples of 4; consecutive threads copy consecutive 16
-// bytes of a column.
-__device__ __forceinline__ void prefetch_block(const float *Vb, int ldv, int m2, float *Vraw, const float *A1b,
-                                               int lda1, float *A1s) {
+// Bytes of block b's operands (V_b, and A1_b when there is one).
+__device__ __forceinline__ uint32_t block_bytes(int m2, bool has_a1) {
+  return (uint32_t)m2 * kIb * 4 + (has_a1 ? kA2Box : 0u);
+}
+
+// The TMA boxes of block b's operands (one thread; the barrier is armed by
+// the caller for every byte of the phase before the first load is issued).
+__device__ __forceinline__ void tma_block(const TcMaps *mp, int b, int m2, unsigned char *Vraw, bool has_a1,
+                                          unsigned char *A1s, uint64_t *bar) {
+  for (int q = 0; q < m2 / 32; ++q) tma_load2d(Vraw + q * kVBox, mp->v, mp->vr + 32 * q, mp->vc + b * kIb, bar);
+  if (has_a1) tma_load2d(A1s, mp->a1, mp->a1r + b * kIb, mp->a1c, bar);
+}
+
+// Block b's raw operands into the swizzled Vraw (V_b, m2 x 32) and A1s
+// (A1_b, 32 x 128; skipped when A1b is null).  TMA: thread 0 arms bar with
+// the byte count and issues the boxes (the caller has synchronised the CTA
+// since the buffers were last read); otherwise every thread issues 16-byte
+// cp.async copies, one commit group.  Sources 16-byte aligned, leading
+// dimensions multiples of 4.
+__device__ __forceinline__ void prefetch_block(const TcMaps *mp, int b, const float *Vb, int ldv, int m2,
+                                               unsigned char *Vraw, const float *A1b, int lda1, unsigned char *A1s,
+                                               uint64_t *bar) {
+  if (mp) {
+    if (threadIdx.x == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      arm_tx(bar, block_bytes(m2, A1b != nullptr));
+      tma_block(mp, b, m2, Vraw, A1b != nullptr, A1s, bar);
+    }
+    return;
+  }
   const int per_col = m2 / 4;
   for (int idx = threadIdx.x; idx < kIb * per_col; idx += TQR_THREADS) {
     const int p = idx / per_col, r4 = idx % per_col;
-    cp16(Vraw + p * kRawLd + 4 * r4, Vb + (size_t)p * ldv + 4 * r4);
+    cp16(Vraw + swz(4 * r4, p, kVBox), Vb + (size_t)p * ldv + 4 * r4);
   }
   for (int idx = threadIdx.x; A1b && idx < kChunk * (kIb / 4); idx += TQR_THREADS) {
     const int cc = idx / (kIb / 4), p4 = idx % (kIb / 4);
-    cp16(A1s + cc * kA1Ld + 4 * p4, A1b + (size_t)cc * lda1 + 4 * p4);
+    cp16(A1s + swz(4 * p4, cc, 0), A1b + (size_t)cc * lda1 + 4 * p4);
   }
   cp_commit();
 }
 
+// Waits (all threads) for the loads prefetch_block or the A2 load issued:
+// the TMA mbarrier phase (bounded), or every cp.async group and a CTA barrier.
+__device__ __forceinline__ bool loads_wait(const TcMaps *mp, uint64_t *bar, uint32_t *phase) {
+  if (mp) return wait_phase(bar, phase);
+  prefetch_wait();
+  __syncthreads();
+  return true;
+}
+
 // GEMM1's B operand for rows [r0, r0 + kKc) from Vraw: row-of-operand p, K =
-// r.  Lanes take 8 p by 4 K runs, so the 16-byte reads (column stride
-// kRawLd) and the core-matrix stores each spread over all banks.
-__device__ __forceinline__ void stage_vb1(const float *Vraw, int r0, unsigned char *hi, unsigned char *lo, int vmode,
-                                          int d0) {
+// r.  Lanes take 8 p by 4 K runs, so the 16-byte reads (swizzled) and the
+// core-matrix stores each spread over all banks.
+__device__ __forceinline__ void stage_vb1(const unsigned char *Vraw, int r0, unsigned char *hi, unsigned char *lo,
+                                          int vmode, int d0) {
   constexpr uint32_t SB = (kKc / 4) * 128;
 #pragma unroll
   for (int u = 0; u < kIb * kKc / 4 / TQR_THREADS; ++u) {
     const int idx = threadIdx.x + u * TQR_THREADS;
     const int rest = idx >> 5;
     const int p = 8 * (rest & 3) + (idx & 7), k4 = 4 * (rest >> 2) + ((idx >> 3) & 3);
-    float4 x = *reinterpret_cast<const float4 *>(Vraw + p * kRawLd + r0 + 4 * k4);
+    float4 x = *reinterpret_cast<const float4 *>(Vraw + swz(r0 + 4 * k4, p, kVBox));
     if (vmode != kVFull) {
       const int r = r0 + 4 * k4, dg = d0 + p;
       x.x = vmask(vmode, r, dg, x.x); x.y = vmask(vmode, r + 1, dg, x.y);
@@ -295,7 +367,7 @@ __device__ __forceinline__ void st32(uint32_t taddr, const float (&v)[32]) {
 // (in at the start, out at the end) instead of twice per block.
 __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2, int lda2, const float *V, int ldv,
                                    const float *T, int ldt, uint32_t tmem, uint64_t *bars, uint32_t *phase,
-                                   unsigned char *smem, int vmode = kVFull) {
+                                   unsigned char *smem, int vmode = kVFull, const TcMaps *mp = nullptr) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // warps w and w + 4 reach TMEM lanes [32 (w % 4), 32 (w % 4) + 32): this
   // thread's lane is chunk column c; the two warp sets split A2's rows
@@ -303,9 +375,9 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
   const uint32_t d2t = tmem + ((uint32_t)((warp & 3) * 32) << 16);
   const uint32_t a2t = d2t + kA2Col;
   unsigned char *st_base[2] = {smem, smem + kStage};
-  float *A2raw = reinterpret_cast<float *>(smem);                                  // 128 x kRawLd
-  float *Vraw = reinterpret_cast<float *>(smem + 2 * kStage);                      // 32 x kRawLd
-  float *A1s = reinterpret_cast<float *>(smem + 2 * kStage + kVraw);               // 128 x kA1Ld
+  unsigned char *A2raw = smem;                                                     // m2 / 32 boxes
+  unsigned char *Vraw = smem + 2 * kStage;                                         // m2 / 32 boxes
+  unsigned char *A1s = smem + 2 * kStage + kVraw;                                  // one box
   float *Ts = reinterpret_cast<float *>(smem + 2 * kStage + kVraw + kA1s);         // 32 x kTLd
   // GEMM2 operands in the stage buffers' A regions
   unsigned char *vHi = smem, *vLo = smem + kBufA;                    // V_b^T: m2 x 32, K-major (B)
@@ -314,26 +386,43 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
   const uint32_t d1 = tmem;
   const int nq = m2 / kKc, half = m2 / 2, per_col = m2 / 4, nblk = k / kIb;
   constexpr uint32_t SB = (kKc / 4) * 128;
+  bool loads_pending = false;
   auto fail = [&]() {
-    prefetch_wait();   // no copy into shared memory outlives the routine
+    // no copy into shared memory outlives the routine
+    if (mp) {
+      if (loads_pending) bar_wait(&bars[3], phase[3]);
+    } else {
+      prefetch_wait();
+    }
     return false;
   };
-  // ---- A2 into TMEM as A2^T: coalesced cp.async into the stage buffers, then
-  //      thread c moves its column (16-byte runs along r) with tcgen05.st ----
-  for (int idx = tid; idx < kChunk * per_col; idx += TQR_THREADS) {
-    const int cc = idx / per_col, r4 = idx % per_col;
-    cp16(A2raw + cc * kRawLd + 4 * r4, A2 + (size_t)cc * lda2 + 4 * r4);
+  // ---- A2 into TMEM as A2^T: the chunk into the stage buffers (TMA boxes, or
+  //      coalesced cp.async), with block 0's operands; then thread c moves its
+  //      column (16-byte runs along r) with tcgen05.st ----
+  if (mp) {
+    if (tid == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      arm_tx(&bars[3], (uint32_t)m2 * kChunk * 4 + (nblk > 0 ? block_bytes(m2, A1 != nullptr) : 0u));
+      for (int q = 0; q < m2 / 32; ++q) tma_load2d(A2raw + q * kA2Box, mp->a2, mp->a2r + 32 * q, mp->a2c, &bars[3]);
+      if (nblk > 0) tma_block(mp, 0, m2, Vraw, A1 != nullptr, A1s, &bars[3]);
+    }
+  } else {
+    for (int idx = tid; idx < kChunk * per_col; idx += TQR_THREADS) {
+      const int cc = idx / per_col, r4 = idx % per_col;
+      cp16(A2raw + swz(4 * r4, cc, kA2Box), A2 + (size_t)cc * lda2 + 4 * r4);
+    }
+    cp_commit();
+    if (nblk > 0) prefetch_block(nullptr, 0, V, ldv, m2, Vraw, A1, lda1, A1s, &bars[3]);
   }
-  cp_commit();
-  if (nblk > 0) prefetch_block(V, ldv, m2, Vraw, A1, lda1, A1s);
-  prefetch_wait();
-  __syncthreads();
+  loads_pending = true;
+  if (!loads_wait(mp, &bars[3], &phase[3])) return fail();
+  loads_pending = false;
 #pragma unroll 1
   for (int r0 = wset * half; r0 < (wset + 1) * half; r0 += 32) {
     float v[32];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
-      const float4 x = *reinterpret_cast<const float4 *>(A2raw + c * kRawLd + r0 + 4 * u);
+      const float4 x = *reinterpret_cast<const float4 *>(A2raw + swz(r0 + 4 * u, c, kA2Box));
       v[4 * u] = x.x; v[4 * u + 1] = x.y; v[4 * u + 2] = x.z; v[4 * u + 3] = x.w;
     }
     st32(a2t + (uint32_t)r0, v);
@@ -348,9 +437,9 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
       const int idx = tid + u * TQR_THREADS, r = idx % kIb, cc = idx / kIb;
       tv[u] = (r <= cc) ? __ldcg(T + (size_t)r + (size_t)(b * kIb + cc) * ldt) : 0.0f;
     }
-    if (b > 0) {
-      prefetch_wait();
-      __syncthreads();   // V_b, A1_b in Vraw, A1s
+    if (b > 0) {   // V_b, A1_b in Vraw, A1s
+      if (!loads_wait(mp, &bars[3], &phase[3])) return fail();
+      loads_pending = false;
     }
     // ---- GEMM1: D1[c][p] = sum_r A2^T[c][r] V_b[r][p], K chunks of 64 rows,
     //      staging of chunk q + 1 overlapping the MMAs of chunk q ----
@@ -413,11 +502,10 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
 #pragma unroll
         for (int p = 0; p < 32; ++p) w[p] += wl[p];   // (A_hi + A_lo) V_hi + (A_hi + A_lo) V_lo
       }
-      float *a1s = A1s + c * kA1Ld;
       if (A1) {
 #pragma unroll
         for (int p4 = 0; p4 < 8; ++p4) {
-          const float4 x = *reinterpret_cast<const float4 *>(a1s + 4 * p4);
+          const float4 x = *reinterpret_cast<const float4 *>(A1s + swz(4 * p4, c, 0));
           w[4 * p4] += x.x; w[4 * p4 + 1] += x.y; w[4 * p4 + 2] += x.z; w[4 * p4 + 3] += x.w;
         }
       }
@@ -440,9 +528,10 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
 #pragma unroll
       for (int p4 = 0; p4 < 8; ++p4) {
         if (A1) {
-          float4 x = *reinterpret_cast<const float4 *>(a1s + 4 * p4);
+          float4 *xa = reinterpret_cast<float4 *>(A1s + swz(4 * p4, c, 0));
+          float4 x = *xa;
           x.x -= w[4 * p4]; x.y -= w[4 * p4 + 1]; x.z -= w[4 * p4 + 2]; x.w -= w[4 * p4 + 3];
-          *reinterpret_cast<float4 *>(a1s + 4 * p4) = x;
+          *xa = x;
         }
         put_split4(wHi, wLo, kmaj(c, 4 * p4, (kIb / 4) * 128), make_float4(w[4 * p4], w[4 * p4 + 1],
                                                                           w[4 * p4 + 2], w[4 * p4 + 3]));
@@ -454,8 +543,8 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
 #pragma unroll 4
       for (int idx = t; idx < m2 * (kIb / 4); idx += 128) {
         const int r = idx % m2, p4 = idx / m2;
-        const float *vp = Vraw + (4 * p4) * kRawLd + r;
-        float4 x = make_float4(vp[0], vp[kRawLd], vp[2 * kRawLd], vp[3 * kRawLd]);
+        auto vat = [&](int p) { return *reinterpret_cast<const float *>(Vraw + swz(r, p, kVBox)); };
+        float4 x = make_float4(vat(4 * p4), vat(4 * p4 + 1), vat(4 * p4 + 2), vat(4 * p4 + 3));
         if (vmode != kVFull) {
           const int dg = b * kIb + 4 * p4;
           x.x = vmask(vmode, r, dg, x.x); x.y = vmask(vmode, r, dg + 1, x.y);
@@ -484,13 +573,15 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
       for (int idx = tid; idx < kChunk * (kIb / 4); idx += TQR_THREADS) {
         const int cc = idx / (kIb / 4), p4 = idx % (kIb / 4);
         *reinterpret_cast<float4 *>(A1b + (size_t)cc * lda1 + 4 * p4) =
-            *reinterpret_cast<const float4 *>(A1s + cc * kA1Ld + 4 * p4);
+            *reinterpret_cast<const float4 *>(A1s + swz(4 * p4, cc, 0));
       }
     }
     __syncthreads();
-    if (b + 1 < nblk)
-      prefetch_block(V + (size_t)(b + 1) * kIb * ldv, ldv, m2, Vraw, A1 ? A1 + (size_t)(b + 1) * kIb : nullptr,
-                     lda1, A1s);
+    if (b + 1 < nblk) {
+      prefetch_block(mp, b + 1, V + (size_t)(b + 1) * kIb * ldv, ldv, m2, Vraw,
+                     A1 ? A1 + (size_t)(b + 1) * kIb : nullptr, lda1, A1s, &bars[3]);
+      loads_pending = true;
+    }
     if (!wait_phase(&bars[2], &phase[2])) return fail();
   }
   // ---- A2 = A2^T - D2 out of TMEM through the stage buffers (coalesced) ----
@@ -507,14 +598,14 @@ __device__ inline bool tsmqr_chunk(int m2, int k, float *A1, int lda1, float *A2
     }
 #pragma unroll
     for (int u = 0; u < 8; ++u)
-      *reinterpret_cast<float4 *>(A2raw + c * kRawLd + r0 + 4 * u) =
+      *reinterpret_cast<float4 *>(A2raw + swz(r0 + 4 * u, c, kA2Box)) =
           make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]);
   }
   __syncthreads();
   for (int idx = tid; idx < kChunk * per_col; idx += TQR_THREADS) {
     const int cc = idx / per_col, r4 = idx % per_col;
     *reinterpret_cast<float4 *>(A2 + (size_t)cc * lda2 + 4 * r4) =
-        *reinterpret_cast<const float4 *>(A2raw + cc * kRawLd + 4 * r4);
+        *reinterpret_cast<const float4 *>(A2raw + swz(4 * r4, cc, kA2Box));
   }
   tmem_sync();
   return true;

@@ -442,6 +442,10 @@ struct TDagArgs {
   // mixed form (FP32 matrix): FP64 diagonal R triangles of the panel steps,
   // ib x nb per (tile row i, panel k) at D + ((k MT + i) nb) ib, ld ib
   double *D = nullptr;
+  // tensor-core tasks with tma: tensor maps of A (32 x 128 and 32 x 32
+  // boxes); the kernel takes TDagArgs as a __grid_constant__ parameter
+  CUtensorMap tmw, tmn;
+  int tma = 0;
   __device__ double *Dtri(int i, int k, int c) const {
     return D + ((size_t)k * g.MT + i) * (size_t)g.nb * g.ib + (size_t)c * g.ib;
   }
@@ -495,7 +499,7 @@ __device__ __forceinline__ unsigned long long tdag_ns() {
 // TC: this instantiation owns the SM's TMEM and runs the tensor-core chunk
 // tasks (FP32, one CTA per SM); the other instantiations never meet one.
 template <typename R, bool TC>
-__global__ void __launch_bounds__(TQR_THREADS, TC ? 1 : 2) k_tree_dag(const TDagArgs<R> a) {
+__global__ void __launch_bounds__(TQR_THREADS, TC ? 1 : 2) k_tree_dag(const __grid_constant__ TDagArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_it, s_err;
   __shared__ __align__(8) uint64_t s_bars[tc::kBars];
@@ -507,7 +511,7 @@ __global__ void __launch_bounds__(TQR_THREADS, TC ? 1 : 2) k_tree_dag(const TDag
     if (tid == 0 && blockIdx.x == 0) atomicExch(&a.hdr->error, 2);
     return;
   }
-  uint32_t phase[tc::kBars] = {0u, 0u, 0u};
+  uint32_t phase[tc::kBars] = {0u, 0u, 0u, 0u};
   uint32_t tmem = 0;
   bool tc_failed = false;
   if constexpr (TC) {
@@ -566,17 +570,21 @@ __global__ void __launch_bounds__(TQR_THREADS, TC ? 1 : 2) k_tree_dag(const TDag
           const int col = (k + 1) * g.nb + (int)it.y * tc::kChunk;
           const int j = col / g.nb, off = col % g.nb;
           unsigned char *al = smem + ((1024 - (tc::saddr(smem) & 1023)) & 1023);
+          const int nb = g.nb, i = it.i;
           if (op.type == OP_GE_TRAIL_TC) {
             // unmqr! of geqrt!'s factor of tile (i, k) on the chunk of tile (i, j)
-            ok = tc::tsmqr_chunk(g.rows(it.i), min(g.rows(it.i), g.cols(k)), nullptr, g.lda,
-                                 g.tile(it.i, j) + (size_t)off * g.lda, g.lda, g.tile(it.i, k), g.lda,
-                                 g.ttile(g.T, it.i, k), g.ldt, tmem, s_bars, phase, al, tc::kVUnitLower);
+            const tc::TcMaps mp{&a.tmw, &a.tmw, &a.tmn, 0, 0, i * nb, col, i * nb, k * nb};
+            ok = tc::tsmqr_chunk(g.rows(i), min(g.rows(i), g.cols(k)), nullptr, g.lda,
+                                 g.tile(i, j) + (size_t)off * g.lda, g.lda, g.tile(i, k), g.lda,
+                                 g.ttile(g.T, i, k), g.ldt, tmem, s_bars, phase, al, tc::kVUnitLower,
+                                 a.tma ? &mp : nullptr);
           } else {
             const int p = it.p;
+            const tc::TcMaps mp{&a.tmw, &a.tmw, &a.tmn, i * nb, col, p * nb, col, p * nb, k * nb};
             ok = tc::tsmqr_chunk(g.rows(p), op.ts ? g.cols(k) : min(g.rows(p), g.cols(k)),
-                                 g.tile(it.i, j) + (size_t)off * g.lda, g.lda, g.tile(p, j) + (size_t)off * g.lda,
+                                 g.tile(i, j) + (size_t)off * g.lda, g.lda, g.tile(p, j) + (size_t)off * g.lda,
                                  g.lda, g.tile(p, k), g.lda, g.ttile(g.T2, p, k), g.ldt, tmem, s_bars, phase, al,
-                                 op.ts ? tc::kVFull : tc::kVUpper);
+                                 op.ts ? tc::kVFull : tc::kVUpper, a.tma ? &mp : nullptr);
           }
         } else {
           ok = false;   // never scheduled without the tensor-core instantiation
@@ -1004,6 +1012,11 @@ static int tree_geqrf_dag_impl(int m, int n, int nb, int ib, R *A, int lda, R *T
   a.key = p->key;
   a.timeout_ns = 20000000000ull;
   if (sh.f64p) a.D = (double *)(w + p->total_bytes);
+  if constexpr (std::is_same<R, float>::value) {
+    if (sh.tc && tc_tma_enabled())
+      a.tma = make_tmap_f32(&a.tmw, A, m, n, lda, 32, tc::kChunk) == cudaSuccess &&
+              make_tmap_f32(&a.tmn, A, m, n, lda, 32, tc::kIb) == cudaSuccess;
+  }
   size_t sm = kTreeSmem;
   if (sh.f64p)
     sm = std::max({sm, panel_f64_smem(nb, ib), tsqrt_f64x_smem(nb, ib), ttqrt_f64_smem(nb, ib)});

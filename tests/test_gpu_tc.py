@@ -90,3 +90,63 @@ def test_fp32_dag_with_tensor_cores(tq, oracle, m, n):
         assert np.max(np.abs(np.linalg.norm(A0 @ x, axis=0) - np.linalg.norm(R @ x, axis=0)) /
                       np.linalg.norm(A0 @ x, axis=0)) < 1e-5
     assert errs[1] < 2e-5 and errs[1] < 3 * errs[0] + 1e-6, errs
+
+
+def _with_tma(tq, on, fn):
+    from tileqr import _lib
+    old = _lib.lib().tqr_tile_tc_tma(1 if on else 0)
+    try:
+        return fn()
+    finally:
+        _lib.lib().tqr_tile_tc_tma(old)
+
+
+def test_tma_and_cp_async_loads_agree_bit_for_bit(tq):
+    """The tensor-core updates load their operands with TMA (128-byte-swizzled
+    boxes) or, switched off, with 16-byte cp.async copies into the same
+    layout: the same values reach the same arithmetic, so the stand-alone
+    tsmqr, the flat FP32 tile QR and the hierarchical tree (plain and mixed
+    forms, every masked-V mode) give identical bits both ways."""
+    import torch
+    from tileqr import _lib
+    g = torch.Generator(device="cuda").manual_seed(77)
+    # stand-alone tsmqr on a 256 x 1024 band
+    m2, k, n = 256, 256, 1024
+    A1 = tq.empty(k, n, dtype=torch.float32)
+    A2 = tq.empty(m2, n, dtype=torch.float32)
+    V = tq.empty(m2, k, dtype=torch.float32)
+    T = tq.empty(32, k, dtype=torch.float32)
+    for t, s in ((A1, 1), (A2, 1), (V, 16), (T, 16)):
+        t.copy_(torch.randn(*t.shape, generator=g, device="cuda") / s)
+    T.copy_(torch.triu(T))
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    st = torch.cuda.current_stream()
+
+    def band():
+        a1, a2 = A1.clone(), A2.clone()
+        assert _lib.lib().tqr_stsmqr_tc(k, n, m2, k, P(a1), k, P(a2), m2, P(V), m2, P(T), 32, P(err),
+                                        ctypes.c_void_p(st.cuda_stream)) == 0
+        torch.cuda.synchronize()
+        return a1, a2
+    for x, y in zip(_with_tma(tq, True, band), _with_tma(tq, False, band)):
+        assert torch.equal(x, y)
+    assert int(err.item()) == 0
+    # flat persistent FP32 tile QR and the hierarchical tree, plain and mixed
+    m, n = 4096, 1024
+    A0 = tq.empty(m, n, dtype=torch.float32)
+    A0.copy_(torch.randn(m, n, generator=g, device="cuda"))
+
+    def flat():
+        A = A0.clone()
+        T_, tau = tq.tile_geqrf(A, 256, 32)
+        return A, T_, tau
+
+    def tree(f64p):
+        def run():
+            A = A0.clone()
+            return (A,) + tuple(tq.tile_geqrf_tree(A, 256, 32, grp=4, f64p=f64p))
+        return run
+    for fn in (flat, tree(False), tree(True)):
+        for x, y in zip(_with_tma(tq, True, fn), _with_tma(tq, False, fn)):
+            assert torch.equal(x, y)
