@@ -632,6 +632,30 @@ int tqr_tile_dag_tensor_cores(int on);
  * copies into the same layout instead (the same results bit for bit), (1)
  * restores TMA.  Returns the previous setting.  Process-wide. */
 int tqr_tile_tc_tma(int on);
+
+/* The same trailing update in compact-WY form (no counterpart call in NextLA:
+ * it replaces the chain of ib-blocks that tsmqr!, src/tsmqr.jl:47-146, unmqr!,
+ * src/unmqr.jl:99-148, and ttmqr!, src/ttmqr.jl:1-95, apply one after another
+ * by Q = I - V T V^T with the k x k T of all blocks).
+ * tqr_swy_build: once per V, fills a slot (tqr_swy_slot_bytes() = 1.5 MB,
+ *   256-byte aligned, device memory) with V masked by vmode (0 as stored,
+ *   tsmqr!; 1 unit lower triangular, geqrt!'s V for unmqr!; 2 upper
+ *   triangular, ttmqr!), V^T and that T (from the blocked T, 32 x k, ldt >= 32),
+ *   each split hi + lo for TF32x3.  m2 = 128 or 256, k a multiple of 32, k <= m2.
+ * tqr_swy_apply: [A1; A2] := Q^T [A1; A2] for n columns (a multiple of 128)
+ *   with a built slot; A1 (k x n, null for vmode 1: A2 := Q^T A2) and A2
+ *   (m2 x n) 16-byte aligned with leading dimensions multiples of 4.
+ * tqr_stsmqr_wy: build (vmode 0) then apply, the tsmqr!('L','C') of
+ *   tqr_stsmqr_tc.
+ * Same results as the blocked form to FP32 rounding (the products are
+ * regrouped).  *err becomes nonzero if a bounded device wait gave up. */
+size_t tqr_swy_slot_bytes(void);
+int tqr_swy_build(int m2, int k, const float *V, int ldv, const float *T, int ldt, int vmode, void *slot,
+                  size_t lslot, int *err, cudaStream_t stream);
+int tqr_swy_apply(int m1, int n, int m2, int k, float *A1, int lda1, float *A2, int lda2, const void *slot, int *err,
+                  cudaStream_t stream);
+int tqr_stsmqr_wy(int m1, int n, int m2, int k, float *A1, int lda1, float *A2, int lda2, const float *V, int ldv,
+                  const float *T, int ldt, void *slot, size_t lslot, int *err, cudaStream_t stream);
 /* Resident CTAs per SM and dynamic shared memory of the persistent tile
  * kernel at nb = 256, ib = 32 (dtype_bytes 8 or 4; tensor_cores for FP32). */
 int tqr_tile_dag_occupancy(int dtype_bytes, int tensor_cores, int *ctas_per_sm, int *smem_bytes);

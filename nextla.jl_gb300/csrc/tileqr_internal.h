@@ -71,12 +71,13 @@ int stile_gels_dag_mixed(int m, int n, int nrhs, int nb, int ib, float *A, int l
 // (tqr_tile_dag_tensor_cores; dag.cu).
 bool tile_tc_enabled();
 
-// Tensor maps for the tensor-core chunk routine's TMA loads (tc.cu): a
+// Tensor maps for the tensor-core chunk routines' TMA loads (tc.cu): a
 // column-major FP32 matrix (rows x cols, leading dimension ld) with boxes of
-// box_rows x box_cols elements and the 128-byte swizzle; tm points to a
-// CUtensorMap.  tc_tma_enabled: whether the loads use TMA (tqr_tile_tc_tma).
+// box_rows x box_cols elements and the 128-byte (or 64-byte) swizzle; tm
+// points to a CUtensorMap.  tc_tma_enabled: whether the blocked chunk routine
+// loads through TMA (tqr_tile_tc_tma).
 cudaError_t make_tmap_f32(void *tm, const float *base, long long rows, long long cols, long long ld, int box_rows,
-                          int box_cols);
+                          int box_cols, int swizzle_bytes = 128);
 bool tc_tma_enabled();
 // Whether tqr_dsgels factors with FP64 panel steps (tqr_dsgels_fp64_panels).
 bool dsgels_f64p_enabled();

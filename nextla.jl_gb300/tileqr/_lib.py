@@ -114,6 +114,10 @@ DIAG = {
     "tqr_tile_dag_occupancy": ([_I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
     "tqr_tile_dag_check_tc": ([_I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)], _I),
     "tqr_stsmqr_tc": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, _P], _I),
+    "tqr_swy_slot_bytes": ([], ctypes.c_size_t),
+    "tqr_swy_build": ([_I, _I, _P, _I, _P, _I, _I, _P, ctypes.c_size_t, _P, _P], _I),
+    "tqr_swy_apply": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _P, _P], _I),
+    "tqr_stsmqr_wy": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, ctypes.c_size_t, _P, _P], _I),
     "tqr_qr_batched_worksize": ([_I, _I, _I, _I, ctypes.POINTER(ctypes.c_size_t)], _I),
     "tqr_dqr_batched_fwd": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
     "tqr_sqr_batched_fwd": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
