@@ -45,10 +45,12 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--kernel", default=None,
-                   choices=["tsmqr", "tsmqr_tc", "tsqrt", "geqrt", "tile", "tile_f64p", "hqr", "larft", "trsm"],
+                   choices=["tsmqr", "tsmqr_tc", "tsmqr_wy", "tsqrt", "geqrt", "tile", "tile_f64p", "hqr",
+                            "hqr_square", "larft", "trsm"],
                    help="time one tile kernel alone (for profiling) instead of the workload")
     p.add_argument("--dtype", default="f64", choices=["f64", "f32", "c64", "c128"],
                    help="element type for --kernel (complex: tile only)")
+    p.add_argument("--grp", type=int, default=4, help="with --kernel hqr_square: tiles per flat group")
     p.add_argument("--no-ls", action="store_true", help="skip the least-squares comparison")
     p.add_argument("--ls-only", action="store_true", help="run only the least-squares comparison")
     p.add_argument("--ls-m", type=int, default=32768)
@@ -120,6 +122,18 @@ def kernel_bench(args):
             A.copy_(A0)
             tq.tile_geqrf_tree(A, NB, IB, dag=True, grp=HQR_GRP)
         fl = 2.0 * n * 512 ** 2 - 2.0 * 512 ** 3 / 3
+    elif args.kernel == "hqr_square":
+        # the n x n tile QR on the hierarchical tree (groups of --grp tiles,
+        # the leaders by the binary tree), one persistent launch
+        dt = torch.float32 if args.dtype == "f32" else torch.float64
+        A0 = tq.empty(n, n, dtype=dt)
+        A0.copy_(torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda"))
+        A = tq.empty(n, n, dtype=dt)
+
+        def run():
+            A.copy_(A0)
+            tq.tile_geqrf_tree(A, NB, IB, dag=True, grp=args.grp)
+        fl = flops_square(n)
     elif args.kernel == "larft":
         # stand-alone larft!('F', 'C') on an n x 32 block of reflectors
         dt = torch.float32 if args.dtype == "f32" else torch.float64
@@ -158,6 +172,26 @@ def kernel_bench(args):
         P = lambda t: ctypes.c_void_p(t.data_ptr())
         run = lambda: _lib.lib().tqr_stsmqr_tc(NB, w, NB, NB, P(A1), NB, P(A2), NB, P(V), NB, P(T), IB, P(err),
                                                ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        fl = 4.0 * NB * NB * w
+    elif args.kernel == "tsmqr_wy":
+        # the same band through the compact-WY form: one slot build for V and
+        # T, then every 128-column chunk as three tensor-core products
+        import ctypes
+        from tileqr import _lib
+        w = ((n - NB) // 128) * 128
+        dt = torch.float32
+        A1, A2, V = tq.empty(NB, w, dtype=dt), tq.empty(NB, w, dtype=dt), tq.empty(NB, NB, dtype=dt)
+        for t in (A1, A2):
+            t.copy_(torch.randn(NB, w, generator=g, dtype=torch.float64, device="cuda"))
+        V.copy_(torch.randn(NB, NB, generator=g, dtype=torch.float64, device="cuda") / 16)
+        T = tq.empty(IB, NB, dtype=dt)
+        T.copy_(torch.triu(torch.randn(IB, NB, generator=g, dtype=torch.float64, device="cuda")) / 16)
+        err = torch.zeros(1, dtype=torch.int32, device="cuda")
+        nslot = _lib.lib().tqr_swy_slot_bytes()
+        slot = torch.empty(nslot // 4, dtype=torch.float32, device="cuda")
+        P = lambda t: ctypes.c_void_p(t.data_ptr())
+        run = lambda: _lib.lib().tqr_stsmqr_wy(NB, w, NB, NB, P(A1), NB, P(A2), NB, P(V), NB, P(T), IB, P(slot),
+                                               nslot, P(err), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
         fl = 4.0 * NB * NB * w
     elif args.kernel == "tsmqr":
         w = n - NB

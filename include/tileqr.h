@@ -656,6 +656,24 @@ int tqr_swy_apply(int m1, int n, int m2, int k, float *A1, int lda1, float *A2, 
                   cudaStream_t stream);
 int tqr_stsmqr_wy(int m1, int n, int m2, int k, float *A1, int lda1, float *A2, int lda2, const float *V, int ldv,
                   const float *T, int ldt, void *slot, size_t lslot, int *err, cudaStream_t stream);
+/* tqr_tile_tc_wy(1) makes the FP32 hierarchical and binary-tree task graphs
+ * (tqr_stile_geqrf_hqr_dag, tqr_stile_geqrf_tree_dag and the mixed solve's
+ * factorisation) run their tensor-core updates in this compact-WY form: one
+ * slot build per reflector tile (geqrt!'s V for the leaders' unmqr!, a
+ * merge's V for its tsmqr! or ttmqr!), then every 128-column chunk through
+ * it.  The slots sit in the caller's `work` (4 * (m / 256) slots; the
+ * worksize queries include them).  Off by default: the graphs apply ib-block
+ * by ib-block (tqr_stsmqr_tc's routine), which is about twice as accurate
+ * (the WY form adds a TF32x3 product with the k x k T to every update) and,
+ * with the mixed solve's FP64 panel steps, no slower.  Returns the previous
+ * setting.  Process-wide. */
+int tqr_tile_tc_wy(int on);
+/* Host replay of that schedule: topological order, every chunk task waits for
+ * its own reflector tile's slot build, and every rebuild of a slot waits for
+ * all chunks that read its previous contents.  *nbuild, *nchunk: how many
+ * builds and chunk tasks.  0 = consistent, 1-3 = which check failed. */
+int tqr_tile_hqr_dag_check_wy(int m, int n, int nb, int ib, int grp, int nrhs, long long *nbuild,
+                              long long *nchunk);
 /* Resident CTAs per SM and dynamic shared memory of the persistent tile
  * kernel at nb = 256, ib = 32 (dtype_bytes 8 or 4; tensor_cores for FP32). */
 int tqr_tile_dag_occupancy(int dtype_bytes, int tensor_cores, int *ctas_per_sm, int *smem_bytes);

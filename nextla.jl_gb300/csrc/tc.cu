@@ -55,6 +55,8 @@ cudaError_t make_tmap_f32(void *tm, const float *base, long long rows, long long
 
 static int g_tma_enabled = 1;
 bool tc_tma_enabled() { return g_tma_enabled != 0; }
+static int g_wy_enabled = 0;
+bool tc_wy_enabled() { return g_wy_enabled != 0; }
 
 // The stand-alone launch's maps of A1, A2 and V (kernel parameter space).
 struct TcLaunchMaps {
@@ -271,6 +273,12 @@ int tqr_stsmqr_wy(int m1, int n, int m2, int k, float *A1, int lda1, float *A2, 
 int tqr_tile_tc_tma(int on) {
   const int old = tqr::g_tma_enabled;
   tqr::g_tma_enabled = on ? 1 : 0;
+  return old;
+}
+
+int tqr_tile_tc_wy(int on) {
+  const int old = tqr::g_wy_enabled;
+  tqr::g_wy_enabled = on ? 1 : 0;
   return old;
 }
 

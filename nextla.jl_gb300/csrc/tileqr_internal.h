@@ -79,6 +79,10 @@ bool tile_tc_enabled();
 cudaError_t make_tmap_f32(void *tm, const float *base, long long rows, long long cols, long long ld, int box_rows,
                           int box_cols, int swizzle_bytes = 128);
 bool tc_tma_enabled();
+// Whether FP32 task graphs run their tensor-core updates in compact-WY form
+// (tc_wy.cuh: one slot build per reflector tile, then three products per
+// chunk) rather than ib-block by ib-block (tqr_tile_tc_wy).
+bool tc_wy_enabled();
 // Whether tqr_dsgels factors with FP64 panel steps (tqr_dsgels_fp64_panels).
 bool dsgels_f64p_enabled();
 

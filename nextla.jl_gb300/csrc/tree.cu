@@ -34,7 +34,7 @@
 
 #include "apply_dev.cuh"
 #include "panel_dev.cuh"
-#include "tc_apply.cuh"
+#include "tc_wy.cuh"
 #include "tileqr.h"
 #include "tileqr_internal.h"
 
@@ -64,7 +64,18 @@ enum TreeOpType { OP_GE_PANEL = 0, OP_GE_APPLY = 1, OP_GE_TRAIL = 2, OP_PR_PANEL
                   // chunk of A per task: the trailing update of a merge
                   // (tsmqr! for a tsqrt merge, ttmqr! for a ttqrt merge) and
                   // of a geqrt! (unmqr!)
-                  OP_PR_TRAIL_TC = 6, OP_GE_TRAIL_TC = 7 };
+                  OP_PR_TRAIL_TC = 6, OP_GE_TRAIL_TC = 7,
+                  // compact-WY form of the two above (tc_wy.cuh): once per
+                  // reflector tile, the stage images every chunk of its
+                  // update shares (a "slot"); the chunk tasks then read it
+                  OP_WY_BUILD = 8 };
+
+// Slot of the compact-WY images of a reflector tile: geqrt!'s V of tile
+// (row, k) (merge 0) or a merge's V in tile (row, k) (merge 1), two per tile
+// row and kind, alternating with k.  A slot is rebuilt only after every chunk
+// that read it two panels earlier (the graph builder tracks each slot as a
+// region).
+__host__ __device__ inline int wy_slot(int MT, int merge, int row, int k) { return ((merge * MT) + row) * 2 + (k & 1); }
 
 struct TreeOp {
   int type;
@@ -446,6 +457,14 @@ struct TDagArgs {
   // boxes); the kernel takes TDagArgs as a __grid_constant__ parameter
   CUtensorMap tmw, tmn;
   int tma = 0;
+  // compact-WY chunk tasks (wy): tensor map of A with 16 x 128 boxes in the
+  // 64-byte swizzle, and the slots (4 MT of tc::wy::kSlotBytes)
+  CUtensorMap tmwy;
+  unsigned char *slots = nullptr;
+  int wy = 0;
+  __device__ unsigned char *slot(int merge, int row, int k) const {
+    return slots + (size_t)wy_slot(g.MT, merge, row, k) * tc::wy::kSlotBytes;
+  }
   __device__ double *Dtri(int i, int k, int c) const {
     return D + ((size_t)k * g.MT + i) * (size_t)g.nb * g.ib + (size_t)c * g.ib;
   }
@@ -503,6 +522,9 @@ __global__ void __launch_bounds__(TQR_THREADS, TC ? 1 : 2) k_tree_dag(const __gr
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_it, s_err;
   __shared__ __align__(8) uint64_t s_bars[tc::kBars];
+  // the compact-WY routines' mbarriers (loads, MMAs, A operands ready,
+  // epilogue, teardown), used by the tensor-core instantiation only
+  __shared__ __align__(8) uint64_t s_wybars[TC ? tc::wy::kBars : 1];
   __shared__ uint32_t s_tmem;
   const int tid = threadIdx.x;
   if (tid == 0) s_err = (a.hdr->key != a.key || a.hdr->nitems != a.nitems) ? 2 : 0;
@@ -512,12 +534,17 @@ __global__ void __launch_bounds__(TQR_THREADS, TC ? 1 : 2) k_tree_dag(const __gr
     return;
   }
   uint32_t phase[tc::kBars] = {0u, 0u, 0u, 0u};
+  uint32_t wyph[tc::wy::kPh] = {};
   uint32_t tmem = 0;
   bool tc_failed = false;
   if constexpr (TC) {
     if (tid == 0) {
       for (int q = 0; q < tc::kBars; ++q)
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::saddr(&s_bars[q])));
+      for (int q = 0; q < tc::wy::kBars; ++q) {
+        const int count = (q >= 2 * tc::wy::kRing && q < 3 * tc::wy::kRing) ? tc::wy::kWorkers : 1;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc::saddr(&s_wybars[q])), "r"(count));
+      }
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if ((tid >> 5) == 0) {
@@ -563,7 +590,52 @@ __global__ void __launch_bounds__(TQR_THREADS, TC ? 1 : 2) k_tree_dag(const __gr
     op.trans = 0; op.a_cols = 1;
     bool ok = true;
     if constexpr (std::is_same<R, float>::value) {
-      if (op.type == OP_PR_TRAIL_TC || op.type == OP_GE_TRAIL_TC) {
+      if (op.type == OP_WY_BUILD) {
+        if constexpr (TC) {
+          // the slot of one reflector tile: geqrt!'s V (it.b == 0, unit
+          // lower) or a merge's V (it.b == 1: tsqrt!'s whole tile, or
+          // ttqrt!'s upper triangle)
+          const TreeGeom<R> &g = a.g;
+          const int k = it.k;
+          unsigned char *al = smem + ((1024 - (tc::saddr(smem) & 1023)) & 1023);
+          if (it.b == 0) {
+            const int i = it.i;
+            ok = tc::wy::wy_build(g.rows(i), min(g.rows(i), g.cols(k)), g.tile(i, k), g.lda, g.ttile(g.T, i, k),
+                                  g.ldt, tc::kVUnitLower, a.slot(0, i, k), tmem, s_wybars, wyph, al);
+          } else {
+            const int p = it.p;
+            ok = tc::wy::wy_build(g.rows(p), op.ts ? g.cols(k) : min(g.rows(p), g.cols(k)), g.tile(p, k), g.lda,
+                                  g.ttile(g.T2, p, k), g.ldt, op.ts ? tc::kVFull : tc::kVUpper, a.slot(1, p, k),
+                                  tmem, s_wybars, wyph, al);
+          }
+        } else {
+          ok = false;   // never scheduled without the tensor-core instantiation
+        }
+      } else if ((op.type == OP_PR_TRAIL_TC || op.type == OP_GE_TRAIL_TC) && a.wy) {
+        if constexpr (TC) {
+          // one 128-column chunk through the tile's compact-WY slot
+          const TreeGeom<R> &g = a.g;
+          const int k = it.k;
+          const int col = (k + 1) * g.nb + (int)it.y * tc::kChunk;
+          const int j = col / g.nb, off = col % g.nb;
+          unsigned char *al = smem + ((1024 - (tc::saddr(smem) & 1023)) & 1023);
+          const int nb = g.nb, i = it.i;
+          if (op.type == OP_GE_TRAIL_TC) {
+            const tc::wy::WyMaps mp{&a.tmwy, &a.tmwy, 0, 0, i * nb, col};
+            ok = tc::wy::wy_chunk(g.rows(i), min(g.rows(i), g.cols(k)), nullptr, g.lda,
+                                  g.tile(i, j) + (size_t)off * g.lda, g.lda, a.slot(0, i, k), mp, tmem, s_wybars,
+                                  wyph, al);
+          } else {
+            const int p = it.p;
+            const tc::wy::WyMaps mp{&a.tmwy, &a.tmwy, i * nb, col, p * nb, col};
+            ok = tc::wy::wy_chunk(g.rows(p), op.ts ? g.cols(k) : min(g.rows(p), g.cols(k)),
+                                  g.tile(i, j) + (size_t)off * g.lda, g.lda, g.tile(p, j) + (size_t)off * g.lda,
+                                  g.lda, a.slot(1, p, k), mp, tmem, s_wybars, wyph, al);
+          }
+        } else {
+          ok = false;
+        }
+      } else if (op.type == OP_PR_TRAIL_TC || op.type == OP_GE_TRAIL_TC) {
         if constexpr (TC) {
           const TreeGeom<R> &g = a.g;
           const int k = it.k;
@@ -629,6 +701,7 @@ struct TreeShape {
   int m, n, nb, ib, nrhs, MT, NT, KT;
   int grp = 1;
   int tc = 0;       // FP32: trailing updates of A as tensor-core chunk tasks
+  int wy = 0;       // with tc: the chunk tasks in compact-WY form, one slot build per reflector tile
   int f64p = 0;     // FP32: panel steps in FP64 (the mixed form)
   int rows(int i) const { return std::min(nb, m - i * nb); }
   int cols(int k) const { return std::min(nb, n - k * nb); }
@@ -663,6 +736,7 @@ static double tree_cost(const TreeShape &sh, const TItem &it) {
     case OP_PR_APPLY: return 4.0 * (ts ? sh.rows(it.p) : (it.b + 1) * ib) * ib * w;
     case OP_PR_TRAIL_TC: return 4.0 * sh.rows(it.p) * sh.cols(it.k) * tc::kChunk / 6.0;   // ~6x a SIMT strip
     case OP_GE_TRAIL_TC: return 4.0 * sh.rows(it.i) * sh.cols(it.k) * tc::kChunk / 6.0;
+    case OP_WY_BUILD: return 4.0 * nb * sh.cols(it.k) * tc::kChunk / 6.0;
     default: return (ts ? 4.0 * sh.rows(it.p) : 2.0 * nb) * sh.cols(it.k) * w;
   }
 }
@@ -678,7 +752,10 @@ static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::
   auto rt = [&](int i, int k, int b, int merge) {
     return nstrip + (((size_t)i * sh.KT + k) * nblk + b) * 2 + merge;
   };
-  const size_t nreg = nstrip + (size_t)sh.MT * sh.KT * nblk * 2;
+  // compact-WY slots (wy_slot), after the T blocks
+  const size_t nslot_reg = nstrip + (size_t)sh.MT * sh.KT * nblk * 2;
+  auto rs = [&](int merge, int row, int k) { return nslot_reg + (size_t)wy_slot(sh.MT, merge, row, k); };
+  const size_t nreg = nslot_reg + (size_t)4 * sh.MT;
   std::vector<int> last(nreg, -1);
   std::vector<std::vector<int>> readers(nreg);
   std::vector<TItem> items;
@@ -748,9 +825,20 @@ static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::
       int y0 = 0;
       const int ca = std::max(0, sh.n - (k + 1) * sh.nb);
       if (sh.tc && sh.rows(i) == sh.nb && kk == sh.nb && ca % tc::kChunk == 0) {
-        for (int ch = 0; ch < ca / tc::kChunk; ++ch) {
+        if (sh.wy && ca > 0) {
+          // the slot of geqrt!'s V and T for the chunks below
           for (int q = 0; q < NSk; ++q) rd(rg(i, k, q, 1));
           for (int b = 0; b < nbk; ++b) rd(rt(i, k, b, 0));
+          wr(rs(0, i, k));
+          emit(OP_WY_BUILD, k, 0, i, i, 0);
+        }
+        for (int ch = 0; ch < ca / tc::kChunk; ++ch) {
+          if (sh.wy) {
+            rd(rs(0, i, k));
+          } else {
+            for (int q = 0; q < NSk; ++q) rd(rg(i, k, q, 1));
+            for (int b = 0; b < nbk; ++b) rd(rt(i, k, b, 0));
+          }
           const int c0 = ch * tc::kChunk, j = k + 1 + c0 / sh.nb, s0 = (c0 % sh.nb) / kTreeNW;
           for (int s = s0; s < s0 + tc::kChunk / kTreeNW; ++s) { wr(rg(i, j, s, 0)); wr(rg(i, j, s, 1)); }
           emit(OP_GE_TRAIL_TC, k, 0, i, i, ch);
@@ -800,12 +888,26 @@ static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::
       int y0 = 0;
       const int ca = std::max(0, sh.n - (k + 1) * sh.nb);
       if (sh.tc && sh.rows(p) == sh.nb && sh.rows(i) == sh.nb && kt == sh.nb && ca % tc::kChunk == 0) {
-        for (int ch = 0; ch < ca / tc::kChunk; ++ch) {
+        if (sh.wy && ca > 0) {
+          // the slot of the merge's V and T for the chunks below
           for (int q = 0; q < NSk; ++q) {
             rd(rg(p, k, q, 0));
             if (ts) rd(rg(p, k, q, 1));
           }
           for (int b = 0; b < nbk; ++b) rd(rt(p, k, b, 1));
+          wr(rs(1, p, k));
+          emit(OP_WY_BUILD | flag, k, 1, i, p, 0);
+        }
+        for (int ch = 0; ch < ca / tc::kChunk; ++ch) {
+          if (sh.wy) {
+            rd(rs(1, p, k));
+          } else {
+            for (int q = 0; q < NSk; ++q) {
+              rd(rg(p, k, q, 0));
+              if (ts) rd(rg(p, k, q, 1));
+            }
+            for (int b = 0; b < nbk; ++b) rd(rt(p, k, b, 1));
+          }
           const int c0 = ch * tc::kChunk, j = k + 1 + c0 / sh.nb, s0 = (c0 % sh.nb) / kTreeNW;
           for (int s = s0; s < s0 + tc::kChunk / kTreeNW; ++s) {
             wr(rg(i, j, s, 0)); wr(rg(i, j, s, 1));
@@ -861,7 +963,7 @@ static long long tree_key(const TreeShape &sh) {
   long long h = 7809847782465536322LL;
   // f64p changes no task or dependency (only the device routines of the
   // panel tasks), so it shares the plan
-  for (int v : {sh.m, sh.n, sh.nb, sh.ib, sh.nrhs, sh.grp, sh.tc, 0x7ee})
+  for (int v : {sh.m, sh.n, sh.nb, sh.ib, sh.nrhs, sh.grp, sh.tc, sh.wy, 0x7ee})
     h = (h ^ (long long)v) * 1099511628211LL;
   return h & 0x7fffffffffffffffLL;
 }
@@ -932,8 +1034,12 @@ static size_t tree_d_bytes(const TreeShape &sh) {
   return align256(sizeof(double) * (size_t)sh.MT * sh.KT * sh.nb * sh.ib);
 }
 
+// Bytes of the compact-WY slots (after the FP64 triangles).
+static size_t tree_wy_bytes(const TreeShape &sh) { return (size_t)4 * sh.MT * tc::wy::kSlotBytes; }
+
 // Workspace covering the plain plan and, for FP32-eligible shapes, the
-// tensor-core plan (another task list) and the FP64 triangles.
+// tensor-core plans (other task lists), the FP64 triangles and the
+// compact-WY slots.
 static size_t tree_work_bytes(TreeShape sh) {
   size_t b = tree_plan(sh)->total_bytes;
   const size_t d = tree_f64p_ok(sh) ? tree_d_bytes(sh) : 0;
@@ -941,6 +1047,8 @@ static size_t tree_work_bytes(TreeShape sh) {
   if (sh.nb == 256 && sh.ib == tc::kIb && sh.m % sh.nb == 0 && sh.n % sh.nb == 0) {
     sh.tc = 1;
     b = std::max(b, tree_plan(sh)->total_bytes + d);
+    sh.wy = 1;
+    b = std::max(b, tree_plan(sh)->total_bytes + d + tree_wy_bytes(sh));
   }
   return b;
 }
@@ -992,17 +1100,24 @@ static int tree_geqrf_dag_impl(int m, int n, int nb, int ib, R *A, int lda, R *T
   } else {
     if (mixed) return -3;
   }
+  TDagArgs<R> a;
+  if constexpr (std::is_same<R, float>::value) {
+    // compact-WY chunks need their tensor map of A (16 x 128 boxes)
+    if (sh.tc && tc_wy_enabled() &&
+        make_tmap_f32(&a.tmwy, A, m, n, lda, tc::wy::kKs, tc::kChunk, 64) == cudaSuccess)
+      sh.wy = 1;
+  }
   std::shared_ptr<TreePlan> p = tree_plan(sh);
   const size_t dbytes = sh.f64p ? tree_d_bytes(sh) : 0;
+  const size_t sbytes = sh.wy ? tree_wy_bytes(sh) : 0;
   if (!work || ((uintptr_t)work & 255)) return -16;
-  if (lwork < p->total_bytes + dbytes) return -17;
+  if (lwork < p->total_bytes + dbytes + sbytes) return -17;
   unsigned char *w = (unsigned char *)work;
   int *done = (int *)(w + align256(p->img_bytes));
   cudaError_t e;
   if ((e = cudaMemcpyAsync(w, p->image(), p->img_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess) return (int)e;
   if ((e = cudaMemsetAsync(done, 0, sizeof(int) * p->items.size(), st)) != cudaSuccess) return (int)e;
   if ((e = cudaMemset2DAsync(T2, sizeof(R) * ldt, 0, sizeof(R) * g.MT * ib, n, st)) != cudaSuccess) return (int)e;
-  TDagArgs<R> a;
   a.g = g;
   a.hdr = (TDagHeader *)w;
   a.done = done;
@@ -1012,6 +1127,10 @@ static int tree_geqrf_dag_impl(int m, int n, int nb, int ib, R *A, int lda, R *T
   a.key = p->key;
   a.timeout_ns = 20000000000ull;
   if (sh.f64p) a.D = (double *)(w + p->total_bytes);
+  if (sh.wy) {
+    a.wy = 1;
+    a.slots = w + p->total_bytes + dbytes;
+  }
   if constexpr (std::is_same<R, float>::value) {
     if (sh.tc && tc_tma_enabled())
       a.tma = make_tmap_f32(&a.tmw, A, m, n, lda, 32, tc::kChunk) == cudaSuccess &&
@@ -1022,7 +1141,7 @@ static int tree_geqrf_dag_impl(int m, int n, int nb, int ib, R *A, int lda, R *T
     sm = std::max({sm, panel_f64_smem(nb, ib), tsqrt_f64x_smem(nb, ib), ttqrt_f64_smem(nb, ib)});
   if constexpr (std::is_same<R, float>::value) {
     if (sh.tc) {
-      e = tree_dag_launch<R, true>(a, std::max(sm, tc::kSmem), st);
+      e = tree_dag_launch<R, true>(a, std::max({sm, tc::kSmem, tc::wy::kSmem}), st);
       return e == cudaSuccess ? 0 : (int)e;
     }
   }
@@ -1146,6 +1265,57 @@ int tqr_tile_hqr_dag_check_tc(int m, int n, int nb, int ib, int grp, int nrhs, l
       if (p->deps[it.dep + d] >= q) return 1;
   }
   if (ntasks) *ntasks = ntc;
+  return 0;
+}
+
+int tqr_tile_hqr_dag_check_wy(int m, int n, int nb, int ib, int grp, int nrhs, long long *nbuild,
+                              long long *nchunk) {
+  TreeShape sh;
+  if (!tree_dag_shape(m, n, nb, ib, nrhs, &sh, grp)) return -1;
+  if (nb != 256 || ib != tc::kIb || m % nb || n % nb) return -1;
+  sh.tc = 1;
+  sh.wy = 1;
+  std::shared_ptr<TreePlan> p = tree_plan(sh);
+  const size_t N = p->items.size();
+  auto slot_of = [&](const TItem &it) {
+    const int t = it.type & 0x7f;
+    const int merge = t == OP_WY_BUILD ? it.b : (t == OP_PR_TRAIL_TC ? 1 : 0);
+    return wy_slot(sh.MT, merge, merge ? it.p : it.i, it.k);
+  };
+  // per slot: the position of its current build and the chunks that read it
+  std::vector<long long> build_at((size_t)4 * sh.MT, -1);
+  std::vector<std::vector<long long>> readers((size_t)4 * sh.MT);
+  long long nb_ = 0, nc = 0;
+  for (size_t q = 0; q < N; ++q) {
+    const TItem &it = p->items[q];
+    const uint32_t *d = p->deps.data() + it.dep;
+    for (int x = 0; x < (int)it.ndep; ++x)
+      if (d[x] >= q) return 1;   // not topological
+    const int t = it.type & 0x7f;
+    if (t != OP_WY_BUILD && t != OP_PR_TRAIL_TC && t != OP_GE_TRAIL_TC) continue;
+    const int s = slot_of(it);
+    auto has_dep = [&](long long on) {
+      for (int x = 0; x < (int)it.ndep; ++x)
+        if ((long long)d[x] == on) return true;
+      return false;
+    };
+    if (t == OP_WY_BUILD) {
+      // the rebuild waits for every chunk that read the slot's previous contents
+      for (long long r : readers[s])
+        if (!has_dep(r)) return 2;
+      readers[s].clear();
+      build_at[s] = (long long)q;
+      ++nb_;
+    } else {
+      // a chunk reads the build of its own reflector tile (same panel)
+      const long long b = build_at[s];
+      if (b < 0 || p->items[b].k != it.k || !has_dep(b)) return 3;
+      readers[s].push_back((long long)q);
+      ++nc;
+    }
+  }
+  if (nbuild) *nbuild = nb_;
+  if (nchunk) *nchunk = nc;
   return 0;
 }
 

@@ -79,6 +79,8 @@ DIAG = {
     "tqr_stile_geqrf_hqr_dag_f64p": ([_I, _I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P,
                                       ctypes.c_size_t, _P], _I),
     "tqr_tile_hqr_dag_check_tc": ([_I, _I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)], _I),
+    "tqr_tile_hqr_dag_check_wy": ([_I, _I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong),
+                                   ctypes.POINTER(ctypes.c_longlong)], _I),
     "tqr_stile_geqrf_dag_f64p": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, ctypes.c_size_t, _P], _I),
     "tqr_dsgels": ([_I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _I, ctypes.c_double, _P, ctypes.c_size_t,
                     ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_double), _P], _I),
@@ -111,6 +113,7 @@ DIAG = {
                                   _P], _I),
     "tqr_tile_dag_tensor_cores": ([_I], _I),
     "tqr_tile_tc_tma": ([_I], _I),
+    "tqr_tile_tc_wy": ([_I], _I),
     "tqr_tile_dag_occupancy": ([_I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
     "tqr_tile_dag_check_tc": ([_I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)], _I),
     "tqr_stsmqr_tc": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, _P], _I),

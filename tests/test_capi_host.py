@@ -221,6 +221,28 @@ def test_hqr_tensor_core_task_graph_is_topological(L, m, n, grp, nrhs):
     assert L.tqr_tile_hqr_dag_check_tc(m + 100, n, 256, 32, grp, nrhs, ctypes.byref(nt)) == -1   # ragged
 
 
+@pytest.mark.parametrize("m,n,grp,nrhs", [(4096, 1024, 4, 3), (8192, 512, 8, 0), (32768, 4096, 16, 4),
+                                        (2048, 2048, 2, 1), (8192, 8192, 1, 0)])
+def test_hqr_compact_wy_task_graph(L, m, n, grp, nrhs):
+    """The same schedule in compact-WY form: one slot build per geqrt and per
+    merge that has trailing columns of A, the same chunk tasks as the blocked
+    form, each waiting for its own tile's build, and every rebuild of a slot
+    (two panels later) waiting for all chunks that read it before."""
+    import ctypes
+    nbld, nch, ntc = ctypes.c_longlong(0), ctypes.c_longlong(0), ctypes.c_longlong(0)
+    assert L.tqr_tile_hqr_dag_check_wy(m, n, 256, 32, grp, nrhs, ctypes.byref(nbld), ctypes.byref(nch)) == 0
+    assert L.tqr_tile_hqr_dag_check_tc(m, n, 256, 32, grp, nrhs, ctypes.byref(ntc)) == 0
+    assert nch.value == ntc.value
+    MT, NT = m // 256, n // 256
+    expect = 0
+    for k in range(min(MT, NT)):
+        if n - (k + 1) * 256 > 0:
+            expect += len(range(k, MT, grp)) + (MT - k) - 1
+    assert nbld.value == expect
+    assert L.tqr_tile_hqr_dag_check_wy(m + 100, n, 256, 32, grp, nrhs, ctypes.byref(nbld),
+                                       ctypes.byref(nch)) == -1   # ragged
+
+
 def test_tile_autotune_argument_errors(L):
     nb, ib = ctypes.c_int(0), ctypes.c_int(0)
     assert L.tqr_tile_autotune(3, 64, 64, 0, ctypes.byref(nb), ctypes.byref(ib), NULL) == -1

@@ -249,3 +249,54 @@ def test_mixed_hqr_is_more_orthogonal_than_fp32_panels(tq):
         orth[f64p] = torch.linalg.norm(Q.t() @ Q - torch.eye(n, dtype=torch.float64, device="cuda")).item()
     print(f"\nhqr {m}x{n} grp {grp}: ||I - Q^T Q||_F FP32 panels {orth[False]:.3e}, FP64 panels {orth[True]:.3e}")
     assert orth[True] < 0.75 * orth[False]
+
+
+@pytest.mark.parametrize("m,n,grp,f64p", [(4096, 1024, 4, False), (2048, 1024, 1, False), (8192, 512, 8, True),
+                                          (2048, 2048, 2, True), (4096, 1280, 16, True)])
+def test_hqr_compact_wy_matches_oracle_and_blocked_form(tq, oracle, m, n, grp, f64p):
+    """The FP32 task graph with its tensor-core updates in compact-WY form
+    (tqr_tile_tc_wy(1): one slot build per reflector tile; unmqr!, tsmqr! and
+    ttmqr! chunks as three products over all k reflectors) against the FP64
+    oracle's hierarchical tree on the same FP32-valued input, beside the same
+    graph applying ib-block by ib-block (the default).  grp 1 is the binary
+    tree (every merge a ttqrt!, V upper triangular).
+
+    Bars: the WY form puts one more TF32x3 product (the k x k T) into every
+    update and accumulates 256-term sums in TMEM, so its errors run about
+    twice the blocked form's (measured: 1.9x to 2.9x).  Each output within
+    three times the FP32 bar of the mixed test above normwise and thirty
+    times entrywise, and within four times the blocked form's own error."""
+    import torch
+    from tileqr import _lib
+    nb, ib = 256, 32
+    rng = np.random.default_rng(7 * m + grp)
+    A0 = rng.standard_normal((m, n)).astype(np.float32).astype(np.float64)
+    outs = {}
+    old = _lib.lib().tqr_tile_tc_wy(0)
+    try:
+        for wy in (1, 0):
+            _lib.lib().tqr_tile_tc_wy(wy)
+            A = tq.to_device(A0, dtype=torch.float32)
+            res = tq.tile_geqrf_tree(A, nb, ib, grp=grp, f64p=f64p)
+            torch.cuda.synchronize()
+            outs[wy] = [tq.to_numpy(x).astype(np.float64) for x in (A,) + tuple(res)]
+    finally:
+        _lib.lib().tqr_tile_tc_wy(old)
+    Ao = np.asfortranarray(A0)
+    res = oracle.tile_geqrf_hqr(Ao, nb, ib, grp)
+    ref = [Ao] + list(res)
+    bar = 1e-5 * np.sqrt(m / nb)
+    for x, b, y in zip(outs[1], outs[0], ref):
+        ny = np.linalg.norm(y)
+        e_wy, e_blk = np.linalg.norm(x - y) / ny, np.linalg.norm(b - y) / ny
+        assert e_wy <= 3 * bar
+        assert rel(x, y) < 30 * bar
+        assert e_wy <= 4 * e_blk + 1e-7
+        assert rel(x, y) <= 4 * rel(b, y) + 1e-7
+    # the stored factors take A back to R through the tree's Q^T
+    A = tq.to_device(outs[1][0], dtype=torch.float32)
+    T, tau, T2, tau2 = (tq.to_device(x, dtype=torch.float32) for x in outs[1][1:])
+    QtA = tq.to_device(A0, dtype=torch.float32)
+    tq.tile_unmqr_tree("C", A, T, T2, QtA, nb, ib, grp=grp)
+    R = np.triu(outs[1][0][:n])
+    assert np.linalg.norm(tq.to_numpy(QtA)[:n].astype(np.float64) - R) <= 1e-5 * np.linalg.norm(R)
