@@ -496,7 +496,9 @@ int tqr_stile_gels(int m, int n, int nrhs, int nb, int ib, float *A, int lda, fl
  * `tol` or after `maxit` iterations; `iters` and `relres` (that ratio) report
  * where it stopped.  A and B are not modified.  `work` (256-byte aligned) holds
  * the FP32 factor and the iteration vectors; its size comes from
- * tqr_dsgels_worksize.  Synchronises `stream` once per iteration. */
+ * tqr_dsgels_worksize.  Synchronises `stream` once per iteration.  Returns
+ * cudaErrorTimeout (a positive status) if a bounded device wait of the
+ * refinement's triangular solves ran out (2 s); X is then not the solution. */
 int tqr_dsgels_worksize(int m, int n, int nrhs, int nb, int ib, size_t *bytes);
 int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, const double *B,
                int ldb, double *X, int ldx, int maxit, double tol, void *work, size_t lwork,
@@ -515,6 +517,19 @@ int tqr_dsgels_fp64_panels(int on);
  * Returns the previous setting.  Process-wide; tqr_dsgels_worksize depends
  * on it. */
 int tqr_dsgels_hqr_group(int grp);
+/* The CGLS refinement of tqr_dsgels applies R^-1 and R^-T (R's 256 x 256
+ * diagonal blocks inverted once) as a pipelined task list: 8-row tasks, the
+ * update of a row block by one solved block (B_t -= op(R)_{t,s} X_s) and the
+ * product with an inverted diagonal block (X_t = op(R_tt^-1) B_t), ordered
+ * by per-block counters instead of grid-wide barriers; every sum runs in a
+ * fixed order.  tqr_dsgels_trsv_pipelined(0) selects the previous form, one
+ * cooperative launch with two grid barriers per block (for comparison); 1
+ * restores the default.  Returns the previous setting.  Process-wide.
+ * tqr_dsgels_trsv_pipe_check: host replay of the task list for order n
+ * (every wait on earlier work, each row block's updates in source order,
+ * every task once); 0 = consistent, *ntasks the task count. */
+int tqr_dsgels_trsv_pipelined(int on);
+int tqr_dsgels_trsv_pipe_check(int n, long long *ntasks);
 /* The FP32 tile QR with FP64 panels on its own (the factorisation of
  * tqr_dsgels, without B): as tqr_stile_geqrf_dag, same T/tau layouts; `work`
  * from tqr_tile_dag_worksize (which covers this form). */

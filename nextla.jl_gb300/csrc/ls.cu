@@ -31,6 +31,7 @@
 //   k_trinv_diag / k_blk_solve  triangular solves through inverted diagonal blocks
 //   small column kernels for the CGLS recurrences (dots, axpys)
 #include <algorithm>
+#include <vector>
 #include <cmath>
 #include <cstring>
 
@@ -560,6 +561,203 @@ k_trsv_coop(int trans, int n, const float *__restrict__ Rm, int ldr, const doubl
   }
 }
 
+// ---- the same solve as a pipelined task list (no grid barrier) ------------
+// The cooperative form above spends most of its time in its 2 n / 256 grid
+// barriers.  Here the 256-row blocks are taken in solve order s = 0, 1, ...
+// (trans 0: the last block first; trans 1: the first block first), and the
+// work is cut into tasks of kPipeRows rows (one warp per row) of a block:
+//   X(s, p):    X_s[rows] = op(Rinv_s) B_s            needs every chain U(s, ., q) complete
+//   U(t, s, p): B_t[rows] -= op(R)_{t,s} X_s, s < t   needs X(s) and U(t, s - 1, p)
+// listed as X(0); then for s = 1 .. nblk - 1: U(s, s - 1), X(s), and
+// U(t, s - 1) for t = s + 1 .. nblk - 1.  The critical chain per block is
+// one U and one X, the other U tasks fill the machine meanwhile.  Every
+// dependency is an earlier task and CTAs take tasks in list order, so the
+// first unfinished task can always run.  Each B row is updated by one chain
+// in source order and every sum runs in a fixed order: the result does not
+// depend on timing.  Flags (ints): [0] next task, [1] error (stops this
+// launch), [2] sticky error (kept across launches until the solve reads it),
+// then X parts done per block, U chains completed per block, and per
+// (block, row part) the sources applied so far.
+constexpr int kPipeRows = TQR_WARPS;
+constexpr int kPipeParts = 256 / kPipeRows;
+
+__host__ __device__ inline int pipe_units(int nblk) { return 1 + (nblk - 1) * (nblk + 2) / 2; }
+__host__ __device__ inline size_t pipe_flag_ints(int nblk) { return 4 + 2 * (size_t)nblk + (size_t)nblk * kPipeParts; }
+
+// Unit u of the list: kind 0 = X(t), 1 = U(t, s).
+__host__ __device__ inline void pipe_unit(int u, int nblk, int &kind, int &t, int &s) {
+  kind = 0; t = 0; s = 0;
+  if (u == 0) return;
+  int rem = u - 1;
+  for (int q = 1; q < nblk; ++q) {
+    const int len = nblk + 1 - q;
+    if (rem < len) {
+      if (rem == 1) { kind = 0; t = q; }
+      else { kind = 1; t = rem == 0 ? q : q + rem - 1; s = q - 1; }
+      return;
+    }
+    rem -= len;
+  }
+  kind = -1;
+}
+
+__device__ inline bool pipe_wait(const int *f, int target, int *err) {
+  unsigned long long t0, t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  while (ls_ld_acquire(f) < target) {
+    if (ls_ld_acquire(err)) return false;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (t - t0 > 2000000000ull) {
+      atomicExch(err, 1);
+      atomicExch(err + 1, 1);
+      return false;
+    }
+    __nanosleep(32);
+  }
+  return true;
+}
+
+template <int K>
+__global__ void __launch_bounds__(TQR_THREADS)
+k_trsv_pipe(int trans, int n, const float *__restrict__ Rm, int ldr, const double *__restrict__ Rinv,
+            const double *__restrict__ RinvT, double *B, int ldb, double *X, int ldx, int *flags) {
+  __shared__ int s_task, s_ok;
+  __shared__ double part[TQR_WARPS][kPipeRows][K];
+  const int nblk = (n + 255) / 256, ntask = pipe_units(nblk) * kPipeParts;
+  int *xdone = flags + 4, *ucnt = xdone + nblk, *uprog = ucnt + nblk;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (;;) {
+    if (threadIdx.x == 0) s_task = atomicAdd(flags, 1);
+    __syncthreads();
+    const int task = s_task;
+    if (task >= ntask) return;
+    const int pr = task % kPipeParts;
+    int kind, t, s;
+    pipe_unit(task / kPipeParts, nblk, kind, t, s);
+    if (threadIdx.x == 0) {
+      bool ok = true;
+      if (kind == 0 && t > 0) ok = pipe_wait(ucnt + t, kPipeParts, flags + 1);
+      if (kind == 1) ok = pipe_wait(xdone + s, kPipeParts, flags + 1) && pipe_wait(uprog + t * kPipeParts + pr, s, flags + 1);
+      s_ok = ok && kind >= 0;
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    const int bt = trans ? t : nblk - 1 - t, bt0 = bt * 256, nbt = min(256, n - bt0);
+    const int r0 = pr * kPipeRows;
+    if (kind == 0) {
+      // X_t rows: column r of M holds op(Rinv_t)[r][.]
+      const int r = r0 + warp;
+      if (r < nbt) {
+        const double *M = (trans ? Rinv : RinvT) + (size_t)bt * 65536;
+        double acc[K];
+#pragma unroll
+        for (int c = 0; c < K; ++c) acc[c] = 0.0;
+        const int q0 = trans ? 0 : r, q1 = trans ? r + 1 : nbt;
+        for (int qq = q0 + lane; qq < q1; qq += 32) {
+          const double a = M[ix(qq, r, 256)];
+#pragma unroll
+          for (int c = 0; c < K; ++c) acc[c] = fma(a, __ldcg(B + ix(bt0 + qq, c, ldb)), acc[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < K; ++c) {
+          const double v = warp_sum(acc[c]);
+          if (lane == 0) X[ix(bt0 + r, c, ldx)] = v;
+        }
+      }
+    } else {
+      const int bs = trans ? s : nblk - 1 - s, bs0 = bs * 256, nbs = min(256, n - bs0);
+      if (trans) {
+        // R^T: row r of B_t takes column bt0 + r of R's block (s, t), lanes along it
+        const int r = r0 + warp;
+        if (r < nbt) {
+          double acc[K];
+#pragma unroll
+          for (int c = 0; c < K; ++c) acc[c] = 0.0;
+          for (int j = lane; j < nbs; j += 32) {
+            const double a = widen(Rm[ix(bs0 + j, bt0 + r, ldr)]);
+#pragma unroll
+            for (int c = 0; c < K; ++c) acc[c] = fma(a, __ldcg(X + ix(bs0 + j, c, ldx)), acc[c]);
+          }
+#pragma unroll
+          for (int c = 0; c < K; ++c) {
+            const double v = warp_sum(acc[c]);
+            if (lane == 0) B[ix(bt0 + r, c, ldb)] = __ldcg(B + ix(bt0 + r, c, ldb)) - v;
+          }
+        }
+      } else {
+        // R: the task's rows are 8 consecutive entries of each column of R's
+        // block (t, s); warp w takes columns [32 w, 32 w + 32), lane = row
+        // + 8 x (column mod 4), then a fixed-order sum over lanes and warps
+        const int rr = lane & 7, jj = lane >> 3, r = r0 + rr;
+        double acc[K];
+#pragma unroll
+        for (int c = 0; c < K; ++c) acc[c] = 0.0;
+        if (r < nbt) {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const int j = 32 * warp + jj + 4 * i;
+            if (j < nbs) {
+              const double a = widen(Rm[ix(bt0 + r, bs0 + j, ldr)]);
+#pragma unroll
+              for (int c = 0; c < K; ++c) acc[c] = fma(a, __ldcg(X + ix(bs0 + j, c, ldx)), acc[c]);
+            }
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < K; ++c) {
+          acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 8);
+          acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 16);
+          if (jj == 0) part[warp][rr][c] = acc[c];
+        }
+        __syncthreads();
+        if (threadIdx.x < kPipeRows * K) {
+          const int q = threadIdx.x % kPipeRows, c = threadIdx.x / kPipeRows;
+          if (r0 + q < nbt) {
+            double v = 0.0;
+#pragma unroll
+            for (int w = 0; w < TQR_WARPS; ++w) v += part[w][q][c];
+            B[ix(bt0 + r0 + q, c, ldb)] = __ldcg(B + ix(bt0 + r0 + q, c, ldb)) - v;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      if (kind == 0) {
+        atomicAdd(xdone + t, 1);
+      } else {
+        asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(uprog + t * kPipeParts + pr), "r"(s + 1) : "memory");
+        if (s == t - 1) atomicAdd(ucnt + t, 1);
+      }
+    }
+  }
+}
+
+template <int K>
+static int trsv_pipe_k(int trans, int n, const float *Rm, int ldr, const double *Rinv, const double *RinvT, double *B,
+                       int ldb, double *X, int ldx, int *flags, cudaStream_t st) {
+  int dev = 0, sms = 0, per = 0;
+  LS_CU(cudaGetDevice(&dev));
+  LS_CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  LS_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_trsv_pipe<K>, TQR_THREADS, 0));
+  if (per < 1) return (int)cudaErrorInvalidConfiguration;
+  const int nblk = (n + 255) / 256;
+  const int ntask = pipe_units(nblk) * kPipeParts;
+  // everything but the sticky error word
+  LS_CU(cudaMemsetAsync(flags, 0, sizeof(int) * 2, st));
+  LS_CU(cudaMemsetAsync(flags + 4, 0, sizeof(int) * (pipe_flag_ints(nblk) - 4), st));
+  k_trsv_pipe<K><<<std::min(sms * std::min(per, 2), ntask), TQR_THREADS, 0, st>>>(trans, n, Rm, ldr, Rinv, RinvT,
+                                                                                  B, ldb, X, ldx, flags);
+  count_launch();
+  LS_CU(cudaGetLastError());
+  return 0;
+}
+
+// Whether the mixed solve's CGLS runs its triangular solves as the pipelined
+// task list (tqr_dsgels_trsv_pipelined) or with grid barriers.
+static int g_trsv_pipe = 1;
+
 template <int K>
 static int trsv_coop_k(int trans, int n, const float *Rm, int ldr, const double *Rinv, const double *RinvT, double *B,
                        int ldb, double *X, int ldx, GridBar *gb, cudaStream_t st) {
@@ -606,6 +804,15 @@ static int trsm_sd_inv(int trans, int n, int k, const float *Rm, int ldr, const 
 
 static int trsv_coop(int trans, int n, int k, const float *Rm, int ldr, const double *Rinv, const double *RinvT,
                      double *B, int ldb, double *X, int ldx, GridBar *gb, cudaStream_t st) {
+  if (g_trsv_pipe) {
+    int *flags = reinterpret_cast<int *>(gb);
+    switch (k) {
+      case 4: return trsv_pipe_k<4>(trans, n, Rm, ldr, Rinv, RinvT, B, ldb, X, ldx, flags, st);
+      case 2: return trsv_pipe_k<2>(trans, n, Rm, ldr, Rinv, RinvT, B, ldb, X, ldx, flags, st);
+      case 1: return trsv_pipe_k<1>(trans, n, Rm, ldr, Rinv, RinvT, B, ldb, X, ldx, flags, st);
+      default: break;
+    }
+  }
   switch (k) {
     case 4: return trsv_coop_k<4>(trans, n, Rm, ldr, Rinv, RinvT, B, ldb, X, ldx, gb, st);
     case 2: return trsv_coop_k<2>(trans, n, Rm, ldr, Rinv, RinvT, B, ldb, X, ldx, gb, st);
@@ -703,7 +910,7 @@ static int mixed_ws(int m, int n, int k, int nb, int ib, MixedWs *w) {
   w->rinv = take(sizeof(double) * 65536 * (size_t)((n + 255) / 256));
   w->rinvt = take(sizeof(double) * 65536 * (size_t)((n + 255) / 256));
   w->tmpn = take(sizeof(double) * (size_t)n * k);
-  w->gbar = take(sizeof(GridBar));
+  w->gbar = take(std::max(sizeof(GridBar), sizeof(int) * pipe_flag_ints((n + 255) / 256)));
   w->total = off;
   return dag ? 0 : 1;
 }
@@ -719,6 +926,52 @@ int tqr_dsgels_phases(double *ms, int *iters) {
     for (int i = 0; i < 3; ++i) ms[i] = g_phase_ms[i];
   if (iters) *iters = g_phase_iters;
   return 0;
+}
+
+int tqr_dsgels_trsv_pipe_check(int n, long long *ntasks) {
+  // Host replay of the pipelined solve's task list in list order: every wait
+  // is on work finished earlier in the list, each row part applies its
+  // sources in order 0, 1, ..., t - 1 before X(t), and every X and U runs once.
+  if (n <= 0) return -1;
+  const int nblk = (n + 255) / 256, nu = pipe_units(nblk);
+  std::vector<int> xdone(nblk, 0), ucnt(nblk, 0), uprog((size_t)nblk * kPipeParts, 0);
+  std::vector<int> seen_x(nblk, 0), seen_u((size_t)nblk * nblk, 0);
+  long long nt = 0;
+  for (int u = 0; u < nu; ++u) {
+    int kind, t, s;
+    pipe_unit(u, nblk, kind, t, s);
+    if (kind < 0 || t < 0 || t >= nblk) return 1;
+    if (kind == 0) {
+      if (seen_x[t]++) return 2;
+      if (t > 0 && ucnt[t] < kPipeParts) return 3;
+    } else {
+      if (s < 0 || s >= t || seen_u[(size_t)t * nblk + s]++) return 4;
+      if (xdone[s] < kPipeParts) return 5;
+    }
+    for (int pr = 0; pr < kPipeParts; ++pr, ++nt) {
+      if (kind == 0) {
+        ++xdone[t];
+      } else {
+        int &g = uprog[(size_t)t * kPipeParts + pr];
+        if (g != s) return 6;
+        g = s + 1;
+        if (s == t - 1) ++ucnt[t];
+      }
+    }
+  }
+  for (int t = 0; t < nblk; ++t) {
+    if (!seen_x[t]) return 7;
+    for (int s = 0; s < t; ++s)
+      if (!seen_u[(size_t)t * nblk + s]) return 8;
+  }
+  if (ntasks) *ntasks = nt;
+  return 0;
+}
+
+int tqr_dsgels_trsv_pipelined(int on) {
+  const int old = g_trsv_pipe;
+  g_trsv_pipe = on ? 1 : 0;
+  return old;
 }
 
 int tqr_dsgels_hqr_group(int grp) {
@@ -806,6 +1059,8 @@ int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, 
   double *Rinv = (double *)(base + w.rinv), *tmpn = (double *)(base + w.tmpn);
   double *RinvT = (double *)(base + w.rinvt);
   GridBar *gbar = (GridBar *)(base + w.gbar);
+  int *sticky = reinterpret_cast<int *>(gbar) + 2;   // the pipelined solves' sticky error word
+  LS_CU(cudaMemsetAsync(sticky, 0, sizeof(int), st));
   LS_TRY(trinv_diag(n, F, m, Rinv, RinvT, st));
   LS_TRY(gemm_sd_t(m, n, k, A, lda, r, m, tmpn, n, 1.0, 0.0, st));
   LS_TRY(trsv_coop(1, n, k, F, m, Rinv, RinvT, tmpn, n, s, n, gbar, st));
@@ -843,8 +1098,11 @@ int tqr_dsgels(int m, int n, int nrhs, int nb, int ib, const float *A, int lda, 
     count_launch();
     LS_CU(cudaGetLastError());
     ++it;
+    int wait_err = 0;
     LS_CU(cudaMemcpyAsync(gh, gamma, sizeof(double) * k, cudaMemcpyDeviceToHost, st));
+    if (g_trsv_pipe) LS_CU(cudaMemcpyAsync(&wait_err, sticky, sizeof(int), cudaMemcpyDeviceToHost, st));
     LS_CU(cudaStreamSynchronize(st));
+    if (wait_err) return (int)cudaErrorTimeout;   // a bounded wait of a triangular solve ran out
     worst = 0.0;
     for (int c = 0; c < k; ++c)
       if (g0[c] > 0) worst = std::max(worst, std::sqrt(gh[c] / g0[c]));

@@ -76,6 +76,8 @@ DIAG = {
     "tqr_dsgels_phases": ([ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I)], _I),
     "tqr_dsgels_fp64_panels": ([_I], _I),
     "tqr_dsgels_hqr_group": ([_I], _I),
+    "tqr_dsgels_trsv_pipelined": ([_I], _I),
+    "tqr_dsgels_trsv_pipe_check": ([_I, ctypes.POINTER(ctypes.c_longlong)], _I),
     "tqr_stile_geqrf_hqr_dag_f64p": ([_I, _I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P,
                                       ctypes.c_size_t, _P], _I),
     "tqr_tile_hqr_dag_check_tc": ([_I, _I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)], _I),

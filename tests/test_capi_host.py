@@ -253,3 +253,17 @@ def test_tile_autotune_argument_errors(L):
     # nothing tuned for this shape yet
     assert L.tqr_tile_tuning(8, 12345, 77, ctypes.byref(nb), ctypes.byref(ib)) == 1
     assert L.tqr_tile_tuning(8, 64, 64, NULL, ctypes.byref(ib)) == -4
+
+
+@pytest.mark.parametrize("n", [1, 256, 300, 1024, 4096, 5000, 16384])
+def test_pipelined_triangular_solve_task_list(L, n):
+    """The mixed solve's pipelined R^-1 / R^-T task list: every wait is on
+    work finished earlier in the list (so the first unfinished task can
+    always run), each row block applies the solved blocks in order before
+    its own product, and every task appears once."""
+    import ctypes
+    nt = ctypes.c_longlong(0)
+    assert L.tqr_dsgels_trsv_pipe_check(n, ctypes.byref(nt)) == 0
+    nblk = (n + 255) // 256
+    assert nt.value == 32 * (nblk + nblk * (nblk - 1) // 2)
+    assert L.tqr_dsgels_trsv_pipe_check(0, ctypes.byref(nt)) == -1
