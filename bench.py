@@ -51,6 +51,8 @@ def parse():
     p.add_argument("--dtype", default="f64", choices=["f64", "f32", "c64", "c128"],
                    help="element type for --kernel (complex: tile only)")
     p.add_argument("--grp", type=int, default=4, help="with --kernel hqr_square: tiles per flat group")
+    p.add_argument("--dag-quantum", type=float, default=None,
+                   help="with --kernel tile: bucket width of the persistent kernel's priority sort")
     p.add_argument("--no-ls", action="store_true", help="skip the least-squares comparison")
     p.add_argument("--ls-only", action="store_true", help="run only the least-squares comparison")
     p.add_argument("--ls-m", type=int, default=32768)
@@ -87,6 +89,9 @@ def kernel_bench(args):
     g = torch.Generator(device="cuda").manual_seed(SEED)
     n = args.n
     res = {}
+    if args.dag_quantum is not None:
+        from tileqr import _lib
+        _lib.lib().tqr_tile_dag_order_quantum(args.dag_quantum)
     if args.kernel in ("tile", "tile_f64p"):
         # the persistent tile QR of an n x n matrix in the chosen precision
         # (FP32: its tsmqr updates on the tensor cores; tile_f64p: FP32 with
@@ -234,6 +239,8 @@ def kernel_bench(args):
         times.append(e0.elapsed_time(e1))
     res = {"kernel": args.kernel, "n": n, "ms": min(times), "tflops": fl / min(times) / 1e9,
            "all_ms": times}
+    if args.dag_quantum is not None:
+        res["dag_quantum"] = args.dag_quantum
     print(json.dumps(res), flush=True)
     return 0
 

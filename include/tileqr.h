@@ -640,6 +640,15 @@ int tqr_stsmqr_tc(int m1, int n, int m2, int k, float *A1, int lda1, float *A2, 
  * strips only), (1) back on; returns the previous setting.
  * tqr_tile_dag_check_tc: host replay check of that schedule. */
 int tqr_tile_dag_tensor_cores(int on);
+/* Order of the flat-tree persistent kernel's task list: by default tasks are
+ * sorted by their longest path to the end of the graph.
+ * tqr_tile_dag_order_quantum(q), q > 0, sorts by that length in buckets of q
+ * full-tile strip updates and keeps the algorithm's loop order inside a
+ * bucket, so consecutive tasks share their reflector tile while it is in L2
+ * (the order stays topological); 0 restores the exact sort.  Applies to
+ * schedules built afterwards (each shape's schedule is cached per setting);
+ * returns the previous value.  Process-wide. */
+double tqr_tile_dag_order_quantum(double q);
 /* The tensor-core updates (tqr_stsmqr_tc and the tensor-core tasks of the
  * FP32 persistent kernels) load A2, A1 and V with the tensor memory
  * accelerator (cp.async.bulk.tensor, 128-byte swizzle, tensor maps encoded on

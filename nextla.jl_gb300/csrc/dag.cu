@@ -35,6 +35,7 @@
 // The DAG path needs m, n multiples of nb, nb a multiple of ib and ib a
 // multiple of nw (the benchmark shapes); other shapes use the stream driver.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -597,6 +598,10 @@ static double item_cost(const DagGeom &g, const DagItem &it) {
   }
 }
 
+// Bucket width of the priority sort in full-tile strip updates (0: exact
+// longest-path order; tqr_tile_dag_order_quantum).
+static double g_order_q = 0.0;
+
 // Replays the natural order: for every counter the list of its writers.
 // Returns false if a wait target is not what the replay gives (tested on the
 // host by tqr_tile_dag_check).
@@ -637,7 +642,18 @@ static bool build_schedule(const DagGeom &g, std::vector<DagItem> &sorted, bool 
   }
   std::vector<int> order(N);
   for (int x = 0; x < N; ++x) order[x] = x;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rank[a] > rank[b]; });
+  if (g_order_q > 0.0) {
+    // ranks in buckets of q full-tile strip updates, loop order inside a
+    // bucket: consecutive tasks then share their reflector tile while it is
+    // in L2 (a predecessor's bucket is never lower, and loop order is
+    // topological, so the order stays topological)
+    const double unit = g_order_q * 4.0 * g.nb * g.nb * g.nw;
+    std::vector<long long> bucket(N);
+    for (int x = 0; x < N; ++x) bucket[x] = (long long)std::floor(rank[x] / unit);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return bucket[a] > bucket[b]; });
+  } else {
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rank[a] > rank[b]; });
+  }
   if (verify) {
     std::vector<int> pos(N);
     for (int x = 0; x < N; ++x) pos[order[x]] = x;
@@ -654,7 +670,9 @@ static std::mutex g_plan_mu;
 static std::map<long long, std::shared_ptr<Plan>> g_plans;
 
 static std::shared_ptr<Plan> get_plan(const DagGeom &g) {
-  const long long key = geom_key(g);
+  long long qbits = 0;
+  std::memcpy(&qbits, &g_order_q, sizeof(qbits));
+  const long long key = (geom_key(g) ^ (qbits * 1099511628211LL)) & 0x7fffffffffffffffLL;
   std::lock_guard<std::mutex> l(g_plan_mu);
   auto f = g_plans.find(key);
   if (f != g_plans.end()) return f->second;
@@ -1096,6 +1114,13 @@ int tqr_tile_dag_occupancy(int dtype_bytes, int tensor_cores, int *ctas_per_sm, 
   *ctas_per_sm = per;
   *smem_bytes = (int)sm;
   return 0;
+}
+
+double tqr_tile_dag_order_quantum(double q) {
+  std::lock_guard<std::mutex> l(g_plan_mu);
+  const double old = g_order_q;
+  g_order_q = q > 0.0 ? q : 0.0;
+  return old;
 }
 
 int tqr_tile_dag_tensor_cores(int on) {

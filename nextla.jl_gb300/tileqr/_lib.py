@@ -114,6 +114,7 @@ DIAG = {
     "tqr_stile_geqrf_tree_dag": ([_I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P, ctypes.c_size_t,
                                   _P], _I),
     "tqr_tile_dag_tensor_cores": ([_I], _I),
+    "tqr_tile_dag_order_quantum": ([ctypes.c_double], ctypes.c_double),
     "tqr_tile_tc_tma": ([_I], _I),
     "tqr_tile_tc_wy": ([_I], _I),
     "tqr_tile_dag_occupancy": ([_I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),

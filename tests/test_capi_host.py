@@ -120,6 +120,20 @@ def test_dag_schedule_replay(L, shape):
     assert rc == 0 and ntasks > 0
 
 
+@pytest.mark.parametrize("q", [1.0, 8.0, 64.0])
+@pytest.mark.parametrize("shape", [(1024, 1024, 256, 32), (4096, 2048, 256, 32), (8192, 8192, 256, 32)])
+def test_dag_bucketed_order_stays_topological(L, shape, q):
+    """The priority sort in rank buckets (loop order inside a bucket) keeps
+    every dependency ahead of its task."""
+    import tileqr
+    old = L.tqr_tile_dag_order_quantum(q)
+    try:
+        rc, ntasks = tileqr.dag_check(*shape)
+    finally:
+        L.tqr_tile_dag_order_quantum(old)
+    assert rc == 0 and ntasks > 0
+
+
 def test_dag_shape_eligibility(L):
     import tileqr
     assert tileqr.dag_worksize(1000, 1000, 256, 32) is None      # not a multiple of nb
