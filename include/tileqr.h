@@ -458,6 +458,56 @@ int tqr_dtile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, con
 int tqr_stile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, const float *A, int lda,
                          const float *T, const float *T2, int ldt, float *B, int ldb, cudaStream_t stream);
 
+/* The tree and hierarchical drivers for ComplexF64 (z) and ComplexF32 (c)
+ * elements (no counterpart driver in NextLA; the reference runs its TT
+ * kernels on ComplexF64, test/ttqrt.jl:28-66): the same reductions with the
+ * complex geqrt!/unmqr!/tsqrt!/tsmqr!/ttqrt!/ttmqr! arithmetic, Q^H where the
+ * real forms apply Q^T ('T' acts as 'C').  Same arguments, layouts and
+ * errors as the real forms; element pointers aligned to the element size
+ * (the position of A otherwise).  ComplexF64 runs 8-column strips (one CTA
+ * per SM), ComplexF32 the real geometry; the task-graph forms
+ * (..._dag) take `work` from tqr_tile_hqr_dag_worksize /
+ * tqr_tile_tree_dag_worksize, which cover every element type.
+ * tqr_tile_hqr_dag_check_strips: the host order check of a task graph with
+ * strips of nw columns (16, or 8 for ComplexF64). */
+int tqr_ztile_geqrf_tree(int m, int n, int nb, int ib, tqr_zcomplex *A, int lda, tqr_zcomplex *T,
+                         tqr_zcomplex *T2, int ldt, tqr_zcomplex *tau, tqr_zcomplex *tau2, int ldtau, int nrhs,
+                         tqr_zcomplex *B, int ldb, cudaStream_t stream);
+int tqr_ctile_geqrf_tree(int m, int n, int nb, int ib, tqr_ccomplex *A, int lda, tqr_ccomplex *T,
+                         tqr_ccomplex *T2, int ldt, tqr_ccomplex *tau, tqr_ccomplex *tau2, int ldtau, int nrhs,
+                         tqr_ccomplex *B, int ldb, cudaStream_t stream);
+int tqr_ztile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, const tqr_zcomplex *A, int lda,
+                         const tqr_zcomplex *T, const tqr_zcomplex *T2, int ldt, tqr_zcomplex *B, int ldb,
+                         cudaStream_t stream);
+int tqr_ctile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, const tqr_ccomplex *A, int lda,
+                         const tqr_ccomplex *T, const tqr_ccomplex *T2, int ldt, tqr_ccomplex *B, int ldb,
+                         cudaStream_t stream);
+int tqr_ztile_geqrf_hqr(int m, int n, int nb, int ib, int grp, tqr_zcomplex *A, int lda, tqr_zcomplex *T,
+                        tqr_zcomplex *T2, int ldt, tqr_zcomplex *tau, tqr_zcomplex *tau2, int ldtau, int nrhs,
+                        tqr_zcomplex *B, int ldb, cudaStream_t stream);
+int tqr_ctile_geqrf_hqr(int m, int n, int nb, int ib, int grp, tqr_ccomplex *A, int lda, tqr_ccomplex *T,
+                        tqr_ccomplex *T2, int ldt, tqr_ccomplex *tau, tqr_ccomplex *tau2, int ldtau, int nrhs,
+                        tqr_ccomplex *B, int ldb, cudaStream_t stream);
+int tqr_ztile_unmqr_hqr(char trans, int m, int n, int nrhs, int nb, int ib, int grp, const tqr_zcomplex *A,
+                        int lda, const tqr_zcomplex *T, const tqr_zcomplex *T2, int ldt, tqr_zcomplex *B, int ldb,
+                        cudaStream_t stream);
+int tqr_ctile_unmqr_hqr(char trans, int m, int n, int nrhs, int nb, int ib, int grp, const tqr_ccomplex *A,
+                        int lda, const tqr_ccomplex *T, const tqr_ccomplex *T2, int ldt, tqr_ccomplex *B, int ldb,
+                        cudaStream_t stream);
+int tqr_ztile_geqrf_hqr_dag(int m, int n, int nb, int ib, int grp, tqr_zcomplex *A, int lda, tqr_zcomplex *T,
+                            tqr_zcomplex *T2, int ldt, tqr_zcomplex *tau, tqr_zcomplex *tau2, int ldtau,
+                            int nrhs, tqr_zcomplex *B, int ldb, void *work, size_t lwork, cudaStream_t stream);
+int tqr_ctile_geqrf_hqr_dag(int m, int n, int nb, int ib, int grp, tqr_ccomplex *A, int lda, tqr_ccomplex *T,
+                            tqr_ccomplex *T2, int ldt, tqr_ccomplex *tau, tqr_ccomplex *tau2, int ldtau,
+                            int nrhs, tqr_ccomplex *B, int ldb, void *work, size_t lwork, cudaStream_t stream);
+int tqr_ztile_geqrf_tree_dag(int m, int n, int nb, int ib, tqr_zcomplex *A, int lda, tqr_zcomplex *T,
+                             tqr_zcomplex *T2, int ldt, tqr_zcomplex *tau, tqr_zcomplex *tau2, int ldtau,
+                             int nrhs, tqr_zcomplex *B, int ldb, void *work, size_t lwork, cudaStream_t stream);
+int tqr_ctile_geqrf_tree_dag(int m, int n, int nb, int ib, tqr_ccomplex *A, int lda, tqr_ccomplex *T,
+                             tqr_ccomplex *T2, int ldt, tqr_ccomplex *tau, tqr_ccomplex *tau2, int ldtau,
+                             int nrhs, tqr_ccomplex *B, int ldb, void *work, size_t lwork, cudaStream_t stream);
+int tqr_tile_hqr_dag_check_strips(int m, int n, int nb, int ib, int grp, int nrhs, int nw, long long *ntasks);
+
 /* B (m-by-nrhs) := Q^T B (trans 'C'/'T') or Q B (trans 'N'), Q from tile_geqrf. */
 int tqr_dtile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const double *A, int lda,
                     const double *T, int ldt, double *B, int ldb, cudaStream_t stream);

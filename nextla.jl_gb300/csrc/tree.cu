@@ -42,6 +42,20 @@ namespace tqr {
 
 constexpr int kTreeNW = 16;
 constexpr size_t kTreeSmem = 110976;
+// Strip width per element type: 16 columns for the 8-byte and smaller
+// elements, 8 for ComplexF64, whose 16-byte elements would not fit a strip
+// with its V block in one CTA's shared memory otherwise.
+template <typename R> struct TreeNW { static constexpr int value = kTreeNW; };
+template <> struct TreeNW<cx<double>> { static constexpr int value = 8; };
+
+// Dynamic shared memory of the tree kernels for element type R: the panel
+// block, the tsqrt block and a staged strip apply at nb = 256, ib = 32
+// (kTreeSmem for the real types; ComplexF64 takes one CTA per SM).
+template <typename R>
+static size_t tree_smem() {
+  return std::max({kTreeSmem, apply_smem_elems(256, 32, TreeNW<R>::value, true, true, true) * sizeof(R),
+                   panel_smem<R>(256, 32, true, true), tsqrt_smem<R>(256, 32, true)});
+}
 
 template <typename R>
 struct TreeGeom {
@@ -93,15 +107,15 @@ template <typename R>
 __device__ bool trail_region(const TreeGeom<R> &g, const TreeOp &op, int i, int y, R *&C, int &ld, int &ncols,
                              int &c0) {
   const int ca = op.a_cols ? max(0, g.n - (op.k + 1) * g.nb) : 0;
-  const int sa = (ca + kTreeNW - 1) / kTreeNW;
+  const int sa = (ca + TreeNW<R>::value - 1) / TreeNW<R>::value;
   if (y < sa) {
-    C = g.tile(i, op.k + 1); ld = g.lda; ncols = ca; c0 = y * kTreeNW;
+    C = g.tile(i, op.k + 1); ld = g.lda; ncols = ca; c0 = y * TreeNW<R>::value;
     return true;
   }
   y -= sa;
-  const int sbn = (g.nrhs + kTreeNW - 1) / kTreeNW;
+  const int sbn = (g.nrhs + TreeNW<R>::value - 1) / TreeNW<R>::value;
   if (y < sbn) {
-    C = g.B + (size_t)i * g.nb; ld = g.ldb; ncols = g.nrhs; c0 = y * kTreeNW;
+    C = g.B + (size_t)i * g.nb; ld = g.ldb; ncols = g.nrhs; c0 = y * TreeNW<R>::value;
     return true;
   }
   return false;
@@ -113,7 +127,7 @@ __device__ ApplyArgs<R> tree_args(int mode, int L, int k, int ib, int trans) {
   a.mode = mode; a.L = L; a.k = k; a.ib = ib;
   a.fwd = trans ? 0 : 1; a.transT = trans ? 0 : 1;
   a.c_rs = 1; a.a_rs = 1; a.a_cs = 1; a.A1 = nullptr;
-  a.nw = kTreeNW;
+  a.nw = TreeNW<R>::value;
   a.stage_c = 1; a.stage_v = 1; a.stage_t = 1;
   return a;
 }
@@ -139,13 +153,13 @@ __device__ void tree_task(const TreeGeom<R> &g, const TreeOp &op, int i, int y, 
       const int kk = min(mi, nk), c = op.b * ib;
       if (c >= kk) return;
       const int sb = min(ib, kk - c);
-      const int c0 = c + sb + y * kTreeNW;
+      const int c0 = c + sb + y * TreeNW<R>::value;
       if (c0 >= nk) return;
       ApplyArgs<R> a = tree_args<R>(0, mi - c, sb, sb, 0);
       a.C = Aik + c; a.c_cs = g.lda; a.ncols = nk;
       a.V = Aik + ix(c, c, g.lda); a.ldv = g.lda;
       a.T = g.ttile(g.T, i, k) + ix(0, c, g.ldt); a.ldt = g.ldt;
-      apply_strip<R, kTreeNW>(a, c0, smem);
+      apply_strip<R, TreeNW<R>::value>(a, c0, smem);
       return;
     }
     case OP_GE_TRAIL: {
@@ -155,7 +169,7 @@ __device__ void tree_task(const TreeGeom<R> &g, const TreeOp &op, int i, int y, 
       a.C = C; a.c_cs = ld; a.ncols = ncols;
       a.V = Aik; a.ldv = g.lda;
       a.T = g.ttile(g.T, i, k); a.ldt = g.ldt;
-      apply_strip<R, kTreeNW>(a, c0, smem);
+      apply_strip<R, TreeNW<R>::value>(a, c0, smem);
       return;
     }
     default:
@@ -179,7 +193,7 @@ __device__ void tree_task(const TreeGeom<R> &g, const TreeOp &op, int i, int y, 
       const int c = op.b * ib;
       if (c >= kt) return;
       const int sb = min(ib, kt - c);
-      const int c0 = c + sb + y * kTreeNW;
+      const int c0 = c + sb + y * TreeNW<R>::value;
       if (c0 >= nk) return;
       const int L = op.ts ? mp : min(mp, c + sb);
       ApplyArgs<R> a = tree_args<R>(1, L, sb, sb, 0);
@@ -188,7 +202,7 @@ __device__ void tree_task(const TreeGeom<R> &g, const TreeOp &op, int i, int y, 
       a.V = Apk + ix(0, c, g.lda); a.ldv = g.lda;
       a.T = g.ttile(g.T2, p, k) + ix(0, c, g.ldt); a.ldt = g.ldt;
       a.tt = op.ts ? -1 : c;
-      apply_strip<R, kTreeNW>(a, c0, smem);
+      apply_strip<R, TreeNW<R>::value>(a, c0, smem);
       return;
     }
     case OP_PR_TRAIL: {
@@ -202,7 +216,7 @@ __device__ void tree_task(const TreeGeom<R> &g, const TreeOp &op, int i, int y, 
       a.V = Apk; a.ldv = g.lda;
       a.T = g.ttile(g.T2, p, k); a.ldt = g.ldt;
       a.tt = op.ts ? -1 : 0;
-      apply_strip<R, kTreeNW>(a, c0, smem);
+      apply_strip<R, TreeNW<R>::value>(a, c0, smem);
       return;
     }
     default:
@@ -219,15 +233,16 @@ __global__ void __launch_bounds__(TQR_THREADS, 2) k_tree(const TreeGeom<R> g, co
 template <typename R>
 static cudaError_t tree_launch(const TreeGeom<R> &g, const TreeOp &op, int ntask, int ny, cudaStream_t st) {
   if (ntask <= 0 || ny <= 0) return cudaSuccess;
-  k_tree<R><<<dim3(ntask, ny), TQR_THREADS, kTreeSmem, st>>>(g, op);
+  k_tree<R><<<dim3(ntask, ny), TQR_THREADS, tree_smem<R>(), st>>>(g, op);
   count_launch();
   return cudaGetLastError();
 }
 
 template <typename R>
 static int trail_strips(const TreeGeom<R> &g, int k, int a_cols) {
+  constexpr int nw = TreeNW<R>::value;
   const int ca = a_cols ? std::max(0, g.n - (k + 1) * g.nb) : 0;
-  return (ca + kTreeNW - 1) / kTreeNW + (g.nrhs + kTreeNW - 1) / kTreeNW;
+  return (ca + nw - 1) / nw + (g.nrhs + nw - 1) / nw;
 }
 
 template <typename R>
@@ -250,8 +265,9 @@ static inline int tree_nlead(int k, int MTt, int grp) { return (MTt - k + grp - 
 
 template <typename R>
 static cudaError_t tree_factor(const TreeGeom<R> &g, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(k_tree<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTreeSmem);
+  cudaError_t e = cudaFuncSetAttribute(k_tree<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tree_smem<R>());
   if (e != cudaSuccess) return e;
+  constexpr int nw = TreeNW<R>::value;
   const int ib = g.ib, G = g.grp;
   for (int k = 0; k < g.KT; ++k) {
     const int nk = g.cols(k);
@@ -271,7 +287,7 @@ static cudaError_t tree_factor(const TreeGeom<R> &g, cudaStream_t st) {
       if ((e = tree_launch(g, op, nlead, 1, st)) != cudaSuccess) return e;
       const int rest = nk - std::min(nk, std::min(kkmin, (b + 1) * ib));
       op.type = OP_GE_APPLY;
-      if ((e = tree_launch(g, op, nlead, (rest + kTreeNW - 1) / kTreeNW, st)) != cudaSuccess) return e;
+      if ((e = tree_launch(g, op, nlead, (rest + nw - 1) / nw, st)) != cudaSuccess) return e;
     }
     op.type = OP_GE_TRAIL; op.trans = 0;
     if ((e = tree_launch(g, op, nlead, trail_strips(g, k, 1), st)) != cudaSuccess) return e;
@@ -287,7 +303,7 @@ static cudaError_t tree_factor(const TreeGeom<R> &g, cudaStream_t st) {
         if ((e2 = tree_launch(g, q, npair, 1, st)) != cudaSuccess) return e2;
         const int rest = nk - std::min(nk, std::min(kt, (b + 1) * ib));
         q.type = OP_PR_APPLY;
-        if ((e2 = tree_launch(g, q, npair, (rest + kTreeNW - 1) / kTreeNW, st)) != cudaSuccess) return e2;
+        if ((e2 = tree_launch(g, q, npair, (rest + nw - 1) / nw, st)) != cudaSuccess) return e2;
       }
       q.type = OP_PR_TRAIL; q.trans = 0;
       return tree_launch(g, q, npair, trail_strips(g, k, 1), st);
@@ -308,9 +324,10 @@ static cudaError_t tree_factor(const TreeGeom<R> &g, cudaStream_t st) {
 // B := Q^T B (trans 0) or Q B (trans 1) through the stored tree factors.
 template <typename R>
 static cudaError_t tree_apply_q(const TreeGeom<R> &g, int trans, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(k_tree<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTreeSmem);
+  cudaError_t e = cudaFuncSetAttribute(k_tree<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tree_smem<R>());
   if (e != cudaSuccess) return e;
-  const int ny = (g.nrhs + kTreeNW - 1) / kTreeNW, G = g.grp;
+  constexpr int nw = TreeNW<R>::value;
+  const int ny = (g.nrhs + nw - 1) / nw, G = g.grp;
   for (int kx = 0; kx < g.KT; ++kx) {
     const int k = trans ? g.KT - 1 - kx : kx;
     const bool rag = tree_ragged(g, k);
@@ -700,12 +717,13 @@ __global__ void __launch_bounds__(TQR_THREADS, TC ? 1 : 2) k_tree_dag(const __gr
 struct TreeShape {
   int m, n, nb, ib, nrhs, MT, NT, KT;
   int grp = 1;
+  int nw = kTreeNW; // strip width (TreeNW of the element type)
   int tc = 0;       // FP32: trailing updates of A as tensor-core chunk tasks
   int wy = 0;       // with tc: the chunk tasks in compact-WY form, one slot build per reflector tile
   int f64p = 0;     // FP32: panel steps in FP64 (the mixed form)
   int rows(int i) const { return std::min(nb, m - i * nb); }
   int cols(int k) const { return std::min(nb, n - k * nb); }
-  int strips(int j) const { return j < NT ? (cols(j) + kTreeNW - 1) / kTreeNW : (nrhs + kTreeNW - 1) / kTreeNW; }
+  int strips(int j) const { return j < NT ? (cols(j) + nw - 1) / nw : (nrhs + nw - 1) / nw; }
   bool ragged(int k) const { int p = MT - 1; return p > k && rows(p) < cols(k); }
 };
 
@@ -724,7 +742,7 @@ struct TreePlan {
 };
 
 static double tree_cost(const TreeShape &sh, const TItem &it) {
-  const double ib = sh.ib, w = kTreeNW, nb = sh.nb;
+  const double ib = sh.ib, w = sh.nw, nb = sh.nb;
   const int t = it.type & 0x7f;
   const bool ts = it.type & 0x80;
   const double lat = 64.0 * ib * 600;          // serial column steps of a panel
@@ -743,7 +761,7 @@ static double tree_cost(const TreeShape &sh, const TItem &it) {
 
 // Builds the task list in program order with its dependencies, then sorts it.
 static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::vector<uint32_t> &out_deps) {
-  const int NS = std::max(sh.nb / kTreeNW, (sh.nrhs + kTreeNW - 1) / kTreeNW);
+  const int NS = std::max(sh.nb / sh.nw, (sh.nrhs + sh.nw - 1) / sh.nw);
   const int NJ = sh.NT + 1;                    // tile columns plus the right-hand sides
   const int nblk = (sh.nb + sh.ib - 1) / sh.ib;
   // regions: tile strips (upper / lower part), then T blocks of geqrt and of the merges
@@ -787,13 +805,13 @@ static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::
   // trailing strip y of panel k -> (tile column, strip)
   auto trail_js = [&](int k, int y, int &j, int &s) {
     const int ca = std::max(0, sh.n - (k + 1) * sh.nb);
-    const int sa = (ca + kTreeNW - 1) / kTreeNW;
-    if (y < sa) { const int c = y * kTreeNW; j = k + 1 + c / sh.nb; s = (c % sh.nb) / kTreeNW; }
+    const int sa = (ca + sh.nw - 1) / sh.nw;
+    if (y < sa) { const int c = y * sh.nw; j = k + 1 + c / sh.nb; s = (c % sh.nb) / sh.nw; }
     else { j = sh.NT; s = y - sa; }
   };
   auto ntrail = [&](int k) {
     const int ca = std::max(0, sh.n - (k + 1) * sh.nb);
-    return (ca + kTreeNW - 1) / kTreeNW + (sh.nrhs + kTreeNW - 1) / kTreeNW;
+    return (ca + sh.nw - 1) / sh.nw + (sh.nrhs + sh.nw - 1) / sh.nw;
   };
   const int G = sh.grp;
   for (int k = 0; k < sh.KT; ++k) {
@@ -806,16 +824,16 @@ static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::
       const int kk = std::min(sh.rows(i), nk);
       for (int b = 0, c = 0; c < kk; ++b, c += sh.ib) {
         const int sb = std::min(sh.ib, kk - c);
-        const int q0 = c / kTreeNW, q1 = (c + sb + kTreeNW - 1) / kTreeNW;
+        const int q0 = c / sh.nw, q1 = (c + sb + sh.nw - 1) / sh.nw;
         for (int q = q0; q < q1; ++q) { wr(rg(i, k, q, 0)); wr(rg(i, k, q, 1)); }
         wr(rt(i, k, b, 0));
         emit(OP_GE_PANEL, k, b, i, i, 0);
         // strip y covers columns [c + sb + 16 y, +16) clipped to nk (as in tree_task)
-        for (int y = 0; c + sb + y * kTreeNW < nk; ++y) {
-          const int c0 = c + sb + y * kTreeNW, c1 = std::min(nk, c0 + kTreeNW);
+        for (int y = 0; c + sb + y * sh.nw < nk; ++y) {
+          const int c0 = c + sb + y * sh.nw, c1 = std::min(nk, c0 + sh.nw);
           for (int v = q0; v < q1; ++v) rd(rg(i, k, v, 1));
           rd(rt(i, k, b, 0));
-          for (int q = c0 / kTreeNW; q <= (c1 - 1) / kTreeNW; ++q) { wr(rg(i, k, q, 0)); wr(rg(i, k, q, 1)); }
+          for (int q = c0 / sh.nw; q <= (c1 - 1) / sh.nw; ++q) { wr(rg(i, k, q, 0)); wr(rg(i, k, q, 1)); }
           emit(OP_GE_APPLY, k, b, i, i, y);
         }
       }
@@ -839,11 +857,11 @@ static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::
             for (int q = 0; q < NSk; ++q) rd(rg(i, k, q, 1));
             for (int b = 0; b < nbk; ++b) rd(rt(i, k, b, 0));
           }
-          const int c0 = ch * tc::kChunk, j = k + 1 + c0 / sh.nb, s0 = (c0 % sh.nb) / kTreeNW;
-          for (int s = s0; s < s0 + tc::kChunk / kTreeNW; ++s) { wr(rg(i, j, s, 0)); wr(rg(i, j, s, 1)); }
+          const int c0 = ch * tc::kChunk, j = k + 1 + c0 / sh.nb, s0 = (c0 % sh.nb) / sh.nw;
+          for (int s = s0; s < s0 + tc::kChunk / sh.nw; ++s) { wr(rg(i, j, s, 0)); wr(rg(i, j, s, 1)); }
           emit(OP_GE_TRAIL_TC, k, 0, i, i, ch);
         }
-        y0 = (ca + kTreeNW - 1) / kTreeNW;
+        y0 = (ca + sh.nw - 1) / sh.nw;
       }
       for (int y = y0; y < ntrail(k); ++y) {
         int j, s;
@@ -859,7 +877,7 @@ static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::
       const int flag = ts ? 0x80 : 0;
       for (int b = 0, c = 0; c < kt; ++b, c += sh.ib) {
         const int sb = std::min(sh.ib, kt - c);
-        const int q0 = c / kTreeNW, q1 = (c + sb + kTreeNW - 1) / kTreeNW;
+        const int q0 = c / sh.nw, q1 = (c + sb + sh.nw - 1) / sh.nw;
         for (int q = q0; q < q1; ++q) {
           wr(rg(i, k, q, 0));
           wr(rg(p, k, q, 0));
@@ -867,14 +885,14 @@ static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::
         }
         wr(rt(p, k, b, 1));
         emit(OP_PR_PANEL | flag, k, b, i, p, 0);
-        for (int y = 0; c + sb + y * kTreeNW < nk; ++y) {
-          const int c0 = c + sb + y * kTreeNW, c1 = std::min(nk, c0 + kTreeNW);
+        for (int y = 0; c + sb + y * sh.nw < nk; ++y) {
+          const int c0 = c + sb + y * sh.nw, c1 = std::min(nk, c0 + sh.nw);
           for (int v = q0; v < q1; ++v) {
             rd(rg(p, k, v, 0));
             if (ts) rd(rg(p, k, v, 1));
           }
           rd(rt(p, k, b, 1));
-          for (int q = c0 / kTreeNW; q <= (c1 - 1) / kTreeNW; ++q) {
+          for (int q = c0 / sh.nw; q <= (c1 - 1) / sh.nw; ++q) {
             wr(rg(i, k, q, 0));
             wr(rg(p, k, q, 0));
             if (ts) wr(rg(p, k, q, 1));
@@ -908,14 +926,14 @@ static void tree_build(const TreeShape &sh, std::vector<TItem> &out_items, std::
             }
             for (int b = 0; b < nbk; ++b) rd(rt(p, k, b, 1));
           }
-          const int c0 = ch * tc::kChunk, j = k + 1 + c0 / sh.nb, s0 = (c0 % sh.nb) / kTreeNW;
-          for (int s = s0; s < s0 + tc::kChunk / kTreeNW; ++s) {
+          const int c0 = ch * tc::kChunk, j = k + 1 + c0 / sh.nb, s0 = (c0 % sh.nb) / sh.nw;
+          for (int s = s0; s < s0 + tc::kChunk / sh.nw; ++s) {
             wr(rg(i, j, s, 0)); wr(rg(i, j, s, 1));
             wr(rg(p, j, s, 0)); wr(rg(p, j, s, 1));
           }
           emit(OP_PR_TRAIL_TC | flag, k, 0, i, p, ch);
         }
-        y0 = (ca + kTreeNW - 1) / kTreeNW;
+        y0 = (ca + sh.nw - 1) / sh.nw;
       }
       for (int y = y0; y < ntrail(k); ++y) {
         int j, s;
@@ -963,7 +981,7 @@ static long long tree_key(const TreeShape &sh) {
   long long h = 7809847782465536322LL;
   // f64p changes no task or dependency (only the device routines of the
   // panel tasks), so it shares the plan
-  for (int v : {sh.m, sh.n, sh.nb, sh.ib, sh.nrhs, sh.grp, sh.tc, sh.wy, 0x7ee})
+  for (int v : {sh.m, sh.n, sh.nb, sh.ib, sh.nrhs, sh.grp, sh.tc, sh.wy, sh.nw == kTreeNW ? 0 : sh.nw, 0x7ee})
     h = (h ^ (long long)v) * 1099511628211LL;
   return h & 0x7fffffffffffffffLL;
 }
@@ -971,11 +989,12 @@ static long long tree_key(const TreeShape &sh) {
 static std::mutex g_tplan_mu;
 static std::map<long long, std::shared_ptr<TreePlan>> g_tplans;
 
-static bool tree_dag_shape(int m, int n, int nb, int ib, int nrhs, TreeShape *sh, int grp = 1) {
-  if (m <= 0 || n <= 0 || nb <= 0 || nb > 256 || nb % kTreeNW) return false;
+static bool tree_dag_shape(int m, int n, int nb, int ib, int nrhs, TreeShape *sh, int grp = 1, int nw = kTreeNW) {
+  if (m <= 0 || n <= 0 || nb <= 0 || nb > 256 || nb % nw) return false;
   if (grp <= 0) return false;
   sh->grp = grp;
-  if (ib <= 0 || ib > 32 || ib % kTreeNW || nb % ib) return false;
+  sh->nw = nw;
+  if (ib <= 0 || ib > 32 || ib % nw || nb % ib) return false;
   if (nrhs < 0 || nrhs > 256) return false;
   sh->m = m; sh->n = n; sh->nb = nb; sh->ib = ib; sh->nrhs = nrhs;
   sh->MT = (m + nb - 1) / nb; sh->NT = (n + nb - 1) / nb; sh->KT = std::min(sh->MT, sh->NT);
@@ -1049,7 +1068,13 @@ static size_t tree_work_bytes(TreeShape sh) {
     b = std::max(b, tree_plan(sh)->total_bytes + d);
     sh.wy = 1;
     b = std::max(b, tree_plan(sh)->total_bytes + d + tree_wy_bytes(sh));
+    sh.tc = 0;
+    sh.wy = 0;
   }
+  // ComplexF64 runs 8-column strips: another task list
+  TreeShape sz = sh;
+  if (tree_dag_shape(sh.m, sh.n, sh.nb, sh.ib, sh.nrhs, &sz, sh.grp, TreeNW<cx<double>>::value))
+    b = std::max(b, tree_plan(sz)->total_bytes);
   return b;
 }
 
@@ -1090,7 +1115,7 @@ static int tree_geqrf_dag_impl(int m, int n, int nb, int ib, R *A, int lda, R *T
   if (nrhs < 0) return -13;
   if (nrhs > 0 && (!B || ldb < m)) return -15;
   TreeShape sh;
-  if (!tree_dag_shape(m, n, nb, ib, nrhs, &sh, grp)) return -3;
+  if (!tree_dag_shape(m, n, nb, ib, nrhs, &sh, grp, TreeNW<R>::value)) return -3;
   if constexpr (std::is_same<R, float>::value) {
     if (tree_tc_ok(sh, A, lda) && (mixed || tile_tc_enabled())) sh.tc = 1;
     if (mixed) {
@@ -1136,7 +1161,7 @@ static int tree_geqrf_dag_impl(int m, int n, int nb, int ib, R *A, int lda, R *T
       a.tma = make_tmap_f32(&a.tmw, A, m, n, lda, 32, tc::kChunk) == cudaSuccess &&
               make_tmap_f32(&a.tmn, A, m, n, lda, 32, tc::kIb) == cudaSuccess;
   }
-  size_t sm = kTreeSmem;
+  size_t sm = tree_smem<R>();
   if (sh.f64p)
     sm = std::max({sm, panel_f64_smem(nb, ib), tsqrt_f64x_smem(nb, ib), ttqrt_f64_smem(nb, ib)});
   if constexpr (std::is_same<R, float>::value) {
@@ -1199,6 +1224,73 @@ int tqr_stile_geqrf_tree(int m, int n, int nb, int ib, float *A, int lda, float 
 TQR_HQR(d, double)
 TQR_HQR(s, float)
 #undef TQR_HQR
+
+// ComplexF64 (z) and ComplexF32 (c): the same drivers on cx<double> /
+// cx<float> elements (Julia's Complex layout, real part first); the element
+// pointers must be aligned to the element size.
+#define TQR_TREE_CX(P, CT, E)                                                                                 \
+  int tqr_##P##tile_geqrf_tree(int m, int n, int nb, int ib, CT *A, int lda, CT *T, CT *T2, int ldt, CT *tau,    \
+                               CT *tau2, int ldtau, int nrhs, CT *B, int ldb, cudaStream_t stream) {            \
+    if (((uintptr_t)A | (uintptr_t)T | (uintptr_t)T2 | (uintptr_t)tau | (uintptr_t)tau2 | (uintptr_t)B) %      \
+        alignof(E))                                                                                           \
+      return -5;                                                                                              \
+    return tree_geqrf_impl<E>(m, n, nb, ib, (E *)A, lda, (E *)T, (E *)T2, ldt, (E *)tau, (E *)tau2, ldtau,     \
+                              nrhs, (E *)B, ldb, stream);                                                     \
+  }                                                                                                           \
+  int tqr_##P##tile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, const CT *A, int lda,       \
+                               const CT *T, const CT *T2, int ldt, CT *B, int ldb, cudaStream_t stream) {       \
+    if (((uintptr_t)A | (uintptr_t)T | (uintptr_t)T2 | (uintptr_t)B) % alignof(E)) return -7;                 \
+    return tree_unmqr_impl<E>(trans, m, n, nrhs, nb, ib, (const E *)A, lda, (const E *)T, (const E *)T2, ldt, \
+                              (E *)B, ldb, stream);                                                           \
+  }                                                                                                           \
+  int tqr_##P##tile_geqrf_hqr(int m, int n, int nb, int ib, int grp, CT *A, int lda, CT *T, CT *T2, int ldt,     \
+                              CT *tau, CT *tau2, int ldtau, int nrhs, CT *B, int ldb, cudaStream_t stream) {     \
+    if (((uintptr_t)A | (uintptr_t)T | (uintptr_t)T2 | (uintptr_t)tau | (uintptr_t)tau2 | (uintptr_t)B) %      \
+        alignof(E))                                                                                           \
+      return -6;                                                                                              \
+    return tree_geqrf_impl<E>(m, n, nb, ib, (E *)A, lda, (E *)T, (E *)T2, ldt, (E *)tau, (E *)tau2, ldtau,     \
+                              nrhs, (E *)B, ldb, stream, grp);                                                \
+  }                                                                                                           \
+  int tqr_##P##tile_unmqr_hqr(char trans, int m, int n, int nrhs, int nb, int ib, int grp, const CT *A,       \
+                              int lda, const CT *T, const CT *T2, int ldt, CT *B, int ldb, cudaStream_t stream) { \
+    if (((uintptr_t)A | (uintptr_t)T | (uintptr_t)T2 | (uintptr_t)B) % alignof(E)) return -8;                 \
+    return tree_unmqr_impl<E>(trans, m, n, nrhs, nb, ib, (const E *)A, lda, (const E *)T, (const E *)T2, ldt, \
+                              (E *)B, ldb, stream, grp);                                                      \
+  }                                                                                                           \
+  int tqr_##P##tile_geqrf_hqr_dag(int m, int n, int nb, int ib, int grp, CT *A, int lda, CT *T, CT *T2,        \
+                                  int ldt, CT *tau, CT *tau2, int ldtau, int nrhs, CT *B, int ldb, void *work,    \
+                                  size_t lwork, cudaStream_t stream) {                                        \
+    if (((uintptr_t)A | (uintptr_t)T | (uintptr_t)T2 | (uintptr_t)tau | (uintptr_t)tau2 | (uintptr_t)B) %      \
+        alignof(E))                                                                                           \
+      return -6;                                                                                              \
+    return tree_geqrf_dag_impl<E>(m, n, nb, ib, (E *)A, lda, (E *)T, (E *)T2, ldt, (E *)tau, (E *)tau2, ldtau, \
+                                  nrhs, (E *)B, ldb, work, lwork, stream, grp);                               \
+  }                                                                                                           \
+  int tqr_##P##tile_geqrf_tree_dag(int m, int n, int nb, int ib, CT *A, int lda, CT *T, CT *T2, int ldt,       \
+                                   CT *tau, CT *tau2, int ldtau, int nrhs, CT *B, int ldb, void *work,          \
+                                   size_t lwork, cudaStream_t stream) {                                       \
+    if (((uintptr_t)A | (uintptr_t)T | (uintptr_t)T2 | (uintptr_t)tau | (uintptr_t)tau2 | (uintptr_t)B) %      \
+        alignof(E))                                                                                           \
+      return -5;                                                                                              \
+    return tree_geqrf_dag_impl<E>(m, n, nb, ib, (E *)A, lda, (E *)T, (E *)T2, ldt, (E *)tau, (E *)tau2, ldtau, \
+                                  nrhs, (E *)B, ldb, work, lwork, stream);                                    \
+  }
+TQR_TREE_CX(z, tqr_zcomplex, cx<double>)
+TQR_TREE_CX(c, tqr_ccomplex, cx<float>)
+#undef TQR_TREE_CX
+
+int tqr_tile_hqr_dag_check_strips(int m, int n, int nb, int ib, int grp, int nrhs, int nw, long long *ntasks) {
+  TreeShape sh;
+  if (nw <= 0 || !tree_dag_shape(m, n, nb, ib, nrhs, &sh, grp, nw)) return -1;
+  std::shared_ptr<TreePlan> p = tree_plan(sh);
+  for (size_t q = 0; q < p->items.size(); ++q) {
+    const TItem &it = p->items[q];
+    for (int d = 0; d < (int)it.ndep; ++d)
+      if (p->deps[it.dep + d] >= q) return 1;
+  }
+  if (ntasks) *ntasks = (long long)p->items.size();
+  return 0;
+}
 
 int tqr_dtile_unmqr_tree(char trans, int m, int n, int nrhs, int nb, int ib, const double *A, int lda,
                          const double *T, const double *T2, int ldt, double *B, int ldb, cudaStream_t stream) {

@@ -39,7 +39,8 @@ SIGNATURES = {
 
 # routines that also exist for ComplexF64 (prefix z) and ComplexF32 (prefix c)
 COMPLEX = ("geqr2", "larft", "larfb", "geqrt", "unmqr", "tsqrt", "tsmqr", "parfb", "ttqrt", "ttmqr",
-           "tile_geqrf", "tile_unmqr", "trsm_lun", "tile_gels", "pamm")
+           "tile_geqrf", "tile_unmqr", "trsm_lun", "tile_gels", "pamm", "tile_geqrf_tree", "tile_unmqr_tree",
+           "tile_geqrf_hqr", "tile_unmqr_hqr")
 
 
 def prefixes(name):
@@ -107,6 +108,15 @@ DIAG = {
                                  _P], _I),
     "tqr_stile_geqrf_hqr_dag": ([_I, _I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P, ctypes.c_size_t,
                                  _P], _I),
+    "tqr_ztile_geqrf_hqr_dag": ([_I, _I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P, ctypes.c_size_t,
+                                 _P], _I),
+    "tqr_ctile_geqrf_hqr_dag": ([_I, _I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P, ctypes.c_size_t,
+                                 _P], _I),
+    "tqr_ztile_geqrf_tree_dag": ([_I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P, ctypes.c_size_t,
+                                  _P], _I),
+    "tqr_ctile_geqrf_tree_dag": ([_I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P, ctypes.c_size_t,
+                                  _P], _I),
+    "tqr_tile_hqr_dag_check_strips": ([_I, _I, _I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)], _I),
     "tqr_tile_tree_dag_check": ([_I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)], _I),
     "tqr_tile_tree_dag_status": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I), _P], _I),
     "tqr_dtile_geqrf_tree_dag": ([_I, _I, _I, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _P, _I, _P, ctypes.c_size_t,

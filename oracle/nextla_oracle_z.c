@@ -736,6 +736,160 @@ int ora_ztile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const zc
 }
 
 /* ------------------------------------------------------------------------ */
+/* Hierarchical / binary-tree tile QR and its Q application on complex      */
+/* tiles: the driver of nextla_oracle.c (ora_dtile_geqrf_hqr: geqrt on every */
+/* group leader and unmqr of its row, tsqrt/tsmqr of each other tile of the  */
+/* group into its leader, the ragged last tile into the last leader, then    */
+/* ttqrt/ttmqr between leaders at distances grp, 2 grp, ...), with the       */
+/* complex kernels above; same T, tau, T2, tau2 layouts.  grp = 1 is the     */
+/* binary tree of the TT kernels (src/ttqrt.jl:81-118, src/ttmqr.jl:1-95).   */
+/* ------------------------------------------------------------------------ */
+static int ztree_ragged(int m, int nb, int MT, int k, int nk)
+{
+    int p = MT - 1;
+    return p > k && imin(nb, m - p * nb) < nk;
+}
+
+int ora_ztile_geqrf_hqr(int m, int n, int nb, int ib, int grp, zc *A, int lda, zc *T, int ldt,
+                        zc *tau, int ldtau, zc *T2, zc *tau2)
+{
+    if (m < 0) return -1;
+    if (n < 0) return -2;
+    if (nb <= 0) return -3;
+    if (ib <= 0 || ib > nb) return -4;
+    if (grp <= 0) return -5;
+    if (m == 0 || n == 0) return 0;
+    int MT = (m + nb - 1) / nb, NT = (n + nb - 1) / nb, KT = imin(MT, NT);
+    if (lda < m) return -7;
+    if (ldt < MT * ib) return -9;
+    if (ldtau < n) return -11;
+    zc *w = (zc *)malloc(sizeof(zc) * (size_t)nb * (size_t)nb);
+    zc *tv = (zc *)malloc(sizeof(zc) * (size_t)nb);
+    if (!w || !tv) { free(w); free(tv); return -100; }
+    for (int k = 0; k < KT; ++k) {
+        int nk = imin(nb, n - k * nb);
+        int rag = ztree_ragged(m, nb, MT, k, nk);
+        int MTt = rag ? MT - 1 : MT;
+        int last = k + ((MTt - 1 - k) / grp) * grp;
+        for (int i = k; i < MTt; i += grp) {
+            int mi = imin(nb, m - i * nb), kk = imin(mi, nk);
+            zc *Aik = A + IDX(i * nb, k * nb, lda);
+            zc *Tik = T + IDX(i * ib, k * nb, ldt);
+            ora_zgeqrt(mi, nk, ib, Aik, lda, Tik, ldt, tv, w);
+            for (int c = 0; c < kk; ++c) tau[IDX(k * nb + c, i, ldtau)] = tv[c];
+            for (int j = k + 1; j < NT; ++j) {
+                int nj = imin(nb, n - j * nb);
+                ora_zunmqr('L', 'C', mi, nj, kk, ib, Aik, lda, mi, nk, Tik, ldt,
+                           A + IDX(i * nb, j * nb, lda), lda, w, nj);
+            }
+        }
+        for (int d = 1; d <= grp; ++d) {
+            for (int i = k; i < MTt; i += grp) {
+                int p = (d < grp) ? i + d : (rag && i == last ? MT - 1 : -1);
+                if (p < 0 || (d < grp && p >= MTt)) continue;
+                int mp = imin(nb, m - p * nb), mi = imin(nb, m - i * nb);
+                zc *Apk = A + IDX(p * nb, k * nb, lda);
+                zc *T2p = T2 + IDX(p * ib, k * nb, ldt);
+                ora_ztsqrt(mp, nk, ib, mi, A + IDX(i * nb, k * nb, lda), lda, Apk, lda, T2p, ldt, tv, w);
+                for (int c = 0; c < imin(mi, nk); ++c) tau2[IDX(k * nb + c, p, ldtau)] = tv[c];
+                for (int j = k + 1; j < NT; ++j) {
+                    int nj = imin(nb, n - j * nb);
+                    ora_ztsmqr('L', 'C', mi, nj, mp, nj, imin(mi, nk), ib, imin(mi, nk),
+                               A + IDX(i * nb, j * nb, lda), lda, A + IDX(p * nb, j * nb, lda), lda, Apk, lda,
+                               T2p, ldt, w);
+                }
+            }
+        }
+        for (int s = grp; k + s < MTt; s *= 2) {
+            for (int i = k; i < MTt - s; i += 2 * s) {
+                int p = i + s;
+                int mp = imin(nb, m - p * nb), kt = imin(mp, nk);
+                zc *Apk = A + IDX(p * nb, k * nb, lda);
+                zc *T2p = T2 + IDX(p * ib, k * nb, ldt);
+                ora_zttqrt(mp, nk, ib, A + IDX(i * nb, k * nb, lda), lda, Apk, lda, T2p, ldt, tv, w);
+                for (int c = 0; c < kt; ++c) tau2[IDX(k * nb + c, p, ldtau)] = tv[c];
+                for (int j = k + 1; j < NT; ++j) {
+                    int nj = imin(nb, n - j * nb);
+                    ora_zttmqr('L', 'C', nb, nj, mp, nj, kt, ib, A + IDX(i * nb, j * nb, lda), lda,
+                               A + IDX(p * nb, j * nb, lda), lda, Apk, lda, T2p, ldt, w);
+                }
+            }
+        }
+    }
+    free(w);
+    free(tv);
+    return 0;
+}
+
+int ora_ztile_unmqr_hqr(char trans, int m, int n, int nrhs, int nb, int ib, int grp, const zc *A,
+                        int lda, const zc *T, int ldt, const zc *T2, zc *B, int ldb)
+{
+    if (trans != 'N' && trans != 'C' && trans != 'T') return -1;
+    if (m < 0) return -2;
+    if (n < 0) return -3;
+    if (nrhs < 0) return -4;
+    if (nb <= 0) return -5;
+    if (ib <= 0 || ib > nb) return -6;
+    if (grp <= 0) return -7;
+    if (m == 0 || n == 0 || nrhs == 0) return 0;
+    int MT = (m + nb - 1) / nb, NT = (n + nb - 1) / nb, KT = imin(MT, NT);
+    zc *work = (zc *)malloc(sizeof(zc) * (size_t)nrhs * (size_t)nb);
+    if (!work) return -100;
+    const int tr = (trans != 'N');
+    for (int kx = 0; kx < KT; ++kx) {
+        int k = tr ? kx : KT - 1 - kx;
+        int nk = imin(nb, n - k * nb);
+        int rag = ztree_ragged(m, nb, MT, k, nk);
+        int MTt = rag ? MT - 1 : MT;
+        int last = k + ((MTt - 1 - k) / grp) * grp;
+        int smax = grp;
+        while (k + smax < MTt) smax *= 2;
+#define ZGRP_MERGE(i, p, op)                                                                       \
+        do {                                                                                       \
+            int mi_ = imin(nb, m - (i) * nb), mp_ = imin(nb, m - (p) * nb);                        \
+            ora_ztsmqr('L', op, mi_, nrhs, mp_, nrhs, imin(mi_, nk), ib, imin(mi_, nk),            \
+                       B + IDX((i) * nb, 0, ldb), ldb, B + IDX((p) * nb, 0, ldb), ldb,             \
+                       A + IDX((p) * nb, k * nb, lda), lda, T2 + IDX((p) * ib, k * nb, ldt), ldt,   \
+                       work);                                                                      \
+        } while (0)
+#define ZTREE_MERGE(i, p, op)                                                                      \
+        do {                                                                                       \
+            int mp_ = imin(nb, m - (p) * nb);                                                      \
+            ora_zttmqr('L', op, nb, nrhs, mp_, nrhs, imin(mp_, nk), ib, B + IDX((i) * nb, 0, ldb),  \
+                       ldb, B + IDX((p) * nb, 0, ldb), ldb, A + IDX((p) * nb, k * nb, lda), lda,    \
+                       T2 + IDX((p) * ib, k * nb, ldt), ldt, work);                                \
+        } while (0)
+        if (tr) {
+            for (int i = k; i < MTt; i += grp) {
+                int mi = imin(nb, m - i * nb);
+                ora_zunmqr('L', 'C', mi, nrhs, imin(mi, nk), ib, A + IDX(i * nb, k * nb, lda), lda, mi,
+                           nk, T + IDX(i * ib, k * nb, ldt), ldt, B + IDX(i * nb, 0, ldb), ldb, work, nrhs);
+            }
+            for (int d = 1; d < grp; ++d)
+                for (int i = k; i + d < MTt; i += grp) ZGRP_MERGE(i, i + d, 'C');
+            if (rag) ZGRP_MERGE(last, MT - 1, 'C');
+            for (int s = grp; k + s < MTt; s *= 2)
+                for (int i = k; i < MTt - s; i += 2 * s) ZTREE_MERGE(i, i + s, 'C');
+        } else {
+            for (int s = smax / 2; s >= grp; s /= 2)
+                for (int i = k; i < MTt - s; i += 2 * s) ZTREE_MERGE(i, i + s, 'N');
+            if (rag) ZGRP_MERGE(last, MT - 1, 'N');
+            for (int d = grp - 1; d >= 1; --d)
+                for (int i = k; i + d < MTt; i += grp) ZGRP_MERGE(i, i + d, 'N');
+            for (int i = k; i < MTt; i += grp) {
+                int mi = imin(nb, m - i * nb);
+                ora_zunmqr('L', 'N', mi, nrhs, imin(mi, nk), ib, A + IDX(i * nb, k * nb, lda), lda, mi,
+                           nk, T + IDX(i * ib, k * nb, ldt), ldt, B + IDX(i * nb, 0, ldb), ldb, work, nrhs);
+            }
+        }
+#undef ZGRP_MERGE
+#undef ZTREE_MERGE
+    }
+    free(work);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Upper-triangular solve R X = B with LeftUpperTRSM!'s arithmetic           */
 /* (src/trsm.jl:38-63): B scaled by the diagonal first, then                 */
 /* b[r] -= (A[r,i] / A[r,r]) b[i].  Complex division in Smith's scaled form  */

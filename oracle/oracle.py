@@ -77,7 +77,8 @@ def _declare(L):
         "ora_host_blas_on": [],
     }
     for name in ("geqr2", "larft", "larfb", "geqrt", "unmqr", "parfb", "parfb_l", "tsmqr", "tsqrt", "ttqrt",
-                 "ttmqr", "tile_geqrf", "tile_unmqr", "trsm_lun", "pamm", "parfb_full"):
+                 "ttmqr", "tile_geqrf", "tile_unmqr", "trsm_lun", "pamm", "parfb_full", "tile_geqrf_hqr",
+                 "tile_unmqr_hqr"):
         sig["ora_z" + name] = sig["ora_d" + name]
     for name, args in sig.items():
         f = getattr(L, name)
@@ -379,13 +380,14 @@ def tile_geqrf_hqr(A, nb, ib, grp):
     (T, tau, T2, tau2) as tile_geqrf_tree does."""
     m, n = A.shape
     MT = (m + nb - 1) // nb
-    T = np.zeros((MT * ib, n), order="F")
-    T2 = np.zeros((MT * ib, n), order="F")
-    tau = np.zeros((n, MT), order="F")
-    tau2 = np.zeros((n, MT), order="F")
+    T = np.zeros((MT * ib, n), order="F", dtype=A.dtype)
+    T2 = np.zeros((MT * ib, n), order="F", dtype=A.dtype)
+    tau = np.zeros((n, MT), order="F", dtype=A.dtype)
+    tau2 = np.zeros((n, MT), order="F", dtype=A.dtype)
     pa, lda = _mat(A)
-    _check(lib().ora_dtile_geqrf_hqr(m, n, nb, ib, grp, pa, lda, T.ctypes.data, MT * ib, tau.ctypes.data, n,
-                                     T2.ctypes.data, tau2.ctypes.data), "tile_geqrf_hqr")
+    _check(_fn("tile_geqrf_hqr", A, T, tau, T2, tau2)(m, n, nb, ib, grp, pa, lda, T.ctypes.data, MT * ib,
+                                                      tau.ctypes.data, n, T2.ctypes.data, tau2.ctypes.data),
+           "tile_geqrf_hqr")
     return T, tau, T2, tau2
 
 
@@ -393,8 +395,9 @@ def tile_unmqr_hqr(trans, A, T, T2, B, nb, ib, grp):
     m, n = A.shape
     pa, lda = _mat(A)
     pb, ldb = _mat(B)
-    return _check(lib().ora_dtile_unmqr_hqr(_ch(trans), m, n, B.shape[1], nb, ib, grp, pa, lda, T.ctypes.data,
-                                            T.shape[0], T2.ctypes.data, pb, ldb), "tile_unmqr_hqr")
+    return _check(_fn("tile_unmqr_hqr", A, T, T2, B)(_ch(trans), m, n, B.shape[1], nb, ib, grp, pa, lda,
+                                                     T.ctypes.data, T.shape[0], T2.ctypes.data, pb, ldb),
+                  "tile_unmqr_hqr")
 
 
 def tile_unmqr_tree(trans, A, T, T2, B, nb, ib):

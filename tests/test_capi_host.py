@@ -281,3 +281,15 @@ def test_pipelined_triangular_solve_task_list(L, n):
     nblk = (n + 255) // 256
     assert nt.value == 32 * (nblk + nblk * (nblk - 1) // 2)
     assert L.tqr_dsgels_trsv_pipe_check(0, ctypes.byref(nt)) == -1
+
+
+@pytest.mark.parametrize("m,n,nb,ib,grp,nrhs", [(1024, 512, 128, 32, 2, 3), (1000, 300, 128, 16, 1, 0),
+                                                (32768, 4096, 256, 32, 16, 4), (2048, 256, 256, 32, 4, 5)])
+def test_tree_task_graph_with_8_column_strips(L, m, n, nb, ib, grp, nrhs):
+    """The ComplexF64 task graph (8-column strips): topological, with twice the
+    strip tasks of the 16-column graph; the worksize query covers it."""
+    n8, n16 = ctypes.c_longlong(0), ctypes.c_longlong(0)
+    assert L.tqr_tile_hqr_dag_check_strips(m, n, nb, ib, grp, nrhs, 8, ctypes.byref(n8)) == 0
+    assert L.tqr_tile_hqr_dag_check_strips(m, n, nb, ib, grp, nrhs, 16, ctypes.byref(n16)) == 0
+    assert n8.value > n16.value
+    assert L.tqr_tile_hqr_dag_check_strips(m, n, nb, 20, grp, nrhs, 8, ctypes.byref(n8)) == -1   # ib % 8

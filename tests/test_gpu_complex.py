@@ -424,12 +424,69 @@ def test_ztile_gels(tq, oracle, dt):
 
 
 def test_zcomplex_real_only_paths_refuse(tq):
-    """The tree driver and the mixed-precision solve are real-only: they say
-    so instead of running on reinterpreted complex data."""
+    """The mixed-precision solve is real-only: it says so instead of running
+    on reinterpreted complex data, as do the tree driver's mixed arguments
+    (mismatched element types, the FP64-panel form)."""
     A = tq.to_device(crand(np.random.default_rng(0), (512, 256)), dtype=tdt("complex128"))
     T, tau = tq.tile_geqrf(A, 256, 32, dag=True)
     assert T.dtype == tdt("complex128")
     with pytest.raises(TypeError):
-        tq.tile_unmqr_tree("C", A, T, T, tq.zeros(512, 1, dtype=tdt("complex128")), 256, 32)
+        tq.tile_unmqr_tree("C", A, T, T, tq.zeros(512, 1, dtype=tdt("complex64")), 256, 32)
     with pytest.raises(TypeError):
         tq.lstsq_mixed(A, tq.zeros(512, 1, dtype=tdt("complex128")))
+    with pytest.raises(TypeError):
+        tq.tile_geqrf_tree(A, 256, 32, grp=2, f64p=True)
+
+
+ZHQR_SHAPES = [(1024, 256, 128, 32, 1), (1000, 300, 128, 16, 3), (1024, 256, 128, 32, 2), (517, 130, 64, 16, 3),
+               (300, 400, 256, 32, 2), (768, 256, 128, 32, 100), (2048, 512, 256, 32, 4)]
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+@pytest.mark.parametrize("m,n,nb,ib,grp", ZHQR_SHAPES)
+def test_ztree_hqr_matches_oracle(tq, oracle, dt, m, n, nb, ib, grp):
+    """The tree / hierarchical tile QR on complex elements (grp 1: every
+    merge a ttqrt!, as ttqrt!'s ComplexF64 tests run it, test/ttqrt.jl:28-66)
+    against the complex oracle's driver in the same order, B carried along
+    as Q^H B; then Q^H and Q through the stored factors."""
+    rng = np.random.default_rng(m + 3 * n + grp)
+    A0, B0 = rnd(crand(rng, (m, n)), dt), rnd(crand(rng, (m, 3)), dt)
+    A, B = dev(tq, A0, dt), dev(tq, B0, dt)
+    T, tau, T2, tau2 = tq.tile_geqrf_tree(A, nb, ib, B=B, grp=grp)
+    Ao = A0.copy(order="F")
+    To, tauo, T2o, tau2o = oracle.tile_geqrf_hqr(Ao, nb, ib, grp)
+    Bo = B0.copy(order="F")
+    oracle.tile_unmqr_hqr("C", Ao, To, T2o, Bo, nb, ib, grp)
+    bar = tol(dt, max(n, 16))
+    for x, y in ((A, Ao), (T, To), (tau, tauo), (T2, T2o), (tau2, tau2o), (B, Bo)):
+        assert rel(host(tq, x), y) < bar
+    # the stored factors: Q^H A0 = R, and Q (Q^H C) = C
+    k = min(m, n)
+    QhA = dev(tq, A0, dt)
+    tq.tile_unmqr_tree("C", A, T, T2, QhA, nb, ib, grp=grp)
+    R = np.triu(host(tq, A)[:k])
+    assert np.linalg.norm(host(tq, QhA)[:k] - R) <= bar * np.linalg.norm(R)
+    C0 = rnd(crand(rng, (m, 2)), dt)
+    C = dev(tq, C0, dt)
+    tq.tile_unmqr_tree("C", A, T, T2, C, nb, ib, grp=grp)
+    tq.tile_unmqr_tree("N", A, T, T2, C, nb, ib, grp=grp)
+    assert rel(host(tq, C), C0) < bar
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+@pytest.mark.parametrize("m,n,nb,ib,grp,nrhs", [(1024, 512, 128, 32, 2, 3), (1000, 300, 128, 16, 1, 0),
+                                                (2048, 256, 256, 32, 4, 5)])
+def test_ztree_task_graph_equals_stream_driver(tq, dt, m, n, nb, ib, grp, nrhs):
+    """The persistent task graph on complex elements (8-column strips for
+    ComplexF64) runs the stream driver's per-task arithmetic: bit-identical."""
+    import torch
+    rng = np.random.default_rng(m + n + nrhs)
+    A0, B0 = rnd(crand(rng, (m, n)), dt), rnd(crand(rng, (m, max(nrhs, 1))), dt)
+    outs = []
+    for dag in (False, True):
+        A = dev(tq, A0, dt)
+        B = dev(tq, B0[:, :nrhs], dt) if nrhs else None
+        res = tq.tile_geqrf_tree(A, nb, ib, B=B, dag=dag, grp=grp)
+        outs.append((A,) + tuple(res) + ((B,) if nrhs else ()))
+    for a, b in zip(*outs):
+        assert torch.equal(a, b)

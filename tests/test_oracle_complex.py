@@ -272,3 +272,32 @@ def test_ztrsm_smith_division(oracle):
     X = B.copy(order="F")
     oracle.trsm_lun(R, X)
     assert np.abs(R @ X - B).max() < 1e-13
+
+
+@pytest.mark.parametrize("m,n,nb,ib,grp", [(1024, 256, 128, 32, 1), (1000, 300, 128, 16, 3), (1024, 256, 128, 32, 2),
+                                           (517, 130, 64, 16, 3), (300, 400, 256, 32, 2), (768, 256, 128, 32, 100)])
+def test_ztile_hqr_properties(oracle, m, n, nb, ib, grp):
+    """The complex hierarchical / binary-tree tile QR (geqrt on the leaders,
+    tsqrt merges in each group, ttqrt merges between leaders, as ttqrt!'s
+    ComplexF64 tests run them, test/ttqrt.jl:28-66): Q^H A = [R; 0] and
+    Q Q^H = I through the stored factors, and |R| equal to the flat tree's
+    (R is unique up to a unitary diagonal)."""
+    rng = np.random.default_rng(m + n + grp)
+    A0 = Z(rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n)))
+    A = A0.copy(order="F")
+    T, tau, T2, tau2 = oracle.tile_geqrf_hqr(A, nb, ib, grp)
+    assert T.dtype == np.complex128 and tau2.dtype == np.complex128
+    k = min(m, n)
+    R = np.triu(A[:k])
+    B = A0.copy(order="F")
+    oracle.tile_unmqr_hqr("C", A, T, T2, B, nb, ib, grp)
+    assert np.linalg.norm(B[:k] - R) <= 1e-13 * np.linalg.norm(R) * k
+    assert np.linalg.norm(B[k:]) <= 1e-13 * np.linalg.norm(A0) * k
+    C0 = Z(rng.standard_normal((m, 5)) + 1j * rng.standard_normal((m, 5)))
+    C = C0.copy(order="F")
+    oracle.tile_unmqr_hqr("N", A, T, T2, C, nb, ib, grp)
+    oracle.tile_unmqr_hqr("C", A, T, T2, C, nb, ib, grp)
+    assert np.abs(C - C0).max() < 1e-13 * m
+    F = A0.copy(order="F")
+    oracle.tile_geqrf(F, nb, ib)
+    assert np.allclose(np.abs(R), np.abs(np.triu(F[:k])), atol=1e-11 * np.abs(R).max())
