@@ -634,6 +634,46 @@ k_trsv_pipe(int trans, int n, const float *__restrict__ Rm, int ldr, const doubl
     const int pr = task % kPipeParts;
     int kind, t, s;
     pipe_unit(task / kPipeParts, nblk, kind, t, s);
+    const int bt = trans ? t : nblk - 1 - t, bt0 = bt * 256, nbt = min(256, n - bt0);
+    const int bs = trans ? s : nblk - 1 - s, bs0 = bs * 256, nbs = min(256, n - bs0);
+    const int r0 = pr * kPipeRows;
+    // The matrix operand of the task (an inverted diagonal block or a block
+    // of R) does not depend on other tasks: its eight values per lane are
+    // loaded before the wait, so only X or B is read after it.
+    double mv[8];
+    int jv[8];
+    if (kind == 0) {
+      // X_t rows: column r of M holds op(Rinv_t)[r][.]; lane takes q = q0 + lane + 32 u
+      const int r = r0 + warp;
+      const double *M = (trans ? Rinv : RinvT) + (size_t)bt * 65536;
+      const int q0 = trans ? 0 : r, q1 = trans ? r + 1 : nbt;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int qq = q0 + lane + 32 * u;
+        jv[u] = (r < nbt && qq < q1) ? qq : -1;
+        mv[u] = jv[u] >= 0 ? M[ix(qq, r, 256)] : 0.0;
+      }
+    } else if (trans) {
+      // R^T: row r of B_t takes column bt0 + r of R's block (s, t), lanes along it
+      const int r = r0 + warp;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int j = lane + 32 * u;
+        jv[u] = (r < nbt && j < nbs) ? j : -1;
+        mv[u] = jv[u] >= 0 ? widen(Rm[ix(bs0 + j, bt0 + r, ldr)]) : 0.0;
+      }
+    } else {
+      // R: the task's rows are 8 consecutive entries of each column of R's
+      // block (t, s); warp w takes columns [32 w, 32 w + 32), lane = row +
+      // 8 x (column mod 4)
+      const int rr = lane & 7, jj = lane >> 3, r = r0 + rr;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int j = 32 * warp + jj + 4 * u;
+        jv[u] = (r < nbt && j < nbs) ? j : -1;
+        mv[u] = jv[u] >= 0 ? widen(Rm[ix(bt0 + r, bs0 + j, ldr)]) : 0.0;
+      }
+    }
     if (threadIdx.x == 0) {
       bool ok = true;
       if (kind == 0 && t > 0) ok = pipe_wait(ucnt + t, kPipeParts, flags + 1);
@@ -642,82 +682,50 @@ k_trsv_pipe(int trans, int n, const float *__restrict__ Rm, int ldr, const doubl
     }
     __syncthreads();
     if (!s_ok) return;
-    const int bt = trans ? t : nblk - 1 - t, bt0 = bt * 256, nbt = min(256, n - bt0);
-    const int r0 = pr * kPipeRows;
-    if (kind == 0) {
-      // X_t rows: column r of M holds op(Rinv_t)[r][.]
+    // the dependent operand (B_t for X, X_s for U), all eight terms in flight
+    const double *src = kind == 0 ? B + bt0 : X + bs0;
+    const int lds = kind == 0 ? ldb : ldx;
+    double acc[K];
+#pragma unroll
+    for (int c = 0; c < K; ++c) acc[c] = 0.0;
+    {
+      double xv[8][K];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int c = 0; c < K; ++c) xv[u][c] = jv[u] >= 0 ? __ldcg(src + ix(jv[u], c, lds)) : 0.0;
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int c = 0; c < K; ++c) acc[c] = fma(mv[u], xv[u][c], acc[c]);
+    }
+    if (kind == 0 || trans) {
       const int r = r0 + warp;
-      if (r < nbt) {
-        const double *M = (trans ? Rinv : RinvT) + (size_t)bt * 65536;
-        double acc[K];
 #pragma unroll
-        for (int c = 0; c < K; ++c) acc[c] = 0.0;
-        const int q0 = trans ? 0 : r, q1 = trans ? r + 1 : nbt;
-        for (int qq = q0 + lane; qq < q1; qq += 32) {
-          const double a = M[ix(qq, r, 256)];
-#pragma unroll
-          for (int c = 0; c < K; ++c) acc[c] = fma(a, __ldcg(B + ix(bt0 + qq, c, ldb)), acc[c]);
-        }
-#pragma unroll
-        for (int c = 0; c < K; ++c) {
-          const double v = warp_sum(acc[c]);
-          if (lane == 0) X[ix(bt0 + r, c, ldx)] = v;
+      for (int c = 0; c < K; ++c) {
+        const double v = warp_sum(acc[c]);
+        if (lane == 0 && r < nbt) {
+          if (kind == 0) X[ix(bt0 + r, c, ldx)] = v;
+          else B[ix(bt0 + r, c, ldb)] = __ldcg(B + ix(bt0 + r, c, ldb)) - v;
         }
       }
     } else {
-      const int bs = trans ? s : nblk - 1 - s, bs0 = bs * 256, nbs = min(256, n - bs0);
-      if (trans) {
-        // R^T: row r of B_t takes column bt0 + r of R's block (s, t), lanes along it
-        const int r = r0 + warp;
-        if (r < nbt) {
-          double acc[K];
+      // a fixed-order sum over the lanes of one row, then over the warps
+      const int rr = lane & 7, jj = lane >> 3;
 #pragma unroll
-          for (int c = 0; c < K; ++c) acc[c] = 0.0;
-          for (int j = lane; j < nbs; j += 32) {
-            const double a = widen(Rm[ix(bs0 + j, bt0 + r, ldr)]);
+      for (int c = 0; c < K; ++c) {
+        acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 8);
+        acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 16);
+        if (jj == 0) part[warp][rr][c] = acc[c];
+      }
+      __syncthreads();
+      if (threadIdx.x < kPipeRows * K) {
+        const int q = threadIdx.x % kPipeRows, c = threadIdx.x / kPipeRows;
+        if (r0 + q < nbt) {
+          double v = 0.0;
 #pragma unroll
-            for (int c = 0; c < K; ++c) acc[c] = fma(a, __ldcg(X + ix(bs0 + j, c, ldx)), acc[c]);
-          }
-#pragma unroll
-          for (int c = 0; c < K; ++c) {
-            const double v = warp_sum(acc[c]);
-            if (lane == 0) B[ix(bt0 + r, c, ldb)] = __ldcg(B + ix(bt0 + r, c, ldb)) - v;
-          }
-        }
-      } else {
-        // R: the task's rows are 8 consecutive entries of each column of R's
-        // block (t, s); warp w takes columns [32 w, 32 w + 32), lane = row
-        // + 8 x (column mod 4), then a fixed-order sum over lanes and warps
-        const int rr = lane & 7, jj = lane >> 3, r = r0 + rr;
-        double acc[K];
-#pragma unroll
-        for (int c = 0; c < K; ++c) acc[c] = 0.0;
-        if (r < nbt) {
-#pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            const int j = 32 * warp + jj + 4 * i;
-            if (j < nbs) {
-              const double a = widen(Rm[ix(bt0 + r, bs0 + j, ldr)]);
-#pragma unroll
-              for (int c = 0; c < K; ++c) acc[c] = fma(a, __ldcg(X + ix(bs0 + j, c, ldx)), acc[c]);
-            }
-          }
-        }
-#pragma unroll
-        for (int c = 0; c < K; ++c) {
-          acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 8);
-          acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 16);
-          if (jj == 0) part[warp][rr][c] = acc[c];
-        }
-        __syncthreads();
-        if (threadIdx.x < kPipeRows * K) {
-          const int q = threadIdx.x % kPipeRows, c = threadIdx.x / kPipeRows;
-          if (r0 + q < nbt) {
-            double v = 0.0;
-#pragma unroll
-            for (int w = 0; w < TQR_WARPS; ++w) v += part[w][q][c];
-            B[ix(bt0 + r0 + q, c, ldb)] = __ldcg(B + ix(bt0 + r0 + q, c, ldb)) - v;
-          }
+          for (int w = 0; w < TQR_WARPS; ++w) v += part[w][q][c];
+          B[ix(bt0 + r0 + q, c, ldb)] = __ldcg(B + ix(bt0 + r0 + q, c, ldb)) - v;
         }
       }
     }
