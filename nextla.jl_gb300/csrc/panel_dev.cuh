@@ -230,6 +230,169 @@ __device__ bool column_step(const ColumnStep<E> &c, int i, int x0, int m, int nc
   return true;
 }
 
+// The column loop of a staged FP64 panel (T built in shared memory, 256
+// threads) with nothing waiting on the serial parts of a column.  FORM 0:
+// geqr2 (x rows [i + 1, m) of column i, row i of the panel is P's row i);
+// 1: tsqrt (x rows [0, m), row i of the triangle in rowb); 2: ttqrt (x rows
+// [0, min(m, tt + i + 1)), column j of P holds rows [0, tt + j]).  The same
+// arithmetic as column_step, column by column, except the grouping of the T
+// column's sums; per column i:
+//   S  x *= scale (rounded to FP32 with round32);
+//   A  d_j = -tau (row_j [j > i, or any j != i for geqr2] + x^T P_j), j != i,
+//      laid out as (column j = tid / 8, row group tid % 8), three shuffles;
+//   B  column i + 1 updated first and the squares of its next x region summed;
+//   C  warp 0 forms column i + 1's Householder scalars (a square root and two
+//      divisions, ~30 dependent FP64 instructions) while warps 1..7 update
+//      columns i + 2 .. nc - 1 over all x rows, add d to row i and form the T
+//      column's partial sums (seven per row p < i); warp 0 collects those on
+//      a named barrier and adds them in fixed order.
+// part[] holds 256 values: [0, 8) the norm partials, [32, 256) the T partials.
+template <int FORM>
+__device__ void columns_la_f64(double *P, int ldp, double *rowb, int rs, double *Ts, int ldts, double *d,
+                               double *part, double *scal, int m, int k, int nc, int tt, bool round32,
+                               bool zero_t_on_skip, double *tau)
+{
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  double *tpart = part + 32;
+  auto x0 = [&](int i) { return FORM == 0 ? i + 1 : 0; };
+  auto mx = [&](int i) { return FORM == 2 ? min(m, tt + i + 1) : m; };
+  auto scalars = [&](int col) {   // warp 0
+    double t = lane < TQR_WARPS ? part[lane] : 0.0;
+    t += __shfl_xor_sync(0xffffffffu, t, 4);
+    t += __shfl_xor_sync(0xffffffffu, t, 2);
+    t += __shfl_xor_sync(0xffffffffu, t, 1);
+    if (lane == 0) {
+      double beta, tv, sc;
+      if (householder(rowb[(size_t)col + (size_t)col * rs], t, beta, tv, sc)) {
+        if (round32) tv = (double)(float)tv;
+        scal[0] = beta; scal[1] = tv; scal[2] = sc; scal[3] = 1.0;
+      } else {
+        scal[3] = 0.0;
+      }
+    }
+  };
+  auto norm_partials = [&](int col) {
+    const double *xc = P + (size_t)col * ldp;
+    double s = 0.0;
+    for (int r = x0(col) + tid; r < mx(col); r += TQR_THREADS) s = fma(xc[r], xc[r], s);
+    s = warp_sum(s);
+    if (lane == 0) part[warp] = s;
+  };
+  if (k <= 0) return;
+  norm_partials(0);
+  __syncthreads();
+  if (warp == 0) scalars(0);
+  __syncthreads();
+  const int jd = tid >> 3, gd = tid & 7;
+  for (int i = 0; i < k; ++i) {
+    double *xi = P + (size_t)i * ldp;
+    const double beta = scal[0], tv = scal[1], sc = scal[2];
+    const bool has = scal[3] != 0.0;
+    const int lo = x0(i), hi = mx(i);
+    if (!has) {
+      if (tid == 0) tau[i] = 0.0;
+      if (zero_t_on_skip)
+        for (int p = tid; p <= i; p += TQR_THREADS) Ts[p + (size_t)i * ldts] = 0.0;
+      if (i + 1 < k) {
+        norm_partials(i + 1);
+        __syncthreads();
+        if (warp == 0) scalars(i + 1);
+      }
+      __syncthreads();
+      continue;
+    }
+    // ---- S ----
+    if (round32) {
+      for (int r = lo + tid; r < hi; r += TQR_THREADS) xi[r] = (double)(float)(xi[r] * sc);
+    } else {
+      for (int r = lo + tid; r < hi; r += TQR_THREADS) xi[r] *= sc;
+    }
+    __syncthreads();
+    // ---- A ----
+    {
+      double a0 = 0.0, a1 = 0.0;
+      if (jd < nc && jd != i) {
+        const double *pj = P + (size_t)jd * ldp;
+        const int hj = (FORM == 2 && jd < i) ? min(m, tt + jd + 1) : hi;
+        int r = lo + gd;
+        for (; r + 8 < hj; r += 16) {
+          a0 = fma(xi[r], pj[r], a0);
+          a1 = fma(xi[r + 8], pj[r + 8], a1);
+        }
+        if (r < hj) a0 = fma(xi[r], pj[r], a0);
+      }
+      double a = a0 + a1;
+      a += __shfl_xor_sync(0xffffffffu, a, 4);
+      a += __shfl_xor_sync(0xffffffffu, a, 2);
+      a += __shfl_xor_sync(0xffffffffu, a, 1);
+      if (gd == 0 && jd < nc && jd != i) {
+        if (jd > i || (FORM == 0 && jd < i)) a += rowb[(size_t)i + (size_t)jd * rs];
+        d[jd] = -(tv * a);
+      }
+    }
+    __syncthreads();
+    // ---- B: column i + 1 first, the squares of its x region ----
+    if (i + 1 < nc) {
+      double *pn = P + (size_t)(i + 1) * ldp;
+      const double dn = d[i + 1];
+      const bool nrm = i + 1 < k;
+      const int nlo = nrm ? x0(i + 1) : hi, nhi = nrm ? mx(i + 1) : hi;
+      double s = 0.0;
+      for (int r = min(lo, nlo) + tid; r < max(hi, nhi); r += TQR_THREADS) {
+        double v = pn[r];
+        if (r >= lo && r < hi) {
+          v = fma(xi[r], dn, v);
+          pn[r] = v;
+        }
+        if (r >= nlo && r < nhi) s = fma(v, v, s);
+      }
+      if (tid == 0) rowb[(size_t)i + (size_t)(i + 1) * rs] += dn;
+      s = warp_sum(s);
+      if (lane == 0) part[warp] = s;
+      __syncthreads();
+    }
+    // ---- C ----
+    if (warp == 0) {
+      if (i + 1 < k) scalars(i + 1);
+      asm volatile("bar.sync 1, %0;" ::"r"(TQR_THREADS) : "memory");
+      if (lane < i) {
+        double v = tpart[lane];
+#pragma unroll
+        for (int w = 1; w < 7; ++w) v += tpart[w * 32 + lane];
+        Ts[lane + (size_t)i * ldts] = v;
+      }
+    } else {
+      const int w7 = warp - 1;
+      {
+        double v = 0.0;
+        for (int q = lane + w7; q < i; q += 7) v = fma(Ts[lane + (size_t)q * ldts], d[q], v);
+        tpart[w7 * 32 + lane] = v;
+      }
+      asm volatile("bar.arrive 1, %0;" ::"r"(TQR_THREADS) : "memory");
+      // columns i + 2 .. nc - 1 over the x rows, spread over the 224 threads
+      const int rows = hi - lo;
+      if (rows > 0) {
+        int r = tid - 32, j = i + 2;
+        if (r >= rows) { j += r / rows; r %= rows; }
+        while (j < nc) {
+          double *pr = P + lo + r + (size_t)j * ldp;
+          *pr = fma(xi[lo + r], d[j], *pr);
+          r += TQR_THREADS - 32;
+          if (r >= rows) { j += r / rows; r %= rows; }
+        }
+      }
+      if (warp == 1)
+        for (int j2 = i + 2 + lane; j2 < nc; j2 += 32) rowb[(size_t)i + (size_t)j2 * rs] += d[j2];
+      if (tid == 32) {
+        Ts[i + (size_t)i * ldts] = tv;
+        rowb[(size_t)i + (size_t)i * rs] = beta;
+        tau[i] = tv;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 template <typename R>
 __device__ inline R *carve(unsigned char *&p, size_t n) {
   R *r = reinterpret_cast<R *>(p);
@@ -292,7 +455,17 @@ __device__ void panel_qr_cta(int m, int nc, R *A, int lda, R *tau, R *T, int ldt
   }
   __syncthreads();
   const int k = min(m, nc);
-  for (int i = 0; i < k; ++i) {
+  bool done = false;
+  if constexpr (std::is_same<R, double>::value) {
+    // staged FP64 panel with T in shared memory: the latency-hiding column
+    // loop (a one-row column, geqr2.jl:32-35, is its empty-norm case)
+    if (staged && T && stage_t && nc <= 32) {
+      columns_la_f64<0>(c.P, c.ldp, c.P, c.ldp, c.Ts, c.ldts, c.d, c.part, c.scal, m, k, nc, -1, false, true,
+                        tau);
+      done = true;
+    }
+  }
+  for (int i = 0; i < k && !done; ++i) {
     c.row = c.P + i;
     c.rs = c.ldp;
     if (m - i <= 1) {                                  // geqr2.jl:32-35
@@ -373,7 +546,17 @@ __device__ void tsqrt_block_cta(int m, int sb, R *A1, int lda1, R *A2, int lda2,
   c.tt = tt;
   __syncthreads();
   c.rs = ldb;
-  for (int i = 0; i < sb; ++i) {
+  bool done = false;
+  if constexpr (std::is_same<R, double>::value) {
+    if (staged && sb <= 32) {
+      if (tt >= 0)
+        columns_la_f64<2>(c.P, c.ldp, B, ldb, c.Ts, c.ldts, c.d, c.part, c.scal, m, sb, sb, tt, false, false, tau);
+      else
+        columns_la_f64<1>(c.P, c.ldp, B, ldb, c.Ts, c.ldts, c.d, c.part, c.scal, m, sb, sb, -1, false, false, tau);
+      done = true;
+    }
+  }
+  for (int i = 0; i < sb && !done; ++i) {
     c.row = B + i;
     column_step<R>(c, i, 0, tt >= 0 ? min(m, tt + i + 1) : m, sb, true, tau + i, false);
   }
@@ -441,16 +624,20 @@ __device__ inline void panel_qr_cta_f64(int m, int nc, float *A, int lda, float 
   }
   __syncthreads();
   const int k = min(m, nc);
-  for (int i = 0; i < k; ++i) {
-    c.row = c.P + i;
-    c.rs = c.ldp;
-    if (m - i <= 1) {                                  // geqr2.jl:32-35
-      if (tid == 0) taus[i] = 0.0;
-      for (int p = tid; p <= i; p += TQR_THREADS) c.Ts[p + (size_t)i * c.ldts] = 0.0;
-      __syncthreads();
-      continue;
+  if (nc <= 32) {
+    columns_la_f64<0>(c.P, c.ldp, c.P, c.ldp, c.Ts, c.ldts, c.d, c.part, c.scal, m, k, nc, -1, true, true, taus);
+  } else {
+    for (int i = 0; i < k; ++i) {
+      c.row = c.P + i;
+      c.rs = c.ldp;
+      if (m - i <= 1) {                                  // geqr2.jl:32-35
+        if (tid == 0) taus[i] = 0.0;
+        for (int p = tid; p <= i; p += TQR_THREADS) c.Ts[p + (size_t)i * c.ldts] = 0.0;
+        __syncthreads();
+        continue;
+      }
+      column_step<double>(c, i, i + 1, m, nc, false, taus + i, true);
     }
-    column_step<double>(c, i, i + 1, m, nc, false, taus + i, true);
   }
   for (int idx = tid; idx < m * nc; idx += TQR_THREADS) {
     const int r = idx % m, cc = idx / m;
@@ -498,9 +685,13 @@ __device__ inline void tsqrt_block_cta_f64(int m, int sb, double *D, int ldd, fl
   }
   __syncthreads();
   c.rs = ldb;
-  for (int i = 0; i < sb; ++i) {
-    c.row = B + i;
-    column_step<double>(c, i, 0, m, sb, true, taus + i, false);
+  if (sb <= 32) {
+    columns_la_f64<1>(c.P, c.ldp, B, ldb, c.Ts, c.ldts, c.d, c.part, c.scal, m, sb, sb, -1, true, false, taus);
+  } else {
+    for (int i = 0; i < sb; ++i) {
+      c.row = B + i;
+      column_step<double>(c, i, 0, m, sb, true, taus + i, false);
+    }
   }
   for (int idx = tid; idx < sb * sb; idx += TQR_THREADS) {
     const int r = idx % sb, cc = idx / sb;
@@ -565,9 +756,13 @@ __device__ inline void ttqrt_block_cta_f64(int m, int sb, int tt, double *D1, in
   c.tt = tt;
   __syncthreads();
   c.rs = ldb;
-  for (int i = 0; i < sb; ++i) {
-    c.row = B + i;
-    column_step<double>(c, i, 0, min(m, tt + i + 1), sb, true, taus + i, false);
+  if (sb <= 32) {
+    columns_la_f64<2>(c.P, c.ldp, B, ldb, c.Ts, c.ldts, c.d, c.part, c.scal, m, sb, sb, tt, true, false, taus);
+  } else {
+    for (int i = 0; i < sb; ++i) {
+      c.row = B + i;
+      column_step<double>(c, i, 0, min(m, tt + i + 1), sb, true, taus + i, false);
+    }
   }
   for (int idx = tid; idx < sb * sb; idx += TQR_THREADS) {
     const int r = idx % sb, cc = idx / sb;
