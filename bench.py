@@ -1098,8 +1098,9 @@ def fp64_mma_peak(tq_lib, torch):
 
 def noalloc_vs_workspace(tq, torch, sizes=(4096, 8192), reps=3):
     """The allocation-free tile QR (tqr_dtile_geqrf_noalloc: schedule in a
-    fixed device array, tasks in loop order) against the workspace entry
-    point (critical-path order) on the same matrix."""
+    fixed device array, written on the device in a one-step lookahead order)
+    against the workspace entry point (critical-path order) on the same
+    matrix."""
     import ctypes
     from tileqr import _lib
     st = torch.cuda.current_stream()

@@ -341,7 +341,8 @@ int tqr_stile_gels_dag(int m, int n, int nrhs, int nb, int ib, float *A, int lda
 /* Allocation-free tile QR (no counterpart in NextLA).  Same factorisation and
  * the same bits as tqr_dtile_geqrf_dag (each tile strip sees the same
  * operations in the same order; only the order in which CTAs pick up tasks
- * differs: loop order here, longest path first there), but it needs no
+ * differs: a one-step lookahead order written on the device here, longest
+ * path first there), but it needs no
  * `work` argument: for
  * callers that cannot hand the library device memory -- code running while a
  * framework's caching allocator owns the device, host code that must not
@@ -370,6 +371,11 @@ int tqr_stile_gels_dag(int m, int n, int nrhs, int nb, int ib, float *A, int lda
 int tqr_dtile_geqrf_noalloc(int m, int n, int nb, int ib, double *A, int lda, double *T, int ldt,
                             double *tau, int ldtau, cudaStream_t stream);
 int tqr_tile_noalloc_status(int *status, int *task, cudaStream_t stream);
+/* Host replay of tqr_dtile_geqrf_noalloc's task order for a shape: every
+ * dependency is listed before its task and every task appears once.  0 =
+ * consistent (*ntasks the count), -1 = shape outside the kernel, 1-3 = which
+ * check failed. */
+int tqr_tile_noalloc_check(int m, int n, int nb, int ib, long long *ntasks);
 
 /* Tile QR with a binary reduction tree per panel (no counterpart in NextLA;
  * the composition its TT kernels exist for).  Panel k: geqrt! on every tile

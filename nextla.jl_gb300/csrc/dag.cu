@@ -574,6 +574,56 @@ __host__ __device__ inline long long gen_step(const DagGeom &g, int k, DagItem *
   return n;
 }
 
+// Lookahead order for schedules written on the device (no host sort).  Step
+// k's tasks fall into three sections: P(k), the panel and everything the next
+// panel reads (GB/GA, UN of tile column k + 1, the TB/TA blocks, TM of tile
+// column k + 1); C(k), tile column k + 2 (UN, then TM per tile row); R(k),
+// the columns right of that.  The list is P(0), then C(k), P(k + 1), R(k)
+// for k = 0, 1, ...: the next panel's chain is queued before the bulk of the
+// current step's update, one step ahead.  Every task's producers come
+// earlier in the list (tqr_tile_noalloc_check replays it on the host), and
+// inside a section the tasks keep the loop order.  Section q: 0 is P(0); for
+// q >= 1, k = (q - 1) / 3 and (q - 1) % 3 selects C(k), P(k + 1), R(k).
+// Writes the tasks when out is non-null; returns their count.
+__host__ __device__ inline long long gen_section(const DagGeom &g, int q, DagItem *out) {
+  long long n = 0;
+  int k, kind;
+  if (q == 0) { k = 0; kind = 0; }
+  else { k = (q - 1) / 3; kind = (q - 1) % 3 == 0 ? 1 : ((q - 1) % 3 == 1 ? 0 : 2); if (kind == 0) ++k; }
+  if (k >= g.KT) return 0;
+  auto push = [&](uint8_t type, int i, int j, int b, int s) {
+    if (out) {
+      DagItem it;
+      it.type = type; it.b = (uint8_t)b; it.k = (uint16_t)k; it.i = (uint16_t)i; it.j = (uint16_t)j;
+      it.s = (uint16_t)s; it.pad = 0;
+      out[n] = it;
+    }
+    ++n;
+  };
+  // tile columns of this section: P -> k + 1, C -> k + 2, R -> [k + 3, NT)
+  const int j0 = kind == 0 ? k + 1 : (kind == 1 ? k + 2 : k + 3);
+  const int j1 = kind == 2 ? g.NT : min(g.NT, j0 + 1);
+  if (kind == 0)
+    for (int b = 0; b < g.NBK; ++b) {
+      push(IT_GB, k, k, b, 0);
+      for (int s = (b + 1) * g.SPB; s < g.NS; ++s) push(IT_GA, k, k, b, s);
+    }
+  for (int j = j0; j < j1; ++j)
+    for (int s = 0; s < g.strips(j); ++s) push(IT_UN, k, j, 0, s);
+  for (int i = k + 1; i < g.MT; ++i) {
+    if (kind == 0)
+      for (int b = 0; b < g.NBK; ++b) {
+        push(IT_TB, i, k, b, 0);
+        for (int s = (b + 1) * g.SPB; s < g.NS; ++s) push(IT_TA, i, k, b, s);
+      }
+    for (int j = j0; j < j1; ++j)
+      for (int s = 0; s < g.strips(j); ++s) push(IT_TM, i, j, 0, s);
+  }
+  return n;
+}
+
+__host__ __device__ inline int lookahead_sections(const DagGeom &g) { return 1 + 3 * g.KT; }
+
 // Natural (generation) order: the algorithm's own loop order, topological.
 static void gen_items(const DagGeom &g, std::vector<DagItem> &v) {
   long long total = 0;
@@ -808,8 +858,8 @@ static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int
 // a scratch buffer alive between calls.  For them the schedule and its
 // counters live in one file-scope device array of fixed size that every GPU
 // loading this library keeps until exit.  The task list is written on the
-// device (loop order, which is topological), so neither the host nor the
-// device allocates anything per call.
+// device (the lookahead order of gen_section, which is topological), so
+// neither the host nor the device allocates anything per call.
 // ---------------------------------------------------------------------------
 constexpr size_t kStaticScratchBytes = size_t(4) << 20;   // 4 MiB (see tileqr.h)
 static __device__ __align__(256) unsigned char g_tile_scratch[kStaticScratchBytes];
@@ -838,8 +888,8 @@ static cudaError_t static_scratch(void **out) {
   return cudaSuccess;
 }
 
-// Clears the header and counters and writes the task list (CTA k writes step
-// k at its offset).  Everything the DAG kernel expects to start at zero is
+// Clears the header and counters and writes the task list (CTA q writes
+// section q of the lookahead order at its offset).  Everything the DAG kernel expects to start at zero is
 // cleared here on every call, because the array keeps the previous call's
 // contents.
 __global__ void k_static_schedule(DagGeom g, unsigned char *w, size_t bytes_counters, long long key,
@@ -858,10 +908,10 @@ __global__ void k_static_schedule(DagGeom g, unsigned char *w, size_t bytes_coun
       h->t_first = ~0ull;
     }
   }
-  if (threadIdx.x == 0 && (int)blockIdx.x < g.KT) {
+  if (threadIdx.x == 0 && (int)blockIdx.x < lookahead_sections(g)) {
     long long off = 0;
-    for (int k = 0; k < (int)blockIdx.x; ++k) off += step_tasks(g, k);
-    gen_step(g, blockIdx.x, reinterpret_cast<DagItem *>(w + 256 + bytes_counters) + off);
+    for (int q = 0; q < (int)blockIdx.x; ++q) off += gen_section(g, q, nullptr);
+    gen_section(g, blockIdx.x, reinterpret_cast<DagItem *>(w + 256 + bytes_counters) + off);
   }
 }
 
@@ -887,7 +937,7 @@ static int tile_geqrf_noalloc(int m, int n, int nb, int ib, double *A, int lda, 
   if (e != cudaSuccess) return (int)e;
   unsigned char *w = static_cast<unsigned char *>(wv);
   const long long key = geom_key(g);
-  k_static_schedule<<<std::max(g.KT, 1), TQR_THREADS, 0, st>>>(g, w, bytes_counters, key, (int)nitems);
+  k_static_schedule<<<lookahead_sections(g), TQR_THREADS, 0, st>>>(g, w, bytes_counters, key, (int)nitems);
   count_launch();
   if ((e = cudaGetLastError()) != cudaSuccess) return (int)e;
   DagArgs<double> a;
@@ -1046,6 +1096,39 @@ int tqr_dtile_geqrf_noalloc(int m, int n, int nb, int ib, double *A, int lda, do
 // header sits at the start of the static array, which no caller can address,
 // so this reads it for them (a copy from the symbol, then a stream
 // synchronisation; nothing is allocated).
+int tqr_tile_noalloc_check(int m, int n, int nb, int ib, long long *ntasks) {
+  // Host replay of the allocation-free schedule's order: every wait target of
+  // every task is reached by the writers listed before it, and the list holds
+  // each task of the loop order exactly once.
+  DagGeom g;
+  if (!dag_geom(m, n, nb, ib, &g)) return -1;
+  std::vector<DagItem> v;
+  for (int q = 0; q < lookahead_sections(g); ++q) {
+    const size_t off = v.size();
+    v.resize(off + (size_t)gen_section(g, q, nullptr));
+    gen_section(g, q, v.data() + off);
+  }
+  long long nat = 0;
+  for (int k = 0; k < g.KT; ++k) nat += step_tasks(g, k);
+  if ((long long)v.size() != nat) return 1;
+  std::vector<int> seen(g.ncounters(), 0);
+  int c[kMaxDeps], t[kMaxDeps];
+  for (const DagItem &it : v) {
+    const int nd = item_deps(g, it, c, t);
+    for (int d = 0; d < nd; ++d)
+      if (seen[c[d]] < t[d]) return 2;
+    const int nu = item_updates(g, it, c);
+    for (int u = 0; u < nu; ++u) ++seen[c[u]];
+  }
+  for (int k = 0; k < g.KT; ++k) {
+    if (seen[g.done_g(k)] != g.panel_tasks()) return 3;
+    for (int i = k + 1; i < g.MT; ++i)
+      if (seen[g.done_t(k, i)] != g.panel_tasks()) return 3;
+  }
+  if (ntasks) *ntasks = (long long)v.size();
+  return 0;
+}
+
 int tqr_tile_noalloc_status(int *status, int *task, cudaStream_t stream) {
   void *wv = nullptr;
   cudaError_t e = static_scratch(&wv);

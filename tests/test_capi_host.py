@@ -293,3 +293,20 @@ def test_tree_task_graph_with_8_column_strips(L, m, n, nb, ib, grp, nrhs):
     assert L.tqr_tile_hqr_dag_check_strips(m, n, nb, ib, grp, nrhs, 16, ctypes.byref(n16)) == 0
     assert n8.value > n16.value
     assert L.tqr_tile_hqr_dag_check_strips(m, n, nb, 20, grp, nrhs, 8, ctypes.byref(n8)) == -1   # ib % 8
+
+
+@pytest.mark.parametrize("shape", [(1024, 1024, 256, 32), (2048, 1024, 256, 32), (1024, 2048, 256, 32),
+                                   (512, 512, 128, 32), (768, 512, 128, 16), (256, 256, 256, 32),
+                                   (1024, 1024, 256, 64), (4096, 4096, 256, 32), (8192, 8192, 256, 32),
+                                   (65536, 512, 256, 32), (512, 4096, 256, 32)])
+def test_noalloc_lookahead_order_replays(L, shape):
+    """The allocation-free tile QR's device-written task order (the next
+    panel's tasks queued one step ahead of the bulk of the current update):
+    every dependency listed before its task, every task of the loop order
+    exactly once."""
+    nt = ctypes.c_longlong(0)
+    assert L.tqr_tile_noalloc_check(*shape, ctypes.byref(nt)) == 0
+    import tileqr
+    rc, ntasks = tileqr.dag_check(*shape)
+    assert rc == 0 and nt.value == ntasks
+    assert L.tqr_tile_noalloc_check(1000, 1000, 256, 32, ctypes.byref(nt)) == -1
