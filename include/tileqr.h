@@ -636,6 +636,17 @@ int tqr_dbatched_gels(int nprob, const void *problems, const int *order, double 
                       size_t lwork, cudaStream_t stream);
 int tqr_sbatched_gels(int nprob, const void *problems, const int *order, float *A, float *B, void *work,
                       size_t lwork, cudaStream_t stream);
+/* ComplexF64 (z) and ComplexF32 (c) batches: the same solve with the complex
+ * geqrt!/unmqr!('L','C') arithmetic and LeftUpperTRSM!'s complex divisions
+ * (Smith's method, as the tile back-solve), on A and B of tqr_zcomplex /
+ * tqr_ccomplex elements.  Plan with dtype_bytes 16 (ComplexF64: 8-column
+ * strips) or 8 (ComplexF32, the FP64 table); tqr_batched_worksize(16) covers
+ * ComplexF64 and tqr_batched_worksize(8) both FP64 and ComplexF32.  The
+ * autotuner, the residual kernel and the graph capture are real-only. */
+int tqr_zbatched_gels(int nprob, const void *problems, const int *order, tqr_zcomplex *A, tqr_zcomplex *B,
+                      void *work, size_t lwork, cudaStream_t stream);
+int tqr_cbatched_gels(int nprob, const void *problems, const int *order, tqr_ccomplex *A, tqr_ccomplex *B,
+                      void *work, size_t lwork, cudaStream_t stream);
 int tqr_batched_status(const void *work, int *bad, int *first_bad, cudaStream_t stream);
 int tqr_dbatched_residual(int nprob, const void *problems, const double *A0, const double *B0,
                           const double *X, double *res, cudaStream_t stream);

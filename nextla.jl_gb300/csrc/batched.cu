@@ -26,6 +26,7 @@
 #include <cstring>
 #include <mutex>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "apply_dev.cuh"
@@ -116,13 +117,13 @@ __device__ void solve_one(const BatchProblem &p, R *Abase, R *Bbase, R *Tscr, R 
   __syncthreads();
   for (int idx = threadIdx.x; idx < n * k; idx += TQR_THREADS) {
     const int r = idx % n, c = idx / n;
-    xs[r + (size_t)c * n] = B[ix(r, c, ldb)] / dg[r];
+    xs[r + (size_t)c * n] = div_(B[ix(r, c, ldb)], dg[r]);
   }
   __syncthreads();
   for (int i = n - 1; i > 0; --i) {
     for (int idx = threadIdx.x; idx < i * k; idx += TQR_THREADS) {
       const int r = idx % i, c = idx / i;
-      xs[r + (size_t)c * n] -= (A[ix(r, i, lda)] / dg[r]) * xs[i + (size_t)c * n];
+      xs[r + (size_t)c * n] -= div_(A[ix(r, i, lda)], dg[r]) * xs[i + (size_t)c * n];
     }
     __syncthreads();
   }
@@ -177,7 +178,12 @@ struct LaunchCfg {
   cudaError_t err = cudaSuccess;
 };
 static std::mutex g_cfg_mu;
-static LaunchCfg g_cfg[2][64];
+static LaunchCfg g_cfg[4][64];
+
+// Launch-shape slot of an element type: double, float, ComplexF64, ComplexF32.
+template <typename R> constexpr int cfg_slot() {
+  return std::is_same<R, double>::value ? 0 : std::is_same<R, float>::value ? 1 : std::is_same<R, cx<double>>::value ? 2 : 3;
+}
 
 template <typename R>
 static LaunchCfg launch_cfg() {
@@ -186,7 +192,7 @@ static LaunchCfg launch_cfg() {
   if ((c.err = cudaGetDevice(&dev)) != cudaSuccess) return c;
   if (dev >= 64) { c.err = cudaErrorInvalidDevice; return c; }
   std::lock_guard<std::mutex> l(g_cfg_mu);
-  LaunchCfg &g = g_cfg[sizeof(R) == 4][dev];
+  LaunchCfg &g = g_cfg[cfg_slot<R>()][dev];
   if (g.grid > 0) return g;
   int sms = 0, per_sm = 0;
   if ((c.err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return c;
@@ -421,7 +427,7 @@ int tqr_batched_problem_bytes(void) { return (int)sizeof(BatchProblem); }
 
 int tqr_batched_plan(int dtype_bytes, int nprob, const int *m, const int *n, const int *k, void *problems,
                      int *order, long long *a_elems, long long *b_elems) {
-  if (dtype_bytes != 4 && dtype_bytes != 8) return -1;
+  if (dtype_bytes != 4 && dtype_bytes != 8 && dtype_bytes != 16) return -1;
   if (nprob < 0) return -2;
   if (nprob > 0 && (!m || !n || !k || !problems || !order)) return -3;
   if (!a_elems || !b_elems) return -9;
@@ -434,7 +440,7 @@ int tqr_batched_plan(int dtype_bytes, int nprob, const int *m, const int *n, con
     p.m = m[q]; p.n = n[q]; p.k = k[q];
     const Tune t = g_table[isf][class_of(p.n)];
     p.ib = std::min(t.ib, std::max(p.n, 1));
-    p.nw = t.nw;
+    p.nw = dtype_bytes == 16 ? 8 : t.nw;   // ComplexF64: 8-column strips (16-byte elements)
     p.pad = 0;
     p.a_off = ao; p.b_off = bo;
     if (!problem_ok(p)) return -(1000 + q);           // problem q out of range
@@ -455,11 +461,22 @@ int tqr_batched_plan(int dtype_bytes, int nprob, const int *m, const int *n, con
 }
 
 int tqr_batched_worksize(int dtype_bytes, size_t *bytes) {
-  if (dtype_bytes != 4 && dtype_bytes != 8) return -1;
+  if (dtype_bytes != 4 && dtype_bytes != 8 && dtype_bytes != 16) return -1;
   if (!bytes) return -2;
+  if (dtype_bytes == 16) {
+    LaunchCfg c = launch_cfg<cx<double>>();
+    if (c.err != cudaSuccess) return (int)c.err;
+    *bytes = work_bytes<cx<double>>(c.grid);
+    return 0;
+  }
   LaunchCfg c = dtype_bytes == 4 ? launch_cfg<float>() : launch_cfg<double>();
   if (c.err != cudaSuccess) return (int)c.err;
   *bytes = dtype_bytes == 4 ? work_bytes<float>(c.grid) : work_bytes<double>(c.grid);
+  if (dtype_bytes == 8) {   // also covers ComplexF32 (8-byte elements)
+    LaunchCfg cc = launch_cfg<cx<float>>();
+    if (cc.err != cudaSuccess) return (int)cc.err;
+    *bytes = std::max(*bytes, work_bytes<cx<float>>(cc.grid));
+  }
   return 0;
 }
 
@@ -486,6 +503,18 @@ int tqr_dbatched_gels(int nprob, const void *problems, const int *order, double 
 int tqr_sbatched_gels(int nprob, const void *problems, const int *order, float *A, float *B, void *work,
                       size_t lwork, cudaStream_t stream) {
   return batched_launch<float>(nprob, problems, order, A, B, work, lwork, stream);
+}
+
+int tqr_zbatched_gels(int nprob, const void *problems, const int *order, tqr_zcomplex *A, tqr_zcomplex *B,
+                      void *work, size_t lwork, cudaStream_t stream) {
+  if (((uintptr_t)A | (uintptr_t)B) % alignof(cx<double>)) return -4;
+  return batched_launch<cx<double>>(nprob, problems, order, (cx<double> *)A, (cx<double> *)B, work, lwork, stream);
+}
+
+int tqr_cbatched_gels(int nprob, const void *problems, const int *order, tqr_ccomplex *A, tqr_ccomplex *B,
+                      void *work, size_t lwork, cudaStream_t stream) {
+  if (((uintptr_t)A | (uintptr_t)B) % alignof(cx<float>)) return -4;
+  return batched_launch<cx<float>>(nprob, problems, order, (cx<float> *)A, (cx<float> *)B, work, lwork, stream);
 }
 
 int tqr_batched_status(const void *work, int *bad, int *first_bad, cudaStream_t stream) {

@@ -122,6 +122,21 @@ __device__ __forceinline__ double abs2_add(double v, double s) { return fma(v, v
 __device__ __forceinline__ float abs2_add(float v, float s) { return fmaf(v, v, s); }
 template <typename R> __device__ __forceinline__ R abs2_add(cx<R> v, R s) { return fma(v.x, v.x, fma(v.y, v.y, s)); }
 
+// a / b: the division itself for real elements; for complex elements Smith's
+// algorithm (R. L. Smith, "Algorithm 116: Complex division", CACM 5(8), 1962),
+// which scales by the larger part of b so |b|^2 is never formed.
+__device__ __forceinline__ double div_(double a, double b) { return a / b; }
+__device__ __forceinline__ float div_(float a, float b) { return a / b; }
+template <typename R>
+__device__ __forceinline__ cx<R> div_(cx<R> a, cx<R> b) {
+  if (fabs(b.x) >= fabs(b.y)) {
+    const R r = b.y / b.x, d = b.x + b.y * r;
+    return cx<R>((a.x + a.y * r) / d, (a.y - a.x * r) / d);
+  }
+  const R r = b.x / b.y, d = b.y + b.x * r;
+  return cx<R>((a.x * r + a.y) / d, (a.y * r - a.x) / d);
+}
+
 template <typename R>
 __device__ inline cx<R> warp_sum(cx<R> v) {
   return cx<R>(warp_sum(v.x), warp_sum(v.y));

@@ -202,20 +202,6 @@ int tile_unmqr(char trans, int m, int n, int nrhs, int nb, int ib, const R *A, i
 // diagonal, then b[r] -= (R[r,i] / R[r,r]) b[i]); the rows above are updated
 // with C -= R_blk X_blk.  No size limit (the reference kernel stops at 1024).
 // ---------------------------------------------------------------------------
-// a / b: the division itself for real elements; for complex elements Smith's
-// algorithm (R. L. Smith, "Algorithm 116: Complex division", CACM 5(8), 1962),
-// which scales by the larger part of b so |b|^2 is never formed.
-__device__ __forceinline__ double div_(double a, double b) { return a / b; }
-__device__ __forceinline__ float div_(float a, float b) { return a / b; }
-template <typename R>
-__device__ __forceinline__ cx<R> div_(cx<R> a, cx<R> b) {
-  if (fabs(b.x) >= fabs(b.y)) {
-    const R r = b.y / b.x, d = b.x + b.y * r;
-    return cx<R>((a.x + a.y * r) / d, (a.y - a.x * r) / d);
-  }
-  const R r = b.x / b.y, d = b.y + b.x * r;
-  return cx<R>((a.x * r + a.y) / d, (a.y * r - a.x) / d);
-}
 
 template <typename R>
 __global__ void __launch_bounds__(TQR_THREADS)

@@ -97,6 +97,8 @@ DIAG = {
     "tqr_dbatched_gels": ([_I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
     "tqr_sbatched_gels": ([_I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
     "tqr_batched_status": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I), _P], _I),
+    "tqr_zbatched_gels": ([_I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
+    "tqr_cbatched_gels": ([_I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
     "tqr_dbatched_residual": ([_I, _P, _P, _P, _P, _P, _P], _I),
     "tqr_sbatched_residual": ([_I, _P, _P, _P, _P, _P, _P], _I),
     "tqr_batched_graph": ([_I, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, ctypes.POINTER(_P)], _I),

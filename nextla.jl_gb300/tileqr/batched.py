@@ -35,16 +35,25 @@ def _check(rc, what):
 
 
 def _nbytes(dtype):
-    if dtype == torch.float64:
+    if dtype in (torch.float64, torch.complex64):
         return 8
     if dtype == torch.float32:
         return 4
+    if dtype == torch.complex128:
+        return 16
     raise TypeError(f"unsupported element type {dtype}")
+
+
+_PREFIX = {torch.float64: "d", torch.float32: "s", torch.complex128: "z", torch.complex64: "c"}
 
 
 def autotune(dtype=torch.float64, force=False):
     """Time every (ib, strip width) candidate per column-count class and keep
-    the fastest (allocates; run before planning, outside graph capture)."""
+    the fastest (allocates; run before planning, outside graph capture).
+    Real types only; complex batches plan with the table of their real
+    precision."""
+    if dtype.is_complex:
+        raise TypeError("the batched autotuner times real batches only")
     nb = _nbytes(dtype)
     st = torch.cuda.current_stream()
     _check(_lib.lib().tqr_batched_autotune(nb, 1 if force else 0, st.cuda_stream), "batched_autotune")
@@ -95,7 +104,7 @@ class BatchedGels:
         self.dtype = dtype
         self.device = torch.device(device)
         nb = _nbytes(dtype)
-        if tune and nb not in _TUNED:
+        if tune and not dtype.is_complex and nb not in _TUNED:
             autotune(dtype)
         self.desc, self.order, a_elems, b_elems = plan(ms, ns, ks, dtype)
         self.nprob = len(self.desc)
@@ -135,7 +144,7 @@ class BatchedGels:
 
     # -- solve ----------------------------------------------------------------
     def _fn(self):
-        return getattr(_lib.lib(), f"tqr_{'d' if self.dtype == torch.float64 else 's'}batched_gels")
+        return getattr(_lib.lib(), f"tqr_{_PREFIX[self.dtype]}batched_gels")
 
     def run(self, stream=None, sync=True):
         st = stream or torch.cuda.current_stream()
@@ -148,7 +157,10 @@ class BatchedGels:
             st.synchronize()
 
     def capture(self):
-        """Instantiate a CUDA graph of the launch (counter reset + solve)."""
+        """Instantiate a CUDA graph of the launch (counter reset + solve); real
+        batches."""
+        if self.dtype.is_complex:
+            raise TypeError("graph capture of a batch is available for real element types")
         if self._graph is None:
             ex = ctypes.c_void_p(0)
             rc = _lib.lib().tqr_batched_graph(_nbytes(self.dtype), self.nprob,
@@ -181,8 +193,10 @@ class BatchedGels:
     def residuals(self, A0, B0):
         """Per-problem ||A^T (B - A X)|| / (||A|| (||A|| ||X|| + ||B||)) (float64
         tensor) from the original packed A0, B0 and the current solution."""
+        if self.dtype.is_complex:
+            raise TypeError("the residual kernel is available for real element types")
         res = torch.empty(self.nprob, dtype=torch.float64, device=self.device)
-        fn = getattr(_lib.lib(), f"tqr_{'d' if self.dtype == torch.float64 else 's'}batched_residual")
+        fn = getattr(_lib.lib(), f"tqr_{_PREFIX[self.dtype]}batched_residual")
         st = torch.cuda.current_stream()
         _check(fn(self.nprob, ctypes.c_void_p(self.d_desc.data_ptr()), ctypes.c_void_p(A0.data_ptr()),
                   ctypes.c_void_p(B0.data_ptr()), ctypes.c_void_p(self.B.data_ptr()),

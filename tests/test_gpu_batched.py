@@ -179,3 +179,63 @@ def test_sharded_batch_one_rank(tq):
     r = bench.batched_sharded_bench(torch, 512, 1, 0, steps=1, warmup=1)
     assert r["rank0_problems"] == 512 and abs(r["rank0_cost_share"] - 1.0) < 1e-12
     assert r["rejected_descriptors_rank0"] == 0 and r["problems_per_s"] > 0
+
+
+def zoracle_solve(oracle, A, B, ib):
+    A = np.array(A, order="F", dtype=np.complex128)
+    B = np.array(B, order="F", dtype=np.complex128)
+    m, n = A.shape
+    nb = max(m, n)
+    T, _ = oracle.tile_geqrf(A, nb, ib)
+    X = None
+    if B.shape[1] > 0:
+        oracle.tile_unmqr("C", A, T, B, nb, ib)
+        X = np.array(B[:n], order="F")
+        oracle.trsm_lun(A[:n, :n], X)
+    return A, X
+
+
+@pytest.mark.parametrize("dtype_name", ["complex128", "complex64"])
+def test_complex_batched_matches_oracle(tq, oracle, dtype_name):
+    """ComplexF64 / ComplexF32 batches (the reference's kernels run both,
+    test/lapack_helpers.jl:11): every problem's factored A and its solution
+    against the complex oracle's single-tile path (zgeqrt!, unmqr!('L','C'),
+    LeftUpperTRSM! with Smith's division) on the same inputs, and the
+    normal-equation residual ||A^H (B - A X)|| / (||A|| (||A|| ||X|| + ||B||))."""
+    import torch
+    from tileqr import batched as Bt
+    dt = getattr(torch, dtype_name)
+    ms, ns, ks = sizes_with_edges(30, seed=13)
+    bg = Bt.BatchedGels(ms, ns, ks, dtype=dt, tune=True)
+    g = torch.Generator(device="cuda").manual_seed(9)
+    cre = lambda n: torch.complex(torch.randn(n, generator=g, device="cuda", dtype=torch.float64),
+                                  torch.randn(n, generator=g, device="cuda", dtype=torch.float64))
+    bg.A.copy_(cre(bg.A.shape[0]))
+    bg.B.copy_(cre(bg.B.shape[0]))
+    A0h = bg.A.to(torch.complex128).cpu().numpy()
+    B0h = bg.B.to(torch.complex128).cpu().numpy()
+    bg.run()
+    assert bg.status() == (0, -1)
+    Ah = bg.A.to(torch.complex128).cpu().numpy()
+    Bh = bg.B.to(torch.complex128).cpu().numpy()
+    r_tol, x_unit = (1e-12, 1e-15) if dt == torch.complex128 else (1e-5, 1e-6)
+    worst = 0.0
+    for q in range(bg.nprob):
+        d = bg.desc[q]
+        m, n, k, ib = int(d["m"]), int(d["n"]), int(d["k"]), int(d["ib"])
+        ao, bo = int(d["a_off"]), int(d["b_off"])
+        Aq = A0h[ao:ao + m * n].reshape(n, m).T
+        Bq = B0h[bo:bo + m * k].reshape(k, m).T
+        Af, X = zoracle_solve(oracle, Aq, Bq, ib)
+        Ag = Ah[ao:ao + m * n].reshape(n, m).T
+        rd = np.linalg.norm(Ag - Af) / max(np.linalg.norm(Af), 1e-300)
+        assert rd <= r_tol * max(n, 1), (q, m, n, k, ib, rd)
+        if k > 0:
+            Xg = Bh[bo:bo + m * k].reshape(k, m).T[:n]
+            kappa = np.linalg.cond(Aq)
+            xd = np.linalg.norm(Xg - X) / max(np.linalg.norm(X), 1e-300)
+            assert xd <= max(x_unit * kappa * n, 1e3 * x_unit), (q, m, n, k, xd, kappa)
+            r = Bq - Aq @ Xg
+            na = np.linalg.norm(Aq)
+            worst = max(worst, np.linalg.norm(Aq.conj().T @ r) / (na * (na * np.linalg.norm(Xg) + np.linalg.norm(Bq))))
+    assert worst < (1e-14 if dt == torch.complex128 else 1e-5), worst
