@@ -46,7 +46,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--kernel", default=None,
                    choices=["tsmqr", "tsmqr_tc", "tsmqr_wy", "tsqrt", "geqrt", "tile", "tile_f64p", "hqr",
-                            "hqr_square", "larft", "trsm"],
+                            "hqr_square", "batched", "larft", "trsm"],
                    help="time one tile kernel alone (for profiling) instead of the workload")
     p.add_argument("--dtype", default="f64", choices=["f64", "f32", "c64", "c128"],
                    help="element type for --kernel (complex: tile only)")
@@ -129,16 +129,44 @@ def kernel_bench(args):
         fl = 2.0 * n * 512 ** 2 - 2.0 * 512 ** 3 / 3
     elif args.kernel == "hqr_square":
         # the n x n tile QR on the hierarchical tree (groups of --grp tiles,
-        # the leaders by the binary tree), one persistent launch
-        dt = torch.float32 if args.dtype == "f32" else torch.float64
+        # the leaders by the binary tree), one persistent launch (complex:
+        # 4 real flops per complex one)
+        dt = {"f32": torch.float32, "f64": torch.float64, "c64": torch.complex64,
+              "c128": torch.complex128}[args.dtype]
         A0 = tq.empty(n, n, dtype=dt)
-        A0.copy_(torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda"))
+        if dt.is_complex:
+            A0.copy_(torch.complex(torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda"),
+                                   torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda")))
+        else:
+            A0.copy_(torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda"))
         A = tq.empty(n, n, dtype=dt)
 
         def run():
             A.copy_(A0)
             tq.tile_geqrf_tree(A, NB, IB, dag=True, grp=args.grp)
-        fl = flops_square(n)
+        fl = flops_square(n) * (4 if dt.is_complex else 1)
+    elif args.kernel == "batched":
+        # one launch of the batched uneven QR + solve over --batched-n seeded
+        # problems (m ~ U[32,512], n ~ U[16,m], k ~ U[1,8]) in the chosen type
+        from tileqr import batched as Bt
+        dt = {"f32": torch.float32, "f64": torch.float64, "c64": torch.complex64,
+              "c128": torch.complex128}[args.dtype]
+        ms, ns, ks = Bt.random_sizes(args.batched_n, seed=SEED)
+        bg = Bt.BatchedGels(ms, ns, ks, dtype=dt, tune=not dt.is_complex)
+        if dt.is_complex:
+            A0 = torch.complex(torch.randn(bg.A.shape, generator=g, dtype=torch.float64, device="cuda"),
+                               torch.randn(bg.A.shape, generator=g, dtype=torch.float64, device="cuda")).to(dt)
+            B0 = torch.complex(torch.randn(bg.B.shape, generator=g, dtype=torch.float64, device="cuda"),
+                               torch.randn(bg.B.shape, generator=g, dtype=torch.float64, device="cuda")).to(dt)
+        else:
+            A0 = torch.randn(bg.A.shape, generator=g, dtype=torch.float64, device="cuda").to(dt)
+            B0 = torch.randn(bg.B.shape, generator=g, dtype=torch.float64, device="cuda").to(dt)
+
+        def run():
+            bg.A.copy_(A0)
+            bg.B.copy_(B0)
+            bg.run(sync=False)
+        fl = bg.flops() * (4 if dt.is_complex else 1)
     elif args.kernel == "larft":
         # stand-alone larft!('F', 'C') on an n x 32 block of reflectors
         dt = torch.float32 if args.dtype == "f32" else torch.float64
