@@ -677,6 +677,25 @@ int tqr_batched_graph_destroy(void *graph_exec);
  * scratch), shared by both passes.  Argument errors: -1 batch, -2 m, -3 n,
  * -4 ib, -5.. pointers, -8 work too small. */
 int tqr_qr_batched_worksize(int dtype_bytes, int m, int n, int ib, size_t *bytes);
+/* ComplexF64 (z) and ComplexF32 (c) forms of the forward and the adjoint:
+ * the complex tile QR (R's diagonal real, the Householder beta) and
+ *   Abar = (Qbar + Q X) R^-H,  X = tril(M,-1) + tril(M,-1)^H + Re diag(M),
+ *   M = R Rbar^H - Qbar^H Q,
+ * the gradient of a real loss as dL/dRe(A) + i dL/dIm(A).  The backward needs
+ * m > n (-2 otherwise): with m == n the last column has one row, keeps tau = 0
+ * (src/geqr2.jl:32-35) and a complex R_nn, outside that formula.  Work:
+ * tqr_qr_batched_worksize with dtype_bytes 16 (ComplexF64) or 8 (covers FP64
+ * and ComplexF32).  Element pointers aligned to the element size. */
+int tqr_zqr_batched_fwd(int batch, int m, int n, int ib, tqr_zcomplex *F, tqr_zcomplex *tau, tqr_zcomplex *Q,
+                        tqr_zcomplex *R, void *work, size_t lwork, cudaStream_t stream);
+int tqr_cqr_batched_fwd(int batch, int m, int n, int ib, tqr_ccomplex *F, tqr_ccomplex *tau, tqr_ccomplex *Q,
+                        tqr_ccomplex *R, void *work, size_t lwork, cudaStream_t stream);
+int tqr_zqr_batched_bwd(int batch, int m, int n, int ib, const tqr_zcomplex *F, const tqr_zcomplex *tau,
+                        const tqr_zcomplex *Qbar, const tqr_zcomplex *Rbar, tqr_zcomplex *Abar, void *work,
+                        size_t lwork, cudaStream_t stream);
+int tqr_cqr_batched_bwd(int batch, int m, int n, int ib, const tqr_ccomplex *F, const tqr_ccomplex *tau,
+                        const tqr_ccomplex *Qbar, const tqr_ccomplex *Rbar, tqr_ccomplex *Abar, void *work,
+                        size_t lwork, cudaStream_t stream);
 int tqr_dqr_batched_fwd(int batch, int m, int n, int ib, double *F, double *tau, double *Q, double *R,
                         void *work, size_t lwork, cudaStream_t stream);
 int tqr_sqr_batched_fwd(int batch, int m, int n, int ib, float *F, float *tau, float *Q, float *R,

@@ -22,9 +22,21 @@
 //           Q^T Qbar and Q copyltu(M) applied through the block reflectors
 //           and R^-T by an in-place triangular solve.  The formula holds for
 //           any diagonal sign convention of R as long as Q and R agree.
+// Complex elements (ComplexF64, ComplexF32), gradients in the convention
+// Abar = dL/dRe(A) + i dL/dIm(A) for a real loss L (torch's): transposes
+// become conjugate transposes, M = R Rbar^H - Qbar^H Q and
+//             Abar = (Qbar + Q X) R^-H,   X = tril(M,-1) + tril(M,-1)^H + Re diag(M).
+// The real part of M's diagonal alone enters because R's diagonal is real
+// (the Householder beta): Q^H dQ is skew-Hermitian with the purely imaginary
+// diagonal i Im diag(Q^H dA R^-1), which the Re-diagonal term is the adjoint
+// of.  That needs a reflector below every column, m > n (for m == n the last
+// column keeps tau = 0 and a complex R_nn, src/geqr2.jl:32-35); the complex
+// backward rejects m == n.  Checked against central differences in the real
+// and the imaginary direction of every entry.
 #include <algorithm>
 #include <cmath>
 #include <mutex>
+#include <type_traits>
 
 #include "apply_dev.cuh"
 #include "panel_dev.cuh"
@@ -34,9 +46,20 @@
 namespace tqr {
 
 constexpr int kAdjNb = 256;                 // tile rows
-constexpr int kAdjNW = 16;                  // trailing-update strip width
+constexpr int kAdjNW = 16;                  // trailing-update strip width (8 for ComplexF64)
 constexpr int kAdjMaxIb = 32;
-constexpr size_t kAdjSmem = 110976;         // two CTAs per SM
+constexpr size_t kAdjSmem = 110976;         // two CTAs per SM (ComplexF64: one, adj_smem)
+
+template <typename R> struct AdjNW { static constexpr int value = kAdjNW; };
+template <> struct AdjNW<cx<double>> { static constexpr int value = 8; };
+
+// Dynamic shared memory of the forward and adjoint kernels for element type R:
+// the staged panel, tsqrt block and strip apply at 256 rows, ib = 32.
+template <typename R>
+static size_t adj_smem() {
+  return std::max({kAdjSmem, panel_smem<R>(256, 32, true, true), tsqrt_smem<R>(256, 32, true),
+                   apply_smem_elems(256, 32, AdjNW<R>::value, true, true, true) * sizeof(R)});
+}
 
 struct AdjGeom {
   int m, n, ib, MT;
@@ -72,8 +95,8 @@ struct AdjArgs {
 // Columns [c0, ncols) of an apply, strip by strip.
 template <typename R>
 __device__ void apply_cols(ApplyArgs<R> a, int c0, unsigned char *smem) {
-  for (int c = c0; c < a.ncols; c += kAdjNW) {
-    apply_strip<R, kAdjNW>(a, c, smem);
+  for (int c = c0; c < a.ncols; c += AdjNW<R>::value) {
+    apply_strip<R, AdjNW<R>::value>(a, c, smem);
     __syncthreads();
   }
 }
@@ -83,7 +106,7 @@ __device__ ApplyArgs<R> base_args(int ib) {
   ApplyArgs<R> a;
   a.ib = ib; a.fwd = 1; a.transT = 1;
   a.c_rs = 1; a.a_rs = 1;
-  a.nw = kAdjNW;
+  a.nw = AdjNW<R>::value;
   a.stage_c = 1; a.stage_v = 1; a.stage_t = 1;
   a.A1 = nullptr; a.a_cs = 1;
   return a;
@@ -171,13 +194,13 @@ __device__ void larft_block(int L, int sb, const R *V, int ldv, const R *tau, bo
   const int tid = threadIdx.x;
   for (int idx = tid; idx < sb * sb; idx += TQR_THREADS) {
     const int p = idx % sb, j = idx / sb;
-    R s = 0;
-    if (p < j) {
+    R s = R(0);
+    if (p < j) {   // G = V^H V (complex: the left factor conjugated, src/larft.jl:71-84)
       if (unit) {
-        s = V[ix(j, p, ldv)];
-        for (int r = j + 1; r < L; ++r) s = fma(V[ix(r, p, ldv)], V[ix(r, j, ldv)], s);
+        s = conj_(V[ix(j, p, ldv)]);
+        for (int r = j + 1; r < L; ++r) s = madc(V[ix(r, p, ldv)], V[ix(r, j, ldv)], s);
       } else {
-        for (int r = 0; r < L; ++r) s = fma(V[ix(r, p, ldv)], V[ix(r, j, ldv)], s);
+        for (int r = 0; r < L; ++r) s = madc(V[ix(r, p, ldv)], V[ix(r, j, ldv)], s);
       }
     }
     G[p + 33 * j] = s;
@@ -186,8 +209,8 @@ __device__ void larft_block(int L, int sb, const R *V, int ldv, const R *tau, bo
   for (int j = 0; j < sb; ++j) {
     const R tj = tau[j];
     if (tid < j) {
-      R s = 0;
-      for (int q = tid; q < j; ++q) s = fma(Ts[tid + 33 * q], G[q + 33 * j], s);
+      R s = R(0);
+      for (int q = tid; q < j; ++q) s = mad(Ts[tid + 33 * q], G[q + 33 * j], s);
       Ts[tid + 33 * j] = -tj * s;
     } else if (tid == j) {
       Ts[j + 33 * j] = tj;
@@ -218,25 +241,30 @@ __device__ void recompute_t(const AdjGeom &g, const R *F, const R *tau, R *Tw, u
   }
 }
 
-// X R^T = Y in place for one row tile (X overwrites Y, rows x n, ldy), R
-// n x n upper (ldr): column blocks of kSolveBw from the right; each thread
-// owns one row and keeps the block's entries in registers.
+// X R^T = Y (complex: X R^H = Y) in place for one row tile (X overwrites Y,
+// rows x n, ldy), R n x n upper (ldr): column blocks of SolveBw from the
+// right; each thread owns one row and keeps the block's entries in registers.
 constexpr int kSolveBw = 32;
+template <typename R> struct SolveBw { static constexpr int value = sizeof(R) == 16 ? 16 : kSolveBw; };
 
 template <typename R>
 __device__ void solve_rt(int rows, int n, const R *Rm, int ldr, R *Y, int ldy, unsigned char *smem) {
-  constexpr int BW = kSolveBw;
+  constexpr int BW = SolveBw<R>::value;
   R *Rs = reinterpret_cast<R *>(smem);          // (n - j0) x BW: Rs[(k - j0) * BW + c] = R[j0 + c, k]
   R *rinv = Rs + (size_t)kAdjNb * BW;           // BW
   const int tid = threadIdx.x;
   for (int j0 = ((n - 1) / BW) * BW; j0 >= 0; j0 -= BW) {
     const int jb = min(BW, n - j0);
     const int kn = n - j0;
-    for (int idx = tid; idx < kn * BW; idx += TQR_THREADS) {
+    // rows kk < BW are read by the in-block sweep even past kn (a partial
+    // first block, jb < BW): zero them so 0 * (stale shared memory) never
+    // turns into NaN
+    for (int idx = tid; idx < max(kn, BW) * BW; idx += TQR_THREADS) {
       const int kk = idx / BW, c = idx % BW;
-      Rs[idx] = (c < jb && c <= kk) ? Rm[ix(j0 + c, j0 + kk, ldr)] : R(0);
+      Rs[idx] = (kk < kn && c < jb && c <= kk) ? conj_(Rm[ix(j0 + c, j0 + kk, ldr)]) : R(0);
     }
-    for (int c = tid; c < BW; c += TQR_THREADS) rinv[c] = (c < jb) ? R(1) / Rm[ix(j0 + c, j0 + c, ldr)] : R(0);
+    for (int c = tid; c < BW; c += TQR_THREADS)
+      rinv[c] = (c < jb) ? div_(R(1), conj_(Rm[ix(j0 + c, j0 + c, ldr)])) : R(0);
     __syncthreads();
     for (int r = tid; r < rows; r += TQR_THREADS) {
       R acc[BW];
@@ -246,7 +274,7 @@ __device__ void solve_rt(int rows, int n, const R *Rm, int ldr, R *Y, int ldy, u
         const R x = Y[ix(r, j0 + kk, ldy)];
         const R *rk = Rs + (size_t)kk * BW;
 #pragma unroll
-        for (int c = 0; c < BW; ++c) acc[c] = fma(-x, rk[c], acc[c]);
+        for (int c = 0; c < BW; ++c) acc[c] = mad(-x, rk[c], acc[c]);
       }
 #pragma unroll
       for (int c = BW - 1; c >= 0; --c) {
@@ -254,7 +282,7 @@ __device__ void solve_rt(int rows, int n, const R *Rm, int ldr, R *Y, int ldy, u
         acc[c] = xc;
         const R *rc = Rs + (size_t)c * BW;
 #pragma unroll
-        for (int c2 = 0; c2 < c; ++c2) acc[c2] = fma(-xc, rc[c2], acc[c2]);
+        for (int c2 = 0; c2 < c; ++c2) acc[c2] = mad(-xc, rc[c2], acc[c2]);
       }
 #pragma unroll
       for (int c = 0; c < BW; ++c)
@@ -310,21 +338,26 @@ __device__ void backward_one(const AdjArgs<R> &a, int p, R *Tw, R *Ms, unsigned 
   for (size_t idx = tid; idx < (size_t)m * n; idx += TQR_THREADS) W[idx] = Qb[idx];
   __syncthreads();
   apply_q<R>(g, F, Tw, 1, W, smem);
-  // Ms (lower) = R Rbar^T - (Q^T Qbar)^T
+  // Ms (lower) = R Rbar^H - (Q^H Qbar)^H
   for (int idx = tid; idx < n * n; idx += TQR_THREADS) {
     const int i = idx % n, j = idx / n;
     if (i >= j) {
-      R s = 0;
-      for (int k = i; k < n; ++k) s = fma(F[ix(i, k, m)], Rb[ix(j, k, n)], s);
-      Ms[idx] = s - W[ix(j, i, m)];
+      R s = R(0);
+      for (int k = i; k < n; ++k) s = mad(F[ix(i, k, m)], conj_(Rb[ix(j, k, n)]), s);
+      Ms[idx] = s - conj_(W[ix(j, i, m)]);
     }
   }
   __syncthreads();
-  // W := [copyltu(M); 0], then W := Q W
+  // W := [X; 0] with X = tril(M) + tril(M,-1)^H (complex: Re diag M), then W := Q W
   for (size_t idx = tid; idx < (size_t)m * n; idx += TQR_THREADS) {
     const int r = (int)(idx % m), c = (int)(idx / m);
     R v = R(0);
-    if (r < n) v = (r >= c) ? Ms[r + (size_t)c * n] : Ms[c + (size_t)r * n];
+    if (r < n) {
+      v = (r >= c) ? Ms[r + (size_t)c * n] : conj_(Ms[c + (size_t)r * n]);
+      if constexpr (is_cx<R>) {
+        if (r == c) v = R(v.x);
+      }
+    }
     W[idx] = v;
   }
   __syncthreads();
@@ -373,7 +406,11 @@ __global__ void k_adj_reset(AdjHeader *h) {
 }
 
 static std::mutex g_adj_mu;
-static int g_adj_grid[2][2][64];      // [precision][fwd/bwd][device]
+static int g_adj_grid[4][2][64];      // [element type][fwd/bwd][device]
+
+template <typename R> constexpr int adj_slot() {
+  return std::is_same<R, double>::value ? 0 : std::is_same<R, float>::value ? 1 : std::is_same<R, cx<double>>::value ? 2 : 3;
+}
 
 template <typename R, bool FWD>
 static int adj_grid(int *grid) {
@@ -382,15 +419,15 @@ static int adj_grid(int *grid) {
   if (e != cudaSuccess) return (int)e;
   if (dev >= 64) return (int)cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> l(g_adj_mu);
-  int &gsz = g_adj_grid[sizeof(R) == 4][FWD ? 0 : 1][dev];
+  int &gsz = g_adj_grid[adj_slot<R>()][FWD ? 0 : 1][dev];
   if (gsz == 0) {
     int sms = 0, per = 0;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return (int)e;
     auto kern = FWD ? k_qr_fwd<R> : k_qr_bwd<R>;
-    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kAdjSmem)) !=
+    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)adj_smem<R>())) !=
         cudaSuccess)
       return (int)e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, TQR_THREADS, kAdjSmem)) != cudaSuccess)
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, TQR_THREADS, adj_smem<R>())) != cudaSuccess)
       return (int)e;
     gsz = sms * std::max(per, 1);
   }
@@ -425,6 +462,10 @@ static int adj_launch(int batch, int m, int n, int ib, R *F, R *tau, R *Q, R *Ro
   AdjGeom g;
   if (n < 1 || n > kAdjNb) return -3;
   if (m < n) return -2;
+  // complex adjoint: every diagonal entry of R must be real, which needs a
+  // reflector below every column (m > n; with m == n the last column has one
+  // row, gets tau = 0 as in src/geqr2.jl:32-35, and keeps a complex R_nn)
+  if (!FWD && is_cx<R> && m == n) return -2;
   if (ib < 1 || ib > kAdjMaxIb) return -4;
   adj_geom(m, n, ib, &g);
   if (batch == 0) return 0;
@@ -446,12 +487,12 @@ static int adj_launch(int batch, int m, int n, int ib, R *F, R *tau, R *Q, R *Ro
   count_launch();
   const int gl = std::min(grid, batch);
   if (FWD) {
-    k_qr_fwd<R><<<gl, TQR_THREADS, kAdjSmem, st>>>(a);
+    k_qr_fwd<R><<<gl, TQR_THREADS, adj_smem<R>(), st>>>(a);
     count_launch();
   } else {
-    k_qr_bwd<R><<<gl, TQR_THREADS, kAdjSmem, st>>>(a);
+    k_qr_bwd<R><<<gl, TQR_THREADS, adj_smem<R>(), st>>>(a);
     count_launch();
-    const size_t sm = sizeof(R) * ((size_t)kAdjNb * kSolveBw + kSolveBw);
+    const size_t sm = sizeof(R) * ((size_t)kAdjNb * SolveBw<R>::value + SolveBw<R>::value);
     cudaError_t e = cudaSuccess;
     if (sm > 48 * 1024)
       e = cudaFuncSetAttribute(k_solve_rt<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -471,10 +512,35 @@ extern "C" {
 
 int tqr_qr_batched_worksize(int dtype_bytes, int m, int n, int ib, size_t *bytes) {
   if (!bytes) return -5;
-  if (dtype_bytes == 8) return adj_worksize<double>(m, n, ib, bytes, nullptr);
+  if (dtype_bytes == 8) {   // FP64 and ComplexF32 (8-byte elements)
+    size_t bd = 0, bc = 0;
+    int rc = adj_worksize<double>(m, n, ib, &bd, nullptr);
+    if (rc == 0) rc = adj_worksize<cx<float>>(m, n, ib, &bc, nullptr);
+    if (rc == 0) *bytes = std::max(bd, bc);
+    return rc;
+  }
   if (dtype_bytes == 4) return adj_worksize<float>(m, n, ib, bytes, nullptr);
+  if (dtype_bytes == 16) return adj_worksize<cx<double>>(m, n, ib, bytes, nullptr);
   return -9;
 }
+
+#define TQR_ADJ_CX(P, CT, E)                                                                                  \
+  int tqr_##P##qr_batched_fwd(int batch, int m, int n, int ib, CT *F, CT *tau, CT *Q, CT *R, void *work,       \
+                              size_t lwork, cudaStream_t stream) {                                          \
+    if (((uintptr_t)F | (uintptr_t)tau | (uintptr_t)Q | (uintptr_t)R) % alignof(E)) return -5;             \
+    return adj_launch<E, true>(batch, m, n, ib, (E *)F, (E *)tau, (E *)Q, (E *)R, nullptr, nullptr, nullptr,  \
+                               work, lwork, stream);                                                        \
+  }                                                                                                         \
+  int tqr_##P##qr_batched_bwd(int batch, int m, int n, int ib, const CT *F, const CT *tau, const CT *Qbar,    \
+                              const CT *Rbar, CT *Abar, void *work, size_t lwork, cudaStream_t stream) {      \
+    if (((uintptr_t)F | (uintptr_t)tau | (uintptr_t)Qbar | (uintptr_t)Rbar | (uintptr_t)Abar) % alignof(E))  \
+      return -5;                                                                                            \
+    return adj_launch<E, false>(batch, m, n, ib, (E *)F, (E *)tau, nullptr, nullptr, (const E *)Qbar,       \
+                                (const E *)Rbar, (E *)Abar, work, lwork, stream);                          \
+  }
+TQR_ADJ_CX(z, tqr_zcomplex, cx<double>)
+TQR_ADJ_CX(c, tqr_ccomplex, cx<float>)
+#undef TQR_ADJ_CX
 
 int tqr_dqr_batched_fwd(int batch, int m, int n, int ib, double *F, double *tau, double *Q, double *R,
                         void *work, size_t lwork, cudaStream_t stream) {

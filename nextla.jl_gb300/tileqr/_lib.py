@@ -138,6 +138,10 @@ DIAG = {
     "tqr_swy_apply": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _P, _P], _I),
     "tqr_stsmqr_wy": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, ctypes.c_size_t, _P, _P], _I),
     "tqr_qr_batched_worksize": ([_I, _I, _I, _I, ctypes.POINTER(ctypes.c_size_t)], _I),
+    "tqr_zqr_batched_fwd": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
+    "tqr_cqr_batched_fwd": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
+    "tqr_zqr_batched_bwd": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
+    "tqr_cqr_batched_bwd": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
     "tqr_dqr_batched_fwd": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
     "tqr_sqr_batched_fwd": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
     "tqr_dqr_batched_bwd": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),

@@ -8,6 +8,12 @@ a ChainRulesCore `rrule` for Julia callers: its forward saves only the packed
 factor and tau, and its backward runs the hand-written adjoint kernel, which
 recomputes every T factor from V and tau (larft!, src/larft.jl:53-86) and
 returns Abar = (Qbar + Q copyltu(R Rbar^T - Qbar^T Q)) R^-T.
+
+Complex tensors (complex128, complex64) take the same path with conjugate
+transposes and the real part of M's diagonal (R's diagonal is real):
+Abar = (Qbar + Q X) R^-H, X = tril(M,-1) + tril(M,-1)^H + Re diag(M),
+M = R Rbar^H - Qbar^H Q -- gradients in torch's convention for a real loss
+(dL/dRe + i dL/dIm).
 """
 import ctypes
 
@@ -32,6 +38,10 @@ def _prefix(dtype):
         return "d", 8
     if dtype == torch.float32:
         return "s", 4
+    if dtype == torch.complex128:
+        return "z", 16
+    if dtype == torch.complex64:
+        return "c", 8
     raise TypeError(f"unsupported element type {dtype}")
 
 
@@ -51,7 +61,7 @@ def workspace(dtype, m, n, ib, device):
     _, nb = _prefix(dtype)
     size = ctypes.c_size_t(0)
     _check(_lib.lib().tqr_qr_batched_worksize(nb, m, n, ib, ctypes.byref(size)), "qr_batched_worksize")
-    key = (str(device), nb, m, n, ib)
+    key = (str(device), nb, m, n, ib, str(dtype))
     w = _WORK.get(key)
     if w is None:
         w = torch.empty(size.value + 256, dtype=torch.uint8, device=device)

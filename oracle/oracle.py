@@ -428,11 +428,13 @@ def tile_lstsq(A, B, nb, ib):
 # ---------------------------------------------------------------------------
 
 def qr_explicit(A, nb=256, ib=32):
-    """(Q, R, F): thin Q (m-by-n), R (n-by-n upper) and the packed factor."""
-    F = np.array(A, order="F", dtype=np.float64)
+    """(Q, R, F): thin Q (m-by-n), R (n-by-n upper) and the packed factor
+    (float64, or complex128 for complex input)."""
+    dt = np.complex128 if np.iscomplexobj(A) else np.float64
+    F = np.array(A, order="F", dtype=dt)
     m, n = F.shape
     T, _ = tile_geqrf(F, nb, ib)
-    Q = np.asfortranarray(np.eye(m, n))
+    Q = np.asfortranarray(np.eye(m, n, dtype=dt))
     tile_unmqr("N", F, T, Q, nb, ib)
     R = np.triu(F[:n, :n])
     return Q, R, F
@@ -444,6 +446,18 @@ def qr_adjoint(Q, R, Qbar, Rbar):
     Abar = (Qbar + Q copyltu(M)) R^-T, copyltu(M) = tril(M) + tril(M, -1)^T.
     Only the upper triangle of Rbar enters (R has no other entries)."""
     from scipy.linalg import solve_triangular
+    if np.iscomplexobj(Q) or np.iscomplexobj(Qbar) or np.iscomplexobj(Rbar):
+        # complex, R's diagonal real: Abar = (Qbar + Q X) R^-H with
+        # X = tril(M,-1) + tril(M,-1)^H + Re diag(M), M = R Rbar^H - Qbar^H Q
+        # (the gradient of a real loss as dL/dRe + i dL/dIm); needs m > n so
+        # that every column has a reflector (src/geqr2.jl:32-35 leaves a
+        # one-row last column with tau = 0 and a complex R_nn)
+        if Q.shape[0] <= Q.shape[1]:
+            raise ValueError("complex QR adjoint needs m > n")
+        M = R @ np.triu(Rbar).conj().T - Qbar.conj().T @ Q
+        C = np.tril(M, -1) + np.tril(M, -1).conj().T + np.diag(M.diagonal().real)
+        Y = Qbar + Q @ C
+        return solve_triangular(R, Y.conj().T, lower=False).conj().T      # Y R^-H = (R^-1 Y^H)^H
     M = R @ np.triu(Rbar).T - Qbar.T @ Q
     C = np.tril(M) + np.tril(M, -1).T
     Y = Qbar + Q @ C

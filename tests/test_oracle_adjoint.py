@@ -55,3 +55,33 @@ def test_reference_adjoint_of_q_and_r_separately(oracle):
         fd = (fp - fm) / (2 * h)
         an = float(np.sum(Ab * E))
         assert abs(fd - an) <= 1e-6 * max(1.0, abs(an)), (fd, an)
+
+
+@pytest.mark.parametrize("m,n,nb,ib", [(48, 20, 16, 4), (31, 30, 32, 8), (70, 9, 32, 4)])
+def test_complex_reference_adjoint_matches_central_differences(oracle, m, n, nb, ib):
+    """The complex pullback (R's diagonal real): Abar = (Qbar + Q X) R^-H with
+    X = tril(M,-1) + tril(M,-1)^H + Re diag(M), M = R Rbar^H - Qbar^H Q, the
+    gradient of a real loss as dL/dRe(A) + i dL/dIm(A), against central
+    differences in the real and the imaginary direction of every entry of A
+    for L = Re<dQ, Q> + Re<dR, R> through the complex tile QR; m > n, so every
+    column has a reflector and R's diagonal is real."""
+    rng = np.random.default_rng(m + n)
+    A = rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))
+    dQ = rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))
+    dR = np.triu(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+
+    def L(A_):
+        Q_, R_, _ = oracle.qr_explicit(A_, nb, ib)
+        return float(np.real(np.vdot(dQ, Q_)) + np.real(np.vdot(dR, R_)))
+
+    Q, R, _ = oracle.qr_explicit(A, nb, ib)
+    assert np.abs(R.diagonal().imag).max() == 0.0
+    Ab = oracle.qr_adjoint(Q, R, dQ, dR)
+    h = 1e-6
+    G = np.zeros_like(A)
+    for i in range(m):
+        for j in range(n):
+            E = np.zeros_like(A)
+            E[i, j] = h
+            G[i, j] = (L(A + E) - L(A - E)) / (2 * h) + 1j * (L(A + 1j * E) - L(A - 1j * E)) / (2 * h)
+    assert np.abs(G - Ab).max() <= 1e-6 * np.abs(G).max()
