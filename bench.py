@@ -49,7 +49,7 @@ def parse():
                             "hqr_square", "batched", "larft", "trsm"],
                    help="time one tile kernel alone (for profiling) instead of the workload")
     p.add_argument("--dtype", default="f64", choices=["f64", "f32", "c64", "c128"],
-                   help="element type for --kernel (complex: tile only)")
+                   help="element type for --kernel and --adjoint-only --adjoint-kernels")
     p.add_argument("--grp", type=int, default=4, help="with --kernel hqr_square: tiles per flat group")
     p.add_argument("--dag-quantum", type=float, default=None,
                    help="with --kernel tile: bucket width of the persistent kernel's priority sort")
@@ -970,15 +970,56 @@ def lapack_dgeqrf_tflops(n):
     return flops_square(n) / dt / 1e12, dt
 
 
-def adjoint_bench(torch, batch=256, m=2048, n=256, steps=3, warmup=3, peak=None, kernels_only=False):
+def adjoint_kernels_complex(torch, batch, m, n, steps, warmup, dtype):
+    """Forward and adjoint kernels of the complex differentiable QR on a batch
+    of complex N(0,1) problems with seeded cotangents, CUDA-event timed on the
+    launching stream.  Flops are real flops: 4x the real counts for a complex
+    multiply-add (factorisation 4 (2mn^2 - 2n^3/3), explicit Q 4 (2mn^2 - 2n^3/3))."""
+    from tileqr import autodiff as AD
+    tdt = {"c128": torch.complex128, "c64": torch.complex64}[dtype]
+    st = torch.cuda.current_stream()
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+
+    def cr(*s):
+        return torch.complex(torch.randn(s, generator=g, dtype=torch.float64, device="cuda"),
+                             torch.randn(s, generator=g, dtype=torch.float64, device="cuda")).to(tdt)
+
+    A, Qb, Rb = cr(batch, m, n), cr(batch, m, n), torch.triu(cr(batch, n, n))
+    fwd_ms, bwd_ms = [], []
+    for rep in range(warmup + steps):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record(st)
+        Q, R, F, tau = AD.qr_forward(A)
+        e[1].record(st)
+        Ab = AD.qr_backward(F, tau, Qb, Rb)
+        e[2].record(st)
+        torch.cuda.synchronize()
+        if rep >= warmup:
+            fwd_ms.append(e[0].elapsed_time(e[1]))
+            bwd_ms.append(e[1].elapsed_time(e[2]))
+    finite = bool(torch.isfinite(torch.view_as_real(Ab)).all())
+    f_fwd = batch * 4.0 * 2 * (2.0 * m * n * n - 2.0 * n ** 3 / 3.0)
+    fm, bm = statistics.median(fwd_ms), statistics.median(bwd_ms)
+    return {"workload": f"QR forward and adjoint kernels, batch of {batch} {dtype} {m}x{n}, seeded cotangents",
+            "fwd_ms": fm, "bwd_ms": bm, "fwd_tflops_real": f_fwd / (fm * 1e-3) / 1e12, "finite": finite}
+
+
+def adjoint_bench(torch, batch=256, m=2048, n=256, steps=3, warmup=3, peak=None, kernels_only=False,
+                  dtype="f64"):
     """Differentiable QR: (Q, R) = qr(A) for a batch of 256 Float64 2048x256
     N(0,1) matrices, loss 1/2||R^-1 Q^T b - y||^2 + <dQ, Q> + <dR, R> with
     seeded b, y, dQ, dR, backward through the adjoint kernel.  Times the
     forward kernel, the backward kernel and the whole autograd step; checks
     one problem against the CPU FP64 reference adjoint and the whole batch
-    against a central difference (h = 1e-6)."""
+    against a central difference (h = 1e-6).  With kernels_only the element
+    type may be complex ("c128", "c64": the forward and adjoint kernels on
+    complex N(0,1) problems; real and imaginary parts seeded alike)."""
     import numpy as np
 
+    if dtype != "f64":
+        if not kernels_only:
+            raise SystemExit("--dtype other than f64 needs --adjoint-kernels")
+        return adjoint_kernels_complex(torch, batch, m, n, steps, warmup, dtype)
     import oracle
     from tileqr import _lib
     from tileqr import autodiff as AD
@@ -1290,7 +1331,7 @@ def main():
         tileqr_build.build()
         res = adjoint_bench(torch, 256, 2048, 256, max(1, args.steps), max(3, args.warmup),
                             kernels_only=args.adjoint_kernels,
-                            peak=fp64_peak(_lib, torch))
+                            peak=fp64_peak(_lib, torch), dtype=args.dtype)
         print(json.dumps(res), flush=True)
         return 0
     if args.batched_only:
