@@ -97,7 +97,7 @@ def _shard_worker(rank, world, port, q):
 
 
 def test_batched_shard_by_cost_gloo():
-    """Configs 4 and 5 shard by problem: each of two gloo ranks computes its
+    """The batched solver and the differentiable QR shard by problem: each of two gloo ranks computes its
     part of the cost-balanced partition on its own, the parts cover the batch
     exactly once with costs within 0.1 % of each other, and a host-side gather
     puts every problem's result back in place."""

@@ -10,7 +10,7 @@ seconds on the host cores; tests/test_oracle_host_blas.py pins that form to
 the LAPACK golden vectors and to the plain-loop oracle.
 
 Bars:
-* north_star's "relative differences in R and Q <= 1e-12 n", applied per
+* the parity bar "relative differences in R and Q <= 1e-12 n", applied per
   tile: every nb x nb tile of R, V and explicit Q, every ib x nb block of T
   and every panel's tau, relative to that tile's own Frobenius norm, so a
   wrong small-magnitude block cannot hide behind the large ones;

@@ -84,7 +84,7 @@ def test_dag_repeated_calls_reuse_workspace(tq):
 
 @pytest.mark.parametrize("trans", ["C", "N"])
 def test_tile_unmqr_vs_oracle(tq, oracle, trans):
-    """Config 1's second half: Q applied to 16 seeded right-hand sides."""
+    """The 1024^2 tile QR's second half: Q applied to 16 seeded right-hand sides."""
     rng = np.random.default_rng(16)
     m = n = 1024
     nb, ib = 256, 32
