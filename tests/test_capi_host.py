@@ -199,6 +199,27 @@ def test_complex_argument_errors(L):
     assert L.tqr_ztile_geqrf(8, 8, 4, 8, z, 8, z, 8, z, 8, None) == -4                  # ib > nb
 
 
+def test_complex_adjoint_argument_errors(L):
+    """The differentiable QR's checks, all made before any CUDA call: batch,
+    n <= 256, m >= n, ib <= 32, element alignment, and the complex backward's
+    m > n (a square complex problem keeps a complex R_nn, src/geqr2.jl:32-35)."""
+    import ctypes
+    z = ctypes.c_void_p(256)
+    for p in "zc":
+        fwd, bwd = getattr(L, f"tqr_{p}qr_batched_fwd"), getattr(L, f"tqr_{p}qr_batched_bwd")
+        assert fwd(-1, 64, 32, 32, z, z, z, z, z, 1 << 20, None) == -1
+        assert fwd(1, 600, 257, 32, z, z, z, z, z, 1 << 20, None) == -3
+        assert fwd(1, 31, 32, 32, z, z, z, z, z, 1 << 20, None) == -2
+        assert fwd(1, 64, 32, 33, z, z, z, z, z, 1 << 20, None) == -4
+        assert bwd(1, 40, 40, 32, z, z, z, z, z, z, 1 << 20, None) == -2     # square: refused
+        assert bwd(1, 41, 40, 33, z, z, z, z, z, z, 1 << 20, None) == -4     # m > n passes the -2 check
+        assert bwd(0, 41, 40, 32, z, z, z, z, z, z, 1 << 20, None) == 0      # empty batch: nothing to do
+        assert bwd(1, 41, 40, 32, None, z, z, z, z, z, 1 << 20, None) == -5
+    assert L.tqr_zqr_batched_bwd(1, 41, 40, 32, ctypes.c_void_p(8), z, z, z, z, z, 1 << 20, None) == -5  # 8-byte aligned
+    # the real backward keeps square problems (R's diagonal needs no gauge there)
+    assert L.tqr_dqr_batched_bwd(1, 40, 40, 33, z, z, z, z, z, z, 1 << 20, None) == -4
+
+
 @pytest.mark.parametrize("m,n,nb,ib,grp,nrhs", [(2048, 512, 128, 32, 4, 3), (4096, 1024, 256, 32, 8, 5),
                                                 (517, 130, 64, 16, 3, 2), (32768, 4096, 256, 32, 16, 4),
                                                 (65536, 512, 256, 32, 8, 0)])
