@@ -67,6 +67,8 @@ def parse():
     p.add_argument("--adjoint-only", action="store_true", help="run only the differentiable QR")
     p.add_argument("--adjoint-kernels", action="store_true",
                    help="with --adjoint-only: the forward and adjoint kernels alone, seeded cotangents")
+    p.add_argument("--adjoint-shape", default="256,2048,256",
+                   help="with --adjoint-only --adjoint-kernels: batch,m,n (a smaller case for profiling)")
     p.add_argument("--no-tall", action="store_true", help="skip the tall-skinny flat vs tree comparison")
     p.add_argument("--tall-only", action="store_true", help="run only the tall-skinny flat vs tree comparison")
     p.add_argument("--no-complex", action="store_true", help="skip the complex tile QR")
@@ -1329,7 +1331,10 @@ def main():
         import tileqr_build
         from tileqr import _lib
         tileqr_build.build()
-        res = adjoint_bench(torch, 256, 2048, 256, max(1, args.steps), max(3, args.warmup),
+        ab, am, an = (int(v) for v in args.adjoint_shape.split(","))
+        if (ab, am, an) != (256, 2048, 256) and not args.adjoint_kernels:
+            raise SystemExit("--adjoint-shape needs --adjoint-kernels")
+        res = adjoint_bench(torch, ab, am, an, max(1, args.steps), max(3, args.warmup),
                             kernels_only=args.adjoint_kernels,
                             peak=fp64_peak(_lib, torch), dtype=args.dtype)
         print(json.dumps(res), flush=True)

@@ -114,16 +114,37 @@ __device__ ApplyArgs<R> base_args(int ib) {
 
 // C (m x n, ldc = m) := Q C (trans 0) or Q^T C (trans 1) with Q from the
 // factor F (tile 0's reflectors, then tile t's for t = 1..MT-1) and T.
+//
+// ident (trans 0 only): C holds [I; 0] on entry, so the explicit thin Q is
+// being formed (LAPACK's orgqr).  Blocks are applied last to first, and
+// through every step column c of the top n rows is nonzero only above the
+// end of its own ib-block, while tile rows not yet reached are zero.  A block
+// of reflectors starting at column i0 > c then meets W = 0 on column c and
+// leaves it as it is, so each strip [c0, c0 + NW) applies only the blocks
+// starting before c0 + NW: the same values, about half the work of forming Q.
 template <typename R>
-__device__ void apply_q(const AdjGeom &g, const R *F, const R *Tw, int trans, R *C, unsigned char *smem) {
+__device__ void apply_q(const AdjGeom &g, const R *F, const R *Tw, int trans, R *C, unsigned char *smem,
+                        bool ident = false) {
   const int m = g.m, n = g.n, ib = g.ib;
+  auto run = [&](ApplyArgs<R> a) {
+    if (!ident) {
+      apply_cols<R>(a, 0, smem);
+      return;
+    }
+    constexpr int NW = AdjNW<R>::value;
+    for (int c = 0; c < a.ncols; c += NW) {
+      a.k = min(n, ((c + NW + ib - 1) / ib) * ib);
+      apply_strip<R, NW>(a, c, smem);
+      __syncthreads();
+    }
+  };
   auto tile0 = [&]() {
     ApplyArgs<R> a = base_args<R>(ib);
     a.mode = 0; a.L = g.rows(0); a.k = n; a.fwd = trans; a.transT = trans;
     a.C = C; a.c_cs = m; a.ncols = n;
     a.V = F; a.ldv = m;
     a.T = Tw; a.ldt = ib;
-    apply_cols<R>(a, 0, smem);
+    run(a);
   };
   auto pair = [&](int t) {
     ApplyArgs<R> a = base_args<R>(ib);
@@ -132,7 +153,7 @@ __device__ void apply_q(const AdjGeom &g, const R *F, const R *Tw, int trans, R 
     a.A1 = C; a.a_cs = m;
     a.V = F + (size_t)t * kAdjNb; a.ldv = m;
     a.T = Tw + (size_t)t * kAdjMaxIb * n; a.ldt = ib;
-    apply_cols<R>(a, 0, smem);
+    run(a);
   };
   if (trans) {
     tile0();
@@ -320,7 +341,7 @@ __device__ void forward_one(const AdjArgs<R> &a, int p, R *Tw, unsigned char *sm
     Qp[idx] = (r == c) ? R(1) : R(0);
   }
   __syncthreads();
-  apply_q<R>(g, A, Tw, 0, Qp, smem);
+  apply_q<R>(g, A, Tw, 0, Qp, smem, true);
 }
 
 template <typename R>
