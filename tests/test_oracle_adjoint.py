@@ -85,3 +85,17 @@ def test_complex_reference_adjoint_matches_central_differences(oracle, m, n, nb,
             E[i, j] = h
             G[i, j] = (L(A + E) - L(A - E)) / (2 * h) + 1j * (L(A + 1j * E) - L(A - 1j * E)) / (2 * h)
     assert np.abs(G - Ab).max() <= 1e-6 * np.abs(G).max()
+
+
+def test_complex_reference_adjoint_refuses_square(oracle):
+    """A square complex matrix: the one-row last column keeps tau = 0
+    (src/geqr2.jl:32-35), so R[n-1, n-1] stays complex and the Re-diagonal
+    gauge term does not describe it; the reference pullback refuses, as the
+    GPU backward does (argument error -2)."""
+    rng = np.random.default_rng(9)
+    A = rng.standard_normal((12, 12)) + 1j * rng.standard_normal((12, 12))
+    Q, R, _ = oracle.qr_explicit(A, 32, 4)
+    assert abs(R[-1, -1].imag) > 0.0
+    assert np.abs(R.diagonal()[:-1].imag).max() == 0.0
+    with pytest.raises(ValueError):
+        oracle.qr_adjoint(Q, R, np.zeros_like(Q), np.zeros_like(R))
