@@ -79,6 +79,29 @@ def test_unmqr_argument_errors(L):
     assert L.tqr_dunmqr(b"L", b"N", 32, 24, 0, 4, NULL, 32, NULL, 4, NULL, 32, NULL, 24, NULL) == 0
 
 
+def test_reference_argument_error_cases(L):
+    """The ArgumentError cases of the reference's own tests that the tests
+    above do not already hold, as negative return codes (every element type).
+    Each check happens before any CUDA call."""
+    for p in "dszc":
+        geqr2, ttqrt, ttmqr, parfb = (getattr(L, f"tqr_{p}{n}") for n in ("geqr2", "ttqrt", "ttmqr", "parfb"))
+        # test/geqr2.jl:57-58
+        assert geqr2(-1, 5, NULL, 5, NULL, NULL, NULL) == -1
+        assert geqr2(5, -1, NULL, 5, NULL, NULL, NULL) == -2
+        # test/ttqrt.jl:173-175
+        assert ttqrt(-1, 8, 4, NULL, 8, NULL, 8, NULL, 4, NULL, NULL, NULL) == -1
+        assert ttqrt(8, -1, 4, NULL, 8, NULL, 8, NULL, 4, NULL, NULL, NULL) == -2
+        assert ttqrt(8, 8, -1, NULL, 8, NULL, 8, NULL, 4, NULL, NULL, NULL) == -3
+        # test/ttmqr.jl:163-165
+        t = (8, 8, 8, 8, 4, 2, NULL, 8, NULL, 8, NULL, 8, NULL, 2, NULL, 16, NULL)
+        assert ttmqr(b"X", b"N", *t) == -1
+        assert ttmqr(b"L", b"X", *t) == -2
+        # test/parfb.jl:58-61 (direct and storev are in test_parfb_argument_checks)
+        a = (4, 4, 4, 4, 2, 0, NULL, 4, NULL, 4, NULL, 4, NULL, 2, NULL, 2, NULL)
+        assert parfb(b"X", b"N", b"F", b"C", *a) == -1
+        assert parfb(b"L", b"X", b"F", b"C", *a) == -2
+
+
 def test_larfb_larft_edge_cases(L):
     # test/larfb.jl:191-196 and test/larft.jl:207-210: empty work is a no-op
     assert L.tqr_dlarfb(b"L", b"N", b"F", b"C", 0, 0, 0, NULL, 1, NULL, 1, NULL, 1, NULL, 1, NULL) == 0
