@@ -1169,7 +1169,8 @@ def fp64_mma_peak(tq_lib, torch):
 
 def noalloc_vs_workspace(tq, torch, sizes=(4096, 8192), reps=3):
     """The allocation-free tile QR (tqr_dtile_geqrf_noalloc: schedule in a
-    fixed device array, written on the device in a one-step lookahead order)
+    fixed device array, written on the device in buckets of key
+    4 min(column, k + 1) + row)
     against the workspace entry point (critical-path order) on the same
     matrix."""
     import ctypes

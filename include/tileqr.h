@@ -341,9 +341,9 @@ int tqr_stile_gels_dag(int m, int n, int nrhs, int nb, int ib, float *A, int lda
 /* Allocation-free tile QR (no counterpart in NextLA).  Same factorisation and
  * the same bits as tqr_dtile_geqrf_dag (each tile strip sees the same
  * operations in the same order; only the order in which CTAs pick up tasks
- * differs: a one-step lookahead order written on the device here, longest
- * path first there), but it needs no
- * `work` argument: for
+ * differs: here an order written on the device by key 4 min(column, k+1) +
+ * row, which follows the critical path without a sort; longest path first
+ * there), but it needs no `work` argument: for
  * callers that cannot hand the library device memory -- code running while a
  * framework's caching allocator owns the device, host code that must not
  * take the implicit synchronisation of cudaMalloc/cudaFree mid-pipeline, or
@@ -373,8 +373,10 @@ int tqr_dtile_geqrf_noalloc(int m, int n, int nb, int ib, double *A, int lda, do
 int tqr_tile_noalloc_status(int *status, int *task, cudaStream_t stream);
 /* Host replay of tqr_dtile_geqrf_noalloc's task order for a shape: every
  * dependency is listed before its task and every task appears once.  0 =
- * consistent (*ntasks the count), -1 = shape outside the kernel, 1-3 = which
- * check failed. */
+ * consistent (*ntasks the count), -1 = shape outside the kernel, 1-5 = which
+ * check failed (1 count, 2 a wait target not yet reached, 3 a panel counter's
+ * final value, 4 the device generator's count and list disagree, 5 not the
+ * loop order's tasks). */
 int tqr_tile_noalloc_check(int m, int n, int nb, int ib, long long *ntasks);
 
 /* Tile QR with a binary reduction tree per panel (no counterpart in NextLA;

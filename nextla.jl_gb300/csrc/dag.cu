@@ -574,55 +574,72 @@ __host__ __device__ inline long long gen_step(const DagGeom &g, int k, DagItem *
   return n;
 }
 
-// Lookahead order for schedules written on the device (no host sort).  Step
-// k's tasks fall into three sections: P(k), the panel and everything the next
-// panel reads (GB/GA, UN of tile column k + 1, the TB/TA blocks, TM of tile
-// column k + 1); C(k), tile column k + 2 (UN, then TM per tile row); R(k),
-// the columns right of that.  The list is P(0), then C(k), P(k + 1), R(k)
-// for k = 0, 1, ...: the next panel's chain is queued before the bulk of the
-// current step's update, one step ahead.  Every task's producers come
-// earlier in the list (tqr_tile_noalloc_check replays it on the host), and
-// inside a section the tasks keep the loop order.  Section q: 0 is P(0); for
-// q >= 1, k = (q - 1) / 3 and (q - 1) % 3 selects C(k), P(k + 1), R(k).
-// Writes the tasks when out is non-null; returns their count.
-__host__ __device__ inline long long gen_section(const DagGeom &g, int q, DagItem *out) {
+// Task order for schedules written on the device (no host sort).  Tasks go
+// in increasing key 4 min(column, k + 1) + row, ties in the loop order:
+//   geqrt group of step k (GB, GA)        key 5k
+//   every unmqr of step k (UN)            key 5k + 4
+//   tsqrt group (k, i) (TB, TA)           key 4k + i
+//   tsmqr row (k, i), all columns (TM)    key 4k + i + 4
+// No producer has a larger key than its consumer: a tsqrt (k, i) needs the
+// tsmqr (k - 1, i) on its tile, key 4(k - 1) + i + 4 = 4k + i; the geqrt of
+// step k needs the tsmqr (k - 1, k), key 5k; a tsmqr needs its tsqrt, the
+// tsmqr or unmqr above it in its column and the previous step's update of
+// its tile, all with smaller keys.  With ties in the loop order, which is
+// topological, the list is topological (tqr_tile_noalloc_check replays it).
+// Capping the column at k + 1 keeps far columns' updates from being queued
+// ahead of the next panels, and the row weight 1/4 lets the next step's
+// panel chain start while the current step's lower rows are still queued:
+// the list follows the critical path much as the host's longest-path sort
+// does.  Bucket v holds the tasks of key v, step by step in loop order (for
+// one step: geqrt, unmqr, the tsmqr row v - 4k - 4, then the tsqrt row
+// v - 4k, which is their order in the loop).  Writes the tasks when out is
+// non-null; returns their count.
+__host__ __device__ inline int noalloc_buckets(const DagGeom &g) { return 5 * g.KT + g.MT + 4; }
+
+// strips of the tile columns right of column k (one unmqr or tsmqr row)
+__host__ __device__ inline long long right_strips(const DagGeom &g, int k) {
   long long n = 0;
-  int k, kind;
-  if (q == 0) { k = 0; kind = 0; }
-  else { k = (q - 1) / 3; kind = (q - 1) % 3 == 0 ? 1 : ((q - 1) % 3 == 1 ? 0 : 2); if (kind == 0) ++k; }
-  if (k >= g.KT) return 0;
-  auto push = [&](uint8_t type, int i, int j, int b, int s) {
-    if (out) {
-      DagItem it;
-      it.type = type; it.b = (uint8_t)b; it.k = (uint16_t)k; it.i = (uint16_t)i; it.j = (uint16_t)j;
-      it.s = (uint16_t)s; it.pad = 0;
-      out[n] = it;
-    }
-    ++n;
-  };
-  // tile columns of this section: P -> k + 1, C -> k + 2, R -> [k + 3, NT)
-  const int j0 = kind == 0 ? k + 1 : (kind == 1 ? k + 2 : k + 3);
-  const int j1 = kind == 2 ? g.NT : min(g.NT, j0 + 1);
-  if (kind == 0)
-    for (int b = 0; b < g.NBK; ++b) {
-      push(IT_GB, k, k, b, 0);
-      for (int s = (b + 1) * g.SPB; s < g.NS; ++s) push(IT_GA, k, k, b, s);
-    }
-  for (int j = j0; j < j1; ++j)
-    for (int s = 0; s < g.strips(j); ++s) push(IT_UN, k, j, 0, s);
-  for (int i = k + 1; i < g.MT; ++i) {
-    if (kind == 0)
-      for (int b = 0; b < g.NBK; ++b) {
-        push(IT_TB, i, k, b, 0);
-        for (int s = (b + 1) * g.SPB; s < g.NS; ++s) push(IT_TA, i, k, b, s);
-      }
-    for (int j = j0; j < j1; ++j)
-      for (int s = 0; s < g.strips(j); ++s) push(IT_TM, i, j, 0, s);
-  }
+  for (int j = k + 1; j < g.NT; ++j) n += g.strips(j);
   return n;
 }
 
-__host__ __device__ inline int lookahead_sections(const DagGeom &g) { return 1 + 3 * g.KT; }
+__host__ __device__ inline long long gen_bucket(const DagGeom &g, int v, DagItem *out) {
+  long long n = 0;
+  int k = 0;
+  auto push = [&](uint8_t type, int i, int j, int b, int s) {
+    DagItem it;
+    it.type = type; it.b = (uint8_t)b; it.k = (uint16_t)k; it.i = (uint16_t)i; it.j = (uint16_t)j;
+    it.s = (uint16_t)s; it.pad = 0;
+    out[n++] = it;
+  };
+  for (k = 0; k < g.KT && 5 * k <= v; ++k) {     // every key of step k is >= 5k
+    const int i2 = v - 4 * k - 4, i1 = v - 4 * k;
+    const bool pg = v == 5 * k, un = v == 5 * k + 4;
+    const bool tm = i2 > k && i2 < g.MT, ts = i1 > k && i1 < g.MT;
+    if (!out) {
+      n += (pg ? g.panel_tasks() : 0) + (ts ? g.panel_tasks() : 0) + (un ? right_strips(g, k) : 0) +
+           (tm ? right_strips(g, k) : 0);
+      continue;
+    }
+    if (pg)
+      for (int b = 0; b < g.NBK; ++b) {
+        push(IT_GB, k, k, b, 0);
+        for (int s = (b + 1) * g.SPB; s < g.NS; ++s) push(IT_GA, k, k, b, s);
+      }
+    if (un)
+      for (int j = k + 1; j < g.NT; ++j)
+        for (int s = 0; s < g.strips(j); ++s) push(IT_UN, k, j, 0, s);
+    if (tm)
+      for (int j = k + 1; j < g.NT; ++j)
+        for (int s = 0; s < g.strips(j); ++s) push(IT_TM, i2, j, 0, s);
+    if (ts)
+      for (int b = 0; b < g.NBK; ++b) {
+        push(IT_TB, i1, k, b, 0);
+        for (int s = (b + 1) * g.SPB; s < g.NS; ++s) push(IT_TA, i1, k, b, s);
+      }
+  }
+  return n;
+}
 
 // Natural (generation) order: the algorithm's own loop order, topological.
 static void gen_items(const DagGeom &g, std::vector<DagItem> &v) {
@@ -858,7 +875,7 @@ static int tile_geqrf_dag(int m, int n, int nb, int ib, R *A, int lda, R *T, int
 // a scratch buffer alive between calls.  For them the schedule and its
 // counters live in one file-scope device array of fixed size that every GPU
 // loading this library keeps until exit.  The task list is written on the
-// device (the lookahead order of gen_section, which is topological), so
+// device (the bucket order of gen_bucket, which is topological), so
 // neither the host nor the device allocates anything per call.
 // ---------------------------------------------------------------------------
 constexpr size_t kStaticScratchBytes = size_t(4) << 20;   // 4 MiB (see tileqr.h)
@@ -888,8 +905,8 @@ static cudaError_t static_scratch(void **out) {
   return cudaSuccess;
 }
 
-// Clears the header and counters and writes the task list (CTA q writes
-// section q of the lookahead order at its offset).  Everything the DAG kernel expects to start at zero is
+// Clears the header and counters and writes the task list (CTA v writes
+// bucket v of gen_bucket's order at its offset).  Everything the DAG kernel expects to start at zero is
 // cleared here on every call, because the array keeps the previous call's
 // contents.
 __global__ void k_static_schedule(DagGeom g, unsigned char *w, size_t bytes_counters, long long key,
@@ -908,10 +925,10 @@ __global__ void k_static_schedule(DagGeom g, unsigned char *w, size_t bytes_coun
       h->t_first = ~0ull;
     }
   }
-  if (threadIdx.x == 0 && (int)blockIdx.x < lookahead_sections(g)) {
+  if (threadIdx.x == 0 && (int)blockIdx.x < noalloc_buckets(g)) {
     long long off = 0;
-    for (int q = 0; q < (int)blockIdx.x; ++q) off += gen_section(g, q, nullptr);
-    gen_section(g, blockIdx.x, reinterpret_cast<DagItem *>(w + 256 + bytes_counters) + off);
+    for (int q = 0; q < (int)blockIdx.x; ++q) off += gen_bucket(g, q, nullptr);
+    gen_bucket(g, blockIdx.x, reinterpret_cast<DagItem *>(w + 256 + bytes_counters) + off);
   }
 }
 
@@ -937,7 +954,7 @@ static int tile_geqrf_noalloc(int m, int n, int nb, int ib, double *A, int lda, 
   if (e != cudaSuccess) return (int)e;
   unsigned char *w = static_cast<unsigned char *>(wv);
   const long long key = geom_key(g);
-  k_static_schedule<<<lookahead_sections(g), TQR_THREADS, 0, st>>>(g, w, bytes_counters, key, (int)nitems);
+  k_static_schedule<<<noalloc_buckets(g), TQR_THREADS, 0, st>>>(g, w, bytes_counters, key, (int)nitems);
   count_launch();
   if ((e = cudaGetLastError()) != cudaSuccess) return (int)e;
   DagArgs<double> a;
@@ -1103,14 +1120,27 @@ int tqr_tile_noalloc_check(int m, int n, int nb, int ib, long long *ntasks) {
   DagGeom g;
   if (!dag_geom(m, n, nb, ib, &g)) return -1;
   std::vector<DagItem> v;
-  for (int q = 0; q < lookahead_sections(g); ++q) {
+  for (int q = 0; q < noalloc_buckets(g); ++q) {
     const size_t off = v.size();
-    v.resize(off + (size_t)gen_section(g, q, nullptr));
-    gen_section(g, q, v.data() + off);
+    const long long c = gen_bucket(g, q, nullptr);
+    v.resize(off + (size_t)c);
+    if (gen_bucket(g, q, v.data() + off) != c) return 4;     // counting and writing agree
   }
-  long long nat = 0;
-  for (int k = 0; k < g.KT; ++k) nat += step_tasks(g, k);
-  if ((long long)v.size() != nat) return 1;
+  std::vector<DagItem> nat;
+  gen_items(g, nat);
+  if (v.size() != nat.size()) return 1;
+  // the same tasks as the loop order, each once
+  auto id = [](const DagItem &it) {
+    return ((unsigned long long)it.type << 56) | ((unsigned long long)it.b << 48) | ((unsigned long long)it.k << 32) |
+           ((unsigned long long)it.i << 16) | (unsigned long long)it.j | ((unsigned long long)it.s << 40);
+  };
+  {
+    std::vector<unsigned long long> a(v.size()), b(nat.size());
+    for (size_t x = 0; x < v.size(); ++x) { a[x] = id(v[x]); b[x] = id(nat[x]); }
+    std::sort(a.begin(), a.end());
+    std::sort(b.begin(), b.end());
+    if (a != b) return 5;
+  }
   std::vector<int> seen(g.ncounters(), 0);
   int c[kMaxDeps], t[kMaxDeps];
   for (const DagItem &it : v) {

@@ -342,12 +342,14 @@ def test_tree_task_graph_with_8_column_strips(L, m, n, nb, ib, grp, nrhs):
 @pytest.mark.parametrize("shape", [(1024, 1024, 256, 32), (2048, 1024, 256, 32), (1024, 2048, 256, 32),
                                    (512, 512, 128, 32), (768, 512, 128, 16), (256, 256, 256, 32),
                                    (1024, 1024, 256, 64), (4096, 4096, 256, 32), (8192, 8192, 256, 32),
-                                   (65536, 512, 256, 32), (512, 4096, 256, 32)])
-def test_noalloc_lookahead_order_replays(L, shape):
-    """The allocation-free tile QR's device-written task order (the next
-    panel's tasks queued one step ahead of the bulk of the current update):
-    every dependency listed before its task, every task of the loop order
-    exactly once."""
+                                   (65536, 512, 256, 32), (512, 4096, 256, 32), (16384, 4096, 256, 32),
+                                   (8192, 2048, 256, 32), (4096, 8192, 256, 32), (3072, 2048, 128, 16),
+                                   (2560, 2560, 256, 32)])
+def test_noalloc_bucket_order_replays(L, shape):
+    """The allocation-free tile QR's device-written task order (buckets of
+    key 4 min(column, k + 1) + row, loop order inside a bucket): every
+    dependency listed before its task, every task of the loop order exactly
+    once, and the generator's count pass agrees with its write pass."""
     nt = ctypes.c_longlong(0)
     assert L.tqr_tile_noalloc_check(*shape, ctypes.byref(nt)) == 0
     import tileqr

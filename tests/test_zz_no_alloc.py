@@ -45,7 +45,8 @@ def _noalloc_status(tq):
     return status.value, task.value
 
 
-@pytest.mark.parametrize("m,n,nb,ib", [(1024, 1024, 256, 32), (2048, 1024, 256, 32)])
+@pytest.mark.parametrize("m,n,nb,ib", [(1024, 1024, 256, 32), (2048, 1024, 256, 32), (4096, 4096, 256, 32),
+                                      (8192, 2048, 256, 32)])
 def test_noalloc_matches_workspace_entry_point_twice(tq, m, n, nb, ib):
     import torch
     for call, seed in enumerate((11, 12)):
