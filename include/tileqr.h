@@ -378,6 +378,15 @@ int tqr_tile_noalloc_status(int *status, int *task, cudaStream_t stream);
  * final value, 4 the device generator's count and list disagree, 5 not the
  * loop order's tasks). */
 int tqr_tile_noalloc_check(int m, int n, int nb, int ib, long long *ntasks);
+/* Host simulation of the persistent kernel (no GPU): `workers` CTAs take tasks
+ * strictly in list order, each waits for the task's producers and then runs
+ * it for its modelled duration (FP64 FMAs per task, panel tasks weighted for
+ * their serial column steps).  Gives the makespan of tqr_dtile_geqrf_noalloc's
+ * order, of tqr_dtile_geqrf_dag's longest-path order and the ideal total /
+ * workers, in those units.  0 = ok, -1 = shape outside the kernel, -5
+ * workers, 2 = a list that is not topological. */
+int tqr_tile_dag_simulate(int m, int n, int nb, int ib, int workers, double *noalloc_span, double *sorted_span,
+                          double *ideal_span);
 
 /* Tile QR with a binary reduction tree per panel (no counterpart in NextLA;
  * the composition its TT kernels exist for).  Panel k: geqrt! on every tile

@@ -37,6 +37,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -1156,6 +1157,71 @@ int tqr_tile_noalloc_check(int m, int n, int nb, int ib, long long *ntasks) {
       if (seen[g.done_t(k, i)] != g.panel_tasks()) return 3;
   }
   if (ntasks) *ntasks = (long long)v.size();
+  return 0;
+}
+
+// Host simulation of the persistent kernel running a task list: `workers`
+// CTAs take tasks strictly in list order, each waits for the task's producers
+// (the writers that bring its wait counters to their targets), then runs it
+// for item_cost units.  Returns the makespan in those units.
+static double simulate_order(const DagGeom &g, const std::vector<DagItem> &list, int workers) {
+  std::vector<DagItem> nat;
+  gen_items(g, nat);
+  const int N = (int)nat.size();
+  auto id = [](const DagItem &it) {
+    return ((unsigned long long)it.type << 56) | ((unsigned long long)it.b << 48) | ((unsigned long long)it.k << 32) |
+           ((unsigned long long)it.i << 16) | (unsigned long long)it.j | ((unsigned long long)it.s << 40);
+  };
+  std::map<unsigned long long, int> index;
+  for (int x = 0; x < N; ++x) index[id(nat[x])] = x;
+  // producers of every task, by replaying the loop order's counter writes
+  std::vector<std::vector<int>> writers(g.ncounters()), preds(N);
+  int c[kMaxDeps], t[kMaxDeps];
+  for (int x = 0; x < N; ++x) {
+    const int nd = item_deps(g, nat[x], c, t);
+    for (int d = 0; d < nd; ++d)
+      if (t[d] > 0) preds[x].push_back(writers[c[d]][t[d] - 1]);
+    const int nu = item_updates(g, nat[x], c);
+    for (int u = 0; u < nu; ++u) writers[c[u]].push_back(x);
+  }
+  std::vector<double> fin(N, -1.0);
+  std::vector<double> free_at(workers, 0.0);     // a heap of the workers' free times
+  double span = 0.0;
+  for (const DagItem &it : list) {
+    const int x = index.at(id(it));
+    std::pop_heap(free_at.begin(), free_at.end(), std::greater<double>());
+    double start = free_at.back();
+    for (int p : preds[x]) {
+      if (fin[p] < 0.0) return -1.0;             // a producer after its consumer
+      start = std::max(start, fin[p]);
+    }
+    fin[x] = start + item_cost(g, nat[x]);
+    span = std::max(span, fin[x]);
+    free_at.back() = fin[x];
+    std::push_heap(free_at.begin(), free_at.end(), std::greater<double>());
+  }
+  return span;
+}
+
+int tqr_tile_dag_simulate(int m, int n, int nb, int ib, int workers, double *noalloc_span, double *sorted_span,
+                          double *ideal_span) {
+  DagGeom g;
+  if (!dag_geom(m, n, nb, ib, &g)) return -1;
+  if (workers < 1) return -5;
+  std::vector<DagItem> sorted, buck;
+  build_schedule(g, sorted, false);
+  for (int q = 0; q < noalloc_buckets(g); ++q) {
+    const size_t off = buck.size();
+    buck.resize(off + (size_t)gen_bucket(g, q, nullptr));
+    gen_bucket(g, q, buck.data() + off);
+  }
+  double total = 0.0;
+  for (const DagItem &it : sorted) total += item_cost(g, it);
+  const double a = simulate_order(g, buck, workers), b = simulate_order(g, sorted, workers);
+  if (a < 0.0 || b < 0.0) return 2;
+  if (noalloc_span) *noalloc_span = a;
+  if (sorted_span) *sorted_span = b;
+  if (ideal_span) *ideal_span = total / workers;
   return 0;
 }
 

@@ -70,6 +70,8 @@ DIAG = {
     "tqr_dtile_geqrf_noalloc": ([_I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P], _I),
     "tqr_tile_noalloc_status": ([ctypes.POINTER(_I), ctypes.POINTER(_I), _P], _I),
     "tqr_tile_noalloc_check": ([_I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)], _I),
+    "tqr_tile_dag_simulate": ([_I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                               ctypes.POINTER(ctypes.c_double)], _I),
     "tqr_tile_dag_check_rhs": ([_I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)], _I),
     "tqr_tile_gels_worksize": ([_I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_size_t)], _I),
     "tqr_dtile_gels_dag": ([_I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P, _I, _P, ctypes.c_size_t, _P], _I),

@@ -356,3 +356,21 @@ def test_noalloc_bucket_order_replays(L, shape):
     rc, ntasks = tileqr.dag_check(*shape)
     assert rc == 0 and nt.value == ntasks
     assert L.tqr_tile_noalloc_check(1000, 1000, 256, 32, ctypes.byref(nt)) == -1
+
+
+@pytest.mark.parametrize("shape,bound", [((2048, 2048, 256, 32), 1.05), ((4096, 4096, 256, 32), 1.40),
+                                         ((8192, 8192, 256, 32), 1.33), ((16384, 4096, 256, 32), 1.75)])
+def test_noalloc_order_simulated_makespan(L, shape, bound):
+    """The allocation-free order against the workspace path's longest-path
+    order in the host simulation of the persistent kernel (304 CTAs taking
+    tasks in list order).  The bounds hold the simulated ratios the order was
+    chosen for (1.00 / 1.35 / 1.29 / 1.70; the one-step lookahead it replaced
+    simulated at 1.17 / 2.34 / 2.19 / 5.49).  Measured on a GB300: 1.13x at
+    4096^2 and 1.10x at 8192^2."""
+    a, b, ideal = ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
+    assert L.tqr_tile_dag_simulate(*shape, 304, ctypes.byref(a), ctypes.byref(b), ctypes.byref(ideal)) == 0
+    assert ideal.value > 0 and b.value >= ideal.value
+    assert a.value >= ideal.value
+    assert a.value / b.value <= bound, (a.value / b.value)
+    assert L.tqr_tile_dag_simulate(1000, 1000, 256, 32, 304, None, None, None) == -1
+    assert L.tqr_tile_dag_simulate(*shape, 0, None, None, None) == -5
