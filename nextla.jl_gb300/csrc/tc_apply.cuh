@@ -178,8 +178,8 @@ __device__ __forceinline__ void to_async_proxy() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// Waits (all threads) for the next phase of barrier `bar`; the same verdict
-// in every thread.
+// Waits (all threads) for the next phase of barrier `bar`; every thread gets the
+// same result.
 __device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t *phase) {
   const bool ok = __syncthreads_and(bar_wait(bar, *phase)) != 0;
   *phase ^= 1u;
