@@ -1114,7 +1114,15 @@ int tqr_dtile_geqrf_noalloc(int m, int n, int nb, int ib, double *A, int lda, do
 // header sits at the start of the static array, which no caller can address,
 // so this reads it for them (a copy from the symbol, then a stream
 // synchronisation; nothing is allocated).
+// One 64-bit identity per task: type (3 bits), block b (8), strip or chunk s
+// (5: at most nb / nw = 32 strips), step k, row i and column j (16 each).
+static unsigned long long item_id(const DagItem &it) {
+  return ((unsigned long long)it.type << 61) | ((unsigned long long)it.b << 53) | ((unsigned long long)it.s << 48) |
+         ((unsigned long long)it.k << 32) | ((unsigned long long)it.i << 16) | (unsigned long long)it.j;
+}
+
 int tqr_tile_noalloc_check(int m, int n, int nb, int ib, long long *ntasks) {
+  const auto id = item_id;
   // Host replay of the allocation-free schedule's order: every wait target of
   // every task is reached by the writers listed before it, and the list holds
   // each task of the loop order exactly once.
@@ -1131,10 +1139,6 @@ int tqr_tile_noalloc_check(int m, int n, int nb, int ib, long long *ntasks) {
   gen_items(g, nat);
   if (v.size() != nat.size()) return 1;
   // the same tasks as the loop order, each once
-  auto id = [](const DagItem &it) {
-    return ((unsigned long long)it.type << 56) | ((unsigned long long)it.b << 48) | ((unsigned long long)it.k << 32) |
-           ((unsigned long long)it.i << 16) | (unsigned long long)it.j | ((unsigned long long)it.s << 40);
-  };
   {
     std::vector<unsigned long long> a(v.size()), b(nat.size());
     for (size_t x = 0; x < v.size(); ++x) { a[x] = id(v[x]); b[x] = id(nat[x]); }
@@ -1165,13 +1169,10 @@ int tqr_tile_noalloc_check(int m, int n, int nb, int ib, long long *ntasks) {
 // (the writers that bring its wait counters to their targets), then runs it
 // for item_cost units.  Returns the makespan in those units.
 static double simulate_order(const DagGeom &g, const std::vector<DagItem> &list, int workers) {
+  const auto id = item_id;
   std::vector<DagItem> nat;
   gen_items(g, nat);
   const int N = (int)nat.size();
-  auto id = [](const DagItem &it) {
-    return ((unsigned long long)it.type << 56) | ((unsigned long long)it.b << 48) | ((unsigned long long)it.k << 32) |
-           ((unsigned long long)it.i << 16) | (unsigned long long)it.j | ((unsigned long long)it.s << 40);
-  };
   std::map<unsigned long long, int> index;
   for (int x = 0; x < N; ++x) index[id(nat[x])] = x;
   // producers of every task, by replaying the loop order's counter writes
